@@ -1,0 +1,375 @@
+"""FP64 oracle for the registration + stacking hot path (test infrastructure).
+
+ctypes binding of ``oracle/_build/libsst_oracle.so`` (built by ``make -C oracle``).
+Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` leg of
+``bench.py`` may import this module; the product never does.
+
+Parity status: unpinned by the reference (it ships no tests or golden data and
+cannot be built without OpenCV/TBB). The restatement is pinned by known-answer
+tests in ``tests/test_oracle.py``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libsst_oracle.so")
+
+# IMAGE_MOTION_TYPE (image_transform.h:15-26)
+TRANSLATION, EUCLIDEAN, SCALED_EUCLIDEAN, AFFINE, HOMOGRAPHY, SEMI_QUADRATIC, QUADRATIC, EPIPOLAR = range(8)
+# ECC_ALIGN_METHOD (ecc2.h:57-62)
+FA, IC, LM, ICLM = range(4)
+BORDER_CONSTANT, BORDER_REPLICATE, BORDER_REFLECT, BORDER_REFLECT101 = 0, 1, 2, 4
+
+
+def build(force: bool = False) -> str:
+    srcs = [os.path.join(_HERE, f) for f in ("sst_oracle.cc", "sst_oracle_model.cc", "sst_oracle.h")]
+    if force or not os.path.exists(_LIB_PATH) or any(
+            os.path.getmtime(s) > os.path.getmtime(_LIB_PATH) for s in srcs):
+        subprocess.check_call(["make", "-s", "-C", _HERE])
+    return _LIB_PATH
+
+
+class Model(C.Structure):
+    _fields_ = [("type", C.c_int), ("fix_translation", C.c_int), ("fix_rotation", C.c_int),
+                ("fix_scale", C.c_int)]
+
+
+class AlignOpts(C.Structure):
+    _fields_ = [("method", C.c_int), ("max_iterations", C.c_int), ("max_eps", C.c_double),
+                ("update_step_scale", C.c_double), ("ic_jacobian_at_identity", C.c_int)]
+
+
+class Level(C.Structure):
+    _fields_ = [("w", C.c_int), ("h", C.c_int), ("ref", C.c_void_p), ("ref_mask", C.c_void_p),
+                ("cur", C.c_void_p), ("cw", C.c_int), ("ch", C.c_int), ("cur_mask", C.c_void_p)]
+
+
+class EcchOpts(C.Structure):
+    _fields_ = [("epsx", C.c_double), ("reference_smooth_sigma", C.c_double),
+                ("input_smooth_sigma", C.c_double), ("update_step_scale", C.c_double),
+                ("method", C.c_int), ("max_iterations", C.c_int), ("minimum_image_size", C.c_int),
+                ("maxlevel", C.c_int), ("ic_jacobian_at_identity", C.c_int)]
+
+
+class PipelineOpts(C.Structure):
+    _fields_ = [("ecch", EcchOpts), ("num_passes", C.c_int), ("pass_motion", C.c_int * 3),
+                ("min_rho", C.c_double), ("border_mode", C.c_int), ("use_laplacian_weights", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        d, i, p = C.c_double, C.c_int, C.c_void_p
+        sig = {
+            "orc_model_nparams": (i, [p]),
+            "orc_model_identity": (None, [p, p]),
+            "orc_model_get_params": (None, [p, p, p]),
+            "orc_model_set_params": (None, [p, p, p]),
+            "orc_model_warp": (None, [p, p, d, d, p, p]),
+            "orc_model_sd": (None, [p, p, d, d, d, d, p]),
+            "orc_model_eps": (d, [p, p, p, i, i]),
+            "orc_model_scale": (None, [p, p, d]),
+            "orc_model_invert_and_compose": (i, [p, p, p, p]),
+            "orc_gaussian_kernel": (i, [d, p]),
+            "orc_smooth": (None, [p, i, i, d, p]),
+            "orc_pyrdown": (None, [p, i, i, p, i, i]),
+            "orc_differentiate": (None, [p, i, i, p, p, p]),
+            "orc_sample_bilinear": (d, [p, i, i, d, d, i, d]),
+            "orc_erode5": (None, [p, i, i, i, p]),
+            "orc_remap_model": (None, [p, p, p, i, i, i, i, i, d, p]),
+            "orc_ecc_align": (i, [p, p, p, p, p, p]),
+            "orc_ecch_num_levels": (i, [i, i, p]),
+            "orc_ecch_align": (i, [p, p, p, p, p, i, i, p, p, i, i, p, p]),
+            "orc_correlation": (d, [p, p, i, i, p, p, i, i, p, p]),
+            "orc_stack_remap": (None, [p, p, p, i, i, i, i, i, p, p]),
+            "orc_weighted_average_add": (None, [p, p, i, i, p, p]),
+            "orc_running_mean_add_f32": (None, [p, p, i, i, p, p]),
+            "orc_extract_bayer_planes_u16": (None, [p, i, i, p]),
+            "orc_average_bayer_planes_u16": (None, [p, i, i, p]),
+            "orc_bayer_pattern_mask": (None, [i, i, i, p]),
+            "orc_bayer_accumulate": (None, [p, i, i, p, p, p, p, p, p]),
+            "orc_laplacian_energy": (d, [p, i, i]),
+            "orc_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
+            "orc_set_num_threads": (None, [i]),
+            "orc_get_num_threads": (i, []),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(_lib, name)
+            f.restype = res
+            f.argtypes = args
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _u8(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.uint8)
+
+
+def model(motion: int, fix_translation=0, fix_rotation=0, fix_scale=None) -> Model:
+    """create_image_transform (image_transform.cc:32-60): EUCLIDEAN fixes the scale."""
+    if fix_scale is None:
+        fix_scale = 1 if motion == EUCLIDEAN else 0
+    return Model(motion, fix_translation, fix_rotation, fix_scale)
+
+
+def nparams(m: Model) -> int:
+    return lib().orc_model_nparams(C.byref(m))
+
+
+def identity(m: Model) -> np.ndarray:
+    s = np.zeros(16)
+    lib().orc_model_identity(C.byref(m), _ptr(s))
+    return s
+
+
+def get_params(m: Model, state) -> np.ndarray:
+    p = np.zeros(16)
+    s = _f64(state)
+    lib().orc_model_get_params(C.byref(m), _ptr(s), _ptr(p))
+    return p[:nparams(m)]
+
+
+def set_params(m: Model, state, p) -> np.ndarray:
+    s = _f64(state).copy()
+    pp = np.zeros(16)
+    pp[:len(p)] = p
+    lib().orc_model_set_params(C.byref(m), _ptr(s), _ptr(pp))
+    return s
+
+
+def warp(m: Model, state, x: float, y: float):
+    s = _f64(state)
+    X, Y = C.c_double(), C.c_double()
+    lib().orc_model_warp(C.byref(m), _ptr(s), x, y, C.byref(X), C.byref(Y))
+    return X.value, Y.value
+
+
+def warp_grid(m: Model, state, w: int, h: int):
+    """W(x;p) over the w x h grid (create_remap) -> (mapx, mapy)."""
+    mx = np.empty((h, w))
+    my = np.empty((h, w))
+    for y in range(h):
+        for x in range(w):
+            mx[y, x], my[y, x] = warp(m, state, x, y)
+    return mx, my
+
+
+def sd(m: Model, state, x, y, gx, gy) -> np.ndarray:
+    s = _f64(state)
+    J = np.zeros(12)
+    lib().orc_model_sd(C.byref(m), _ptr(s), x, y, gx, gy, _ptr(J))
+    return J[:nparams(m)]
+
+
+def eps(m: Model, state, dp, w, h) -> float:
+    s = _f64(state)
+    d = np.zeros(16)
+    d[:len(dp)] = dp
+    return lib().orc_model_eps(C.byref(m), _ptr(s), _ptr(d), w, h)
+
+
+def scale(m: Model, state, f) -> np.ndarray:
+    s = _f64(state).copy()
+    lib().orc_model_scale(C.byref(m), _ptr(s), f)
+    return s
+
+
+def invert_and_compose(m: Model, state, dp) -> np.ndarray:
+    s = _f64(state)
+    d = np.zeros(16)
+    d[:len(dp)] = dp
+    out = np.zeros(16)
+    lib().orc_model_invert_and_compose(C.byref(m), _ptr(s), _ptr(d), _ptr(out))
+    return out
+
+
+def gaussian_kernel(sigma: float) -> np.ndarray:
+    k = np.zeros(512)
+    n = lib().orc_gaussian_kernel(sigma, _ptr(k))
+    return k[:n]
+
+
+def smooth(img, sigma):
+    a = _f64(img)
+    out = np.empty_like(a)
+    lib().orc_smooth(_ptr(a), a.shape[1], a.shape[0], sigma, _ptr(out))
+    return out
+
+
+def next_size(w, h):
+    """c_ecch::compute_next_pyramid_layer_size (ecc2.h:290-293)"""
+    return ((w + 1) >> 1) & ~1, ((h + 1) >> 1) & ~1
+
+
+def pyrdown(img, dw=None, dh=None):
+    a = _f64(img)
+    h, w = a.shape
+    if dw is None:
+        dw, dh = next_size(w, h)
+    out = np.empty((dh, dw))
+    lib().orc_pyrdown(_ptr(a), w, h, _ptr(out), dw, dh)
+    return out
+
+
+def differentiate(img, valid=None):
+    a = _f64(img)
+    gx = np.empty_like(a)
+    gy = np.empty_like(a)
+    lib().orc_differentiate(_ptr(a), a.shape[1], a.shape[0], _ptr(_u8(valid)), _ptr(gx), _ptr(gy))
+    return gx, gy
+
+
+def erode5(mask):
+    m = _u8(mask)
+    out = np.empty_like(m)
+    lib().orc_erode5(_ptr(m), m.shape[1], m.shape[0], 1, _ptr(out))
+    return out
+
+
+def remap(m: Model, state, src, dw, dh, border=BORDER_REPLICATE, bval=0.0):
+    s = _f64(state)
+    a = _f64(src)
+    out = np.empty((dh, dw))
+    lib().orc_remap_model(C.byref(m), _ptr(s), _ptr(a), a.shape[1], a.shape[0], dw, dh, border, bval, _ptr(out))
+    return out
+
+
+def ecc_align(m: Model, state, ref, cur, method=IC, max_iterations=50, max_eps=0.2, step=1.0,
+              ref_mask=None, cur_mask=None, ic_jacobian_at_identity=1):
+    """Single-level c_ecc_align::align(). Returns (ok, state, iterations, eps)."""
+    s = _f64(state).copy()
+    r, c = _f64(ref), _f64(cur)
+    rm, cm = _u8(ref_mask), _u8(cur_mask)
+    lv = Level(r.shape[1], r.shape[0], _ptr(r), _ptr(rm), _ptr(c), c.shape[1], c.shape[0], _ptr(cm))
+    o = AlignOpts(method, max_iterations, max_eps, step, ic_jacobian_at_identity)
+    it, e = C.c_int(), C.c_double()
+    ok = lib().orc_ecc_align(C.byref(m), _ptr(s), C.byref(lv), C.byref(o), C.byref(it), C.byref(e))
+    return bool(ok), s, it.value, e.value
+
+
+def ecch_opts(method=IC, maxlevel=4, max_iterations=50, epsx=0.2, ref_sigma=1.0, in_sigma=1.0, step=1.0,
+              minimum_image_size=16, ic_jacobian_at_identity=1) -> EcchOpts:
+    return EcchOpts(epsx, ref_sigma, in_sigma, step, method, max_iterations, minimum_image_size, maxlevel,
+                    ic_jacobian_at_identity)
+
+
+def ecch_num_levels(w, h, o: EcchOpts) -> int:
+    return lib().orc_ecch_num_levels(w, h, C.byref(o))
+
+
+def ecch_align(m: Model, state, ref, cur, o: EcchOpts, ref_mask=None, cur_mask=None):
+    s = _f64(state).copy()
+    r, c = _f64(ref), _f64(cur)
+    rm, cm = _u8(ref_mask), _u8(cur_mask)
+    it, e = C.c_int(), C.c_double()
+    lib().orc_ecch_align(C.byref(m), _ptr(s), C.byref(o), _ptr(r), _ptr(rm), r.shape[1], r.shape[0],
+                         _ptr(c), _ptr(cm), c.shape[1], c.shape[0], C.byref(it), C.byref(e))
+    return s, it.value, e.value
+
+
+def correlation(m: Model, state, cur, ref, cur_mask=None, ref_mask=None) -> float:
+    s = _f64(state)
+    c, r = _f64(cur), _f64(ref)
+    return lib().orc_correlation(_ptr(c), _ptr(_u8(cur_mask)), c.shape[1], c.shape[0], _ptr(r),
+                                 _ptr(_u8(ref_mask)), r.shape[1], r.shape[0], C.byref(m), _ptr(s))
+
+
+def stack_remap(m: Model, state, src, dw, dh, border=BORDER_REFLECT101):
+    s = _f64(state)
+    a = _f64(src)
+    out = np.empty((dh, dw))
+    msk = np.empty((dh, dw), np.uint8)
+    lib().orc_stack_remap(C.byref(m), _ptr(s), _ptr(a), a.shape[1], a.shape[0], dw, dh, border, _ptr(out),
+                          _ptr(msk))
+    return out, msk
+
+
+def laplacian_energy(img) -> float:
+    a = _f64(img)
+    return lib().orc_laplacian_energy(_ptr(a), a.shape[1], a.shape[0])
+
+
+def extract_bayer_planes(raw):
+    a = np.ascontiguousarray(raw, dtype=np.uint16)
+    h, w = a.shape
+    out = np.empty((h // 2, w // 2, 4), np.uint16)
+    lib().orc_extract_bayer_planes_u16(_ptr(a), w, h, _ptr(out))
+    return out
+
+
+def average_bayer_planes(raw):
+    a = np.ascontiguousarray(raw, dtype=np.uint16)
+    h, w = a.shape
+    out = np.empty((h // 2, w // 2), np.uint16)
+    lib().orc_average_bayer_planes_u16(_ptr(a), w, h, _ptr(out))
+    return out
+
+
+def bayer_pattern_mask(colorid, w, h):
+    out = np.empty((h, w), np.uint8)
+    lib().orc_bayer_pattern_mask(colorid, w, h, _ptr(out))
+    return out
+
+
+def bayer_accumulate(src, mapx, mapy, pattern, weights, acc, cntr):
+    a = _f64(src)
+    h, w = a.shape
+    mx, my = _f64(mapx), _f64(mapy)
+    wt = None if weights is None else _f64(weights)
+    lib().orc_bayer_accumulate(_ptr(a), w, h, _ptr(mx), _ptr(my), _ptr(_u8(pattern)), _ptr(wt), _ptr(acc),
+                               _ptr(cntr))
+
+
+def pipeline_opts(passes=(AFFINE, HOMOGRAPHY), method=IC, maxlevel=4, max_iterations=50, epsx=0.2,
+                  min_rho=0.8, border=BORDER_REFLECT101, laplacian_weights=1, ic_jacobian_at_identity=1,
+                  minimum_image_size=16) -> PipelineOpts:
+    o = PipelineOpts()
+    o.ecch = ecch_opts(method, maxlevel, max_iterations, epsx, 1.0, 1.0, 1.0, minimum_image_size,
+                       ic_jacobian_at_identity)
+    o.num_passes = len(passes)
+    for k, p in enumerate(passes):
+        o.pass_motion[k] = p
+    o.min_rho = min_rho
+    o.border_mode = border
+    o.use_laplacian_weights = laplacian_weights
+    return o
+
+
+def register_and_stack(o: PipelineOpts, ref, frames, frame_scale):
+    """CPU restatement of register_frame + the stacking loop body for n frames."""
+    r = _f64(ref)
+    fr = np.ascontiguousarray(frames, dtype=np.uint16)
+    n = fr.shape[0]
+    h, w = r.shape
+    states = np.zeros((n, 16))
+    status = np.zeros(n, np.int32)
+    rho = np.zeros(n)
+    acc = np.zeros((h, w))
+    accw = np.zeros((h, w))
+    lib().orc_register_and_stack(C.byref(o), _ptr(r), w, h, _ptr(fr), n, frame_scale, _ptr(states),
+                                 _ptr(status), _ptr(rho), _ptr(acc), _ptr(accw))
+    return states, status, rho, acc, accw
+
+
+def set_num_threads(n: int):
+    lib().orc_set_num_threads(n)
+
+
+def get_num_threads() -> int:
+    return lib().orc_get_num_threads()

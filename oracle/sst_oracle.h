@@ -1,0 +1,172 @@
+/*
+ * sst_oracle.h -- FP64 CPU restatement of SerStacker's frame registration +
+ * stacking hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the parity checker for the
+ * CUDA path and the timed CPU baseline; the product never links, loads or
+ * calls it. It restates the algorithms of the reference files
+ *   core/proc/image_registration/ecc2.cc
+ *   core/proc/image_registration/c_image_transform.cc
+ *   core/proc/image_registration/c_frame_registration.cc
+ *   core/average/c_frame_accumulation.cc
+ *   core/io/debayer.cc
+ * in double precision. OpenCV primitives the reference calls (sepFilter2D,
+ * pyrDown, remap, meanStdDev, erode, resize NEAREST, Cholesky solve) are
+ * re-implemented from their documented semantics; bilinear sampling is exact
+ * (no 1/32 px grid) unless ORC_SNAP32 is requested.
+ *
+ * Parity status: unpinned by the reference (the reference ships no tests and
+ * no golden data, and cannot be compiled here: OpenCV/TBB/libconfig absent).
+ * The oracle is pinned by known-answer tests instead (tests/test_oracle.py).
+ */
+#pragma once
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* IMAGE_MOTION_TYPE values (image_transform.h:15-26) */
+enum {
+  ORC_MOTION_TRANSLATION = 0,
+  ORC_MOTION_EUCLIDEAN = 1,
+  ORC_MOTION_SCALED_EUCLIDEAN = 2,
+  ORC_MOTION_AFFINE = 3,
+  ORC_MOTION_HOMOGRAPHY = 4,
+  ORC_MOTION_SEMI_QUADRATIC = 5,
+  ORC_MOTION_QUADRATIC = 6,
+  ORC_MOTION_EPIPOLAR_DEROTATION = 7,
+};
+
+/* ECC_ALIGN_METHOD values (ecc2.h:57-62) */
+enum {
+  ORC_ECC_FORWARD_ADDITIVE = 0,
+  ORC_ECC_INVERSE_COMPOSITIONAL = 1,
+  ORC_ECC_LM = 2,
+  ORC_ECC_INVERSE_COMPOSITIONAL_LM = 3,
+};
+
+/* cv::BorderTypes values used on the path */
+enum {
+  ORC_BORDER_CONSTANT = 0,
+  ORC_BORDER_REPLICATE = 1,
+  ORC_BORDER_REFLECT = 2,
+  ORC_BORDER_REFLECT101 = 4,
+};
+
+/* Motion model. The transform state is a vector of up to 16 doubles:
+ *   translation : tx ty
+ *   euclidean   : Tx Ty angle scale Cx Cy  (adjustable subset per fix flags)
+ *   affine      : a00 a01 a02 a10 a11 a12
+ *   homography  : a00 a01 a02 a10 a11 a12 a20 a21   (a22 = 1)
+ *   semi-quad.  : a00 a01 a02 a03 a10 a11 a12 a13
+ *   quadratic   : a00..a05 a10..a15
+ * The ECC parameter vector p (c_image_transform::parameters()) equals the
+ * state for every model but euclidean, where it is the adjustable subset. */
+typedef struct orc_model {
+  int type;
+  int fix_translation, fix_rotation, fix_scale;
+} orc_model;
+
+int  orc_model_nparams(const orc_model * m);
+void orc_model_identity(const orc_model * m, double * state);
+void orc_model_get_params(const orc_model * m, const double * state, double * p);
+void orc_model_set_params(const orc_model * m, double * state, const double * p);
+void orc_model_warp(const orc_model * m, const double * state, double x, double y, double * X, double * Y);
+void orc_model_sd(const orc_model * m, const double * state, double x, double y, double gx, double gy, double * J);
+double orc_model_eps(const orc_model * m, const double * state, const double * dp, int w, int h);
+void orc_model_scale(const orc_model * m, double * state, double factor);
+int  orc_model_invert_and_compose(const orc_model * m, const double * state, const double * dp, double * out_state);
+int  orc_model_invertible(const orc_model * m);
+
+/* primitives */
+int  orc_gaussian_kernel(double sigma, double * k /* >= 2*int(3 sigma)+1 */);
+void orc_smooth(const double * src, int w, int h, double sigma, double * dst);
+void orc_pyrdown(const double * src, int w, int h, double * dst, int dw, int dh);
+void orc_resize_nearest_u8(const uint8_t * src, int w, int h, uint8_t * dst, int dw, int dh);
+void orc_differentiate(const double * src, int w, int h, const uint8_t * valid, double * gx, double * gy);
+double orc_sample_bilinear(const double * src, int w, int h, double sx, double sy, int border, double bval);
+double orc_mask_coverage(const uint8_t * mask, int w, int h, double sx, double sy);
+void orc_erode5(const uint8_t * src, int w, int h, int border_is_max, uint8_t * dst);
+void orc_remap_model(const orc_model * m, const double * state, const double * src, int sw, int sh,
+    int dw, int dh, int border, double bval, double * dst);
+
+/* single-level ECC (c_ecc_align::align) */
+typedef struct orc_align_opts {
+  int method;
+  int max_iterations;
+  double max_eps;
+  double update_step_scale;
+  int ic_jacobian_at_identity;    /* 1: IC steepest-descent images at the identity warp */
+} orc_align_opts;
+
+typedef struct orc_level {
+  int w, h;
+  const double * ref;   const uint8_t * ref_mask;   /* mask may be NULL */
+  const double * cur;   int cw, ch;  const uint8_t * cur_mask;
+} orc_level;
+
+/* returns the reference's align() bool; *iters, *eps filled. */
+int orc_ecc_align(const orc_model * m, double * state, const orc_level * lvl, const orc_align_opts * o,
+    int * iters, double * eps);
+
+/* c_ecch: Gaussian pre-smooth, pyramid, coarse-to-fine align.
+ * ref / cur are f64 images already converted (ecc_convert_input_image). */
+typedef struct orc_ecch_opts {
+  double epsx;
+  double reference_smooth_sigma, input_smooth_sigma;
+  double update_step_scale;
+  int method, max_iterations, minimum_image_size, maxlevel;
+  int ic_jacobian_at_identity;
+} orc_ecch_opts;
+
+int  orc_ecch_num_levels(int w, int h, const orc_ecch_opts * o);
+int  orc_ecch_align(const orc_model * m, double * state, const orc_ecch_opts * o,
+    const double * ref, const uint8_t * ref_mask, int w, int h,
+    const double * cur, const uint8_t * cur_mask, int cw, int ch,
+    int * iters, double * eps);
+
+double orc_correlation(const double * cur, const uint8_t * cur_mask, int cw, int ch,
+    const double * ref, const uint8_t * ref_mask, int w, int h, const orc_model * m, const double * state);
+
+/* base_remap of a frame for stacking: LINEAR + border, mask LINEAR/CONSTANT >=255 + 5x5 erode */
+void orc_stack_remap(const orc_model * m, const double * state, const double * src, int sw, int sh,
+    int dw, int dh, int border, double * dst, uint8_t * dst_mask);
+
+/* accumulators */
+void orc_weighted_average_add(double * acc, double * accw, int w, int h, const double * src, const double * weights);
+void orc_running_mean_add_f32(float * acc, float * accw, int w, int h, const float * src, const float * weights);
+void orc_extract_bayer_planes_u16(const uint16_t * src, int w, int h, uint16_t * dst);
+void orc_average_bayer_planes_u16(const uint16_t * src, int w, int h, uint16_t * dst);
+void orc_bayer_pattern_mask(int colorid, int w, int h, uint8_t * dst);
+void orc_bayer_accumulate(const double * src, int w, int h, const double * mapx, const double * mapy,
+    const uint8_t * pattern, const double * weights, double * acc, double * cntr);
+
+/* sharpness weight of a frame: mean of the squared 5-point Laplacian over the
+ * interior of a level image */
+double orc_laplacian_energy(const double * img, int w, int h);
+
+/* whole pipeline for the CPU baseline: register (ecch passes) + rho gate +
+ * final warp + weighted stack of n frames. */
+typedef struct orc_pipeline_opts {
+  orc_ecch_opts ecch;
+  int num_passes;
+  int pass_motion[3];
+  double min_rho;
+  int border_mode;
+  int use_laplacian_weights;
+} orc_pipeline_opts;
+
+int orc_register_and_stack(const orc_pipeline_opts * o,
+    const double * ref, int w, int h,
+    const uint16_t * frames, int n, double frame_scale,
+    double * out_states /* n x 16 */, int * out_status, double * out_rho,
+    double * acc, double * accw);
+
+void orc_set_num_threads(int n);
+int  orc_get_num_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
