@@ -1,0 +1,398 @@
+"""Benchmark: frames/s registered + warped + stacked on GB300.
+
+Workload (the headline configuration): 2000 synthetic mono uint16 frames of
+1280x960 (Gaussian-blurred banded disk, per-frame seeing blur U(0.8, 2.5) px,
+random homography, Poisson + read noise), registered against the noiseless
+reference with a 4-level c_ecch pyramid, inverse-compositional ECC, affine
+then homography, gated by rho >= 0.8, weighted by Laplacian energy and
+stacked with compensated FP32 sums. One step = one pass of that whole
+sequence through sst_stack_frames.
+
+  value : frames already resident in HBM when the timed region starts
+  e2e   : the same call with pinned HOST frames (H2D inside the timed region)
+          plus the D2H of every result and of the stacked image
+
+--impl reference times the CPU restatement of the reference path (the FP64
+oracle, OpenMP over all host cores) on a bounded sample of the same workload.
+Multi-GPU runs (torchrun) are replicas: each rank stacks its own sequence.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/sec registered+warped+stacked, batched vs plain on GB300 at ≤0.02 px"
+WIDTH, HEIGHT = 1280, 960
+GAIN = 64.0
+SCALE = 1.0 / 65535.0
+SEED = 1001
+
+
+def workload_cfg(frames: int):
+    return {
+        "workload": f"{frames} x {WIDTH}x{HEIGHT} u16 frames; c_ecch 4 levels, inverse-compositional ECC, "
+                    "affine then homography; rho>=0.8 gate; Laplacian-energy frame weights; "
+                    "compensated FP32 weighted average",
+        "frames": frames, "width": WIDTH, "height": HEIGHT, "levels": 4, "method": "INVERSE_COMPOSITIONAL",
+        "passes": ["AFFINE", "HOMOGRAPHY"], "epsx": 0.01, "max_iterations": 50,
+        "l2": "inputs (frames x 2.46 MB > 129 MB L2) stream from HBM every step; no flush needed",
+    }
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"], f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes of one level-0 IC pass launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "ecc_ic_pass_traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except (OSError, ValueError):
+            return None
+    return None
+
+
+def make_workload(n: int, device):
+    import torch
+    from serstacker_gb300 import synth
+    sc = synth.scene_config1()
+    frames_i32, Hs, blurs = synth.make_sequence_torch(sc, n, SEED, kind="config1", gain=GAIN,
+                                                      blur_range=(0.8, 2.5), device=device)
+    frames = torch.where(frames_i32 > 32767, frames_i32 - 65536, frames_i32).to(torch.int16)
+    del frames_i32
+    ref = (synth.reference_np(sc) * GAIN).astype(np.float32)
+    return frames, ref, Hs
+
+
+def warp_rms_vs_truth(params: np.ndarray, Hs: np.ndarray, status: np.ndarray, step: int = 40):
+    ys, xs = np.mgrid[0:HEIGHT:step, 0:WIDTH:step].astype(np.float64)
+    out = []
+    for p, H, s in zip(params, Hs, status):
+        if s != 0:
+            continue
+        w = p[6] * xs + p[7] * ys + 1.0
+        X = (p[0] * xs + p[1] * ys + p[2]) / w
+        Y = (p[3] * xs + p[4] * ys + p[5]) / w
+        wt = H[2, 0] * xs + H[2, 1] * ys + 1.0
+        Xt = (H[0, 0] * xs + H[0, 1] * ys + H[0, 2]) / wt
+        Yt = (H[1, 0] * xs + H[1, 1] * ys + H[1, 2]) / wt
+        out.append(math.sqrt(float(np.mean((X - Xt) ** 2 + (Y - Yt) ** 2))))
+    return float(np.median(out)) if out else None, float(np.max(out)) if out else None
+
+
+def cpu_reference_rate(frames_host: np.ndarray, ref: np.ndarray, sample: int, threads: int):
+    """Oracle (CPU restatement of the reference path) on `sample` frames: frames/s."""
+    import oracle as O
+    O.set_num_threads(threads)
+    po = O.pipeline_opts(passes=(O.AFFINE, O.HOMOGRAPHY), method=O.IC, maxlevel=4, max_iterations=50, epsx=0.01,
+                         min_rho=0.8, minimum_image_size=16)
+    sub = frames_host[:sample]
+    t0 = time.perf_counter()
+    O.register_and_stack(po, ref.astype(np.float64) * SCALE, sub, SCALE)
+    dt = time.perf_counter() - t0
+    return sample / dt, dt
+
+
+def run_reference_arm(args, ws, rank):
+    """--impl reference: the reference path's CPU implementation, timed per step."""
+    if rank != 0:
+        return
+    import oracle as O
+    O.build()
+    from serstacker_gb300 import synth
+    threads = os.cpu_count() or 1
+    sample = args.ref_sample
+    sc = synth.scene_config1()
+    frames, _, _ = synth.make_sequence_np(sc, sample, SEED, kind="config1", dtype=np.uint16, gain=GAIN,
+                                          blur_range=(0.8, 2.5))
+    ref = synth.reference_np(sc) * GAIN
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_reference_rate(frames, ref, min(2, sample), threads)
+    rates = []
+    t_all = 0.0
+    for _ in range(args.steps):
+        r, dt = cpu_reference_rate(frames, ref, sample, threads)
+        rates.append(r)
+        t_all += dt
+    v = float(np.median(rates))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_all / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_cfg(args.frames),
+            "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample} frames of the workload per step (oracle pipeline, FP64, OpenMP)"},
+            "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--frames", type=int, default=2000)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--chunk", type=int, default=256, help="frames per streamed chunk in the e2e leg")
+    ap.add_argument("--ref-sample", type=int, default=6, help="frames per CPU baseline sample")
+    ap.add_argument("--plain-frames", type=int, default=12)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    if args.impl == "reference":
+        run_reference_arm(args, ws, rank)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    import torch
+    from serstacker_gb300 import capi as C
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    C.lib()
+    n = args.frames
+    frames, ref, Hs = make_workload(n, device)
+    frame_bytes = WIDTH * HEIGHT * 2
+    opts = C.default_options(method=C.IC, maxlevel=4, max_iterations=50, epsx=0.01, minimum_image_size=16,
+                             min_rho=0.8)
+    reg = C.c_ecch(opts)
+    reg.set_reference_image(ref, scale=SCALE)
+    acc = C.c_weigthed_average(WIDTH, HEIGHT)
+    passes = [C.AFFINE, C.HOMOGRAPHY]
+    dev_out = {"params": torch.zeros((n, 12), dtype=torch.float32, device=device),
+               "status": torch.zeros(n, dtype=torch.int32, device=device),
+               "rho": torch.zeros(n, dtype=torch.float32, device=device),
+               "weight": torch.zeros(n, dtype=torch.float32, device=device)}
+
+    def step_device():
+        acc.clear()
+        reg.set_chunk_frames(n)
+        C.stack_frames(reg, acc, frames, passes, SCALE, weighting=1, on_device=True, n=n, width=WIDTH,
+                       height=HEIGHT, depth=C.DEPTH_U16, row_stride=WIDTH * 2, frame_stride=frame_bytes,
+                       outputs=dev_out)
+
+    # ---------------------------------------------------------------- value
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    C.kernel_launch_count(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step_device()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = C.kernel_launch_count()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(ms, ws)
+    clk = clocks.stop()
+    value = ws * n / (ms / 1000.0)
+
+    # roofline of the dominant kernel: the level-0 Gauss-Newton passes
+    peak, peak_kind = measured_peaks()
+    lv_ms, lv_bytes, lv_fi = 0.0, 0.0, 0.0
+    level_table = []
+    for k in range(len(passes)):
+        for lvl in range(reg.num_levels()):
+            t, fi, ab = reg.level_stats(k, lvl)
+            level_table.append({"pass": k, "level": lvl, "ms": t, "frame_iterations": fi, "alg_bytes": ab})
+            if lvl == 0:
+                lv_ms += t
+                lv_bytes += ab
+                lv_fi += fi
+    achieved = lv_bytes / (lv_ms / 1000.0) / 1e9 if lv_ms > 0 else 0.0
+    tr = traffic_per_launch()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": tr.get("dram_bytes_per_launch") if tr else None,
+            "kernel": "k_pass_pointwise<IC> level 0 (1280x960), all frames x iterations",
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+            "alg_bytes_model": "16 B per pixel and frame-iteration (warped source 4 + template 4 + gradients 8)",
+            "level0_ms_per_step": lv_ms, "level0_frame_iterations": lv_fi}
+
+    res = {k: v.cpu().numpy() for k, v in dev_out.items()}
+    med_rms, max_rms = warp_rms_vs_truth(res["params"][:, :8].astype(np.float64), Hs, res["status"])
+
+    # ---------------------------------------------------------------- e2e
+    host_frames = torch.empty((n, HEIGHT, WIDTH), dtype=torch.int16, pin_memory=True)
+    host_frames.copy_(frames)
+    torch.cuda.synchronize()
+    pinned_out = {"params": torch.zeros((n, 12), dtype=torch.float32, pin_memory=True),
+                  "status": torch.zeros(n, dtype=torch.int32, pin_memory=True),
+                  "rho": torch.zeros(n, dtype=torch.float32, pin_memory=True),
+                  "weight": torch.zeros(n, dtype=torch.float32, pin_memory=True)}
+    avg_host = torch.zeros((HEIGHT, WIDTH), dtype=torch.float32, pin_memory=True)
+    mask_host = torch.zeros((HEIGHT, WIDTH), dtype=torch.uint8, pin_memory=True)
+
+    def step_e2e():
+        acc.clear()
+        reg.set_chunk_frames(args.chunk)
+        C.stack_frames(reg, acc, host_frames.data_ptr(), passes, SCALE, weighting=1, on_device=True, n=n,
+                       width=WIDTH, height=HEIGHT, depth=C.DEPTH_U16, row_stride=WIDTH * 2,
+                       frame_stride=frame_bytes, outputs=pinned_out, host_input=True)
+        C.lib().sst_weighted_average_compute(acc.handle, avg_host.data_ptr(), mask_host.data_ptr(), 0, None)
+
+    for _ in range(max(1, args.warmup)):
+        step_e2e()
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    torch.cuda.synchronize()
+    barrier(ws)
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000.0 / args.steps, ws)
+    d2h = n * (12 * 4 + 3 * 4) + WIDTH * HEIGHT * 5
+    e2e = {"value": ws * n / (e2e_ms / 1000.0), "unit": "frames/s", "h2d_bytes_per_step": n * frame_bytes,
+           "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "api": "sst_stack_frames (host pinned) + "
+                                                                      "sst_weighted_average_compute"}
+
+    # ---------------------------------------------------------- plain form
+    pn = min(args.plain_frames, n)
+    sub = frames[:pn].cpu().numpy().view(np.uint16)
+    reg_p = C.c_ecch(opts)
+    reg_p.set_reference_image(ref, scale=SCALE)
+    acc_p = C.c_weigthed_average(WIDTH, HEIGHT)
+    reg_p.align(sub[:1], passes, scale=SCALE, plain=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(pn):
+        o = reg_p.align(sub[i:i + 1], passes, scale=SCALE, plain=True)
+        acc_p.add_warped(sub[i:i + 1], C.HOMOGRAPHY, o["params"], status=o["status"], weights=o["weight"],
+                         scale=SCALE)
+    torch.cuda.synchronize()
+    plain_fps = pn / (time.perf_counter() - t0)
+
+    # ---------------------------------------------------------- CPU baseline
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle as O
+        O.build()
+        threads = os.cpu_count() or 1
+        rate, dt = cpu_reference_rate(sub, ref, min(args.ref_sample, pn), threads)
+        cpu = {"value": rate, "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": f"{min(args.ref_sample, pn)} frames of the workload (oracle FP64 pipeline, OpenMP, "
+                         f"{dt:.1f} s)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {**workload_cfg(n), "parallelism": f"replicas x{ws}"},
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+                "clocks": clk, "gpu_launches": launches,
+                "plain": {"value": plain_fps, "unit": "frames/s", "frames": pn,
+                          "form": "one frame per call, one launch per Gauss-Newton step, host sync per step"},
+                "batched_over_plain": value / ws / plain_fps,
+                "accuracy": {"warp_rms_vs_truth_px_median": med_rms, "warp_rms_vs_truth_px_max": max_rms,
+                             "frames_ok": int((res["status"] == 0).sum())},
+                "levels": level_table}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,285 @@
+/*
+ * serstacker_gb300.h -- C ABI of the GB300 (sm_103a) frame registration +
+ * stacking library (libsst_gb300.so).
+ *
+ * This is the drop-in boundary for SerStacker's registration and stacking hot
+ * path. Every entry point names the reference interface it replaces
+ * (paths relative to the SerStacker source tree). Plain C: pointers, sizes
+ * and ints only; every call returns an int status (SST_OK = 0, negative on
+ * error) and sst_last_error() describes the most recent failure of the
+ * calling thread. No C++ exception crosses this boundary.
+ *
+ * Images are row-major. `depth` uses OpenCV depth codes (CV_8U = 0,
+ * CV_16U = 2, CV_32F = 5). Buffers are host or device memory as stated by
+ * each call's `on_device` flag; host buffers may be pageable or pinned
+ * (pinned host memory is copied asynchronously).
+ */
+#ifndef SERSTACKER_GB300_H
+#define SERSTACKER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+#define SST_OK                  0
+#define SST_ERR_INVALID_ARG    -1
+#define SST_ERR_CUDA           -2
+#define SST_ERR_UNSUPPORTED    -3
+#define SST_ERR_STATE          -4
+#define SST_ERR_NOMEM          -5
+#define SST_ERR_TIMEOUT        -6
+
+/* per-frame registration status */
+#define SST_FRAME_OK              0
+#define SST_FRAME_SINGULAR        1   /* Cholesky of the Gauss-Newton matrix failed (ecc2.cc:1331-1335) */
+#define SST_FRAME_EMPTY_MASK      2   /* no valid pixel after warping */
+#define SST_FRAME_LOW_RHO         3   /* rho < min_rho (c_frame_registration.cc:861-868) */
+#define SST_FRAME_NAN             4   /* non-finite parameters */
+#define SST_FRAME_NOT_INVERTIBLE  5   /* IC / IC-LM with a non-invertible model (ecc2.cc:1702-1705) */
+
+/* IMAGE_MOTION_TYPE (core/proc/image_registration/image_transform.h:15-26) */
+#define SST_MOTION_TRANSLATION          0
+#define SST_MOTION_EUCLIDEAN            1   /* euclidean with fixed scale (image_transform.cc:35-39) */
+#define SST_MOTION_SCALED_EUCLIDEAN     2
+#define SST_MOTION_AFFINE               3
+#define SST_MOTION_HOMOGRAPHY           4
+#define SST_MOTION_SEMI_QUADRATIC       5
+#define SST_MOTION_QUADRATIC            6
+#define SST_MOTION_EPIPOLAR_DEROTATION  7
+
+/* ECC_ALIGN_METHOD (core/proc/image_registration/ecc2.h:57-62) */
+#define SST_ECC_FORWARD_ADDITIVE          0
+#define SST_ECC_INVERSE_COMPOSITIONAL     1
+#define SST_ECC_LM                        2
+#define SST_ECC_INVERSE_COMPOSITIONAL_LM  3
+
+/* cv::BorderTypes subset (ECC_BORDER_MODE, ecc2.h:44-54) */
+#define SST_BORDER_CONSTANT    0
+#define SST_BORDER_REPLICATE   1
+#define SST_BORDER_REFLECT     2
+#define SST_BORDER_REFLECT101  4
+
+/* pixel depths (OpenCV codes) */
+#define SST_DEPTH_U8   0
+#define SST_DEPTH_U16  2
+#define SST_DEPTH_F32  5
+
+/* COLORID Bayer patterns (core/io/debayer.h:19-34) */
+#define SST_COLORID_BAYER_RGGB  8
+#define SST_COLORID_BAYER_GRBG  9
+#define SST_COLORID_BAYER_GBRG 10
+#define SST_COLORID_BAYER_BGGR 11
+
+/* Motion model: the transform object of create_image_transform()
+ * (core/proc/image_registration/image_transform.cc:32-60). The fix flags
+ * apply to the euclidean models; EUCLIDEAN forces fix_scale = 1. The
+ * euclidean centre is (0,0), as in the reference default
+ * (c_image_transform.cc:275-286). */
+typedef struct sst_motion_model {
+  int32_t type;
+  int32_t fix_translation;
+  int32_t fix_rotation;
+  int32_t fix_scale;
+} sst_motion_model;
+
+/* c_ecch_options (core/proc/image_registration/ecc2.h:158-172) with the
+ * registration-level settings of c_ecc_registration_options
+ * (core/proc/image_registration/c_frame_registration.h:47-63) that the
+ * batched registration uses. */
+typedef struct sst_ecch_options {
+  double epsx;                     /* stop when eps(dp) < epsx at level 0; x2 per coarser level */
+  double reference_smooth_sigma;   /* Gaussian pre-smooth of the reference (sepFilter2D, REPLICATE) */
+  double input_smooth_sigma;       /* Gaussian pre-smooth of each frame */
+  double update_step_scale;
+  int32_t method;                  /* SST_ECC_* */
+  int32_t interpolation;           /* only ECC_INTER_LINEAR (1) is accepted */
+  int32_t max_iterations;
+  int32_t minimum_image_size;
+  int32_t maxlevel;                /* c_ecch maxlevel: number of pyramid levels limit */
+  double min_rho;                  /* correlation gate after alignment; <= 0 reports rho without gating */
+  int32_t ic_jacobian_at_identity; /* must be 1: IC steepest-descent images at the identity warp */
+  int32_t reserved;
+} sst_ecch_options;
+
+/* The reference defaults of c_ecch_options (ecc2.h:158-172). */
+void sst_ecch_options_default(sst_ecch_options * opts);
+
+/* ---------------------------------------------------------------- library */
+
+/* Human-readable description of the calling thread's last error. */
+const char * sst_last_error(void);
+
+/* Library version string. */
+const char * sst_version(void);
+
+/* Number of visible CUDA devices (0 when no driver / no GPU). */
+int sst_device_count(void);
+
+/* --------------------------------------------------- batched c_ecch engine */
+
+typedef struct sst_ecch sst_ecch;
+
+/* c_ecch::c_ecch(const c_ecch_options &) (ecc2.h:198-203). Allocates nothing
+ * on the device until set_reference_image. */
+int sst_ecch_create(sst_ecch ** out, const sst_ecch_options * opts);
+int sst_ecch_destroy(sst_ecch * h);
+
+/* c_ecch::set_reference_image(reference_image, reference_mask)
+ * (ecc2.cc:984-1057): converts to f32 (ecc_convert_input_image,
+ * ecc2.cc:345-382; `scale` multiplies the converted values), smooths with
+ * reference_smooth_sigma, builds the pyramid (pyrDown, nearest mask resize)
+ * and precomputes the inverse-compositional Gauss-Newton matrices per level.
+ * mask may be NULL (u8, 0 = invalid). */
+int sst_ecch_set_reference_image(sst_ecch * h, const void * image, int depth, int width, int height,
+    size_t row_stride, double scale, const uint8_t * mask, size_t mask_stride, int on_device, void * stream);
+
+/* Number of pyramid levels of the current reference (c_ecch::_pyramid.size()). */
+int sst_ecch_num_levels(const sst_ecch * h);
+
+/* Batched c_ecch::align(current_image, current_mask) (ecc2.cc:1123-1176)
+ * for n frames, followed by compute_correlation (ecc2.cc:100-137) and the
+ * min_rho gate of c_frame_registration::register_frame
+ * (c_frame_registration.cc:852-868).
+ *
+ * frames : n images, frame k at frames + k * frame_stride (bytes)
+ * passes : motion models run in sequence; pass k+1 starts from the result of
+ *          pass k (e.g. AFFINE then HOMOGRAPHY). 1 <= num_passes <= 3.
+ * params_inout : n x 12 floats. On input, when `use_initial_params` is
+ *          non-zero, the initial parameter vector of the first pass at full
+ *          resolution (c_image_transform::parameters() layout); otherwise
+ *          the model's identity. On output, the final parameter vector of the
+ *          last pass (first M entries).
+ * status_out, iterations_out (summed over levels and passes), eps_out
+ *          (level-0 eps of the last pass), rho_out: n entries each, may be NULL.
+ * All frames of one call are registered together: one launch per
+ * Gauss-Newton step covers every frame still iterating (per-frame
+ * convergence masks), and the whole level x iteration schedule is replayed
+ * as one CUDA graph. */
+int sst_ecch_align_batch(sst_ecch * h, const void * frames, int depth, int n, int width, int height,
+    size_t row_stride, size_t frame_stride, double scale, int on_device,
+    int num_passes, const sst_motion_model * passes, int use_initial_params,
+    float * params_inout, int32_t * status_out, int32_t * iterations_out, float * eps_out,
+    float * rho_out, float * weight_out, void * stream);
+
+/* The same registration, driven one frame at a time with one launch per
+ * Gauss-Newton step and a host synchronisation after every step: the plain
+ * one-frame-per-launch CUDA form the batched engine is measured against. */
+int sst_ecch_align_plain(sst_ecch * h, const void * frames, int depth, int n, int width, int height,
+    size_t row_stride, size_t frame_stride, double scale, int on_device,
+    int num_passes, const sst_motion_model * passes, int use_initial_params,
+    float * params_inout, int32_t * status_out, int32_t * iterations_out, float * eps_out,
+    float * rho_out, float * weight_out, void * stream);
+
+/* Timing of the last registration call, per motion pass and pyramid level
+ * (the reference's c_image_registration_status::timings,
+ * c_frame_registration.h:185-207, at level granularity): milliseconds
+ * between CUDA events around the level's Gauss-Newton launches, the number
+ * of frame-iterations executed, and their algorithmic bytes (16 B per pixel
+ * and iteration for IC / IC-LM, 8 B for FA / LM). */
+int sst_ecch_level_stats(sst_ecch * h, int pass, int level, float * ms, double * frame_iterations,
+    double * algorithmic_bytes);
+
+/* --------------------------------------------- weighted average accumulator */
+
+typedef struct sst_weighted_average sst_weighted_average;
+
+/* c_weigthed_average (core/average/c_frame_accumulation.h:39-63). The
+ * accumulator holds compensated (Kahan-Babuska) FP32 sums of w*I and w;
+ * compute() returns their ratio, which equals the reference's running mean
+ * A += (I - A) w / W (c_frame_accumulation.cc:104-122) in exact arithmetic. */
+int sst_weighted_average_create(sst_weighted_average ** out, int width, int height);
+int sst_weighted_average_destroy(sst_weighted_average * h);
+
+/* c_weigthed_average::clear (c_frame_accumulation.cc:164-169) */
+int sst_weighted_average_clear(sst_weighted_average * h, void * stream);
+
+/* c_weigthed_average::add(src, weights) (c_frame_accumulation.cc:182-221):
+ * one already-warped frame; weights NULL, u8 mask (depth 0) or f32 (depth 5). */
+int sst_weighted_average_add(sst_weighted_average * h, const void * src, int depth, size_t row_stride,
+    double scale, const void * weights, int weights_depth, size_t weights_stride, int on_device, void * stream);
+
+/* Batched remap + add: for each of n frames, warp the frame with its
+ * parameters (c_frame_registration::base_remap, c_frame_registration.cc:
+ * 1265-1340: LINEAR, `border`, mask LINEAR/CONSTANT >= 255 then 5x5 erode),
+ * multiply the mask by the frame weight (c_image_stacking_pipeline.cc:
+ * 1704-1714) and add (c_frame_accumulation.cc:182-221). Frames whose
+ * status is not SST_FRAME_OK or whose weight is <= 0 are skipped. Each
+ * output pixel is owned by one thread, which accumulates all n frames in
+ * registers before one update of the accumulator. */
+int sst_weighted_average_add_warped_batch(sst_weighted_average * h, const void * frames, int depth, int n,
+    int src_width, int src_height, size_t row_stride, size_t frame_stride, double scale, int on_device,
+    const sst_motion_model * model, const float * params, const int32_t * status, const float * weights,
+    int border, void * stream);
+
+/* c_weigthed_average::compute(avg, mask) (c_frame_accumulation.cc:223-248):
+ * avg (f32, width x height) and mask (u8, 255 where the weight sum > 0) are
+ * host or device buffers per on_device; either may be NULL. */
+int sst_weighted_average_compute(sst_weighted_average * h, float * avg, uint8_t * mask, int on_device, void * stream);
+
+/* c_weigthed_average::get_acc_counters (c_frame_accumulation.cc:250-260): the weight sum. */
+int sst_weighted_average_get_acc_counters(sst_weighted_average * h, float * accw, int on_device, void * stream);
+
+/* c_weigthed_average::reinitialize(src, accw) (c_frame_accumulation.cc:171-180) */
+int sst_weighted_average_reinitialize(sst_weighted_average * h, const float * avg, const float * accw,
+    int on_device, void * stream);
+
+/* c_frame_accumulation::accumulated_frames (c_frame_accumulation.h:29-32) */
+int sst_weighted_average_accumulated_frames(const sst_weighted_average * h);
+
+/* Checkpoint: the full compensated state (4 x width x height f32, sum,
+ * compensation, weight sum, compensation) and the frame count. */
+int sst_weighted_average_save_state(sst_weighted_average * h, float * state4, int32_t * frames, void * stream);
+int sst_weighted_average_load_state(sst_weighted_average * h, const float * state4, int32_t frames, void * stream);
+
+/* ------------------------------------------------------- stacking pipeline */
+
+/* The per-frame body of the stacking pipeline for n frames
+ * (c_image_stacking_pipeline.cc:1539-1790): register each frame against the
+ * reference of `reg` (sst_ecch_align_batch semantics, min_rho gate), warp it
+ * with the registered transform (base_remap, c_frame_registration.cc:
+ * 1265-1340), weight it (1, or its Laplacian-energy sharpness when
+ * `weighting` is 1) and add it to `acc`. Host frames are streamed to the
+ * device in chunks whose copies overlap the registration of the previous
+ * chunk. Outputs follow `on_device` and may be NULL. */
+int sst_stack_frames(sst_ecch * reg, sst_weighted_average * acc, const void * frames, int depth, int n,
+    int width, int height, size_t row_stride, size_t frame_stride, double scale, int on_device,
+    int num_passes, const sst_motion_model * passes, int border, int weighting,
+    float * params_out, int32_t * status_out, float * rho_out, float * weight_out, void * stream);
+
+/* Frames per chunk used by sst_stack_frames (default 256). */
+int sst_set_chunk_frames(sst_ecch * h, int frames);
+
+/* Number of kernels the library launched since the last call of this
+ * function (graph replays count every kernel node they run). */
+long long sst_kernel_launch_count(int reset);
+
+/* ----------------------------------------------------------- utilities */
+
+/* c_frame_registration::base_remap of one frame (c_frame_registration.cc:
+ * 1265-1340) with the transform of `model`/`params`: dst f32 (dst_width x
+ * dst_height), dst_mask u8 (LINEAR/CONSTANT >= 255, 5x5 erode), either may
+ * be NULL. Device buffers only. */
+int sst_remap(const void * src, int depth, int src_width, int src_height, size_t row_stride, double scale,
+    const sst_motion_model * model, const float * params, int border,
+    float * dst, uint8_t * dst_mask, int dst_width, int dst_height, void * stream);
+
+/* extract_bayer_planes (core/io/debayer.cc:96-147): u16 mosaic (even
+ * width/height) -> 4 interleaved u16 planes of (width/2 x height/2), in the
+ * mosaic order. Bit-exact. Device buffers. */
+int sst_extract_bayer_planes_u16(const uint16_t * src, int width, int height, size_t row_stride,
+    uint16_t * dst, void * stream);
+
+/* average_bayer_planes (core/io/debayer.cc:277-330) of a raw mosaic:
+ * (c1 + sum of the 2x2 block) / 4 in integer arithmetic. Bit-exact. */
+int sst_average_bayer_planes_u16(const uint16_t * src, int width, int height, size_t row_stride,
+    uint16_t * dst, void * stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SERSTACKER_GB300_H */

@@ -1019,6 +1019,12 @@ static void convert_state(const orc_model * from, const double * s, const orc_mo
     a[3] = sc * sa, a[4] = sc * ca, a[5] = s[1] - sc * sa * s[4] - sc * ca * s[5];
     break;
   }
+  case ORC_MOTION_SEMI_QUADRATIC:
+    a[0] = s[0], a[1] = s[1], a[2] = s[2], a[3] = s[4], a[4] = s[5], a[5] = s[6];
+    break;
+  case ORC_MOTION_QUADRATIC:
+    a[0] = s[0], a[1] = s[1], a[2] = s[2], a[3] = s[6], a[4] = s[7], a[5] = s[8];
+    break;
   default: memcpy(a, s, sizeof(a));
   }
   switch ( to->type ) {
@@ -1031,9 +1037,18 @@ static void convert_state(const orc_model * from, const double * s, const orc_mo
     break;
   case ORC_MOTION_SEMI_QUADRATIC:
     out[0] = a[0], out[1] = a[1], out[2] = a[2], out[4] = a[3], out[5] = a[4], out[6] = a[5];
+    if( from->type == ORC_MOTION_SEMI_QUADRATIC ) memcpy(out, s, 8 * sizeof(double));
     break;
   case ORC_MOTION_QUADRATIC:
     out[0] = a[0], out[1] = a[1], out[2] = a[2], out[6] = a[3], out[7] = a[4], out[8] = a[5];
+    if( from->type == ORC_MOTION_SEMI_QUADRATIC ) out[3] = s[3], out[9] = s[7];
+    if( from->type == ORC_MOTION_QUADRATIC ) memcpy(out, s, 12 * sizeof(double));
+    break;
+  case ORC_MOTION_EUCLIDEAN:
+  case ORC_MOTION_SCALED_EUCLIDEAN:
+    out[0] = a[2], out[1] = a[5];
+    out[2] = std::atan2(a[3], a[0]);
+    if( to->type == ORC_MOTION_SCALED_EUCLIDEAN ) out[3] = std::sqrt(a[0] * a[0] + a[3] * a[3]);
     break;
   default: break;
   }

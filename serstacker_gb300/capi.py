@@ -1,0 +1,346 @@
+"""ctypes binding of the C ABI in ``include/serstacker_gb300.h``.
+
+Thin Python classes with the reference's names (``c_ecch``,
+``c_weigthed_average``) over ``libsst_gb300.so``. Host numpy buffers are
+passed with ``on_device=0``; device buffers (e.g. torch CUDA tensors) with
+``on_device=1`` and their ``data_ptr()``. Errors raise ``SSTError`` carrying
+``sst_last_error()``. There is no CPU fallback: if the library cannot be
+loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+# status / enums (serstacker_gb300.h)
+SST_OK = 0
+FRAME_OK, FRAME_SINGULAR, FRAME_EMPTY_MASK, FRAME_LOW_RHO, FRAME_NAN, FRAME_NOT_INVERTIBLE = range(6)
+TRANSLATION, EUCLIDEAN, SCALED_EUCLIDEAN, AFFINE, HOMOGRAPHY, SEMI_QUADRATIC, QUADRATIC, EPIPOLAR = range(8)
+FA, IC, LM, ICLM = range(4)
+BORDER_CONSTANT, BORDER_REPLICATE, BORDER_REFLECT, BORDER_REFLECT101 = 0, 1, 2, 4
+DEPTH_U8, DEPTH_U16, DEPTH_F32 = 0, 2, 5
+
+_NP_DEPTH = {np.dtype(np.uint8): DEPTH_U8, np.dtype(np.uint16): DEPTH_U16, np.dtype(np.float32): DEPTH_F32}
+
+
+class SSTError(RuntimeError):
+    pass
+
+
+class MotionModel(C.Structure):
+    _fields_ = [("type", C.c_int32), ("fix_translation", C.c_int32), ("fix_rotation", C.c_int32),
+                ("fix_scale", C.c_int32)]
+
+
+def motion(t: int) -> MotionModel:
+    """create_image_transform(t): EUCLIDEAN fixes the scale (image_transform.cc:35-39)."""
+    return MotionModel(t, 0, 0, 1 if t == EUCLIDEAN else 0)
+
+
+def nparams(t: int) -> int:
+    return {TRANSLATION: 2, EUCLIDEAN: 3, SCALED_EUCLIDEAN: 4, AFFINE: 6, HOMOGRAPHY: 8, SEMI_QUADRATIC: 8,
+            QUADRATIC: 12, EPIPOLAR: 8}[t]
+
+
+class EcchOptions(C.Structure):
+    """c_ecch_options (ecc2.h:158-172) + the registration's min_rho."""
+    _fields_ = [("epsx", C.c_double), ("reference_smooth_sigma", C.c_double), ("input_smooth_sigma", C.c_double),
+                ("update_step_scale", C.c_double), ("method", C.c_int32), ("interpolation", C.c_int32),
+                ("max_iterations", C.c_int32), ("minimum_image_size", C.c_int32), ("maxlevel", C.c_int32),
+                ("min_rho", C.c_double), ("ic_jacobian_at_identity", C.c_int32), ("reserved", C.c_int32)]
+
+
+_lib = None
+LIB_PATH = _build.LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = C.CDLL(path)
+        p, i, d, sz = C.c_void_p, C.c_int, C.c_double, C.c_size_t
+        sigs = {
+            "sst_last_error": (C.c_char_p, []),
+            "sst_version": (C.c_char_p, []),
+            "sst_device_count": (i, []),
+            "sst_kernel_launch_count": (C.c_longlong, [i]),
+            "sst_ecch_options_default": (None, [p]),
+            "sst_ecch_create": (i, [p, p]),
+            "sst_ecch_destroy": (i, [p]),
+            "sst_ecch_set_reference_image": (i, [p, p, i, i, i, sz, d, p, sz, i, p]),
+            "sst_ecch_num_levels": (i, [p]),
+            "sst_ecch_align_batch": (i, [p, p, i, i, i, i, sz, sz, d, i, i, p, i, p, p, p, p, p, p, p]),
+            "sst_ecch_align_plain": (i, [p, p, i, i, i, i, sz, sz, d, i, i, p, i, p, p, p, p, p, p, p]),
+            "sst_set_chunk_frames": (i, [p, i]),
+            "sst_ecch_level_stats": (i, [p, i, i, p, p, p]),
+            "sst_weighted_average_create": (i, [p, i, i]),
+            "sst_weighted_average_destroy": (i, [p]),
+            "sst_weighted_average_clear": (i, [p, p]),
+            "sst_weighted_average_add": (i, [p, p, i, sz, d, p, i, sz, i, p]),
+            "sst_weighted_average_add_warped_batch": (i, [p, p, i, i, i, i, sz, sz, d, i, p, p, p, p, i, p]),
+            "sst_weighted_average_compute": (i, [p, p, p, i, p]),
+            "sst_weighted_average_get_acc_counters": (i, [p, p, i, p]),
+            "sst_weighted_average_reinitialize": (i, [p, p, p, i, p]),
+            "sst_weighted_average_accumulated_frames": (i, [p]),
+            "sst_weighted_average_save_state": (i, [p, p, p, p]),
+            "sst_weighted_average_load_state": (i, [p, p, C.c_int32, p]),
+            "sst_stack_frames": (i, [p, p, p, i, i, i, i, sz, sz, d, i, i, p, i, i, p, p, p, p, p]),
+            "sst_remap": (i, [p, i, i, i, sz, d, p, p, i, p, p, i, i, p]),
+            "sst_extract_bayer_planes_u16": (i, [p, i, i, sz, p, p]),
+            "sst_average_bayer_planes_u16": (i, [p, i, i, sz, p, p]),
+        }
+        for name, (res, args) in sigs.items():
+            f = getattr(_lib, name)
+            f.restype = res
+            f.argtypes = args
+    return _lib
+
+
+def exported_symbols() -> list:
+    """Names of every entry point declared in include/serstacker_gb300.h."""
+    import re
+    hdr = os.path.join(os.path.dirname(_build.HERE), "include", "serstacker_gb300.h")
+    names = re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(sst_\w+)\s*\(", open(hdr).read(), re.M)
+    return sorted(set(names))
+
+
+def _check(rc: int, what: str):
+    if rc != SST_OK:
+        raise SSTError(f"{what} failed ({rc}): {lib().sst_last_error().decode(errors='replace')}")
+
+
+def last_error() -> str:
+    return lib().sst_last_error().decode(errors="replace")
+
+
+def kernel_launch_count(reset: bool = False) -> int:
+    return lib().sst_kernel_launch_count(1 if reset else 0)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if isinstance(a, int):
+        return a
+    return a.data_ptr()   # torch tensor
+
+
+def default_options(**kw) -> EcchOptions:
+    o = EcchOptions()
+    lib().sst_ecch_options_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class c_ecch:
+    """Batched c_ecch (ecc2.h:193-308) over the C ABI."""
+
+    def __init__(self, options: Optional[EcchOptions] = None, **kw):
+        self.options = options if options is not None else default_options(**kw)
+        self._h = C.c_void_p()
+        _check(lib().sst_ecch_create(C.byref(self._h), C.byref(self.options)), "sst_ecch_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_ecch_destroy(h)
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_reference_image(self, image: np.ndarray, mask: Optional[np.ndarray] = None, scale: float = 1.0):
+        img = np.ascontiguousarray(image)
+        depth = _NP_DEPTH[img.dtype]
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        _check(lib().sst_ecch_set_reference_image(self._h, _ptr(img), depth, img.shape[1], img.shape[0],
+                                                  img.strides[0], scale, _ptr(m), 0 if m is None else m.strides[0],
+                                                  0, None), "set_reference_image")
+
+    def num_levels(self) -> int:
+        return lib().sst_ecch_num_levels(self._h)
+
+    def set_chunk_frames(self, n: int):
+        _check(lib().sst_set_chunk_frames(self._h, n), "set_chunk_frames")
+
+    def level_stats(self, pass_index: int, level: int):
+        """(ms, frame_iterations, algorithmic_bytes) of the last call at one pass / level."""
+        ms, fi, ab = C.c_float(), C.c_double(), C.c_double()
+        _check(lib().sst_ecch_level_stats(self._h, pass_index, level, C.byref(ms), C.byref(fi), C.byref(ab)),
+               "level_stats")
+        return ms.value, fi.value, ab.value
+
+    def align(self, frames: np.ndarray, passes: Sequence[int], scale: float = 1.0, init_params=None,
+              plain: bool = False):
+        """Register a (n, h, w) stack of host frames. Returns a dict of arrays."""
+        fr = np.ascontiguousarray(frames)
+        if fr.ndim == 2:
+            fr = fr[None]
+        n, hh, ww = fr.shape
+        depth = _NP_DEPTH[fr.dtype]
+        models = (MotionModel * len(passes))(*[motion(t) for t in passes])
+        params = np.zeros((n, 12), np.float32)
+        if init_params is not None:
+            ip = np.asarray(init_params, np.float32)
+            params[:, :ip.shape[-1]] = ip
+        status = np.zeros(n, np.int32)
+        iters = np.zeros(n, np.int32)
+        eps = np.zeros(n, np.float32)
+        rho = np.zeros(n, np.float32)
+        weight = np.zeros(n, np.float32)
+        fn = lib().sst_ecch_align_plain if plain else lib().sst_ecch_align_batch
+        _check(fn(self._h, _ptr(fr), depth, n, ww, hh, fr.strides[1], fr.strides[0], scale, 0, len(passes), models,
+                  1 if init_params is not None else 0, _ptr(params), _ptr(status), _ptr(iters), _ptr(eps), _ptr(rho),
+                  _ptr(weight), None), "align")
+        M = nparams(passes[-1])
+        return {"params": params[:, :M], "status": status, "iterations": iters, "eps": eps, "rho": rho,
+                "weight": weight}
+
+
+class c_weigthed_average:
+    """c_weigthed_average (c_frame_accumulation.h:39-63) over the C ABI."""
+
+    def __init__(self, width: int, height: int):
+        self.width, self.height = width, height
+        self._h = C.c_void_p()
+        _check(lib().sst_weighted_average_create(C.byref(self._h), width, height), "sst_weighted_average_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_weighted_average_destroy(h)
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def clear(self):
+        _check(lib().sst_weighted_average_clear(self._h, None), "clear")
+
+    def add(self, src: np.ndarray, weights: Optional[np.ndarray] = None, scale: float = 1.0):
+        s = np.ascontiguousarray(src)
+        w = None if weights is None else np.ascontiguousarray(weights)
+        wd = 0 if w is None else _NP_DEPTH[w.dtype]
+        _check(lib().sst_weighted_average_add(self._h, _ptr(s), _NP_DEPTH[s.dtype], s.strides[0], scale, _ptr(w), wd,
+                                              0 if w is None else w.strides[0], 0, None), "add")
+
+    def add_warped(self, frames: np.ndarray, motion_type: int, params: np.ndarray, status=None, weights=None,
+                   scale: float = 1.0, border: int = BORDER_REFLECT101):
+        fr = np.ascontiguousarray(frames)
+        if fr.ndim == 2:
+            fr = fr[None]
+        n, hh, ww = fr.shape
+        p = np.zeros((n, 12), np.float32)
+        pp = np.asarray(params, np.float32).reshape(n, -1)
+        p[:, :pp.shape[1]] = pp
+        st = None if status is None else np.ascontiguousarray(status, np.int32)
+        wt = None if weights is None else np.ascontiguousarray(weights, np.float32)
+        m = motion(motion_type)
+        _check(lib().sst_weighted_average_add_warped_batch(self._h, _ptr(fr), _NP_DEPTH[fr.dtype], n, ww, hh,
+                                                           fr.strides[1], fr.strides[0], scale, 0, C.byref(m),
+                                                           _ptr(p), _ptr(st), _ptr(wt), border, None), "add_warped")
+
+    def compute(self):
+        avg = np.zeros((self.height, self.width), np.float32)
+        mask = np.zeros((self.height, self.width), np.uint8)
+        _check(lib().sst_weighted_average_compute(self._h, _ptr(avg), _ptr(mask), 0, None), "compute")
+        return avg, mask
+
+    def get_acc_counters(self):
+        w = np.zeros((self.height, self.width), np.float32)
+        _check(lib().sst_weighted_average_get_acc_counters(self._h, _ptr(w), 0, None), "get_acc_counters")
+        return w
+
+    def reinitialize(self, avg: np.ndarray, accw: np.ndarray):
+        a = np.ascontiguousarray(avg, np.float32)
+        w = np.ascontiguousarray(accw, np.float32)
+        _check(lib().sst_weighted_average_reinitialize(self._h, _ptr(a), _ptr(w), 0, None), "reinitialize")
+
+    def accumulated_frames(self) -> int:
+        return lib().sst_weighted_average_accumulated_frames(self._h)
+
+    def save_state(self):
+        st = np.zeros((4, self.height, self.width), np.float32)
+        fr = C.c_int32()
+        _check(lib().sst_weighted_average_save_state(self._h, _ptr(st), C.byref(fr), None), "save_state")
+        return st, fr.value
+
+    def load_state(self, state: np.ndarray, frames: int):
+        s = np.ascontiguousarray(state, np.float32)
+        _check(lib().sst_weighted_average_load_state(self._h, _ptr(s), frames, None), "load_state")
+
+
+def stack_frames(reg: c_ecch, acc: c_weigthed_average, frames, passes: Sequence[int], scale: float,
+                 weighting: int = 1, border: int = BORDER_REFLECT101, on_device: bool = False, n=None,
+                 width=None, height=None, depth=None, row_stride=None, frame_stride=None, outputs=None,
+                 host_input: bool = False):
+    """sst_stack_frames: register + warp + stack a sequence.
+
+    frames: a numpy (n, h, w) array (host), or a raw pointer / torch tensor with
+    explicit n, width, height, depth and strides. `on_device` says where the
+    frames and the outputs live; `host_input` marks a raw host pointer (e.g. a
+    pinned torch tensor's data_ptr()) whose outputs are host buffers too.
+    """
+    if isinstance(frames, np.ndarray):
+        fr = np.ascontiguousarray(frames)
+        n, height, width = fr.shape
+        depth = _NP_DEPTH[fr.dtype]
+        row_stride, frame_stride = fr.strides[1], fr.strides[0]
+        ptr = _ptr(fr)
+        dev = 0
+    else:
+        ptr = _ptr(frames)
+        dev = 0 if host_input else (1 if on_device else 0)
+    models = (MotionModel * len(passes))(*[motion(t) for t in passes])
+    if outputs is None:
+        outputs = {"params": np.zeros((n, 12), np.float32), "status": np.zeros(n, np.int32),
+                   "rho": np.zeros(n, np.float32), "weight": np.zeros(n, np.float32)}
+    _check(lib().sst_stack_frames(reg.handle, acc.handle, ptr, depth, n, width, height, row_stride, frame_stride,
+                                  scale, dev, len(passes), models, border, weighting,
+                                  _ptr(outputs["params"]), _ptr(outputs["status"]), _ptr(outputs["rho"]),
+                                  _ptr(outputs["weight"]), None), "sst_stack_frames")
+    return outputs
+
+
+def remap(src: np.ndarray, motion_type: int, params, dst_shape=None, border=BORDER_REFLECT101, scale=1.0):
+    """base_remap of one frame on the device (numpy in/out via torch device buffers)."""
+    import torch
+    s = np.ascontiguousarray(src)
+    h, w = s.shape if dst_shape is None else dst_shape
+    ds = torch.from_numpy(s.view(np.uint8) if s.dtype != np.float32 else s).cuda()
+    dst = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+    msk = torch.zeros((h, w), dtype=torch.uint8, device="cuda")
+    p = np.zeros(12, np.float32)
+    pp = np.asarray(params, np.float32).ravel()
+    p[:pp.size] = pp
+    m = motion(motion_type)
+    _check(lib().sst_remap(ds.data_ptr(), _NP_DEPTH[s.dtype], s.shape[1], s.shape[0], s.strides[0], scale,
+                           C.byref(m), _ptr(p), border, dst.data_ptr(), msk.data_ptr(), w, h, None), "sst_remap")
+    torch.cuda.synchronize()
+    return dst.cpu().numpy(), msk.cpu().numpy()
+
+
+def bayer_planes(raw: np.ndarray, average: bool = False):
+    import torch
+    r = np.ascontiguousarray(raw, np.uint16)
+    h, w = r.shape
+    d = torch.from_numpy(r.view(np.int16)).cuda()
+    if average:
+        out = torch.zeros((h // 2, w // 2), dtype=torch.int16, device="cuda")
+        _check(lib().sst_average_bayer_planes_u16(d.data_ptr(), w, h, r.strides[0], out.data_ptr(), None), "bayer")
+    else:
+        out = torch.zeros((h // 2, w // 2, 4), dtype=torch.int16, device="cuda")
+        _check(lib().sst_extract_bayer_planes_u16(d.data_ptr(), w, h, r.strides[0], out.data_ptr(), None), "bayer")
+    torch.cuda.synchronize()
+    return out.cpu().numpy().view(np.uint16)

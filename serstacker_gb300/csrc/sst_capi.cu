@@ -1,0 +1,1198 @@
+/*
+ * sst_capi.cu -- the C ABI of libsst_gb300.so: engine objects, memory layout,
+ * scheduling of the batched registration (CUDA graphs) and the streamed
+ * register + stack pipeline.
+ *
+ * Memory layout in HBM (one engine):
+ *   reference : f32 pyramid (levels back to back), float2 gradient pyramid,
+ *               optional u8 mask pyramid and its 5x5 erosion, per-model IC
+ *               Gauss-Newton matrices (levels x 12 x 12 doubles)
+ *   batch     : per frame slot an f32 pyramid (sum of level areas), a
+ *               FrameState, tile partials (tiles x sums doubles) and a tile
+ *               ticket; one active-frame list per Gauss-Newton step
+ *   staging   : two chunks of input frames for the streamed pipeline
+ * The reference pyramid (~17 MB at 1280x960) stays L2-resident while the
+ * batch streams through.
+ */
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+#include <math.h>
+#include <string>
+#include <vector>
+#include <map>
+#include <atomic>
+#include <algorithm>
+
+#include "sst_engine.cuh"
+#include "sst_stack.cuh"
+
+using namespace sst;
+
+/* ------------------------------------------------------------ errors */
+
+static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches(0);
+
+static int set_error(int code, const char * fmt, ...)
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define SST_CK(call)                                                                  \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if( e_ != cudaSuccess ) {                                                         \
+      return set_error(SST_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+          __FILE__, __LINE__);                                                        \
+    }                                                                                 \
+  } while ( 0 )
+
+#define SST_CK_LAUNCH(call)                                                           \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if( e_ != cudaSuccess ) {                                                         \
+      return set_error(SST_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+          __FILE__, __LINE__);                                                        \
+    }                                                                                 \
+    g_launches.fetch_add(1);                                                          \
+  } while ( 0 )
+
+#define SST_TRY(expr)                                                                 \
+  do {                                                                                \
+    int r_ = (expr);                                                                  \
+    if( r_ != SST_OK ) return r_;                                                     \
+  } while ( 0 )
+
+extern "C" const char * sst_last_error(void)
+{
+  return g_last_error.c_str();
+}
+
+extern "C" const char * sst_version(void)
+{
+  return "serstacker_gb300 0.1 (sm_103a)";
+}
+
+extern "C" int sst_device_count(void)
+{
+  int n = 0;
+  if( cudaGetDeviceCount(&n) != cudaSuccess ) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+extern "C" long long sst_kernel_launch_count(int reset)
+{
+  return reset ? g_launches.exchange(0) : g_launches.load();
+}
+
+extern "C" void sst_ecch_options_default(sst_ecch_options * o)
+{
+  if( !o ) return;
+  memset(o, 0, sizeof(*o));
+  o->epsx = 1e-5;
+  o->reference_smooth_sigma = 1;
+  o->input_smooth_sigma = 1;
+  o->update_step_scale = 1;
+  o->method = SST_ECC_INVERSE_COMPOSITIONAL_LM;
+  o->interpolation = 1;
+  o->max_iterations = 50;
+  o->minimum_image_size = 8;
+  o->maxlevel = 0;
+  o->min_rho = 0;
+  o->ic_jacobian_at_identity = 1;
+}
+
+/* ------------------------------------------------------- device buffers */
+
+namespace {
+
+struct DevBuf {
+  void * p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t bytes)
+  {
+    if( bytes <= n && p ) return cudaSuccess;
+    release();
+    if( bytes == 0 ) bytes = 16;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if( e == cudaSuccess ) n = bytes;
+    else p = nullptr;
+    return e;
+  }
+  void release()
+  {
+    if( p ) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  template<class T> T * as() const { return (T *) p; }
+};
+
+inline int depth_bytes(int depth)
+{
+  switch ( depth ) {
+  case SST_DEPTH_U8: return 1;
+  case SST_DEPTH_U16: return 2;
+  case SST_DEPTH_F32: return 4;
+  }
+  return 0;
+}
+
+/* getGaussianKernel(ksize, sigma > 0) with c_ecch's ksize rule (ecc2.cc:1001-1003) */
+inline int gaussian_kernel(double sigma, float * k)
+{
+  const int n = std::max(3, 2 * ((int) (3 * sigma)) + 1);
+  double t[64], sum = 0;
+  for( int i = 0; i < n && i < 64; ++i ) {
+    const double x = i - (n - 1) * 0.5;
+    t[i] = exp(-0.5 * x * x / (sigma * sigma));
+    sum += t[i];
+  }
+  for( int i = 0; i < n && i < 64; ++i ) k[i] = (float) (t[i] / sum);
+  return n;
+}
+
+struct GraphEntry {
+  std::vector<long long> key;
+  cudaGraphExec_t exec = nullptr;
+  long long kernels = 0;
+};
+
+}  // namespace
+
+/* ============================================================ sst_ecch */
+
+struct sst_ecch {
+  sst_ecch_options o;
+  cudaStream_t st = nullptr, st_copy = nullptr;
+  cudaEvent_t ev_user = nullptr, ev_done = nullptr, ev_copy[2] = { nullptr, nullptr }, ev_free[2] = { nullptr, nullptr };
+  int num_sms = 0;
+
+  // reference
+  int w = 0, h = 0, L = 0;
+  int lw[32], lh[32];
+  size_t loff[32];
+  size_t pyr_px = 0;
+  DevBuf ref, grad, mask, mask_e, refsrc, jc_id, hpart, gk_in, gk_ref;
+  bool has_mask = false;
+  double RMA[32];
+  float tshift[32];
+  int ks_in = 0;
+  std::map<int, DevBuf> H;
+
+  // batch
+  int cap = 0;
+  int chunk = 256;
+  DevBuf stage[2];
+  DevBuf pyr, fs, part, cnt, lists, counts, lap, init;
+  DevBuf out_params, out_status, out_iters, out_eps, out_rho, out_weight, weff, coeffs;
+  DevBuf res_params, res_status, res_rho, res_weight;   // whole-sequence results of sst_stack_frames
+  size_t part_stride = 0;
+  int steps_cap = 0;
+  int lap_t = 0;
+  std::vector<GraphEntry> graphs;
+  cudaEvent_t prof[3][32][2];
+  bool prof_ready = false;
+  int last_steps[3][32];
+  int last_method = 0;
+
+  ~sst_ecch()
+  {
+    if( prof_ready ) for( auto & a : prof ) for( auto & b : a ) for( auto & e : b ) cudaEventDestroy(e);
+    for( auto & g : graphs ) if( g.exec ) cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+    DevBuf * bufs[] = { &ref, &grad, &mask, &mask_e, &refsrc, &jc_id, &hpart, &gk_in, &gk_ref, &stage[0], &stage[1],
+        &pyr, &fs, &part, &cnt, &lists, &counts, &lap, &init, &out_params, &out_status, &out_iters, &out_eps,
+        &out_rho, &out_weight, &weff, &coeffs, &res_params, &res_status, &res_rho, &res_weight };
+    for( DevBuf * b : bufs ) b->release();
+    for( auto & kv : H ) kv.second.release();
+    if( ev_user ) cudaEventDestroy(ev_user);
+    if( ev_done ) cudaEventDestroy(ev_done);
+    for( int i = 0; i < 2; ++i ) {
+      if( ev_copy[i] ) cudaEventDestroy(ev_copy[i]);
+      if( ev_free[i] ) cudaEventDestroy(ev_free[i]);
+    }
+    if( st ) cudaStreamDestroy(st);
+    if( st_copy ) cudaStreamDestroy(st_copy);
+  }
+
+  void drop_graphs()
+  {
+    for( auto & g : graphs ) if( g.exec ) cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+  }
+};
+
+/* c_ecch::set_reference_image level-count rule (ecc2.cc:1009-1026) */
+static int ecch_num_levels(int w, int h, const sst_ecch_options & o)
+{
+  const int min_size = std::max(4, o.minimum_image_size);
+  int tw = w, th = h, lv = 1;
+  while ( lv < 32 ) {
+    if( o.maxlevel >= 0 && lv >= std::max(0, o.maxlevel) ) break;
+    const int nw = ((tw + 1) >> 1) & ~1, nh = ((th + 1) >> 1) & ~1;
+    if( nw < min_size || nh < min_size ) break;
+    tw = nw, th = nh, ++lv;
+  }
+  return lv;
+}
+
+static int ensure_streams(sst_ecch * h)
+{
+  if( h->st ) return SST_OK;
+  SST_CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  SST_CK(cudaStreamCreateWithFlags(&h->st_copy, cudaStreamNonBlocking));
+  SST_CK(cudaEventCreateWithFlags(&h->ev_user, cudaEventDisableTiming));
+  SST_CK(cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming));
+  for( int i = 0; i < 2; ++i ) {
+    SST_CK(cudaEventCreateWithFlags(&h->ev_copy[i], cudaEventDisableTiming));
+    SST_CK(cudaEventCreateWithFlags(&h->ev_free[i], cudaEventDisableTiming));
+  }
+  for( auto & a : h->prof ) for( auto & b : a ) for( auto & e : b ) SST_CK(cudaEventCreate(&e));
+  h->prof_ready = true;
+  int dev = 0;
+  SST_CK(cudaGetDevice(&dev));
+  SST_CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev));
+  return SST_OK;
+}
+
+/* the internal stream starts after the work the caller queued on its stream */
+static int join_user(sst_ecch * h, void * stream)
+{
+  SST_CK(cudaEventRecord(h->ev_user, (cudaStream_t) stream));
+  SST_CK(cudaStreamWaitEvent(h->st, h->ev_user, 0));
+  return SST_OK;
+}
+
+static int release_to_user(sst_ecch * h, void * stream)
+{
+  SST_CK(cudaEventRecord(h->ev_done, h->st));
+  SST_CK(cudaStreamWaitEvent((cudaStream_t) stream, h->ev_done, 0));
+  return SST_OK;
+}
+
+extern "C" int sst_ecch_create(sst_ecch ** out, const sst_ecch_options * opts)
+{
+  if( !out ) return set_error(SST_ERR_INVALID_ARG, "sst_ecch_create: out is NULL");
+  sst_ecch_options o;
+  if( opts ) o = *opts;
+  else sst_ecch_options_default(&o);
+  if( o.interpolation != 1 ) return set_error(SST_ERR_UNSUPPORTED, "only ECC_INTER_LINEAR interpolation is implemented");
+  if( o.method < 0 || o.method > 3 ) return set_error(SST_ERR_INVALID_ARG, "invalid ECC method %d", o.method);
+  if( o.max_iterations < 0 || o.max_iterations > 1000 ) return set_error(SST_ERR_INVALID_ARG, "max_iterations out of range");
+  if( o.input_smooth_sigma > 5 || o.reference_smooth_sigma > 5 )
+    return set_error(SST_ERR_UNSUPPORTED, "smoothing sigma > 5 is not supported");
+  if( !o.ic_jacobian_at_identity )
+    return set_error(SST_ERR_UNSUPPORTED, "only identity-warp IC steepest-descent images are implemented");
+  sst_ecch * h = new (std::nothrow) sst_ecch();
+  if( !h ) return set_error(SST_ERR_NOMEM, "out of host memory");
+  h->o = o;
+  *out = h;
+  return SST_OK;
+}
+
+extern "C" int sst_ecch_destroy(sst_ecch * h)
+{
+  delete h;
+  return SST_OK;
+}
+
+extern "C" int sst_ecch_num_levels(const sst_ecch * h)
+{
+  return h ? h->L : 0;
+}
+
+extern "C" int sst_set_chunk_frames(sst_ecch * h, int frames)
+{
+  if( !h || frames < 1 ) return set_error(SST_ERR_INVALID_ARG, "invalid chunk size");
+  h->chunk = frames;
+  return SST_OK;
+}
+
+static int upload_image(DevBuf & dst, const void * src, size_t row_stride, int rows, int on_device, const void ** dptr,
+    cudaStream_t st)
+{
+  if( on_device ) {
+    *dptr = src;
+    return SST_OK;
+  }
+  SST_CK(dst.ensure(row_stride * rows));
+  SST_CK(cudaMemcpyAsync(dst.p, src, row_stride * rows, cudaMemcpyHostToDevice, st));
+  *dptr = dst.p;
+  return SST_OK;
+}
+
+extern "C" int sst_ecch_set_reference_image(sst_ecch * h, const void * image, int depth, int width, int height,
+    size_t row_stride, double scale, const uint8_t * mask, size_t mask_stride, int on_device, void * stream)
+{
+  if( !h || !image ) return set_error(SST_ERR_INVALID_ARG, "sst_ecch_set_reference_image: NULL argument");
+  if( depth_bytes(depth) == 0 ) return set_error(SST_ERR_INVALID_ARG, "unsupported depth %d", depth);
+  if( width < 4 || height < 4 ) return set_error(SST_ERR_INVALID_ARG, "image too small: %dx%d", width, height);
+  if( row_stride < (size_t) width * depth_bytes(depth) ) return set_error(SST_ERR_INVALID_ARG, "row_stride too small");
+  if( mask && mask_stride < (size_t) width ) return set_error(SST_ERR_INVALID_ARG, "mask_stride too small");
+  SST_TRY(ensure_streams(h));
+  SST_TRY(join_user(h, stream));
+  cudaStream_t st = h->st;
+  h->drop_graphs();
+  h->H.clear();
+
+  const int L = ecch_num_levels(width, height, h->o);
+  h->w = width, h->h = height, h->L = L;
+  size_t off = 0;
+  for( int l = 0; l < L; ++l ) {
+    if( l == 0 ) h->lw[0] = width, h->lh[0] = height;
+    else h->lw[l] = ((h->lw[l - 1] + 1) >> 1) & ~1, h->lh[l] = ((h->lh[l - 1] + 1) >> 1) & ~1;
+    h->loff[l] = off;
+    off += (size_t) h->lw[l] * h->lh[l];
+  }
+  h->pyr_px = off;
+  SST_CK(h->ref.ensure(off * sizeof(float)));
+  SST_CK(h->grad.ensure(off * sizeof(float2)));
+
+  // Gaussian kernels of the reference and the input pre-smooth
+  float gk[64];
+  int ks_ref = 0;
+  if( h->o.reference_smooth_sigma > 0 ) {
+    ks_ref = gaussian_kernel(h->o.reference_smooth_sigma, gk);
+    SST_CK(h->gk_ref.ensure(64 * sizeof(float)));
+    SST_CK(cudaMemcpyAsync(h->gk_ref.p, gk, ks_ref * sizeof(float), cudaMemcpyHostToDevice, st));
+    SST_CK(cudaStreamSynchronize(st));
+  }
+  if( h->o.input_smooth_sigma > 0 ) {
+    h->ks_in = gaussian_kernel(h->o.input_smooth_sigma, gk);
+    SST_CK(h->gk_in.ensure(64 * sizeof(float)));
+    SST_CK(cudaMemcpyAsync(h->gk_in.p, gk, h->ks_in * sizeof(float), cudaMemcpyHostToDevice, st));
+    SST_CK(cudaStreamSynchronize(st));
+  }
+  else h->ks_in = 0;
+
+  const void * src = nullptr;
+  SST_TRY(upload_image(h->refsrc, image, row_stride, height, on_device, &src, st));
+  float * ref = h->ref.as<float>();
+  SST_CK_LAUNCH(launch_convert_smooth(src, depth, 1, width, height, row_stride, 0, scale,
+      ks_ref ? h->gk_ref.as<float>() : nullptr, ks_ref, ref, 0, st));
+  for( int l = 1; l < L; ++l ) {
+    SST_CK_LAUNCH(launch_pyrdown(ref + h->loff[l - 1], h->lw[l - 1], h->lh[l - 1], 0, ref + h->loff[l], h->lw[l],
+        h->lh[l], 0, 1, st));
+  }
+
+  // masks: level 0 copy, nearest resize per level (c_ecch::downscale_image), 5x5 erosion
+  h->has_mask = mask != nullptr;
+  if( mask ) {
+    SST_CK(h->mask.ensure(off));
+    SST_CK(h->mask_e.ensure(off));
+    uint8_t * m = h->mask.as<uint8_t>();
+    SST_CK(cudaMemcpy2DAsync(m, width, mask, mask_stride, width, height,
+        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    for( int l = 1; l < L; ++l ) {
+      SST_CK_LAUNCH(launch_resize_nearest_u8(m + h->loff[l - 1], h->lw[l - 1], h->lh[l - 1], m + h->loff[l], h->lw[l],
+          h->lh[l], st));
+    }
+    for( int l = 0; l < L; ++l ) {
+      SST_CK_LAUNCH(launch_erode5(m + h->loff[l], h->lw[l], h->lh[l], h->mask_e.as<uint8_t>() + h->loff[l], st));
+    }
+  }
+  for( int l = 0; l < L; ++l ) {
+    SST_CK_LAUNCH(launch_ref_gradients(ref + h->loff[l], mask ? h->mask.as<uint8_t>() + h->loff[l] : nullptr,
+        h->lw[l], h->lh[l], h->grad.as<float2>() + h->loff[l], st));
+  }
+  // per-level statistics: mean (numerical shift) and RMA (valid reference pixels)
+  int tx;
+  const int tmax = tiles_of(width, height, PW_TX, PW_TY, &tx);
+  SST_CK(h->hpart.ensure((size_t) tmax * 78 * sizeof(double)));
+  std::vector<double> hp((size_t) tmax * 3);
+  for( int l = 0; l < L; ++l ) {
+    int tiles = 0;
+    SST_CK_LAUNCH(launch_ref_stats(ref + h->loff[l], mask ? h->mask.as<uint8_t>() + h->loff[l] : nullptr, h->lw[l],
+        h->lh[l], h->hpart.as<double>(), &tiles, st));
+    SST_CK(cudaMemcpyAsync(hp.data(), h->hpart.p, (size_t) tiles * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SST_CK(cudaStreamSynchronize(st));
+    double s = 0, n = 0, m = 0;
+    for( int t = 0; t < tiles; ++t ) s += hp[t * 3], n += hp[t * 3 + 1], m += hp[t * 3 + 2];
+    h->tshift[l] = (float) (n > 0 ? s / n : 0);
+    h->RMA[l] = m;
+  }
+  SST_CK(cudaStreamSynchronize(st));
+  SST_TRY(release_to_user(h, stream));
+  return SST_OK;
+}
+
+/* IC Gauss-Newton matrix per level for one model (identity warp) */
+static int ensure_H(sst_ecch * h, const sst_motion_model & m, const double ** out)
+{
+  const int M = model_nparams(m);
+  const int key = m.type * 16 + M;
+  auto it = h->H.find(key);
+  if( it != h->H.end() ) {
+    *out = it->second.as<double>();
+    return SST_OK;
+  }
+  DevBuf & buf = h->H[key];
+  SST_CK(buf.ensure((size_t) h->L * 144 * sizeof(double)));
+  double s[16];
+  float jc[8];
+  model_identity(m, s);
+  model_sd_coeffs(m, s, jc);
+  SST_CK(h->jc_id.ensure(8 * sizeof(float)));
+  SST_CK(cudaMemcpy(h->jc_id.p, jc, sizeof(jc), cudaMemcpyHostToDevice));
+  const int NS = M * (M + 1) / 2;
+  std::vector<double> hp, Hm((size_t) h->L * 144, 0.0);
+  for( int l = 0; l < h->L; ++l ) {
+    int tiles = 0;
+    SST_CK_LAUNCH(launch_ref_hessian(h->grad.as<float2>() + h->loff[l], h->lw[l], h->lh[l], jac_kind(m.type), M,
+        h->jc_id.as<float>(), h->hpart.as<double>(), &tiles, h->st));
+    hp.resize((size_t) tiles * NS);
+    SST_CK(cudaMemcpyAsync(hp.data(), h->hpart.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    SST_CK(cudaStreamSynchronize(h->st));
+    double * Hl = Hm.data() + (size_t) l * 144;
+    for( int t = 0; t < tiles; ++t ) {
+      for( int u = 0, k = 0; u < M; ++u )
+        for( int v = 0; v <= u; ++v, ++k ) Hl[u * M + v] += hp[(size_t) t * NS + k];
+    }
+    for( int u = 0; u < M; ++u ) for( int v = u + 1; v < M; ++v ) Hl[u * M + v] = Hl[v * M + u];
+  }
+  SST_CK(cudaMemcpy(buf.p, Hm.data(), Hm.size() * sizeof(double), cudaMemcpyHostToDevice));
+  *out = buf.as<double>();
+  return SST_OK;
+}
+
+/* timing event: a graph event node while capturing, a plain record otherwise */
+static cudaError_t record_prof(cudaEvent_t e, cudaStream_t st, bool host_driven)
+{
+  return host_driven ? cudaEventRecord(e, st) : cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+}
+
+static int level_tiles(const sst_ecch * h, int l, int method, int * tiles_x)
+{
+  if( method == M_FA || method == M_LM ) return tiles_of(h->lw[l], h->lh[l], ST_TX, ST_TY, tiles_x);
+  return tiles_of(h->lw[l], h->lh[l], PW_TX, PW_TY, tiles_x);
+}
+
+static int ensure_capacity(sst_ecch * h, int n, int method, int num_passes, const sst_motion_model * passes)
+{
+  size_t pstride = 0;
+  for( int k = 0; k < num_passes; ++k ) {
+    const int NS = pass_num_sums(method, model_nparams(passes[k]));
+    for( int l = 0; l < h->L; ++l ) {
+      int tx;
+      pstride = std::max(pstride, (size_t) level_tiles(h, l, method, &tx) * NS);
+    }
+  }
+  int tx;
+  pstride = std::max(pstride, (size_t) tiles_of(h->w, h->h, PW_TX, PW_TY, &tx) * 6);
+  const int steps = 1 + num_passes * h->L * (h->o.max_iterations + 2);
+  const int lap_level = h->L > 1 ? 1 : 0;
+  const int lt = lap_tiles(h->lw[lap_level], h->lh[lap_level]);
+  const bool grow = n > h->cap || pstride > h->part_stride || steps > h->steps_cap || lt != h->lap_t;
+  if( !grow ) return SST_OK;
+  h->drop_graphs();
+  const int cap = std::max(n, h->cap);
+  h->part_stride = std::max(pstride, h->part_stride);
+  h->steps_cap = std::max(steps, h->steps_cap);
+  h->lap_t = lt;
+  SST_CK(h->pyr.ensure((size_t) cap * h->pyr_px * sizeof(float)));
+  SST_CK(h->fs.ensure((size_t) cap * sizeof(FrameState)));
+  SST_CK(h->part.ensure((size_t) cap * h->part_stride * sizeof(double)));
+  SST_CK(h->cnt.ensure((size_t) cap * sizeof(unsigned)));
+  SST_CK(cudaMemsetAsync(h->cnt.p, 0, (size_t) cap * sizeof(unsigned), h->st));
+  SST_CK(h->lists.ensure((size_t) h->steps_cap * cap * sizeof(int)));
+  SST_CK(h->counts.ensure((size_t) h->steps_cap * sizeof(int)));
+  SST_CK(h->lap.ensure((size_t) cap * lt * 2 * sizeof(double)));
+  SST_CK(h->init.ensure((size_t) cap * 16 * sizeof(double)));
+  SST_CK(h->out_params.ensure((size_t) cap * 12 * sizeof(float)));
+  SST_CK(h->out_status.ensure((size_t) cap * sizeof(int32_t)));
+  SST_CK(h->out_iters.ensure((size_t) cap * sizeof(int32_t)));
+  SST_CK(h->out_eps.ensure((size_t) cap * sizeof(float)));
+  SST_CK(h->out_rho.ensure((size_t) cap * sizeof(float)));
+  SST_CK(h->out_weight.ensure((size_t) cap * sizeof(float)));
+  SST_CK(h->weff.ensure((size_t) cap * sizeof(float)));
+  SST_CK(h->coeffs.ensure((size_t) cap * SST_NCOEF * sizeof(float)));
+  h->cap = cap;
+  return SST_OK;
+}
+
+/* The Gauss-Newton schedule of one batch: pass begin, per level a level
+ * begin and max_iterations + 1 pass launches, then the correlation. In
+ * host-driven mode every step is followed by a synchronisation and an early
+ * exit when no frame is left (the plain one-frame-per-launch form). */
+static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, const sst_motion_model * passes,
+    bool have_init, bool host_driven, long long * kernels)
+{
+  cudaStream_t st = h->st;
+  const int L = h->L;
+  const int max_it = h->o.max_iterations;
+  const int grid = std::max(1, h->num_sms) * 4;
+  long long k = 0;
+  SST_CK(cudaMemsetAsync(h->counts.p, 0, (size_t) h->steps_cap * sizeof(int), st));
+  int step = 0;
+  int * lists = h->lists.as<int>();
+  int * counts = h->counts.as<int>();
+  FrameState * fs = h->fs.as<FrameState>();
+  for( int k_pass = 0; k_pass < num_passes; ++k_pass ) {
+    const sst_motion_model & m = passes[k_pass];
+    PassBeginArgs pb;
+    pb.fs = fs, pb.n = n, pb.pass = k_pass, pb.model = m, pb.prev_model = k_pass ? passes[k_pass - 1] : m;
+    pb.init_states = (k_pass == 0 && have_init) ? h->init.as<double>() : nullptr;
+    pb.scale_to_coarsest = L > 1 ? (double) h->lw[L - 1] / (double) h->lw[0] : 0.0;
+    SST_CK_LAUNCH(launch_pass_begin(pb, st));
+    ++k;
+    const double * H = nullptr;
+    if( method == M_IC || method == M_ICLM ) SST_TRY(ensure_H(h, m, &H));
+    for( int l = L - 1; l >= 0; --l ) {
+      SST_CK(record_prof(h->prof[k_pass][l][0], st, host_driven));
+      h->last_steps[k_pass][l] = step;
+      LevelBeginArgs lb;
+      lb.fs = fs, lb.n = n, lb.model = m, lb.method = method;
+      lb.list_out = lists + (size_t) step * h->cap;
+      lb.count_out = counts + step;
+      lb.level_is_first = l == L - 1;
+      SST_CK_LAUNCH(launch_level_begin(lb, st));
+      ++k;
+      PassArgs a;
+      memset(&a, 0, sizeof(a));
+      a.pyr = h->pyr.as<float>();
+      a.pyr_stride = h->pyr_px;
+      a.lvl_off = h->loff[l];
+      a.w = h->lw[l], a.h = h->lh[l];
+      a.tiles = level_tiles(h, l, method, &a.tiles_x);
+      a.refT = h->ref.as<float>() + h->loff[l];
+      a.refG = h->grad.as<float2>() + h->loff[l];
+      a.refM = h->has_mask ? h->mask.as<uint8_t>() + h->loff[l] : nullptr;
+      a.refMe = h->has_mask ? h->mask_e.as<uint8_t>() + h->loff[l] : nullptr;
+      a.H = H ? H + (size_t) l * 144 : nullptr;
+      a.RMA = h->RMA[l];
+      a.tshift = h->tshift[l];
+      {
+        double s[16];
+        model_identity(m, s);
+        model_sd_coeffs(m, s, a.jc_id);
+      }
+      a.fs = fs;
+      a.partials = h->part.as<double>();
+      a.part_stride = h->part_stride;
+      a.counters = h->cnt.as<unsigned>();
+      a.model = m;
+      a.M = model_nparams(m);
+      a.max_eps = h->o.epsx * pow(2.0, l);
+      a.step = h->o.update_step_scale;
+      a.max_it = max_it;
+      a.scale_next = l > 0 ? (double) h->lw[l - 1] / (double) h->lw[l] : 0.0;
+      for( int it = 0; it <= max_it; ++it ) {
+        a.list_in = lists + (size_t) (step + it) * h->cap;
+        a.count_in = counts + step + it;
+        a.list_out = lists + (size_t) (step + it + 1) * h->cap;
+        a.count_out = counts + step + it + 1;
+        SST_CK_LAUNCH(launch_pass(method, a, grid, st));
+        ++k;
+        if( host_driven ) {
+          int c = 0;
+          SST_CK(cudaMemcpyAsync(&c, counts + step + it + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+          SST_CK(cudaStreamSynchronize(st));
+          if( c == 0 ) break;
+        }
+      }
+      SST_CK(record_prof(h->prof[k_pass][l][1], st, host_driven));
+      step += max_it + 2;
+    }
+  }
+  CorrArgs c;
+  c.pyr = h->pyr.as<float>();
+  c.pyr_stride = h->pyr_px;
+  c.w = h->w, c.h = h->h;
+  c.tiles = tiles_of(h->w, h->h, PW_TX, PW_TY, &c.tiles_x);
+  c.refT = h->ref.as<float>();
+  c.refM = h->has_mask ? h->mask.as<uint8_t>() : nullptr;
+  c.tshift = h->tshift[0];
+  c.fs = fs;
+  c.n = n;
+  c.partials = h->part.as<double>();
+  c.part_stride = h->part_stride;
+  c.counters = h->cnt.as<unsigned>();
+  c.model = passes[num_passes - 1];
+  c.min_rho = h->o.min_rho;
+  SST_CK_LAUNCH(launch_correlation(c, grid, st));
+  ++k;
+  if( kernels ) *kernels = k;
+  return SST_OK;
+}
+
+/* per-level timing of the last registration call (CUDA events around each
+ * level's Gauss-Newton launches) and the frame-iterations it executed */
+extern "C" int sst_ecch_level_stats(sst_ecch * h, int pass, int level, float * ms, double * frame_iterations,
+    double * algorithmic_bytes)
+{
+  if( !h || pass < 0 || pass > 2 || level < 0 || level >= h->L || !h->prof_ready )
+    return set_error(SST_ERR_INVALID_ARG, "sst_ecch_level_stats: invalid arguments");
+  SST_CK(cudaStreamSynchronize(h->st));
+  float t = 0;
+  SST_CK(cudaEventElapsedTime(&t, h->prof[pass][level][0], h->prof[pass][level][1]));
+  std::vector<int> c(h->o.max_iterations + 1);
+  SST_CK(cudaMemcpy(c.data(), h->counts.as<int>() + h->last_steps[pass][level], c.size() * sizeof(int),
+      cudaMemcpyDeviceToHost));
+  double fi = 0;
+  for( int v : c ) fi += v;
+  // algorithmic bytes per pixel and frame-iteration: IC / IC-LM read the warped
+  // source (4 B), the template (4 B) and its gradients (8 B); FA / LM read the
+  // warped source and the template and recompute gradients on chip (8 B)
+  const double bpp = (h->last_method == M_IC || h->last_method == M_ICLM) ? 16.0 : 8.0;
+  if( ms ) *ms = t;
+  if( frame_iterations ) *frame_iterations = fi;
+  if( algorithmic_bytes ) *algorithmic_bytes = fi * bpp * (double) h->lw[level] * h->lh[level];
+  return SST_OK;
+}
+
+static int validate_passes(const sst_ecch * h, int num_passes, const sst_motion_model * passes)
+{
+  if( num_passes < 1 || num_passes > 3 || !passes ) return set_error(SST_ERR_INVALID_ARG, "1..3 motion passes are required");
+  for( int k = 0; k < num_passes; ++k ) {
+    const sst_motion_model & m = passes[k];
+    if( m.type < 0 || m.type > 7 ) return set_error(SST_ERR_INVALID_ARG, "invalid motion type %d", m.type);
+    if( is_euclid(m.type) && (m.fix_translation || m.fix_rotation) )
+      return set_error(SST_ERR_UNSUPPORTED, "euclidean with fixed translation or rotation is not implemented");
+    if( m.type == SST_MOTION_EUCLIDEAN && !m.fix_scale )
+      return set_error(SST_ERR_INVALID_ARG, "EUCLIDEAN motion requires fix_scale = 1 (image_transform.cc:35-39)");
+    if( m.type == SST_MOTION_SCALED_EUCLIDEAN && m.fix_scale )
+      return set_error(SST_ERR_INVALID_ARG, "SCALED_EUCLIDEAN motion requires fix_scale = 0");
+  }
+  return SST_OK;
+}
+
+/* Register n device-resident frames; results stay in the engine's device
+ * output arrays. */
+static int register_device(sst_ecch * h, const void * d_frames, int depth, int n, size_t row_stride,
+    size_t frame_stride, double scale, int num_passes, const sst_motion_model * passes,
+    const double * init_states_host, bool plain)
+{
+  cudaStream_t st = h->st;
+  const int method = h->o.method;
+  h->last_method = method;
+  SST_TRY(ensure_capacity(h, n, method, num_passes, passes));
+  if( init_states_host ) {
+    SST_CK(cudaMemcpyAsync(h->init.p, init_states_host, (size_t) n * 16 * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  // pyramid of every frame: convert + pre-smooth, pyrDown
+  float * pyr = h->pyr.as<float>();
+  SST_CK_LAUNCH(launch_convert_smooth(d_frames, depth, n, h->w, h->h, row_stride, frame_stride, scale,
+      h->ks_in ? h->gk_in.as<float>() : nullptr, h->ks_in, pyr, h->pyr_px, st));
+  for( int l = 1; l < h->L; ++l ) {
+    SST_CK_LAUNCH(launch_pyrdown(pyr + h->loff[l - 1], h->lw[l - 1], h->lh[l - 1], h->pyr_px, pyr + h->loff[l], h->lw[l],
+        h->lh[l], h->pyr_px, n, st));
+  }
+  const int lap_level = h->L > 1 ? 1 : 0;
+  SST_CK_LAUNCH(launch_lap_energy(pyr, h->pyr_px, h->loff[lap_level], h->lw[lap_level], h->lh[lap_level], n,
+      h->lap.as<double>(), h->lap_t, st));
+
+  // IC / IC-LM: the per-level matrices must exist before graph capture
+  if( method == M_IC || method == M_ICLM ) {
+    for( int k = 0; k < num_passes; ++k ) {
+      const double * Hd;
+      SST_TRY(ensure_H(h, passes[k], &Hd));
+    }
+  }
+  if( plain ) {
+    long long kk = 0;
+    SST_TRY(enqueue_schedule(h, n, method, num_passes, passes, init_states_host != nullptr, true, &kk));
+  }
+  else {
+    std::vector<long long> key = { n, method, num_passes, init_states_host ? 1 : 0, h->o.max_iterations };
+    for( int k = 0; k < num_passes; ++k ) {
+      key.push_back(passes[k].type);
+      key.push_back(passes[k].fix_scale);
+    }
+    GraphEntry * ge = nullptr;
+    for( auto & g : h->graphs ) if( g.key == key ) ge = &g;
+    if( !ge ) {
+      cudaGraph_t graph = nullptr;
+      SST_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      long long kk = 0;
+      const long long before = g_launches.load();
+      const int r = enqueue_schedule(h, n, method, num_passes, passes, init_states_host != nullptr, false, &kk);
+      g_launches.store(before);
+      cudaError_t e = cudaStreamEndCapture(st, &graph);
+      if( r != SST_OK ) {
+        if( graph ) cudaGraphDestroy(graph);
+        return r;
+      }
+      if( e != cudaSuccess ) return set_error(SST_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+      GraphEntry g;
+      g.key = key;
+      g.kernels = kk;
+      e = cudaGraphInstantiate(&g.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if( e != cudaSuccess ) return set_error(SST_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+      h->graphs.push_back(g);
+      ge = &h->graphs.back();
+    }
+    SST_CK(cudaGraphLaunch(ge->exec, st));
+    g_launches.fetch_add(ge->kernels);
+  }
+  FinalizeArgs fa;
+  fa.fs = h->fs.as<FrameState>();
+  fa.n = n;
+  fa.model = passes[num_passes - 1];
+  fa.lap_partials = h->lap.as<double>();
+  fa.lap_tiles = h->lap_t;
+  fa.params_out = h->out_params.as<float>();
+  fa.status_out = h->out_status.as<int32_t>();
+  fa.iters_out = h->out_iters.as<int32_t>();
+  fa.eps_out = h->out_eps.as<float>();
+  fa.rho_out = h->out_rho.as<float>();
+  fa.weight_out = h->out_weight.as<float>();
+  SST_CK_LAUNCH(launch_finalize(fa, st));
+  return SST_OK;
+}
+
+static int copy_out(void * dst, const void * src, size_t bytes, int on_device, cudaStream_t st)
+{
+  if( !dst ) return SST_OK;
+  SST_CK(cudaMemcpyAsync(dst, src, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+  return SST_OK;
+}
+
+static int init_states_from_params(const sst_motion_model & m, const float * params, int n, int on_device,
+    std::vector<double> & states)
+{
+  std::vector<float> hp((size_t) n * 12);
+  if( on_device ) SST_CK(cudaMemcpy(hp.data(), params, hp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  else memcpy(hp.data(), params, hp.size() * sizeof(float));
+  states.assign((size_t) n * 16, 0.0);
+  const int M = model_nparams(m);
+  for( int f = 0; f < n; ++f ) {
+    double p[12];
+    for( int j = 0; j < M; ++j ) p[j] = hp[(size_t) f * 12 + j];
+    model_identity(m, &states[(size_t) f * 16]);
+    model_set_params(m, &states[(size_t) f * 16], p);
+  }
+  return SST_OK;
+}
+
+static int align_common(sst_ecch * h, const void * frames, int depth, int n, int width, int height,
+    size_t row_stride, size_t frame_stride, double scale, int on_device,
+    int num_passes, const sst_motion_model * passes, int use_initial_params,
+    float * params_inout, int32_t * status_out, int32_t * iterations_out, float * eps_out,
+    float * rho_out, float * weight_out, void * stream, bool plain)
+{
+  if( !h || !frames ) return set_error(SST_ERR_INVALID_ARG, "align: NULL argument");
+  if( h->L == 0 ) return set_error(SST_ERR_STATE, "c_ecch: no reference image was set");
+  if( n < 1 || n > 65535 ) return set_error(SST_ERR_INVALID_ARG, "n = %d out of range 1..65535", n);
+  if( width != h->w || height != h->h )
+    return set_error(SST_ERR_INVALID_ARG, "frame size %dx%d differs from the reference %dx%d", width, height, h->w, h->h);
+  if( depth_bytes(depth) == 0 ) return set_error(SST_ERR_INVALID_ARG, "unsupported depth %d", depth);
+  if( row_stride < (size_t) width * depth_bytes(depth) || frame_stride < row_stride * height )
+    return set_error(SST_ERR_INVALID_ARG, "invalid strides");
+  if( use_initial_params && !params_inout ) return set_error(SST_ERR_INVALID_ARG, "initial parameters are NULL");
+  SST_TRY(validate_passes(h, num_passes, passes));
+  const int method = h->o.method;
+  if( method == M_IC || method == M_ICLM ) {
+    for( int k = 0; k < num_passes; ++k ) {
+      if( !model_invertible(passes[k]) ) {
+        // c_ecc_inverse_compositional::align refuses non-invertible transforms (ecc2.cc:1702-1705)
+        return set_error(SST_ERR_UNSUPPORTED, "inverse compositional ECC requires an invertible motion model");
+      }
+    }
+  }
+  SST_TRY(ensure_streams(h));
+  SST_TRY(join_user(h, stream));
+  cudaStream_t st = h->st;
+  std::vector<double> init;
+  if( use_initial_params ) SST_TRY(init_states_from_params(passes[0], params_inout, n, on_device, init));
+
+  const int chunk = plain ? 1 : n;
+  for( int f0 = 0; f0 < n; f0 += chunk ) {
+    const int nc = std::min(chunk, n - f0);
+    const void * d_frames = nullptr;
+    const uint8_t * fsrc = (const uint8_t *) frames + (size_t) f0 * frame_stride;
+    if( on_device ) d_frames = fsrc;
+    else {
+      SST_CK(h->stage[0].ensure(frame_stride * nc));
+      SST_CK(cudaMemcpyAsync(h->stage[0].p, fsrc, frame_stride * nc, cudaMemcpyHostToDevice, st));
+      d_frames = h->stage[0].p;
+    }
+    SST_TRY(register_device(h, d_frames, depth, nc, row_stride, frame_stride, scale, num_passes, passes,
+        use_initial_params ? init.data() + (size_t) f0 * 16 : nullptr, plain));
+    SST_TRY(copy_out(params_inout ? params_inout + (size_t) f0 * 12 : nullptr, h->out_params.p, (size_t) nc * 12 * sizeof(float), on_device, st));
+    SST_TRY(copy_out(status_out ? status_out + f0 : nullptr, h->out_status.p, (size_t) nc * sizeof(int32_t), on_device, st));
+    SST_TRY(copy_out(iterations_out ? iterations_out + f0 : nullptr, h->out_iters.p, (size_t) nc * sizeof(int32_t), on_device, st));
+    SST_TRY(copy_out(eps_out ? eps_out + f0 : nullptr, h->out_eps.p, (size_t) nc * sizeof(float), on_device, st));
+    SST_TRY(copy_out(rho_out ? rho_out + f0 : nullptr, h->out_rho.p, (size_t) nc * sizeof(float), on_device, st));
+    SST_TRY(copy_out(weight_out ? weight_out + f0 : nullptr, h->out_weight.p, (size_t) nc * sizeof(float), on_device, st));
+    if( plain || !on_device ) SST_CK(cudaStreamSynchronize(st));
+  }
+  if( !on_device ) SST_CK(cudaStreamSynchronize(st));
+  SST_TRY(release_to_user(h, stream));
+  return SST_OK;
+}
+
+extern "C" int sst_ecch_align_batch(sst_ecch * h, const void * frames, int depth, int n, int width, int height,
+    size_t row_stride, size_t frame_stride, double scale, int on_device,
+    int num_passes, const sst_motion_model * passes, int use_initial_params,
+    float * params_inout, int32_t * status_out, int32_t * iterations_out, float * eps_out,
+    float * rho_out, float * weight_out, void * stream)
+{
+  return align_common(h, frames, depth, n, width, height, row_stride, frame_stride, scale, on_device, num_passes,
+      passes, use_initial_params, params_inout, status_out, iterations_out, eps_out, rho_out, weight_out, stream, false);
+}
+
+extern "C" int sst_ecch_align_plain(sst_ecch * h, const void * frames, int depth, int n, int width, int height,
+    size_t row_stride, size_t frame_stride, double scale, int on_device,
+    int num_passes, const sst_motion_model * passes, int use_initial_params,
+    float * params_inout, int32_t * status_out, int32_t * iterations_out, float * eps_out,
+    float * rho_out, float * weight_out, void * stream)
+{
+  return align_common(h, frames, depth, n, width, height, row_stride, frame_stride, scale, on_device, num_passes,
+      passes, use_initial_params, params_inout, status_out, iterations_out, eps_out, rho_out, weight_out, stream, true);
+}
+
+/* ================================================ sst_weighted_average */
+
+struct sst_weighted_average {
+  int w = 0, h = 0;
+  DevBuf acc, coeffs, weff, src, wsrc;
+  int frames = 0;
+  size_t plane() const { return (size_t) w * h; }
+  ~sst_weighted_average()
+  {
+    acc.release(), coeffs.release(), weff.release(), src.release(), wsrc.release();
+  }
+};
+
+extern "C" int sst_weighted_average_create(sst_weighted_average ** out, int width, int height)
+{
+  if( !out || width < 1 || height < 1 ) return set_error(SST_ERR_INVALID_ARG, "sst_weighted_average_create: invalid arguments");
+  sst_weighted_average * a = new (std::nothrow) sst_weighted_average();
+  if( !a ) return set_error(SST_ERR_NOMEM, "out of host memory");
+  a->w = width, a->h = height;
+  cudaError_t e = a->acc.ensure(4 * a->plane() * sizeof(float));
+  if( e == cudaSuccess ) e = cudaMemset(a->acc.p, 0, 4 * a->plane() * sizeof(float));
+  if( e != cudaSuccess ) {
+    delete a;
+    return set_error(SST_ERR_CUDA, "accumulator allocation failed: %s", cudaGetErrorString(e));
+  }
+  *out = a;
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_destroy(sst_weighted_average * a)
+{
+  delete a;
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_clear(sst_weighted_average * a, void * stream)
+{
+  if( !a ) return set_error(SST_ERR_INVALID_ARG, "NULL accumulator");
+  SST_CK(cudaMemsetAsync(a->acc.p, 0, 4 * a->plane() * sizeof(float), (cudaStream_t) stream));
+  a->frames = 0;
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_accumulated_frames(const sst_weighted_average * a)
+{
+  return a ? a->frames : 0;
+}
+
+extern "C" int sst_weighted_average_add(sst_weighted_average * a, const void * src, int depth, size_t row_stride,
+    double scale, const void * weights, int weights_depth, size_t weights_stride, int on_device, void * stream)
+{
+  if( !a || !src ) return set_error(SST_ERR_INVALID_ARG, "sst_weighted_average_add: NULL argument");
+  if( depth_bytes(depth) == 0 ) return set_error(SST_ERR_INVALID_ARG, "unsupported depth %d", depth);
+  if( weights && weights_depth != SST_DEPTH_U8 && weights_depth != SST_DEPTH_F32 )
+    return set_error(SST_ERR_INVALID_ARG, "weights must be CV_8UC1 or CV_32FC1");
+  cudaStream_t st = (cudaStream_t) stream;
+  const void * dsrc = src, * dw = weights;
+  if( !on_device ) {
+    SST_CK(a->src.ensure(row_stride * a->h));
+    SST_CK(cudaMemcpyAsync(a->src.p, src, row_stride * a->h, cudaMemcpyHostToDevice, st));
+    dsrc = a->src.p;
+    if( weights ) {
+      SST_CK(a->wsrc.ensure(weights_stride * a->h));
+      SST_CK(cudaMemcpyAsync(a->wsrc.p, weights, weights_stride * a->h, cudaMemcpyHostToDevice, st));
+      dw = a->wsrc.p;
+    }
+  }
+  SST_CK_LAUNCH(launch_stack_add_plain(dsrc, depth, row_stride, scale, dw, weights_depth, weights_stride, a->w, a->h,
+      a->acc.as<float>(), a->plane(), st));
+  if( !on_device ) SST_CK(cudaStreamSynchronize(st));
+  ++a->frames;
+  return SST_OK;
+}
+
+static int add_warped_device(sst_weighted_average * a, const void * d_frames, int depth, int n, int sw, int sh,
+    size_t row_stride, size_t frame_stride, double scale, const sst_motion_model & m, const float * d_params,
+    const int32_t * d_status, const float * d_weights, cudaStream_t st)
+{
+  SST_CK(a->coeffs.ensure((size_t) n * SST_NCOEF * sizeof(float)));
+  SST_CK(a->weff.ensure((size_t) n * sizeof(float)));
+  SST_CK_LAUNCH(launch_coeffs_from_params(m, d_params, n, a->coeffs.as<float>(), st));
+  SST_CK_LAUNCH(launch_effective_weights(d_weights, d_status, n, a->weff.as<float>(), st));
+  StackArgs s;
+  s.frames = (const uint8_t *) d_frames;
+  s.row_stride = row_stride, s.frame_stride = frame_stride;
+  s.sw = sw, s.sh = sh, s.n = n;
+  s.scale = (float) scale;
+  s.coeffs = a->coeffs.as<float>();
+  s.weights = a->weff.as<float>();
+  s.dw = a->w, s.dh = a->h;
+  s.acc = a->acc.as<float>();
+  s.plane = a->plane();
+  SST_CK_LAUNCH(launch_stack_add_warped(s, m.type, depth, st));
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_add_warped_batch(sst_weighted_average * a, const void * frames, int depth, int n,
+    int src_width, int src_height, size_t row_stride, size_t frame_stride, double scale, int on_device,
+    const sst_motion_model * model, const float * params, const int32_t * status, const float * weights,
+    int border, void * stream)
+{
+  if( !a || !frames || !model || !params ) return set_error(SST_ERR_INVALID_ARG, "add_warped_batch: NULL argument");
+  if( n < 1 ) return set_error(SST_ERR_INVALID_ARG, "n must be >= 1");
+  if( depth_bytes(depth) == 0 ) return set_error(SST_ERR_INVALID_ARG, "unsupported depth %d", depth);
+  if( row_stride < (size_t) src_width * depth_bytes(depth) || frame_stride < row_stride * src_height )
+    return set_error(SST_ERR_INVALID_ARG, "invalid strides");
+  if( model->type < 0 || model->type > 7 ) return set_error(SST_ERR_INVALID_ARG, "invalid motion type");
+  (void) border;  // only pixels whose 5x5-eroded mask is set are accumulated: the image border mode never contributes
+  cudaStream_t st = (cudaStream_t) stream;
+  const void * dframes = frames;
+  const float * dparams = params;
+  const int32_t * dstatus = status;
+  const float * dweights = weights;
+  DevBuf tf, tp, ts, tw;
+  if( !on_device ) {
+    SST_CK(tf.ensure(frame_stride * n));
+    SST_CK(cudaMemcpyAsync(tf.p, frames, frame_stride * n, cudaMemcpyHostToDevice, st));
+    dframes = tf.p;
+    SST_CK(tp.ensure((size_t) n * 12 * sizeof(float)));
+    SST_CK(cudaMemcpyAsync(tp.p, params, (size_t) n * 12 * sizeof(float), cudaMemcpyHostToDevice, st));
+    dparams = tp.as<float>();
+    if( status ) {
+      SST_CK(ts.ensure((size_t) n * sizeof(int32_t)));
+      SST_CK(cudaMemcpyAsync(ts.p, status, (size_t) n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+      dstatus = ts.as<int32_t>();
+    }
+    if( weights ) {
+      SST_CK(tw.ensure((size_t) n * sizeof(float)));
+      SST_CK(cudaMemcpyAsync(tw.p, weights, (size_t) n * sizeof(float), cudaMemcpyHostToDevice, st));
+      dweights = tw.as<float>();
+    }
+  }
+  const int r = add_warped_device(a, dframes, depth, n, src_width, src_height, row_stride, frame_stride, scale, *model,
+      dparams, dstatus, dweights, st);
+  if( !on_device ) {
+    cudaStreamSynchronize(st);
+    tf.release(), tp.release(), ts.release(), tw.release();
+  }
+  if( r != SST_OK ) return r;
+  a->frames += n;
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_compute(sst_weighted_average * a, float * avg, uint8_t * mask, int on_device, void * stream)
+{
+  if( !a ) return set_error(SST_ERR_INVALID_ARG, "NULL accumulator");
+  if( a->frames < 1 ) return set_error(SST_ERR_STATE, "no frames accumulated");
+  cudaStream_t st = (cudaStream_t) stream;
+  const size_t N = a->plane();
+  if( on_device ) {
+    SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, avg, mask, nullptr, st));
+    return SST_OK;
+  }
+  DevBuf da, dm;
+  if( avg ) SST_CK(da.ensure(N * sizeof(float)));
+  if( mask ) SST_CK(dm.ensure(N));
+  SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, avg ? da.as<float>() : nullptr,
+      mask ? dm.as<uint8_t>() : nullptr, nullptr, st));
+  if( avg ) SST_CK(cudaMemcpyAsync(avg, da.p, N * sizeof(float), cudaMemcpyDeviceToHost, st));
+  if( mask ) SST_CK(cudaMemcpyAsync(mask, dm.p, N, cudaMemcpyDeviceToHost, st));
+  SST_CK(cudaStreamSynchronize(st));
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_get_acc_counters(sst_weighted_average * a, float * accw, int on_device, void * stream)
+{
+  if( !a || !accw ) return set_error(SST_ERR_INVALID_ARG, "NULL argument");
+  cudaStream_t st = (cudaStream_t) stream;
+  const size_t N = a->plane();
+  if( on_device ) {
+    SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, nullptr, nullptr, accw, st));
+    return SST_OK;
+  }
+  DevBuf d;
+  SST_CK(d.ensure(N * sizeof(float)));
+  SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, nullptr, nullptr, d.as<float>(), st));
+  SST_CK(cudaMemcpyAsync(accw, d.p, N * sizeof(float), cudaMemcpyDeviceToHost, st));
+  SST_CK(cudaStreamSynchronize(st));
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_reinitialize(sst_weighted_average * a, const float * avg, const float * accw,
+    int on_device, void * stream)
+{
+  if( !a || !avg || !accw ) return set_error(SST_ERR_INVALID_ARG, "NULL argument");
+  cudaStream_t st = (cudaStream_t) stream;
+  const size_t N = a->plane();
+  const float * da = avg, * dw = accw;
+  DevBuf ta, tw;
+  if( !on_device ) {
+    SST_CK(ta.ensure(N * sizeof(float)));
+    SST_CK(tw.ensure(N * sizeof(float)));
+    SST_CK(cudaMemcpyAsync(ta.p, avg, N * sizeof(float), cudaMemcpyHostToDevice, st));
+    SST_CK(cudaMemcpyAsync(tw.p, accw, N * sizeof(float), cudaMemcpyHostToDevice, st));
+    da = ta.as<float>(), dw = tw.as<float>();
+  }
+  SST_CK_LAUNCH(launch_stack_reinit(a->acc.as<float>(), N, (int) N, da, dw, st));
+  if( !on_device ) SST_CK(cudaStreamSynchronize(st));
+  a->frames = 1;   // c_weigthed_average::reinitialize sets _accumulated_frames = 1
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_save_state(sst_weighted_average * a, float * state4, int32_t * frames, void * stream)
+{
+  if( !a || !state4 ) return set_error(SST_ERR_INVALID_ARG, "NULL argument");
+  cudaStream_t st = (cudaStream_t) stream;
+  SST_CK(cudaMemcpyAsync(state4, a->acc.p, 4 * a->plane() * sizeof(float), cudaMemcpyDeviceToHost, st));
+  SST_CK(cudaStreamSynchronize(st));
+  if( frames ) *frames = a->frames;
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_load_state(sst_weighted_average * a, const float * state4, int32_t frames, void * stream)
+{
+  if( !a || !state4 ) return set_error(SST_ERR_INVALID_ARG, "NULL argument");
+  cudaStream_t st = (cudaStream_t) stream;
+  SST_CK(cudaMemcpyAsync(a->acc.p, state4, 4 * a->plane() * sizeof(float), cudaMemcpyHostToDevice, st));
+  SST_CK(cudaStreamSynchronize(st));
+  a->frames = frames;
+  return SST_OK;
+}
+
+/* ================================================ streamed pipeline */
+
+extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const void * frames, int depth, int n,
+    int width, int height, size_t row_stride, size_t frame_stride, double scale, int on_device,
+    int num_passes, const sst_motion_model * passes, int border, int weighting,
+    float * params_out, int32_t * status_out, float * rho_out, float * weight_out, void * stream)
+{
+  (void) border;
+  if( !h || !acc || !frames ) return set_error(SST_ERR_INVALID_ARG, "sst_stack_frames: NULL argument");
+  if( h->L == 0 ) return set_error(SST_ERR_STATE, "c_ecch: no reference image was set");
+  if( n < 1 ) return set_error(SST_ERR_INVALID_ARG, "n must be >= 1");
+  if( width != h->w || height != h->h || acc->w != h->w || acc->h != h->h )
+    return set_error(SST_ERR_INVALID_ARG, "frame, reference and accumulator sizes must match");
+  if( depth_bytes(depth) == 0 ) return set_error(SST_ERR_INVALID_ARG, "unsupported depth %d", depth);
+  if( row_stride < (size_t) width * depth_bytes(depth) || frame_stride < row_stride * height )
+    return set_error(SST_ERR_INVALID_ARG, "invalid strides");
+  SST_TRY(validate_passes(h, num_passes, passes));
+  if( h->o.method == M_IC || h->o.method == M_ICLM ) {
+    for( int k = 0; k < num_passes; ++k )
+      if( !model_invertible(passes[k]) )
+        return set_error(SST_ERR_UNSUPPORTED, "inverse compositional ECC requires an invertible motion model");
+  }
+  SST_TRY(ensure_streams(h));
+  SST_TRY(join_user(h, stream));
+  cudaStream_t st = h->st, cp = h->st_copy;
+  const int chunk = std::max(1, std::min(h->chunk, n));
+  const sst_motion_model & last = passes[num_passes - 1];
+  if( !on_device ) {
+    SST_CK(h->stage[0].ensure(frame_stride * chunk));
+    SST_CK(h->stage[1].ensure(frame_stride * chunk));
+    SST_CK(cudaEventRecord(h->ev_free[0], st));
+    SST_CK(cudaEventRecord(h->ev_free[1], st));
+  }
+  SST_CK(h->res_params.ensure((size_t) n * 12 * sizeof(float)));
+  SST_CK(h->res_status.ensure((size_t) n * sizeof(int32_t)));
+  SST_CK(h->res_rho.ensure((size_t) n * sizeof(float)));
+  SST_CK(h->res_weight.ensure((size_t) n * sizeof(float)));
+  int buf = 0;
+  for( int f0 = 0; f0 < n; f0 += chunk, buf ^= 1 ) {
+    const int nc = std::min(chunk, n - f0);
+    const uint8_t * fsrc = (const uint8_t *) frames + (size_t) f0 * frame_stride;
+    const void * d_frames = fsrc;
+    if( !on_device ) {
+      // copy engine: wait until this staging buffer's previous chunk is consumed
+      SST_CK(cudaStreamWaitEvent(cp, h->ev_free[buf], 0));
+      SST_CK(cudaMemcpyAsync(h->stage[buf].p, fsrc, frame_stride * nc, cudaMemcpyHostToDevice, cp));
+      SST_CK(cudaEventRecord(h->ev_copy[buf], cp));
+      SST_CK(cudaStreamWaitEvent(st, h->ev_copy[buf], 0));
+      d_frames = h->stage[buf].p;
+    }
+    SST_TRY(register_device(h, d_frames, depth, nc, row_stride, frame_stride, scale, num_passes, passes, nullptr, false));
+    SST_TRY(add_warped_device(acc, d_frames, depth, nc, width, height, row_stride, frame_stride, scale, last,
+        h->out_params.as<float>(), h->out_status.as<int32_t>(), weighting ? h->out_weight.as<float>() : nullptr, st));
+    if( !on_device ) SST_CK(cudaEventRecord(h->ev_free[buf], st));
+    SST_TRY(copy_out(h->res_params.as<float>() + (size_t) f0 * 12, h->out_params.p, (size_t) nc * 12 * sizeof(float), 1, st));
+    SST_TRY(copy_out(h->res_status.as<int32_t>() + f0, h->out_status.p, (size_t) nc * sizeof(int32_t), 1, st));
+    SST_TRY(copy_out(h->res_rho.as<float>() + f0, h->out_rho.p, (size_t) nc * sizeof(float), 1, st));
+    SST_TRY(copy_out(h->res_weight.as<float>() + f0, h->out_weight.p, (size_t) nc * sizeof(float), 1, st));
+  }
+  SST_TRY(copy_out(params_out, h->res_params.p, (size_t) n * 12 * sizeof(float), on_device, st));
+  SST_TRY(copy_out(status_out, h->res_status.p, (size_t) n * sizeof(int32_t), on_device, st));
+  SST_TRY(copy_out(rho_out, h->res_rho.p, (size_t) n * sizeof(float), on_device, st));
+  SST_TRY(copy_out(weight_out, h->res_weight.p, (size_t) n * sizeof(float), on_device, st));
+  // c_frame_accumulation::_accumulated_frames counts the frames actually added
+  std::vector<int32_t> stv(n);
+  SST_CK(cudaMemcpyAsync(stv.data(), h->res_status.p, (size_t) n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  SST_CK(cudaStreamSynchronize(st));
+  for( int f = 0; f < n; ++f ) acc->frames += stv[f] == SST_FRAME_OK ? 1 : 0;
+  SST_TRY(release_to_user(h, stream));
+  return SST_OK;
+}
+
+/* ================================================ utilities */
+
+extern "C" int sst_remap(const void * src, int depth, int src_width, int src_height, size_t row_stride, double scale,
+    const sst_motion_model * model, const float * params, int border,
+    float * dst, uint8_t * dst_mask, int dst_width, int dst_height, void * stream)
+{
+  if( !src || !model || !params ) return set_error(SST_ERR_INVALID_ARG, "sst_remap: NULL argument");
+  if( depth_bytes(depth) == 0 ) return set_error(SST_ERR_INVALID_ARG, "unsupported depth %d", depth);
+  if( border != SST_BORDER_CONSTANT && border != SST_BORDER_REPLICATE && border != SST_BORDER_REFLECT &&
+      border != SST_BORDER_REFLECT101 )
+    return set_error(SST_ERR_UNSUPPORTED, "unsupported border mode %d", border);
+  cudaStream_t st = (cudaStream_t) stream;
+  double s[16], p[12];
+  model_identity(*model, s);
+  const int M = model_nparams(*model);
+  for( int j = 0; j < M; ++j ) p[j] = params[j];
+  model_set_params(*model, s, p);
+  float c[SST_NCOEF];
+  model_warp_coeffs(*model, s, c);
+  DevBuf dc;
+  SST_CK(dc.ensure(sizeof(c)));
+  SST_CK(cudaMemcpyAsync(dc.p, c, sizeof(c), cudaMemcpyHostToDevice, st));
+  SST_CK_LAUNCH(launch_remap(src, depth, src_width, src_height, row_stride, scale, model->type, dc.as<float>(), border,
+      dst, dst_mask, dst_width, dst_height, st));
+  SST_CK(cudaStreamSynchronize(st));
+  return SST_OK;
+}
+
+extern "C" int sst_extract_bayer_planes_u16(const uint16_t * src, int width, int height, size_t row_stride,
+    uint16_t * dst, void * stream)
+{
+  if( !src || !dst ) return set_error(SST_ERR_INVALID_ARG, "NULL argument");
+  if( (width & 1) || (height & 1) ) return set_error(SST_ERR_INVALID_ARG, "Can not make debayer for uneven image size %dx%d", width, height);
+  if( (row_stride & 3) || ((uintptr_t) src & 3) || ((uintptr_t) dst & 7) )
+    return set_error(SST_ERR_INVALID_ARG, "misaligned bayer buffers");
+  SST_CK_LAUNCH(launch_bayer_planes(0, src, width, height, row_stride, dst, (cudaStream_t) stream));
+  return SST_OK;
+}
+
+extern "C" int sst_average_bayer_planes_u16(const uint16_t * src, int width, int height, size_t row_stride,
+    uint16_t * dst, void * stream)
+{
+  if( !src || !dst ) return set_error(SST_ERR_INVALID_ARG, "NULL argument");
+  if( (width & 1) || (height & 1) ) return set_error(SST_ERR_INVALID_ARG, "Can not average raw bayer planes for uneven image size %dx%d", width, height);
+  if( (row_stride & 3) || ((uintptr_t) src & 3) ) return set_error(SST_ERR_INVALID_ARG, "misaligned bayer buffers");
+  SST_CK_LAUNCH(launch_bayer_planes(1, src, width, height, row_stride, dst, (cudaStream_t) stream));
+  return SST_OK;
+}

@@ -1,0 +1,883 @@
+/*
+ * sst_ecc.cu -- batched ECC Gauss-Newton passes for sm_103a.
+ *
+ * One launch = one Gauss-Newton step of every frame still iterating at the
+ * current level. Per pixel the kernels evaluate W(x;p), sample the frame's
+ * pyramid level bilinearly, form the residual and accumulate the
+ * steepest-descent projections in FP32 registers; CTAs reduce in FP64 and the
+ * last CTA of a frame runs the reference's per-iteration logic in FP64:
+ *
+ *   IC    c_ecc_inverse_compositional::align   ecc2.cc:1693-1788
+ *   IC-LM c_ecclm_inverse_compositional::align ecc2.cc:1926-2086
+ *   FA    c_ecc_forward_additive::align        ecc2.cc:1247-1365
+ *   LM    c_ecclm::align                       ecc2.cc:1528-1650
+ *
+ * followed, when a frame leaves a level, by c_ecch::align's rescale to the
+ * next finer level (ecc2.cc:1159-1171: only after a successful level).
+ *
+ * Fusions relative to the reference: the remap, the mask remap + threshold,
+ * the residual, the steepest-descent images and the Hessian / projection dot
+ * products of one iteration are one pass over the level (the reference makes
+ * M(M+1)/2 + M full-image passes); an LM / IC-LM trial evaluation also
+ * produces the Jacobian products at the trial point, which the reference
+ * recomputes after accepting it (identical values).
+ */
+#include "sst_engine.cuh"
+#include <float.h>
+
+namespace sst {
+
+/* ------------------------------------------------- steepest-descent images */
+
+/* create_steepest_descent_images for one pixel (c_image_transform.cc:262-269,
+ * 587-668, 1045-1070, 1319-1366, 1583-1612, 1834-1868). jc holds the per-frame
+ * constants of model_sd_coeffs(). */
+template<int JK, int M>
+__device__ __forceinline__ void sd_pixel(const float * jc, float x, float y, float gx, float gy, float * J)
+{
+  if( JK == J_TRANS ) {
+    J[0] = gx, J[1] = gy;
+  }
+  else if( JK == J_EUCL ) {
+    const float sc = jc[0], sa = jc[1], ca = jc[2];
+    const float xx = x - jc[3], yy = y - jc[4];
+    J[0] = gx, J[1] = gy;
+    const float u = ca * xx - sa * yy, v = sa * xx + ca * yy;
+    J[2] = sc * (-gx * v + gy * u);
+    if( M > 3 ) J[3 < M ? 3 : 0] = gx * u + gy * v;
+  }
+  else if( JK == J_AFFINE ) {
+    J[0] = gx * x, J[1] = gx * y, J[2] = gx;
+    J[3] = gy * x, J[4] = gy * y, J[5] = gy;
+  }
+  else if( JK == J_HOMOG ) {
+    const float den = 1.0f / fmaf(x, jc[6], fmaf(y, jc[7], 1.0f));
+    const float hatX = -fmaf(x, jc[0], fmaf(y, jc[1], jc[2])) * den;
+    const float hatY = -fmaf(x, jc[3], fmaf(y, jc[4], jc[5])) * den;
+    const float ggx = gx * den, ggy = gy * den;
+    const float gg = hatX * ggx + hatY * ggy;
+    J[0] = ggx * x, J[1] = ggx * y, J[2] = ggx;
+    J[3] = ggy * x, J[4] = ggy * y, J[5] = ggy;
+    J[6 < M ? 6 : 0] = gg * x;
+    J[7 < M ? 7 : 0] = gg * y;
+  }
+  else if( JK == J_SEMIQ ) {
+    const float xy = x * y;
+    J[0] = gx * x, J[1] = gx * y, J[2] = gx, J[3] = gx * xy;
+    J[4] = gy * x, J[5] = gy * y, J[6 < M ? 6 : 0] = gy, J[7 < M ? 7 : 0] = gy * xy;
+  }
+  else {
+    const float xy = x * y, xx = x * x, yy = y * y;
+    J[0] = gx * x, J[1] = gx * y, J[2] = gx, J[3] = gx * xy, J[4] = gx * xx, J[5] = gx * yy;
+    J[6 < M ? 6 : 0] = gy * x, J[7 < M ? 7 : 0] = gy * y, J[8 < M ? 8 : 0] = gy;
+    J[9 < M ? 9 : 0] = gy * xy, J[10 < M ? 10 : 0] = gy * xx, J[11 < M ? 11 : 0] = gy * yy;
+  }
+}
+
+/* ------------------------------------------------------- tile bookkeeping */
+
+/* Deterministic combine of a frame's tile partials: thread group g sums tiles
+ * g, g+G, ... of sum k; the G group results are added in order. */
+template<int NS>
+__device__ void combine_partials(const double * P, int tiles, double * tmp, double * out)
+{
+  constexpr int G = (256 / NS) > 0 ? (256 / NS) : 1;
+  const int tid = threadIdx.x;
+  if( tid < NS * G ) {
+    const int k = tid % NS, g = tid / NS;
+    double s = 0;
+    for( int t = g; t < tiles; t += G ) s += __ldcg(P + (size_t) t * NS + k);
+    tmp[tid] = s;
+  }
+  __syncthreads();
+  if( tid < NS ) {
+    double s = 0;
+    for( int g = 0; g < G; ++g ) s += tmp[g * NS + tid];
+    out[tid] = s;
+  }
+  __syncthreads();
+}
+
+template<int NS>
+__device__ __forceinline__ void block_reduce_d(const float (&acc)[NS], double * scratch, double * out)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for( int k = 0; k < NS; ++k ) {
+    const double s = warp_sum((double) acc[k]);
+    if( lane == 0 ) scratch[wid * NS + k] = s;
+  }
+  __syncthreads();
+  for( int k = threadIdx.x; k < NS; k += 256 ) {
+    double t = 0;
+#pragma unroll
+    for( int wv = 0; wv < 8; ++wv ) t += scratch[wv * NS + k];
+    out[k] = t;
+  }
+  __syncthreads();
+}
+
+/* Write the tile partials and take a ticket; returns (in smem flag) whether
+ * this CTA is the frame's last one, in which case `sums` holds the frame
+ * totals on return. */
+template<int NS>
+__device__ bool finish_tile(const PassArgs & a, int f, int t, double * tile_sums, double * tmp, double * sums, int * s_flag)
+{
+  double * P = a.partials + (size_t) f * a.part_stride;
+  if( threadIdx.x < NS ) P[(size_t) t * NS + threadIdx.x] = tile_sums[threadIdx.x];
+  __threadfence();
+  __syncthreads();
+  if( threadIdx.x == 0 ) {
+    const unsigned prev = atomicAdd(a.counters + f, 1u);
+    *s_flag = (prev == (unsigned) (a.tiles - 1));
+  }
+  __syncthreads();
+  const bool last = *s_flag != 0;
+  if( last ) {
+    __threadfence();
+    combine_partials<NS>(P, a.tiles, tmp, sums);
+  }
+  return last;
+}
+
+/* ------------------------------------------------------ per-frame control */
+
+__device__ void set_eval(FrameState * F, const sst_motion_model & m, const double * s)
+{
+  for( int i = 0; i < 16; ++i ) F->eval[i] = s[i];
+  model_warp_coeffs(m, s, F->wc);
+  model_sd_coeffs(m, s, F->jc);
+}
+
+__device__ bool state_finite(const double * s, int n)
+{
+  for( int i = 0; i < n; ++i ) if( !isfinite(s[i]) ) return false;
+  return true;
+}
+
+/* c_ecch::align per-level epilogue (ecc2.cc:1159-1173) */
+__device__ void level_finish(FrameState * F, const PassArgs & a, bool ok)
+{
+  F->level_ok = ok;
+  F->total_iters += F->n;
+  if( !state_finite(F->state, 16) ) {
+    F->status = SST_FRAME_NAN;
+    ok = false;
+  }
+  if( ok && a.scale_next > 0 ) model_scale(a.model, F->state, a.scale_next);
+  set_eval(F, a.model, F->state);
+}
+
+__device__ void append(const PassArgs & a, int f)
+{
+  const int k = atomicAdd(a.count_out, 1);
+  a.list_out[k] = f;
+}
+
+/* IC: ecc2.cc:1740-1785 */
+__device__ void solve_ic(FrameState * F, const double * S, const PassArgs & a, int f)
+{
+  const int M = a.M;
+  F->n += 1;
+  const double cnt = S[M + 1];
+  if( !(cnt > 0) ) {
+    F->status = SST_FRAME_EMPTY_MASK;
+    level_finish(F, a, false);
+    return;
+  }
+  const double q = a.RMA / cnt;
+  const double rmsnew = S[M] * q * q;
+  double b[12], x[12];
+  for( int j = 0; j < M; ++j ) b[j] = S[j] * q;
+  if( !cholesky_solve(a.H, b, M, x) ) for( int j = 0; j < M; ++j ) x[j] = 0;
+  if( rmsnew >= F->rmsold ) {
+    level_finish(F, a, true);
+    return;
+  }
+  double sdp[12], ns[16];
+  for( int j = 0; j < M; ++j ) sdp[j] = a.step * x[j];
+  model_invert_and_compose(a.model, F->state, sdp, ns);
+  for( int i = 0; i < 16; ++i ) F->state[i] = ns[i];
+  F->rmsold = rmsnew;
+  F->eps = model_eps(a.model, F->state, x, a.w, a.h);
+  if( F->eps < a.max_eps ) {
+    level_finish(F, a, true);
+    return;
+  }
+  if( F->n >= a.max_it ) {
+    F->n += 1;   // the failing `_num_iterations++ < _max_iterations` test
+    level_finish(F, a, true);
+    return;
+  }
+  set_eval(F, a.model, F->state);
+  append(a, f);
+}
+
+/* IC-LM: ecc2.cc:1983-2083 as a state machine over pass results */
+__device__ void solve_iclm(FrameState * F, const double * S, const PassArgs & a, int f)
+{
+  const int M = a.M;
+  const double cnt = S[M + 1];
+  if( !(cnt > 0) ) {
+    F->status = SST_FRAME_EMPTY_MASK;
+    level_finish(F, a, false);
+    return;
+  }
+  const double q = a.RMA / cnt;
+  const double rms = S[M] * q * q;
+  double vv[12];
+  for( int j = 0; j < M; ++j ) vv[j] = S[j] * q;
+
+  bool go_after = false;
+  double newerr = 0;
+  if( F->phase == PH_START ) {
+    F->err = rms;
+    for( int j = 0; j < M; ++j ) F->v[j] = vv[j];
+  }
+  else {
+    newerr = rms;
+    F->dpe = model_eps(a.model, F->state, F->dpv, a.w, a.h);
+    if( F->dpe < a.max_eps ) go_after = true;
+    else {
+      double dS = 0;
+      for( int i = 0; i < M; ++i ) {
+        double t = 2 * F->v[i];
+        for( int j = 0; j < M; ++j ) t -= a.H[i * M + j] * F->dpv[j];
+        dS += F->dpv[i] * t;
+      }
+      const double rho = (F->err - newerr) / (fabs(dS) > DBL_EPSILON ? dS : 1.0);
+      if( rho > 0.25 ) {
+        if( F->lambda > 1e-6 ) F->lambda = fmax(1e-6, F->lambda / 5);
+      }
+      else if( rho > 0.1 ) {
+      }
+      else if( F->lambda < 1 ) F->lambda = 1;
+      else F->lambda *= 10;
+      if( newerr < F->err ) go_after = true;
+      else if( !(F->n < a.max_it) ) go_after = true;
+    }
+    if( go_after ) {
+      if( newerr < F->err ) {
+        F->err = newerr;
+        for( int i = 0; i < 16; ++i ) F->state[i] = F->eval[i];
+        for( int j = 0; j < M; ++j ) F->v[j] = vv[j];
+      }
+      if( F->dpe < a.max_eps || !(F->n < a.max_it) ) {
+        F->eps = F->dpe;
+        level_finish(F, a, true);
+        return;
+      }
+    }
+  }
+  // do { ... } body: damped solve and the next trial point
+  F->n += 1;
+  double H[144], x[12];
+  for( int i = 0; i < M * M; ++i ) H[i] = a.H[i];
+  for( int i = 0; i < M; ++i ) H[i * M + i] = (1 + F->lambda) * a.H[i * M + i];
+  if( !cholesky_solve(H, F->v, M, x) ) for( int j = 0; j < M; ++j ) x[j] = 0;
+  for( int j = 0; j < M; ++j ) F->dpv[j] = x[j];
+  double sdp[12], ns[16];
+  for( int j = 0; j < M; ++j ) sdp[j] = a.step * x[j];
+  model_invert_and_compose(a.model, F->state, sdp, ns);
+  F->phase = PH_TRIAL;
+  set_eval(F, a.model, ns);
+  append(a, f);
+}
+
+/* FA: ecc2.cc:1295-1360. Sum layout: H (packed lower), SJg, SJf, SJ, Sf, Sf2, Sg, Sg2, n */
+__device__ void solve_fa(FrameState * F, const double * S, const PassArgs & a, int f)
+{
+  const int M = a.M, nH = M * (M + 1) / 2;
+  F->n += 1;
+  const double * SJg = S + nH, * SJf = S + nH + M, * SJ = S + nH + 2 * M;
+  const double Sf = S[nH + 3 * M], Sf2 = S[nH + 3 * M + 1], Sg = S[nH + 3 * M + 2], Sg2 = S[nH + 3 * M + 3];
+  const double cnt = S[nH + 3 * M + 4];
+  if( !(cnt > 0) ) {
+    F->status = SST_FRAME_EMPTY_MASK;
+    level_finish(F, a, false);
+    return;
+  }
+  const double fm = Sf / cnt, gm = Sg / cnt;
+  const double fs = sqrt(fmax(Sf2 / cnt - fm * fm, 0.0)), gs = sqrt(fmax(Sg2 / cnt - gm * gm, 0.0));
+  const double r = gs / fs;
+  double H[144], ep[12], x[12];
+  for( int i = 0, k = 0; i < M; ++i ) {
+    for( int j = 0; j <= i; ++j, ++k ) H[i * M + j] = H[j * M + i] = S[k];
+  }
+  for( int j = 0; j < M; ++j ) ep[j] = SJg[j] - r * SJf[j] - (gm - r * fm) * SJ[j];
+  if( !cholesky_solve(H, ep, M, x) ) {
+    level_finish(F, a, false);   // _failed = true: align() returns false, no rescale
+    return;
+  }
+  double p[12], dp[12];
+  model_get_params(a.model, F->state, p);
+  for( int j = 0; j < M; ++j ) {
+    dp[j] = -a.step * x[j];
+    p[j] += dp[j];
+  }
+  model_set_params(a.model, F->state, p);
+  F->eps = model_eps(a.model, F->state, dp, a.w, a.h);
+  const double max_eps = a.max_eps > 0 ? a.max_eps : 1e-3;
+  if( F->eps < max_eps ) {
+    level_finish(F, a, true);
+    return;
+  }
+  if( F->n >= a.max_it ) {
+    F->n += 1;
+    level_finish(F, a, true);
+    return;
+  }
+  set_eval(F, a.model, F->state);
+  append(a, f);
+}
+
+/* LM: ecc2.cc:1564-1646. Sum layout: H (packed lower), v, ssq, n */
+__device__ void solve_lm(FrameState * F, const double * S, const PassArgs & a, int f)
+{
+  const int M = a.M, nH = M * (M + 1) / 2;
+  const double ssq = S[nH + M];
+  enum { OUTER, INNER } next;
+  if( F->phase == PH_START ) {
+    F->err = ssq;
+    for( int i = 0, k = 0; i < M; ++i ) for( int j = 0; j <= i; ++j, ++k ) F->Hs[i * M + j] = F->Hs[j * M + i] = S[k];
+    for( int j = 0; j < M; ++j ) F->v[j] = S[nH + j];
+    next = OUTER;
+  }
+  else {
+    const double newerr = ssq;
+    if( newerr > F->err ) {
+      if( F->lambda > 1e6 ) next = OUTER;     // no convergence at this lambda: back to the outer loop
+      else {
+        F->lambda *= 10.0;
+        next = INNER;
+      }
+    }
+    else {
+      // accept: the trial point becomes the state; its Jacobian products are the new H, v
+      for( int i = 0; i < 16; ++i ) F->state[i] = F->eval[i];
+      const double diff = F->err - newerr;
+      double dS = 0;
+      for( int i = 0; i < M; ++i ) {
+        double t = 2 * F->v[i];
+        for( int j = 0; j < M; ++j ) t -= F->Hs[i * M + j] * F->dpv[j];
+        dS += F->dpv[i] * t;
+      }
+      const double err_old = F->err;
+      F->err = newerr;
+      for( int i = 0, k = 0; i < M; ++i ) for( int j = 0; j <= i; ++j, ++k ) F->Hs[i * M + j] = F->Hs[j * M + i] = S[k];
+      for( int j = 0; j < M; ++j ) F->v[j] = S[nH + j];
+      if( diff < err_old * 1e-4 ) {
+        F->converged = 1;
+        level_finish(F, a, true);
+        return;
+      }
+      const double rho = fabs(dS) > 1e-9 ? diff / fabs(dS) : diff;
+      if( rho > 0.25 ) F->lambda = fmax(1e-8, 0.2 * F->lambda);
+      else if( rho < 0.1 ) F->lambda = F->lambda < 1.0 ? 1.0 : F->lambda * 10.0;
+      next = OUTER;
+    }
+  }
+  if( next == OUTER ) {
+    if( !(F->n < a.max_it) ) {
+      level_finish(F, a, F->converged != 0);
+      return;
+    }
+    if( F->err < 1 ) {
+      F->converged = 1;
+      level_finish(F, a, true);
+      return;
+    }
+  }
+  // inner loop head: while (iteration++ < max_iterations)
+  if( !(F->n < a.max_it) ) {
+    F->n += 1;
+    level_finish(F, a, F->converged != 0);
+    return;
+  }
+  F->n += 1;
+  double H[144], x[12], p[12];
+  for( int i = 0; i < M * M; ++i ) H[i] = F->Hs[i];
+  for( int i = 0; i < M; ++i ) H[i * M + i] = (1 + F->lambda) * F->Hs[i * M + i];
+  if( !cholesky_solve(H, F->v, M, x) ) for( int j = 0; j < M; ++j ) x[j] = 0;
+  for( int j = 0; j < M; ++j ) F->dpv[j] = x[j];
+  model_get_params(a.model, F->state, p);
+  for( int j = 0; j < M; ++j ) p[j] -= a.step * x[j];
+  F->eps = model_eps(a.model, F->state, x, a.w, a.h);
+  double ns[16];
+  for( int i = 0; i < 16; ++i ) ns[i] = F->state[i];
+  model_set_params(a.model, ns, p);
+  if( F->eps <= a.max_eps ) {
+    for( int i = 0; i < 16; ++i ) F->state[i] = ns[i];
+    F->converged = 1;
+    level_finish(F, a, true);
+    return;
+  }
+  F->phase = PH_TRIAL;
+  set_eval(F, a.model, ns);
+  append(a, f);
+}
+
+/* ------------------------------------------------------ pointwise passes */
+
+/* IC / IC-LM pass: sums {J^T r (M), |r|^2, count}, J from the reference gradients */
+template<int METHOD, int FAM, int JK, int M>
+__global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
+{
+  constexpr int NS = M + 2;
+  constexpr int GMAX = (256 / NS) > 0 ? (256 / NS) : 1;
+  __shared__ double s_red[8 * NS];
+  __shared__ double s_tile[NS];
+  __shared__ double s_tmp[NS * GMAX];
+  __shared__ double s_sum[NS];
+  __shared__ float s_c[16];
+  __shared__ int s_flag;
+
+  const int nitems = __ldcg(a.count_in) * a.tiles;
+  for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
+    const int fi = item / a.tiles;
+    const int t = item - fi * a.tiles;
+    const int f = __ldcg(a.list_in + fi);
+    FrameState * F = a.fs + f;
+    if( threadIdx.x < 16 ) s_c[threadIdx.x] = F->wc[threadIdx.x];
+    __syncthreads();
+    float c[16];
+#pragma unroll
+    for( int i = 0; i < 16; ++i ) c[i] = s_c[i];
+    const float * img = a.pyr + (size_t) f * a.pyr_stride + a.lvl_off;
+    const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
+    const int x = tx0 + (threadIdx.x & (PW_TX - 1));
+    float acc[NS];
+#pragma unroll
+    for( int k = 0; k < NS; ++k ) acc[k] = 0.f;
+    if( x < a.w ) {
+#pragma unroll 2
+      for( int k = 0; k < PW_TY / 2; ++k ) {
+        const int y = ty0 + (threadIdx.x >> 7) + 2 * k;
+        if( y < a.h ) {
+          const float fx = (float) x, fy = (float) y;
+          const spos s = warp_pos<FAM>(c, x, y);
+          const size_t i = (size_t) y * a.w + x;
+          bool ok;
+          if( METHOD == M_IC ) {
+            ok = mask_ok(coverage(a.w, a.h, s), 250);
+          }
+          else {
+            int rx, ry;
+            warp_nearest<FAM>(c, x, y, rx, ry);
+            ok = rx >= 0 && rx < a.w && ry >= 0 && ry < a.h;
+            if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
+          }
+          const float T = __ldg(a.refT + i);
+          const float2 g = __ldg(a.refG + i);
+          const float v = sample_replicate(img, a.w, a.h, s);
+          const float r = ok ? v - T : 0.f;
+          acc[M] = fmaf(r, r, acc[M]);
+          acc[M + 1] += ok ? 1.f : 0.f;
+          float J[M];
+          sd_pixel<JK, M>(a.jc_id, fx, fy, g.x, g.y, J);
+#pragma unroll
+          for( int j = 0; j < M; ++j ) acc[j] = fmaf(J[j], r, acc[j]);
+        }
+      }
+    }
+    block_reduce_d<NS>(acc, s_red, s_tile);
+    if( finish_tile<NS>(a, f, t, s_tile, s_tmp, s_sum, &s_flag) ) {
+      if( threadIdx.x == 0 ) {
+        a.counters[f] = 0;
+        if( METHOD == M_IC ) solve_ic(F, s_sum, a, f);
+        else solve_iclm(F, s_sum, a, f);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+/* -------------------------------------------------------- stencil passes */
+
+/* FA / LM pass: the warped tile (+2 px halo, REPLICATE at the level border)
+ * is staged in shared memory and differentiated there (ecc_differentiate),
+ * so the warped image and its gradients never touch HBM. */
+template<int METHOD, int FAM, int JK, int M>
+__global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
+{
+  constexpr int nH = M * (M + 1) / 2;
+  constexpr int NS = (METHOD == M_FA) ? nH + 3 * M + 5 : nH + M + 2;
+  constexpr int GMAX = (256 / NS) > 0 ? (256 / NS) : 1;
+  constexpr int SW = ST_TX + 4, SH = ST_TY + 4;
+  __shared__ double s_red[8 * NS];
+  __shared__ double s_tile[NS];
+  __shared__ double s_tmp[NS * GMAX > 256 ? NS * GMAX : 256];
+  __shared__ double s_sum[NS];
+  __shared__ float s_img[SH * SW];
+  __shared__ float s_c[16];
+  __shared__ float s_j[8];
+  __shared__ int s_flag;
+
+  const int nitems = __ldcg(a.count_in) * a.tiles;
+  for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
+    const int fi = item / a.tiles;
+    const int t = item - fi * a.tiles;
+    const int f = __ldcg(a.list_in + fi);
+    FrameState * F = a.fs + f;
+    if( threadIdx.x < 16 ) s_c[threadIdx.x] = F->wc[threadIdx.x];
+    if( threadIdx.x < 8 ) s_j[threadIdx.x] = F->jc[threadIdx.x];
+    __syncthreads();
+    float c[16], jc[8];
+#pragma unroll
+    for( int i = 0; i < 16; ++i ) c[i] = s_c[i];
+#pragma unroll
+    for( int i = 0; i < 8; ++i ) jc[i] = s_j[i];
+    const float * img = a.pyr + (size_t) f * a.pyr_stride + a.lvl_off;
+    const int tx0 = (t % a.tiles_x) * ST_TX, ty0 = (t / a.tiles_x) * ST_TY;
+
+    // stage the warped image gw over the tile + halo (positions clamped: BORDER_REPLICATE)
+    for( int q = threadIdx.x; q < SW * SH; q += 256 ) {
+      const int xx = clampi(tx0 - 2 + q % SW, 0, a.w - 1);
+      const int yy = clampi(ty0 - 2 + q / SW, 0, a.h - 1);
+      s_img[q] = sample_replicate(img, a.w, a.h, warp_pos<FAM>(c, xx, yy));
+    }
+    __syncthreads();
+
+    float acc[NS];
+#pragma unroll
+    for( int k = 0; k < NS; ++k ) acc[k] = 0.f;
+    const int lx = threadIdx.x & (ST_TX - 1);
+    const int x = tx0 + lx;
+#pragma unroll 1
+    for( int k = 0; k < ST_TY / 4; ++k ) {
+      const int ly = (threadIdx.x >> 6) + 4 * k;
+      const int y = ty0 + ly;
+      if( x < a.w && y < a.h ) {
+        const float fx = (float) x, fy = (float) y;
+        const spos s = warp_pos<FAM>(c, x, y);
+        const size_t i = (size_t) y * a.w + x;
+        const float cov = coverage(a.w, a.h, s);
+        bool ok;
+        if( METHOD == M_FA ) {
+          ok = mask_ok(cov, 255);
+          if( a.refMe ) ok = ok && __ldg(a.refMe + i) != 0;
+        }
+        else {
+          ok = mask_ok(cov, 250);
+          if( a.refMe ) ok = ok && __ldg(a.refMe + i) != 0;
+        }
+        // gx = d5 (x) (*) s3 (y), gy = s3 (x) (*) d5 (y)
+        const float * p = s_img + (ly + 2) * SW + (lx + 2);
+        const float d5a = 1.f / 12.f, d5b = -2.f / 3.f;
+        float gxw = 0.f, gyw = 0.f;
+        {
+          const float r0 = d5a * p[-SW - 2] + d5b * p[-SW - 1] - d5b * p[-SW + 1] - d5a * p[-SW + 2];
+          const float r1 = d5a * p[-2] + d5b * p[-1] - d5b * p[1] - d5a * p[2];
+          const float r2 = d5a * p[SW - 2] + d5b * p[SW - 1] - d5b * p[SW + 1] - d5a * p[SW + 2];
+          gxw = 0.25f * r0 + 0.5f * r1 + 0.25f * r2;
+          const float c0 = d5a * p[-2 * SW - 1] + d5b * p[-SW - 1] - d5b * p[SW - 1] - d5a * p[2 * SW - 1];
+          const float c1 = d5a * p[-2 * SW] + d5b * p[-SW] - d5b * p[SW] - d5a * p[2 * SW];
+          const float c2 = d5a * p[-2 * SW + 1] + d5b * p[-SW + 1] - d5b * p[SW + 1] - d5a * p[2 * SW + 1];
+          gyw = 0.25f * c0 + 0.5f * c1 + 0.25f * c2;
+        }
+        if( !ok ) gxw = gyw = 0.f;
+        const float gw = p[0];
+        const float T = __ldg(a.refT + i);
+        float J[M];
+        sd_pixel<JK, M>(jc, fx, fy, gxw, gyw, J);
+#pragma unroll
+        for( int u = 0, kk = 0; u < M; ++u ) {
+#pragma unroll
+          for( int v = 0; v <= u; ++v, ++kk ) acc[kk] = fmaf(J[u], J[v], acc[kk]);
+        }
+        if( METHOD == M_FA ) {
+          const float fv = T - a.tshift, gv = gw - a.tshift;
+#pragma unroll
+          for( int u = 0; u < M; ++u ) {
+            acc[nH + u] = fmaf(J[u], gv, acc[nH + u]);
+            acc[nH + M + u] = fmaf(J[u], fv, acc[nH + M + u]);
+            acc[nH + 2 * M + u] += J[u];
+          }
+          if( ok ) {
+            acc[nH + 3 * M] += fv;
+            acc[nH + 3 * M + 1] = fmaf(fv, fv, acc[nH + 3 * M + 1]);
+            acc[nH + 3 * M + 2] += gv;
+            acc[nH + 3 * M + 3] = fmaf(gv, gv, acc[nH + 3 * M + 3]);
+            acc[nH + 3 * M + 4] += 1.f;
+          }
+        }
+        else {
+          const float r = ok ? gw - T : 0.f;
+#pragma unroll
+          for( int u = 0; u < M; ++u ) acc[nH + u] = fmaf(J[u], r, acc[nH + u]);
+          acc[nH + M] = fmaf(r, r, acc[nH + M]);
+          acc[nH + M + 1] += ok ? 1.f : 0.f;
+        }
+      }
+    }
+    block_reduce_d<NS>(acc, s_red, s_tile);
+    if( finish_tile<NS>(a, f, t, s_tile, s_tmp, s_sum, &s_flag) ) {
+      if( threadIdx.x == 0 ) {
+        a.counters[f] = 0;
+        if( METHOD == M_FA ) solve_fa(F, s_sum, a, f);
+        else solve_lm(F, s_sum, a, f);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+/* ------------------------------------------------------------- dispatch */
+
+int pass_num_sums(int method, int M)
+{
+  const int nH = M * (M + 1) / 2;
+  switch ( method ) {
+  case M_FA: return nH + 3 * M + 5;
+  case M_LM: return nH + M + 2;
+  default: return M + 2;
+  }
+}
+
+template<int METHOD, int FAM, int JK, int M>
+static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st)
+{
+  if( METHOD == M_IC || METHOD == M_ICLM ) k_pass_pointwise<METHOD, FAM, JK, M><<<grid, 256, 0, st>>>(a);
+  else k_pass_stencil<METHOD, FAM, JK, M><<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+template<int METHOD>
+static cudaError_t launch_m(const PassArgs & a, int grid, cudaStream_t st)
+{
+  switch ( a.model.type ) {
+  case SST_MOTION_TRANSLATION: return launch_t<METHOD, FAM_AFFINE, J_TRANS, 2>(a, grid, st);
+  case SST_MOTION_EUCLIDEAN:
+  case SST_MOTION_SCALED_EUCLIDEAN:
+    if( a.M == 3 ) return launch_t<METHOD, FAM_AFFINE, J_EUCL, 3>(a, grid, st);
+    return launch_t<METHOD, FAM_AFFINE, J_EUCL, 4>(a, grid, st);
+  case SST_MOTION_AFFINE: return launch_t<METHOD, FAM_AFFINE, J_AFFINE, 6>(a, grid, st);
+  case SST_MOTION_HOMOGRAPHY:
+  case SST_MOTION_EPIPOLAR_DEROTATION: return launch_t<METHOD, FAM_HOMOG, J_HOMOG, 8>(a, grid, st);
+  case SST_MOTION_SEMI_QUADRATIC:
+    if( METHOD == M_FA || METHOD == M_LM ) return launch_t<(METHOD == M_FA ? M_FA : M_LM), FAM_QUAD, J_SEMIQ, 8>(a, grid, st);
+    return cudaErrorInvalidValue;
+  case SST_MOTION_QUADRATIC:
+    if( METHOD == M_FA || METHOD == M_LM ) return launch_t<(METHOD == M_FA ? M_FA : M_LM), FAM_QUAD, J_QUAD, 12>(a, grid, st);
+    return cudaErrorInvalidValue;
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pass(int method, const PassArgs & a, int grid, cudaStream_t st)
+{
+  switch ( method ) {
+  case M_IC: return launch_m<M_IC>(a, grid, st);
+  case M_ICLM: return launch_m<M_ICLM>(a, grid, st);
+  case M_FA: return launch_m<M_FA>(a, grid, st);
+  case M_LM: return launch_m<M_LM>(a, grid, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+/* ------------------------------------------------------ level / pass glue */
+
+/* c_ecch per-level align() prologue: reset the per-level solver state and
+ * list every frame still registering (block-wide ordered compaction). */
+__global__ void k_level_begin(LevelBeginArgs a)
+{
+  __shared__ int s_base;
+  __shared__ int s_warp[32];
+  if( threadIdx.x == 0 ) s_base = 0;
+  __syncthreads();
+  for( int f0 = 0; f0 < a.n; f0 += blockDim.x ) {
+    const int f = f0 + threadIdx.x;
+    bool alive = false;
+    if( f < a.n ) {
+      FrameState * F = a.fs + f;
+      alive = F->status == SST_FRAME_OK;
+      F->n = 0;
+      F->phase = PH_START;
+      F->converged = 0;
+      F->level_ok = 0;
+      F->err = 0;
+      F->rmsold = FLT_MAX;
+      F->eps = FLT_MAX;
+      F->dpe = 0;
+      F->lambda = a.method == M_LM ? 0.1 : 0.001;
+      set_eval(F, a.model, F->state);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, alive);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if( lane == 0 ) s_warp[wid] = __popc(b);
+    __syncthreads();
+    if( threadIdx.x == 0 ) {
+      int run = s_base;
+      for( int w = 0; w < (int) (blockDim.x >> 5); ++w ) {
+        const int c = s_warp[w];
+        s_warp[w] = run;
+        run += c;
+      }
+      s_base = run;
+    }
+    __syncthreads();
+    if( alive ) a.list_out[s_warp[wid] + __popc(b & ((1u << lane) - 1u))] = f;
+    __syncthreads();
+  }
+  if( threadIdx.x == 0 ) *a.count_out = s_base;
+}
+
+cudaError_t launch_level_begin(const LevelBeginArgs & a, cudaStream_t st)
+{
+  k_level_begin<<<1, 1024, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+/* c_ecch::align prologue (ecc2.cc:1133-1151): start state of the pass, then
+ * scale_transfrom to the coarsest level. */
+__global__ void k_pass_begin(PassBeginArgs a)
+{
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if( f >= a.n ) return;
+  FrameState * F = a.fs + f;
+  if( a.pass == 0 ) {
+    F->status = SST_FRAME_OK;
+    F->total_iters = 0;
+    F->rho = 0;
+    F->weight = 0;
+    F->eps = FLT_MAX;
+    if( a.init_states ) for( int i = 0; i < 16; ++i ) F->state[i] = a.init_states[(size_t) f * 16 + i];
+    else model_identity(a.model, F->state);
+  }
+  else {
+    double s[16];
+    model_convert(a.prev_model, F->state, a.model, s);
+    for( int i = 0; i < 16; ++i ) F->state[i] = s[i];
+  }
+  if( a.scale_to_coarsest > 0 ) model_scale(a.model, F->state, a.scale_to_coarsest);
+  set_eval(F, a.model, F->state);
+}
+
+cudaError_t launch_pass_begin(const PassBeginArgs & a, cudaStream_t st)
+{
+  k_pass_begin<<<(a.n + 127) / 128, 128, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+/* --------------------------------------------------------- correlation */
+
+/* compute_correlation(current, mask, reference, mask, rmap) (ecc2.cc:100-137)
+ * on level 0 at the final state: LINEAR / BORDER_CONSTANT remap, mask >= 254.
+ * Sums of the values shifted by the reference mean. */
+template<int FAM>
+__global__ void __launch_bounds__(256) k_correlation(CorrArgs a)
+{
+  constexpr int NS = 6;
+  __shared__ double s_red[8 * NS];
+  __shared__ double s_tile[NS];
+  __shared__ double s_tmp[256];
+  __shared__ double s_sum[NS];
+  __shared__ float s_c[16];
+  __shared__ int s_flag;
+  const int nitems = a.n * a.tiles;
+  for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
+    const int f = item / a.tiles;
+    const int t = item - f * a.tiles;
+    FrameState * F = a.fs + f;
+    if( F->status != SST_FRAME_OK ) continue;   // uniform per CTA: no barrier skipped unevenly
+    if( threadIdx.x < 16 ) s_c[threadIdx.x] = F->wc[threadIdx.x];
+    __syncthreads();
+    float c[16];
+#pragma unroll
+    for( int i = 0; i < 16; ++i ) c[i] = s_c[i];
+    const float * img = a.pyr + (size_t) f * a.pyr_stride;
+    const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
+    const int x = tx0 + (threadIdx.x & (PW_TX - 1));
+    float acc[NS] = { 0, 0, 0, 0, 0, 0 };
+    if( x < a.w ) {
+      for( int k = 0; k < PW_TY / 2; ++k ) {
+        const int y = ty0 + (threadIdx.x >> 7) + 2 * k;
+        if( y < a.h ) {
+          const spos s = warp_pos<FAM>(c, x, y);
+          const size_t i = (size_t) y * a.w + x;
+          bool ok = mask_ok(coverage(a.w, a.h, s), 254);
+          if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
+          if( ok ) {
+            const float av = __ldg(a.refT + i) - a.tshift;
+            const float bv = sample_constant0(img, a.w, a.h, s) - a.tshift;
+            acc[0] += av, acc[1] += bv;
+            acc[2] = fmaf(av, av, acc[2]);
+            acc[3] = fmaf(bv, bv, acc[3]);
+            acc[4] = fmaf(av, bv, acc[4]);
+            acc[5] += 1.f;
+          }
+        }
+      }
+    }
+    block_reduce_d<NS>(acc, s_red, s_tile);
+    double * P = a.partials + (size_t) f * a.part_stride;
+    if( threadIdx.x < NS ) P[(size_t) t * NS + threadIdx.x] = s_tile[threadIdx.x];
+    __threadfence();
+    __syncthreads();
+    if( threadIdx.x == 0 ) s_flag = (atomicAdd(a.counters + f, 1u) == (unsigned) (a.tiles - 1));
+    __syncthreads();
+    if( s_flag ) {
+      __threadfence();
+      combine_partials<NS>(P, a.tiles, s_tmp, s_sum);
+      if( threadIdx.x == 0 ) {
+        a.counters[f] = 0;
+        const double n = s_sum[5];
+        double rho = 0;
+        if( n > 0 ) {
+          const double ma = s_sum[0] / n, mb = s_sum[1] / n;
+          const double va = s_sum[2] / n - ma * ma, vb = s_sum[3] / n - mb * mb;
+          const double cv = s_sum[4] / n - ma * mb;
+          rho = cv / (sqrt(fmax(va, 0.0)) * sqrt(fmax(vb, 0.0)));
+        }
+        F->rho = (float) rho;
+        if( a.min_rho > 0 && !(rho >= a.min_rho) ) F->status = SST_FRAME_LOW_RHO;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st)
+{
+  switch ( motion_family(a.model.type) ) {
+  case FAM_AFFINE: k_correlation<FAM_AFFINE><<<grid, 256, 0, st>>>(a); break;
+  case FAM_HOMOG: k_correlation<FAM_HOMOG><<<grid, 256, 0, st>>>(a); break;
+  default: k_correlation<FAM_QUAD><<<grid, 256, 0, st>>>(a); break;
+  }
+  return cudaGetLastError();
+}
+
+/* ----------------------------------------------------------- finalize */
+
+__global__ void k_finalize(FinalizeArgs a)
+{
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if( f >= a.n ) return;
+  FrameState * F = a.fs + f;
+  double p[12] = { 0 };
+  model_get_params(a.model, F->state, p);
+  const int M = model_nparams(a.model);
+  for( int j = 0; j < 12; ++j ) a.params_out[(size_t) f * 12 + j] = j < M ? (float) p[j] : 0.f;
+  if( F->status == SST_FRAME_OK && !state_finite(F->state, 16) ) F->status = SST_FRAME_NAN;
+  double w = 0;
+  if( a.lap_partials ) {
+    double s = 0, n = 0;
+    const double * P = a.lap_partials + (size_t) f * a.lap_tiles * 2;
+    for( int t = 0; t < a.lap_tiles; ++t ) s += P[2 * t], n += P[2 * t + 1];
+    w = n > 0 ? s / n : 0;
+  }
+  F->weight = (float) w;
+  if( a.status_out ) a.status_out[f] = F->status;
+  if( a.iters_out ) a.iters_out[f] = F->total_iters;
+  if( a.eps_out ) a.eps_out[f] = (float) F->eps;
+  if( a.rho_out ) a.rho_out[f] = F->rho;
+  if( a.weight_out ) a.weight_out[f] = F->weight;
+}
+
+cudaError_t launch_finalize(const FinalizeArgs & a, cudaStream_t st)
+{
+  k_finalize<<<(a.n + 127) / 128, 128, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace sst

@@ -1,0 +1,378 @@
+/*
+ * sst_pyramid.cu -- c_ecch image pyramid and reference precompute kernels.
+ *
+ *   convert + Gaussian pre-smooth : ecc_convert_input_image (ecc2.cc:345-382) and
+ *                                   sepFilter2D(G, G, BORDER_REPLICATE) (ecc2.cc:998-1006, 1079-1087)
+ *   pyrDown                       : c_ecch::downscale_image (ecc2.cc:972-982), 5-tap
+ *                                   [1 4 6 4 1]/16, BORDER_REFLECT_101
+ *   reference gradients           : ecc_differentiate (ecc2.cc:142-169)
+ *   IC Gauss-Newton matrix        : ecc_compute_hessian_matrix (ecc2.cc:295-321) of the
+ *                                   steepest-descent images (c_image_transform.cc)
+ *
+ * All kernels are batched over frames (grid.z) and stage halo'd tiles in
+ * shared memory; each input pixel is read from HBM once per kernel.
+ */
+#include "sst_engine.cuh"
+
+namespace sst {
+
+/* ------------------------------------------------ convert + pre-smooth */
+
+constexpr int CS_TX = 64, CS_TY = 16, CS_RMAX = 15;
+
+template<typename T>
+__device__ __forceinline__ float load_px(const uint8_t * base, size_t row_stride, int x, int y)
+{
+  return (float) (*(const T *) (base + (size_t) y * row_stride + (size_t) x * sizeof(T)));
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256) k_convert_smooth(const uint8_t * src, int w, int h, size_t row_stride,
+    size_t frame_stride, float scale, const float * __restrict__ gk, int R, float * dst, size_t dst_stride)
+{
+  __shared__ float s_in[(CS_TY + 2 * CS_RMAX) * (CS_TX + 2 * CS_RMAX)];
+  __shared__ float s_h[(CS_TY + 2 * CS_RMAX) * CS_TX];
+  __shared__ float c_gauss[2 * CS_RMAX + 1];
+  if( threadIdx.x <= 2 * R && R > 0 ) c_gauss[threadIdx.x] = gk[threadIdx.x];
+  const uint8_t * fb = src + (size_t) blockIdx.z * frame_stride;
+  float * out = dst + (size_t) blockIdx.z * dst_stride;
+  const int tx0 = blockIdx.x * CS_TX, ty0 = blockIdx.y * CS_TY;
+  if( R <= 0 ) {
+    for( int q = threadIdx.x; q < CS_TX * CS_TY; q += 256 ) {
+      const int x = tx0 + q % CS_TX, y = ty0 + q / CS_TX;
+      if( x < w && y < h ) out[(size_t) y * w + x] = load_px<T>(fb, row_stride, x, y) * scale;
+    }
+    return;
+  }
+  const int SW = CS_TX + 2 * R, SH = CS_TY + 2 * R;
+  for( int q = threadIdx.x; q < SW * SH; q += 256 ) {
+    const int x = clampi(tx0 - R + q % SW, 0, w - 1);
+    const int y = clampi(ty0 - R + q / SW, 0, h - 1);
+    s_in[q] = load_px<T>(fb, row_stride, x, y) * scale;
+  }
+  __syncthreads();
+  for( int q = threadIdx.x; q < CS_TX * SH; q += 256 ) {
+    const int xx = q % CS_TX, yy = q / CS_TX;
+    const float * p = s_in + yy * SW + xx;
+    float a = 0.f;
+    for( int i = 0; i <= 2 * R; ++i ) a = fmaf(c_gauss[i], p[i], a);
+    s_h[yy * CS_TX + xx] = a;
+  }
+  __syncthreads();
+  for( int q = threadIdx.x; q < CS_TX * CS_TY; q += 256 ) {
+    const int xx = q % CS_TX, yy = q / CS_TX;
+    const int x = tx0 + xx, y = ty0 + yy;
+    if( x < w && y < h ) {
+      float a = 0.f;
+      for( int j = 0; j <= 2 * R; ++j ) a = fmaf(c_gauss[j], s_h[(yy + j) * CS_TX + xx], a);
+      out[(size_t) y * w + x] = a;
+    }
+  }
+}
+
+cudaError_t launch_convert_smooth(const void * src, int depth, int n, int w, int h, size_t row_stride,
+    size_t frame_stride, double scale, const float * gk, int ksize, float * dst, size_t dst_stride, cudaStream_t st)
+{
+  // gk: device array of ksize weights (nullptr: no smoothing)
+  const int R = gk ? ksize / 2 : 0;
+  if( R > CS_RMAX ) return cudaErrorInvalidValue;
+  dim3 grid((w + CS_TX - 1) / CS_TX, (h + CS_TY - 1) / CS_TY, n);
+  const uint8_t * s = (const uint8_t *) src;
+  switch ( depth ) {
+  case SST_DEPTH_U8: k_convert_smooth<uint8_t><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
+  case SST_DEPTH_U16: k_convert_smooth<uint16_t><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
+  case SST_DEPTH_F32: k_convert_smooth<float><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
+  default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------- pyrDown */
+
+constexpr int PD_TX = 32, PD_TY = 16;
+
+__global__ void __launch_bounds__(256) k_pyrdown(const float * src, int sw, int sh, size_t src_stride,
+    float * dst, int dw, int dh, size_t dst_stride)
+{
+  constexpr int SW = 2 * PD_TX + 4, SH = 2 * PD_TY + 4;
+  __shared__ float s_in[SH * SW];
+  __shared__ float s_h[SH * PD_TX];
+  const float * in = src + (size_t) blockIdx.z * src_stride;
+  float * out = dst + (size_t) blockIdx.z * dst_stride;
+  const int tx0 = blockIdx.x * PD_TX, ty0 = blockIdx.y * PD_TY;
+  const int sx0 = 2 * tx0 - 2, sy0 = 2 * ty0 - 2;
+  for( int q = threadIdx.x; q < SW * SH; q += 256 ) {
+    const int x = reflect101(sx0 + q % SW, sw), y = reflect101(sy0 + q / SW, sh);
+    s_in[q] = __ldg(in + (size_t) y * sw + x);
+  }
+  __syncthreads();
+  for( int q = threadIdx.x; q < PD_TX * SH; q += 256 ) {
+    const int xx = q % PD_TX, yy = q / PD_TX;
+    const float * p = s_in + yy * SW + 2 * xx;
+    s_h[yy * PD_TX + xx] = (p[0] + p[4]) * 0.0625f + (p[1] + p[3]) * 0.25f + p[2] * 0.375f;
+  }
+  __syncthreads();
+  for( int q = threadIdx.x; q < PD_TX * PD_TY; q += 256 ) {
+    const int xx = q % PD_TX, yy = q / PD_TX;
+    const int x = tx0 + xx, y = ty0 + yy;
+    if( x < dw && y < dh ) {
+      const float * p = s_h + (2 * yy) * PD_TX + xx;
+      out[(size_t) y * dw + x] = (p[0] + p[4 * PD_TX]) * 0.0625f + (p[PD_TX] + p[3 * PD_TX]) * 0.25f +
+          p[2 * PD_TX] * 0.375f;
+    }
+  }
+}
+
+cudaError_t launch_pyrdown(const float * src, int sw, int sh, size_t src_stride, float * dst, int dw, int dh,
+    size_t dst_stride, int n, cudaStream_t st)
+{
+  dim3 grid((dw + PD_TX - 1) / PD_TX, (dh + PD_TY - 1) / PD_TY, n);
+  k_pyrdown<<<grid, 256, 0, st>>>(src, sw, sh, src_stride, dst, dw, dh, dst_stride);
+  return cudaGetLastError();
+}
+
+/* cv::resize(INTER_NEAREST) of a mask: sx = floor(dx * sw / dw) */
+__global__ void k_resize_nearest_u8(const uint8_t * src, int sw, int sh, uint8_t * dst, int dw, int dh)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if( x >= dw || y >= dh ) return;
+  const int sx = min((int) floor(x * ((double) sw / dw)), sw - 1);
+  const int sy = min((int) floor(y * ((double) sh / dh)), sh - 1);
+  dst[(size_t) y * dw + x] = src[(size_t) sy * sw + sx];
+}
+
+cudaError_t launch_resize_nearest_u8(const uint8_t * src, int sw, int sh, uint8_t * dst, int dw, int dh, cudaStream_t st)
+{
+  k_resize_nearest_u8<<<dim3((dw + 127) / 128, dh), 128, 0, st>>>(src, sw, sh, dst, dw, dh);
+  return cudaGetLastError();
+}
+
+/* 5x5 erosion of a binary mask, window clipped to the image (every border
+ * mode the path uses for erode reduces to this) */
+__global__ void k_erode5(const uint8_t * src, int w, int h, uint8_t * dst)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if( x >= w || y >= h ) return;
+  uint8_t m = 255;
+  for( int j = max(0, y - 2); j <= min(h - 1, y + 2); ++j )
+    for( int i = max(0, x - 2); i <= min(w - 1, x + 2); ++i ) m = min(m, src[(size_t) j * w + i]);
+  dst[(size_t) y * w + x] = m;
+}
+
+cudaError_t launch_erode5(const uint8_t * src, int w, int h, uint8_t * dst, cudaStream_t st)
+{
+  k_erode5<<<dim3((w + 127) / 128, h), 128, 0, st>>>(src, w, h, dst);
+  return cudaGetLastError();
+}
+
+/* ---------------------------------------------------- reference gradients */
+
+constexpr int RG_TX = 32, RG_TY = 8;
+
+__global__ void __launch_bounds__(256) k_ref_gradients(const float * img, const uint8_t * mask, int w, int h, float2 * grad)
+{
+  constexpr int SW = RG_TX + 4, SH = RG_TY + 4;
+  __shared__ float s[SH * SW];
+  const int tx0 = blockIdx.x * RG_TX, ty0 = blockIdx.y * RG_TY;
+  for( int q = threadIdx.x; q < SW * SH; q += 256 ) {
+    const int x = clampi(tx0 - 2 + q % SW, 0, w - 1), y = clampi(ty0 - 2 + q / SW, 0, h - 1);
+    s[q] = __ldg(img + (size_t) y * w + x);
+  }
+  __syncthreads();
+  const int lx = threadIdx.x % RG_TX, ly = threadIdx.x / RG_TX;
+  const int x = tx0 + lx, y = ty0 + ly;
+  if( x >= w || y >= h ) return;
+  const float * p = s + (ly + 2) * SW + lx + 2;
+  const float a = 1.f / 12.f, b = -2.f / 3.f;
+  const float r0 = a * p[-SW - 2] + b * p[-SW - 1] - b * p[-SW + 1] - a * p[-SW + 2];
+  const float r1 = a * p[-2] + b * p[-1] - b * p[1] - a * p[2];
+  const float r2 = a * p[SW - 2] + b * p[SW - 1] - b * p[SW + 1] - a * p[SW + 2];
+  const float c0 = a * p[-2 * SW - 1] + b * p[-SW - 1] - b * p[SW - 1] - a * p[2 * SW - 1];
+  const float c1 = a * p[-2 * SW] + b * p[-SW] - b * p[SW] - a * p[2 * SW];
+  const float c2 = a * p[-2 * SW + 1] + b * p[-SW + 1] - b * p[SW + 1] - a * p[2 * SW + 1];
+  float2 g = make_float2(0.25f * r0 + 0.5f * r1 + 0.25f * r2, 0.25f * c0 + 0.5f * c1 + 0.25f * c2);
+  if( mask && !mask[(size_t) y * w + x] ) g = make_float2(0.f, 0.f);
+  grad[(size_t) y * w + x] = g;
+}
+
+cudaError_t launch_ref_gradients(const float * img, const uint8_t * mask, int w, int h, float2 * grad, cudaStream_t st)
+{
+  dim3 grid((w + RG_TX - 1) / RG_TX, (h + RG_TY - 1) / RG_TY);
+  k_ref_gradients<<<grid, 256, 0, st>>>(img, mask, w, h, grad);
+  return cudaGetLastError();
+}
+
+/* --------------------------------------------- IC Gauss-Newton matrix */
+
+/* per-tile lower-triangle sums of J J^T with J at the identity warp */
+template<int JK, int M>
+__global__ void __launch_bounds__(256) k_ref_hessian(const float2 * grad, int w, int h, int tiles_x, const float * jc_in,
+    double * partials)
+{
+  constexpr int NS = M * (M + 1) / 2;
+  __shared__ double s_red[8 * NS];
+  float jc[8];
+  for( int i = 0; i < 8; ++i ) jc[i] = jc_in[i];
+  const int t = blockIdx.x;
+  const int tx0 = (t % tiles_x) * PW_TX, ty0 = (t / tiles_x) * PW_TY;
+  const int x = tx0 + (threadIdx.x & (PW_TX - 1));
+  float acc[NS];
+  for( int k = 0; k < NS; ++k ) acc[k] = 0.f;
+  if( x < w ) {
+    for( int k = 0; k < PW_TY / 2; ++k ) {
+      const int y = ty0 + (threadIdx.x >> 7) + 2 * k;
+      if( y < h ) {
+        const float2 g = grad[(size_t) y * w + x];
+        float J[M];
+        // same formulas as the pass kernels (sd_pixel), at the identity
+        if( JK == J_TRANS ) { J[0] = g.x, J[1 < M ? 1 : 0] = g.y; }
+        else if( JK == J_EUCL ) {
+          const float xx = x - jc[3], yy = y - jc[4];
+          J[0] = g.x, J[1] = g.y;
+          const float u = jc[2] * xx - jc[1] * yy, v = jc[1] * xx + jc[2] * yy;
+          J[2 < M ? 2 : 0] = jc[0] * (-g.x * v + g.y * u);
+          if( M > 3 ) J[3 < M ? 3 : 0] = g.x * u + g.y * v;
+        }
+        else if( JK == J_AFFINE ) {
+          J[0] = g.x * x, J[1] = g.x * y, J[2] = g.x;
+          J[3 < M ? 3 : 0] = g.y * x, J[4 < M ? 4 : 0] = g.y * y, J[5 < M ? 5 : 0] = g.y;
+        }
+        else {
+          const float den = 1.0f / fmaf((float) x, jc[6], fmaf((float) y, jc[7], 1.0f));
+          const float hatX = -fmaf((float) x, jc[0], fmaf((float) y, jc[1], jc[2])) * den;
+          const float hatY = -fmaf((float) x, jc[3], fmaf((float) y, jc[4], jc[5])) * den;
+          const float ggx = g.x * den, ggy = g.y * den, gg = hatX * ggx + hatY * ggy;
+          J[0] = ggx * x, J[1] = ggx * y, J[2] = ggx;
+          J[3 < M ? 3 : 0] = ggy * x, J[4 < M ? 4 : 0] = ggy * y, J[5 < M ? 5 : 0] = ggy;
+          J[6 < M ? 6 : 0] = gg * x, J[7 < M ? 7 : 0] = gg * y;
+        }
+        for( int u = 0, kk = 0; u < M; ++u )
+          for( int v = 0; v <= u; ++v, ++kk ) acc[kk] = fmaf(J[u], J[v], acc[kk]);
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for( int k = 0; k < NS; ++k ) {
+    const double s = warp_sum((double) acc[k]);
+    if( lane == 0 ) s_red[wid * NS + k] = s;
+  }
+  __syncthreads();
+  for( int k = threadIdx.x; k < NS; k += 256 ) {
+    double s = 0;
+    for( int wv = 0; wv < 8; ++wv ) s += s_red[wv * NS + k];
+    partials[(size_t) t * NS + k] = s;
+  }
+}
+
+cudaError_t launch_ref_hessian(const float2 * grad, int w, int h, int jkind, int M, const float * jc,
+    double * partials, int * tiles_out, cudaStream_t st)
+{
+  int tx;
+  const int tiles = tiles_of(w, h, PW_TX, PW_TY, &tx);
+  *tiles_out = tiles;
+  switch ( jkind ) {
+  case J_TRANS: k_ref_hessian<J_TRANS, 2><<<tiles, 256, 0, st>>>(grad, w, h, tx, jc, partials); break;
+  case J_EUCL:
+    if( M == 3 ) k_ref_hessian<J_EUCL, 3><<<tiles, 256, 0, st>>>(grad, w, h, tx, jc, partials);
+    else k_ref_hessian<J_EUCL, 4><<<tiles, 256, 0, st>>>(grad, w, h, tx, jc, partials);
+    break;
+  case J_AFFINE: k_ref_hessian<J_AFFINE, 6><<<tiles, 256, 0, st>>>(grad, w, h, tx, jc, partials); break;
+  case J_HOMOG: k_ref_hessian<J_HOMOG, 8><<<tiles, 256, 0, st>>>(grad, w, h, tx, jc, partials); break;
+  default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+/* per-tile {sum T, n(all), n(mask != 0)} of a reference level */
+__global__ void __launch_bounds__(256) k_ref_stats(const float * img, const uint8_t * mask, int w, int h, int tiles_x,
+    double * partials)
+{
+  __shared__ double s_red[8 * 3];
+  const int t = blockIdx.x;
+  const int tx0 = (t % tiles_x) * PW_TX, ty0 = (t / tiles_x) * PW_TY;
+  const int x = tx0 + (threadIdx.x & (PW_TX - 1));
+  float acc[3] = { 0, 0, 0 };
+  if( x < w ) {
+    for( int k = 0; k < PW_TY / 2; ++k ) {
+      const int y = ty0 + (threadIdx.x >> 7) + 2 * k;
+      if( y < h ) {
+        acc[0] += img[(size_t) y * w + x];
+        acc[1] += 1.f;
+        acc[2] += (!mask || mask[(size_t) y * w + x]) ? 1.f : 0.f;
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for( int k = 0; k < 3; ++k ) {
+    const double s = warp_sum((double) acc[k]);
+    if( lane == 0 ) s_red[wid * 3 + k] = s;
+  }
+  __syncthreads();
+  if( threadIdx.x < 3 ) {
+    double s = 0;
+    for( int wv = 0; wv < 8; ++wv ) s += s_red[wv * 3 + threadIdx.x];
+    partials[(size_t) t * 3 + threadIdx.x] = s;
+  }
+}
+
+cudaError_t launch_ref_stats(const float * img, const uint8_t * mask, int w, int h, double * partials,
+    int * tiles_out, cudaStream_t st)
+{
+  int tx;
+  const int tiles = tiles_of(w, h, PW_TX, PW_TY, &tx);
+  *tiles_out = tiles;
+  k_ref_stats<<<tiles, 256, 0, st>>>(img, mask, w, h, tx, partials);
+  return cudaGetLastError();
+}
+
+/* -------------------------------------------------- frame sharpness weight */
+
+/* mean over the interior of a pyramid level of the squared 5-point Laplacian:
+ * per-tile {sum, count} partials, combined in order by k_finalize */
+constexpr int LE_TX = 64, LE_TY = 16;
+
+int lap_tiles(int w, int h)
+{
+  return ((w + LE_TX - 1) / LE_TX) * ((h + LE_TY - 1) / LE_TY);
+}
+
+__global__ void __launch_bounds__(256) k_lap_energy(const float * pyr, size_t pyr_stride, size_t lvl_off, int w, int h,
+    double * partials, int tiles)
+{
+  __shared__ double s_red[8 * 2];
+  const int f = blockIdx.y, t = blockIdx.x;
+  const float * img = pyr + (size_t) f * pyr_stride + lvl_off;
+  const int tiles_x = (w + LE_TX - 1) / LE_TX;
+  const int tx0 = (t % tiles_x) * LE_TX, ty0 = (t / tiles_x) * LE_TY;
+  float acc[2] = { 0, 0 };
+  const int x = tx0 + (threadIdx.x & (LE_TX - 1));
+  for( int k = 0; k < LE_TY / 4; ++k ) {
+    const int y = ty0 + (threadIdx.x >> 6) + 4 * k;
+    if( x >= 1 && x < w - 1 && y >= 1 && y < h - 1 ) {
+      const float * p = img + (size_t) y * w + x;
+      const float l = __ldg(p - 1) + __ldg(p + 1) + __ldg(p - w) + __ldg(p + w) - 4.f * __ldg(p);
+      acc[0] = fmaf(l, l, acc[0]);
+      acc[1] += 1.f;
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for( int k = 0; k < 2; ++k ) {
+    const double s = warp_sum((double) acc[k]);
+    if( lane == 0 ) s_red[wid * 2 + k] = s;
+  }
+  __syncthreads();
+  if( threadIdx.x < 2 ) {
+    double s = 0;
+    for( int wv = 0; wv < 8; ++wv ) s += s_red[wv * 2 + threadIdx.x];
+    partials[((size_t) f * tiles + t) * 2 + threadIdx.x] = s;
+  }
+}
+
+cudaError_t launch_lap_energy(const float * pyr, size_t pyr_stride, size_t lvl_off, int w, int h, int n,
+    double * partials, int tiles, cudaStream_t st)
+{
+  k_lap_energy<<<dim3(tiles, n), 256, 0, st>>>(pyr, pyr_stride, lvl_off, w, h, partials, tiles);
+  return cudaGetLastError();
+}
+
+}  // namespace sst

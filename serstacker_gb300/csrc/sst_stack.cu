@@ -1,0 +1,354 @@
+/*
+ * sst_stack.cu -- warp + weighted accumulation kernels (sm_103a).
+ *
+ *   batched warp + stack : c_frame_registration::base_remap
+ *                          (c_frame_registration.cc:1265-1340) fused with
+ *                          multiply_weights (c_image_stacking_pipeline.cc:1704-1714)
+ *                          and c_weigthed_average::add (c_frame_accumulation.cc:182-221)
+ *   plain add            : _weighted_average_update (c_frame_accumulation.cc:20-129)
+ *   compute              : c_weigthed_average::compute (c_frame_accumulation.cc:223-248)
+ *   remap                : base_remap for one frame (image + mask)
+ *   Bayer planes         : extract_bayer_planes / average_bayer_planes (debayer.cc:96-147, 277-330)
+ *
+ * Accumulator layout in HBM: four planar FP32 planes of width x height:
+ * S (sum of w*I), cS (its Kahan-Babuska compensation), W (sum of w), cW.
+ * The batched kernel assigns each output pixel to one thread, which warps
+ * and accumulates every frame of the batch in registers (compensated) and
+ * touches the accumulator planes once per batch: no atomics, deterministic.
+ */
+#include "sst_engine.cuh"
+#include "sst_stack.cuh"
+
+namespace sst {
+
+template<typename T>
+__device__ __forceinline__ float ldpx(const uint8_t * base, size_t row_stride, int x, int y)
+{
+  return (float) __ldg((const T *) (base + (size_t) y * row_stride) + x);
+}
+
+/* per-frame FP32 displacement coefficients from API parameter vectors */
+__global__ void k_coeffs_from_params(sst_motion_model m, const float * params, int n, float * coeffs)
+{
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if( f >= n ) return;
+  double s[16], p[12];
+  model_identity(m, s);
+  const int M = model_nparams(m);
+  for( int j = 0; j < M; ++j ) p[j] = params[(size_t) f * 12 + j];
+  model_set_params(m, s, p);
+  model_warp_coeffs(m, s, coeffs + (size_t) f * SST_NCOEF);
+}
+
+cudaError_t launch_coeffs_from_params(const sst_motion_model & m, const float * params, int n, float * coeffs, cudaStream_t st)
+{
+  k_coeffs_from_params<<<(n + 127) / 128, 128, 0, st>>>(m, params, n, coeffs);
+  return cudaGetLastError();
+}
+
+/* effective per-frame weight: weight (or 1) where status == OK, else 0 */
+__global__ void k_effective_weights(const float * weights, const int32_t * status, int n, float * out)
+{
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if( f >= n ) return;
+  float w = weights ? weights[f] : 1.0f;
+  if( status && status[f] != SST_FRAME_OK ) w = 0.f;
+  out[f] = w > 0 ? w : 0.f;
+}
+
+cudaError_t launch_effective_weights(const float * weights, const int32_t * status, int n, float * out, cudaStream_t st)
+{
+  k_effective_weights<<<(n + 127) / 128, 128, 0, st>>>(weights, status, n, out);
+  return cudaGetLastError();
+}
+
+constexpr int SK_TX = 32, SK_TY = 8;
+
+template<int FAM, typename T>
+__global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
+{
+  constexpr int VW = SK_TX + 4, VH = SK_TY + 4;
+  __shared__ uint8_t s_v[VH * VW];
+  __shared__ uint8_t s_h[VH * SK_TX];
+  __shared__ float s_c[SST_NCOEF];
+  const int tx0 = blockIdx.x * SK_TX, ty0 = blockIdx.y * SK_TY;
+  const int lx = threadIdx.x % SK_TX, ly = threadIdx.x / SK_TX;
+  const int x = tx0 + lx, y = ty0 + ly;
+  float S = 0.f, cS = 0.f, Wt = 0.f, cW = 0.f;
+  for( int f = 0; f < a.n; ++f ) {
+    const float wf = __ldg(a.weights + f);
+    if( !(wf > 0.f) ) continue;                 // uniform over the CTA
+    if( threadIdx.x < SST_NCOEF ) s_c[threadIdx.x] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + threadIdx.x);
+    __syncthreads();
+    float c[SST_NCOEF];
+#pragma unroll
+    for( int i = 0; i < SST_NCOEF; ++i ) c[i] = s_c[i];
+    // remap(255-mask, LINEAR, CONSTANT 0) >= 255 over the tile + 2 px halo;
+    // positions outside the output count as 255 (erode border value)
+    for( int q = threadIdx.x; q < VW * VH; q += 256 ) {
+      const int qx = tx0 - 2 + q % VW, qy = ty0 - 2 + q / VW;
+      uint8_t v = 1;
+      if( qx >= 0 && qx < a.dw && qy >= 0 && qy < a.dh ) {
+        v = mask_ok(coverage(a.sw, a.sh, warp_pos<FAM>(c, qx, qy)), 255) ? 1 : 0;
+      }
+      s_v[q] = v;
+    }
+    __syncthreads();
+    for( int q = threadIdx.x; q < SK_TX * VH; q += 256 ) {
+      const int xx = q % SK_TX, yy = q / SK_TX;
+      const uint8_t * p = s_v + yy * VW + xx;
+      s_h[yy * SK_TX + xx] = p[0] & p[1] & p[2] & p[3] & p[4];
+    }
+    __syncthreads();
+    if( x < a.dw && y < a.dh ) {
+      const uint8_t * p = s_h + ly * SK_TX + lx;
+      if( p[0] & p[SK_TX] & p[2 * SK_TX] & p[3 * SK_TX] & p[4 * SK_TX] ) {
+        const spos s = warp_pos<FAM>(c, x, y);
+        // valid => every tap with a non-zero weight is inside; clamp the rest
+        const int xa = clampi(s.x0, 0, a.sw - 1), xb = clampi(s.x0 + 1, 0, a.sw - 1);
+        const int ya = clampi(s.y0, 0, a.sh - 1), yb = clampi(s.y0 + 1, 0, a.sh - 1);
+        const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
+        const float v00 = ldpx<T>(fb, a.row_stride, xa, ya), v01 = ldpx<T>(fb, a.row_stride, xb, ya);
+        const float v10 = ldpx<T>(fb, a.row_stride, xa, yb), v11 = ldpx<T>(fb, a.row_stride, xb, yb);
+        const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+        const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
+        kahan_add(S, cS, wf * val);
+        kahan_add(Wt, cW, wf);
+      }
+    }
+    __syncthreads();
+  }
+  if( x < a.dw && y < a.dh ) {
+    const size_t i = (size_t) y * a.dw + x;
+    float gS = a.acc[i], gcS = a.acc[a.plane + i], gW = a.acc[2 * a.plane + i], gcW = a.acc[3 * a.plane + i];
+    kahan_add(gS, gcS, S);
+    gcS += cS;
+    kahan_add(gW, gcW, Wt);
+    gcW += cW;
+    a.acc[i] = gS, a.acc[a.plane + i] = gcS, a.acc[2 * a.plane + i] = gW, a.acc[3 * a.plane + i] = gcW;
+  }
+}
+
+cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, cudaStream_t st)
+{
+  dim3 grid((a.dw + SK_TX - 1) / SK_TX, (a.dh + SK_TY - 1) / SK_TY);
+  const int fam = motion_family(motion);
+#define SST_LAUNCH_STACK(FAMV, TV) k_stack_add_warped<FAMV, TV><<<grid, 256, 0, st>>>(a)
+  switch ( depth ) {
+  case SST_DEPTH_U8:
+    if( fam == FAM_AFFINE ) SST_LAUNCH_STACK(FAM_AFFINE, uint8_t);
+    else if( fam == FAM_HOMOG ) SST_LAUNCH_STACK(FAM_HOMOG, uint8_t);
+    else SST_LAUNCH_STACK(FAM_QUAD, uint8_t);
+    break;
+  case SST_DEPTH_U16:
+    if( fam == FAM_AFFINE ) SST_LAUNCH_STACK(FAM_AFFINE, uint16_t);
+    else if( fam == FAM_HOMOG ) SST_LAUNCH_STACK(FAM_HOMOG, uint16_t);
+    else SST_LAUNCH_STACK(FAM_QUAD, uint16_t);
+    break;
+  case SST_DEPTH_F32:
+    if( fam == FAM_AFFINE ) SST_LAUNCH_STACK(FAM_AFFINE, float);
+    else if( fam == FAM_HOMOG ) SST_LAUNCH_STACK(FAM_HOMOG, float);
+    else SST_LAUNCH_STACK(FAM_QUAD, float);
+    break;
+  default: return cudaErrorInvalidValue;
+  }
+#undef SST_LAUNCH_STACK
+  return cudaGetLastError();
+}
+
+/* c_weigthed_average::add of one already-warped frame */
+template<typename T>
+__global__ void k_stack_add_plain(const uint8_t * src, size_t row_stride, float scale, const uint8_t * wts,
+    int wdepth, size_t wstride, int w, int h, float * acc, size_t plane)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if( x >= w || y >= h ) return;
+  float wt = 1.f;
+  if( wts ) {
+    if( wdepth == SST_DEPTH_U8 ) wt = wts[(size_t) y * wstride + x] ? 1.f : 0.f;
+    else wt = *(const float *) (wts + (size_t) y * wstride + (size_t) x * 4);
+  }
+  if( !(wt > 0.f) ) return;
+  const float v = (float) (*(const T *) (src + (size_t) y * row_stride + (size_t) x * sizeof(T))) * scale;
+  const size_t i = (size_t) y * w + x;
+  float gS = acc[i], gcS = acc[plane + i], gW = acc[2 * plane + i], gcW = acc[3 * plane + i];
+  kahan_add(gS, gcS, wt * v);
+  kahan_add(gW, gcW, wt);
+  acc[i] = gS, acc[plane + i] = gcS, acc[2 * plane + i] = gW, acc[3 * plane + i] = gcW;
+}
+
+cudaError_t launch_stack_add_plain(const void * src, int depth, size_t row_stride, double scale, const void * wts,
+    int wdepth, size_t wstride, int w, int h, float * acc, size_t plane, cudaStream_t st)
+{
+  dim3 grid((w + 127) / 128, h);
+  const uint8_t * s = (const uint8_t *) src;
+  const uint8_t * wp = (const uint8_t *) wts;
+  switch ( depth ) {
+  case SST_DEPTH_U8: k_stack_add_plain<uint8_t><<<grid, 128, 0, st>>>(s, row_stride, (float) scale, wp, wdepth, wstride, w, h, acc, plane); break;
+  case SST_DEPTH_U16: k_stack_add_plain<uint16_t><<<grid, 128, 0, st>>>(s, row_stride, (float) scale, wp, wdepth, wstride, w, h, acc, plane); break;
+  case SST_DEPTH_F32: k_stack_add_plain<float><<<grid, 128, 0, st>>>(s, row_stride, (float) scale, wp, wdepth, wstride, w, h, acc, plane); break;
+  default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+__global__ void k_stack_compute(const float * acc, size_t plane, int n, float * avg, uint8_t * mask, float * accw)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if( i >= n ) return;
+  const double S = (double) acc[i] + (double) acc[plane + i];
+  const double W = (double) acc[2 * plane + i] + (double) acc[3 * plane + i];
+  if( avg ) avg[i] = W > 0 ? (float) (S / W) : 0.f;
+  if( mask ) mask[i] = W > 0 ? 255 : 0;
+  if( accw ) accw[i] = (float) W;
+}
+
+cudaError_t launch_stack_compute(const float * acc, size_t plane, int n, float * avg, uint8_t * mask, float * accw, cudaStream_t st)
+{
+  k_stack_compute<<<(n + 255) / 256, 256, 0, st>>>(acc, plane, n, avg, mask, accw);
+  return cudaGetLastError();
+}
+
+/* reinitialize(avg, accw): S = avg * accw, W = accw, compensations 0 */
+__global__ void k_stack_reinit(float * acc, size_t plane, int n, const float * avg, const float * accw)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if( i >= n ) return;
+  acc[i] = avg[i] * accw[i];
+  acc[plane + i] = 0.f;
+  acc[2 * plane + i] = accw[i];
+  acc[3 * plane + i] = 0.f;
+}
+
+cudaError_t launch_stack_reinit(float * acc, size_t plane, int n, const float * avg, const float * accw, cudaStream_t st)
+{
+  k_stack_reinit<<<(n + 255) / 256, 256, 0, st>>>(acc, plane, n, avg, accw);
+  return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------- remap */
+
+template<typename T>
+__device__ __forceinline__ float tap(const uint8_t * fb, size_t rs, int sw, int sh, int xi, int yi, int border)
+{
+  if( xi >= 0 && xi < sw && yi >= 0 && yi < sh ) return ldpx<T>(fb, rs, xi, yi);
+  switch ( border ) {
+  case SST_BORDER_REPLICATE: return ldpx<T>(fb, rs, clampi(xi, 0, sw - 1), clampi(yi, 0, sh - 1));
+  case SST_BORDER_REFLECT101: return ldpx<T>(fb, rs, reflect101(xi, sw), reflect101(yi, sh));
+  case SST_BORDER_REFLECT: return ldpx<T>(fb, rs, reflect(xi, sw), reflect(yi, sh));
+  default: return 0.f;
+  }
+}
+
+template<int FAM, typename T>
+__global__ void __launch_bounds__(256) k_remap(const uint8_t * src, int sw, int sh, size_t rs, float scale,
+    const float * coeffs, int border, float * dst, uint8_t * dst_mask, int dw, int dh)
+{
+  constexpr int VW = SK_TX + 4, VH = SK_TY + 4;
+  __shared__ uint8_t s_v[VH * VW];
+  __shared__ uint8_t s_h[VH * SK_TX];
+  float c[SST_NCOEF];
+#pragma unroll
+  for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __ldg(coeffs + i);
+  const int tx0 = blockIdx.x * SK_TX, ty0 = blockIdx.y * SK_TY;
+  const int lx = threadIdx.x % SK_TX, ly = threadIdx.x / SK_TX;
+  const int x = tx0 + lx, y = ty0 + ly;
+  if( dst_mask ) {
+    for( int q = threadIdx.x; q < VW * VH; q += 256 ) {
+      const int qx = tx0 - 2 + q % VW, qy = ty0 - 2 + q / VW;
+      uint8_t v = 1;
+      if( qx >= 0 && qx < dw && qy >= 0 && qy < dh ) {
+        v = mask_ok(coverage(sw, sh, warp_pos<FAM>(c, qx, qy)), 255) ? 1 : 0;
+      }
+      s_v[q] = v;
+    }
+    __syncthreads();
+    for( int q = threadIdx.x; q < SK_TX * VH; q += 256 ) {
+      const int xx = q % SK_TX, yy = q / SK_TX;
+      const uint8_t * p = s_v + yy * VW + xx;
+      s_h[yy * SK_TX + xx] = p[0] & p[1] & p[2] & p[3] & p[4];
+    }
+    __syncthreads();
+  }
+  if( x >= dw || y >= dh ) return;
+  const size_t i = (size_t) y * dw + x;
+  if( dst_mask ) {
+    const uint8_t * p = s_h + ly * SK_TX + lx;
+    dst_mask[i] = (p[0] & p[SK_TX] & p[2 * SK_TX] & p[3 * SK_TX] & p[4 * SK_TX]) ? 255 : 0;
+  }
+  if( dst ) {
+    const spos s = warp_pos<FAM>(c, x, y);
+    const float v00 = tap<T>(src, rs, sw, sh, s.x0, s.y0, border), v01 = tap<T>(src, rs, sw, sh, s.x0 + 1, s.y0, border);
+    const float v10 = tap<T>(src, rs, sw, sh, s.x0, s.y0 + 1, border), v11 = tap<T>(src, rs, sw, sh, s.x0 + 1, s.y0 + 1, border);
+    const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+    dst[i] = fmaf(s.fy, t1 - t0, t0) * scale;
+  }
+}
+
+cudaError_t launch_remap(const void * src, int depth, int sw, int sh, size_t rs, double scale, int motion,
+    const float * coeffs, int border, float * dst, uint8_t * dst_mask, int dw, int dh, cudaStream_t st)
+{
+  dim3 grid((dw + SK_TX - 1) / SK_TX, (dh + SK_TY - 1) / SK_TY);
+  const int fam = motion_family(motion);
+  const uint8_t * s = (const uint8_t *) src;
+  const float sc = (float) scale;
+#define SST_LAUNCH_REMAP(FAMV, TV) k_remap<FAMV, TV><<<grid, 256, 0, st>>>(s, sw, sh, rs, sc, coeffs, border, dst, dst_mask, dw, dh)
+  switch ( depth ) {
+  case SST_DEPTH_U8:
+    if( fam == FAM_AFFINE ) SST_LAUNCH_REMAP(FAM_AFFINE, uint8_t);
+    else if( fam == FAM_HOMOG ) SST_LAUNCH_REMAP(FAM_HOMOG, uint8_t);
+    else SST_LAUNCH_REMAP(FAM_QUAD, uint8_t);
+    break;
+  case SST_DEPTH_U16:
+    if( fam == FAM_AFFINE ) SST_LAUNCH_REMAP(FAM_AFFINE, uint16_t);
+    else if( fam == FAM_HOMOG ) SST_LAUNCH_REMAP(FAM_HOMOG, uint16_t);
+    else SST_LAUNCH_REMAP(FAM_QUAD, uint16_t);
+    break;
+  case SST_DEPTH_F32:
+    if( fam == FAM_AFFINE ) SST_LAUNCH_REMAP(FAM_AFFINE, float);
+    else if( fam == FAM_HOMOG ) SST_LAUNCH_REMAP(FAM_HOMOG, float);
+    else SST_LAUNCH_REMAP(FAM_QUAD, float);
+    break;
+  default: return cudaErrorInvalidValue;
+  }
+#undef SST_LAUNCH_REMAP
+  return cudaGetLastError();
+}
+
+/* ----------------------------------------------------------- Bayer planes */
+
+/* extract_bayer_planes: dst[y][x][0..3] = src(2y,2x), src(2y,2x+1), src(2y+1,2x), src(2y+1,2x+1) */
+__global__ void k_extract_bayer_planes_u16(const uint8_t * src, int w, int h, size_t rs, uint16_t * dst)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  const int c4 = w / 2;
+  if( x >= c4 || y >= h / 2 ) return;
+  const uint32_t r0 = __ldg((const uint32_t *) (src + (size_t) (2 * y) * rs) + x);
+  const uint32_t r1 = __ldg((const uint32_t *) (src + (size_t) (2 * y + 1) * rs) + x);
+  uint2 o;
+  o.x = (r0 & 0xffffu) | (r0 & 0xffff0000u);
+  o.y = (r1 & 0xffffu) | (r1 & 0xffff0000u);
+  reinterpret_cast<uint2 *>(dst)[(size_t) y * c4 + x] = o;
+}
+
+/* average_bayer_planes of a raw mosaic: (2 + sum of the 2x2 block) / 4 */
+__global__ void k_average_bayer_planes_u16(const uint8_t * src, int w, int h, size_t rs, uint16_t * dst)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  const int c4 = w / 2;
+  if( x >= c4 || y >= h / 2 ) return;
+  const uint32_t r0 = __ldg((const uint32_t *) (src + (size_t) (2 * y) * rs) + x);
+  const uint32_t r1 = __ldg((const uint32_t *) (src + (size_t) (2 * y + 1) * rs) + x);
+  const int s = 2 + (int) (r0 & 0xffffu) + (int) (r0 >> 16) + (int) (r1 & 0xffffu) + (int) (r1 >> 16);
+  dst[(size_t) y * c4 + x] = (uint16_t) min(s / 4, 65535);
+}
+
+cudaError_t launch_bayer_planes(int op, const uint16_t * src, int w, int h, size_t rs, uint16_t * dst, cudaStream_t st)
+{
+  dim3 grid((w / 2 + 127) / 128, h / 2);
+  if( op == 0 ) k_extract_bayer_planes_u16<<<grid, 128, 0, st>>>((const uint8_t *) src, w, h, rs, dst);
+  else k_average_bayer_planes_u16<<<grid, 128, 0, st>>>((const uint8_t *) src, w, h, rs, dst);
+  return cudaGetLastError();
+}
+
+}  // namespace sst

@@ -1,0 +1,266 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle.
+
+Tolerances (stated by the benchmark spec): registration within 0.02 px RMS of the
+oracle's warp over the frame grid; stacked pixels within 1e-5 relative of the
+FP64 sums; Bayer plane extraction and 2x2 binning bit-exact.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from serstacker_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+WARP_RMS_TOL = 0.02      # px
+STACK_REL_TOL = 1e-5
+
+
+def _grid_rms(O, m, s_a, s_b, w, h, step=4):
+    ys, xs = np.mgrid[0:h:step, 0:w:step]
+    d2 = []
+    for y, x in zip(ys.ravel(), xs.ravel()):
+        xa, ya = O.warp(m, s_a, float(x), float(y))
+        xb, yb = O.warp(m, s_b, float(x), float(y))
+        d2.append((xa - xb) ** 2 + (ya - yb) ** 2)
+    return math.sqrt(float(np.mean(d2)))
+
+
+def _sequence(n, w, h, seed, kind="config1", noise=True):
+    sc = synth.Scene(w, h, 0.28 * min(w, h))
+    rng = np.random.default_rng(seed)
+    Hs = synth.random_warps(rng, n, kind)
+    Hs[:, 0, 2] *= w / 640.0
+    Hs[:, 1, 2] *= h / 480.0
+    frames = np.empty((n, h, w), np.float32)
+    for i in range(n):
+        img = synth.render_frame_np(sc, Hs[i], 0.5)
+        if noise:
+            img = synth.add_noise_np(rng, img, 2.0, 1.0, 1e9)
+        frames[i] = img.astype(np.float32)
+    return synth.reference_np(sc), frames, Hs
+
+
+def _state_from_params(O, m, p):
+    s = O.identity(m)
+    return O.set_params(m, s, np.asarray(p, np.float64))
+
+
+CASES = [
+    (1, 3), (1, 4), (1, 0), (1, 1),     # IC: affine, homography, translation, euclidean
+    (3, 3), (3, 4),                     # IC-LM
+    (0, 3), (0, 1),                     # FA
+    (2, 3), (2, 6),                     # LM (quadratic only runs with FA / LM)
+]
+
+
+@pytest.mark.parametrize("method,motion", CASES)
+def test_registration_matches_oracle(gpu, oracle, method, motion):
+    C, O = gpu, oracle
+    w, h, n = 192, 144, 4
+    ref, frames, Hs = _sequence(n, w, h, seed=100 + 10 * method + motion)
+    maxlevel = 3
+    opts = C.default_options(method=method, maxlevel=maxlevel, max_iterations=40, epsx=0.01,
+                             minimum_image_size=16)
+    reg = C.c_ecch(opts)
+    reg.set_reference_image(ref.astype(np.float32))
+    out = reg.align(frames, [motion])
+    oo = O.ecch_opts(method=method, maxlevel=maxlevel, max_iterations=40, epsx=0.01, minimum_image_size=16)
+    m = O.model(motion)
+    for i in range(n):
+        s_o, it_o, e_o = O.ecch_align(m, O.identity(m), ref, frames[i].astype(np.float64), oo)
+        s_g = _state_from_params(O, m, out["params"][i])
+        rms = _grid_rms(O, m, s_o, s_g, w, h)
+        assert out["status"][i] == 0, out["status"]
+        assert rms <= WARP_RMS_TOL, (method, motion, i, rms, out["iterations"][i], it_o)
+
+
+def test_two_pass_affine_then_homography(gpu, oracle):
+    C, O = gpu, oracle
+    w, h, n = 256, 192, 3
+    ref, frames, Hs = _sequence(n, w, h, seed=7)
+    opts = C.default_options(method=1, maxlevel=3, max_iterations=40, epsx=0.01, minimum_image_size=16)
+    reg = C.c_ecch(opts)
+    reg.set_reference_image(ref.astype(np.float32))
+    out = reg.align(frames, [3, 4])
+    po = O.pipeline_opts(passes=(3, 4), method=1, maxlevel=3, max_iterations=40, epsx=0.01, min_rho=0.0,
+                         minimum_image_size=16)
+    m = O.model(4)
+    for i in range(n):
+        s = O.identity(O.model(3))
+        s_a, _, _ = O.ecch_align(O.model(3), s, ref, frames[i].astype(np.float64), po.ecch)
+        s_h = O.identity(m)
+        s_h[:6] = s_a[:6]
+        s_o, _, _ = O.ecch_align(m, s_h, ref, frames[i].astype(np.float64), po.ecch)
+        rms = _grid_rms(O, m, s_o, _state_from_params(O, m, out["params"][i]), w, h)
+        assert rms <= WARP_RMS_TOL, (i, rms)
+
+
+def test_batch_equals_plain_bitwise(gpu):
+    C = gpu
+    w, h, n = 160, 128, 6
+    ref, frames, _ = _sequence(n, w, h, seed=3)
+    for method in (1, 3, 0, 2):
+        reg = C.c_ecch(C.default_options(method=method, maxlevel=2, max_iterations=30, epsx=0.01,
+                                         minimum_image_size=16))
+        reg.set_reference_image(ref.astype(np.float32))
+        a = reg.align(frames, [3])
+        b = reg.align(frames, [3], plain=True)
+        c = reg.align(frames[2:4], [3])
+        assert np.array_equal(a["params"], b["params"]), method
+        assert np.array_equal(a["iterations"], b["iterations"]), method
+        assert np.array_equal(a["params"][2:4], c["params"]), method
+
+
+@pytest.mark.parametrize("data", ["scene", "noise"])
+def test_stack_matches_fp64(gpu, oracle, data):
+    """Batched warp + weighted stack vs FP64 sums with the same parameters.
+
+    Relative error is measured against max(|avg|, 1% of full scale): pixels whose
+    stacked value is ~0 carry no relative information."""
+    C, O = gpu, oracle
+    w, h, n = 200, 150, 12
+    rng = np.random.default_rng(5)
+    if data == "noise":
+        frames = rng.integers(0, 60000, size=(n, h, w), dtype=np.uint16)
+    else:
+        sc = synth.Scene(w, h, 55.0)
+        frames, _, _ = synth.make_sequence_np(sc, n, seed=5, kind="config1", dtype=np.uint16, gain=200.0,
+                                               blur_range=(0.8, 2.5))
+    motion = 4
+    params = np.zeros((n, 8), np.float32)
+    for i in range(n):
+        params[i] = [1 + rng.normal(0, 1e-3), rng.normal(0, 1e-3), rng.uniform(-5, 5), rng.normal(0, 1e-3),
+                     1 + rng.normal(0, 1e-3), rng.uniform(-5, 5), rng.normal(0, 1e-6), rng.normal(0, 1e-6)]
+    weights = rng.uniform(0.5, 2.0, size=n).astype(np.float32)
+    scale = 1.0 / 65535.0
+    acc = C.c_weigthed_average(w, h)
+    acc.add_warped(frames, motion, params, weights=weights, scale=scale)
+    avg, mask = acc.compute()
+    m = O.model(motion)
+    S = np.zeros((h, w))
+    W = np.zeros((h, w))
+    for i in range(n):
+        s = _state_from_params(O, m, params[i].astype(np.float64))
+        dst, msk = O.stack_remap(m, s, frames[i].astype(np.float64) * scale, w, h)
+        wt = np.where(msk > 0, float(weights[i]), 0.0)
+        S += wt * dst
+        W += wt
+    ref_avg = np.where(W > 0, S / np.where(W > 0, W, 1), 0)
+    agree = (mask > 0) == (W > 0)
+    assert agree.mean() > 0.999
+    both = (mask > 0) & (W > 0)
+    floor = 0.01 * float(ref_avg.max())
+    rel = np.abs(avg[both] - ref_avg[both]) / np.maximum(np.abs(ref_avg[both]), floor)
+    assert rel.max() <= STACK_REL_TOL, rel.max()
+    assert acc.accumulated_frames() == n
+
+
+def test_plain_add_and_counters(gpu):
+    C = gpu
+    w, h = 64, 48
+    rng = np.random.default_rng(6)
+    acc = C.c_weigthed_average(w, h)
+    imgs = [rng.random((h, w)).astype(np.float32) for _ in range(5)]
+    wts = [rng.random((h, w)).astype(np.float32) for _ in range(5)]
+    for im, wt in zip(imgs, wts):
+        acc.add(im, wt)
+    avg, mask = acc.compute()
+    S = sum(wt.astype(np.float64) * im for im, wt in zip(imgs, wts))
+    W = sum(wt.astype(np.float64) for wt in wts)
+    assert np.allclose(avg, S / W, rtol=1e-6)
+    assert np.allclose(acc.get_acc_counters(), W, rtol=1e-6)
+    # constant frames -> exact mean
+    acc2 = C.c_weigthed_average(w, h)
+    for _ in range(7):
+        acc2.add(np.full((h, w), 0.375, np.float32))
+    avg2, _ = acc2.compute()
+    assert np.all(avg2 == np.float32(0.375))
+
+
+@pytest.mark.parametrize("border", [0, 1, 2, 4])
+def test_remap_matches_oracle(gpu, oracle, border):
+    C, O = gpu, oracle
+    rng = np.random.default_rng(8)
+    src = rng.random((90, 120)).astype(np.float32)
+    p = np.array([1.01, 0.02, -6.3, -0.015, 0.99, 4.7], np.float32)
+    dst, msk = C.remap(src, 3, p, border=border)
+    m = O.model(3)
+    s = _state_from_params(O, m, p.astype(np.float64))
+    ref = O.remap(m, s, src.astype(np.float64), 120, 90, border=border)
+    _, ref_m = O.stack_remap(m, s, src.astype(np.float64), 120, 90)
+    assert np.abs(dst - ref).max() < 2e-6
+    assert (msk == ref_m).mean() > 0.999
+
+
+def test_bayer_planes_bit_exact(gpu, oracle):
+    C, O = gpu, oracle
+    rng = np.random.default_rng(9)
+    raw = rng.integers(0, 4096, size=(208, 310), dtype=np.uint16)
+    assert np.array_equal(C.bayer_planes(raw), O.extract_bayer_planes(raw))
+    assert np.array_equal(C.bayer_planes(raw, average=True), O.average_bayer_planes(raw))
+
+
+def test_pipeline_matches_oracle(gpu, oracle):
+    """sst_stack_frames (register + warp + weight + stack) vs the oracle pipeline."""
+    C, O = gpu, oracle
+    w, h, n = 192, 144, 5
+    sc = synth.Scene(w, h, 0.28 * min(w, h))
+    frames, Hs, _ = synth.make_sequence_np(sc, n, seed=11, kind="config1", dtype=np.uint16, gain=64.0,
+                                           blur_range=(0.8, 2.0))
+    ref = synth.reference_np(sc) * 64.0
+    scale = 1.0 / 65535.0
+    opts = C.default_options(method=1, maxlevel=3, max_iterations=40, epsx=0.01, minimum_image_size=16, min_rho=0.5)
+    reg = C.c_ecch(opts)
+    reg.set_reference_image(ref.astype(np.float32), scale=scale)
+    acc = C.c_weigthed_average(w, h)
+    out = C.stack_frames(reg, acc, frames, [3, 4], scale, weighting=1)
+    avg, mask = acc.compute()
+    po = O.pipeline_opts(passes=(3, 4), method=1, maxlevel=3, max_iterations=40, epsx=0.01, min_rho=0.5,
+                         minimum_image_size=16)
+    states, status, rho, S, W = O.register_and_stack(po, ref * scale, frames, scale)
+    m = O.model(4)
+    for i in range(n):
+        assert out["status"][i] == status[i]
+        rms = _grid_rms(O, m, states[i], _state_from_params(O, m, out["params"][i][:8]), w, h)
+        assert rms <= WARP_RMS_TOL, (i, rms)
+        assert out["rho"][i] == pytest.approx(rho[i], abs=1e-4)
+    both = (mask > 0) & (W > 0)
+    assert ((mask > 0) == (W > 0)).mean() > 0.995
+    ref_avg = S[both] / W[both]
+    rel = np.abs(avg[both] - ref_avg) / np.maximum(np.abs(ref_avg), 1e-3)
+    # registration differences within 0.02 px move edge pixels; compare where both agree closely
+    assert np.median(rel) < 1e-4
+
+
+def test_checkpoint_resume_is_bitwise(gpu):
+    C = gpu
+    w, h = 96, 64
+    rng = np.random.default_rng(12)
+    frames = rng.integers(0, 4000, size=(8, h, w), dtype=np.uint16)
+    params = np.tile(np.array([1, 0, 0.5, 0, 1, -0.25], np.float32), (8, 1))
+    one = C.c_weigthed_average(w, h)
+    one.add_warped(frames[:4], 3, params[:4])
+    state, nf = one.save_state()
+    one.add_warped(frames[4:], 3, params[4:])
+    two = C.c_weigthed_average(w, h)
+    two.load_state(state, nf)
+    two.add_warped(frames[4:], 3, params[4:])
+    assert np.array_equal(one.save_state()[0], two.save_state()[0])
+
+
+def test_failure_status_codes(gpu):
+    C = gpu
+    w, h = 128, 96
+    ref, frames, _ = _sequence(3, w, h, seed=13)
+    frames[1] = np.nan
+    reg = C.c_ecch(C.default_options(method=1, maxlevel=2, max_iterations=20, epsx=0.01, minimum_image_size=16,
+                                     min_rho=0.5))
+    reg.set_reference_image(ref.astype(np.float32))
+    init = np.tile(np.array([1, 0, 0, 0, 1, 0], np.float32), (3, 1))
+    init[2, 2] = 5000.0   # frame 2 starts far outside the reference: nothing overlaps
+    out = reg.align(frames, [3], init_params=init)
+    assert out["status"][0] == C.FRAME_OK
+    assert out["status"][1] in (C.FRAME_NAN, C.FRAME_LOW_RHO)
+    assert out["status"][2] in (C.FRAME_EMPTY_MASK, C.FRAME_LOW_RHO)

@@ -1,0 +1,265 @@
+"""Known-answer tests pinning the FP64 oracle (CPU only).
+
+The reference ships no tests or golden data, so the oracle is pinned to the
+mathematics it restates: motion-model formulas (c_image_transform.cc),
+OpenCV primitive semantics (pyrDown, sepFilter2D, remap), the ECC solvers'
+fixed points on exactly-known warps, and the integer Bayer operations
+(debayer.cc) against independent numpy formulations.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from serstacker_gb300 import synth
+
+MOTIONS = [0, 1, 2, 3, 4, 5, 6]
+
+
+def rand_state(O, rng, t):
+    m = O.model(t)
+    s = O.identity(m)
+    n = O.nparams(m)
+    p = O.get_params(m, s)
+    p = p + rng.normal(0, 1, size=n) * np.array({
+        0: [2, 2], 1: [2, 2, 0.01], 2: [2, 2, 0.01, 0.01], 3: [1e-3, 1e-3, 2, 1e-3, 1e-3, 2],
+        4: [1e-3, 1e-3, 2, 1e-3, 1e-3, 2, 1e-6, 1e-6], 5: [1e-3, 1e-3, 2, 1e-6, 1e-3, 1e-3, 2, 1e-6],
+        6: [1e-3, 1e-3, 2, 1e-6, 1e-6, 1e-6, 1e-3, 1e-3, 2, 1e-6, 1e-6, 1e-6]}[t])
+    return m, O.set_params(m, s, p)
+
+
+@pytest.mark.parametrize("t", MOTIONS)
+def test_sd_images_match_finite_differences(oracle, t):
+    """create_steepest_descent_images == gx dWx/dp + gy dWy/dp (central FD of W)."""
+    O = oracle
+    rng = np.random.default_rng(t)
+    m, s = rand_state(O, rng, t)
+    n = O.nparams(m)
+    p0 = O.get_params(m, s)
+    for (x, y) in [(0.0, 0.0), (37.0, 11.0), (300.0, 200.0)]:
+        gx, gy = 0.7, -1.3
+        J = O.sd(m, s, x, y, gx, gy)
+        for i in range(n):
+            h = 1e-6 * max(1.0, abs(p0[i]))
+            pp, pm = p0.copy(), p0.copy()
+            pp[i] += h
+            pm[i] -= h
+            Xp, Yp = O.warp(m, O.set_params(m, s, pp), x, y)
+            Xm, Ym = O.warp(m, O.set_params(m, s, pm), x, y)
+            fd = gx * (Xp - Xm) / (2 * h) + gy * (Yp - Ym) / (2 * h)
+            if t in (1, 2) and i == 2:   # reference's rotation SD carries the scale factor (c_image_transform.cc:647)
+                pass
+            assert J[i] == pytest.approx(fd, rel=1e-5, abs=1e-6), (t, i, x, y)
+
+
+@pytest.mark.parametrize("t", MOTIONS)
+def test_scale_transform_is_coordinate_scaling(oracle, t):
+    """scale_transfrom(f): W_f(f x) = f W(x)"""
+    O = oracle
+    rng = np.random.default_rng(10 + t)
+    m, s = rand_state(O, rng, t)
+    f = 0.5
+    sf = O.scale(m, s, f)
+    for (x, y) in [(3.0, 4.0), (100.0, 50.0)]:
+        X, Y = O.warp(m, s, x, y)
+        Xf, Yf = O.warp(m, sf, f * x, f * y)
+        assert Xf == pytest.approx(f * X, abs=1e-9)
+        assert Yf == pytest.approx(f * Y, abs=1e-9)
+
+
+@pytest.mark.parametrize("t", [0, 1, 2, 3, 4])
+def test_invert_and_compose(oracle, t):
+    """invert_and_compose(p, dp) (c_image_transform.h:159-167, 309-317, 372-377; .cc:737-833):
+    translation / euclidean compose exactly W(p) o W(dp)^-1; affine / homography use the
+    reference's first-order form inv(inv(M(p)) + M(dp)). dp = 0 returns p."""
+    O = oracle
+    rng = np.random.default_rng(20 + t)
+    m, s = rand_state(O, rng, t)
+    n = O.nparams(m)
+    out = O.invert_and_compose(m, s, np.zeros(n))
+    X0, Y0 = O.warp(m, s, 12.0, 34.0)
+    X1, Y1 = O.warp(m, out, 12.0, 34.0)
+    assert X1 == pytest.approx(X0, abs=1e-7) and Y1 == pytest.approx(Y0, abs=1e-7)
+    dp = rng.normal(0, 1e-3, size=n)
+    if t in (0, 1, 2):
+        dp[:2] *= 1000
+    out = O.invert_and_compose(m, s, dp)
+    if t in (0, 1, 2):
+        mid = O.identity(m)
+        sinc = O.set_params(m, mid, O.get_params(m, mid) + dp if t else dp)
+        for (x, y) in [(5.0, 7.0), (200.0, 150.0)]:
+            xi, yi = O.warp(m, sinc, x, y)
+            Xa, Ya = O.warp(m, out, xi, yi)
+            Xb, Yb = O.warp(m, s, x, y)
+            assert Xa == pytest.approx(Xb, abs=1e-6) and Ya == pytest.approx(Yb, abs=1e-6)
+    else:
+        Mp = synth.homography_from_state(t, s)
+        D = np.zeros((3, 3))
+        D.flat[:n] = dp
+        R = np.linalg.inv(np.linalg.inv(Mp) + D)
+        if t == 4:
+            R = R / R[2, 2]
+        assert np.allclose(R.flat[:n], out[:n], rtol=1e-9, atol=1e-12)
+
+
+def test_euclidean_fixed_scale_eps_quirk(oracle):
+    """eps() of EUCLIDEAN (fixed scale) includes max(W,H)*scale: it never drops below max(W,H)."""
+    O = oracle
+    m = O.model(O.EUCLIDEAN)
+    s = O.identity(m)
+    e = O.eps(m, s, np.zeros(3), 640, 480)
+    assert e == pytest.approx(640.0)
+
+
+def test_gaussian_kernel(oracle):
+    k = oracle.gaussian_kernel(1.0)
+    assert len(k) == 7 and k.sum() == pytest.approx(1.0)
+    assert np.allclose(k, k[::-1])
+    x = np.arange(7) - 3.0
+    ref = np.exp(-x * x / 2)
+    assert np.allclose(k, ref / ref.sum())
+    assert len(oracle.gaussian_kernel(0.2)) == 3
+
+
+def test_pyrdown_semantics(oracle):
+    rng = np.random.default_rng(0)
+    img = rng.random((37, 50))
+    d = oracle.pyrdown(img)
+    assert d.shape == (18, 24)   # ((w+1)>>1)&~1
+    k = np.array([1, 4, 6, 4, 1]) / 16.0
+
+    def refl(p, n):
+        while p < 0 or p >= n:
+            p = -p if p < 0 else 2 * (n - 1) - p
+        return p
+    for (y, x) in [(0, 0), (5, 7), (17, 23)]:
+        v = sum(k[i] * k[j] * img[refl(2 * y + j - 2, 37), refl(2 * x + i - 2, 50)] for i in range(5) for j in range(5))
+        assert d[y, x] == pytest.approx(v, abs=1e-12)
+    assert np.allclose(oracle.pyrdown(np.full((16, 16), 3.5)), 3.5)
+
+
+def test_differentiate_linear_ramp(oracle):
+    y, x = np.mgrid[0:20, 0:30].astype(float)
+    gx, gy = oracle.differentiate(2.0 * x - 3.0 * y + 1.0)
+    assert np.allclose(gx[:, 2:-2], 2.0) and np.allclose(gy[2:-2, :], -3.0)
+    valid = np.ones((20, 30), np.uint8)
+    valid[5, 6] = 0
+    gx, gy = oracle.differentiate(2.0 * x, valid)
+    assert gx[5, 6] == 0 and gy[5, 6] == 0
+
+
+def test_bilinear_and_borders(oracle):
+    img = np.arange(12, dtype=float).reshape(3, 4)
+    lib = oracle.lib()
+    a = img.ctypes.data
+    assert lib.orc_sample_bilinear(a, 4, 3, 1.5, 1.0, oracle.BORDER_REPLICATE, 0) == pytest.approx(5.5)
+    assert lib.orc_sample_bilinear(a, 4, 3, -1.0, 0.0, oracle.BORDER_REPLICATE, 0) == 0.0
+    assert lib.orc_sample_bilinear(a, 4, 3, -1.0, 0.0, oracle.BORDER_REFLECT101, 0) == 1.0
+    assert lib.orc_sample_bilinear(a, 4, 3, 4.0, 0.0, oracle.BORDER_REFLECT101, 0) == 2.0
+    assert lib.orc_sample_bilinear(a, 4, 3, -0.5, 0.0, oracle.BORDER_CONSTANT, 0) == pytest.approx(0.0)
+
+
+def test_erode5(oracle):
+    m = np.full((12, 12), 255, np.uint8)
+    m[6, 6] = 0
+    e = oracle.erode5(m)
+    assert (e[4:9, 4:9] == 0).all() and e[3, 6] == 255 and e[0, 0] == 255
+
+
+@pytest.mark.parametrize("method", [0, 1, 2, 3])
+def test_align_recovers_known_translation(oracle, method):
+    """Every ECC method recovers an exactly-rendered sub-pixel shift."""
+    O = oracle
+    sc = synth.Scene(160, 120, 45.0, edge_sigma=2.0)
+    ref = synth.reference_np(sc)
+    H = np.array([[1, 0, 2.3], [0, 1, -1.7], [0, 0, 1.0]])
+    cur = synth.render_frame_np(sc, H)
+    m = O.model(O.AFFINE)
+    ok, s, it, e = O.ecc_align(m, O.identity(m), ref, cur, method=method, max_iterations=60, max_eps=1e-3)
+    assert ok
+    assert s[2] == pytest.approx(2.3, abs=0.01) and s[5] == pytest.approx(-1.7, abs=0.01)
+
+
+def test_identity_warp_first_update_is_zero(oracle):
+    O = oracle
+    sc = synth.Scene(96, 80, 30.0)
+    ref = synth.reference_np(sc)
+    m = O.model(O.AFFINE)
+    ok, s, it, e = O.ecc_align(m, O.identity(m), ref, ref.copy(), method=O.IC, max_iterations=1, max_eps=1e-9)
+    assert np.allclose(s[:6], O.identity(m)[:6], atol=1e-9)
+
+
+def test_ecch_pyramid_homography(oracle):
+    O = oracle
+    sc = synth.Scene(256, 192, 70.0)
+    ref = synth.reference_np(sc)
+    Hs = np.array([[1.002, 0.004, 5.2], [-0.003, 0.998, -3.1], [1e-6, -2e-6, 1.0]])
+    cur = synth.render_frame_np(sc, Hs)
+    o = O.ecch_opts(method=O.IC, maxlevel=3, epsx=1e-3)
+    m = O.model(O.HOMOGRAPHY)
+    s, it, e = O.ecch_align(m, O.identity(m), ref, cur, o)
+    mx, my = O.warp_grid(m, s, 256, 192)
+    y, x = np.mgrid[0:192, 0:256].astype(float)
+    w = Hs[2, 0] * x + Hs[2, 1] * y + 1
+    tx = (Hs[0, 0] * x + Hs[0, 1] * y + Hs[0, 2]) / w
+    ty = (Hs[1, 0] * x + Hs[1, 1] * y + Hs[1, 2]) / w
+    rms = math.sqrt(np.mean((mx - tx) ** 2 + (my - ty) ** 2))
+    assert rms < 0.05   # bilinear-interpolation bias of ECC on a 2 px edge; not a parity bound
+
+
+def test_correlation_of_identical_images(oracle):
+    O = oracle
+    sc = synth.Scene(96, 80, 30.0)
+    ref = synth.reference_np(sc)
+    m = O.model(O.AFFINE)
+    assert O.correlation(m, O.identity(m), ref, ref) == pytest.approx(1.0, abs=1e-12)
+
+
+def test_extract_bayer_planes_matches_slicing(oracle):
+    rng = np.random.default_rng(3)
+    raw = rng.integers(0, 4096, size=(20, 30), dtype=np.uint16)
+    planes = oracle.extract_bayer_planes(raw)
+    assert np.array_equal(planes[..., 0], raw[0::2, 0::2])
+    assert np.array_equal(planes[..., 1], raw[0::2, 1::2])
+    assert np.array_equal(planes[..., 2], raw[1::2, 0::2])
+    assert np.array_equal(planes[..., 3], raw[1::2, 1::2])
+    avg = oracle.average_bayer_planes(raw)
+    s = raw[0::2, 0::2].astype(int) + raw[0::2, 1::2] + raw[1::2, 0::2] + raw[1::2, 1::2]
+    assert np.array_equal(avg, ((2 + s) // 4).astype(np.uint16))
+
+
+def test_bayer_pattern_mask(oracle):
+    m = oracle.bayer_pattern_mask(8, 4, 4)   # RGGB: R=2, G=1, B=0
+    assert m[0, 0] == 2 and m[0, 1] == 1 and m[1, 0] == 1 and m[1, 1] == 0
+
+
+def test_running_mean_equals_weighted_sum(oracle):
+    """The reference's running mean A += (I - A) w / W equals sum(w I) / sum(w)."""
+    rng = np.random.default_rng(4)
+    h, w, n = 8, 9, 50
+    acc32 = np.zeros((h, w), np.float32)
+    accw32 = np.zeros((h, w), np.float32)
+    acc = np.zeros((h, w))
+    accw = np.zeros((h, w))
+    lib = oracle.lib()
+    for _ in range(n):
+        img = rng.random((h, w)).astype(np.float32)
+        wt = (rng.random((h, w)) * (rng.random((h, w)) > 0.2)).astype(np.float32)
+        lib.orc_running_mean_add_f32(acc32.ctypes.data, accw32.ctypes.data, w, h, img.ctypes.data, wt.ctypes.data)
+        img64, wt64 = img.astype(float), wt.astype(float)
+        oracle.lib().orc_weighted_average_add(acc.ctypes.data, accw.ctypes.data, w, h, img64.ctypes.data,
+                                              wt64.ctypes.data)
+    ok = accw > 0
+    assert np.allclose(acc32[ok], (acc / np.where(ok, accw, 1))[ok], rtol=1e-5)
+
+
+def test_stack_remap_mask_is_eroded(oracle):
+    O = oracle
+    img = np.ones((40, 50))
+    m = O.model(O.TRANSLATION)
+    s = O.identity(m)
+    s[0], s[1] = 3.25, 0.0
+    dst, msk = O.stack_remap(m, s, img, 50, 40)
+    # both taps inside needs x + 4 <= 49 -> x <= 45; the 5x5 erosion removes 2 more columns
+    assert msk[20, 43] == 255 and msk[20, 44] == 0
+    assert msk[20, 0] == 255
