@@ -226,6 +226,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=6, help="frames per CPU baseline sample")
     ap.add_argument("--plain-frames", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form leg (profiling runs)")
     args = ap.parse_args()
 
     ws, rank, local = dist_env()
@@ -315,6 +317,47 @@ def main():
     med_rms, max_rms = warp_rms_vs_truth(res["params"][:, :8].astype(np.float64), Hs, res["status"])
 
     # ---------------------------------------------------------------- e2e
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, ws, n, frames, reg, acc, passes, frame_bytes)
+    plain_fps = run_plain(args, n, frames, ref, opts, passes) if not args.no_plain else None
+    pn = min(args.plain_frames, n)
+    sub = frames[:pn].cpu().numpy().view(np.uint16)
+
+    # ---------------------------------------------------------- CPU baseline
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle as O
+        O.build()
+        threads = os.cpu_count() or 1
+        rate, dt = cpu_reference_rate(sub, ref, min(args.ref_sample, pn), threads)
+        cpu = {"value": rate, "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": f"{min(args.ref_sample, pn)} frames of the workload (oracle FP64 pipeline, OpenMP, "
+                         f"{dt:.1f} s)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {**workload_cfg(n), "parallelism": f"replicas x{ws}"},
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+                "clocks": clk, "gpu_launches": launches,
+                "plain": None if plain_fps is None else {
+                    "value": plain_fps, "unit": "frames/s", "frames": pn,
+                    "form": "one frame per call, one launch per Gauss-Newton step, host sync per step"},
+                "batched_over_plain": None if plain_fps is None else value / ws / plain_fps,
+                "accuracy": {"warp_rms_vs_truth_px_median": med_rms, "warp_rms_vs_truth_px_max": max_rms,
+                             "frames_ok": int((res["status"] == 0).sum())},
+                "levels": level_table}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_e2e(args, ws, n, frames, reg, acc, passes, frame_bytes):
+    import torch
+    from serstacker_gb300 import capi as C
     host_frames = torch.empty((n, HEIGHT, WIDTH), dtype=torch.int16, pin_memory=True)
     host_frames.copy_(frames)
     torch.cuda.synchronize()
@@ -344,11 +387,15 @@ def main():
     barrier(ws)
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000.0 / args.steps, ws)
     d2h = n * (12 * 4 + 3 * 4) + WIDTH * HEIGHT * 5
-    e2e = {"value": ws * n / (e2e_ms / 1000.0), "unit": "frames/s", "h2d_bytes_per_step": n * frame_bytes,
-           "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "api": "sst_stack_frames (host pinned) + "
-                                                                      "sst_weighted_average_compute"}
+    return {"value": ws * n / (e2e_ms / 1000.0), "unit": "frames/s", "h2d_bytes_per_step": n * frame_bytes,
+            "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+            "api": "sst_stack_frames (host pinned) + sst_weighted_average_compute"}
 
-    # ---------------------------------------------------------- plain form
+
+def run_plain(args, n, frames, ref, opts, passes):
+    """The plain one-frame-per-launch form on a subset of the sequence: frames/s."""
+    import torch
+    from serstacker_gb300 import capi as C
     pn = min(args.plain_frames, n)
     sub = frames[:pn].cpu().numpy().view(np.uint16)
     reg_p = C.c_ecch(opts)
@@ -362,36 +409,7 @@ def main():
         acc_p.add_warped(sub[i:i + 1], C.HOMOGRAPHY, o["params"], status=o["status"], weights=o["weight"],
                          scale=SCALE)
     torch.cuda.synchronize()
-    plain_fps = pn / (time.perf_counter() - t0)
-
-    # ---------------------------------------------------------- CPU baseline
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        import oracle as O
-        O.build()
-        threads = os.cpu_count() or 1
-        rate, dt = cpu_reference_rate(sub, ref, min(args.ref_sample, pn), threads)
-        cpu = {"value": rate, "unit": "frames/s", "cores": threads, "kind": "port",
-               "sample": f"{min(args.ref_sample, pn)} frames of the workload (oracle FP64 pipeline, OpenMP, "
-                         f"{dt:.1f} s)"}
-
-    if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {**workload_cfg(n), "parallelism": f"replicas x{ws}"},
-                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-                "clocks": clk, "gpu_launches": launches,
-                "plain": {"value": plain_fps, "unit": "frames/s", "frames": pn,
-                          "form": "one frame per call, one launch per Gauss-Newton step, host sync per step"},
-                "batched_over_plain": value / ws / plain_fps,
-                "accuracy": {"warp_rms_vs_truth_px_median": med_rms, "warp_rms_vs_truth_px_max": max_rms,
-                             "frames_ok": int((res["status"] == 0).sum())},
-                "levels": level_table}
-        print(json.dumps(line), flush=True)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    return pn / (time.perf_counter() - t0)
 
 
 if __name__ == "__main__":

@@ -930,7 +930,7 @@ extern "C" int sst_weighted_average_add(sst_weighted_average * a, const void * s
 
 static int add_warped_device(sst_weighted_average * a, const void * d_frames, int depth, int n, int sw, int sh,
     size_t row_stride, size_t frame_stride, double scale, const sst_motion_model & m, const float * d_params,
-    const int32_t * d_status, const float * d_weights, cudaStream_t st)
+    const int32_t * d_status, const float * d_weights, int border, cudaStream_t st)
 {
   SST_CK(a->coeffs.ensure((size_t) n * SST_NCOEF * sizeof(float)));
   SST_CK(a->weff.ensure((size_t) n * sizeof(float)));
@@ -946,6 +946,7 @@ static int add_warped_device(sst_weighted_average * a, const void * d_frames, in
   s.dw = a->w, s.dh = a->h;
   s.acc = a->acc.as<float>();
   s.plane = a->plane();
+  s.border = border;
   SST_CK_LAUNCH(launch_stack_add_warped(s, m.type, depth, st));
   return SST_OK;
 }
@@ -961,7 +962,9 @@ extern "C" int sst_weighted_average_add_warped_batch(sst_weighted_average * a, c
   if( row_stride < (size_t) src_width * depth_bytes(depth) || frame_stride < row_stride * src_height )
     return set_error(SST_ERR_INVALID_ARG, "invalid strides");
   if( model->type < 0 || model->type > 7 ) return set_error(SST_ERR_INVALID_ARG, "invalid motion type");
-  (void) border;  // only pixels whose 5x5-eroded mask is set are accumulated: the image border mode never contributes
+  if( border != SST_BORDER_CONSTANT && border != SST_BORDER_REPLICATE && border != SST_BORDER_REFLECT &&
+      border != SST_BORDER_REFLECT101 )
+    return set_error(SST_ERR_UNSUPPORTED, "unsupported border mode %d", border);
   cudaStream_t st = (cudaStream_t) stream;
   const void * dframes = frames;
   const float * dparams = params;
@@ -987,7 +990,7 @@ extern "C" int sst_weighted_average_add_warped_batch(sst_weighted_average * a, c
     }
   }
   const int r = add_warped_device(a, dframes, depth, n, src_width, src_height, row_stride, frame_stride, scale, *model,
-      dparams, dstatus, dweights, st);
+      dparams, dstatus, dweights, border, st);
   if( !on_device ) {
     cudaStreamSynchronize(st);
     tf.release(), tp.release(), ts.release(), tw.release();
@@ -1083,8 +1086,10 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
     int num_passes, const sst_motion_model * passes, int border, int weighting,
     float * params_out, int32_t * status_out, float * rho_out, float * weight_out, void * stream)
 {
-  (void) border;
   if( !h || !acc || !frames ) return set_error(SST_ERR_INVALID_ARG, "sst_stack_frames: NULL argument");
+  if( border != SST_BORDER_CONSTANT && border != SST_BORDER_REPLICATE && border != SST_BORDER_REFLECT &&
+      border != SST_BORDER_REFLECT101 )
+    return set_error(SST_ERR_UNSUPPORTED, "unsupported border mode %d", border);
   if( h->L == 0 ) return set_error(SST_ERR_STATE, "c_ecch: no reference image was set");
   if( n < 1 ) return set_error(SST_ERR_INVALID_ARG, "n must be >= 1");
   if( width != h->w || height != h->h || acc->w != h->w || acc->h != h->h )
@@ -1128,7 +1133,8 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
     }
     SST_TRY(register_device(h, d_frames, depth, nc, row_stride, frame_stride, scale, num_passes, passes, nullptr, false));
     SST_TRY(add_warped_device(acc, d_frames, depth, nc, width, height, row_stride, frame_stride, scale, last,
-        h->out_params.as<float>(), h->out_status.as<int32_t>(), weighting ? h->out_weight.as<float>() : nullptr, st));
+        h->out_params.as<float>(), h->out_status.as<int32_t>(), weighting ? h->out_weight.as<float>() : nullptr,
+        border, st));
     if( !on_device ) SST_CK(cudaEventRecord(h->ev_free[buf], st));
     SST_TRY(copy_out(h->res_params.as<float>() + (size_t) f0 * 12, h->out_params.p, (size_t) nc * 12 * sizeof(float), 1, st));
     SST_TRY(copy_out(h->res_status.as<int32_t>() + f0, h->out_status.p, (size_t) nc * sizeof(int32_t), 1, st));

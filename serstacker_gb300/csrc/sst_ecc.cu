@@ -98,20 +98,23 @@ __device__ void combine_partials(const double * P, int tiles, double * tmp, doub
   __syncthreads();
 }
 
+/* Tile reduction: FP32 warp shuffles (32 lanes x a few pixels each), then
+ * the 8 warp sums added in FP64 in a fixed order (GB300's FP64 rate is a
+ * small fraction of FP32: keep it off the per-thread path). */
 template<int NS>
-__device__ __forceinline__ void block_reduce_d(const float (&acc)[NS], double * scratch, double * out)
+__device__ __forceinline__ void block_reduce_d(const float (&acc)[NS], float * scratch, double * out)
 {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for( int k = 0; k < NS; ++k ) {
-    const double s = warp_sum((double) acc[k]);
+    const float s = warp_sum(acc[k]);
     if( lane == 0 ) scratch[wid * NS + k] = s;
   }
   __syncthreads();
   for( int k = threadIdx.x; k < NS; k += 256 ) {
     double t = 0;
 #pragma unroll
-    for( int wv = 0; wv < 8; ++wv ) t += scratch[wv * NS + k];
+    for( int wv = 0; wv < 8; ++wv ) t += (double) scratch[wv * NS + k];
     out[k] = t;
   }
   __syncthreads();
@@ -124,8 +127,10 @@ template<int NS>
 __device__ bool finish_tile(const PassArgs & a, int f, int t, double * tile_sums, double * tmp, double * sums, int * s_flag)
 {
   double * P = a.partials + (size_t) f * a.part_stride;
-  if( threadIdx.x < NS ) P[(size_t) t * NS + threadIdx.x] = tile_sums[threadIdx.x];
-  __threadfence();
+  if( threadIdx.x < NS ) {
+    P[(size_t) t * NS + threadIdx.x] = tile_sums[threadIdx.x];
+    __threadfence();
+  }
   __syncthreads();
   if( threadIdx.x == 0 ) {
     const unsigned prev = atomicAdd(a.counters + f, 1u);
@@ -425,7 +430,7 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
 {
   constexpr int NS = M + 2;
   constexpr int GMAX = (256 / NS) > 0 ? (256 / NS) : 1;
-  __shared__ double s_red[8 * NS];
+  __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
   __shared__ double s_tmp[NS * GMAX];
   __shared__ double s_sum[NS];
@@ -450,7 +455,7 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
 #pragma unroll
     for( int k = 0; k < NS; ++k ) acc[k] = 0.f;
     if( x < a.w ) {
-#pragma unroll 2
+#pragma unroll
       for( int k = 0; k < PW_TY / 2; ++k ) {
         const int y = ty0 + (threadIdx.x >> 7) + 2 * k;
         if( y < a.h ) {
@@ -504,7 +509,7 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
   constexpr int NS = (METHOD == M_FA) ? nH + 3 * M + 5 : nH + M + 2;
   constexpr int GMAX = (256 / NS) > 0 ? (256 / NS) : 1;
   constexpr int SW = ST_TX + 4, SH = ST_TY + 4;
-  __shared__ double s_red[8 * NS];
+  __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
   __shared__ double s_tmp[NS * GMAX > 256 ? NS * GMAX : 256];
   __shared__ double s_sum[NS];
@@ -768,7 +773,7 @@ template<int FAM>
 __global__ void __launch_bounds__(256) k_correlation(CorrArgs a)
 {
   constexpr int NS = 6;
-  __shared__ double s_red[8 * NS];
+  __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
   __shared__ double s_tmp[256];
   __shared__ double s_sum[NS];

@@ -62,6 +62,19 @@ cudaError_t launch_effective_weights(const float * weights, const int32_t * stat
   return cudaGetLastError();
 }
 
+/* one bilinear tap with the remap border mode (cv::remap, per-tap borderInterpolate) */
+template<typename T>
+__device__ __forceinline__ float tap(const uint8_t * fb, size_t rs, int sw, int sh, int xi, int yi, int border)
+{
+  if( xi >= 0 && xi < sw && yi >= 0 && yi < sh ) return ldpx<T>(fb, rs, xi, yi);
+  switch ( border ) {
+  case SST_BORDER_REPLICATE: return ldpx<T>(fb, rs, clampi(xi, 0, sw - 1), clampi(yi, 0, sh - 1));
+  case SST_BORDER_REFLECT101: return ldpx<T>(fb, rs, reflect101(xi, sw), reflect101(yi, sh));
+  case SST_BORDER_REFLECT: return ldpx<T>(fb, rs, reflect(xi, sw), reflect(yi, sh));
+  default: return 0.f;
+  }
+}
+
 constexpr int SK_TX = 32, SK_TY = 8;
 
 template<int FAM, typename T>
@@ -104,12 +117,13 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
       const uint8_t * p = s_h + ly * SK_TX + lx;
       if( p[0] & p[SK_TX] & p[2 * SK_TX] & p[3 * SK_TX] & p[4 * SK_TX] ) {
         const spos s = warp_pos<FAM>(c, x, y);
-        // valid => every tap with a non-zero weight is inside; clamp the rest
-        const int xa = clampi(s.x0, 0, a.sw - 1), xb = clampi(s.x0 + 1, 0, a.sw - 1);
-        const int ya = clampi(s.y0, 0, a.sh - 1), yb = clampi(s.y0 + 1, 0, a.sh - 1);
+        // the >= 255 test admits footprints with < 0.2 % of the weight outside the
+        // frame: those taps take the image border mode (base_remap's cv::remap)
         const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
-        const float v00 = ldpx<T>(fb, a.row_stride, xa, ya), v01 = ldpx<T>(fb, a.row_stride, xb, ya);
-        const float v10 = ldpx<T>(fb, a.row_stride, xa, yb), v11 = ldpx<T>(fb, a.row_stride, xb, yb);
+        const float v00 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
+        const float v01 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
+        const float v10 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
+        const float v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
         const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
         const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
         kahan_add(S, cS, wf * val);
@@ -227,18 +241,6 @@ cudaError_t launch_stack_reinit(float * acc, size_t plane, int n, const float * 
 }
 
 /* ------------------------------------------------------------- remap */
-
-template<typename T>
-__device__ __forceinline__ float tap(const uint8_t * fb, size_t rs, int sw, int sh, int xi, int yi, int border)
-{
-  if( xi >= 0 && xi < sw && yi >= 0 && yi < sh ) return ldpx<T>(fb, rs, xi, yi);
-  switch ( border ) {
-  case SST_BORDER_REPLICATE: return ldpx<T>(fb, rs, clampi(xi, 0, sw - 1), clampi(yi, 0, sh - 1));
-  case SST_BORDER_REFLECT101: return ldpx<T>(fb, rs, reflect101(xi, sw), reflect101(yi, sh));
-  case SST_BORDER_REFLECT: return ldpx<T>(fb, rs, reflect(xi, sw), reflect(yi, sh));
-  default: return 0.f;
-  }
-}
 
 template<int FAM, typename T>
 __global__ void __launch_bounds__(256) k_remap(const uint8_t * src, int sw, int sh, size_t rs, float scale,

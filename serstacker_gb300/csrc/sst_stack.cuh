@@ -19,6 +19,7 @@ struct StackArgs {
   int dw, dh;               // accumulator size
   float * acc;              // 4 planes: S, cS, W, cW
   size_t plane;             // floats per plane
+  int border;               // image border mode of the remap (SST_BORDER_*)
 };
 
 cudaError_t launch_coeffs_from_params(const sst_motion_model & m, const float * params, int n, float * coeffs, cudaStream_t st);
