@@ -533,6 +533,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
   const int L = h->L;
   const int max_it = h->o.max_iterations;
   const int grid = std::max(1, h->num_sms) * 4;
+  const int solve_grid = std::max(1, std::min(n, std::max(1, h->num_sms) * 4));
   long long k = 0;
   SST_CK(cudaMemsetAsync(h->counts.p, 0, (size_t) h->steps_cap * sizeof(int), st));
   int step = 0;
@@ -593,8 +594,9 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
         a.count_in = counts + step + it;
         a.list_out = lists + (size_t) (step + it + 1) * h->cap;
         a.count_out = counts + step + it + 1;
-        SST_CK_LAUNCH(launch_pass(method, a, grid, st));
-        ++k;
+        SST_CK_LAUNCH(launch_pass(method, a, -1, st));
+        SST_CK_LAUNCH(launch_solve(method, a, solve_grid, st));
+        k += 2;
         if( host_driven ) {
           int c = 0;
           SST_CK(cudaMemcpyAsync(&c, counts + step + it + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -622,7 +624,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
   c.model = passes[num_passes - 1];
   c.min_rho = h->o.min_rho;
   SST_CK_LAUNCH(launch_correlation(c, grid, st));
-  ++k;
+  k += 2;
   if( kernels ) *kernels = k;
   return SST_OK;
 }

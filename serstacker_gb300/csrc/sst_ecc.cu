@@ -78,10 +78,9 @@ __device__ __forceinline__ void sd_pixel(const float * jc, float x, float y, flo
 
 /* Deterministic combine of a frame's tile partials: thread group g sums tiles
  * g, g+G, ... of sum k; the G group results are added in order. */
-template<int NS>
-__device__ void combine_partials(const double * P, int tiles, double * tmp, double * out)
+__device__ void combine_partials(const double * P, int tiles, int NS, double * tmp, double * out)
 {
-  constexpr int G = (256 / NS) > 0 ? (256 / NS) : 1;
+  const int G = (256 / NS) > 0 ? (256 / NS) : 1;
   const int tid = threadIdx.x;
   if( tid < NS * G ) {
     const int k = tid % NS, g = tid / NS;
@@ -120,29 +119,12 @@ __device__ __forceinline__ void block_reduce_d(const float (&acc)[NS], float * s
   __syncthreads();
 }
 
-/* Write the tile partials and take a ticket; returns (in smem flag) whether
- * this CTA is the frame's last one, in which case `sums` holds the frame
- * totals on return. */
+/* Store one tile's sums; the frame's solve kernel combines them after the
+ * launch (the kernel boundary orders the stores before the loads). */
 template<int NS>
-__device__ bool finish_tile(const PassArgs & a, int f, int t, double * tile_sums, double * tmp, double * sums, int * s_flag)
+__device__ __forceinline__ void write_tile(const PassArgs & a, int f, int t, const double * tile_sums)
 {
-  double * P = a.partials + (size_t) f * a.part_stride;
-  if( threadIdx.x < NS ) {
-    P[(size_t) t * NS + threadIdx.x] = tile_sums[threadIdx.x];
-    __threadfence();
-  }
-  __syncthreads();
-  if( threadIdx.x == 0 ) {
-    const unsigned prev = atomicAdd(a.counters + f, 1u);
-    *s_flag = (prev == (unsigned) (a.tiles - 1));
-  }
-  __syncthreads();
-  const bool last = *s_flag != 0;
-  if( last ) {
-    __threadfence();
-    combine_partials<NS>(P, a.tiles, tmp, sums);
-  }
-  return last;
+  if( threadIdx.x < NS ) a.partials[(size_t) f * a.part_stride + (size_t) t * NS + threadIdx.x] = tile_sums[threadIdx.x];
 }
 
 /* ------------------------------------------------------ per-frame control */
@@ -429,20 +411,16 @@ template<int METHOD, int FAM, int JK, int M>
 __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
 {
   constexpr int NS = M + 2;
-  constexpr int GMAX = (256 / NS) > 0 ? (256 / NS) : 1;
   __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
-  __shared__ double s_tmp[NS * GMAX];
-  __shared__ double s_sum[NS];
   __shared__ float s_c[16];
-  __shared__ int s_flag;
 
   const int nitems = __ldcg(a.count_in) * a.tiles;
   for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
     const int fi = item / a.tiles;
     const int t = item - fi * a.tiles;
     const int f = __ldcg(a.list_in + fi);
-    FrameState * F = a.fs + f;
+    const FrameState * F = a.fs + f;
     if( threadIdx.x < 16 ) s_c[threadIdx.x] = F->wc[threadIdx.x];
     __syncthreads();
     float c[16];
@@ -451,49 +429,40 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
     const float * img = a.pyr + (size_t) f * a.pyr_stride + a.lvl_off;
     const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
+    const int yend = min(ty0 + PW_TY, a.h);
     float acc[NS];
 #pragma unroll
     for( int k = 0; k < NS; ++k ) acc[k] = 0.f;
     if( x < a.w ) {
-#pragma unroll
-      for( int k = 0; k < PW_TY / 2; ++k ) {
-        const int y = ty0 + (threadIdx.x >> 7) + 2 * k;
-        if( y < a.h ) {
-          const float fx = (float) x, fy = (float) y;
-          const spos s = warp_pos<FAM>(c, x, y);
-          const size_t i = (size_t) y * a.w + x;
-          bool ok;
-          if( METHOD == M_IC ) {
-            ok = mask_ok(coverage(a.w, a.h, s), 250);
-          }
-          else {
-            int rx, ry;
-            warp_nearest<FAM>(c, x, y, rx, ry);
-            ok = rx >= 0 && rx < a.w && ry >= 0 && ry < a.h;
-            if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
-          }
-          const float T = __ldg(a.refT + i);
-          const float2 g = __ldg(a.refG + i);
-          const float v = sample_replicate(img, a.w, a.h, s);
-          const float r = ok ? v - T : 0.f;
-          acc[M] = fmaf(r, r, acc[M]);
-          acc[M + 1] += ok ? 1.f : 0.f;
-          float J[M];
-          sd_pixel<JK, M>(a.jc_id, fx, fy, g.x, g.y, J);
-#pragma unroll
-          for( int j = 0; j < M; ++j ) acc[j] = fmaf(J[j], r, acc[j]);
+#pragma unroll 4
+      for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
+        const float fx = (float) x, fy = (float) y;
+        const spos s = warp_pos<FAM>(c, x, y);
+        const size_t i = (size_t) y * a.w + x;
+        bool ok;
+        if( METHOD == M_IC ) {
+          ok = mask_ok(coverage(a.w, a.h, s), 250);
         }
+        else {
+          int rx, ry;
+          warp_nearest<FAM>(c, x, y, rx, ry);
+          ok = rx >= 0 && rx < a.w && ry >= 0 && ry < a.h;
+          if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
+        }
+        const float T = __ldg(a.refT + i);
+        const float2 g = __ldg(a.refG + i);
+        const float v = sample_replicate(img, a.w, a.h, s);
+        const float r = ok ? v - T : 0.f;
+        acc[M] = fmaf(r, r, acc[M]);
+        acc[M + 1] += ok ? 1.f : 0.f;
+        float J[M];
+        sd_pixel<JK, M>(a.jc_id, fx, fy, g.x, g.y, J);
+#pragma unroll
+        for( int j = 0; j < M; ++j ) acc[j] = fmaf(J[j], r, acc[j]);
       }
     }
     block_reduce_d<NS>(acc, s_red, s_tile);
-    if( finish_tile<NS>(a, f, t, s_tile, s_tmp, s_sum, &s_flag) ) {
-      if( threadIdx.x == 0 ) {
-        a.counters[f] = 0;
-        if( METHOD == M_IC ) solve_ic(F, s_sum, a, f);
-        else solve_iclm(F, s_sum, a, f);
-      }
-    }
-    __syncthreads();
+    write_tile<NS>(a, f, t, s_tile);
   }
 }
 
@@ -523,7 +492,7 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
     const int fi = item / a.tiles;
     const int t = item - fi * a.tiles;
     const int f = __ldcg(a.list_in + fi);
-    FrameState * F = a.fs + f;
+    const FrameState * F = a.fs + f;
     if( threadIdx.x < 16 ) s_c[threadIdx.x] = F->wc[threadIdx.x];
     if( threadIdx.x < 8 ) s_j[threadIdx.x] = F->jc[threadIdx.x];
     __syncthreads();
@@ -616,20 +585,13 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
       }
     }
     block_reduce_d<NS>(acc, s_red, s_tile);
-    if( finish_tile<NS>(a, f, t, s_tile, s_tmp, s_sum, &s_flag) ) {
-      if( threadIdx.x == 0 ) {
-        a.counters[f] = 0;
-        if( METHOD == M_FA ) solve_fa(F, s_sum, a, f);
-        else solve_lm(F, s_sum, a, f);
-      }
-    }
-    __syncthreads();
+    write_tile<NS>(a, f, t, s_tile);
   }
 }
 
 /* ------------------------------------------------------------- dispatch */
 
-int pass_num_sums(int method, int M)
+__host__ __device__ int pass_num_sums(int method, int M)
 {
   const int nH = M * (M + 1) / 2;
   switch ( method ) {
@@ -639,11 +601,69 @@ int pass_num_sums(int method, int M)
   }
 }
 
+/* The per-frame Gauss-Newton logic of one step: one CTA per active frame
+ * combines the frame's tile partials in a fixed order and thread 0 runs the
+ * reference's per-iteration update in FP64. */
+__global__ void __launch_bounds__(256) k_solve(PassArgs a, int method)
+{
+  __shared__ double s_tmp[256];
+  __shared__ double s_sum[160];
+  const int NS = pass_num_sums(method, a.M);
+  const int count = __ldcg(a.count_in);
+  for( int fi = blockIdx.x; fi < count; fi += gridDim.x ) {
+    const int f = __ldcg(a.list_in + fi);
+    combine_partials(a.partials + (size_t) f * a.part_stride, a.tiles, NS, s_tmp, s_sum);
+    if( threadIdx.x == 0 ) {
+      FrameState * F = a.fs + f;
+      switch ( method ) {
+      case M_IC: solve_ic(F, s_sum, a, f); break;
+      case M_ICLM: solve_iclm(F, s_sum, a, f); break;
+      case M_FA: solve_fa(F, s_sum, a, f); break;
+      default: solve_lm(F, s_sum, a, f); break;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_solve(int method, const PassArgs & a, int grid, cudaStream_t st)
+{
+  k_solve<<<grid, 256, 0, st>>>(a, method);
+  return cudaGetLastError();
+}
+
+/* persistent grid: every SM filled to the kernel's occupancy */
+template<typename K>
+static int persistent_grid(K kernel)
+{
+  static int sms = 0;
+  if( !sms ) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if( sms <= 0 ) sms = 1;
+  }
+  int per_sm = 0;
+  if( cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1 ) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return sms * per_sm;
+}
+
 template<int METHOD, int FAM, int JK, int M>
 static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st)
 {
-  if( METHOD == M_IC || METHOD == M_ICLM ) k_pass_pointwise<METHOD, FAM, JK, M><<<grid, 256, 0, st>>>(a);
-  else k_pass_stencil<METHOD, FAM, JK, M><<<grid, 256, 0, st>>>(a);
+  if constexpr( METHOD == M_IC || METHOD == M_ICLM ) {
+    static int g = 0;
+    if( !g ) g = persistent_grid(k_pass_pointwise<METHOD, FAM, JK, M>);
+    k_pass_pointwise<METHOD, FAM, JK, M><<<grid > 0 ? grid : g, 256, 0, st>>>(a);
+  }
+  else {
+    static int g = 0;
+    if( !g ) g = persistent_grid(k_pass_stencil<METHOD, FAM, JK, M>);
+    k_pass_stencil<METHOD, FAM, JK, M><<<grid > 0 ? grid : g, 256, 0, st>>>(a);
+  }
   return cudaGetLastError();
 }
 
@@ -775,15 +795,12 @@ __global__ void __launch_bounds__(256) k_correlation(CorrArgs a)
   constexpr int NS = 6;
   __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
-  __shared__ double s_tmp[256];
-  __shared__ double s_sum[NS];
   __shared__ float s_c[16];
-  __shared__ int s_flag;
   const int nitems = a.n * a.tiles;
   for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
     const int f = item / a.tiles;
     const int t = item - f * a.tiles;
-    FrameState * F = a.fs + f;
+    const FrameState * F = a.fs + f;
     if( F->status != SST_FRAME_OK ) continue;   // uniform per CTA: no barrier skipped unevenly
     if( threadIdx.x < 16 ) s_c[threadIdx.x] = F->wc[threadIdx.x];
     __syncthreads();
@@ -793,50 +810,51 @@ __global__ void __launch_bounds__(256) k_correlation(CorrArgs a)
     const float * img = a.pyr + (size_t) f * a.pyr_stride;
     const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
+    const int yend = min(ty0 + PW_TY, a.h);
     float acc[NS] = { 0, 0, 0, 0, 0, 0 };
     if( x < a.w ) {
-      for( int k = 0; k < PW_TY / 2; ++k ) {
-        const int y = ty0 + (threadIdx.x >> 7) + 2 * k;
-        if( y < a.h ) {
-          const spos s = warp_pos<FAM>(c, x, y);
-          const size_t i = (size_t) y * a.w + x;
-          bool ok = mask_ok(coverage(a.w, a.h, s), 254);
-          if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
-          if( ok ) {
-            const float av = __ldg(a.refT + i) - a.tshift;
-            const float bv = sample_constant0(img, a.w, a.h, s) - a.tshift;
-            acc[0] += av, acc[1] += bv;
-            acc[2] = fmaf(av, av, acc[2]);
-            acc[3] = fmaf(bv, bv, acc[3]);
-            acc[4] = fmaf(av, bv, acc[4]);
-            acc[5] += 1.f;
-          }
+#pragma unroll 4
+      for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
+        const spos s = warp_pos<FAM>(c, x, y);
+        const size_t i = (size_t) y * a.w + x;
+        bool ok = mask_ok(coverage(a.w, a.h, s), 254);
+        if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
+        if( ok ) {
+          const float av = __ldg(a.refT + i) - a.tshift;
+          const float bv = sample_constant0(img, a.w, a.h, s) - a.tshift;
+          acc[0] += av, acc[1] += bv;
+          acc[2] = fmaf(av, av, acc[2]);
+          acc[3] = fmaf(bv, bv, acc[3]);
+          acc[4] = fmaf(av, bv, acc[4]);
+          acc[5] += 1.f;
         }
       }
     }
     block_reduce_d<NS>(acc, s_red, s_tile);
-    double * P = a.partials + (size_t) f * a.part_stride;
-    if( threadIdx.x < NS ) P[(size_t) t * NS + threadIdx.x] = s_tile[threadIdx.x];
-    __threadfence();
-    __syncthreads();
-    if( threadIdx.x == 0 ) s_flag = (atomicAdd(a.counters + f, 1u) == (unsigned) (a.tiles - 1));
-    __syncthreads();
-    if( s_flag ) {
-      __threadfence();
-      combine_partials<NS>(P, a.tiles, s_tmp, s_sum);
-      if( threadIdx.x == 0 ) {
-        a.counters[f] = 0;
-        const double n = s_sum[5];
-        double rho = 0;
-        if( n > 0 ) {
-          const double ma = s_sum[0] / n, mb = s_sum[1] / n;
-          const double va = s_sum[2] / n - ma * ma, vb = s_sum[3] / n - mb * mb;
-          const double cv = s_sum[4] / n - ma * mb;
-          rho = cv / (sqrt(fmax(va, 0.0)) * sqrt(fmax(vb, 0.0)));
-        }
-        F->rho = (float) rho;
-        if( a.min_rho > 0 && !(rho >= a.min_rho) ) F->status = SST_FRAME_LOW_RHO;
+    if( threadIdx.x < NS ) a.partials[(size_t) f * a.part_stride + (size_t) t * NS + threadIdx.x] = s_tile[threadIdx.x];
+  }
+}
+
+/* rho = cov / (sigma1 sigma2) per frame and the min_rho gate */
+__global__ void __launch_bounds__(256) k_correlation_finish(CorrArgs a)
+{
+  __shared__ double s_tmp[256];
+  __shared__ double s_sum[8];
+  for( int f = blockIdx.x; f < a.n; f += gridDim.x ) {
+    FrameState * F = a.fs + f;
+    if( F->status != SST_FRAME_OK ) continue;
+    combine_partials(a.partials + (size_t) f * a.part_stride, a.tiles, 6, s_tmp, s_sum);
+    if( threadIdx.x == 0 ) {
+      const double n = s_sum[5];
+      double rho = 0;
+      if( n > 0 ) {
+        const double ma = s_sum[0] / n, mb = s_sum[1] / n;
+        const double va = s_sum[2] / n - ma * ma, vb = s_sum[3] / n - mb * mb;
+        const double cv = s_sum[4] / n - ma * mb;
+        rho = cv / (sqrt(fmax(va, 0.0)) * sqrt(fmax(vb, 0.0)));
       }
+      F->rho = (float) rho;
+      if( a.min_rho > 0 && !(rho >= a.min_rho) ) F->status = SST_FRAME_LOW_RHO;
     }
     __syncthreads();
   }
@@ -849,6 +867,9 @@ cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st)
   case FAM_HOMOG: k_correlation<FAM_HOMOG><<<grid, 256, 0, st>>>(a); break;
   default: k_correlation<FAM_QUAD><<<grid, 256, 0, st>>>(a); break;
   }
+  cudaError_t e = cudaGetLastError();
+  if( e != cudaSuccess ) return e;
+  k_correlation_finish<<<grid, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -96,8 +96,8 @@ struct PassArgs {
   double scale_next;        // scale_transfrom factor to the next finer level, 0 at level 0
 };
 
-/* pointwise passes (IC, IC-LM, correlation): 128 x 16 pixel tiles, 256 threads */
-constexpr int PW_TX = 128, PW_TY = 16;
+/* pointwise passes (IC, IC-LM, correlation): 128 x 64 pixel tiles, 256 threads */
+constexpr int PW_TX = 128, PW_TY = 64;
 /* stencil passes (FA, LM): 64 x 16 pixel tiles + 2 px halo, 256 threads */
 constexpr int ST_TX = 64, ST_TY = 16;
 
@@ -109,7 +109,8 @@ inline int tiles_of(int w, int h, int tx, int ty, int * tiles_x)
 
 /* kernel launchers (defined in the .cu files) */
 cudaError_t launch_pass(int method, const PassArgs & a, int grid, cudaStream_t st);
-int pass_num_sums(int method, int M);
+__host__ __device__ int pass_num_sums(int method, int M);
+cudaError_t launch_solve(int method, const PassArgs & a, int grid, cudaStream_t st);
 
 struct LevelBeginArgs {
   FrameState * fs;
