@@ -1,0 +1,245 @@
+/*
+ * serstacker_gb300.hpp -- C++ drop-in classes for SerStacker's registration
+ * and stacking hot path, over the C ABI of libsst_gb300.so.
+ *
+ * The class, option and method names follow the reference interfaces they
+ * replace (paths relative to the SerStacker source tree):
+ *   sst_gb300::c_ecch_options      core/proc/image_registration/ecc2.h:158-172
+ *   sst_gb300::c_ecch              core/proc/image_registration/ecc2.h:193-308
+ *   sst_gb300::c_weigthed_average  core/average/c_frame_accumulation.h:39-63
+ * Images are passed as `image_view` (pointer, size, OpenCV depth code,
+ * stride) instead of cv::Mat, so this header needs no OpenCV; define
+ * SST_GB300_WITH_OPENCV before including it to get cv::Mat overloads.
+ * Errors follow the reference convention: methods return bool, and the
+ * reason is available from last_error() (the reference logs it with CF_ERROR).
+ */
+#pragma once
+#include "serstacker_gb300.h"
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#ifdef SST_GB300_WITH_OPENCV
+#include <opencv2/core.hpp>
+#endif
+
+namespace sst_gb300 {
+
+inline std::string last_error() { return sst_last_error(); }
+
+/* A host image: row-major pixels of OpenCV depth `depth` (CV_8U, CV_16U, CV_32F). */
+struct image_view {
+  const void * data = nullptr;
+  int width = 0, height = 0;
+  int depth = SST_DEPTH_F32;
+  size_t stride = 0;        // bytes per row
+
+  image_view() = default;
+  image_view(const void * d, int w, int h, int dp, size_t s) : data(d), width(w), height(h), depth(dp), stride(s) {}
+#ifdef SST_GB300_WITH_OPENCV
+  image_view(const cv::Mat & m) : data(m.data), width(m.cols), height(m.rows), depth(m.depth()), stride(m.step) {}
+#endif
+  bool empty() const { return data == nullptr || width <= 0 || height <= 0; }
+};
+
+/* c_ecch_options (ecc2.h:158-172), same field names and defaults */
+struct c_ecch_options {
+  double epsx = 1e-5;
+  double reference_smooth_sigma = 1;
+  double input_smooth_sigma = 1;
+  double update_step_scale = 1;
+  int method = SST_ECC_INVERSE_COMPOSITIONAL_LM;
+  int interpolation = 1;      // ECC_INTER_LINEAR
+  int max_iterations = 50;
+  int minimum_image_size = 8;
+  int maxlevel = 0;
+};
+
+/* The motion model and its parameter vector (c_image_transform::parameters()). */
+struct image_transform {
+  sst_motion_model model { SST_MOTION_AFFINE, 0, 0, 0 };
+  std::vector<float> parameters;
+
+  explicit image_transform(int motion_type = SST_MOTION_AFFINE)
+  {
+    model.type = motion_type;
+    model.fix_scale = motion_type == SST_MOTION_EUCLIDEAN ? 1 : 0;
+  }
+};
+
+/* c_ecch on the GPU. align() registers one frame (one launch per
+ * Gauss-Newton step, like the reference's per-frame loop); align_batch()
+ * registers a whole sequence in one graph replay. */
+class c_ecch {
+public:
+  c_ecch() { create(); }
+  explicit c_ecch(const c_ecch_options & opts) : _opts(opts) { create(); }
+  ~c_ecch() { if( _h ) sst_ecch_destroy(_h); }
+  c_ecch(const c_ecch &) = delete;
+  c_ecch & operator=(const c_ecch &) = delete;
+
+  const c_ecch_options & options() const { return _opts; }
+  void set_options(const c_ecch_options & o) { _opts = o; create(); }
+  void set_min_rho(double v) { _min_rho = v; create(); }
+
+  void set_image_transform(image_transform * t) { _transform = t; }
+  image_transform * image_transform_ptr() const { return _transform; }
+
+  /* c_ecch::set_reference_image (ecc2.cc:984-1057) */
+  bool set_reference_image(const image_view & img, const image_view & mask = image_view(), double scale = 1.0)
+  {
+    if( !_h ) return false;
+    return sst_ecch_set_reference_image(_h, img.data, img.depth, img.width, img.height, img.stride, scale,
+        (const uint8_t *) mask.data, mask.stride, 0, nullptr) == SST_OK;
+  }
+
+  /* c_ecch::align(current_image, current_mask) (ecc2.cc:1123-1176): updates the
+   * attached image_transform's parameters in place, as the reference does. */
+  bool align(const image_view & img, double scale = 1.0)
+  {
+    if( !_h || !_transform ) return false;
+    float params[12] = { 0 };
+    for( size_t i = 0; i < _transform->parameters.size() && i < 12; ++i ) params[i] = _transform->parameters[i];
+    int32_t status = 0, iters = 0;
+    float eps = 0, rho = 0;
+    const int rc = sst_ecch_align_plain(_h, img.data, img.depth, 1, img.width, img.height, img.stride,
+        img.stride * img.height, scale, 0, 1, &_transform->model, _transform->parameters.empty() ? 0 : 1,
+        params, &status, &iters, &eps, &rho, nullptr, nullptr);
+    if( rc != SST_OK ) return false;
+    const int M = nparams(_transform->model);
+    _transform->parameters.assign(params, params + M);
+    _eps = eps, _num_iterations = iters, _rho = rho;
+    return status == SST_FRAME_OK;
+  }
+
+  /* n frames (host, consecutive with `frame_stride` bytes) through the batched engine. */
+  bool align_batch(const void * frames, int depth, int n, int width, int height, size_t row_stride, size_t frame_stride,
+      const std::vector<sst_motion_model> & passes, std::vector<float> & params /* n x 12 */,
+      std::vector<int32_t> & status, double scale = 1.0)
+  {
+    if( !_h ) return false;
+    params.assign((size_t) n * 12, 0.f);
+    status.assign(n, 0);
+    return sst_ecch_align_batch(_h, frames, depth, n, width, height, row_stride, frame_stride, scale, 0,
+        (int) passes.size(), passes.data(), 0, params.data(), status.data(), nullptr, nullptr, nullptr, nullptr,
+        nullptr) == SST_OK;
+  }
+
+  double eps() const { return _eps; }
+  int num_iterations() const { return _num_iterations; }
+  double rho() const { return _rho; }
+  int num_levels() const { return _h ? sst_ecch_num_levels(_h) : 0; }
+  sst_ecch * handle() const { return _h; }
+
+  static int nparams(const sst_motion_model & m)
+  {
+    switch ( m.type ) {
+    case SST_MOTION_TRANSLATION: return 2;
+    case SST_MOTION_EUCLIDEAN:
+    case SST_MOTION_SCALED_EUCLIDEAN:
+      return (m.fix_translation ? 0 : 2) + (m.fix_rotation ? 0 : 1) + (m.fix_scale ? 0 : 1);
+    case SST_MOTION_AFFINE: return 6;
+    case SST_MOTION_QUADRATIC: return 12;
+    default: return 8;
+    }
+  }
+
+private:
+  void create()
+  {
+    if( _h ) sst_ecch_destroy(_h), _h = nullptr;
+    sst_ecch_options o;
+    sst_ecch_options_default(&o);
+    o.epsx = _opts.epsx;
+    o.reference_smooth_sigma = _opts.reference_smooth_sigma;
+    o.input_smooth_sigma = _opts.input_smooth_sigma;
+    o.update_step_scale = _opts.update_step_scale;
+    o.method = _opts.method;
+    o.interpolation = _opts.interpolation;
+    o.max_iterations = _opts.max_iterations;
+    o.minimum_image_size = _opts.minimum_image_size;
+    o.maxlevel = _opts.maxlevel;
+    o.min_rho = _min_rho;
+    if( sst_ecch_create(&_h, &o) != SST_OK ) _h = nullptr;
+  }
+
+  c_ecch_options _opts;
+  double _min_rho = 0;
+  sst_ecch * _h = nullptr;
+  image_transform * _transform = nullptr;
+  double _eps = -1, _rho = -1;
+  int _num_iterations = -1;
+};
+
+/* c_weigthed_average (c_frame_accumulation.h:39-63) on the GPU */
+class c_weigthed_average {
+public:
+  c_weigthed_average() = default;
+  ~c_weigthed_average() { if( _h ) sst_weighted_average_destroy(_h); }
+  c_weigthed_average(const c_weigthed_average &) = delete;
+  c_weigthed_average & operator=(const c_weigthed_average &) = delete;
+
+  /* c_weigthed_average::add(src, weights) (c_frame_accumulation.cc:182-221) */
+  bool add(const image_view & src, const image_view & weights = image_view(), double scale = 1.0)
+  {
+    if( !ensure(src.width, src.height) ) return false;
+    return sst_weighted_average_add(_h, src.data, src.depth, src.stride, scale, weights.data, weights.depth,
+        weights.stride, 0, nullptr) == SST_OK;
+  }
+
+  /* warp with the registered transform, weight and add (the stacking
+   * pipeline's per-frame body, c_image_stacking_pipeline.cc:1644-1790) */
+  bool add_warped(const image_view & src, const image_transform & t, float weight = 1.f, double scale = 1.0,
+      int border = SST_BORDER_REFLECT101)
+  {
+    if( !ensure(src.width, src.height) ) return false;
+    float p[12] = { 0 };
+    for( size_t i = 0; i < t.parameters.size() && i < 12; ++i ) p[i] = t.parameters[i];
+    int32_t st = SST_FRAME_OK;
+    return sst_weighted_average_add_warped_batch(_h, src.data, src.depth, 1, src.width, src.height, src.stride,
+        src.stride * src.height, scale, 0, &t.model, p, &st, &weight, border, nullptr) == SST_OK;
+  }
+
+  /* c_weigthed_average::compute (c_frame_accumulation.cc:223-248) */
+  bool compute(std::vector<float> & avg, std::vector<uint8_t> & mask) const
+  {
+    if( !_h ) return false;
+    avg.resize((size_t) _w * _hh);
+    mask.resize((size_t) _w * _hh);
+    return sst_weighted_average_compute(_h, avg.data(), mask.data(), 0, nullptr) == SST_OK;
+  }
+
+  bool get_acc_counters(std::vector<float> & accw) const
+  {
+    if( !_h ) return false;
+    accw.resize((size_t) _w * _hh);
+    return sst_weighted_average_get_acc_counters(_h, accw.data(), 0, nullptr) == SST_OK;
+  }
+
+  bool reinitialize(const std::vector<float> & avg, const std::vector<float> & accw, int width, int height)
+  {
+    if( !ensure(width, height) ) return false;
+    return sst_weighted_average_reinitialize(_h, avg.data(), accw.data(), 0, nullptr) == SST_OK;
+  }
+
+  void clear() { if( _h ) sst_weighted_average_clear(_h, nullptr); }
+  int accumulated_frames() const { return _h ? sst_weighted_average_accumulated_frames(_h) : 0; }
+  int width() const { return _w; }
+  int height() const { return _hh; }
+  sst_weighted_average * handle() const { return _h; }
+
+private:
+  bool ensure(int w, int h)
+  {
+    if( _h && w == _w && h == _hh ) return true;
+    if( _h ) return false;   // size mismatch: the reference rejects it (c_frame_accumulation.cc:195-200)
+    if( sst_weighted_average_create(&_h, w, h) != SST_OK ) return false;
+    _w = w, _hh = h;
+    return true;
+  }
+  sst_weighted_average * _h = nullptr;
+  int _w = 0, _hh = 0;
+};
+
+}  // namespace sst_gb300

@@ -49,3 +49,38 @@ def test_device_count_without_gpu_is_safe(capi):
 def test_kernel_launch_counter(capi):
     capi.kernel_launch_count(reset=True)
     assert capi.kernel_launch_count() == 0
+
+
+def test_cpp_dropin_header_compiles_and_links(capi, tmp_path):
+    """The C++ drop-in classes (include/serstacker_gb300.hpp) compile against the C ABI
+    and run their host-only parts (option defaults, handle creation) without a GPU."""
+    import os
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "t.cc"
+    src.write_text(r'''
+#include "serstacker_gb300.hpp"
+#include <cstdio>
+int main() {
+  sst_gb300::c_ecch_options o;
+  if( o.max_iterations != 50 || o.method != SST_ECC_INVERSE_COMPOSITIONAL_LM ) return 1;
+  sst_gb300::c_ecch e(o);
+  if( !e.handle() ) return 2;
+  sst_gb300::image_transform t(SST_MOTION_HOMOGRAPHY);
+  e.set_image_transform(&t);
+  if( sst_gb300::c_ecch::nparams(t.model) != 8 ) return 3;
+  std::printf("ok %s\n", sst_version());
+  return 0;
+}
+''')
+    libdir = os.path.dirname(capi.LIB_PATH)
+    exe = tmp_path / "t"
+    subprocess.check_call([gxx, "-std=c++17", "-I", os.path.join(root, "include"), str(src), "-o", str(exe),
+                           "-L", libdir, "-lsst_gb300", f"-Wl,-rpath,{libdir}"])
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.startswith("ok")
