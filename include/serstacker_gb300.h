@@ -278,6 +278,45 @@ int sst_extract_bayer_planes_u16(const uint16_t * src, int width, int height, si
 int sst_average_bayer_planes_u16(const uint16_t * src, int width, int height, size_t row_stride,
     uint16_t * dst, void * stream);
 
+/* ------------------------------------------------ allocation-free stacking */
+
+/* Largest batch the allocation-free entry point accepts. */
+#define SST_NOALLOC_MAX_FRAMES 4096
+
+/* Allocation-free variant of sst_weighted_average_add_warped_batch. This
+ * entry point has no counterpart in the reference: SerStacker allocates its
+ * accumulators with OpenCV and never runs on a GPU.
+ *
+ * It exists for callers that cannot let the library call cudaMalloc:
+ *   - code that issues the call while its stream is being captured into a
+ *     CUDA graph (cudaMalloc is not allowed during capture);
+ *   - hosts that own all device memory through their own pool or arena;
+ *   - real-time capture loops that cannot afford cudaMalloc's implicit
+ *     device synchronisation.
+ * It warps, weights and accumulates n device-resident frames exactly like
+ * sst_weighted_average_add_warped_batch (same kernels), but allocates
+ * nothing: the per-frame scratch (warp coefficients and effective weights)
+ * lives in a fixed device array of SST_NOALLOC_MAX_FRAMES entries that the
+ * library declares at file scope, so every GPU that loads the library holds
+ * it (about 272 KB) until the process exits, and the accumulator is the
+ * caller's: acc_state holds 4 planes of dst_width x dst_height floats (sum
+ * of w*I, its compensation, sum of w, its compensation), zeroed by the
+ * caller before the first call and read back with any kernel or copy.
+ *
+ * All pointers are device pointers; params is n x 12 floats, status and
+ * weights (n entries each) may be NULL. n > SST_NOALLOC_MAX_FRAMES is
+ * rejected with SST_ERR_INVALID_ARG.
+ *
+ * The first call on each device looks up the scratch array's device address
+ * (cudaGetSymbolAddress) with that device current: make that first call
+ * before capturing a stream. All calls share the one array: calls whose work
+ * can overlap on the GPU (e.g. on unordered streams) race and must not be
+ * issued concurrently. */
+int sst_weighted_average_add_warped_batch_noalloc(const void * frames, int depth, int n,
+    int src_width, int src_height, size_t row_stride, size_t frame_stride, double scale,
+    const sst_motion_model * model, const float * params, const int32_t * status, const float * weights,
+    int border, float * acc_state, int dst_width, int dst_height, void * stream);
+
 #ifdef __cplusplus
 }
 #endif

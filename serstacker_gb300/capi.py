@@ -94,6 +94,8 @@ def lib():
             "sst_remap": (i, [p, i, i, i, sz, d, p, p, i, p, p, i, i, p]),
             "sst_extract_bayer_planes_u16": (i, [p, i, i, sz, p, p]),
             "sst_average_bayer_planes_u16": (i, [p, i, i, sz, p, p]),
+            "sst_weighted_average_add_warped_batch_noalloc": (i, [p, i, i, i, i, sz, sz, d, p, p, p, p, i, p, i, i,
+                                                                  p]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(_lib, name)

@@ -71,6 +71,12 @@ static int set_error(int code, const char * fmt, ...)
     if( r_ != SST_OK ) return r_;                                                     \
   } while ( 0 )
 
+/* error reporting for entry points defined in other translation units */
+int sst_internal_error(int code, const char * msg)
+{
+  return set_error(code, "%s", msg);
+}
+
 extern "C" const char * sst_last_error(void)
 {
   return g_last_error.c_str();
