@@ -306,8 +306,12 @@ def main():
                 lv_fi += fi
     achieved = lv_bytes / (lv_ms / 1000.0) / 1e9 if lv_ms > 0 else 0.0
     tr = traffic_per_launch()
+    # ncu DRAM bytes of one level-0 launch covering all n frames (small-case capture scaled
+    # by frames; the per-frame traffic does not depend on the batch size)
+    traffic = tr["dram_bytes_per_frame_iteration"] * n if tr else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": tr.get("dram_bytes_per_launch") if tr else None,
+            "traffic": traffic, "alg_bytes_per_launch": 16.0 * WIDTH * HEIGHT * n,
+            "traffic_note": "DRAM bytes of a level-0 launch with all frames active (ncu, scaled from 64 frames)",
             "kernel": "k_pass_pointwise<IC> level 0 (1280x960), all frames x iterations",
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
             "alg_bytes_model": "16 B per pixel and frame-iteration (warped source 4 + template 4 + gradients 8)",
