@@ -51,7 +51,7 @@ __device__ __forceinline__ void sd_pixel(const float * jc, float x, float y, flo
     J[3] = gy * x, J[4] = gy * y, J[5] = gy;
   }
   else if( JK == J_HOMOG ) {
-    const float den = 1.0f / fmaf(x, jc[6], fmaf(y, jc[7], 1.0f));
+    const float den = __frcp_rn(fmaf(x, jc[6], fmaf(y, jc[7], 1.0f)));
     const float hatX = -fmaf(x, jc[0], fmaf(y, jc[1], jc[2])) * den;
     const float hatY = -fmaf(x, jc[3], fmaf(y, jc[4], jc[5])) * den;
     const float ggx = gx * den, ggy = gy * den;
@@ -407,10 +407,55 @@ __device__ void solve_lm(FrameState * F, const double * S, const PassArgs & a, i
 /* ------------------------------------------------------ pointwise passes */
 
 /* IC / IC-LM pass: sums {J^T r (M), |r|^2, count}, J from the reference gradients */
+/* Number of per-thread column partials the identity-warp steepest-descent
+ * projection needs. Each thread owns one column x, so with u = gx r and
+ * w = gy r the projections factor into x-free sums:
+ *   translation  U, W
+ *   euclidean    U, W, Uy            (+ Wy when the scale is free)
+ *   affine       U, W, Uy, Wy
+ *   homography   U, W, Uy, Wy, Wyy
+ * where Uy = sum y u, Wy = sum y w, Wyy = sum y^2 w. */
+template<int JK, int M>
+struct column_sums {
+  static constexpr int N = JK == J_TRANS ? 2 : JK == J_EUCL ? (M > 3 ? 4 : 3) : JK == J_AFFINE ? 4 : 5;
+};
+
+/* J^T r at the identity warp from the column partials (c_image_transform.cc SD formulas
+ * with the identity parameters): P = {U, W, Uy, Wy, Wyy} */
+template<int JK, int M>
+__device__ __forceinline__ void column_project(const float * P, float x, float * acc)
+{
+  const float U = P[0], W = P[1];
+  if( JK == J_TRANS ) {
+    acc[0] = U, acc[1 < M ? 1 : 0] = W;
+  }
+  else if( JK == J_EUCL ) {
+    const float Uy = P[2];
+    acc[0] = U, acc[1] = W;
+    acc[2 < M ? 2 : 0] = fmaf(x, W, -Uy);                 // -gx y + gy x
+    if( M > 3 ) acc[3 < M ? 3 : 0] = fmaf(x, U, P[3 < column_sums<JK, M>::N ? 3 : 0]);   // gx x + gy y
+  }
+  else if( JK == J_AFFINE ) {
+    const float Uy = P[2], Wy = P[3];
+    acc[0] = x * U, acc[1] = Uy, acc[2] = U;
+    acc[3 < M ? 3 : 0] = x * W, acc[4 < M ? 4 : 0] = Wy, acc[5 < M ? 5 : 0] = W;
+  }
+  else {
+    const float Uy = P[2], Wy = P[3], Wyy = P[4 < column_sums<JK, M>::N ? 4 : 0];
+    acc[0] = x * U, acc[1] = Uy, acc[2] = U;
+    acc[3 < M ? 3 : 0] = x * W, acc[4 < M ? 4 : 0] = Wy, acc[5 < M ? 5 : 0] = W;
+    acc[6 < M ? 6 : 0] = -x * fmaf(x, U, Wy);             // -x (x u + y w)
+    acc[7 < M ? 7 : 0] = -fmaf(x, Uy, Wyy);               // -y (x u + y w)
+  }
+}
+
+/* IC / IC-LM pass: sums {J^T r (M), |r|^2, count}, J = steepest-descent images of
+ * the reference at the identity warp */
 template<int METHOD, int FAM, int JK, int M>
 __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
 {
   constexpr int NS = M + 2;
+  constexpr int NP = column_sums<JK, M>::N;
   __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
   __shared__ float s_c[16];
@@ -430,37 +475,69 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
     const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
     const int yend = min(ty0 + PW_TY, a.h);
+    // every tap of the tile inside the level: no coverage / mask / clamping work
+    const bool interior = (METHOD == M_IC || !a.refM) &&
+        rect_interior<FAM>(c, tx0, ty0, min(tx0 + PW_TX, a.w) - 1, yend - 1, a.w, a.h);
+    float P[NP], rr = 0.f, cnt = 0.f;
+#pragma unroll
+    for( int k = 0; k < NP; ++k ) P[k] = 0.f;
+    if( x < a.w ) {
+      const float fx = (float) x;
+      if( interior ) {
+#pragma unroll 4
+        for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
+          const spos s = warp_pos<FAM>(c, x, y);
+          const size_t i = (size_t) y * a.w + x;
+          const float * r0 = img + (size_t) s.y0 * a.w + s.x0;
+          const float v00 = __ldg(r0), v01 = __ldg(r0 + 1), v10 = __ldg(r0 + a.w), v11 = __ldg(r0 + a.w + 1);
+          const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+          const float r = fmaf(s.fy, t1 - t0, t0) - __ldg(a.refT + i);
+          const float2 g = __ldg(a.refG + i);
+          const float fy = (float) y;
+          const float u = g.x * r, w = g.y * r;
+          rr = fmaf(r, r, rr);
+          P[0] += u, P[1] += w;
+          if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
+          if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
+          if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fy * fy, w, P[4 < NP ? 4 : 0]);
+        }
+        cnt = (float) ((yend - ty0 - (int) (threadIdx.x >> 7) + 1) / 2);
+      }
+      else {
+#pragma unroll 4
+        for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
+          const spos s = warp_pos<FAM>(c, x, y);
+          const size_t i = (size_t) y * a.w + x;
+          bool ok;
+          if( METHOD == M_IC ) {
+            ok = mask_ok(coverage(a.w, a.h, s), 250);
+          }
+          else {
+            int rx, ry;
+            warp_nearest<FAM>(c, x, y, rx, ry);
+            ok = rx >= 0 && rx < a.w && ry >= 0 && ry < a.h;
+            if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
+          }
+          const float v = sample_replicate(img, a.w, a.h, s);
+          const float r = ok ? v - __ldg(a.refT + i) : 0.f;
+          const float2 g = __ldg(a.refG + i);
+          const float fy = (float) y;
+          const float u = g.x * r, w = g.y * r;
+          rr = fmaf(r, r, rr);
+          cnt += ok ? 1.f : 0.f;
+          P[0] += u, P[1] += w;
+          if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
+          if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
+          if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fy * fy, w, P[4 < NP ? 4 : 0]);
+        }
+      }
+    }
     float acc[NS];
 #pragma unroll
     for( int k = 0; k < NS; ++k ) acc[k] = 0.f;
-    if( x < a.w ) {
-#pragma unroll 4
-      for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
-        const float fx = (float) x, fy = (float) y;
-        const spos s = warp_pos<FAM>(c, x, y);
-        const size_t i = (size_t) y * a.w + x;
-        bool ok;
-        if( METHOD == M_IC ) {
-          ok = mask_ok(coverage(a.w, a.h, s), 250);
-        }
-        else {
-          int rx, ry;
-          warp_nearest<FAM>(c, x, y, rx, ry);
-          ok = rx >= 0 && rx < a.w && ry >= 0 && ry < a.h;
-          if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
-        }
-        const float T = __ldg(a.refT + i);
-        const float2 g = __ldg(a.refG + i);
-        const float v = sample_replicate(img, a.w, a.h, s);
-        const float r = ok ? v - T : 0.f;
-        acc[M] = fmaf(r, r, acc[M]);
-        acc[M + 1] += ok ? 1.f : 0.f;
-        float J[M];
-        sd_pixel<JK, M>(a.jc_id, fx, fy, g.x, g.y, J);
-#pragma unroll
-        for( int j = 0; j < M; ++j ) acc[j] = fmaf(J[j], r, acc[j]);
-      }
-    }
+    if( x < a.w ) column_project<JK, M>(P, (float) x, acc);
+    acc[M] = rr;
+    acc[M + 1] = cnt;
     block_reduce_d<NS>(acc, s_red, s_tile);
     write_tile<NS>(a, f, t, s_tile);
   }
@@ -811,17 +888,18 @@ __global__ void __launch_bounds__(256) k_correlation(CorrArgs a)
     const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
     const int yend = min(ty0 + PW_TY, a.h);
+    const bool interior = !a.refM && rect_interior<FAM>(c, tx0, ty0, min(tx0 + PW_TX, a.w) - 1, yend - 1, a.w, a.h);
     float acc[NS] = { 0, 0, 0, 0, 0, 0 };
     if( x < a.w ) {
 #pragma unroll 4
       for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
         const spos s = warp_pos<FAM>(c, x, y);
         const size_t i = (size_t) y * a.w + x;
-        bool ok = mask_ok(coverage(a.w, a.h, s), 254);
+        bool ok = interior || mask_ok(coverage(a.w, a.h, s), 254);
         if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
         if( ok ) {
           const float av = __ldg(a.refT + i) - a.tshift;
-          const float bv = sample_constant0(img, a.w, a.h, s) - a.tshift;
+          const float bv = (interior ? sample_replicate(img, a.w, a.h, s) : sample_constant0(img, a.w, a.h, s)) - a.tshift;
           acc[0] += av, acc[1] += bv;
           acc[2] = fmaf(av, av, acc[2]);
           acc[3] = fmaf(bv, bv, acc[3]);

@@ -53,7 +53,7 @@ __device__ __forceinline__ void warp_disp(const float * __restrict__ c, float x,
   }
   else if( FAM == FAM_HOMOG ) {
     const float q = fmaf(c[6], x, c[7] * y);       // a20 x + a21 y
-    const float iw = 1.0f / (1.0f + q);
+    const float iw = __frcp_rn(1.0f + q);
     const float nx = fmaf(c[0], x, fmaf(c[1], y, c[2])) - q * (x + c[12]);
     const float ny = fmaf(c[3], x, fmaf(c[4], y, c[5])) - q * (y + c[13]);
     dx = nx * iw;
@@ -90,6 +90,30 @@ __device__ __forceinline__ spos warp_pos(const float * __restrict__ c, int x, in
   float dx, dy;
   warp_disp<FAM>(c, (float) x, (float) y, dx, dy);
   return make_spos(x + (int) c[12], y + (int) c[13], dx, dy);
+}
+
+/* True when every bilinear tap of every output pixel of the rectangle
+ * [x0, x1] x [y0, y1] lies inside a w x h source: the warp maps the
+ * rectangle's corners to positions in [0, w-2] x [0, h-2] (with a small
+ * margin). Exact for the projective family (the image of a rectangle is the
+ * convex hull of its mapped corners when w > 0 on it); never used for the
+ * quadratic family. Evaluated by lanes 0..3 and broadcast: warp-uniform, and
+ * CTA-uniform when every warp tests the same rectangle. */
+template<int FAM>
+__device__ __forceinline__ bool rect_interior(const float * __restrict__ c, int x0, int y0, int x1, int y1, int w, int h)
+{
+  if( FAM == FAM_QUAD ) return false;
+  const int lane = threadIdx.x & 31;
+  bool ok = true;
+  if( lane < 4 ) {
+    const int x = (lane & 1) ? x1 : x0, y = (lane & 2) ? y1 : y0;
+    float dx, dy;
+    warp_disp<FAM>(c, (float) x, (float) y, dx, dy);
+    const float X = (float) (x + (int) c[12]) + dx, Y = (float) (y + (int) c[13]) + dy;
+    ok = X >= 0.01f && X <= (float) (w - 2) - 0.01f && Y >= 0.01f && Y <= (float) (h - 2) - 0.01f;
+    if( FAM == FAM_HOMOG ) ok = ok && (1.0f + fmaf(c[6], (float) x, c[7] * (float) y)) > 0.f;
+  }
+  return __all_sync(0xffffffffu, ok);
 }
 
 /* nearest source pixel of output pixel (x, y) (cvRound of the map, INTER_NEAREST) */

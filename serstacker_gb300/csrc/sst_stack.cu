@@ -75,27 +75,53 @@ __device__ __forceinline__ float tap(const uint8_t * fb, size_t rs, int sw, int 
   }
 }
 
-constexpr int SK_TX = 32, SK_TY = 8;
+constexpr int SK_TX = 32, SK_TY = 8;          // remap utility tile
+constexpr int SA_TX = 64, SA_TY = 16;         // batched stack tile: 4 pixels per thread
 
 template<int FAM, typename T>
 __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
 {
-  constexpr int VW = SK_TX + 4, VH = SK_TY + 4;
+  constexpr int VW = SA_TX + 4, VH = SA_TY + 4;
+  constexpr int PPT = SA_TX * SA_TY / 256;
   __shared__ uint8_t s_v[VH * VW];
-  __shared__ uint8_t s_h[VH * SK_TX];
-  __shared__ float s_c[SST_NCOEF];
-  const int tx0 = blockIdx.x * SK_TX, ty0 = blockIdx.y * SK_TY;
-  const int lx = threadIdx.x % SK_TX, ly = threadIdx.x / SK_TX;
-  const int x = tx0 + lx, y = ty0 + ly;
-  float S = 0.f, cS = 0.f, Wt = 0.f, cW = 0.f;
+  __shared__ uint8_t s_h[VH * SA_TX];
+  const int tx0 = blockIdx.x * SA_TX, ty0 = blockIdx.y * SA_TY;
+  const int lx = threadIdx.x % SA_TX, ly0 = threadIdx.x / SA_TX;
+  const int x = tx0 + lx;
+  // window whose validity decides the tile's eroded mask (tile + 2 px halo, clipped)
+  const int wx0 = max(tx0 - 2, 0), wy0 = max(ty0 - 2, 0);
+  const int wx1 = min(tx0 + SA_TX + 1, a.dw - 1), wy1 = min(ty0 + SA_TY + 1, a.dh - 1);
+  float S[PPT], cS[PPT], Wt[PPT], cW[PPT];
+#pragma unroll
+  for( int k = 0; k < PPT; ++k ) S[k] = cS[k] = Wt[k] = cW[k] = 0.f;
   for( int f = 0; f < a.n; ++f ) {
     const float wf = __ldg(a.weights + f);
     if( !(wf > 0.f) ) continue;                 // uniform over the CTA
-    if( threadIdx.x < SST_NCOEF ) s_c[threadIdx.x] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + threadIdx.x);
-    __syncthreads();
     float c[SST_NCOEF];
 #pragma unroll
-    for( int i = 0; i < SST_NCOEF; ++i ) c[i] = s_c[i];
+    for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + i);
+    const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
+    if( rect_interior<FAM>(c, wx0, wy0, wx1, wy1, a.sw, a.sh) ) {
+      // every pixel of the window is valid and every tap is inside the frame
+      if( x < a.dw ) {
+#pragma unroll
+        for( int k = 0; k < PPT; ++k ) {
+          const int y = ty0 + ly0 + 4 * k;
+          if( y < a.dh ) {
+            const spos s = warp_pos<FAM>(c, x, y);
+            const T * r0 = (const T *) (fb + (size_t) s.y0 * a.row_stride) + s.x0;
+            const T * r1 = (const T *) ((const uint8_t *) r0 + a.row_stride);
+            const float v00 = (float) __ldg(r0), v01 = (float) __ldg(r0 + 1);
+            const float v10 = (float) __ldg(r1), v11 = (float) __ldg(r1 + 1);
+            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+            const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
+            kahan_add(S[k], cS[k], wf * val);
+            kahan_add(Wt[k], cW[k], wf);
+          }
+        }
+      }
+      continue;
+    }
     // remap(255-mask, LINEAR, CONSTANT 0) >= 255 over the tile + 2 px halo;
     // positions outside the output count as 255 (erode border value)
     for( int q = threadIdx.x; q < VW * VH; q += 256 ) {
@@ -107,45 +133,54 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
       s_v[q] = v;
     }
     __syncthreads();
-    for( int q = threadIdx.x; q < SK_TX * VH; q += 256 ) {
-      const int xx = q % SK_TX, yy = q / SK_TX;
+    for( int q = threadIdx.x; q < SA_TX * VH; q += 256 ) {
+      const int xx = q % SA_TX, yy = q / SA_TX;
       const uint8_t * p = s_v + yy * VW + xx;
-      s_h[yy * SK_TX + xx] = p[0] & p[1] & p[2] & p[3] & p[4];
+      s_h[yy * SA_TX + xx] = p[0] & p[1] & p[2] & p[3] & p[4];
     }
     __syncthreads();
-    if( x < a.dw && y < a.dh ) {
-      const uint8_t * p = s_h + ly * SK_TX + lx;
-      if( p[0] & p[SK_TX] & p[2 * SK_TX] & p[3 * SK_TX] & p[4 * SK_TX] ) {
-        const spos s = warp_pos<FAM>(c, x, y);
-        // the >= 255 test admits footprints with < 0.2 % of the weight outside the
-        // frame: those taps take the image border mode (base_remap's cv::remap)
-        const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
-        const float v00 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
-        const float v01 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
-        const float v10 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
-        const float v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
-        const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-        const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
-        kahan_add(S, cS, wf * val);
-        kahan_add(Wt, cW, wf);
+    if( x < a.dw ) {
+#pragma unroll
+      for( int k = 0; k < PPT; ++k ) {
+        const int ly = ly0 + 4 * k, y = ty0 + ly;
+        if( y >= a.dh ) continue;
+        const uint8_t * p = s_h + ly * SA_TX + lx;
+        if( p[0] & p[SA_TX] & p[2 * SA_TX] & p[3 * SA_TX] & p[4 * SA_TX] ) {
+          const spos s = warp_pos<FAM>(c, x, y);
+          // the >= 255 test admits footprints with < 0.2 % of the weight outside the
+          // frame: those taps take the image border mode (base_remap's cv::remap)
+          const float v00 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
+          const float v01 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
+          const float v10 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
+          const float v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
+          const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+          const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
+          kahan_add(S[k], cS[k], wf * val);
+          kahan_add(Wt[k], cW[k], wf);
+        }
       }
     }
     __syncthreads();
   }
-  if( x < a.dw && y < a.dh ) {
-    const size_t i = (size_t) y * a.dw + x;
-    float gS = a.acc[i], gcS = a.acc[a.plane + i], gW = a.acc[2 * a.plane + i], gcW = a.acc[3 * a.plane + i];
-    kahan_add(gS, gcS, S);
-    gcS += cS;
-    kahan_add(gW, gcW, Wt);
-    gcW += cW;
-    a.acc[i] = gS, a.acc[a.plane + i] = gcS, a.acc[2 * a.plane + i] = gW, a.acc[3 * a.plane + i] = gcW;
+  if( x < a.dw ) {
+#pragma unroll
+    for( int k = 0; k < PPT; ++k ) {
+      const int y = ty0 + ly0 + 4 * k;
+      if( y >= a.dh ) continue;
+      const size_t i = (size_t) y * a.dw + x;
+      float gS = a.acc[i], gcS = a.acc[a.plane + i], gW = a.acc[2 * a.plane + i], gcW = a.acc[3 * a.plane + i];
+      kahan_add(gS, gcS, S[k]);
+      gcS += cS[k];
+      kahan_add(gW, gcW, Wt[k]);
+      gcW += cW[k];
+      a.acc[i] = gS, a.acc[a.plane + i] = gcS, a.acc[2 * a.plane + i] = gW, a.acc[3 * a.plane + i] = gcW;
+    }
   }
 }
 
 cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, cudaStream_t st)
 {
-  dim3 grid((a.dw + SK_TX - 1) / SK_TX, (a.dh + SK_TY - 1) / SK_TY);
+  dim3 grid((a.dw + SA_TX - 1) / SA_TX, (a.dh + SA_TY - 1) / SA_TY);
   const int fam = motion_family(motion);
 #define SST_LAUNCH_STACK(FAMV, TV) k_stack_add_warped<FAMV, TV><<<grid, 256, 0, st>>>(a)
   switch ( depth ) {
