@@ -451,6 +451,17 @@ __device__ __forceinline__ void column_project(const float * P, float x, float *
 
 /* IC / IC-LM pass: sums {J^T r (M), |r|^2, count}, J = steepest-descent images of
  * the reference at the identity warp */
+/* staged source box of one pointwise tile (floats): the warped footprint of
+ * a 128 x 64 tile plus the bilinear taps, for rotations / scales up to a few
+ * degrees / percent */
+constexpr int SB_W = 144, SB_H = 80;
+
+/* IC / IC-LM pass: sums {J^T r (M), |r|^2, count}, J = steepest-descent images of
+ * the reference at the identity warp. When every tap of a tile is inside the
+ * level and the tile's source footprint fits SB_W x SB_H, the footprint is
+ * loaded once into shared memory (coalesced rows) and sampled there;
+ * otherwise the taps are gathered from global memory with the full
+ * coverage / mask / border logic. */
 template<int METHOD, int FAM, int JK, int M>
 __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
 {
@@ -459,6 +470,7 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
   __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
   __shared__ float s_c[16];
+  __shared__ float s_src[SB_H * SB_W];
 
   const int nitems = __ldcg(a.count_in) * a.tiles;
   for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
@@ -475,15 +487,44 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
     const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
     const int yend = min(ty0 + PW_TY, a.h);
-    // every tap of the tile inside the level: no coverage / mask / clamping work
+    int bx0, by0, bx1, by1;
     const bool interior = (METHOD == M_IC || !a.refM) &&
-        rect_interior<FAM>(c, tx0, ty0, min(tx0 + PW_TX, a.w) - 1, yend - 1, a.w, a.h);
+        rect_footprint<FAM>(c, tx0, ty0, min(tx0 + PW_TX, a.w) - 1, yend - 1, a.w, a.h, bx0, by0, bx1, by1);
+    const bool staged = interior && bx1 - bx0 < SB_W && by1 - by0 < SB_H;
     float P[NP], rr = 0.f, cnt = 0.f;
 #pragma unroll
     for( int k = 0; k < NP; ++k ) P[k] = 0.f;
+    if( staged ) {
+      const int bw = bx1 - bx0 + 1, bh = by1 - by0 + 1;
+      for( int q = threadIdx.x; q < bw * bh; q += 256 ) {
+        const int qy = q / bw, qx = q - qy * bw;
+        s_src[qy * SB_W + qx] = __ldg(img + (size_t) (by0 + qy) * a.w + bx0 + qx);
+      }
+      __syncthreads();
+    }
     if( x < a.w ) {
       const float fx = (float) x;
-      if( interior ) {
+      if( staged ) {
+#pragma unroll 4
+        for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
+          const spos s = warp_pos<FAM>(c, x, y);
+          const size_t i = (size_t) y * a.w + x;
+          const float * r0 = s_src + (s.y0 - by0) * SB_W + (s.x0 - bx0);
+          const float v00 = r0[0], v01 = r0[1], v10 = r0[SB_W], v11 = r0[SB_W + 1];
+          const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+          const float r = fmaf(s.fy, t1 - t0, t0) - __ldg(a.refT + i);
+          const float2 g = __ldg(a.refG + i);
+          const float fy = (float) y;
+          const float u = g.x * r, w = g.y * r;
+          rr = fmaf(r, r, rr);
+          P[0] += u, P[1] += w;
+          if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
+          if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
+          if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fy * fy, w, P[4 < NP ? 4 : 0]);
+        }
+        cnt = (float) ((yend - ty0 - (int) (threadIdx.x >> 7) + 1) / 2);
+      }
+      else if( interior ) {
 #pragma unroll 4
         for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
           const spos s = warp_pos<FAM>(c, x, y);
@@ -733,7 +774,11 @@ static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st)
 {
   if constexpr( METHOD == M_IC || METHOD == M_ICLM ) {
     static int g = 0;
-    if( !g ) g = persistent_grid(k_pass_pointwise<METHOD, FAM, JK, M>);
+    if( !g ) {
+      cudaFuncSetAttribute(k_pass_pointwise<METHOD, FAM, JK, M>, cudaFuncAttributePreferredSharedMemoryCarveout,
+          cudaSharedmemCarveoutMaxShared);
+      g = persistent_grid(k_pass_pointwise<METHOD, FAM, JK, M>);
+    }
     k_pass_pointwise<METHOD, FAM, JK, M><<<grid > 0 ? grid : g, 256, 0, st>>>(a);
   }
   else {
