@@ -195,7 +195,8 @@ struct sst_ecch {
   double RMA[32];
   float tshift[32];
   int ks_in = 0;
-  std::map<int, DevBuf> H;
+  std::map<int, DevBuf> H;           // per model: levels x 144 matrices, then levels x 144 inverses
+  std::map<int, std::vector<int>> Hinv_ok;
 
   // batch
   int cap = 0;
@@ -351,7 +352,9 @@ extern "C" int sst_ecch_set_reference_image(sst_ecch * h, const void * image, in
   SST_TRY(join_user(h, stream));
   cudaStream_t st = h->st;
   h->drop_graphs();
+  for( auto & kv : h->H ) kv.second.release();
   h->H.clear();
+  h->Hinv_ok.clear();
 
   const int L = ecch_num_levels(width, height, h->o);
   h->w = width, h->h = height, h->L = L;
@@ -434,6 +437,11 @@ extern "C" int sst_ecch_set_reference_image(sst_ecch * h, const void * image, in
   return SST_OK;
 }
 
+static bool model_cholesky_solve_host(const double * A, const double * b, int n, double * x)
+{
+  return cholesky_solve(A, b, n, x);
+}
+
 /* IC Gauss-Newton matrix per level for one model (identity warp) */
 static int ensure_H(sst_ecch * h, const sst_motion_model & m, const double ** out)
 {
@@ -445,7 +453,7 @@ static int ensure_H(sst_ecch * h, const sst_motion_model & m, const double ** ou
     return SST_OK;
   }
   DevBuf & buf = h->H[key];
-  SST_CK(buf.ensure((size_t) h->L * 144 * sizeof(double)));
+  SST_CK(buf.ensure((size_t) h->L * 2 * 144 * sizeof(double)));
   double s[16];
   float jc[8];
   model_identity(m, s);
@@ -453,7 +461,9 @@ static int ensure_H(sst_ecch * h, const sst_motion_model & m, const double ** ou
   SST_CK(h->jc_id.ensure(8 * sizeof(float)));
   SST_CK(cudaMemcpy(h->jc_id.p, jc, sizeof(jc), cudaMemcpyHostToDevice));
   const int NS = M * (M + 1) / 2;
-  std::vector<double> hp, Hm((size_t) h->L * 144, 0.0);
+  std::vector<double> hp, Hm((size_t) h->L * 2 * 144, 0.0);
+  std::vector<int> & okv = h->Hinv_ok[key];
+  okv.assign(h->L, 0);
   for( int l = 0; l < h->L; ++l ) {
     int tiles = 0;
     SST_CK_LAUNCH(launch_ref_hessian(h->grad.as<float2>() + h->loff[l], h->lw[l], h->lh[l], jac_kind(m.type), M,
@@ -467,6 +477,16 @@ static int ensure_H(sst_ecch * h, const sst_motion_model & m, const double ** ou
         for( int v = 0; v <= u; ++v, ++k ) Hl[u * M + v] += hp[(size_t) t * NS + k];
     }
     for( int u = 0; u < M; ++u ) for( int v = u + 1; v < M; ++v ) Hl[u * M + v] = Hl[v * M + u];
+    // inverse by FP64 Cholesky solves of the unit vectors (the matrix is constant per level)
+    double * Hi = Hm.data() + (size_t) (h->L + l) * 144;
+    bool ok = true;
+    for( int j = 0; j < M && ok; ++j ) {
+      double e[12] = { 0 }, col[12];
+      e[j] = 1;
+      ok = model_cholesky_solve_host(Hl, e, M, col);
+      for( int i = 0; i < M; ++i ) Hi[i * M + j] = col[i];
+    }
+    okv[l] = ok ? 1 : 0;
   }
   SST_CK(cudaMemcpy(buf.p, Hm.data(), Hm.size() * sizeof(double), cudaMemcpyHostToDevice));
   *out = buf.as<double>();
@@ -539,7 +559,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
   const int L = h->L;
   const int max_it = h->o.max_iterations;
   const int grid = std::max(1, h->num_sms) * 4;
-  const int solve_grid = std::max(1, std::min(n, std::max(1, h->num_sms) * 4));
+  const int solve_grid = std::max(1, std::min((n + 7) / 8, std::max(1, h->num_sms) * 8));
   long long k = 0;
   SST_CK(cudaMemsetAsync(h->counts.p, 0, (size_t) h->steps_cap * sizeof(int), st));
   int step = 0;
@@ -578,6 +598,11 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
       a.refM = h->has_mask ? h->mask.as<uint8_t>() + h->loff[l] : nullptr;
       a.refMe = h->has_mask ? h->mask_e.as<uint8_t>() + h->loff[l] : nullptr;
       a.H = H ? H + (size_t) l * 144 : nullptr;
+      {
+        const int key = m.type * 16 + model_nparams(m);
+        const bool inv_ok = H && h->Hinv_ok.count(key) && h->Hinv_ok[key][l];
+        a.Hinv = (method == M_IC && inv_ok) ? H + (size_t) (L + l) * 144 : nullptr;
+      }
       a.RMA = h->RMA[l];
       a.tshift = h->tshift[l];
       {

@@ -176,7 +176,15 @@ __device__ void solve_ic(FrameState * F, const double * S, const PassArgs & a, i
   const double rmsnew = S[M] * q * q;
   double b[12], x[12];
   for( int j = 0; j < M; ++j ) b[j] = S[j] * q;
-  if( !cholesky_solve(a.H, b, M, x) ) for( int j = 0; j < M; ++j ) x[j] = 0;
+  if( a.Hinv ) {
+    // the IC matrix is constant per level: its inverse (FP64 Cholesky on the host) replaces the solve
+    for( int i = 0; i < M; ++i ) {
+      double t = 0;
+      for( int j = 0; j < M; ++j ) t += a.Hinv[i * M + j] * b[j];
+      x[i] = t;
+    }
+  }
+  else if( !cholesky_solve(a.H, b, M, x) ) for( int j = 0; j < M; ++j ) x[j] = 0;
   if( rmsnew >= F->rmsold ) {
     level_finish(F, a, true);
     return;
@@ -451,16 +459,9 @@ __device__ __forceinline__ void column_project(const float * P, float x, float *
 
 /* IC / IC-LM pass: sums {J^T r (M), |r|^2, count}, J = steepest-descent images of
  * the reference at the identity warp */
-/* staged source box of one pointwise tile (floats): the warped footprint of
- * a 128 x 64 tile plus the bilinear taps, for rotations / scales up to a few
- * degrees / percent */
-constexpr int SB_W = 144, SB_H = 80;
-
 /* IC / IC-LM pass: sums {J^T r (M), |r|^2, count}, J = steepest-descent images of
  * the reference at the identity warp. When every tap of a tile is inside the
- * level and the tile's source footprint fits SB_W x SB_H, the footprint is
- * loaded once into shared memory (coalesced rows) and sampled there;
- * otherwise the taps are gathered from global memory with the full
+ * level (warp-uniform corner test) the taps are gathered without the
  * coverage / mask / border logic. */
 template<int METHOD, int FAM, int JK, int M>
 __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
@@ -470,7 +471,6 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
   __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
   __shared__ float s_c[16];
-  __shared__ float s_src[SB_H * SB_W];
 
   const int nitems = __ldcg(a.count_in) * a.tiles;
   for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
@@ -487,44 +487,14 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
     const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
     const int yend = min(ty0 + PW_TY, a.h);
-    int bx0, by0, bx1, by1;
     const bool interior = (METHOD == M_IC || !a.refM) &&
-        rect_footprint<FAM>(c, tx0, ty0, min(tx0 + PW_TX, a.w) - 1, yend - 1, a.w, a.h, bx0, by0, bx1, by1);
-    const bool staged = interior && bx1 - bx0 < SB_W && by1 - by0 < SB_H;
+        rect_interior<FAM>(c, tx0, ty0, min(tx0 + PW_TX, a.w) - 1, yend - 1, a.w, a.h);
     float P[NP], rr = 0.f, cnt = 0.f;
 #pragma unroll
     for( int k = 0; k < NP; ++k ) P[k] = 0.f;
-    if( staged ) {
-      const int bw = bx1 - bx0 + 1, bh = by1 - by0 + 1;
-      for( int q = threadIdx.x; q < bw * bh; q += 256 ) {
-        const int qy = q / bw, qx = q - qy * bw;
-        s_src[qy * SB_W + qx] = __ldg(img + (size_t) (by0 + qy) * a.w + bx0 + qx);
-      }
-      __syncthreads();
-    }
     if( x < a.w ) {
       const float fx = (float) x;
-      if( staged ) {
-#pragma unroll 4
-        for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
-          const spos s = warp_pos<FAM>(c, x, y);
-          const size_t i = (size_t) y * a.w + x;
-          const float * r0 = s_src + (s.y0 - by0) * SB_W + (s.x0 - bx0);
-          const float v00 = r0[0], v01 = r0[1], v10 = r0[SB_W], v11 = r0[SB_W + 1];
-          const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-          const float r = fmaf(s.fy, t1 - t0, t0) - __ldg(a.refT + i);
-          const float2 g = __ldg(a.refG + i);
-          const float fy = (float) y;
-          const float u = g.x * r, w = g.y * r;
-          rr = fmaf(r, r, rr);
-          P[0] += u, P[1] += w;
-          if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
-          if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
-          if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fy * fy, w, P[4 < NP ? 4 : 0]);
-        }
-        cnt = (float) ((yend - ty0 - (int) (threadIdx.x >> 7) + 1) / 2);
-      }
-      else if( interior ) {
+      if( interior ) {
 #pragma unroll 4
         for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
           const spos s = warp_pos<FAM>(c, x, y);
@@ -719,28 +689,37 @@ __host__ __device__ int pass_num_sums(int method, int M)
   }
 }
 
-/* The per-frame Gauss-Newton logic of one step: one CTA per active frame
- * combines the frame's tile partials in a fixed order and thread 0 runs the
- * reference's per-iteration update in FP64. */
+/* The per-frame Gauss-Newton logic of one step: one warp per active frame
+ * combines the frame's tile partials in a fixed order (lane-strided sums, then
+ * a fixed butterfly) and lane 0 runs the reference's per-iteration update in
+ * FP64. */
 __global__ void __launch_bounds__(256) k_solve(PassArgs a, int method)
 {
-  __shared__ double s_tmp[256];
-  __shared__ double s_sum[160];
+  __shared__ double s_sum[8][160];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int warp = blockIdx.x * 8 + wid, nwarps = gridDim.x * 8;
   const int NS = pass_num_sums(method, a.M);
   const int count = __ldcg(a.count_in);
-  for( int fi = blockIdx.x; fi < count; fi += gridDim.x ) {
+  for( int fi = warp; fi < count; fi += nwarps ) {
     const int f = __ldcg(a.list_in + fi);
-    combine_partials(a.partials + (size_t) f * a.part_stride, a.tiles, NS, s_tmp, s_sum);
-    if( threadIdx.x == 0 ) {
+    const double * P = a.partials + (size_t) f * a.part_stride;
+    for( int k = 0; k < NS; ++k ) {
+      double v = 0;
+      for( int t = lane; t < a.tiles; t += 32 ) v += __ldcg(P + (size_t) t * NS + k);
+      v = warp_sum(v);
+      if( lane == 0 ) s_sum[wid][k] = v;
+    }
+    __syncwarp();
+    if( lane == 0 ) {
       FrameState * F = a.fs + f;
       switch ( method ) {
-      case M_IC: solve_ic(F, s_sum, a, f); break;
-      case M_ICLM: solve_iclm(F, s_sum, a, f); break;
-      case M_FA: solve_fa(F, s_sum, a, f); break;
-      default: solve_lm(F, s_sum, a, f); break;
+      case M_IC: solve_ic(F, s_sum[wid], a, f); break;
+      case M_ICLM: solve_iclm(F, s_sum[wid], a, f); break;
+      case M_FA: solve_fa(F, s_sum[wid], a, f); break;
+      default: solve_lm(F, s_sum[wid], a, f); break;
       }
     }
-    __syncthreads();
+    __syncwarp();
   }
 }
 
@@ -775,8 +754,6 @@ static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st)
   if constexpr( METHOD == M_IC || METHOD == M_ICLM ) {
     static int g = 0;
     if( !g ) {
-      cudaFuncSetAttribute(k_pass_pointwise<METHOD, FAM, JK, M>, cudaFuncAttributePreferredSharedMemoryCarveout,
-          cudaSharedmemCarveoutMaxShared);
       g = persistent_grid(k_pass_pointwise<METHOD, FAM, JK, M>);
     }
     k_pass_pointwise<METHOD, FAM, JK, M><<<grid > 0 ? grid : g, 256, 0, st>>>(a);

@@ -78,6 +78,7 @@ struct PassArgs {
   const uint8_t * refM;     // reference level mask or nullptr
   const uint8_t * refMe;    // 5x5-eroded reference mask (LM) or nullptr
   const double * H;         // IC / IC-LM: M x M Gauss-Newton matrix at this level
+  const double * Hinv;      // IC: its inverse (nullptr when H is not positive definite)
   double RMA;               // number of valid reference pixels
   float tshift;             // mean of the reference level (numerical shift for FA sums)
   float jc_id[8];           // identity steepest-descent coefficients (IC / IC-LM)

@@ -168,6 +168,7 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi)
 /* BORDER_REFLECT_101 index for any p (always inside [0, n)) */
 __device__ __forceinline__ int reflect101(int p, int n)
 {
+  if( (unsigned) p < (unsigned) n ) return p;
   if( n == 1 ) return 0;
   const int period = 2 * (n - 1);
   p = clampi(p, -(1 << 29), 1 << 29);
@@ -179,6 +180,7 @@ __device__ __forceinline__ int reflect101(int p, int n)
 /* BORDER_REFLECT index for any p (always inside [0, n)) */
 __device__ __forceinline__ int reflect(int p, int n)
 {
+  if( (unsigned) p < (unsigned) n ) return p;
   const int period = 2 * n;
   p = clampi(p, -(1 << 29), 1 << 29);
   p = p < 0 ? -p - 1 : p;

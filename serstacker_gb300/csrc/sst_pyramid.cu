@@ -18,54 +18,75 @@ namespace sst {
 
 /* ------------------------------------------------ convert + pre-smooth */
 
-constexpr int CS_TX = 64, CS_TY = 16, CS_RMAX = 15;
+constexpr int CS_TX = 128, CS_TY = 32, CS_RMAX = 15;
 
 template<typename T>
 __device__ __forceinline__ float load_px(const uint8_t * base, size_t row_stride, int x, int y)
 {
-  return (float) (*(const T *) (base + (size_t) y * row_stride + (size_t) x * sizeof(T)));
+  return (float) __ldg((const T *) (base + (size_t) y * row_stride) + x);
 }
 
+/* One 128 x 32 output tile per CTA: the (128 + 2R) x (32 + 2R) input window
+ * (REPLICATE) is converted and staged in shared memory row by row (coalesced),
+ * filtered horizontally then vertically. */
 template<typename T>
 __global__ void __launch_bounds__(256) k_convert_smooth(const uint8_t * src, int w, int h, size_t row_stride,
     size_t frame_stride, float scale, const float * __restrict__ gk, int R, float * dst, size_t dst_stride)
 {
-  __shared__ float s_in[(CS_TY + 2 * CS_RMAX) * (CS_TX + 2 * CS_RMAX)];
-  __shared__ float s_h[(CS_TY + 2 * CS_RMAX) * CS_TX];
-  __shared__ float c_gauss[2 * CS_RMAX + 1];
-  if( threadIdx.x <= 2 * R && R > 0 ) c_gauss[threadIdx.x] = gk[threadIdx.x];
+  extern __shared__ float sm[];
   const uint8_t * fb = src + (size_t) blockIdx.z * frame_stride;
   float * out = dst + (size_t) blockIdx.z * dst_stride;
   const int tx0 = blockIdx.x * CS_TX, ty0 = blockIdx.y * CS_TY;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if( R <= 0 ) {
-    for( int q = threadIdx.x; q < CS_TX * CS_TY; q += 256 ) {
-      const int x = tx0 + q % CS_TX, y = ty0 + q / CS_TX;
-      if( x < w && y < h ) out[(size_t) y * w + x] = load_px<T>(fb, row_stride, x, y) * scale;
+    for( int yy = wid; yy < CS_TY; yy += 8 ) {
+      const int y = ty0 + yy;
+      if( y >= h ) break;
+#pragma unroll
+      for( int k = 0; k < CS_TX / 32; ++k ) {
+        const int x = tx0 + lane + 32 * k;
+        if( x < w ) out[(size_t) y * w + x] = load_px<T>(fb, row_stride, x, y) * scale;
+      }
     }
     return;
   }
   const int SW = CS_TX + 2 * R, SH = CS_TY + 2 * R;
-  for( int q = threadIdx.x; q < SW * SH; q += 256 ) {
-    const int x = clampi(tx0 - R + q % SW, 0, w - 1);
-    const int y = clampi(ty0 - R + q / SW, 0, h - 1);
-    s_in[q] = load_px<T>(fb, row_stride, x, y) * scale;
+  float * s_in = sm;
+  float * s_h = sm + SW * SH;
+  float * g = s_h + CS_TX * SH;
+  if( threadIdx.x <= 2 * R ) g[threadIdx.x] = gk[threadIdx.x];
+  for( int yy = wid; yy < SH; yy += 8 ) {
+    const int y = clampi(ty0 - R + yy, 0, h - 1);
+    const uint8_t * rowp = fb + (size_t) y * row_stride;
+#pragma unroll 4
+    for( int xx = lane; xx < SW; xx += 32 ) {
+      const int x = clampi(tx0 - R + xx, 0, w - 1);
+      s_in[yy * SW + xx] = (float) __ldg((const T *) rowp + x) * scale;
+    }
   }
   __syncthreads();
-  for( int q = threadIdx.x; q < CS_TX * SH; q += 256 ) {
-    const int xx = q % CS_TX, yy = q / CS_TX;
-    const float * p = s_in + yy * SW + xx;
-    float a = 0.f;
-    for( int i = 0; i <= 2 * R; ++i ) a = fmaf(c_gauss[i], p[i], a);
-    s_h[yy * CS_TX + xx] = a;
-  }
-  __syncthreads();
-  for( int q = threadIdx.x; q < CS_TX * CS_TY; q += 256 ) {
-    const int xx = q % CS_TX, yy = q / CS_TX;
-    const int x = tx0 + xx, y = ty0 + yy;
-    if( x < w && y < h ) {
+  for( int yy = wid; yy < SH; yy += 8 ) {
+#pragma unroll
+    for( int k = 0; k < CS_TX / 32; ++k ) {
+      const int xx = lane + 32 * k;
+      const float * p = s_in + yy * SW + xx;
       float a = 0.f;
-      for( int j = 0; j <= 2 * R; ++j ) a = fmaf(c_gauss[j], s_h[(yy + j) * CS_TX + xx], a);
-      out[(size_t) y * w + x] = a;
+      for( int i = 0; i <= 2 * R; ++i ) a = fmaf(g[i], p[i], a);
+      s_h[yy * CS_TX + xx] = a;
+    }
+  }
+  __syncthreads();
+  for( int yy = wid; yy < CS_TY; yy += 8 ) {
+    const int y = ty0 + yy;
+    if( y >= h ) break;
+#pragma unroll
+    for( int k = 0; k < CS_TX / 32; ++k ) {
+      const int xx = lane + 32 * k, x = tx0 + xx;
+      if( x < w ) {
+        float a = 0.f;
+        for( int j = 0; j <= 2 * R; ++j ) a = fmaf(g[j], s_h[(yy + j) * CS_TX + xx], a);
+        out[(size_t) y * w + x] = a;
+      }
     }
   }
 }
@@ -76,12 +97,21 @@ cudaError_t launch_convert_smooth(const void * src, int depth, int n, int w, int
   // gk: device array of ksize weights (nullptr: no smoothing)
   const int R = gk ? ksize / 2 : 0;
   if( R > CS_RMAX ) return cudaErrorInvalidValue;
+  const size_t smem = R > 0 ? ((size_t) (CS_TX + 2 * R) * (CS_TY + 2 * R) + (size_t) CS_TX * (CS_TY + 2 * R) + 32) * sizeof(float) : 0;
   dim3 grid((w + CS_TX - 1) / CS_TX, (h + CS_TY - 1) / CS_TY, n);
   const uint8_t * s = (const uint8_t *) src;
+  static bool attr = false;
+  if( !attr ) {
+    const int mx = (int) (((CS_TX + 2 * CS_RMAX) * (CS_TY + 2 * CS_RMAX) + CS_TX * (CS_TY + 2 * CS_RMAX) + 32) * sizeof(float));
+    cudaFuncSetAttribute(k_convert_smooth<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_convert_smooth<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_convert_smooth<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    attr = true;
+  }
   switch ( depth ) {
-  case SST_DEPTH_U8: k_convert_smooth<uint8_t><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
-  case SST_DEPTH_U16: k_convert_smooth<uint16_t><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
-  case SST_DEPTH_F32: k_convert_smooth<float><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
+  case SST_DEPTH_U8: k_convert_smooth<uint8_t><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
+  case SST_DEPTH_U16: k_convert_smooth<uint16_t><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
+  case SST_DEPTH_F32: k_convert_smooth<float><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
   default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -89,7 +119,7 @@ cudaError_t launch_convert_smooth(const void * src, int depth, int n, int w, int
 
 /* ------------------------------------------------------------- pyrDown */
 
-constexpr int PD_TX = 32, PD_TY = 16;
+constexpr int PD_TX = 64, PD_TY = 16;
 
 __global__ void __launch_bounds__(256) k_pyrdown(const float * src, int sw, int sh, size_t src_stride,
     float * dst, int dw, int dh, size_t dst_stride)
@@ -101,24 +131,33 @@ __global__ void __launch_bounds__(256) k_pyrdown(const float * src, int sw, int 
   float * out = dst + (size_t) blockIdx.z * dst_stride;
   const int tx0 = blockIdx.x * PD_TX, ty0 = blockIdx.y * PD_TY;
   const int sx0 = 2 * tx0 - 2, sy0 = 2 * ty0 - 2;
-  for( int q = threadIdx.x; q < SW * SH; q += 256 ) {
-    const int x = reflect101(sx0 + q % SW, sw), y = reflect101(sy0 + q / SW, sh);
-    s_in[q] = __ldg(in + (size_t) y * sw + x);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for( int yy = wid; yy < SH; yy += 8 ) {
+    const float * rowp = in + (size_t) reflect101(sy0 + yy, sh) * sw;
+#pragma unroll
+    for( int xx = lane; xx < SW; xx += 32 ) s_in[yy * SW + xx] = __ldg(rowp + reflect101(sx0 + xx, sw));
   }
   __syncthreads();
-  for( int q = threadIdx.x; q < PD_TX * SH; q += 256 ) {
-    const int xx = q % PD_TX, yy = q / PD_TX;
-    const float * p = s_in + yy * SW + 2 * xx;
-    s_h[yy * PD_TX + xx] = (p[0] + p[4]) * 0.0625f + (p[1] + p[3]) * 0.25f + p[2] * 0.375f;
+  for( int yy = wid; yy < SH; yy += 8 ) {
+#pragma unroll
+    for( int k = 0; k < PD_TX / 32; ++k ) {
+      const int xx = lane + 32 * k;
+      const float * p = s_in + yy * SW + 2 * xx;
+      s_h[yy * PD_TX + xx] = (p[0] + p[4]) * 0.0625f + (p[1] + p[3]) * 0.25f + p[2] * 0.375f;
+    }
   }
   __syncthreads();
-  for( int q = threadIdx.x; q < PD_TX * PD_TY; q += 256 ) {
-    const int xx = q % PD_TX, yy = q / PD_TX;
-    const int x = tx0 + xx, y = ty0 + yy;
-    if( x < dw && y < dh ) {
-      const float * p = s_h + (2 * yy) * PD_TX + xx;
-      out[(size_t) y * dw + x] = (p[0] + p[4 * PD_TX]) * 0.0625f + (p[PD_TX] + p[3 * PD_TX]) * 0.25f +
-          p[2 * PD_TX] * 0.375f;
+  for( int yy = wid; yy < PD_TY; yy += 8 ) {
+    const int y = ty0 + yy;
+    if( y >= dh ) break;
+#pragma unroll
+    for( int k = 0; k < PD_TX / 32; ++k ) {
+      const int xx = lane + 32 * k, x = tx0 + xx;
+      if( x < dw ) {
+        const float * p = s_h + (2 * yy) * PD_TX + xx;
+        out[(size_t) y * dw + x] = (p[0] + p[4 * PD_TX]) * 0.0625f + (p[PD_TX] + p[3 * PD_TX]) * 0.25f +
+            p[2 * PD_TX] * 0.375f;
+      }
     }
   }
 }
