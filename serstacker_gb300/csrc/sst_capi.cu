@@ -190,7 +190,7 @@ struct sst_ecch {
   int lw[32], lh[32];
   size_t loff[32];
   size_t pyr_px = 0;
-  DevBuf ref, grad, mask, mask_e, refsrc, jc_id, hpart, gk_in, gk_ref;
+  DevBuf ref, grad, refTG, mask, mask_e, refsrc, jc_id, hpart, gk_in, gk_ref;
   bool has_mask = false;
   double RMA[32];
   float tshift[32];
@@ -219,7 +219,7 @@ struct sst_ecch {
     if( prof_ready ) for( auto & a : prof ) for( auto & b : a ) for( auto & e : b ) cudaEventDestroy(e);
     for( auto & g : graphs ) if( g.exec ) cudaGraphExecDestroy(g.exec);
     graphs.clear();
-    DevBuf * bufs[] = { &ref, &grad, &mask, &mask_e, &refsrc, &jc_id, &hpart, &gk_in, &gk_ref, &stage[0], &stage[1],
+    DevBuf * bufs[] = { &ref, &grad, &refTG, &mask, &mask_e, &refsrc, &jc_id, &hpart, &gk_in, &gk_ref, &stage[0], &stage[1],
         &pyr, &fs, &part, &cnt, &lists, &counts, &lap, &init, &out_params, &out_status, &out_iters, &out_eps,
         &out_rho, &out_weight, &weff, &coeffs, &res_params, &res_status, &res_rho, &res_weight };
     for( DevBuf * b : bufs ) b->release();
@@ -416,6 +416,8 @@ extern "C" int sst_ecch_set_reference_image(sst_ecch * h, const void * image, in
     SST_CK_LAUNCH(launch_ref_gradients(ref + h->loff[l], mask ? h->mask.as<uint8_t>() + h->loff[l] : nullptr,
         h->lw[l], h->lh[l], h->grad.as<float2>() + h->loff[l], st));
   }
+  SST_CK(h->refTG.ensure(off * sizeof(float4)));
+  SST_CK_LAUNCH(launch_pack_reference(ref, h->grad.as<float2>(), off, h->refTG.as<float4>(), st));
   // per-level statistics: mean (numerical shift) and RMA (valid reference pixels)
   int tx;
   const int tmax = tiles_of(width, height, PW_TX, PW_TY, &tx);
@@ -595,6 +597,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
       a.tiles = level_tiles(h, l, method, &a.tiles_x);
       a.refT = h->ref.as<float>() + h->loff[l];
       a.refG = h->grad.as<float2>() + h->loff[l];
+      a.refTG = h->refTG.as<float4>() + h->loff[l];
       a.refM = h->has_mask ? h->mask.as<uint8_t>() + h->loff[l] : nullptr;
       a.refMe = h->has_mask ? h->mask_e.as<uint8_t>() + h->loff[l] : nullptr;
       a.H = H ? H + (size_t) l * 144 : nullptr;

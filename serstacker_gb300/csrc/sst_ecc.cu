@@ -489,6 +489,25 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
     const int yend = min(ty0 + PW_TY, a.h);
     const bool interior = (METHOD == M_IC || !a.refM) &&
         rect_interior<FAM>(c, tx0, ty0, min(tx0 + PW_TX, a.w) - 1, yend - 1, a.w, a.h);
+    // warm L2 with the source footprint of this CTA's next item (its taps otherwise come from DRAM)
+    if( item + (int) gridDim.x < nitems ) {
+      const int nitem = item + gridDim.x;
+      const int nfi = nitem / a.tiles, nt = nitem - nfi * a.tiles;
+      const int nf = __ldcg(a.list_in + nfi);
+      const float * nw = a.fs[nf].wc;
+      const int nx0 = (nt % a.tiles_x) * PW_TX, ny0 = (nt / a.tiles_x) * PW_TY;
+      const int row = threadIdx.x >> 2;                 // 64 rows, 4 lines of 32 floats per row
+      if( row < PW_TY ) {
+        const int y = min(ny0 + row, a.h - 1);
+        const int x = min(nx0 + (threadIdx.x & 3) * 32, a.w - 1);
+        const float dx = fmaf(__ldg(nw + 0), (float) x, fmaf(__ldg(nw + 1), (float) y, __ldg(nw + 2)));
+        const float dy = fmaf(__ldg(nw + 3), (float) x, fmaf(__ldg(nw + 4), (float) y, __ldg(nw + 5)));
+        const int sx = clampi(x + (int) __ldg(nw + 12) + (int) floorf(dx), 0, a.w - 1);
+        const int sy = clampi(y + (int) __ldg(nw + 13) + (int) floorf(dy), 0, a.h - 1);
+        const float * p = a.pyr + (size_t) nf * a.pyr_stride + a.lvl_off + (size_t) sy * a.w + sx;
+        asm volatile("prefetch.global.L2 [%0];" :: "l"(p));
+      }
+    }
     float P[NP], rr = 0.f, cnt = 0.f;
 #pragma unroll
     for( int k = 0; k < NP; ++k ) P[k] = 0.f;
@@ -502,10 +521,10 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
           const float * r0 = img + (size_t) s.y0 * a.w + s.x0;
           const float v00 = __ldg(r0), v01 = __ldg(r0 + 1), v10 = __ldg(r0 + a.w), v11 = __ldg(r0 + a.w + 1);
           const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-          const float r = fmaf(s.fy, t1 - t0, t0) - __ldg(a.refT + i);
-          const float2 g = __ldg(a.refG + i);
+          const float4 tg = __ldg(a.refTG + i);
+          const float r = fmaf(s.fy, t1 - t0, t0) - tg.x;
           const float fy = (float) y;
-          const float u = g.x * r, w = g.y * r;
+          const float u = tg.y * r, w = tg.z * r;
           rr = fmaf(r, r, rr);
           P[0] += u, P[1] += w;
           if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);

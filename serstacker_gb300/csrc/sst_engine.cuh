@@ -75,6 +75,7 @@ struct PassArgs {
   int tiles, tiles_x;       // tiles of this level for this kernel's tile shape
   const float * refT;       // reference level image
   const float2 * refG;      // reference level gradients (zero where the reference mask is 0)
+  const float4 * refTG;     // packed {T, gx, gy, 0} of the level (one 128-bit load per pixel)
   const uint8_t * refM;     // reference level mask or nullptr
   const uint8_t * refMe;    // 5x5-eroded reference mask (LM) or nullptr
   const double * H;         // IC / IC-LM: M x M Gauss-Newton matrix at this level
@@ -170,6 +171,7 @@ cudaError_t launch_pyrdown(const float * src, int sw, int sh, size_t src_stride,
     size_t dst_stride, int n, cudaStream_t st);
 cudaError_t launch_resize_nearest_u8(const uint8_t * src, int sw, int sh, uint8_t * dst, int dw, int dh, cudaStream_t st);
 cudaError_t launch_ref_gradients(const float * img, const uint8_t * mask, int w, int h, float2 * grad, cudaStream_t st);
+cudaError_t launch_pack_reference(const float * img, const float2 * grad, size_t n, float4 * out, cudaStream_t st);
 cudaError_t launch_erode5(const uint8_t * src, int w, int h, uint8_t * dst, cudaStream_t st);
 cudaError_t launch_ref_hessian(const float2 * grad, int w, int h, int jkind, int M, const float * jc,
     double * partials, int * tiles_out, cudaStream_t st);

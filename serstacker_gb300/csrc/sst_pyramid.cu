@@ -241,6 +241,21 @@ cudaError_t launch_ref_gradients(const float * img, const uint8_t * mask, int w,
   return cudaGetLastError();
 }
 
+/* packed {T, gx, gy, 0} reference level for the pointwise passes */
+__global__ void k_pack_reference(const float * img, const float2 * grad, size_t n, float4 * out)
+{
+  const size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if( i >= n ) return;
+  const float2 g = grad[i];
+  out[i] = make_float4(img[i], g.x, g.y, 0.f);
+}
+
+cudaError_t launch_pack_reference(const float * img, const float2 * grad, size_t n, float4 * out, cudaStream_t st)
+{
+  k_pack_reference<<<(unsigned) ((n + 255) / 256), 256, 0, st>>>(img, grad, n, out);
+  return cudaGetLastError();
+}
+
 /* --------------------------------------------- IC Gauss-Newton matrix */
 
 /* per-tile lower-triangle sums of J J^T with J at the identity warp */
