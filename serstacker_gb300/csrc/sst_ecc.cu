@@ -487,8 +487,6 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
     const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
     const int yend = min(ty0 + PW_TY, a.h);
-    const bool interior = (METHOD == M_IC || !a.refM) &&
-        rect_interior<FAM>(c, tx0, ty0, min(tx0 + PW_TX, a.w) - 1, yend - 1, a.w, a.h);
     // warm L2 with the source footprint of this CTA's next item (its taps otherwise come from DRAM)
     if( item + (int) gridDim.x < nitems ) {
       const int nitem = item + gridDim.x;
@@ -511,11 +509,20 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
     float P[NP], rr = 0.f, cnt = 0.f;
 #pragma unroll
     for( int k = 0; k < NP; ++k ) P[k] = 0.f;
-    if( x < a.w ) {
-      const float fx = (float) x;
+    // each warp owns a 32-column strip (one row parity); the interior test runs per
+    // 16-row chunk of the strip, so only chunks near the level border take the
+    // coverage / mask / border path
+    const int xs0 = tx0 + (threadIdx.x & (PW_TX - 1) & ~31);
+    const int xs1 = min(xs0 + 31, a.w - 1);
+    const float fx = (float) x;
+    for( int yc = ty0; yc < yend; yc += 16 ) {
+      const int yc1 = min(yc + 15, yend - 1);
+      const bool interior = (METHOD == M_IC || !a.refM) && xs0 < a.w &&
+          rect_interior<FAM>(c, xs0, yc, xs1, yc1, a.w, a.h);
+      if( x >= a.w ) continue;
       if( interior ) {
 #pragma unroll 4
-        for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
+        for( int y = yc + (threadIdx.x >> 7); y <= yc1; y += 2 ) {
           const spos s = warp_pos<FAM>(c, x, y);
           const size_t i = (size_t) y * a.w + x;
           const float * r0 = img + (size_t) s.y0 * a.w + s.x0;
@@ -526,16 +533,16 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
           const float fy = (float) y;
           const float u = tg.y * r, w = tg.z * r;
           rr = fmaf(r, r, rr);
+          cnt += 1.f;
           P[0] += u, P[1] += w;
           if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
           if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
           if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fy * fy, w, P[4 < NP ? 4 : 0]);
         }
-        cnt = (float) ((yend - ty0 - (int) (threadIdx.x >> 7) + 1) / 2);
       }
       else {
-#pragma unroll 4
-        for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
+#pragma unroll 2
+        for( int y = yc + (threadIdx.x >> 7); y <= yc1; y += 2 ) {
           const spos s = warp_pos<FAM>(c, x, y);
           const size_t i = (size_t) y * a.w + x;
           bool ok;
@@ -549,10 +556,10 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
             if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
           }
           const float v = sample_replicate(img, a.w, a.h, s);
-          const float r = ok ? v - __ldg(a.refT + i) : 0.f;
-          const float2 g = __ldg(a.refG + i);
+          const float4 tg = __ldg(a.refTG + i);
+          const float r = ok ? v - tg.x : 0.f;
           const float fy = (float) y;
-          const float u = g.x * r, w = g.y * r;
+          const float u = tg.y * r, w = tg.z * r;
           rr = fmaf(r, r, rr);
           cnt += ok ? 1.f : 0.f;
           P[0] += u, P[1] += w;
@@ -562,6 +569,7 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
         }
       }
     }
+    (void) fx;
     float acc[NS];
 #pragma unroll
     for( int k = 0; k < NS; ++k ) acc[k] = 0.f;
