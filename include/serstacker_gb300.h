@@ -278,6 +278,53 @@ int sst_extract_bayer_planes_u16(const uint16_t * src, int width, int height, si
 int sst_average_bayer_planes_u16(const uint16_t * src, int width, int height, size_t row_stride,
     uint16_t * dst, void * stream);
 
+/* ------------------------------------------------ Bayer mosaic accumulator */
+
+typedef struct sst_bayer_average sst_bayer_average;
+
+/* c_bayer_average (core/average/c_frame_accumulation.h:222-262) with its
+ * pattern set by set_bayer_pattern (c_frame_accumulation.cc:1138-1144).
+ * width x height is the raw mosaic size of frames and accumulator alike.
+ * colorid is one of SST_COLORID_BAYER_*; other patterns are rejected with
+ * SST_ERR_UNSUPPORTED. */
+int sst_bayer_average_create(sst_bayer_average ** out, int width, int height, int colorid);
+int sst_bayer_average_destroy(sst_bayer_average * h);
+
+/* c_bayer_average::clear (c_frame_accumulation.cc:1161-1168) */
+int sst_bayer_average_clear(sst_bayer_average * h, void * stream);
+
+/* set_remap + add for n raw mosaic frames (c_frame_accumulation.cc:
+ * 1151-1203, _bayer_accumulate :988-1126, pipeline call site
+ * c_image_stacking_pipeline.cc:1730-1749). With a model, frame f's remap is
+ * the transform of params[f] (12 floats per frame) and the per-pixel weight
+ * is the frame's remapped mask (LINEAR/CONSTANT >= 255, 5x5 erode) times
+ * weights[f]; each output pixel gathers the four raw samples around its
+ * truncated remap position into the colour channels of their mosaic
+ * positions. Without a model (model NULL: no registration, empty rmap) each
+ * raw sample goes to its own channel with weight weights[f]. Frames whose
+ * status is not SST_FRAME_OK or whose weight is <= 0 are skipped; status
+ * and weights may be NULL. Raw values are multiplied by `scale`. */
+int sst_bayer_average_add_batch(sst_bayer_average * h, const void * frames, int depth, int n,
+    size_t row_stride, size_t frame_stride, double scale, int on_device, const sst_motion_model * model,
+    const float * params, const int32_t * status, const float * weights, void * stream);
+
+/* c_bayer_average::compute (c_frame_accumulation.cc:1205-1238) and
+ * get_acc_counters (:1240-1250): avg is width x height x 3 f32 (B, G, R
+ * interleaved as the reference's Mat3f), 0 where a channel has no weight;
+ * mask u8 is 255 where any channel has weight; accw is width x height x 3
+ * f32, the channel weight sums with green halved. Any output may be NULL. */
+int sst_bayer_average_compute(sst_bayer_average * h, float * avg, uint8_t * mask, float * accw,
+    int on_device, void * stream);
+
+/* c_frame_accumulation::accumulated_frames */
+int sst_bayer_average_accumulated_frames(const sst_bayer_average * h);
+
+/* Checkpoint: the 12 compensated planes (for channel B, G, R: sum of w*I,
+ * its compensation, sum of w, its compensation; width x height f32 each) in
+ * a host buffer, and the frame count. */
+int sst_bayer_average_save_state(sst_bayer_average * h, float * state12, int32_t * frames, void * stream);
+int sst_bayer_average_load_state(sst_bayer_average * h, const float * state12, int32_t frames, void * stream);
+
 /* ------------------------------------------------ allocation-free stacking */
 
 /* Largest batch the allocation-free entry point accepts. */

@@ -97,6 +97,7 @@ def lib():
             "orc_average_bayer_planes_u16": (None, [p, i, i, p]),
             "orc_bayer_pattern_mask": (None, [i, i, i, p]),
             "orc_bayer_accumulate": (None, [p, i, i, p, p, p, p, p, p]),
+            "orc_warp_grid": (None, [p, p, i, i, p, p]),
             "orc_laplacian_energy": (d, [p, i, i]),
             "orc_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
             "orc_set_num_threads": (None, [i]),
@@ -164,9 +165,8 @@ def warp_grid(m: Model, state, w: int, h: int):
     """W(x;p) over the w x h grid (create_remap) -> (mapx, mapy)."""
     mx = np.empty((h, w))
     my = np.empty((h, w))
-    for y in range(h):
-        for x in range(w):
-            mx[y, x], my[y, x] = warp(m, state, x, y)
+    s = _f64(state)
+    lib().orc_warp_grid(C.byref(m), _ptr(s), w, h, _ptr(mx), _ptr(my))
     return mx, my
 
 
@@ -330,10 +330,42 @@ def bayer_pattern_mask(colorid, w, h):
 def bayer_accumulate(src, mapx, mapy, pattern, weights, acc, cntr):
     a = _f64(src)
     h, w = a.shape
-    mx, my = _f64(mapx), _f64(mapy)
+    mx = None if mapx is None else _f64(mapx)
+    my = None if mapy is None else _f64(mapy)
     wt = None if weights is None else _f64(weights)
     lib().orc_bayer_accumulate(_ptr(a), w, h, _ptr(mx), _ptr(my), _ptr(_u8(pattern)), _ptr(wt), _ptr(acc),
                                _ptr(cntr))
+
+
+def bayer_average(colorid, frames, motion_type=None, params=None, weights=None, status=None, scale=1.0):
+    """c_bayer_average fed as the stacking pipeline feeds it
+    (c_image_stacking_pipeline.cc:1704-1749): per frame the remap of the
+    transform of params[f], the per-pixel weight = remapped frame mask
+    (>= 255, 5x5 erode) x weights[f], then _bayer_accumulate. Returns the
+    channel sums (h, w, 3) and channel weights (h, w, 3), B, G, R order."""
+    fr = np.asarray(frames)
+    if fr.ndim == 2:
+        fr = fr[None]
+    n, h, w = fr.shape
+    pat = bayer_pattern_mask(colorid, w, h)
+    acc = np.zeros((h, w, 3))
+    cntr = np.zeros((h, w, 3))
+    for f in range(n):
+        wf = 1.0 if weights is None else float(weights[f])
+        if status is not None and status[f] != 0:
+            continue
+        if not wf > 0:
+            continue
+        img = fr[f].astype(np.float64) * scale
+        if motion_type is None:
+            bayer_accumulate(img, None, None, pat, np.full((h, w), wf), acc, cntr)
+            continue
+        m = model(motion_type)
+        st = set_params(m, identity(m), np.asarray(params[f], np.float64)[:nparams(m)])
+        _, msk = stack_remap(m, st, img, w, h)
+        mx, my = warp_grid(m, st, w, h)
+        bayer_accumulate(img, mx, my, pat, np.where(msk > 0, wf, 0.0), acc, cntr)
+    return acc, cntr
 
 
 def pipeline_opts(passes=(AFFINE, HOMOGRAPHY), method=IC, maxlevel=4, max_iterations=50, epsx=0.2,

@@ -254,6 +254,17 @@ extern "C" void orc_remap_model(const orc_model * m, const double * state, const
   }
 }
 
+/* create_remap of a transform: W(x; p) at every pixel of a w x h grid */
+extern "C" void orc_warp_grid(const orc_model * m, const double * state, int w, int h, double * mapx, double * mapy)
+{
+#pragma omp parallel for schedule(static)
+  for( int y = 0; y < h; ++y ) {
+    for( int x = 0; x < w; ++x ) {
+      orc_model_warp(m, state, x, y, mapx + (size_t) y * w + x, mapy + (size_t) y * w + x);
+    }
+  }
+}
+
 /* FP64 Cholesky: solves A x = b (A n x n SPD). Returns 0 if not positive definite. */
 static bool cholesky_solve(const double * A, const double * b, int n, double * x)
 {
@@ -949,13 +960,12 @@ extern "C" void orc_bayer_pattern_mask(int colorid, int w, int h, uint8_t * dst)
   case 11: q[0] = 0, q[1] = 1, q[2] = 1, q[3] = 2; break;  // BGGR
   default: memset(dst, 0, (size_t) w * h); return;
   }
-  memset(dst, 0, (size_t) w * h);
-  for( int y = 0; y < h / 2; ++y ) {
-    for( int x = 0; x < w / 2; ++x ) {
-      dst[(size_t) (2 * y) * w + 2 * x] = q[0];
-      dst[(size_t) (2 * y) * w + 2 * x + 1] = q[1];
-      dst[(size_t) (2 * y + 1) * w + 2 * x] = q[2];
-      dst[(size_t) (2 * y + 1) * w + 2 * x + 1] = q[3];
+  // whole 2x2 cells as generate_bayer_pattern_mask; the reference leaves the
+  // last row / column of an odd-sized frame uninitialised, here the pattern
+  // continues by parity there
+  for( int y = 0; y < h; ++y ) {
+    for( int x = 0; x < w; ++x ) {
+      dst[(size_t) y * w + x] = q[((y & 1) << 1) | (x & 1)];
     }
   }
 }
@@ -964,6 +974,15 @@ extern "C" void orc_bayer_pattern_mask(int colorid, int w, int h, uint8_t * dst)
 extern "C" void orc_bayer_accumulate(const double * src, int w, int h, const double * mapx, const double * mapy,
     const uint8_t * pat, const double * weights, double * acc, double * cntr)
 {
+  if( !mapx || !mapy ) {
+    // empty rmap: each raw sample to its own channel (c_frame_accumulation.cc:996-1041)
+    for( size_t i = 0; i < (size_t) w * h; ++i ) {
+      const double wt = weights ? weights[i] : 1.0;
+      acc[i * 3 + pat[i]] += src[i] * wt;
+      cntr[i * 3 + pat[i]] += wt;
+    }
+    return;
+  }
   for( int y = 0; y < h; ++y ) {
     for( int x = 0; x < w; ++x ) {
       const size_t i = (size_t) y * w + x;

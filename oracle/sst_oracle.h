@@ -140,6 +140,7 @@ void orc_running_mean_add_f32(float * acc, float * accw, int w, int h, const flo
 void orc_extract_bayer_planes_u16(const uint16_t * src, int w, int h, uint16_t * dst);
 void orc_average_bayer_planes_u16(const uint16_t * src, int w, int h, uint16_t * dst);
 void orc_bayer_pattern_mask(int colorid, int w, int h, uint8_t * dst);
+void orc_warp_grid(const orc_model * m, const double * state, int w, int h, double * mapx, double * mapy);
 void orc_bayer_accumulate(const double * src, int w, int h, const double * mapx, const double * mapy,
     const uint8_t * pattern, const double * weights, double * acc, double * cntr);
 

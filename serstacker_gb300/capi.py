@@ -23,6 +23,7 @@ FRAME_OK, FRAME_SINGULAR, FRAME_EMPTY_MASK, FRAME_LOW_RHO, FRAME_NAN, FRAME_NOT_
 TRANSLATION, EUCLIDEAN, SCALED_EUCLIDEAN, AFFINE, HOMOGRAPHY, SEMI_QUADRATIC, QUADRATIC, EPIPOLAR = range(8)
 FA, IC, LM, ICLM = range(4)
 BORDER_CONSTANT, BORDER_REPLICATE, BORDER_REFLECT, BORDER_REFLECT101 = 0, 1, 2, 4
+COLORID_BAYER_RGGB, COLORID_BAYER_GRBG, COLORID_BAYER_GBRG, COLORID_BAYER_BGGR = 8, 9, 10, 11
 DEPTH_U8, DEPTH_U16, DEPTH_F32 = 0, 2, 5
 
 _NP_DEPTH = {np.dtype(np.uint8): DEPTH_U8, np.dtype(np.uint16): DEPTH_U16, np.dtype(np.float32): DEPTH_F32}
@@ -96,6 +97,14 @@ def lib():
             "sst_average_bayer_planes_u16": (i, [p, i, i, sz, p, p]),
             "sst_weighted_average_add_warped_batch_noalloc": (i, [p, i, i, i, i, sz, sz, d, p, p, p, p, i, p, i, i,
                                                                   p]),
+            "sst_bayer_average_create": (i, [p, i, i, i]),
+            "sst_bayer_average_destroy": (i, [p]),
+            "sst_bayer_average_clear": (i, [p, p]),
+            "sst_bayer_average_add_batch": (i, [p, p, i, i, sz, sz, d, i, p, p, p, p, p]),
+            "sst_bayer_average_compute": (i, [p, p, p, p, i, p]),
+            "sst_bayer_average_accumulated_frames": (i, [p]),
+            "sst_bayer_average_save_state": (i, [p, p, p, p]),
+            "sst_bayer_average_load_state": (i, [p, p, C.c_int32, p]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(_lib, name)
@@ -281,6 +290,70 @@ class c_weigthed_average:
     def load_state(self, state: np.ndarray, frames: int):
         s = np.ascontiguousarray(state, np.float32)
         _check(lib().sst_weighted_average_load_state(self._h, _ptr(s), frames, None), "load_state")
+
+
+class c_bayer_average:
+    """c_bayer_average (c_frame_accumulation.h:222-262) over the C ABI: raw
+    mosaic frames in, a 3-channel (B, G, R) average out."""
+
+    def __init__(self, width: int, height: int, colorid: int = COLORID_BAYER_RGGB):
+        self.width, self.height, self.colorid = width, height, colorid
+        self._h = C.c_void_p()
+        _check(lib().sst_bayer_average_create(C.byref(self._h), width, height, colorid), "sst_bayer_average_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_bayer_average_destroy(h)
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def clear(self):
+        _check(lib().sst_bayer_average_clear(self._h, None), "clear")
+
+    def add(self, frames: np.ndarray, motion_type: Optional[int] = None, params=None, status=None, weights=None,
+            scale: float = 1.0):
+        """set_remap(transform of params) + add(frame, mask * weight) for each
+        frame; motion_type None adds the frames without a remap."""
+        fr = np.ascontiguousarray(frames)
+        if fr.ndim == 2:
+            fr = fr[None]
+        n = fr.shape[0]
+        m, p = None, None
+        if motion_type is not None:
+            m = motion(motion_type)
+            p = np.zeros((n, 12), np.float32)
+            pp = np.asarray(params, np.float32).reshape(n, -1)
+            p[:, :pp.shape[1]] = pp
+        st = None if status is None else np.ascontiguousarray(status, np.int32)
+        wt = None if weights is None else np.ascontiguousarray(weights, np.float32)
+        _check(lib().sst_bayer_average_add_batch(self._h, _ptr(fr), _NP_DEPTH[fr.dtype], n, fr.strides[1],
+                                                 fr.strides[0], scale, 0, None if m is None else C.byref(m),
+                                                 _ptr(p), _ptr(st), _ptr(wt), None), "add")
+
+    def compute(self):
+        """(avg (h, w, 3) f32, mask (h, w) u8, accw (h, w, 3) f32 with green halved)"""
+        avg = np.zeros((self.height, self.width, 3), np.float32)
+        mask = np.zeros((self.height, self.width), np.uint8)
+        accw = np.zeros((self.height, self.width, 3), np.float32)
+        _check(lib().sst_bayer_average_compute(self._h, _ptr(avg), _ptr(mask), _ptr(accw), 0, None), "compute")
+        return avg, mask, accw
+
+    def accumulated_frames(self) -> int:
+        return lib().sst_bayer_average_accumulated_frames(self._h)
+
+    def save_state(self):
+        st = np.zeros((3, 4, self.height, self.width), np.float32)
+        fr = C.c_int32()
+        _check(lib().sst_bayer_average_save_state(self._h, _ptr(st), C.byref(fr), None), "save_state")
+        return st, fr.value
+
+    def load_state(self, state: np.ndarray, frames: int):
+        s = np.ascontiguousarray(state, np.float32)
+        _check(lib().sst_bayer_average_load_state(self._h, _ptr(s), frames, None), "load_state")
 
 
 def stack_frames(reg: c_ecch, acc: c_weigthed_average, frames, passes: Sequence[int], scale: float,

@@ -77,6 +77,12 @@ int sst_internal_error(int code, const char * msg)
   return set_error(code, "%s", msg);
 }
 
+/* kernel launches made by entry points defined in other translation units */
+void sst_internal_count_launches(int n)
+{
+  g_launches.fetch_add(n);
+}
+
 extern "C" const char * sst_last_error(void)
 {
   return g_last_error.c_str();

@@ -231,6 +231,50 @@ def test_extract_bayer_planes_matches_slicing(oracle):
 def test_bayer_pattern_mask(oracle):
     m = oracle.bayer_pattern_mask(8, 4, 4)   # RGGB: R=2, G=1, B=0
     assert m[0, 0] == 2 and m[0, 1] == 1 and m[1, 0] == 1 and m[1, 1] == 0
+    cells = {9: [[1, 2], [0, 1]], 10: [[1, 0], [2, 1]], 11: [[0, 1], [1, 2]]}   # GRBG, GBRG, BGGR
+    for cid, q in cells.items():
+        assert np.array_equal(oracle.bayer_pattern_mask(cid, 2, 2), np.array(q, np.uint8))
+    # odd sizes: the pattern continues by parity into the last row / column
+    m = oracle.bayer_pattern_mask(8, 5, 3)
+    assert np.array_equal(m, np.tile(np.array([[2, 1], [1, 0]], np.uint8), (2, 3))[:3, :5])
+
+
+def test_bayer_accumulate_constant_channels(oracle):
+    """Each raw sample lands in its own cell's channel, so a mosaic with one
+    constant per channel averages to those constants under any warp."""
+    h, w = 40, 50
+    pat = oracle.bayer_pattern_mask(8, w, h)
+    raw = np.choose(pat, [300.0, 200.0, 100.0])          # B, G, R
+    acc = np.zeros((h, w, 3))
+    cntr = np.zeros((h, w, 3))
+    m = oracle.model(oracle.AFFINE)
+    st = oracle.set_params(m, oracle.identity(m), [1.01, 0.02, 3.3, -0.01, 0.99, -2.7])
+    mx, my = oracle.warp_grid(m, st, w, h)
+    oracle.bayer_accumulate(raw, mx, my, pat, None, acc, cntr)
+    sel = cntr > 1e-9
+    assert sel.mean() > 0.5
+    avg = np.where(sel, acc / np.where(sel, cntr, 1), 0)
+    for ch, v in ((0, 300.0), (1, 200.0), (2, 100.0)):
+        assert np.allclose(avg[..., ch][sel[..., ch]], v, rtol=1e-12)
+    # the four bilinear weights of a gathered pixel sum to 1 across channels
+    inside = cntr.sum(axis=2) > 0
+    assert np.allclose(cntr.sum(axis=2)[inside], 1.0, atol=1e-12)
+
+
+def test_bayer_accumulate_truncates_toward_zero(oracle):
+    """(int) p truncates: a position in (-1, 0) gathers from column 0 with a
+    negative right-hand weight, as the reference's interpolate lambda does."""
+    h, w = 4, 4
+    pat = oracle.bayer_pattern_mask(8, w, h)
+    raw = np.arange(16, dtype=np.float64).reshape(h, w)
+    mx = np.full((h, w), -0.25)
+    my = np.full((h, w), 1.0)
+    acc = np.zeros((h, w, 3))
+    cntr = np.zeros((h, w, 3))
+    oracle.bayer_accumulate(raw, mx, my, pat, None, acc, cntr)
+    # sx = 0, ax = 1.25, bx = -0.25; sy = 1, ay = 1, by = 0: row 1 holds G (x=0) and B (x=1)
+    assert np.allclose(cntr[0, 0], [-0.25, 1.25, 0.0])
+    assert np.allclose(acc[0, 0], [-0.25 * raw[1, 1], 1.25 * raw[1, 0], 0.0])
 
 
 def test_running_mean_equals_weighted_sum(oracle):
