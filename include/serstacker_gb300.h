@@ -325,6 +325,17 @@ int sst_bayer_average_accumulated_frames(const sst_bayer_average * h);
 int sst_bayer_average_save_state(sst_bayer_average * h, float * state12, int32_t * frames, void * stream);
 int sst_bayer_average_load_state(sst_bayer_average * h, const float * state12, int32_t frames, void * stream);
 
+/* ------------------------------------------------ replicas: state merge */
+
+/* Adds the accumulator state `src` into `dst` (host buffers), both `groups`
+ * groups of four planes of `plane` floats (sum of w*I, its compensation, sum
+ * of w, its compensation): 1 group for sst_weighted_average_save_state, 3 for
+ * sst_bayer_average_save_state. The leading sums are merged with TwoSum, so
+ * no rounding error is lost. Replicas that each stacked a contiguous range
+ * of frames merge their states in rank order and load the result. Not in
+ * the reference, whose stacking runs in one process. */
+int sst_state_merge(float * dst, const float * src, int groups, size_t plane);
+
 /* ------------------------------------------------ allocation-free stacking */
 
 /* Largest batch the allocation-free entry point accepts. */

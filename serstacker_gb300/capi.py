@@ -97,6 +97,7 @@ def lib():
             "sst_average_bayer_planes_u16": (i, [p, i, i, sz, p, p]),
             "sst_weighted_average_add_warped_batch_noalloc": (i, [p, i, i, i, i, sz, sz, d, p, p, p, p, i, p, i, i,
                                                                   p]),
+            "sst_state_merge": (i, [p, p, i, sz]),
             "sst_bayer_average_create": (i, [p, i, i, i]),
             "sst_bayer_average_destroy": (i, [p]),
             "sst_bayer_average_clear": (i, [p, p]),
