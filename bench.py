@@ -223,11 +223,15 @@ def main():
     ap.add_argument("--frames", type=int, default=2000)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--chunk", type=int, default=256, help="frames per streamed chunk in the e2e leg")
-    ap.add_argument("--ref-sample", type=int, default=6, help="frames per CPU baseline sample")
+    ap.add_argument("--ref-sample", type=int, default=6, help="frames per step of the --impl reference arm")
+    ap.add_argument("--cpu-sample", type=int, default=160,
+                    help="frames of the cpu_baseline sample (about 10 s of the oracle on 16 cores)")
     ap.add_argument("--plain-frames", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form leg (profiling runs)")
+    ap.add_argument("--workload", choices=["mono", "bayer"], default="mono",
+                    help="mono: the headline 1280x960 sequence; bayer: raw RGGB 3096x2080 frames")
     args = ap.parse_args()
 
     ws, rank, local = dist_env()
@@ -239,6 +243,12 @@ def main():
 
     if args.impl == "reference":
         run_reference_arm(args, ws, rank)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    if args.workload == "bayer":
+        main_bayer(args, ws, rank, local)
         if ws > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
@@ -326,7 +336,6 @@ def main():
         e2e = run_e2e(args, ws, n, frames, reg, acc, passes, frame_bytes)
     plain_fps = run_plain(args, n, frames, ref, opts, passes) if not args.no_plain else None
     pn = min(args.plain_frames, n)
-    sub = frames[:pn].cpu().numpy().view(np.uint16)
 
     # ---------------------------------------------------------- CPU baseline
     cpu = None
@@ -334,10 +343,11 @@ def main():
         import oracle as O
         O.build()
         threads = os.cpu_count() or 1
-        rate, dt = cpu_reference_rate(sub, ref, min(args.ref_sample, pn), threads)
+        cs = max(1, min(args.cpu_sample, n))
+        sub = frames[:cs].cpu().numpy().view(np.uint16)
+        rate, dt = cpu_reference_rate(sub, ref, cs, threads)
         cpu = {"value": rate, "unit": "frames/s", "cores": threads, "kind": "port",
-               "sample": f"{min(args.ref_sample, pn)} frames of the workload (oracle FP64 pipeline, OpenMP, "
-                         f"{dt:.1f} s)"}
+               "sample": f"{cs} frames of the workload (oracle FP64 pipeline, OpenMP, {dt:.1f} s)"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
@@ -414,6 +424,184 @@ def run_plain(args, n, frames, ref, opts, passes):
                          scale=SCALE)
     torch.cuda.synchronize()
     return pn / (time.perf_counter() - t0)
+
+
+# ------------------------------------------------------------------ Bayer workload
+
+BAYER_W, BAYER_H = 3096, 2080
+BAYER_SCALE = 1.0 / 4096.0
+
+
+def bayer_cfg(frames: int):
+    return {
+        "workload": f"{frames} x {BAYER_W}x{BAYER_H} raw RGGB u16 12-bit frames (peak 1500 ADU, Poisson + read "
+                    "noise); translation-only inverse-compositional c_ecch (4 levels) on the 2x2-binned "
+                    f"luminance ({BAYER_W // 2}x{BAYER_H // 2}); rho>=0.8 gate; Laplacian-energy frame weights; "
+                    "the four Bayer planes warped and stacked with compensated FP32 sums",
+        "frames": frames, "width": BAYER_W, "height": BAYER_H, "levels": 4, "method": "INVERSE_COMPOSITIONAL",
+        "passes": ["TRANSLATION"], "epsx": 0.01, "max_iterations": 50,
+        "l2": "inputs (frames x 12.9 MB > 129 MB L2) stream from HBM every step; no flush needed",
+    }
+
+
+def bayer_cpu_rate(frames: np.ndarray, ref_bin: np.ndarray, sample: int, threads: int):
+    """The oracle's Bayer path on `sample` raw frames: bin, register, weight,
+    extract planes, warp + accumulate four planes. Returns (frames/s, seconds)."""
+    import oracle as O
+    O.set_num_threads(threads)
+    m = O.model(O.TRANSLATION)
+    oo = O.ecch_opts(method=O.IC, maxlevel=4, max_iterations=50, epsx=0.01, minimum_image_size=16)
+    pw, ph = BAYER_W // 2, BAYER_H // 2
+    ref = ref_bin.astype(np.float64) * BAYER_SCALE
+    S = np.zeros((4, ph, pw))
+    W = np.zeros((ph, pw))
+    t0 = time.perf_counter()
+    for i in range(sample):
+        b = O.average_bayer_planes(frames[i]).astype(np.float64) * BAYER_SCALE
+        st, _, _ = O.ecch_align(m, O.identity(m), ref, b, oo)
+        lw = O.laplacian_energy(O.pyrdown(O.smooth(b, 1.0)))
+        planes = O.extract_bayer_planes(frames[i])
+        for k in range(4):
+            dst, msk = O.stack_remap(m, st, planes[..., k].astype(np.float64) * BAYER_SCALE, pw, ph)
+            wt = np.where(msk > 0, lw, 0.0)
+            S[k] += wt * dst
+            if k == 0:
+                W += wt
+    dt = time.perf_counter() - t0
+    return sample / dt, dt
+
+
+def make_bayer_workload(n: int, device):
+    import torch
+    from serstacker_gb300 import synth
+    sc = synth.scene_bayer()
+    fr32, Hs, _ = synth.make_sequence_torch(sc, n, SEED + 2, kind="translation", gain=1.0, blur_range=(0.8, 2.5),
+                                            device=device, chunk=8, cell_gains=synth.BAYER_GAINS, maxval=4095)
+    frames = fr32.to(torch.int16)                       # values <= 4095: the same bits as u16
+    del fr32
+    cg = np.tile(np.asarray(synth.BAYER_GAINS), (BAYER_H // 2, BAYER_W // 2))
+    ref_raw = np.clip(np.rint(synth.reference_np(sc) * cg), 0, 4095).astype(np.uint16)
+    return frames, ref_raw, Hs
+
+
+def main_bayer(args, ws, rank, local):
+    import torch
+    from serstacker_gb300 import capi as C
+    import oracle as O
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    C.lib()
+    n = args.frames
+    frames, ref_raw, Hs = make_bayer_workload(n, device)
+    ref_bin = O.average_bayer_planes(ref_raw)
+    pw, ph = BAYER_W // 2, BAYER_H // 2
+    frame_bytes = BAYER_W * BAYER_H * 2
+    opts = C.default_options(method=C.IC, maxlevel=4, max_iterations=50, epsx=0.01, minimum_image_size=16,
+                             min_rho=0.8)
+    reg = C.c_ecch(opts)
+    reg.set_reference_image(ref_bin.astype(np.float32), scale=BAYER_SCALE)
+    accs = [C.c_weigthed_average(pw, ph) for _ in range(4)]
+    passes = [C.TRANSLATION]
+    dev_out = {"params": torch.zeros((n, 12), dtype=torch.float32, device=device),
+               "status": torch.zeros(n, dtype=torch.int32, device=device),
+               "rho": torch.zeros(n, dtype=torch.float32, device=device),
+               "weight": torch.zeros(n, dtype=torch.float32, device=device)}
+
+    def step(ptr, on_device, host_input, outputs, chunk):
+        for a in accs:
+            a.clear()
+        reg.set_chunk_frames(chunk)
+        C.stack_bayer_frames(reg, accs, ptr, passes, BAYER_SCALE, weighting=1, on_device=on_device, n=n,
+                             width=BAYER_W, height=BAYER_H, row_stride=BAYER_W * 2, frame_stride=frame_bytes,
+                             outputs=outputs, host_input=host_input)
+
+    for _ in range(args.warmup):
+        step(frames, True, False, dev_out, n)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    C.kernel_launch_count(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step(frames, True, False, dev_out, n)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = C.kernel_launch_count()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, ws)
+    clk = clocks.stop()
+    value = ws * n / (ms / 1000.0)
+    peak, peak_kind = measured_peaks()
+    lv_ms, lv_bytes = 0.0, 0.0
+    level_table = []
+    for lvl in range(reg.num_levels()):
+        t, fi, ab = reg.level_stats(0, lvl)
+        level_table.append({"pass": 0, "level": lvl, "ms": t, "frame_iterations": fi, "alg_bytes": ab})
+        if lvl == 0:
+            lv_ms, lv_bytes = t, ab
+    achieved = lv_bytes / (lv_ms / 1000.0) / 1e9 if lv_ms > 0 else 0.0
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": f"k_pass_pointwise<IC> level 0 ({pw}x{ph}), all frames x iterations",
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+            "alg_bytes_model": "16 B per pixel and frame-iteration"}
+    res = {k: v.cpu().numpy() for k, v in dev_out.items()}
+    ok = res["status"] == 0
+    err = np.hypot(res["params"][ok, 0] - Hs[ok, 0, 2] / 2, res["params"][ok, 1] - Hs[ok, 1, 2] / 2)
+
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((n, BAYER_H, BAYER_W), dtype=torch.int16, pin_memory=True)
+        host.copy_(frames)
+        pinned = {"params": torch.zeros((n, 12), dtype=torch.float32, pin_memory=True),
+                  "status": torch.zeros(n, dtype=torch.int32, pin_memory=True),
+                  "rho": torch.zeros(n, dtype=torch.float32, pin_memory=True),
+                  "weight": torch.zeros(n, dtype=torch.float32, pin_memory=True)}
+        avg_host = torch.zeros((4, ph, pw), dtype=torch.float32, pin_memory=True)
+        mask_host = torch.zeros((ph, pw), dtype=torch.uint8, pin_memory=True)
+
+        def step_e2e():
+            step(host.data_ptr(), True, True, pinned, args.chunk)
+            for k, a in enumerate(accs):
+                C.lib().sst_weighted_average_compute(a.handle, avg_host[k].data_ptr(),
+                                                     mask_host.data_ptr() if k == 0 else None, 0, None)
+
+        for _ in range(max(1, args.warmup)):
+            step_e2e()
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step_e2e()
+        torch.cuda.synchronize()
+        barrier(ws)
+        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000.0 / args.steps, ws)
+        e2e = {"value": ws * n / (e2e_ms / 1000.0), "unit": "frames/s", "h2d_bytes_per_step": n * frame_bytes,
+               "d2h_bytes_per_step": n * 60 + pw * ph * (16 + 1), "ms_per_step": e2e_ms,
+               "api": "sst_stack_bayer_frames (host pinned) + 4 x sst_weighted_average_compute"}
+        del host
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = max(1, min(args.cpu_sample, n))
+        sub = frames[:sample].cpu().numpy().view(np.uint16)
+        rate, dt = bayer_cpu_rate(sub, ref_bin, sample, threads)
+        cpu = {"value": rate, "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": f"{sample} raw frames of the workload (oracle FP64 Bayer path, OpenMP, {dt:.1f} s)"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {**bayer_cfg(n), "parallelism": f"replicas x{ws}"},
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+                "accuracy": {"translation_err_vs_truth_px_median": float(np.median(err)) if err.size else None,
+                             "translation_err_vs_truth_px_max": float(np.max(err)) if err.size else None,
+                             "frames_ok": int(ok.sum())},
+                "levels": level_table}
+        print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -250,6 +250,22 @@ int sst_stack_frames(sst_ecch * reg, sst_weighted_average * acc, const void * fr
     int num_passes, const sst_motion_model * passes, int border, int weighting,
     float * params_out, int32_t * status_out, float * rho_out, float * weight_out, void * stream);
 
+/* The Bayer form of the stacking loop body for n raw u16 mosaic frames of
+ * width x height (both even): each frame's 2x2-binned luminance
+ * (average_bayer_planes, core/io/debayer.cc:277-330) is registered against
+ * the reference of `reg`, which must hold the binned reference (width/2 x
+ * height/2); then the four Bayer planes of the raw frame
+ * (extract_bayer_planes order, debayer.cc:96-147: cell positions (0,0),
+ * (0,1), (1,0), (1,1)) are warped with the registered transform (the binned
+ * and plane grids coincide) and added to acc[0..3], four width/2 x height/2
+ * accumulators: the planar form of c_weigthed_average over the 4-channel
+ * plane image. Weights, statuses, streaming and outputs as sst_stack_frames;
+ * `scale` applies to the binned and the plane values alike. */
+int sst_stack_bayer_frames(sst_ecch * reg, sst_weighted_average * const * acc, const void * frames, int n,
+    int width, int height, size_t row_stride, size_t frame_stride, double scale, int on_device,
+    int num_passes, const sst_motion_model * passes, int border, int weighting,
+    float * params_out, int32_t * status_out, float * rho_out, float * weight_out, void * stream);
+
 /* Frames per chunk used by sst_stack_frames (default 256). */
 int sst_set_chunk_frames(sst_ecch * h, int frames);
 

@@ -98,6 +98,7 @@ def lib():
             "sst_weighted_average_add_warped_batch_noalloc": (i, [p, i, i, i, i, sz, sz, d, p, p, p, p, i, p, i, i,
                                                                   p]),
             "sst_state_merge": (i, [p, p, i, sz]),
+            "sst_stack_bayer_frames": (i, [p, p, p, i, i, i, sz, sz, d, i, i, p, i, i, p, p, p, p, p]),
             "sst_bayer_average_create": (i, [p, i, i, i]),
             "sst_bayer_average_destroy": (i, [p]),
             "sst_bayer_average_clear": (i, [p, p]),
@@ -386,6 +387,35 @@ def stack_frames(reg: c_ecch, acc: c_weigthed_average, frames, passes: Sequence[
                                   scale, dev, len(passes), models, border, weighting,
                                   _ptr(outputs["params"]), _ptr(outputs["status"]), _ptr(outputs["rho"]),
                                   _ptr(outputs["weight"]), None), "sst_stack_frames")
+    return outputs
+
+
+def stack_bayer_frames(reg: c_ecch, accs: Sequence[c_weigthed_average], frames, passes: Sequence[int],
+                       scale: float, weighting: int = 1, border: int = BORDER_REFLECT101, on_device: bool = False,
+                       n=None, width=None, height=None, row_stride=None, frame_stride=None, outputs=None,
+                       host_input: bool = False):
+    """sst_stack_bayer_frames: register the binned luminance of raw u16 mosaic
+    frames and stack their four Bayer planes into accs[0..3]."""
+    if isinstance(frames, np.ndarray):
+        fr = np.ascontiguousarray(frames, np.uint16)
+        n, height, width = fr.shape
+        row_stride, frame_stride = fr.strides[1], fr.strides[0]
+        ptr = _ptr(fr)
+        dev = 0
+    else:
+        ptr = _ptr(frames)
+        dev = 0 if host_input else (1 if on_device else 0)
+    if len(accs) != 4:
+        raise ValueError("four plane accumulators are required")
+    handles = (C.c_void_p * 4)(*[a.handle.value for a in accs])
+    models = (MotionModel * len(passes))(*[motion(t) for t in passes])
+    if outputs is None:
+        outputs = {"params": np.zeros((n, 12), np.float32), "status": np.zeros(n, np.int32),
+                   "rho": np.zeros(n, np.float32), "weight": np.zeros(n, np.float32)}
+    _check(lib().sst_stack_bayer_frames(reg.handle, handles, ptr, n, width, height, row_stride, frame_stride, scale,
+                                        dev, len(passes), models, border, weighting, _ptr(outputs["params"]),
+                                        _ptr(outputs["status"]), _ptr(outputs["rho"]), _ptr(outputs["weight"]),
+                                        None), "sst_stack_bayer_frames")
     return outputs
 
 

@@ -211,6 +211,7 @@ struct sst_ecch {
   DevBuf pyr, fs, part, cnt, lists, counts, lap, init;
   DevBuf out_params, out_status, out_iters, out_eps, out_rho, out_weight, weff, coeffs;
   DevBuf res_params, res_status, res_rho, res_weight;   // whole-sequence results of sst_stack_frames
+  DevBuf binned;                     // 2x2-binned luminance of a chunk of raw Bayer frames
   size_t part_stride = 0;
   int steps_cap = 0;
   int lap_t = 0;
@@ -227,7 +228,7 @@ struct sst_ecch {
     graphs.clear();
     DevBuf * bufs[] = { &ref, &grad, &refTG, &mask, &mask_e, &refsrc, &jc_id, &hpart, &gk_in, &gk_ref, &stage[0], &stage[1],
         &pyr, &fs, &part, &cnt, &lists, &counts, &lap, &init, &out_params, &out_status, &out_iters, &out_eps,
-        &out_rho, &out_weight, &weff, &coeffs, &res_params, &res_status, &res_rho, &res_weight };
+        &out_rho, &out_weight, &weff, &coeffs, &res_params, &res_status, &res_rho, &res_weight, &binned };
     for( DevBuf * b : bufs ) b->release();
     for( auto & kv : H ) kv.second.release();
     if( ev_user ) cudaEventDestroy(ev_user);
@@ -1192,6 +1193,110 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
   SST_CK(cudaMemcpyAsync(stv.data(), h->res_status.p, (size_t) n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   SST_CK(cudaStreamSynchronize(st));
   for( int f = 0; f < n; ++f ) acc->frames += stv[f] == SST_FRAME_OK ? 1 : 0;
+  SST_TRY(release_to_user(h, stream));
+  return SST_OK;
+}
+
+/* The Bayer form of the stacking loop body: register the 2x2-binned
+ * luminance of each raw frame (average_bayer_planes, debayer.cc:277-330)
+ * against the binned reference of `h`, then warp the four Bayer planes of
+ * the raw frame (extract_bayer_planes order, debayer.cc:96-147) with the
+ * registered transform and add them to the four plane accumulators. */
+extern "C" int sst_stack_bayer_frames(sst_ecch * h, sst_weighted_average * const * acc, const void * frames, int n,
+    int width, int height, size_t row_stride, size_t frame_stride, double scale, int on_device,
+    int num_passes, const sst_motion_model * passes, int border, int weighting,
+    float * params_out, int32_t * status_out, float * rho_out, float * weight_out, void * stream)
+{
+  if( !h || !acc || !frames ) return set_error(SST_ERR_INVALID_ARG, "sst_stack_bayer_frames: NULL argument");
+  for( int k = 0; k < 4; ++k )
+    if( !acc[k] ) return set_error(SST_ERR_INVALID_ARG, "sst_stack_bayer_frames: NULL plane accumulator");
+  if( border != SST_BORDER_CONSTANT && border != SST_BORDER_REPLICATE && border != SST_BORDER_REFLECT &&
+      border != SST_BORDER_REFLECT101 )
+    return set_error(SST_ERR_UNSUPPORTED, "unsupported border mode %d", border);
+  if( h->L == 0 ) return set_error(SST_ERR_STATE, "c_ecch: no reference image was set");
+  if( n < 1 ) return set_error(SST_ERR_INVALID_ARG, "n must be >= 1");
+  if( (width & 1) || (height & 1) )
+    return set_error(SST_ERR_INVALID_ARG, "Can not average raw bayer planes for uneven image size %dx%d", width, height);
+  const int pw = width / 2, ph = height / 2;
+  if( pw != h->w || ph != h->h )
+    return set_error(SST_ERR_INVALID_ARG, "the reference must be the binned size (width/2 x height/2)");
+  for( int k = 0; k < 4; ++k )
+    if( acc[k]->w != pw || acc[k]->h != ph ) return set_error(SST_ERR_INVALID_ARG, "plane accumulators must be width/2 x height/2");
+  if( row_stride < (size_t) width * 2 || frame_stride < row_stride * height || (row_stride & 3) || (frame_stride & 3) ||
+      ((uintptr_t) frames & 3) )
+    return set_error(SST_ERR_INVALID_ARG, "invalid or misaligned strides");
+  SST_TRY(validate_passes(h, num_passes, passes));
+  if( h->o.method == M_IC || h->o.method == M_ICLM ) {
+    for( int k = 0; k < num_passes; ++k )
+      if( !model_invertible(passes[k]) )
+        return set_error(SST_ERR_UNSUPPORTED, "inverse compositional ECC requires an invertible motion model");
+  }
+  SST_TRY(ensure_streams(h));
+  SST_TRY(join_user(h, stream));
+  cudaStream_t st = h->st, cp = h->st_copy;
+  const int chunk = std::max(1, std::min(std::min(h->chunk, n), 65535));
+  const sst_motion_model & last = passes[num_passes - 1];
+  const size_t bin_frame = (size_t) pw * ph * 2;
+  if( !on_device ) {
+    SST_CK(h->stage[0].ensure(frame_stride * chunk));
+    SST_CK(h->stage[1].ensure(frame_stride * chunk));
+    SST_CK(cudaEventRecord(h->ev_free[0], st));
+    SST_CK(cudaEventRecord(h->ev_free[1], st));
+  }
+  SST_CK(h->binned.ensure(bin_frame * chunk));
+  SST_CK(h->res_params.ensure((size_t) n * 12 * sizeof(float)));
+  SST_CK(h->res_status.ensure((size_t) n * sizeof(int32_t)));
+  SST_CK(h->res_rho.ensure((size_t) n * sizeof(float)));
+  SST_CK(h->res_weight.ensure((size_t) n * sizeof(float)));
+  sst_weighted_average * a0 = acc[0];
+  SST_CK(a0->coeffs.ensure((size_t) chunk * SST_NCOEF * sizeof(float)));
+  SST_CK(a0->weff.ensure((size_t) chunk * sizeof(float)));
+  int buf = 0;
+  for( int f0 = 0; f0 < n; f0 += chunk, buf ^= 1 ) {
+    const int nc = std::min(chunk, n - f0);
+    const uint8_t * fsrc = (const uint8_t *) frames + (size_t) f0 * frame_stride;
+    const void * d_frames = fsrc;
+    if( !on_device ) {
+      SST_CK(cudaStreamWaitEvent(cp, h->ev_free[buf], 0));
+      SST_CK(cudaMemcpyAsync(h->stage[buf].p, fsrc, frame_stride * nc, cudaMemcpyHostToDevice, cp));
+      SST_CK(cudaEventRecord(h->ev_copy[buf], cp));
+      SST_CK(cudaStreamWaitEvent(st, h->ev_copy[buf], 0));
+      d_frames = h->stage[buf].p;
+    }
+    SST_CK_LAUNCH(launch_average_bayer_planes_batch(d_frames, width, height, row_stride, frame_stride, nc,
+        h->binned.as<uint16_t>(), st));
+    SST_TRY(register_device(h, h->binned.p, SST_DEPTH_U16, nc, (size_t) pw * 2, bin_frame, scale, num_passes, passes,
+        nullptr, false));
+    SST_CK_LAUNCH(launch_coeffs_from_params(last, h->out_params.as<float>(), nc, a0->coeffs.as<float>(), st));
+    SST_CK_LAUNCH(launch_effective_weights(weighting ? h->out_weight.as<float>() : nullptr, h->out_status.as<int32_t>(), nc,
+        a0->weff.as<float>(), st));
+    BayerPlanesArgs b;
+    b.frames = (const uint8_t *) d_frames;
+    b.row_stride = row_stride, b.frame_stride = frame_stride;
+    b.pw = pw, b.ph = ph, b.n = nc;
+    b.scale = (float) scale;
+    b.coeffs = a0->coeffs.as<float>();
+    b.weights = a0->weff.as<float>();
+    for( int k = 0; k < 4; ++k ) b.acc[k] = acc[k]->acc.as<float>();
+    b.plane = a0->plane();
+    b.border = border;
+    SST_CK_LAUNCH(launch_stack_bayer_planes(b, last.type, st));
+    if( !on_device ) SST_CK(cudaEventRecord(h->ev_free[buf], st));
+    SST_TRY(copy_out(h->res_params.as<float>() + (size_t) f0 * 12, h->out_params.p, (size_t) nc * 12 * sizeof(float), 1, st));
+    SST_TRY(copy_out(h->res_status.as<int32_t>() + f0, h->out_status.p, (size_t) nc * sizeof(int32_t), 1, st));
+    SST_TRY(copy_out(h->res_rho.as<float>() + f0, h->out_rho.p, (size_t) nc * sizeof(float), 1, st));
+    SST_TRY(copy_out(h->res_weight.as<float>() + f0, h->out_weight.p, (size_t) nc * sizeof(float), 1, st));
+  }
+  SST_TRY(copy_out(params_out, h->res_params.p, (size_t) n * 12 * sizeof(float), on_device, st));
+  SST_TRY(copy_out(status_out, h->res_status.p, (size_t) n * sizeof(int32_t), on_device, st));
+  SST_TRY(copy_out(rho_out, h->res_rho.p, (size_t) n * sizeof(float), on_device, st));
+  SST_TRY(copy_out(weight_out, h->res_weight.p, (size_t) n * sizeof(float), on_device, st));
+  std::vector<int32_t> stv(n);
+  SST_CK(cudaMemcpyAsync(stv.data(), h->res_status.p, (size_t) n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  SST_CK(cudaStreamSynchronize(st));
+  int added = 0;
+  for( int f = 0; f < n; ++f ) added += stv[f] == SST_FRAME_OK ? 1 : 0;
+  for( int k = 0; k < 4; ++k ) acc[k]->frames += added;
   SST_TRY(release_to_user(h, stream));
   return SST_OK;
 }

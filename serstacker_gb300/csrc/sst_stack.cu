@@ -388,4 +388,174 @@ cudaError_t launch_bayer_planes(int op, const uint16_t * src, int w, int h, size
   return cudaGetLastError();
 }
 
+/* average_bayer_planes of n mosaic frames: frame f at src + f * frame_stride,
+ * binned frame f at dst + f * (w/2) * (h/2), rows of w/2 u16 */
+__global__ void k_average_bayer_planes_batch(const uint8_t * src, int w, int h, size_t rs, size_t frame_stride,
+    uint16_t * dst)
+{
+  const int f = blockIdx.z;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  const int c4 = w / 2;
+  if( x >= c4 ) return;
+  const uint8_t * fs = src + (size_t) f * frame_stride;
+  const uint32_t r0 = __ldg((const uint32_t *) (fs + (size_t) (2 * y) * rs) + x);
+  const uint32_t r1 = __ldg((const uint32_t *) (fs + (size_t) (2 * y + 1) * rs) + x);
+  const int s = 2 + (int) (r0 & 0xffffu) + (int) (r0 >> 16) + (int) (r1 & 0xffffu) + (int) (r1 >> 16);
+  dst[((size_t) f * (h / 2) + y) * c4 + x] = (uint16_t) min(s / 4, 65535);
+}
+
+cudaError_t launch_average_bayer_planes_batch(const void * src, int w, int h, size_t rs, size_t frame_stride, int n,
+    uint16_t * dst, cudaStream_t st)
+{
+  dim3 grid((w / 2 + 127) / 128, h / 2, n);
+  k_average_bayer_planes_batch<<<grid, 128, 0, st>>>((const uint8_t *) src, w, h, rs, frame_stride, dst);
+  return cudaGetLastError();
+}
+
+/* ------------------------------------------------ Bayer planes, stacked */
+
+/* Plane k (mosaic order: k = 0 (0,0), 1 (0,1), 2 (1,0), 3 (1,1) within each
+ * 2x2 cell) of a raw mosaic is the pw x ph image plane_k(x, y) =
+ * raw(2x + (k & 1), 2y + (k >> 1)), the channels extract_bayer_planes
+ * produces (debayer.cc:96-147). The four planes of a frame share the plane
+ * transform, so they share every sample position, the remapped mask and the
+ * weight: one thread gathers the 4 x 4 raw block that holds all 16 taps of
+ * its output pixel and updates four accumulators. */
+__device__ __forceinline__ float raw_tap(const uint8_t * fb, size_t rs, int pw, int ph, int xi, int yi, int k,
+    int border)
+{
+  if( xi < 0 || xi >= pw || yi < 0 || yi >= ph ) {
+    switch ( border ) {
+    case SST_BORDER_REPLICATE: xi = clampi(xi, 0, pw - 1), yi = clampi(yi, 0, ph - 1); break;
+    case SST_BORDER_REFLECT101: xi = reflect101(xi, pw), yi = reflect101(yi, ph); break;
+    case SST_BORDER_REFLECT: xi = reflect(xi, pw), yi = reflect(yi, ph); break;
+    default: return 0.f;
+    }
+  }
+  return (float) __ldg((const uint16_t *) (fb + (size_t) (2 * yi + (k >> 1)) * rs) + 2 * xi + (k & 1));
+}
+
+template<int FAM>
+__global__ void __launch_bounds__(256) k_stack_bayer_planes(BayerPlanesArgs a)
+{
+  constexpr int VW = SA_TX + 4, VH = SA_TY + 4;
+  constexpr int PPT = SA_TX * SA_TY / 256;
+  __shared__ uint8_t s_v[VH * VW];
+  __shared__ uint8_t s_h[VH * SA_TX];
+  const int tx0 = blockIdx.x * SA_TX, ty0 = blockIdx.y * SA_TY;
+  const int lx = threadIdx.x % SA_TX, ly0 = threadIdx.x / SA_TX;
+  const int x = tx0 + lx;
+  const int wx0 = max(tx0 - 2, 0), wy0 = max(ty0 - 2, 0);
+  const int wx1 = min(tx0 + SA_TX + 1, a.pw - 1), wy1 = min(ty0 + SA_TY + 1, a.ph - 1);
+  float S[PPT][4], cS[PPT][4], Wt[PPT], cW[PPT];
+#pragma unroll
+  for( int k = 0; k < PPT; ++k ) {
+    Wt[k] = cW[k] = 0.f;
+#pragma unroll
+    for( int q = 0; q < 4; ++q ) S[k][q] = cS[k][q] = 0.f;
+  }
+  for( int f = 0; f < a.n; ++f ) {
+    const float wf = __ldg(a.weights + f);
+    if( !(wf > 0.f) ) continue;                 // uniform over the CTA
+    float c[SST_NCOEF];
+#pragma unroll
+    for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + i);
+    const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
+    if( rect_interior<FAM>(c, wx0, wy0, wx1, wy1, a.pw, a.ph) ) {
+      if( x < a.pw ) {
+#pragma unroll
+        for( int k = 0; k < PPT; ++k ) {
+          const int y = ty0 + ly0 + 4 * k;
+          if( y >= a.ph ) continue;
+          const spos s = warp_pos<FAM>(c, x, y);
+          // raw rows 2 y0 .. 2 y0 + 3, columns 2 x0 .. 2 x0 + 3 (two u32 per row)
+          const uint8_t * r = fb + (size_t) (2 * s.y0) * a.row_stride + (size_t) s.x0 * 4;
+          uint32_t q[4][2];
+#pragma unroll
+          for( int rr = 0; rr < 4; ++rr ) {
+            q[rr][0] = __ldg((const uint32_t *) (r + (size_t) rr * a.row_stride));
+            q[rr][1] = __ldg((const uint32_t *) (r + (size_t) rr * a.row_stride) + 1);
+          }
+#pragma unroll
+          for( int p = 0; p < 4; ++p ) {
+            const int dy = p >> 1, sh = (p & 1) * 16;
+            const float v00 = (float) ((q[dy][0] >> sh) & 0xffffu), v01 = (float) ((q[dy][1] >> sh) & 0xffffu);
+            const float v10 = (float) ((q[dy + 2][0] >> sh) & 0xffffu), v11 = (float) ((q[dy + 2][1] >> sh) & 0xffffu);
+            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+            kahan_add(S[k][p], cS[k][p], wf * (fmaf(s.fy, t1 - t0, t0) * a.scale));
+          }
+          kahan_add(Wt[k], cW[k], wf);
+        }
+      }
+      continue;
+    }
+    for( int q = threadIdx.x; q < VW * VH; q += 256 ) {
+      const int qx = tx0 - 2 + q % VW, qy = ty0 - 2 + q / VW;
+      uint8_t v = 1;
+      if( qx >= 0 && qx < a.pw && qy >= 0 && qy < a.ph ) {
+        v = mask_ok(coverage(a.pw, a.ph, warp_pos<FAM>(c, qx, qy)), 255) ? 1 : 0;
+      }
+      s_v[q] = v;
+    }
+    __syncthreads();
+    for( int q = threadIdx.x; q < SA_TX * VH; q += 256 ) {
+      const int xx = q % SA_TX, yy = q / SA_TX;
+      const uint8_t * p = s_v + yy * VW + xx;
+      s_h[yy * SA_TX + xx] = p[0] & p[1] & p[2] & p[3] & p[4];
+    }
+    __syncthreads();
+    if( x < a.pw ) {
+#pragma unroll
+      for( int k = 0; k < PPT; ++k ) {
+        const int ly = ly0 + 4 * k, y = ty0 + ly;
+        if( y >= a.ph ) continue;
+        const uint8_t * pm = s_h + ly * SA_TX + lx;
+        if( pm[0] & pm[SA_TX] & pm[2 * SA_TX] & pm[3 * SA_TX] & pm[4 * SA_TX] ) {
+          const spos s = warp_pos<FAM>(c, x, y);
+#pragma unroll
+          for( int p = 0; p < 4; ++p ) {
+            const float v00 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0, s.y0, p, a.border);
+            const float v01 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0 + 1, s.y0, p, a.border);
+            const float v10 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0, s.y0 + 1, p, a.border);
+            const float v11 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0 + 1, s.y0 + 1, p, a.border);
+            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+            kahan_add(S[k][p], cS[k][p], wf * (fmaf(s.fy, t1 - t0, t0) * a.scale));
+          }
+          kahan_add(Wt[k], cW[k], wf);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if( x < a.pw ) {
+#pragma unroll
+    for( int k = 0; k < PPT; ++k ) {
+      const int y = ty0 + ly0 + 4 * k;
+      if( y >= a.ph ) continue;
+      const size_t i = (size_t) y * a.pw + x;
+#pragma unroll
+      for( int p = 0; p < 4; ++p ) {
+        float * P = a.acc[p];
+        float gS = P[i], gcS = P[a.plane + i], gW = P[2 * a.plane + i], gcW = P[3 * a.plane + i];
+        kahan_add(gS, gcS, S[k][p]);
+        gcS += cS[k][p];
+        kahan_add(gW, gcW, Wt[k]);
+        gcW += cW[k];
+        P[i] = gS, P[a.plane + i] = gcS, P[2 * a.plane + i] = gW, P[3 * a.plane + i] = gcW;
+      }
+    }
+  }
+}
+
+cudaError_t launch_stack_bayer_planes(const BayerPlanesArgs & a, int motion, cudaStream_t st)
+{
+  dim3 grid((a.pw + SA_TX - 1) / SA_TX, (a.ph + SA_TY - 1) / SA_TY);
+  switch ( motion_family(motion) ) {
+  case FAM_AFFINE: k_stack_bayer_planes<FAM_AFFINE><<<grid, 256, 0, st>>>(a); break;
+  case FAM_HOMOG: k_stack_bayer_planes<FAM_HOMOG><<<grid, 256, 0, st>>>(a); break;
+  default: k_stack_bayer_planes<FAM_QUAD><<<grid, 256, 0, st>>>(a); break;
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace sst

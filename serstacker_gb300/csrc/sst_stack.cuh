@@ -22,6 +22,20 @@ struct StackArgs {
   int border;               // image border mode of the remap (SST_BORDER_*)
 };
 
+/* four Bayer planes of raw u16 mosaic frames, stacked into four accumulators */
+struct BayerPlanesArgs {
+  const uint8_t * frames;   // raw mosaic frame 0 (u16)
+  size_t row_stride, frame_stride;
+  int pw, ph;               // plane size = raw size / 2 = accumulator size
+  int n;
+  float scale;
+  const float * coeffs;     // n x 16, plane coordinates
+  const float * weights;    // n effective weights
+  float * acc[4];           // 4 planes (S, cS, W, cW) per Bayer plane
+  size_t plane;
+  int border;
+};
+
 cudaError_t launch_coeffs_from_params(const sst_motion_model & m, const float * params, int n, float * coeffs, cudaStream_t st);
 cudaError_t launch_effective_weights(const float * weights, const int32_t * status, int n, float * out, cudaStream_t st);
 cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, cudaStream_t st);
@@ -31,6 +45,9 @@ cudaError_t launch_stack_compute(const float * acc, size_t plane, int n, float *
 cudaError_t launch_stack_reinit(float * acc, size_t plane, int n, const float * avg, const float * accw, cudaStream_t st);
 cudaError_t launch_remap(const void * src, int depth, int sw, int sh, size_t rs, double scale, int motion,
     const float * coeffs, int border, float * dst, uint8_t * dst_mask, int dw, int dh, cudaStream_t st);
+cudaError_t launch_average_bayer_planes_batch(const void * src, int w, int h, size_t rs, size_t frame_stride, int n,
+    uint16_t * dst, cudaStream_t st);
+cudaError_t launch_stack_bayer_planes(const BayerPlanesArgs & a, int motion, cudaStream_t st);
 cudaError_t launch_bayer_planes(int op, const uint16_t * src, int w, int h, size_t rs, uint16_t * dst, cudaStream_t st);
 
 }  // namespace sst

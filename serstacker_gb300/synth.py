@@ -43,6 +43,17 @@ def scene_config1() -> Scene:
     return Scene(1280, 960, 360.0)
 
 
+def scene_bayer() -> Scene:
+    """Raw 12-bit RGGB mosaic scene: the config-0 scene scaled to 3096x2080
+    (disk radius and band period scaled by the width ratio), peak 1500 ADU."""
+    f = 3096 / 640.0
+    return Scene(3096, 2080, 180.0 * f, edge_sigma=2.0 * f, band_period=24.0 * f, peak=1500.0)
+
+
+# RGGB cell gains (R, G / G, B) applied to the mosaic: the channels differ in level
+BAYER_GAINS = ((1.0, 0.7), (0.7, 0.45))
+
+
 def _erfc_np(x):
     from scipy.special import erfc
     return erfc(x)
@@ -102,10 +113,14 @@ def random_warps(rng, n: int, kind: str):
     config0: euclidean about (0,0): tx,ty ~ U(-8,8), theta ~ N(0, 0.5 deg)
     config1: homography: the config0 euclidean part, scale 1+U(-0.005,0.005),
              projective terms U(-2e-6, 2e-6) per pixel
+    translation: tx,ty ~ U(-8,8) only
     """
     Hs = np.zeros((n, 3, 3))
     for i in range(n):
         tx, ty = rng.uniform(-8, 8, size=2)
+        if kind == "translation":
+            Hs[i] = np.array([[1.0, 0, tx], [0, 1.0, ty], [0, 0, 1.0]])
+            continue
         th = math.radians(rng.normal(0.0, 0.5))
         c, s = math.cos(th), math.sin(th)
         H = np.array([[c, -s, tx], [s, c, ty], [0, 0, 1.0]])
@@ -134,12 +149,14 @@ def make_sequence_np(sc: Scene, n: int, seed: int, kind: str = "config0", dtype=
 # --------------------------------------------------------------------------- torch back end
 
 def make_sequence_torch(sc: Scene, n: int, seed: int, kind: str = "config1", gain: float = 64.0,
-                        blur_range=(0.8, 2.5), read_sigma: float = 2.0, device="cuda", chunk: int = 64):
-    """Full-size u16 sequences generated on the device (bench workloads).
+                        blur_range=(0.8, 2.5), read_sigma: float = 2.0, device="cuda", chunk: int = 64,
+                        cell_gains=None, maxval: int = 65535):
+    """Full-size sequences generated on the device (bench workloads).
 
-    Same formulas as the numpy back end; returns (frames uint16 tensor stored as
-    int16 bit patterns? no: torch has uint16 since 2.3, so uint16), warps (n,3,3)
-    float64 numpy, blurs numpy.
+    Same formulas as the numpy back end. ``cell_gains`` (2x2) multiplies the
+    radiance per mosaic cell before the noise (raw Bayer frames); counts are
+    clipped to [0, maxval]. Returns (frames as an int32 tensor holding the
+    unsigned values, warps (n, 3, 3) float64 numpy, blurs numpy).
     """
     import torch
     rng = np.random.default_rng(seed)
@@ -164,8 +181,11 @@ def make_sequence_torch(sc: Scene, n: int, seed: int, kind: str = "config1", gai
         amp = sc.band_amp * torch.exp(-2.0 * math.pi ** 2 * (sc.edge_sigma ** 2 + bl ** 2) / sc.band_period ** 2)
         bands = 1.0 + amp * torch.sin(2.0 * math.pi * (Y - cy) / sc.band_period)
         img = sc.peak * disk * bands / (1.0 + sc.band_amp)
+        if cell_gains is not None:
+            cg = torch.as_tensor(np.asarray(cell_gains, np.float64), device=device)
+            img = img * cg.repeat(sc.height // 2 + 1, sc.width // 2 + 1)[:sc.height, :sc.width]
         counts = torch.poisson(img.clamp_min(0), generator=g)
         counts = counts + read_sigma * torch.randn(counts.shape, generator=g, device=device, dtype=counts.dtype)
-        out[b0:b1] = torch.clamp(torch.round(counts * gain), 0, 65535).to(torch.int32)
+        out[b0:b1] = torch.clamp(torch.round(counts * gain), 0, maxval).to(torch.int32)
         del w, X, Y, r, disk, bands, img, counts
     return out, Hs, blurs

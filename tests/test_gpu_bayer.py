@@ -156,3 +156,102 @@ def test_bayer_state_roundtrip(gpu):
     assert b.accumulated_frames() == 0
     with pytest.raises(C.SSTError):
         b.compute()
+
+
+def _raw_sequence(n, W, H, seed):
+    """raw RGGB u16 12-bit mosaic frames of a scene translated by up to
+    +-6 raw px, Poisson-like noise; returns frames, reference mosaic, shifts"""
+    rng = np.random.default_rng(seed)
+    sc = synth.Scene(W, H, 0.3 * min(W, H))
+    g = np.array([[1.0, 0.7], [0.7, 0.45]])
+    gains = np.tile(g, (H // 2, W // 2))
+    shifts = rng.uniform(-6, 6, size=(n, 2))
+    frames = np.empty((n, H, W), np.uint16)
+    for i in range(n):
+        Hm = np.eye(3)
+        Hm[0, 2], Hm[1, 2] = shifts[i]
+        img = synth.render_frame_np(sc, Hm, 1.0) * 12.0 * gains
+        img = rng.poisson(np.maximum(img, 0)).astype(np.float64) + rng.normal(0, 2.0, size=img.shape)
+        frames[i] = np.clip(np.rint(img), 0, 4095).astype(np.uint16)
+    ref = np.clip(np.rint(synth.reference_np(sc) * 12.0 * gains), 0, 4095).astype(np.uint16)
+    return frames, ref, shifts
+
+
+def test_stack_bayer_frames_matches_oracle(gpu, oracle):
+    """Binned-luminance registration + four-plane stack (sst_stack_bayer_frames)
+    against the oracle: registration within 0.02 px RMS of the oracle's
+    c_ecch on the same binned frames, plane stacks within 1e-5 relative of
+    FP64 sums of the bit-exact extracted planes under the same transforms."""
+    C, O = gpu, oracle
+    W, H, n = 256, 192, 6
+    pw, ph = W // 2, H // 2
+    frames, ref_raw, shifts = _raw_sequence(n, W, H, 21)
+    scale = 1.0 / 4096
+    ref_bin = O.average_bayer_planes(ref_raw)
+    opts = C.default_options(method=C.IC, maxlevel=2, max_iterations=40, epsx=0.01, minimum_image_size=16,
+                             min_rho=0.5)
+    reg = C.c_ecch(opts)
+    reg.set_reference_image(ref_bin.astype(np.float32), scale=scale)
+    accs = [C.c_weigthed_average(pw, ph) for _ in range(4)]
+    out = C.stack_bayer_frames(reg, accs, frames, [C.TRANSLATION], scale, weighting=1)
+    assert (out["status"] == 0).all(), out["status"]
+    # registration: GPU vs the oracle's c_ecch on the oracle-binned frames
+    oo = O.ecch_opts(method=1, maxlevel=2, max_iterations=40, epsx=0.01, minimum_image_size=16)
+    m = O.model(C.TRANSLATION)
+    for i in range(n):
+        b = O.average_bayer_planes(frames[i]).astype(np.float64) * scale
+        s_o, _, _ = O.ecch_align(m, O.identity(m), ref_bin.astype(np.float64) * scale, b, oo)
+        p_o = O.get_params(m, s_o)
+        assert np.hypot(*(p_o - out["params"][i][:2])) <= 0.02, (i, p_o, out["params"][i][:2])
+        # and close to the true shift (raw px / 2)
+        assert np.hypot(*(out["params"][i][:2] - shifts[i] / 2)) <= 0.1
+    # stacks: the same transforms applied to the extracted planes, in FP64
+    planes = np.stack([O.extract_bayer_planes(frames[i]) for i in range(n)])     # (n, ph, pw, 4)
+    for k in range(4):
+        S = np.zeros((ph, pw))
+        Wt = np.zeros((ph, pw))
+        for i in range(n):
+            st = O.set_params(m, O.identity(m), out["params"][i][:2].astype(np.float64))
+            dst, msk = O.stack_remap(m, st, planes[i, ..., k].astype(np.float64) * scale, pw, ph)
+            wt = np.where(msk > 0, float(out["weight"][i]), 0.0)
+            S += wt * dst
+            Wt += wt
+        st_g, nf = accs[k].save_state()
+        assert nf == n
+        Sg = st_g[0].astype(np.float64) + st_g[1]
+        Wg = st_g[2].astype(np.float64) + st_g[3]
+        _check(Sg[..., None], Wg[..., None], S[..., None], Wt[..., None])
+
+
+def test_stack_bayer_frames_device_and_host_inputs_agree(gpu):
+    """The streamed host path and the device-resident path give identical
+    planes for the same chunking (chunks of 3 frames: the compensated
+    register sums are folded into the planes once per chunk)."""
+    import torch
+    C = gpu
+    W, H, n = 128, 96, 7
+    frames, ref_raw, _ = _raw_sequence(n, W, H, 4)
+    scale = 1.0 / 4096
+    from oracle import average_bayer_planes
+    ref_bin = average_bayer_planes(ref_raw)
+    opts = C.default_options(method=C.IC, maxlevel=2, max_iterations=30, epsx=0.01, minimum_image_size=16)
+    states = []
+    for dev in (False, True):
+        reg = C.c_ecch(opts)
+        reg.set_reference_image(ref_bin.astype(np.float32), scale=scale)
+        reg.set_chunk_frames(3)
+        accs = [C.c_weigthed_average(W // 2, H // 2) for _ in range(4)]
+        if dev:
+            d = torch.from_numpy(frames.view(np.int16)).cuda()
+            outs = {"params": torch.zeros((n, 12), dtype=torch.float32, device="cuda"),
+                    "status": torch.zeros(n, dtype=torch.int32, device="cuda"),
+                    "rho": torch.zeros(n, dtype=torch.float32, device="cuda"),
+                    "weight": torch.zeros(n, dtype=torch.float32, device="cuda")}
+            C.stack_bayer_frames(reg, accs, d, [C.TRANSLATION], scale, on_device=True, n=n, width=W, height=H,
+                                 row_stride=W * 2, frame_stride=W * H * 2, outputs=outs)
+            torch.cuda.synchronize()
+        else:
+            C.stack_bayer_frames(reg, accs, frames, [C.TRANSLATION], scale)
+        states.append([a.save_state()[0] for a in accs])
+    for k in range(4):
+        assert np.array_equal(states[0][k], states[1][k]), k
