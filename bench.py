@@ -230,8 +230,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form leg (profiling runs)")
-    ap.add_argument("--workload", choices=["mono", "bayer"], default="mono",
-                    help="mono: the headline 1280x960 sequence; bayer: raw RGGB 3096x2080 frames")
+    ap.add_argument("--workload", choices=["mono", "bayer", "roi"], default="mono",
+                    help="mono: the headline 1280x960 sequence; bayer: raw RGGB 3096x2080 frames; "
+                         "roi: uneven-ROI crops (--frames crops)")
+    ap.add_argument("--roi-method", choices=["fa", "lm"], default="fa")
+    ap.add_argument("--roi-sample", type=int, default=8, help="crops checked against the oracle")
     args = ap.parse_args()
 
     ws, rank, local = dist_env()
@@ -247,8 +250,8 @@ def main():
             import torch.distributed as dist
             dist.destroy_process_group()
         return
-    if args.workload == "bayer":
-        main_bayer(args, ws, rank, local)
+    if args.workload in ("bayer", "roi"):
+        (main_bayer if args.workload == "bayer" else main_roi)(args, ws, rank, local)
         if ws > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
@@ -601,6 +604,185 @@ def main_bayer(args, ws, rank, local):
                              "translation_err_vs_truth_px_max": float(np.max(err)) if err.size else None,
                              "frames_ok": int(ok.sum())},
                 "levels": level_table}
+        print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ ROI workload
+
+ROI_CANVAS = 4096
+
+
+def roi_cfg(n: int, method: str):
+    return {
+        "workload": f"{n} f32 crops, width and height ~ U(128, 1024) independently, cut from a {ROI_CANVAS}^2 "
+                    "tiled banded-disk scene; each crop registered against its own reference crop by c_ecch "
+                    f"({method}, QUADRATIC 12-parameter motion, 4 levels, epsx 0.01, 50 iterations); warps: "
+                    "translation U(-12, 12) px, scale 1 + U(-0.01, 0.01), quadratic terms <= 1 px at the corner",
+        "crops": n, "method": method, "motion": "QUADRATIC", "levels": 4, "epsx": 0.01, "max_iterations": 50,
+        "l2": "pools (2 x ~5.4 GB) stream from HBM every step; no flush needed",
+    }
+
+
+def tiled_scene_torch(X, Y):
+    """banded disks (radius 200, edge sigma 2, bands of period 24) tiled every
+    512 px over a faint two-frequency ripple, so that every crop has texture"""
+    import torch
+    P, Rd, es = 512.0, 200.0, 2.0
+    cx = torch.remainder(X, P) - P / 2
+    cy = torch.remainder(Y, P) - P / 2
+    r = torch.hypot(cx, cy)
+    disk = 0.5 * torch.special.erfc((r - Rd) / (math.sqrt(2.0) * es))
+    amp = 0.2 * math.exp(-2.0 * math.pi ** 2 * es ** 2 / 24.0 ** 2)
+    bands = 1.0 + amp * torch.sin(2 * math.pi * cy / 24.0)
+    ripple = 20.0 * (1.0 + 0.5 * torch.sin(2 * math.pi * X / 37.0) * torch.sin(2 * math.pi * Y / 53.0))
+    return 200.0 * disk * bands / 1.2 + ripple
+
+
+def make_roi_workload(n: int, device, seed: int = SEED + 1):
+    """crop sizes, offsets and quadratic warps (seeded), rendered on the device into two packed pools"""
+    import torch
+    rng = np.random.default_rng(seed)
+    ws = rng.integers(128, 1025, size=n)
+    hs = rng.integers(128, 1025, size=n)
+    ox = rng.uniform(16, ROI_CANVAS - 16 - ws)
+    oy = rng.uniform(16, ROI_CANVAS - 16 - hs)
+    t = rng.uniform(-12, 12, size=(n, 2))
+    sc = 1.0 + rng.uniform(-0.01, 0.01, size=n)
+    qx = rng.uniform(-1, 1, size=(n, 3))      # x*y, x*x, y*y terms, scaled to <= 1 px at the corner
+    qy = rng.uniform(-1, 1, size=(n, 3))
+    sizes = ws * hs
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    ref_pool = torch.empty(int(offs[-1]), dtype=torch.float32, device=device)
+    cur_pool = torch.empty(int(offs[-1]), dtype=torch.float32, device=device)
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    for i in range(n):
+        w, h = int(ws[i]), int(hs[i])
+        y, x = torch.meshgrid(torch.arange(h, device=device, dtype=torch.float64),
+                              torch.arange(w, device=device, dtype=torch.float64), indexing="ij")
+        ref_pool[offs[i]:offs[i + 1]] = tiled_scene_torch(x + ox[i], y + oy[i]).reshape(-1).float()
+        d = 3.0 * float(max(w, h)) ** 2
+        X = sc[i] * x + t[i, 0] + (qx[i, 0] * x * y + qx[i, 1] * x * x + qx[i, 2] * y * y) / d
+        Y = sc[i] * y + t[i, 1] + (qy[i, 0] * x * y + qy[i, 1] * x * x + qy[i, 2] * y * y) / d
+        img = tiled_scene_torch(X + ox[i], Y + oy[i])
+        img = img + torch.randn(img.shape, generator=g, device=device, dtype=img.dtype)
+        cur_pool[offs[i]:offs[i + 1]] = img.reshape(-1).float()
+    return ref_pool, cur_pool, ws, hs, offs
+
+
+def main_roi(args, ws_, rank, local):
+    import torch
+    from serstacker_gb300 import capi as C
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    C.lib()
+    n = args.frames
+    method = C.FA if args.roi_method == "fa" else C.LM
+    ref_pool, cur_pool, wv, hv, offs = make_roi_workload(n, device)
+    rois = (C.Roi * n)()
+    for i in range(n):
+        rois[i] = C.Roi(int(offs[i]) * 4, int(offs[i]) * 4, int(wv[i]) * 4, int(wv[i]) * 4, int(wv[i]), int(hv[i]))
+    opts = C.default_options(method=method, maxlevel=4, max_iterations=50, epsx=0.01, minimum_image_size=16)
+    rb = C.c_roi_batch(opts)
+    outs = {"params": torch.zeros((n, 12), dtype=torch.float32, device=device),
+            "status": torch.zeros(n, dtype=torch.int32, device=device),
+            "iterations": torch.zeros(n, dtype=torch.int32, device=device),
+            "eps": torch.zeros(n, dtype=torch.float32, device=device),
+            "rho": torch.zeros(n, dtype=torch.float32, device=device)}
+
+    def step():
+        rb.align_device(n, rois, ref_pool, cur_pool, C.DEPTH_F32, [C.QUADRATIC], 1.0, outs)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(ws_)
+    torch.cuda.synchronize()
+    C.kernel_launch_count(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(ws_)
+    launches = C.kernel_launch_count()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, ws_)
+    clk = clocks.stop()
+    value = ws_ * n / (ms / 1000.0)
+    # dominant kernel: the level-0 stencil passes
+    peak, peak_kind = measured_peaks()
+    t0_ms, fi0, px0, ab0 = rb.level_stats(0, 0)
+    levels = []
+    for lvl in range(4):
+        try:
+            t, fi, px, ab = rb.level_stats(0, lvl)
+        except C.SSTError:
+            break
+        levels.append({"level": lvl, "ms": t, "frame_iterations": fi, "pixel_iterations": px, "alg_bytes": ab})
+    M = 12
+    nH = M * (M + 1) // 2
+    flops_px = 2 * nH + 4 * M + M if method == C.FA else 2 * nH + 2 * M + 2
+    achieved = ab0 / (t0_ms / 1000.0) / 1e9 if t0_ms > 0 else 0.0
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    fp32_peak = sms * 128 * 2 * (clk["sm_max_mhz"] if clk else 2070.0) * 1e6 / 1e12
+    tflops = flops_px * px0 / (t0_ms / 1000.0) / 1e12 if t0_ms > 0 else 0.0
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "k_pass_stencil<ROI> level 0, all crops x iterations",
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+            "alg_bytes_model": "8 B per pixel-iteration (warped source + template; gradients on chip)",
+            "fp32": {"achieved_tflops": tflops, "nominal_peak_tflops": fp32_peak, "frac": tflops / fp32_peak,
+                     "flops_per_pixel_iteration": flops_px,
+                     "note": "M = 12: the Hessian and projection FMAs make the pass FP32-bound"}}
+    res = {k: v.cpu().numpy() for k, v in outs.items()}
+
+    # accuracy against the FP64 oracle on a sample of crops, and the CPU baseline on the same sample
+    acc = None
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle as O
+        O.build()
+        threads = os.cpu_count() or 1
+        O.set_num_threads(threads)
+        m = O.model(O.QUADRATIC)
+        oo = O.ecch_opts(method=method, maxlevel=4, max_iterations=50, epsx=0.01, minimum_image_size=16)
+        k = max(1, min(args.roi_sample, n))
+        rp, cp = ref_pool.cpu().numpy(), cur_pool.cpu().numpy()
+        rms_l = []
+        t0 = time.perf_counter()
+        states = []
+        for i in range(k):
+            w, h = int(wv[i]), int(hv[i])
+            r = rp[offs[i]:offs[i + 1]].reshape(h, w).astype(np.float64)
+            c = cp[offs[i]:offs[i + 1]].reshape(h, w).astype(np.float64)
+            s_o, _, _ = O.ecch_align(m, O.identity(m), r, c, oo)
+            states.append(s_o)
+        dt = time.perf_counter() - t0
+        for i in range(k):
+            w, h = int(wv[i]), int(hv[i])
+            s_g = O.set_params(m, O.identity(m), res["params"][i][:12].astype(np.float64))
+            ys, xs = np.mgrid[0:h:16, 0:w:16]
+            d2 = [(np.subtract(O.warp(m, states[i], float(x), float(y)), O.warp(m, s_g, float(x), float(y))) ** 2).sum()
+                  for y, x in zip(ys.ravel(), xs.ravel())]
+            rms_l.append(math.sqrt(float(np.mean(d2))))
+        fin = [v for v in rms_l if math.isfinite(v)]
+        acc = {"warp_rms_vs_oracle_px_median": float(np.median(fin)) if fin else None,
+               "warp_rms_vs_oracle_px_max": float(max(fin)) if fin else None,
+               "sample_crops": k, "oracle_nonfinite": len(rms_l) - len(fin),
+               "status_sample": [int(v) for v in res["status"][:k]]}
+        cpu = {"value": k / dt, "unit": "crops/s", "cores": threads, "kind": "port",
+               "sample": f"the first {k} crops (oracle FP64 c_ecch, OpenMP, {dt:.1f} s)"}
+    if rank == 0:
+        line = {"metric": "crops/sec registered (uneven-ROI batch, quadratic c_ecch)", "value": value,
+                "unit": "crops/s", "n_gpus": ws_, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": {**roi_cfg(n, "FORWARD_ADDITIVE" if method == C.FA else "LM"),
+                                                "parallelism": f"replicas x{ws_}"},
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+                "accuracy": acc, "frames_ok": int((res["status"] == 0).sum()),
+                "iterations_median": float(np.median(res["iterations"])), "levels": levels}
         print(json.dumps(line), flush=True)
 
 

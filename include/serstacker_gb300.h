@@ -294,6 +294,43 @@ int sst_extract_bayer_planes_u16(const uint16_t * src, int width, int height, si
 int sst_average_bayer_planes_u16(const uint16_t * src, int width, int height, size_t row_stride,
     uint16_t * dst, void * stream);
 
+/* ------------------------------------------------------------ ROI batches */
+
+/* One crop of a ROI batch: its reference and current images (same size),
+ * as byte offsets into the reference and current pools with row strides. */
+typedef struct sst_roi {
+  int64_t ref_offset, cur_offset;
+  int64_t ref_row_stride, cur_row_stride;
+  int32_t width, height;
+} sst_roi;
+
+typedef struct sst_roi_batch sst_roi_batch;
+
+/* A batch of independent c_ecch problems (ecc2.h:158-308): crop i is
+ * registered against its own reference crop exactly as c_ecch(options)
+ * with set_reference_image(reference crop) and align(current crop) would
+ * (ecc2.cc:984-1176), for crops of different sizes in one schedule. The
+ * options' method must be SST_ECC_FORWARD_ADDITIVE or SST_ECC_LM (the
+ * quadratic models are not invertible, so IC and IC-LM cannot run them:
+ * ecc2.cc:1702-1705). */
+int sst_roi_batch_create(sst_roi_batch ** out, const sst_ecch_options * options);
+int sst_roi_batch_destroy(sst_roi_batch * h);
+
+/* Registers n crops (1..65535). Pools and outputs are host or device
+ * memory per on_device; init_params (n x 12, NULL: identity) seeds the first
+ * pass. Outputs per crop as sst_ecch_align_batch: params (n x 12), status,
+ * iterations, eps, rho (min_rho gate of the options). Any output may be NULL. */
+int sst_roi_batch_align(sst_roi_batch * h, int n, const sst_roi * rois, const void * ref_pool,
+    const void * cur_pool, int depth, double scale, int on_device, int num_passes,
+    const sst_motion_model * passes, const float * init_params, float * params_out, int32_t * status_out,
+    int32_t * iters_out, float * eps_out, float * rho_out, void * stream);
+
+/* Timing of one pass / level of the last call (CUDA events around its
+ * launches), the frame-iterations and pixel-iterations it executed, and their
+ * algorithmic bytes (8 per pixel-iteration: warped source and template). */
+int sst_roi_batch_level_stats(sst_roi_batch * h, int pass, int level, float * ms, double * frame_iterations,
+    double * pixel_iterations, double * algorithmic_bytes);
+
 /* ------------------------------------------------ Bayer mosaic accumulator */
 
 typedef struct sst_bayer_average sst_bayer_average;

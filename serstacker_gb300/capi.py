@@ -98,6 +98,10 @@ def lib():
             "sst_weighted_average_add_warped_batch_noalloc": (i, [p, i, i, i, i, sz, sz, d, p, p, p, p, i, p, i, i,
                                                                   p]),
             "sst_state_merge": (i, [p, p, i, sz]),
+            "sst_roi_batch_create": (i, [p, p]),
+            "sst_roi_batch_destroy": (i, [p]),
+            "sst_roi_batch_align": (i, [p, i, p, p, p, i, d, i, i, p, p, p, p, p, p, p, p]),
+            "sst_roi_batch_level_stats": (i, [p, i, i, p, p, p, p]),
             "sst_stack_bayer_frames": (i, [p, p, p, i, i, i, sz, sz, d, i, i, p, i, i, p, p, p, p, p]),
             "sst_bayer_average_create": (i, [p, i, i, i]),
             "sst_bayer_average_destroy": (i, [p]),
@@ -218,6 +222,85 @@ class c_ecch:
         M = nparams(passes[-1])
         return {"params": params[:, :M], "status": status, "iterations": iters, "eps": eps, "rho": rho,
                 "weight": weight}
+
+
+class Roi(C.Structure):
+    _fields_ = [("ref_offset", C.c_int64), ("cur_offset", C.c_int64), ("ref_row_stride", C.c_int64),
+                ("cur_row_stride", C.c_int64), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+def pack_rois(refs, curs):
+    """Pack lists of same-dtype 2D crops (reference i and current i of equal
+    size) into two contiguous pools; returns (ref_pool, cur_pool, Roi array)."""
+    if len(refs) != len(curs) or not refs:
+        raise ValueError("refs and curs must be non-empty lists of equal length")
+    dt = np.asarray(refs[0]).dtype
+    sizes = [np.asarray(r).size for r in refs]
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    ref_pool = np.empty(int(offs[-1]), dt)
+    cur_pool = np.empty(int(offs[-1]), dt)
+    rois = (Roi * len(refs))()
+    for i, (r, c) in enumerate(zip(refs, curs)):
+        r = np.asarray(r, dt)
+        c = np.asarray(c, dt)
+        if r.shape != c.shape:
+            raise ValueError(f"crop {i}: reference and current sizes differ")
+        hh, ww = r.shape
+        ref_pool[offs[i]:offs[i + 1]] = r.ravel()
+        cur_pool[offs[i]:offs[i + 1]] = c.ravel()
+        b = dt.itemsize
+        rois[i] = Roi(int(offs[i]) * b, int(offs[i]) * b, ww * b, ww * b, ww, hh)
+    return ref_pool, cur_pool, rois
+
+
+class c_roi_batch:
+    """A batch of independent c_ecch problems of different sizes (crop i
+    registered against reference crop i) over sst_roi_batch_*."""
+
+    def __init__(self, options: EcchOptions):
+        self._h = C.c_void_p()
+        _check(lib().sst_roi_batch_create(C.byref(self._h), C.byref(options)), "sst_roi_batch_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_roi_batch_destroy(h)
+            self._h = C.c_void_p()
+
+    def align(self, refs, curs, passes: Sequence[int], scale: float = 1.0, init_params=None):
+        ref_pool, cur_pool, rois = pack_rois(refs, curs)
+        n = len(refs)
+        models = (MotionModel * len(passes))(*[motion(t) for t in passes])
+        ip = None
+        if init_params is not None:
+            ip = np.zeros((n, 12), np.float32)
+            pp = np.asarray(init_params, np.float32).reshape(n, -1)
+            ip[:, :pp.shape[1]] = pp
+        out = {"params": np.zeros((n, 12), np.float32), "status": np.zeros(n, np.int32),
+               "iterations": np.zeros(n, np.int32), "eps": np.zeros(n, np.float32), "rho": np.zeros(n, np.float32)}
+        _check(lib().sst_roi_batch_align(self._h, n, rois, _ptr(ref_pool), _ptr(cur_pool), _NP_DEPTH[ref_pool.dtype],
+                                         scale, 0, len(passes), models, _ptr(ip), _ptr(out["params"]),
+                                         _ptr(out["status"]), _ptr(out["iterations"]), _ptr(out["eps"]),
+                                         _ptr(out["rho"]), None), "sst_roi_batch_align")
+        return out
+
+    def align_device(self, n, rois, ref_pool, cur_pool, depth, passes: Sequence[int], scale: float, outputs,
+                     init_params=None):
+        """Device-resident pools (torch tensors or pointers) and outputs."""
+        models = (MotionModel * len(passes))(*[motion(t) for t in passes])
+        _check(lib().sst_roi_batch_align(self._h, n, rois, _ptr(ref_pool), _ptr(cur_pool), depth, scale, 1,
+                                         len(passes), models, _ptr(init_params), _ptr(outputs.get("params")),
+                                         _ptr(outputs.get("status")), _ptr(outputs.get("iterations")),
+                                         _ptr(outputs.get("eps")), _ptr(outputs.get("rho")), None),
+               "sst_roi_batch_align")
+        return outputs
+
+    def level_stats(self, pass_index: int, level: int):
+        ms = C.c_float()
+        fi, px, ab = C.c_double(), C.c_double(), C.c_double()
+        _check(lib().sst_roi_batch_level_stats(self._h, pass_index, level, C.byref(ms), C.byref(fi), C.byref(px),
+                                               C.byref(ab)), "level_stats")
+        return ms.value, fi.value, px.value, ab.value
 
 
 class c_weigthed_average:

@@ -27,6 +27,7 @@
 
 #include "sst_engine.cuh"
 #include "sst_stack.cuh"
+#include "sst_host.h"
 
 using namespace sst;
 
@@ -129,52 +130,6 @@ extern "C" void sst_ecch_options_default(sst_ecch_options * o)
 
 namespace {
 
-struct DevBuf {
-  void * p = nullptr;
-  size_t n = 0;
-  cudaError_t ensure(size_t bytes)
-  {
-    if( bytes <= n && p ) return cudaSuccess;
-    release();
-    if( bytes == 0 ) bytes = 16;
-    cudaError_t e = cudaMalloc(&p, bytes);
-    if( e == cudaSuccess ) n = bytes;
-    else p = nullptr;
-    return e;
-  }
-  void release()
-  {
-    if( p ) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  template<class T> T * as() const { return (T *) p; }
-};
-
-inline int depth_bytes(int depth)
-{
-  switch ( depth ) {
-  case SST_DEPTH_U8: return 1;
-  case SST_DEPTH_U16: return 2;
-  case SST_DEPTH_F32: return 4;
-  }
-  return 0;
-}
-
-/* getGaussianKernel(ksize, sigma > 0) with c_ecch's ksize rule (ecc2.cc:1001-1003) */
-inline int gaussian_kernel(double sigma, float * k)
-{
-  const int n = std::max(3, 2 * ((int) (3 * sigma)) + 1);
-  double t[64], sum = 0;
-  for( int i = 0; i < n && i < 64; ++i ) {
-    const double x = i - (n - 1) * 0.5;
-    t[i] = exp(-0.5 * x * x / (sigma * sigma));
-    sum += t[i];
-  }
-  for( int i = 0; i < n && i < 64; ++i ) k[i] = (float) (t[i] / sum);
-  return n;
-}
-
 struct GraphEntry {
   std::vector<long long> key;
   cudaGraphExec_t exec = nullptr;
@@ -247,20 +202,6 @@ struct sst_ecch {
     graphs.clear();
   }
 };
-
-/* c_ecch::set_reference_image level-count rule (ecc2.cc:1009-1026) */
-static int ecch_num_levels(int w, int h, const sst_ecch_options & o)
-{
-  const int min_size = std::max(4, o.minimum_image_size);
-  int tw = w, th = h, lv = 1;
-  while ( lv < 32 ) {
-    if( o.maxlevel >= 0 && lv >= std::max(0, o.maxlevel) ) break;
-    const int nw = ((tw + 1) >> 1) & ~1, nh = ((th + 1) >> 1) & ~1;
-    if( nw < min_size || nh < min_size ) break;
-    tw = nw, th = nh, ++lv;
-  }
-  return lv;
-}
 
 static int ensure_streams(sst_ecch * h)
 {
@@ -578,6 +519,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
   for( int k_pass = 0; k_pass < num_passes; ++k_pass ) {
     const sst_motion_model & m = passes[k_pass];
     PassBeginArgs pb;
+    memset(&pb, 0, sizeof(pb));
     pb.fs = fs, pb.n = n, pb.pass = k_pass, pb.model = m, pb.prev_model = k_pass ? passes[k_pass - 1] : m;
     pb.init_states = (k_pass == 0 && have_init) ? h->init.as<double>() : nullptr;
     pb.scale_to_coarsest = L > 1 ? (double) h->lw[L - 1] / (double) h->lw[0] : 0.0;
@@ -589,6 +531,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
       SST_CK(record_prof(h->prof[k_pass][l][0], st, host_driven));
       h->last_steps[k_pass][l] = step;
       LevelBeginArgs lb;
+      memset(&lb, 0, sizeof(lb));
       lb.fs = fs, lb.n = n, lb.model = m, lb.method = method;
       lb.list_out = lists + (size_t) step * h->cap;
       lb.count_out = counts + step;
@@ -650,6 +593,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
     }
   }
   CorrArgs c;
+  memset(&c, 0, sizeof(c));
   c.pyr = h->pyr.as<float>();
   c.pyr_stride = h->pyr_px;
   c.w = h->w, c.h = h->h;

@@ -127,6 +127,25 @@ __device__ __forceinline__ void write_tile(const PassArgs & a, int f, int t, con
   if( threadIdx.x < NS ) a.partials[(size_t) f * a.part_stride + (size_t) t * NS + threadIdx.x] = tile_sums[threadIdx.x];
 }
 
+template<int NS>
+__device__ __forceinline__ void write_tile_at(double * base, int t, const double * tile_sums)
+{
+  if( threadIdx.x < NS ) base[(size_t) t * NS + threadIdx.x] = tile_sums[threadIdx.x];
+}
+
+/* ROI batches: entry k of the active list that owns work index `item`
+ * (largest k with prefix[k] <= item; prefix is strictly increasing) */
+__device__ __forceinline__ int roi_entry(const int * prefix, int count, int item)
+{
+  int lo = 0, hi = count - 1;
+  while ( lo < hi ) {
+    const int mid = (lo + hi + 1) >> 1;
+    if( __ldcg(prefix + mid) <= item ) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 /* ------------------------------------------------------ per-frame control */
 
 __device__ void set_eval(FrameState * F, const sst_motion_model & m, const double * s)
@@ -586,27 +605,49 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
 /* FA / LM pass: the warped tile (+2 px halo, REPLICATE at the level border)
  * is staged in shared memory and differentiated there (ecc_differentiate),
  * so the warped image and its gradients never touch HBM. */
-template<int METHOD, int FAM, int JK, int M>
+template<int METHOD, int FAM, int JK, int M, bool ROI>
 __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
 {
   constexpr int nH = M * (M + 1) / 2;
   constexpr int NS = (METHOD == M_FA) ? nH + 3 * M + 5 : nH + M + 2;
-  constexpr int GMAX = (256 / NS) > 0 ? (256 / NS) : 1;
   constexpr int SW = ST_TX + 4, SH = ST_TY + 4;
   __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
-  __shared__ double s_tmp[NS * GMAX > 256 ? NS * GMAX : 256];
-  __shared__ double s_sum[NS];
   __shared__ float s_img[SH * SW];
   __shared__ float s_c[16];
   __shared__ float s_j[8];
-  __shared__ int s_flag;
 
-  const int nitems = __ldcg(a.count_in) * a.tiles;
+  const int count = __ldcg(a.count_in);
+  const int nitems = ROI ? (count > 0 ? __ldcg(a.tile_total) : 0) : count * a.tiles;
   for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
-    const int fi = item / a.tiles;
-    const int t = item - fi * a.tiles;
-    const int f = __ldcg(a.list_in + fi);
+    int fi, t, f, lw, lh, tiles_x;
+    const float * img, * refT;
+    const uint8_t * refMe;
+    float tshift;
+    double * part;
+    if constexpr( ROI ) {
+      fi = roi_entry(a.tile_prefix, count, item);
+      t = item - __ldcg(a.tile_prefix + fi);
+      f = __ldcg(a.list_in + fi);
+      const RoiLevel & R = a.roi[(size_t) f * a.lmax + a.level];
+      lw = R.w, lh = R.h, tiles_x = R.tiles_x;
+      img = a.pyr + R.cur_off;
+      refT = a.refT + R.ref_off;
+      refMe = nullptr;
+      tshift = R.tshift;
+      part = a.partials + R.part_off;
+    }
+    else {
+      fi = item / a.tiles;
+      t = item - fi * a.tiles;
+      f = __ldcg(a.list_in + fi);
+      lw = a.w, lh = a.h, tiles_x = a.tiles_x;
+      img = a.pyr + (size_t) f * a.pyr_stride + a.lvl_off;
+      refT = a.refT;
+      refMe = a.refMe;
+      tshift = a.tshift;
+      part = a.partials + (size_t) f * a.part_stride;
+    }
     const FrameState * F = a.fs + f;
     if( threadIdx.x < 16 ) s_c[threadIdx.x] = F->wc[threadIdx.x];
     if( threadIdx.x < 8 ) s_j[threadIdx.x] = F->jc[threadIdx.x];
@@ -616,14 +657,13 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
     for( int i = 0; i < 16; ++i ) c[i] = s_c[i];
 #pragma unroll
     for( int i = 0; i < 8; ++i ) jc[i] = s_j[i];
-    const float * img = a.pyr + (size_t) f * a.pyr_stride + a.lvl_off;
-    const int tx0 = (t % a.tiles_x) * ST_TX, ty0 = (t / a.tiles_x) * ST_TY;
+    const int tx0 = (t % tiles_x) * ST_TX, ty0 = (t / tiles_x) * ST_TY;
 
     // stage the warped image gw over the tile + halo (positions clamped: BORDER_REPLICATE)
     for( int q = threadIdx.x; q < SW * SH; q += 256 ) {
-      const int xx = clampi(tx0 - 2 + q % SW, 0, a.w - 1);
-      const int yy = clampi(ty0 - 2 + q / SW, 0, a.h - 1);
-      s_img[q] = sample_replicate(img, a.w, a.h, warp_pos<FAM>(c, xx, yy));
+      const int xx = clampi(tx0 - 2 + q % SW, 0, lw - 1);
+      const int yy = clampi(ty0 - 2 + q / SW, 0, lh - 1);
+      s_img[q] = sample_replicate(img, lw, lh, warp_pos<FAM>(c, xx, yy));
     }
     __syncthreads();
 
@@ -636,19 +676,19 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
     for( int k = 0; k < ST_TY / 4; ++k ) {
       const int ly = (threadIdx.x >> 6) + 4 * k;
       const int y = ty0 + ly;
-      if( x < a.w && y < a.h ) {
+      if( x < lw && y < lh ) {
         const float fx = (float) x, fy = (float) y;
         const spos s = warp_pos<FAM>(c, x, y);
-        const size_t i = (size_t) y * a.w + x;
-        const float cov = coverage(a.w, a.h, s);
+        const size_t i = (size_t) y * lw + x;
+        const float cov = coverage(lw, lh, s);
         bool ok;
         if( METHOD == M_FA ) {
           ok = mask_ok(cov, 255);
-          if( a.refMe ) ok = ok && __ldg(a.refMe + i) != 0;
+          if( refMe ) ok = ok && __ldg(refMe + i) != 0;
         }
         else {
           ok = mask_ok(cov, 250);
-          if( a.refMe ) ok = ok && __ldg(a.refMe + i) != 0;
+          if( refMe ) ok = ok && __ldg(refMe + i) != 0;
         }
         // gx = d5 (x) (*) s3 (y), gy = s3 (x) (*) d5 (y)
         const float * p = s_img + (ly + 2) * SW + (lx + 2);
@@ -666,7 +706,7 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
         }
         if( !ok ) gxw = gyw = 0.f;
         const float gw = p[0];
-        const float T = __ldg(a.refT + i);
+        const float T = __ldg(refT + i);
         float J[M];
         sd_pixel<JK, M>(jc, fx, fy, gxw, gyw, J);
 #pragma unroll
@@ -675,7 +715,7 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
           for( int v = 0; v <= u; ++v, ++kk ) acc[kk] = fmaf(J[u], J[v], acc[kk]);
         }
         if( METHOD == M_FA ) {
-          const float fv = T - a.tshift, gv = gw - a.tshift;
+          const float fv = T - tshift, gv = gw - tshift;
 #pragma unroll
           for( int u = 0; u < M; ++u ) {
             acc[nH + u] = fmaf(J[u], gv, acc[nH + u]);
@@ -700,7 +740,7 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
       }
     }
     block_reduce_d<NS>(acc, s_red, s_tile);
-    write_tile<NS>(a, f, t, s_tile);
+    write_tile_at<NS>(part, t, s_tile);
   }
 }
 
@@ -729,21 +769,32 @@ __global__ void __launch_bounds__(256) k_solve(PassArgs a, int method)
   const int count = __ldcg(a.count_in);
   for( int fi = warp; fi < count; fi += nwarps ) {
     const int f = __ldcg(a.list_in + fi);
-    const double * P = a.partials + (size_t) f * a.part_stride;
+    const RoiLevel * R = a.roi ? a.roi + (size_t) f * a.lmax + a.level : nullptr;
+    const double * P = R ? a.partials + R->part_off : a.partials + (size_t) f * a.part_stride;
+    const int tiles = R ? R->tiles : a.tiles;
     for( int k = 0; k < NS; ++k ) {
       double v = 0;
-      for( int t = lane; t < a.tiles; t += 32 ) v += __ldcg(P + (size_t) t * NS + k);
+      for( int t = lane; t < tiles; t += 32 ) v += __ldcg(P + (size_t) t * NS + k);
       v = warp_sum(v);
       if( lane == 0 ) s_sum[wid][k] = v;
     }
     __syncwarp();
     if( lane == 0 ) {
       FrameState * F = a.fs + f;
-      switch ( method ) {
-      case M_IC: solve_ic(F, s_sum[wid], a, f); break;
-      case M_ICLM: solve_iclm(F, s_sum[wid], a, f); break;
-      case M_FA: solve_fa(F, s_sum[wid], a, f); break;
-      default: solve_lm(F, s_sum[wid], a, f); break;
+      if( R ) {
+        // ROI batch: this frame's level size and rescale factor
+        PassArgs b = a;
+        b.w = R->w, b.h = R->h, b.scale_next = R->scale_next, b.tiles = R->tiles;
+        if( method == M_FA ) solve_fa(F, s_sum[wid], b, f);
+        else solve_lm(F, s_sum[wid], b, f);
+      }
+      else {
+        switch ( method ) {
+        case M_IC: solve_ic(F, s_sum[wid], a, f); break;
+        case M_ICLM: solve_iclm(F, s_sum[wid], a, f); break;
+        case M_FA: solve_fa(F, s_sum[wid], a, f); break;
+        default: solve_lm(F, s_sum[wid], a, f); break;
+        }
       }
     }
     __syncwarp();
@@ -785,10 +836,15 @@ static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st)
     }
     k_pass_pointwise<METHOD, FAM, JK, M><<<grid > 0 ? grid : g, 256, 0, st>>>(a);
   }
+  else if( a.roi ) {
+    static int g = 0;
+    if( !g ) g = persistent_grid(k_pass_stencil<METHOD, FAM, JK, M, true>);
+    k_pass_stencil<METHOD, FAM, JK, M, true><<<grid > 0 ? grid : g, 256, 0, st>>>(a);
+  }
   else {
     static int g = 0;
-    if( !g ) g = persistent_grid(k_pass_stencil<METHOD, FAM, JK, M>);
-    k_pass_stencil<METHOD, FAM, JK, M><<<grid > 0 ? grid : g, 256, 0, st>>>(a);
+    if( !g ) g = persistent_grid(k_pass_stencil<METHOD, FAM, JK, M, false>);
+    k_pass_stencil<METHOD, FAM, JK, M, false><<<grid > 0 ? grid : g, 256, 0, st>>>(a);
   }
   return cudaGetLastError();
 }
@@ -817,6 +873,7 @@ static cudaError_t launch_m(const PassArgs & a, int grid, cudaStream_t st)
 
 cudaError_t launch_pass(int method, const PassArgs & a, int grid, cudaStream_t st)
 {
+  if( a.roi && method != M_FA && method != M_LM ) return cudaErrorInvalidValue;
   switch ( method ) {
   case M_IC: return launch_m<M_IC>(a, grid, st);
   case M_ICLM: return launch_m<M_ICLM>(a, grid, st);
@@ -842,6 +899,7 @@ __global__ void k_level_begin(LevelBeginArgs a)
     if( f < a.n ) {
       FrameState * F = a.fs + f;
       alive = F->status == SST_FRAME_OK;
+      if( a.roi && a.roi[(size_t) f * a.lmax + a.level].w == 0 ) alive = false;   // no such level
       F->n = 0;
       F->phase = PH_START;
       F->converged = 0;
@@ -900,7 +958,8 @@ __global__ void k_pass_begin(PassBeginArgs a)
     model_convert(a.prev_model, F->state, a.model, s);
     for( int i = 0; i < 16; ++i ) F->state[i] = s[i];
   }
-  if( a.scale_to_coarsest > 0 ) model_scale(a.model, F->state, a.scale_to_coarsest);
+  const double sc = a.roi ? a.roi[(size_t) f * a.lmax].scale_first : a.scale_to_coarsest;
+  if( sc > 0 ) model_scale(a.model, F->state, sc);
   set_eval(F, a.model, F->state);
 }
 
@@ -922,10 +981,31 @@ __global__ void __launch_bounds__(256) k_correlation(CorrArgs a)
   __shared__ float s_red[8 * NS];
   __shared__ double s_tile[NS];
   __shared__ float s_c[16];
-  const int nitems = a.n * a.tiles;
+  const int nitems = a.roi ? __ldg(a.tile_prefix + a.n) : a.n * a.tiles;
   for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
-    const int f = item / a.tiles;
-    const int t = item - f * a.tiles;
+    int f, t, lw, lh, tiles_x;
+    const float * img, * refT;
+    float tshift;
+    double * part;
+    if( a.roi ) {
+      f = roi_entry(a.tile_prefix, a.n, item);
+      t = item - __ldg(a.tile_prefix + f);
+      const RoiLevel & R = a.roi[(size_t) f * a.lmax];
+      lw = R.w, lh = R.h, tiles_x = R.ctiles_x;
+      img = a.pyr + R.cur_off;
+      refT = a.refT + R.ref_off;
+      tshift = R.tshift;
+      part = a.partials + R.part_off;
+    }
+    else {
+      f = item / a.tiles;
+      t = item - f * a.tiles;
+      lw = a.w, lh = a.h, tiles_x = a.tiles_x;
+      img = a.pyr + (size_t) f * a.pyr_stride;
+      refT = a.refT;
+      tshift = a.tshift;
+      part = a.partials + (size_t) f * a.part_stride;
+    }
     const FrameState * F = a.fs + f;
     if( F->status != SST_FRAME_OK ) continue;   // uniform per CTA: no barrier skipped unevenly
     if( threadIdx.x < 16 ) s_c[threadIdx.x] = F->wc[threadIdx.x];
@@ -933,22 +1013,21 @@ __global__ void __launch_bounds__(256) k_correlation(CorrArgs a)
     float c[16];
 #pragma unroll
     for( int i = 0; i < 16; ++i ) c[i] = s_c[i];
-    const float * img = a.pyr + (size_t) f * a.pyr_stride;
-    const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
+    const int tx0 = (t % tiles_x) * PW_TX, ty0 = (t / tiles_x) * PW_TY;
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
-    const int yend = min(ty0 + PW_TY, a.h);
-    const bool interior = !a.refM && rect_interior<FAM>(c, tx0, ty0, min(tx0 + PW_TX, a.w) - 1, yend - 1, a.w, a.h);
+    const int yend = min(ty0 + PW_TY, lh);
+    const bool interior = !a.refM && rect_interior<FAM>(c, tx0, ty0, min(tx0 + PW_TX, lw) - 1, yend - 1, lw, lh);
     float acc[NS] = { 0, 0, 0, 0, 0, 0 };
-    if( x < a.w ) {
+    if( x < lw ) {
 #pragma unroll 4
       for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
         const spos s = warp_pos<FAM>(c, x, y);
-        const size_t i = (size_t) y * a.w + x;
-        bool ok = interior || mask_ok(coverage(a.w, a.h, s), 254);
+        const size_t i = (size_t) y * lw + x;
+        bool ok = interior || mask_ok(coverage(lw, lh, s), 254);
         if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
         if( ok ) {
-          const float av = __ldg(a.refT + i) - a.tshift;
-          const float bv = (interior ? sample_replicate(img, a.w, a.h, s) : sample_constant0(img, a.w, a.h, s)) - a.tshift;
+          const float av = __ldg(refT + i) - tshift;
+          const float bv = (interior ? sample_replicate(img, lw, lh, s) : sample_constant0(img, lw, lh, s)) - tshift;
           acc[0] += av, acc[1] += bv;
           acc[2] = fmaf(av, av, acc[2]);
           acc[3] = fmaf(bv, bv, acc[3]);
@@ -958,7 +1037,7 @@ __global__ void __launch_bounds__(256) k_correlation(CorrArgs a)
       }
     }
     block_reduce_d<NS>(acc, s_red, s_tile);
-    if( threadIdx.x < NS ) a.partials[(size_t) f * a.part_stride + (size_t) t * NS + threadIdx.x] = s_tile[threadIdx.x];
+    write_tile_at<NS>(part, t, s_tile);
   }
 }
 
@@ -970,7 +1049,9 @@ __global__ void __launch_bounds__(256) k_correlation_finish(CorrArgs a)
   for( int f = blockIdx.x; f < a.n; f += gridDim.x ) {
     FrameState * F = a.fs + f;
     if( F->status != SST_FRAME_OK ) continue;
-    combine_partials(a.partials + (size_t) f * a.part_stride, a.tiles, 6, s_tmp, s_sum);
+    const RoiLevel * R = a.roi ? a.roi + (size_t) f * a.lmax : nullptr;
+    combine_partials(R ? a.partials + R->part_off : a.partials + (size_t) f * a.part_stride, R ? R->ctiles : a.tiles,
+        6, s_tmp, s_sum);
     if( threadIdx.x == 0 ) {
       const double n = s_sum[5];
       double rho = 0;
@@ -997,6 +1078,56 @@ cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st)
   cudaError_t e = cudaGetLastError();
   if( e != cudaSuccess ) return e;
   k_correlation_finish<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+/* ---------------------------------------------------------- ROI scan */
+
+/* Exclusive prefix sums of the tile counts of the active list's frames at
+ * `level` (one CTA; a list of up to a few thousand frames) and their total. */
+__global__ void __launch_bounds__(1024) k_roi_scan(const int * list, const int * count, const RoiLevel * roi,
+    int lmax, int level, int * prefix, int * total)
+{
+  __shared__ int s_w[32];
+  __shared__ int s_base;
+  const int n = __ldcg(count);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if( threadIdx.x == 0 ) s_base = 0;
+  __syncthreads();
+  for( int k0 = 0; k0 < n; k0 += 1024 ) {
+    const int k = k0 + threadIdx.x;
+    const int v = k < n ? roi[(size_t) __ldcg(list + k) * lmax + level].tiles : 0;
+    int incl = v;
+#pragma unroll
+    for( int o = 1; o < 32; o <<= 1 ) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if( lane >= o ) incl += u;
+    }
+    if( lane == 31 ) s_w[wid] = incl;
+    __syncthreads();
+    if( wid == 0 ) {
+      int x = s_w[lane];
+#pragma unroll
+      for( int o = 1; o < 32; o <<= 1 ) {
+        const int u = __shfl_up_sync(0xffffffffu, x, o);
+        if( lane >= o ) x += u;
+      }
+      s_w[lane] = x;
+    }
+    __syncthreads();
+    const int base = s_base + (wid > 0 ? s_w[wid - 1] : 0);
+    if( k < n ) prefix[k] = base + incl - v;
+    __syncthreads();
+    if( threadIdx.x == 0 ) s_base += s_w[31];
+    __syncthreads();
+  }
+  if( threadIdx.x == 0 ) *total = s_base;
+}
+
+cudaError_t launch_roi_scan(const int * list, const int * count, const RoiLevel * roi, int lmax, int level,
+    int * prefix, int * total, cudaStream_t st)
+{
+  k_roi_scan<<<1, 1024, 0, st>>>(list, count, roi, lmax, level, prefix, total);
   return cudaGetLastError();
 }
 

@@ -3,15 +3,20 @@
  * the launch helpers shared by the kernel translation units and the C ABI.
  *
  * Execution model (one GPU): the frames of a batch live side by side in HBM
- * (one f32 pyramid per frame). A Gauss-Newton "step" is ONE kernel launch
- * over every frame that still iterates at the current pyramid level: the
- * launch walks a compacted list of active frames x tiles, each CTA reduces
- * its tile, and the last CTA to finish a frame (atomic ticket) combines the
- * frame's tile partials in a fixed order and runs that frame's FP64 solve /
- * convergence logic, appending the frame to the next step's active list if
- * it keeps iterating. Step k reads list k and writes list k+1, so the whole
- * level x iteration schedule is a static sequence of launches that is
- * captured once into a CUDA graph and replayed.
+ * (one f32 pyramid per frame). A Gauss-Newton "step" is two launches over
+ * every frame that still iterates at the current pyramid level: the pass
+ * kernel walks a compacted list of active frames x tiles and stores one set
+ * of FP64 partial sums per tile; the solve kernel gives each active frame a
+ * warp that combines the frame's tile partials in a fixed order and runs the
+ * frame's FP64 solve / convergence logic, appending the frame to the next
+ * step's active list if it keeps iterating. Step k reads list k and writes
+ * list k+1, so the whole level x iteration schedule is a static sequence of
+ * launches that is captured once into a CUDA graph and replayed.
+ *
+ * ROI batches (frames of different sizes, each with its own reference) use
+ * the same schedule with per-frame level geometry (RoiLevel): the pass
+ * kernel maps its work index to (frame, tile) through a prefix sum of the
+ * active frames' tile counts, rebuilt for every step by k_roi_scan.
  */
 #pragma once
 #include <cuda_runtime.h>
@@ -66,6 +71,20 @@ struct FrameState {
   float rho, weight;
 };
 
+/* Geometry of one frame at one pyramid level in a ROI batch. */
+struct RoiLevel {
+  size_t cur_off;           // floats from the current pool to this frame's level
+  size_t ref_off;           // floats from the reference pool to this frame's level
+  size_t part_off;          // doubles from the partials base to this frame's partials (all levels)
+  int w, h;                 // level size; w == 0: the frame has no such level
+  int tiles_x, tiles;       // stencil tiles (ST_TX x ST_TY) of the level
+  int ctiles_x, ctiles;     // correlation tiles (PW_TX x PW_TY), level 0 only
+  double scale_next;        // scale_transfrom factor to the next finer level (0 at level 0)
+  double scale_first;       // level-0 entry: factor from level 0 to the frame's coarsest level
+  float tshift;             // mean of the frame's reference (numerical shift of the FA sums)
+  int pad;
+};
+
 /* Arguments of one Gauss-Newton pass launch (by value). */
 struct PassArgs {
   const float * pyr;        // frame 0 level 0
@@ -96,6 +115,11 @@ struct PassArgs {
   double max_eps, step;
   int max_it;
   double scale_next;        // scale_transfrom factor to the next finer level, 0 at level 0
+  // ROI batches (roi != nullptr): per-frame geometry replaces pyr_stride / lvl_off / w / h / tiles
+  const RoiLevel * roi;     // n x lmax entries
+  int lmax, level;
+  const int * tile_prefix;  // per entry of list_in: tiles of the entries before it (k_roi_scan)
+  const int * tile_total;   // tiles of the whole list
 };
 
 /* pointwise passes (IC, IC-LM, correlation): 128 x 64 pixel tiles, 256 threads */
@@ -122,6 +146,8 @@ struct LevelBeginArgs {
   int * list_out;
   int * count_out;
   int level_is_first;
+  const RoiLevel * roi;     // ROI batches: frames without this level are not listed
+  int lmax, level;
 };
 cudaError_t launch_level_begin(const LevelBeginArgs & a, cudaStream_t st);
 
@@ -132,6 +158,8 @@ struct PassBeginArgs {
   sst_motion_model model, prev_model;
   const double * init_states;   // n x 16 or nullptr
   double scale_to_coarsest;
+  const RoiLevel * roi;          // ROI batches: per-frame factor (RoiLevel::scale_first)
+  int lmax;
 };
 cudaError_t launch_pass_begin(const PassBeginArgs & a, cudaStream_t st);
 
@@ -149,8 +177,15 @@ struct CorrArgs {
   unsigned * counters;
   sst_motion_model model;
   double min_rho;
+  const RoiLevel * roi;          // ROI batches: per-frame level-0 geometry
+  int lmax;
+  const int * tile_prefix;       // n + 1 correlation tile offsets (all frames)
 };
 cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st);
+
+/* ROI batches: prefix sums of the active frames' tile counts for one step */
+cudaError_t launch_roi_scan(const int * list, const int * count, const RoiLevel * roi, int lmax, int level,
+    int * prefix, int * total, cudaStream_t st);
 
 struct FinalizeArgs {
   FrameState * fs;
@@ -164,7 +199,20 @@ struct FinalizeArgs {
 };
 cudaError_t launch_finalize(const FinalizeArgs & a, cudaStream_t st);
 
+/* One image of a ragged batch job (grid.z = job): source at src_off (bytes
+ * for convert, floats for pyrDown) of sw x sh with src_stride bytes per row
+ * (convert), destination at dst_off floats of dw x dh. */
+struct RaggedImg {
+  size_t src_off, dst_off, src_stride;
+  int sw, sh, dw, dh;
+};
+
 /* pyramid / reference kernels (sst_pyramid.cu) */
+cudaError_t launch_convert_smooth_ragged(const void * src, int depth, const RaggedImg * jobs, int n, int max_w,
+    int max_h, double scale, const float * gk, int ksize, float * dst, cudaStream_t st);
+cudaError_t launch_pyrdown_ragged(const float * src, const RaggedImg * jobs, int n, int max_dw, int max_dh,
+    float * dst, cudaStream_t st);
+cudaError_t launch_roi_means(const float * pool, const RaggedImg * jobs, int n, double * sums, cudaStream_t st);
 cudaError_t launch_convert_smooth(const void * src, int depth, int n, int w, int h, size_t row_stride,
     size_t frame_stride, double scale, const float * gk, int ksize, float * dst, size_t dst_stride, cudaStream_t st);
 cudaError_t launch_pyrdown(const float * src, int sw, int sh, size_t src_stride, float * dst, int dw, int dh,

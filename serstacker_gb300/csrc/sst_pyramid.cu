@@ -31,11 +31,20 @@ __device__ __forceinline__ float load_px(const uint8_t * base, size_t row_stride
  * filtered horizontally then vertically. */
 template<typename T>
 __global__ void __launch_bounds__(256) k_convert_smooth(const uint8_t * src, int w, int h, size_t row_stride,
-    size_t frame_stride, float scale, const float * __restrict__ gk, int R, float * dst, size_t dst_stride)
+    size_t frame_stride, float scale, const float * __restrict__ gk, int R, float * dst, size_t dst_stride,
+    const RaggedImg * __restrict__ jobs)
 {
   extern __shared__ float sm[];
   const uint8_t * fb = src + (size_t) blockIdx.z * frame_stride;
   float * out = dst + (size_t) blockIdx.z * dst_stride;
+  if( jobs ) {
+    // ragged batch: this image's size, rows and destination (uniform over the CTA)
+    const RaggedImg j = jobs[blockIdx.z];
+    w = j.sw, h = j.sh, row_stride = j.src_stride;
+    fb = src + j.src_off;
+    out = dst + j.dst_off;
+    if( (int) blockIdx.x * CS_TX >= w || (int) blockIdx.y * CS_TY >= h ) return;
+  }
   const int tx0 = blockIdx.x * CS_TX, ty0 = blockIdx.y * CS_TY;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if( R <= 0 ) {
@@ -109,9 +118,30 @@ cudaError_t launch_convert_smooth(const void * src, int depth, int n, int w, int
     attr = true;
   }
   switch ( depth ) {
-  case SST_DEPTH_U8: k_convert_smooth<uint8_t><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
-  case SST_DEPTH_U16: k_convert_smooth<uint16_t><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
-  case SST_DEPTH_F32: k_convert_smooth<float><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride); break;
+  case SST_DEPTH_U8: k_convert_smooth<uint8_t><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride, nullptr); break;
+  case SST_DEPTH_U16: k_convert_smooth<uint16_t><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride, nullptr); break;
+  case SST_DEPTH_F32: k_convert_smooth<float><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride, nullptr); break;
+  default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_convert_smooth_ragged(const void * src, int depth, const RaggedImg * jobs, int n, int max_w,
+    int max_h, double scale, const float * gk, int ksize, float * dst, cudaStream_t st)
+{
+  const int R = gk ? ksize / 2 : 0;
+  if( R > CS_RMAX || n > 65535 ) return cudaErrorInvalidValue;
+  const size_t smem = R > 0 ? ((size_t) (CS_TX + 2 * R) * (CS_TY + 2 * R) + (size_t) CS_TX * (CS_TY + 2 * R) + 32) * sizeof(float) : 0;
+  dim3 grid((max_w + CS_TX - 1) / CS_TX, (max_h + CS_TY - 1) / CS_TY, n);
+  const uint8_t * s = (const uint8_t *) src;
+  const int mx = (int) (((CS_TX + 2 * CS_RMAX) * (CS_TY + 2 * CS_RMAX) + CS_TX * (CS_TY + 2 * CS_RMAX) + 32) * sizeof(float));
+  cudaFuncSetAttribute(k_convert_smooth<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_convert_smooth<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_convert_smooth<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  switch ( depth ) {
+  case SST_DEPTH_U8: k_convert_smooth<uint8_t><<<grid, 256, smem, st>>>(s, 0, 0, 0, 0, (float) scale, gk, R, dst, 0, jobs); break;
+  case SST_DEPTH_U16: k_convert_smooth<uint16_t><<<grid, 256, smem, st>>>(s, 0, 0, 0, 0, (float) scale, gk, R, dst, 0, jobs); break;
+  case SST_DEPTH_F32: k_convert_smooth<float><<<grid, 256, smem, st>>>(s, 0, 0, 0, 0, (float) scale, gk, R, dst, 0, jobs); break;
   default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -122,13 +152,20 @@ cudaError_t launch_convert_smooth(const void * src, int depth, int n, int w, int
 constexpr int PD_TX = 64, PD_TY = 16;
 
 __global__ void __launch_bounds__(256) k_pyrdown(const float * src, int sw, int sh, size_t src_stride,
-    float * dst, int dw, int dh, size_t dst_stride)
+    float * dst, int dw, int dh, size_t dst_stride, const RaggedImg * __restrict__ jobs)
 {
   constexpr int SW = 2 * PD_TX + 4, SH = 2 * PD_TY + 4;
   __shared__ float s_in[SH * SW];
   __shared__ float s_h[SH * PD_TX];
   const float * in = src + (size_t) blockIdx.z * src_stride;
   float * out = dst + (size_t) blockIdx.z * dst_stride;
+  if( jobs ) {
+    const RaggedImg j = jobs[blockIdx.z];
+    sw = j.sw, sh = j.sh, dw = j.dw, dh = j.dh;
+    in = src + j.src_off;
+    out = dst + j.dst_off;
+    if( (int) blockIdx.x * PD_TX >= dw || (int) blockIdx.y * PD_TY >= dh ) return;
+  }
   const int tx0 = blockIdx.x * PD_TX, ty0 = blockIdx.y * PD_TY;
   const int sx0 = 2 * tx0 - 2, sy0 = 2 * ty0 - 2;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -166,7 +203,48 @@ cudaError_t launch_pyrdown(const float * src, int sw, int sh, size_t src_stride,
     size_t dst_stride, int n, cudaStream_t st)
 {
   dim3 grid((dw + PD_TX - 1) / PD_TX, (dh + PD_TY - 1) / PD_TY, n);
-  k_pyrdown<<<grid, 256, 0, st>>>(src, sw, sh, src_stride, dst, dw, dh, dst_stride);
+  k_pyrdown<<<grid, 256, 0, st>>>(src, sw, sh, src_stride, dst, dw, dh, dst_stride, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pyrdown_ragged(const float * src, const RaggedImg * jobs, int n, int max_dw, int max_dh,
+    float * dst, cudaStream_t st)
+{
+  if( n > 65535 ) return cudaErrorInvalidValue;
+  dim3 grid((max_dw + PD_TX - 1) / PD_TX, (max_dh + PD_TY - 1) / PD_TY, n);
+  k_pyrdown<<<grid, 256, 0, st>>>(src, 0, 0, 0, dst, 0, 0, 0, jobs);
+  return cudaGetLastError();
+}
+
+/* Sum of each image of a ragged job list (one CTA per image, fixed-order
+ * FP64 reduction): sums[j] = sum of image j's sw x sh floats at src_off. */
+__global__ void __launch_bounds__(256) k_roi_means(const float * pool, const RaggedImg * jobs, double * sums)
+{
+  __shared__ double s_w[8];
+  const RaggedImg j = jobs[blockIdx.x];
+  const float * p = pool + j.src_off;
+  const size_t N = (size_t) j.sw * j.sh;
+  double acc = 0;
+  float part = 0.f;
+  int k = 0;
+  for( size_t i = threadIdx.x; i < N; i += 256 ) {
+    part += __ldg(p + i);
+    if( ++k == 64 ) acc += part, part = 0.f, k = 0;   // FP32 runs of 64 pixels, FP64 across runs
+  }
+  acc += part;
+  acc = warp_sum(acc);
+  if( (threadIdx.x & 31) == 0 ) s_w[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if( threadIdx.x == 0 ) {
+    double t = 0;
+    for( int w = 0; w < 8; ++w ) t += s_w[w];
+    sums[blockIdx.x] = t;
+  }
+}
+
+cudaError_t launch_roi_means(const float * pool, const RaggedImg * jobs, int n, double * sums, cudaStream_t st)
+{
+  k_roi_means<<<n, 256, 0, st>>>(pool, jobs, sums);
   return cudaGetLastError();
 }
 
