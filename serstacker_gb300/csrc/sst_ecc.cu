@@ -602,21 +602,111 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
 
 /* -------------------------------------------------------- stencil passes */
 
+/* ---- tensor-core Gram matrix (3xTF32 mma.sync) */
+
+/* f32 -> tf32 (round to nearest, ties away), as the b32 operand of mma */
+__device__ __forceinline__ uint32_t to_tf32(float x)
+{
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+/* D = A B + D, A 16 x 8 (row), B 8 x 8 (col), tf32 operands, f32 accumulate */
+__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+    uint32_t b0, uint32_t b1)
+{
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+/* G += V^T V over the 32 pixels staged by one warp: sv holds 32 rows of 16
+ * components (row stride GV_LD floats). A = V^T in k-chunks of 8 pixels,
+ * B = V; the operands are split x = hi + lo (tf32 each) and the three
+ * products hi.hi + hi.lo + lo.hi keep FP32-level accuracy. g0 holds
+ * G[:, 0:8], g1 G[:, 8:16] in the m16n8 accumulator layout. */
+constexpr int GV_LD = 24;   // 16 components + pad: conflict-free fragment loads
+
+__device__ __forceinline__ void gram_accumulate(const float * sv, float (&g0)[4], float (&g1)[4])
+{
+  const int lane = threadIdx.x & 31, gq = lane >> 2, tq = lane & 3;
+#pragma unroll
+  for( int c = 0; c < 4; ++c ) {
+    const float * r0 = sv + (8 * c + tq) * GV_LD, * r1 = sv + (8 * c + tq + 4) * GV_LD;
+    const float x0 = r0[gq], x1 = r0[gq + 8], x2 = r1[gq], x3 = r1[gq + 8];
+    const uint32_t h0 = to_tf32(x0), h1 = to_tf32(x1), h2 = to_tf32(x2), h3 = to_tf32(x3);
+    const uint32_t l0 = to_tf32(x0 - __uint_as_float(h0)), l1 = to_tf32(x1 - __uint_as_float(h1));
+    const uint32_t l2 = to_tf32(x2 - __uint_as_float(h2)), l3 = to_tf32(x3 - __uint_as_float(h3));
+    // A fragment: rows (components) gq / gq + 8, columns (pixels) tq / tq + 4;
+    // B fragment of the n-tile [n0, n0 + 8): rows (pixels) tq / tq + 4, column n0 + gq
+    mma_tf32(g0, h0, h1, h2, h3, h0, h2);
+    mma_tf32(g0, h0, h1, h2, h3, l0, l2);
+    mma_tf32(g0, l0, l1, l2, l3, h0, h2);
+    mma_tf32(g1, h0, h1, h2, h3, h1, h3);
+    mma_tf32(g1, h0, h1, h2, h3, l1, l3);
+    mma_tf32(g1, l0, l1, l2, l3, h1, h3);
+  }
+}
+
+/* Gram-matrix entry (i, j) that holds pass sum k. FA: V = [J (M), g - s, f - s, 1],
+ * sums H (packed lower), SJg, SJf, SJ, Sf, Sf2, Sg, Sg2, n. LM: V = [J (M), r, 1],
+ * sums H (packed lower), J^T r, |r|^2, n. */
+template<int METHOD, int M>
+__device__ __forceinline__ void sum_entry(int k, int & i, int & j)
+{
+  constexpr int nH = M * (M + 1) / 2;
+  if( k < nH ) {
+    int r = 0;
+    while ( (r + 1) * (r + 2) / 2 <= k ) ++r;
+    i = r, j = k - r * (r + 1) / 2;
+    return;
+  }
+  k -= nH;
+  if( METHOD == M_FA ) {
+    if( k < 3 * M ) {
+      i = k % M, j = M + k / M;                  // SJg: col M, SJf: col M + 1, SJ: col M + 2
+      return;
+    }
+    switch ( k - 3 * M ) {
+    case 0: i = M + 1, j = M + 2; return;        // Sf
+    case 1: i = M + 1, j = M + 1; return;        // Sf2
+    case 2: i = M, j = M + 2; return;            // Sg
+    case 3: i = M, j = M; return;                // Sg2
+    default: i = M + 2, j = M + 2; return;       // n
+    }
+  }
+  else {
+    if( k < M ) {
+      i = k, j = M;
+      return;
+    }
+    if( k == M ) i = j = M;
+    else i = j = M + 1;
+  }
+}
+
 /* FA / LM pass: the warped tile (+2 px halo, REPLICATE at the level border)
  * is staged in shared memory and differentiated there (ecc_differentiate),
- * so the warped image and its gradients never touch HBM. */
+ * so the warped image and its gradients never touch HBM. Each pixel forms
+ * V = [steepest-descent row, residual terms, 1]; the tile's sums are the
+ * entries of the Gram matrix sum V^T V, accumulated on the tensor cores
+ * (32 pixels per warp per mma batch), then reduced over the 8 warps in FP64. */
 template<int METHOD, int FAM, int JK, int M, bool ROI>
 __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
 {
   constexpr int nH = M * (M + 1) / 2;
   constexpr int NS = (METHOD == M_FA) ? nH + 3 * M + 5 : nH + M + 2;
   constexpr int SW = ST_TX + 4, SH = ST_TY + 4;
-  __shared__ float s_red[8 * NS];
-  __shared__ double s_tile[NS];
+  static_assert(M + 3 <= 16, "V must fit 16 components");
   __shared__ float s_img[SH * SW];
+  __shared__ __align__(16) float s_v[8][32 * GV_LD];      // per warp: V of 32 pixels, then its Gram matrix
+  __shared__ double s_tile[NS];
   __shared__ float s_c[16];
   __shared__ float s_j[8];
 
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int count = __ldcg(a.count_in);
   const int nitems = ROI ? (count > 0 ? __ldcg(a.tile_total) : 0) : count * a.tiles;
   for( int item = blockIdx.x; item < nitems; item += gridDim.x ) {
@@ -667,33 +757,28 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
     }
     __syncthreads();
 
-    float acc[NS];
-#pragma unroll
-    for( int k = 0; k < NS; ++k ) acc[k] = 0.f;
+    float g0[4] = { 0.f, 0.f, 0.f, 0.f }, g1[4] = { 0.f, 0.f, 0.f, 0.f };
+    float * sv = s_v[wid];
     const int lx = threadIdx.x & (ST_TX - 1);
     const int x = tx0 + lx;
 #pragma unroll 1
     for( int k = 0; k < ST_TY / 4; ++k ) {
       const int ly = (threadIdx.x >> 6) + 4 * k;
       const int y = ty0 + ly;
+      float v[16];
+#pragma unroll
+      for( int u = 0; u < 16; ++u ) v[u] = 0.f;
       if( x < lw && y < lh ) {
         const float fx = (float) x, fy = (float) y;
         const spos s = warp_pos<FAM>(c, x, y);
         const size_t i = (size_t) y * lw + x;
         const float cov = coverage(lw, lh, s);
-        bool ok;
-        if( METHOD == M_FA ) {
-          ok = mask_ok(cov, 255);
-          if( refMe ) ok = ok && __ldg(refMe + i) != 0;
-        }
-        else {
-          ok = mask_ok(cov, 250);
-          if( refMe ) ok = ok && __ldg(refMe + i) != 0;
-        }
+        bool ok = mask_ok(cov, METHOD == M_FA ? 255 : 250);
+        if( refMe ) ok = ok && __ldg(refMe + i) != 0;
         // gx = d5 (x) (*) s3 (y), gy = s3 (x) (*) d5 (y)
         const float * p = s_img + (ly + 2) * SW + (lx + 2);
         const float d5a = 1.f / 12.f, d5b = -2.f / 3.f;
-        float gxw = 0.f, gyw = 0.f;
+        float gxw, gyw;
         {
           const float r0 = d5a * p[-SW - 2] + d5b * p[-SW - 1] - d5b * p[-SW + 1] - d5a * p[-SW + 2];
           const float r1 = d5a * p[-2] + d5b * p[-1] - d5b * p[1] - d5a * p[2];
@@ -710,36 +795,45 @@ __global__ void __launch_bounds__(256) k_pass_stencil(PassArgs a)
         float J[M];
         sd_pixel<JK, M>(jc, fx, fy, gxw, gyw, J);
 #pragma unroll
-        for( int u = 0, kk = 0; u < M; ++u ) {
-#pragma unroll
-          for( int v = 0; v <= u; ++v, ++kk ) acc[kk] = fmaf(J[u], J[v], acc[kk]);
-        }
-        if( METHOD == M_FA ) {
-          const float fv = T - tshift, gv = gw - tshift;
-#pragma unroll
-          for( int u = 0; u < M; ++u ) {
-            acc[nH + u] = fmaf(J[u], gv, acc[nH + u]);
-            acc[nH + M + u] = fmaf(J[u], fv, acc[nH + M + u]);
-            acc[nH + 2 * M + u] += J[u];
+        for( int u = 0; u < M; ++u ) v[u] = J[u];
+        if( ok ) {
+          if( METHOD == M_FA ) {
+            v[M] = gw - tshift;
+            v[M + 1] = T - tshift;
+            v[M + 2] = 1.f;
           }
-          if( ok ) {
-            acc[nH + 3 * M] += fv;
-            acc[nH + 3 * M + 1] = fmaf(fv, fv, acc[nH + 3 * M + 1]);
-            acc[nH + 3 * M + 2] += gv;
-            acc[nH + 3 * M + 3] = fmaf(gv, gv, acc[nH + 3 * M + 3]);
-            acc[nH + 3 * M + 4] += 1.f;
+          else {
+            v[M] = gw - T;
+            v[M + 1] = 1.f;
           }
-        }
-        else {
-          const float r = ok ? gw - T : 0.f;
-#pragma unroll
-          for( int u = 0; u < M; ++u ) acc[nH + u] = fmaf(J[u], r, acc[nH + u]);
-          acc[nH + M] = fmaf(r, r, acc[nH + M]);
-          acc[nH + M + 1] += ok ? 1.f : 0.f;
         }
       }
+      __syncwarp();
+      float4 * dst = reinterpret_cast<float4 *>(sv + lane * GV_LD);
+#pragma unroll
+      for( int q = 0; q < 4; ++q ) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      __syncwarp();
+      gram_accumulate(sv, g0, g1);
     }
-    block_reduce_d<NS>(acc, s_red, s_tile);
+    // this warp's Gram matrix into its staging area (16 x 16, row stride 16)
+    __syncwarp();
+    {
+      const int gq = lane >> 2, tq = lane & 3;
+      sv[gq * 16 + 2 * tq] = g0[0], sv[gq * 16 + 2 * tq + 1] = g0[1];
+      sv[(gq + 8) * 16 + 2 * tq] = g0[2], sv[(gq + 8) * 16 + 2 * tq + 1] = g0[3];
+      sv[gq * 16 + 8 + 2 * tq] = g1[0], sv[gq * 16 + 8 + 2 * tq + 1] = g1[1];
+      sv[(gq + 8) * 16 + 8 + 2 * tq] = g1[2], sv[(gq + 8) * 16 + 8 + 2 * tq + 1] = g1[3];
+    }
+    __syncthreads();
+    if( threadIdx.x < NS ) {
+      int gi, gj;
+      sum_entry<METHOD, M>(threadIdx.x, gi, gj);
+      double tsum = 0;
+#pragma unroll
+      for( int wv = 0; wv < 8; ++wv ) tsum += (double) s_v[wv][gi * 16 + gj];
+      s_tile[threadIdx.x] = tsum;
+    }
+    __syncthreads();
     write_tile_at<NS>(part, t, s_tile);
   }
 }
