@@ -294,6 +294,74 @@ int sst_extract_bayer_planes_u16(const uint16_t * src, int width, int height, si
 int sst_average_bayer_planes_u16(const uint16_t * src, int width, int height, size_t row_stride,
     uint16_t * dst, void * stream);
 
+/* ------------------------------------------------------------- c_eccflow */
+
+/* ECCFlowDownscaleMethod (ecc2.h:509-513) */
+#define SST_ECCFLOW_DOWNSCALE_RECURSIVE_RESIZE 0
+#define SST_ECCFLOW_DOWNSCALE_FULL_RESIZE      1
+#define SST_ECCFLOW_DOWNSCALE_PYRAMID          2
+
+/* c_eccflow_options (ecc2.h:515-527). input_smooth_sigma and
+ * reference_smooth_sigma are carried but, as in the reference, unused. */
+typedef struct sst_eccflow_options {
+  double update_multiplier;
+  double scale_factor;
+  double noise_level;
+  double input_smooth_sigma;
+  double reference_smooth_sigma;
+  int32_t max_iterations;
+  int32_t support_scale;
+  int32_t min_image_size;
+  int32_t max_pyramid_level;
+  int32_t downscale;
+  int32_t reserved;
+} sst_eccflow_options;
+
+typedef struct sst_eccflow sst_eccflow;
+
+/* c_eccflow_options defaults (ecc2.h:515-527) */
+void sst_eccflow_options_default(sst_eccflow_options * o);
+int sst_eccflow_create(sst_eccflow ** out, const sst_eccflow_options * options);
+int sst_eccflow_destroy(sst_eccflow * h);
+
+/* c_eccflow::set_reference_image(reference) (ecc2.cc:2489-2672): the
+ * reference pyramid, its gradients and the per-level 2x2 systems D. Values
+ * are multiplied by `scale`. Masks are not supported. */
+int sst_eccflow_set_reference_image(sst_eccflow * h, const void * image, int depth, int width, int height,
+    size_t row_stride, double scale, int on_device, void * stream);
+
+/* number of pyramid levels of the current reference */
+int sst_eccflow_num_levels(const sst_eccflow * h);
+
+/* c_eccflow::compute(current, rmap) (ecc2.cc:2856-2865) for n frames of the
+ * reference's size: rmap_out (n x height x width x 2 floats, interleaved
+ * (x, y) as cv::Mat2f) receives identity + flow. init_rmap (same layout, or
+ * NULL for a zero start) seeds the flow as the reference's input rmap does.
+ * Buffers are host or device memory per on_device. */
+int sst_eccflow_compute_batch(sst_eccflow * h, const void * frames, int depth, int n, size_t row_stride,
+    size_t frame_stride, double scale, int on_device, const float * init_rmap, float * rmap_out, void * stream);
+
+/* -------------------------------------------- differentiable warp residual */
+
+/* The ECC warp residual of n frames against a template and its adjoint (no
+ * counterpart in the reference; the objective c_ecc_forward_additive and
+ * c_ecclm minimise, ecc2.cc:1247-1365, 1444-1650):
+ *   r_f(x) = I_f(W(x; p_f) + u_f(x)) - T(x)   (bilinear, BORDER_REPLICATE)
+ *   L_f = 1/2 sum_x r_f(x)^2
+ * frames: n x height x width f32 (frame_stride floats apart), tmpl: height x
+ * width f32, params: n x 12 f32 (the model's parameter vectors), flow: n x
+ * height x width x 2 f32 or NULL. Outputs (each may be NULL): loss (n f64),
+ * grad_params (n x 12 f32: g_f dL_f/dp_f), grad_template (height x width f32:
+ * sum_f g_f dL_f/dT), grad_flow (n x height x width x 2 f32: g_f dL_f/du_f),
+ * hessian (n x 144 f64: the Gauss-Newton matrix J^T J, M x M row-major),
+ * where g_f = grad_loss[f] (NULL: 1). The backward pass recomputes the warp
+ * instead of storing it. Device buffers; stream ordered. Calls on one device
+ * share scratch memory: do not overlap them. */
+int sst_warp_residual(const float * frames, int n, int width, int height, size_t frame_stride,
+    const float * tmpl, const sst_motion_model * model, const float * params, const float * flow,
+    const double * grad_loss, double * loss, float * grad_params, float * grad_template, float * grad_flow,
+    double * hessian, void * stream);
+
 /* ------------------------------------------------------------ ROI batches */
 
 /* One crop of a ROI batch: its reference and current images (same size),

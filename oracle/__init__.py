@@ -98,6 +98,11 @@ def lib():
             "orc_bayer_pattern_mask": (None, [i, i, i, p]),
             "orc_bayer_accumulate": (None, [p, i, i, p, p, p, p, p, p]),
             "orc_warp_grid": (None, [p, p, i, i, p, p]),
+            "orc_resize_area": (None, [p, i, i, p, i, i]),
+            "orc_resize_cubic": (None, [p, i, i, p, i, i]),
+            "orc_eccflow_levels": (i, [i, i, p, p, p, i]),
+            "orc_eccflow": (i, [p, p, p, i, i, p, p]),
+            "orc_warp_residual": (d, [p, p, p, p, p, i, i, p, p, p]),
             "orc_laplacian_energy": (d, [p, i, i]),
             "orc_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
             "orc_set_num_threads": (None, [i]),
@@ -366,6 +371,63 @@ def bayer_average(colorid, frames, motion_type=None, params=None, weights=None, 
         mx, my = warp_grid(m, st, w, h)
         bayer_accumulate(img, mx, my, pat, np.where(msk > 0, wf, 0.0), acc, cntr)
     return acc, cntr
+
+
+class FlowOpts(C.Structure):
+    """c_eccflow_options (ecc2.h:515-527); downscale 0 recursive resize, 1 full resize, 2 pyrDown"""
+    _fields_ = [("update_multiplier", C.c_double), ("scale_factor", C.c_double), ("noise_level", C.c_double),
+                ("max_iterations", C.c_int), ("support_scale", C.c_int), ("min_image_size", C.c_int),
+                ("max_pyramid_level", C.c_int), ("downscale", C.c_int)]
+
+
+def flow_opts(update_multiplier=1.5, scale_factor=0.5, noise_level=-1.0, max_iterations=1, support_scale=5,
+              min_image_size=4, max_pyramid_level=-1, downscale=0) -> FlowOpts:
+    """defaults of c_eccflow_options (ecc2.h:515-527)"""
+    return FlowOpts(update_multiplier, scale_factor, noise_level, max_iterations, support_scale, min_image_size,
+                    max_pyramid_level, downscale)
+
+
+def resize_area(img, dw, dh):
+    a = _f64(img)
+    out = np.empty((dh, dw))
+    lib().orc_resize_area(_ptr(a), a.shape[1], a.shape[0], _ptr(out), dw, dh)
+    return out
+
+
+def resize_cubic(img, dw, dh):
+    a = _f64(img)
+    out = np.empty((dh, dw))
+    lib().orc_resize_cubic(_ptr(a), a.shape[1], a.shape[0], _ptr(out), dw, dh)
+    return out
+
+
+def eccflow_levels(w, h, o: FlowOpts):
+    ws = np.zeros(64, np.int32)
+    hs = np.zeros(64, np.int32)
+    n = lib().orc_eccflow_levels(w, h, C.byref(o), _ptr(ws), _ptr(hs), 64)
+    return list(zip(ws[:n].tolist(), hs[:n].tolist()))
+
+
+def eccflow(o: FlowOpts, ref, cur, init_flow=None):
+    """c_eccflow: reference + current -> flow (h, w, 2) (rmap = identity + flow)"""
+    r, c = _f64(ref), _f64(cur)
+    h, w = r.shape
+    init = None if init_flow is None else _f64(init_flow)
+    out = np.empty((h, w, 2))
+    lib().orc_eccflow(C.byref(o), _ptr(r), _ptr(c), w, h, _ptr(init), _ptr(out))
+    return out
+
+
+def warp_residual(m: Model, state, img, tmpl, flow=None):
+    """L = 1/2 sum (I(W(x; p) + u(x)) - T(x))^2 and its exact gradients (p, T, u)."""
+    s, a, t = _f64(state), _f64(img), _f64(tmpl)
+    h, w = a.shape
+    f = None if flow is None else _f64(flow)
+    gp = np.zeros(16)
+    gt = np.zeros((h, w))
+    gu = np.zeros((h, w, 2))
+    L = lib().orc_warp_residual(C.byref(m), _ptr(s), _ptr(a), _ptr(t), _ptr(f), w, h, _ptr(gp), _ptr(gt), _ptr(gu))
+    return L, gp[:nparams(m)], gt, gu
 
 
 def pipeline_opts(passes=(AFFINE, HOMOGRAPHY), method=IC, maxlevel=4, max_iterations=50, epsx=0.2,

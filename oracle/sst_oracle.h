@@ -144,6 +144,34 @@ void orc_warp_grid(const orc_model * m, const double * state, int w, int h, doub
 void orc_bayer_accumulate(const double * src, int w, int h, const double * mapx, const double * mapy,
     const uint8_t * pattern, const double * weights, double * acc, double * cntr);
 
+/* ------------------------------------------------------------- c_eccflow */
+
+/* c_eccflow_options (ecc2.h:515-527); downscale: 0 recursive INTER_AREA
+ * resize, 1 full INTER_AREA resize from level 0, 2 pyrDown */
+typedef struct orc_flow_opts {
+  double update_multiplier, scale_factor, noise_level;
+  int max_iterations, support_scale, min_image_size, max_pyramid_level, downscale;
+} orc_flow_opts;
+
+/* cv::resize INTER_AREA (pixel-area relation) and INTER_CUBIC (a = -0.75) */
+void orc_resize_area(const double * src, int sw, int sh, double * dst, int dw, int dh);
+void orc_resize_cubic(const double * src, int sw, int sh, double * dst, int dw, int dh);
+/* pyramid level sizes of c_eccflow::set_reference_image; returns the count */
+int orc_eccflow_levels(int w, int h, const orc_flow_opts * o, int * ws, int * hs, int max_levels);
+/* c_eccflow::compute_uv(current, rmap) after set_reference_image(reference):
+ * flow (h x w x 2, interleaved u, v); init_flow may be NULL (zero start) */
+int orc_eccflow(const orc_flow_opts * o, const double * ref, const double * cur, int w, int h,
+    const double * init_flow, double * flow);
+
+/* The warp residual objective of the adjoint: for frame f,
+ *   r(x) = I_f(W(x; p_f) + u_f(x)) - T(x)   (bilinear, BORDER_REPLICATE)
+ *   L_f = 1/2 sum_x r(x)^2
+ * with its exact gradients: dL/dp (M) through the derivative of the
+ * bilinear interpolant, dL/dT(x) = -r(x), and dL/du(x) = r(x) grad I.
+ * flow may be NULL; grad outputs may be NULL. Returns L_f. */
+double orc_warp_residual(const orc_model * m, const double * state, const double * img, const double * tmpl,
+    const double * flow, int w, int h, double * grad_p, double * grad_t, double * grad_u);
+
 /* sharpness weight of a frame: mean of the squared 5-point Laplacian over the
  * interior of a level image */
 double orc_laplacian_energy(const double * img, int w, int h);

@@ -98,6 +98,13 @@ def lib():
             "sst_weighted_average_add_warped_batch_noalloc": (i, [p, i, i, i, i, sz, sz, d, p, p, p, p, i, p, i, i,
                                                                   p]),
             "sst_state_merge": (i, [p, p, i, sz]),
+            "sst_warp_residual": (i, [p, i, i, i, sz, p, p, p, p, p, p, p, p, p, p, p]),
+            "sst_eccflow_options_default": (None, [p]),
+            "sst_eccflow_create": (i, [p, p]),
+            "sst_eccflow_destroy": (i, [p]),
+            "sst_eccflow_set_reference_image": (i, [p, p, i, i, i, sz, d, i, p]),
+            "sst_eccflow_num_levels": (i, [p]),
+            "sst_eccflow_compute_batch": (i, [p, p, i, i, sz, sz, d, i, p, p, p]),
             "sst_roi_batch_create": (i, [p, p]),
             "sst_roi_batch_destroy": (i, [p]),
             "sst_roi_batch_align": (i, [p, i, p, p, p, i, d, i, i, p, p, p, p, p, p, p, p]),
@@ -222,6 +229,69 @@ class c_ecch:
         M = nparams(passes[-1])
         return {"params": params[:, :M], "status": status, "iterations": iters, "eps": eps, "rho": rho,
                 "weight": weight}
+
+
+class EccflowOptions(C.Structure):
+    """c_eccflow_options (ecc2.h:515-527)"""
+    _fields_ = [("update_multiplier", C.c_double), ("scale_factor", C.c_double), ("noise_level", C.c_double),
+                ("input_smooth_sigma", C.c_double), ("reference_smooth_sigma", C.c_double),
+                ("max_iterations", C.c_int32), ("support_scale", C.c_int32), ("min_image_size", C.c_int32),
+                ("max_pyramid_level", C.c_int32), ("downscale", C.c_int32), ("reserved", C.c_int32)]
+
+
+def eccflow_options(**kw) -> EccflowOptions:
+    o = EccflowOptions()
+    lib().sst_eccflow_options_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class c_eccflow:
+    """c_eccflow (ecc2.h:548-662) over sst_eccflow_*: dense flow of a batch of
+    frames against one reference."""
+
+    def __init__(self, options: Optional[EccflowOptions] = None):
+        self._h = C.c_void_p()
+        o = options if options is not None else eccflow_options()
+        _check(lib().sst_eccflow_create(C.byref(self._h), C.byref(o)), "sst_eccflow_create")
+        self.shape = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_eccflow_destroy(h)
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_reference_image(self, img: np.ndarray, scale: float = 1.0):
+        a = np.ascontiguousarray(img)
+        _check(lib().sst_eccflow_set_reference_image(self._h, _ptr(a), _NP_DEPTH[a.dtype], a.shape[1], a.shape[0],
+                                                      a.strides[0], scale, 0, None), "set_reference_image")
+        self.shape = a.shape
+
+    def num_levels(self) -> int:
+        return lib().sst_eccflow_num_levels(self._h)
+
+    def compute(self, frames: np.ndarray, init_rmap=None, scale: float = 1.0):
+        """frames (n, h, w) -> rmaps (n, h, w, 2) = identity + flow"""
+        fr = np.ascontiguousarray(frames)
+        if fr.ndim == 2:
+            fr = fr[None]
+        n, hh, ww = fr.shape
+        out = np.zeros((n, hh, ww, 2), np.float32)
+        init = None if init_rmap is None else np.ascontiguousarray(init_rmap, np.float32).reshape(n, hh, ww, 2)
+        _check(lib().sst_eccflow_compute_batch(self._h, _ptr(fr), _NP_DEPTH[fr.dtype], n, fr.strides[1], fr.strides[0],
+                                               scale, 0, _ptr(init), _ptr(out), None), "sst_eccflow_compute_batch")
+        return out
+
+    def compute_device(self, frames, n, depth, row_stride, frame_stride, rmap_out, init_rmap=None, scale=1.0):
+        _check(lib().sst_eccflow_compute_batch(self._h, _ptr(frames), depth, n, row_stride, frame_stride, scale, 1,
+                                               _ptr(init_rmap), _ptr(rmap_out), None), "sst_eccflow_compute_batch")
+        return rmap_out
 
 
 class Roi(C.Structure):

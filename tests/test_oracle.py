@@ -307,3 +307,115 @@ def test_stack_remap_mask_is_eroded(oracle):
     # both taps inside needs x + 4 <= 49 -> x <= 45; the 5x5 erosion removes 2 more columns
     assert msk[20, 43] == 255 and msk[20, 44] == 0
     assert msk[20, 0] == 255
+
+
+# ----------------------------------------------------------------- c_eccflow
+
+def test_resize_area_integer_factor_is_block_mean(oracle):
+    rng = np.random.default_rng(21)
+    img = rng.uniform(0, 1, size=(32, 48))
+    out = oracle.resize_area(img, 12, 8)
+    assert np.allclose(out, img.reshape(8, 4, 12, 4).mean(axis=(1, 3)), atol=1e-12)
+
+
+def test_resize_area_fractional_preserves_constants_and_mean(oracle):
+    img = np.full((37, 53), 3.25)
+    assert np.allclose(oracle.resize_area(img, 20, 14), 3.25, atol=1e-12)
+    ramp = np.add.outer(np.arange(37.0), np.arange(53.0))
+    out = oracle.resize_area(ramp, 40, 28)       # scale 1.325: partial cells on both ends
+    assert abs(out.mean() - ramp.mean()) < 0.05
+
+
+def _keys(t, a=-0.75):
+    t = abs(t)
+    if t <= 1:
+        return (a + 2) * t ** 3 - (a + 3) * t ** 2 + 1
+    if t < 2:
+        return a * t ** 3 - 5 * a * t ** 2 + 8 * a * t - 4 * a
+    return 0.0
+
+
+def test_resize_cubic_matches_the_keys_kernel(oracle):
+    """INTER_CUBIC: Keys convolution (a = -0.75) at (x + 0.5) s - 0.5, taps clamped"""
+    rng = np.random.default_rng(8)
+    img = rng.uniform(0, 1, size=(9, 11))
+    out = oracle.resize_cubic(img, 17, 13)
+    sx, sy = 11 / 17, 9 / 13
+
+    def axis(n_src, d, s):
+        f = (d + 0.5) * s - 0.5
+        i0 = int(np.floor(f))
+        return [(min(max(i0 - 1 + k, 0), n_src - 1), _keys(f - (i0 - 1 + k))) for k in range(4)]
+
+    for dy in range(13):
+        for dx in range(17):
+            v = sum(wy * wx * img[iy, ix] for iy, wy in axis(9, dy, sy) for ix, wx in axis(11, dx, sx))
+            assert abs(out[dy, dx] - v) < 1e-12
+    assert np.allclose(oracle.resize_cubic(np.full((9, 11), 2.5), 17, 13), 2.5, atol=1e-12)
+
+
+def test_eccflow_levels_follow_the_reference_rule(oracle):
+    o = oracle.flow_opts(scale_factor=0.75, support_scale=4, min_image_size=-1)
+    lv = oracle.eccflow_levels(100, 80, o)
+    assert lv[0] == (100, 80)
+    for (pw, ph), (nw, nh) in zip(lv, lv[1:]):
+        assert (nw, nh) == (int((pw + 1) * 0.75), int((ph + 1) * 0.75))
+    assert max(lv[-1]) > 4
+    nw, nh = int((lv[-1][0] + 1) * 0.75), int((lv[-1][1] + 1) * 0.75)
+    assert max(nw, nh) <= 4                      # the next level would be at or below the minimum
+    assert len(oracle.eccflow_levels(100, 80, oracle.flow_opts(max_pyramid_level=2))) == 3
+
+
+def _textured(w, h, dx=0.0, dy=0.0):
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    X, Y = x - dx, y - dy
+    return (10 + 4 * np.sin(2 * np.pi * X / 17.0) * np.cos(2 * np.pi * Y / 13.0) + 3 * np.sin(2 * np.pi * (X + Y) / 23.0))
+
+
+def test_eccflow_identical_images_give_zero_flow(oracle):
+    img = _textured(96, 64)
+    flow = oracle.eccflow(oracle.flow_opts(scale_factor=0.75, support_scale=3, max_iterations=2), img, img)
+    assert np.abs(flow).max() < 1e-9
+
+
+def test_eccflow_recovers_a_translation(oracle):
+    """current(x) = reference(x - d): the flow (rmap - x) is +d where the
+    warped current matches the reference"""
+    ref = _textured(128, 96)
+    cur = _textured(128, 96, dx=1.2, dy=-0.7)
+    o = oracle.flow_opts(scale_factor=0.5, support_scale=3, max_iterations=3)
+    flow = oracle.eccflow(o, ref, cur)
+    inner = flow[16:-16, 16:-16]
+    assert abs(np.median(inner[..., 0]) - 1.2) < 0.1
+    assert abs(np.median(inner[..., 1]) + 0.7) < 0.1
+
+
+def test_warp_residual_gradients_match_finite_differences(oracle):
+    """Exact gradients of the bilinear warp residual vs central differences.
+    The bilinear interpolant has kinks on the pixel grid, so the parameters are
+    generic (no sample lands exactly on a grid line) and the tolerance covers
+    the samples that cross a grid line within the step: 1e-3 relative at
+    h = 1e-6, 5e-3 relative at the h = 1e-3 of the adjoint checks."""
+    rng = np.random.default_rng(5)
+    h, w = 40, 50
+    img = _textured(w, h) + rng.normal(0, 0.1, size=(h, w))
+    tmpl = _textured(w, h, 0.6, -0.3)
+    m = oracle.model(oracle.AFFINE)
+    p0 = np.array([1.0103217, 0.0201387, 0.4137113, -0.0103911, 0.9903187, -0.2171393])
+    st = oracle.set_params(m, oracle.identity(m), p0)
+    L, gp, gt, gu = oracle.warp_residual(m, st, img, tmpl)
+    for h_fd, tol in ((1e-6, 1e-3), (1e-3, 5e-3)):
+        for k in range(6):
+            pp, pm = p0.copy(), p0.copy()
+            pp[k] += h_fd
+            pm[k] -= h_fd
+            Lp = oracle.warp_residual(m, oracle.set_params(m, oracle.identity(m), pp), img, tmpl)[0]
+            Lm = oracle.warp_residual(m, oracle.set_params(m, oracle.identity(m), pm), img, tmpl)[0]
+            fd = (Lp - Lm) / (2 * h_fd)
+            assert abs(fd - gp[k]) <= tol * abs(gp[k]), (h_fd, k, fd, gp[k])
+    # template gradient: dL/dT = -r (L is quadratic in T: central differences are exact)
+    t2, t3 = tmpl.copy(), tmpl.copy()
+    t2[7, 9] += 1e-3
+    t3[7, 9] -= 1e-3
+    fd_t = (oracle.warp_residual(m, st, img, t2)[0] - oracle.warp_residual(m, st, img, t3)[0]) / 2e-3
+    assert abs(fd_t - gt[7, 9]) < 1e-6
