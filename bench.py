@@ -230,11 +230,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form leg (profiling runs)")
-    ap.add_argument("--workload", choices=["mono", "bayer", "roi"], default="mono",
+    ap.add_argument("--workload", choices=["mono", "bayer", "roi", "flow"], default="mono",
                     help="mono: the headline 1280x960 sequence; bayer: raw RGGB 3096x2080 frames; "
                          "roi: uneven-ROI crops (--frames crops)")
     ap.add_argument("--roi-method", choices=["fa", "lm"], default="fa")
     ap.add_argument("--roi-sample", type=int, default=8, help="crops checked against the oracle")
+    ap.add_argument("--flow-sample", type=int, default=32, help="frames checked against the oracle (flow)")
     args = ap.parse_args()
 
     ws, rank, local = dist_env()
@@ -250,8 +251,8 @@ def main():
             import torch.distributed as dist
             dist.destroy_process_group()
         return
-    if args.workload in ("bayer", "roi"):
-        (main_bayer if args.workload == "bayer" else main_roi)(args, ws, rank, local)
+    if args.workload in ("bayer", "roi", "flow"):
+        {"bayer": main_bayer, "roi": main_roi, "flow": main_flow}[args.workload](args, ws, rank, local)
         if ws > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
@@ -783,6 +784,166 @@ def main_roi(args, ws_, rank, local):
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
                 "accuracy": acc, "frames_ok": int((res["status"] == 0).sum()),
                 "iterations_median": float(np.median(res["iterations"])), "levels": levels}
+        print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- flow workload
+
+FLOW_W = FLOW_H = 1024
+
+
+def flow_cfg(n: int):
+    return {
+        "workload": f"{n} f32 frames {FLOW_W}x{FLOW_H} of a textured scene warped by smooth random fields "
+                    "(Gaussian-filtered white noise, correlation length 64 px, 3 px RMS); c_eccflow with the "
+                    "registration defaults (support_scale 4, scale_factor 0.75, 3 iterations per level, "
+                    "update_multiplier 1.5); adjoint leg: warp residual + gradients to params, template and flow",
+        "frames": n, "width": FLOW_W, "height": FLOW_H, "support_scale": 4, "scale_factor": 0.75,
+        "max_iterations": 3, "l2": "frames (n x 4 MB) and flow planes stream from HBM; no flush needed",
+    }
+
+
+def make_flow_workload(n: int, device, seed: int = SEED + 4):
+    """frames_f(y) = scene(y - d_f(y)), d_f smooth (FFT Gaussian filter of white noise)"""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    ys, xs = torch.meshgrid(torch.arange(FLOW_H, device=device, dtype=torch.float64),
+                            torch.arange(FLOW_W, device=device, dtype=torch.float64), indexing="ij")
+    ref = tiled_scene_torch(xs + 300.0, ys + 200.0).float()
+    fy = torch.fft.fftfreq(FLOW_H, device=device, dtype=torch.float64)
+    fx = torch.fft.rfftfreq(FLOW_W, device=device, dtype=torch.float64)
+    sigma = 64.0
+    tf = torch.exp(-2 * math.pi ** 2 * sigma ** 2 * (fy[:, None] ** 2 + fx[None, :] ** 2))
+    frames = torch.empty((n, FLOW_H, FLOW_W), dtype=torch.float32, device=device)
+    truth = torch.empty((n, FLOW_H, FLOW_W, 2), dtype=torch.float32, device=device)
+    for i in range(n):
+        d = []
+        for _ in range(2):
+            wn = torch.randn((FLOW_H, FLOW_W), generator=g, device=device, dtype=torch.float64)
+            f = torch.fft.irfft2(torch.fft.rfft2(wn) * tf, s=(FLOW_H, FLOW_W))
+            d.append(f * (3.0 / math.sqrt(2.0)) / f.std())
+        truth[i] = torch.stack(d, dim=-1).float()
+        img = tiled_scene_torch(xs - d[0] + 300.0, ys - d[1] + 200.0)
+        frames[i] = (img + torch.randn(img.shape, generator=g, device=device, dtype=img.dtype)).float()
+    return frames, ref, truth
+
+
+def main_flow(args, ws_, rank, local):
+    import torch
+    from serstacker_gb300 import capi as C
+    from serstacker_gb300 import adjoint
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    C.lib()
+    n = args.frames
+    frames, ref, truth = make_flow_workload(n, device)
+    opts = C.eccflow_options(support_scale=4, scale_factor=0.75, max_iterations=3, update_multiplier=1.5,
+                             min_image_size=-1)
+    fl = C.c_eccflow(opts)
+    fl.set_reference_image(ref.cpu().numpy())
+    rmap = torch.empty((n, FLOW_H, FLOW_W, 2), dtype=torch.float32, device=device)
+
+    def step():
+        fl.compute_device(frames, n, C.DEPTH_F32, FLOW_W * 4, FLOW_W * FLOW_H * 4, rmap)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(ws_)
+    torch.cuda.synchronize()
+    C.kernel_launch_count(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(ws_)
+    launches = C.kernel_launch_count()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, ws_)
+    clk = clocks.stop()
+    value = ws_ * n / (ms / 1000.0)
+    # algorithmic bytes: per level and iteration, the fused residual + area pass reads {T, gx, gy} (16 B),
+    # the flow (8 B) and the warped frame (4 B); the cubic update reads and writes the flow (16 B);
+    # per level change the flow is rewritten (8 B); plus the frame read and pyramid writes
+    import oracle as O
+    oo = O.flow_opts(support_scale=4, scale_factor=0.75, max_iterations=3, update_multiplier=1.5, min_image_size=-1)
+    levels = O.eccflow_levels(FLOW_W, FLOW_H, oo)
+    px = sum(w * h for w, h in levels)
+    bytes_frame = 4 * FLOW_W * FLOW_H + 4 * px + 3 * 44 * px + 8 * px + 8 * FLOW_W * FLOW_H
+    achieved = n * bytes_frame / (ms / 1000.0) / 1e9
+    peak, peak_kind = measured_peaks()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "whole c_eccflow step (k_flow_area + k_flow_solve + k_resample)",
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+            "alg_bytes_model": "per pixel of every level: 3 iterations x (28 B residual/area + 16 B flow update) "
+                               "+ 8 B level change + 4 B pyramid; + 12 B per level-0 pixel (frame in, rmap out)",
+            "alg_bytes_per_frame": bytes_frame, "levels": len(levels)}
+    # accuracy: the flow against the true deformation (interior), all frames
+    y, x = torch.meshgrid(torch.arange(FLOW_H, device=device, dtype=torch.float32),
+                          torch.arange(FLOW_W, device=device, dtype=torch.float32), indexing="ij")
+    fl_est = rmap - torch.stack([x, y], dim=-1)
+    err = (fl_est - truth)[:, 32:-32, 32:-32].norm(dim=-1)
+    acc = {"flow_err_vs_truth_px_median": float(err.median()), "truth_rms_px": float(truth.norm(dim=-1).pow(2).mean().sqrt())}
+
+    # adjoint leg: loss + gradients (params, template, flow) + Gauss-Newton matrices, all frames
+    T = ref.contiguous()
+    p = torch.tensor([[1.0, 0.0, 0.0, 0.0, 1.0, 0.0]], device=device).repeat(n, 1)
+    flow_in = fl_est.contiguous()
+    p12 = adjoint._pad12(p)
+    loss = torch.empty(n, dtype=torch.float64, device=device)
+    gp = torch.zeros((n, 12), dtype=torch.float32, device=device)
+    gt = torch.zeros((FLOW_H, FLOW_W), dtype=torch.float32, device=device)
+    gu = torch.zeros((n, FLOW_H, FLOW_W, 2), dtype=torch.float32, device=device)
+    hs = torch.zeros((n, 144), dtype=torch.float64, device=device)
+
+    def adj_step():
+        adjoint._call(frames, T, p12, flow_in, C.AFFINE, loss=loss, grad_params=gp, grad_template=gt,
+                      grad_flow=gu, hessian=hs)
+
+    for _ in range(max(1, args.warmup)):
+        adj_step()
+    torch.cuda.synchronize()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record()
+    for _ in range(args.steps):
+        adj_step()
+    a1.record()
+    torch.cuda.synchronize()
+    adj_ms = a0.elapsed_time(a1) / args.steps
+    # per frame: frame gathers (4), template (4) twice (tiles + template pass), flow read twice (16),
+    # flow gradient write (8)
+    adj_bytes = n * FLOW_W * FLOW_H * (4 + 4 + 16 + 8 + 4)
+    adjoint_line = {"value": n / (adj_ms / 1000.0), "unit": "frames/s", "ms_per_step": adj_ms,
+                    "achieved_gbs": adj_bytes / (adj_ms / 1000.0) / 1e9,
+                    "outputs": "loss, dL/dp (affine), dL/dT, dL/du, J^T J per frame"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        O.build()
+        threads = os.cpu_count() or 1
+        O.set_num_threads(threads)
+        k = max(1, min(args.flow_sample, n))
+        refd = ref.double().cpu().numpy()
+        t0 = time.perf_counter()
+        diffs = []
+        for i in range(k):
+            f_o = O.eccflow(oo, refd, frames[i].double().cpu().numpy())
+            diffs.append(float(np.sqrt(np.mean((fl_est[i].double().cpu().numpy() - f_o) ** 2))))
+        dt = time.perf_counter() - t0
+        cpu = {"value": k / dt, "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": f"the first {k} frames (oracle FP64 c_eccflow, OpenMP, {dt:.1f} s)"}
+        acc["flow_rms_vs_oracle_px"] = diffs
+    if rank == 0:
+        line = {"metric": "frames/sec of c_eccflow dense flow", "value": value, "unit": "frames/s", "n_gpus": ws_,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {**flow_cfg(n), "parallelism": f"replicas x{ws_}"}, "roofline": roof,
+                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "accuracy": acc,
+                "adjoint": adjoint_line}
         print(json.dumps(line), flush=True)
 
 
