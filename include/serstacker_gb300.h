@@ -241,8 +241,10 @@ int sst_weighted_average_load_state(sst_weighted_average * h, const float * stat
  * (c_image_stacking_pipeline.cc:1539-1790): register each frame against the
  * reference of `reg` (sst_ecch_align_batch semantics, min_rho gate), warp it
  * with the registered transform (base_remap, c_frame_registration.cc:
- * 1265-1340), weight it (1, or its Laplacian-energy sharpness when
- * `weighting` is 1) and add it to `acc`. Host frames are streamed to the
+ * 1265-1340), weight it and add it to `acc`. `weighting`: 0 none; 1 the
+ * frame's Laplacian-energy sharpness; 2 focus stacking: per pixel
+ * W = (6 lap^2 + |grad|^2)^2 of the warped frame (5-point Laplacian and
+ * central differences, BORDER_REPLICATE) blurred by a Gaussian of sigma 3. Host frames are streamed to the
  * device in chunks whose copies overlap the registration of the previous
  * chunk. Outputs follow `on_device` and may be NULL. */
 int sst_stack_frames(sst_ecch * reg, sst_weighted_average * acc, const void * frames, int depth, int n,

@@ -103,6 +103,7 @@ def lib():
             "orc_eccflow_levels": (i, [i, i, p, p, p, i]),
             "orc_eccflow": (i, [p, p, p, i, i, p, p]),
             "orc_warp_residual": (d, [p, p, p, p, p, i, i, p, p, p]),
+            "orc_focus_weights": (None, [p, p, p, i, i, i, i, p]),
             "orc_laplacian_energy": (d, [p, i, i]),
             "orc_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
             "orc_set_num_threads": (None, [i]),
@@ -415,6 +416,14 @@ def eccflow(o: FlowOpts, ref, cur, init_flow=None):
     init = None if init_flow is None else _f64(init_flow)
     out = np.empty((h, w, 2))
     lib().orc_eccflow(C.byref(o), _ptr(r), _ptr(c), w, h, _ptr(init), _ptr(out))
+    return out
+
+
+def focus_weights(m: Model, state, src, dw, dh):
+    """focus weights (6 lap^2 + |grad|^2)^2 of the warped frame, Gaussian sigma 3"""
+    s, a = _f64(state), _f64(src)
+    out = np.empty((dh, dw))
+    lib().orc_focus_weights(C.byref(m), _ptr(s), _ptr(a), a.shape[1], a.shape[0], dw, dh, _ptr(out))
     return out
 
 

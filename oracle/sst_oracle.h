@@ -163,6 +163,11 @@ int orc_eccflow_levels(int w, int h, const orc_flow_opts * o, int * ws, int * hs
 int orc_eccflow(const orc_flow_opts * o, const double * ref, const double * cur, int w, int h,
     const double * init_flow, double * flow);
 
+/* focus-stacking weights of a frame warped to the dw x dh grid:
+ * W = (6 lap^2 + |grad|^2)^2 blurred by a Gaussian of sigma 3 */
+void orc_focus_weights(const orc_model * m, const double * state, const double * src, int sw, int sh,
+    int dw, int dh, double * out);
+
 /* The warp residual objective of the adjoint: for frame f,
  *   r(x) = I_f(W(x; p_f) + u_f(x)) - T(x)   (bilinear, BORDER_REPLICATE)
  *   L_f = 1/2 sum_x r(x)^2

@@ -312,3 +312,28 @@ extern "C" double orc_warp_residual(const orc_model * m, const double * state, c
   if( grad_p ) for( int k = 0; k < M; ++k ) grad_p[k] = gp[k];
   return L;
 }
+
+/* ------------------------------------------------------- focus weights */
+
+/* W = (6 lap^2 + |grad|^2)^2 of the frame warped to the dw x dh grid
+ * (bilinear, BORDER_REPLICATE), 5-point Laplacian and central differences
+ * with the output grid replicated at its border, then a Gaussian of sigma 3
+ * (getGaussianKernel(19, 3), BORDER_REPLICATE) */
+extern "C" void orc_focus_weights(const orc_model * m, const double * state, const double * src, int sw, int sh,
+    int dw, int dh, double * out)
+{
+  std::vector<double> wv((size_t) dw * dh), e((size_t) dw * dh);
+  orc_remap_model(m, state, src, sw, sh, dw, dh, ORC_BORDER_REPLICATE, 0, wv.data());
+  auto at = [&](int x, int y) {
+    return wv[(size_t) std::min(std::max(y, 0), dh - 1) * dw + std::min(std::max(x, 0), dw - 1)];
+  };
+  for( int y = 0; y < dh; ++y ) {
+    for( int x = 0; x < dw; ++x ) {
+      const double c = at(x, y), l = at(x - 1, y), r = at(x + 1, y), u = at(x, y - 1), d = at(x, y + 1);
+      const double lap = l + r + u + d - 4 * c, gx = 0.5 * (r - l), gy = 0.5 * (d - u);
+      const double v = 6 * lap * lap + gx * gx + gy * gy;
+      e[(size_t) y * dw + x] = v * v;
+    }
+  }
+  orc_smooth(e.data(), dw, dh, 3.0, out);
+}

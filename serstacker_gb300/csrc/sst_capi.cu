@@ -846,13 +846,40 @@ extern "C" int sst_ecch_align_plain(sst_ecch * h, const void * frames, int depth
 struct sst_weighted_average {
   int w = 0, h = 0;
   DevBuf acc, coeffs, weff, src, wsrc;
+  DevBuf focus_e, focus_w, gk_focus;   // focus weighting: energy maps, blurred maps, Gaussian taps
+  int gk_n = 0;
   int frames = 0;
   size_t plane() const { return (size_t) w * h; }
   ~sst_weighted_average()
   {
     acc.release(), coeffs.release(), weff.release(), src.release(), wsrc.release();
+    focus_e.release(), focus_w.release(), gk_focus.release();
   }
 };
+
+/* focus weighting: per-pixel W = (6 lap^2 + grad^2)^2 of each warped frame,
+ * blurred by a Gaussian of sigma 3 (ksize 19, BORDER_REPLICATE); returns the
+ * n maps on the accumulator's grid */
+static int focus_maps(sst_weighted_average * a, const void * d_frames, int depth, int n, int sw, int sh,
+    size_t row_stride, size_t frame_stride, double scale, int motion, const float * coeffs, const float ** maps,
+    cudaStream_t st)
+{
+  const size_t plane = a->plane();
+  SST_CK(a->focus_e.ensure((size_t) n * plane * sizeof(float)));
+  SST_CK(a->focus_w.ensure((size_t) n * plane * sizeof(float)));
+  if( !a->gk_n ) {
+    float gk[64];
+    a->gk_n = gaussian_kernel(3.0, gk);
+    SST_CK(a->gk_focus.ensure(64 * sizeof(float)));
+    SST_CK(cudaMemcpy(a->gk_focus.p, gk, a->gk_n * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  SST_CK_LAUNCH(launch_focus_energy(d_frames, depth, row_stride, frame_stride, sw, sh, scale, motion, coeffs, n, a->w,
+      a->h, a->focus_e.as<float>(), st));
+  SST_CK_LAUNCH(launch_convert_smooth(a->focus_e.p, SST_DEPTH_F32, n, a->w, a->h, (size_t) a->w * sizeof(float),
+      plane * sizeof(float), 1.0, a->gk_focus.as<float>(), a->gk_n, a->focus_w.as<float>(), plane, st));
+  *maps = a->focus_w.as<float>();
+  return SST_OK;
+}
 
 extern "C" int sst_weighted_average_create(sst_weighted_average ** out, int width, int height)
 {
@@ -917,13 +944,17 @@ extern "C" int sst_weighted_average_add(sst_weighted_average * a, const void * s
 
 static int add_warped_device(sst_weighted_average * a, const void * d_frames, int depth, int n, int sw, int sh,
     size_t row_stride, size_t frame_stride, double scale, const sst_motion_model & m, const float * d_params,
-    const int32_t * d_status, const float * d_weights, int border, cudaStream_t st)
+    const int32_t * d_status, const float * d_weights, int border, cudaStream_t st, bool focus = false)
 {
   SST_CK(a->coeffs.ensure((size_t) n * SST_NCOEF * sizeof(float)));
   SST_CK(a->weff.ensure((size_t) n * sizeof(float)));
   SST_CK_LAUNCH(launch_coeffs_from_params(m, d_params, n, a->coeffs.as<float>(), st));
   SST_CK_LAUNCH(launch_effective_weights(d_weights, d_status, n, a->weff.as<float>(), st));
+  const float * maps = nullptr;
+  if( focus ) SST_TRY(focus_maps(a, d_frames, depth, n, sw, sh, row_stride, frame_stride, scale, m.type,
+      a->coeffs.as<float>(), &maps, st));
   StackArgs s;
+  s.wmap = maps;
   s.frames = (const uint8_t *) d_frames;
   s.row_stride = row_stride, s.frame_stride = frame_stride;
   s.sw = sw, s.sh = sh, s.n = n;
@@ -1079,6 +1110,7 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
     return set_error(SST_ERR_UNSUPPORTED, "unsupported border mode %d", border);
   if( h->L == 0 ) return set_error(SST_ERR_STATE, "c_ecch: no reference image was set");
   if( n < 1 ) return set_error(SST_ERR_INVALID_ARG, "n must be >= 1");
+  if( weighting < 0 || weighting > 2 ) return set_error(SST_ERR_INVALID_ARG, "weighting must be 0, 1 or 2");
   if( width != h->w || height != h->h || acc->w != h->w || acc->h != h->h )
     return set_error(SST_ERR_INVALID_ARG, "frame, reference and accumulator sizes must match");
   if( depth_bytes(depth) == 0 ) return set_error(SST_ERR_INVALID_ARG, "unsupported depth %d", depth);
@@ -1120,8 +1152,8 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
     }
     SST_TRY(register_device(h, d_frames, depth, nc, row_stride, frame_stride, scale, num_passes, passes, nullptr, false));
     SST_TRY(add_warped_device(acc, d_frames, depth, nc, width, height, row_stride, frame_stride, scale, last,
-        h->out_params.as<float>(), h->out_status.as<int32_t>(), weighting ? h->out_weight.as<float>() : nullptr,
-        border, st));
+        h->out_params.as<float>(), h->out_status.as<int32_t>(), weighting == 1 ? h->out_weight.as<float>() : nullptr,
+        border, st, weighting == 2));
     if( !on_device ) SST_CK(cudaEventRecord(h->ev_free[buf], st));
     SST_TRY(copy_out(h->res_params.as<float>() + (size_t) f0 * 12, h->out_params.p, (size_t) nc * 12 * sizeof(float), 1, st));
     SST_TRY(copy_out(h->res_status.as<int32_t>() + f0, h->out_status.p, (size_t) nc * sizeof(int32_t), 1, st));
@@ -1161,6 +1193,7 @@ extern "C" int sst_stack_bayer_frames(sst_ecch * h, sst_weighted_average * const
   if( n < 1 ) return set_error(SST_ERR_INVALID_ARG, "n must be >= 1");
   if( (width & 1) || (height & 1) )
     return set_error(SST_ERR_INVALID_ARG, "Can not average raw bayer planes for uneven image size %dx%d", width, height);
+  if( weighting < 0 || weighting > 2 ) return set_error(SST_ERR_INVALID_ARG, "weighting must be 0, 1 or 2");
   const int pw = width / 2, ph = height / 2;
   if( pw != h->w || ph != h->h )
     return set_error(SST_ERR_INVALID_ARG, "the reference must be the binned size (width/2 x height/2)");
@@ -1212,9 +1245,16 @@ extern "C" int sst_stack_bayer_frames(sst_ecch * h, sst_weighted_average * const
     SST_TRY(register_device(h, h->binned.p, SST_DEPTH_U16, nc, (size_t) pw * 2, bin_frame, scale, num_passes, passes,
         nullptr, false));
     SST_CK_LAUNCH(launch_coeffs_from_params(last, h->out_params.as<float>(), nc, a0->coeffs.as<float>(), st));
-    SST_CK_LAUNCH(launch_effective_weights(weighting ? h->out_weight.as<float>() : nullptr, h->out_status.as<int32_t>(), nc,
-        a0->weff.as<float>(), st));
+    SST_CK_LAUNCH(launch_effective_weights(weighting == 1 ? h->out_weight.as<float>() : nullptr,
+        h->out_status.as<int32_t>(), nc, a0->weff.as<float>(), st));
+    const float * maps = nullptr;
+    if( weighting == 2 ) {
+      // focus weights of the warped binned luminance, shared by the four planes
+      SST_TRY(focus_maps(a0, h->binned.p, SST_DEPTH_U16, nc, pw, ph, (size_t) pw * 2, bin_frame, scale, last.type,
+          a0->coeffs.as<float>(), &maps, st));
+    }
     BayerPlanesArgs b;
+    b.wmap = maps;
     b.frames = (const uint8_t *) d_frames;
     b.row_stride = row_stride, b.frame_stride = frame_stride;
     b.pw = pw, b.ph = ph, b.n = nc;

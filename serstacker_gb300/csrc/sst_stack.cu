@@ -115,8 +115,9 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
             const float v10 = (float) __ldg(r1), v11 = (float) __ldg(r1 + 1);
             const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
             const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
-            kahan_add(S[k], cS[k], wf * val);
-            kahan_add(Wt[k], cW[k], wf);
+            const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
+            kahan_add(S[k], cS[k], wp * val);
+            kahan_add(Wt[k], cW[k], wp);
           }
         }
       }
@@ -155,8 +156,9 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
           const float v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
           const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
           const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
-          kahan_add(S[k], cS[k], wf * val);
-          kahan_add(Wt[k], cW[k], wf);
+          const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
+          kahan_add(S[k], cS[k], wp * val);
+          kahan_add(Wt[k], cW[k], wp);
         }
       }
     }
@@ -352,6 +354,68 @@ cudaError_t launch_remap(const void * src, int depth, int sw, int sh, size_t rs,
   return cudaGetLastError();
 }
 
+/* ------------------------------------------------------- focus weights */
+
+/* Focus-stacking weight of every output pixel of every frame (the README's
+ * W(x, y) = (6 lap^2 + grad^2)^2 before its Gaussian blur): the frame warped to
+ * the output grid (bilinear, BORDER_REPLICATE), its 5-point Laplacian and
+ * central-difference gradient with the output grid replicated at its border. */
+template<int FAM, typename T>
+__global__ void __launch_bounds__(256) k_focus_energy(const uint8_t * frames, size_t rs, size_t fstride, int sw, int sh,
+    float scale, const float * coeffs, int dw, int dh, float * out)
+{
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if( x >= dw || y >= dh ) return;
+  const int f = blockIdx.z;
+  float c[SST_NCOEF];
+#pragma unroll
+  for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __ldg(coeffs + (size_t) f * SST_NCOEF + i);
+  const uint8_t * fb = frames + (size_t) f * fstride;
+  auto warped = [&](int xx, int yy) {
+    const spos s = warp_pos<FAM>(c, clampi(xx, 0, dw - 1), clampi(yy, 0, dh - 1));
+    const float v00 = tap<T>(fb, rs, sw, sh, s.x0, s.y0, SST_BORDER_REPLICATE);
+    const float v01 = tap<T>(fb, rs, sw, sh, s.x0 + 1, s.y0, SST_BORDER_REPLICATE);
+    const float v10 = tap<T>(fb, rs, sw, sh, s.x0, s.y0 + 1, SST_BORDER_REPLICATE);
+    const float v11 = tap<T>(fb, rs, sw, sh, s.x0 + 1, s.y0 + 1, SST_BORDER_REPLICATE);
+    const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+    return fmaf(s.fy, t1 - t0, t0) * scale;
+  };
+  const float c0 = warped(x, y), l = warped(x - 1, y), r = warped(x + 1, y), u = warped(x, y - 1), d = warped(x, y + 1);
+  const float lap = (l + r + u + d) - 4.f * c0;
+  const float gx = 0.5f * (r - l), gy = 0.5f * (d - u);
+  const float e = fmaf(6.f * lap, lap, fmaf(gx, gx, gy * gy));
+  out[(size_t) f * dw * dh + (size_t) y * dw + x] = e * e;
+}
+
+cudaError_t launch_focus_energy(const void * frames, int depth, size_t row_stride, size_t frame_stride, int sw, int sh,
+    double scale, int motion, const float * coeffs, int n, int dw, int dh, float * out, cudaStream_t st)
+{
+  dim3 grid((dw + 31) / 32, (dh + 7) / 8, n);
+  const uint8_t * fr = (const uint8_t *) frames;
+  const int fam = motion_family(motion);
+#define SST_LAUNCH_FOCUS(FAMV, TV) k_focus_energy<FAMV, TV><<<grid, 256, 0, st>>>(fr, row_stride, frame_stride, sw, sh, (float) scale, coeffs, dw, dh, out)
+  switch ( depth ) {
+  case SST_DEPTH_U8:
+    if( fam == FAM_AFFINE ) SST_LAUNCH_FOCUS(FAM_AFFINE, uint8_t);
+    else if( fam == FAM_HOMOG ) SST_LAUNCH_FOCUS(FAM_HOMOG, uint8_t);
+    else SST_LAUNCH_FOCUS(FAM_QUAD, uint8_t);
+    break;
+  case SST_DEPTH_U16:
+    if( fam == FAM_AFFINE ) SST_LAUNCH_FOCUS(FAM_AFFINE, uint16_t);
+    else if( fam == FAM_HOMOG ) SST_LAUNCH_FOCUS(FAM_HOMOG, uint16_t);
+    else SST_LAUNCH_FOCUS(FAM_QUAD, uint16_t);
+    break;
+  case SST_DEPTH_F32:
+    if( fam == FAM_AFFINE ) SST_LAUNCH_FOCUS(FAM_AFFINE, float);
+    else if( fam == FAM_HOMOG ) SST_LAUNCH_FOCUS(FAM_HOMOG, float);
+    else SST_LAUNCH_FOCUS(FAM_QUAD, float);
+    break;
+  default: return cudaErrorInvalidValue;
+  }
+#undef SST_LAUNCH_FOCUS
+  return cudaGetLastError();
+}
+
 /* ----------------------------------------------------------- Bayer planes */
 
 /* extract_bayer_planes: dst[y][x][0..3] = src(2y,2x), src(2y,2x+1), src(2y+1,2x), src(2y+1,2x+1) */
@@ -468,6 +532,7 @@ __global__ void __launch_bounds__(256) k_stack_bayer_planes(BayerPlanesArgs a)
           const int y = ty0 + ly0 + 4 * k;
           if( y >= a.ph ) continue;
           const spos s = warp_pos<FAM>(c, x, y);
+          const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.pw + x) : wf;
           // raw rows 2 y0 .. 2 y0 + 3, columns 2 x0 .. 2 x0 + 3 (two u32 per row)
           const uint8_t * r = fb + (size_t) (2 * s.y0) * a.row_stride + (size_t) s.x0 * 4;
           uint32_t q[4][2];
@@ -482,9 +547,9 @@ __global__ void __launch_bounds__(256) k_stack_bayer_planes(BayerPlanesArgs a)
             const float v00 = (float) ((q[dy][0] >> sh) & 0xffffu), v01 = (float) ((q[dy][1] >> sh) & 0xffffu);
             const float v10 = (float) ((q[dy + 2][0] >> sh) & 0xffffu), v11 = (float) ((q[dy + 2][1] >> sh) & 0xffffu);
             const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-            kahan_add(S[k][p], cS[k][p], wf * (fmaf(s.fy, t1 - t0, t0) * a.scale));
+            kahan_add(S[k][p], cS[k][p], wp * (fmaf(s.fy, t1 - t0, t0) * a.scale));
           }
-          kahan_add(Wt[k], cW[k], wf);
+          kahan_add(Wt[k], cW[k], wp);
         }
       }
       continue;
@@ -512,6 +577,7 @@ __global__ void __launch_bounds__(256) k_stack_bayer_planes(BayerPlanesArgs a)
         const uint8_t * pm = s_h + ly * SA_TX + lx;
         if( pm[0] & pm[SA_TX] & pm[2 * SA_TX] & pm[3 * SA_TX] & pm[4 * SA_TX] ) {
           const spos s = warp_pos<FAM>(c, x, y);
+          const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.pw + x) : wf;
 #pragma unroll
           for( int p = 0; p < 4; ++p ) {
             const float v00 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0, s.y0, p, a.border);
@@ -519,9 +585,9 @@ __global__ void __launch_bounds__(256) k_stack_bayer_planes(BayerPlanesArgs a)
             const float v10 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0, s.y0 + 1, p, a.border);
             const float v11 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0 + 1, s.y0 + 1, p, a.border);
             const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-            kahan_add(S[k][p], cS[k][p], wf * (fmaf(s.fy, t1 - t0, t0) * a.scale));
+            kahan_add(S[k][p], cS[k][p], wp * (fmaf(s.fy, t1 - t0, t0) * a.scale));
           }
-          kahan_add(Wt[k], cW[k], wf);
+          kahan_add(Wt[k], cW[k], wp);
         }
       }
     }

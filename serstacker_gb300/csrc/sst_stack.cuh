@@ -20,6 +20,7 @@ struct StackArgs {
   float * acc;              // 4 planes: S, cS, W, cW
   size_t plane;             // floats per plane
   int border;               // image border mode of the remap (SST_BORDER_*)
+  const float * wmap = nullptr;   // optional per-pixel weight maps (n x plane, output grid)
 };
 
 /* four Bayer planes of raw u16 mosaic frames, stacked into four accumulators */
@@ -34,6 +35,7 @@ struct BayerPlanesArgs {
   float * acc[4];           // 4 planes (S, cS, W, cW) per Bayer plane
   size_t plane;
   int border;
+  const float * wmap = nullptr;   // optional per-pixel weight maps (n x plane)
 };
 
 cudaError_t launch_coeffs_from_params(const sst_motion_model & m, const float * params, int n, float * coeffs, cudaStream_t st);
@@ -48,6 +50,9 @@ cudaError_t launch_remap(const void * src, int depth, int sw, int sh, size_t rs,
 cudaError_t launch_average_bayer_planes_batch(const void * src, int w, int h, size_t rs, size_t frame_stride, int n,
     uint16_t * dst, cudaStream_t st);
 cudaError_t launch_stack_bayer_planes(const BayerPlanesArgs & a, int motion, cudaStream_t st);
+/* focus weights W = (6 lap^2 + |grad|^2)^2 of each frame warped to the output grid */
+cudaError_t launch_focus_energy(const void * frames, int depth, size_t row_stride, size_t frame_stride, int sw, int sh,
+    double scale, int motion, const float * coeffs, int n, int dw, int dh, float * out, cudaStream_t st);
 cudaError_t launch_bayer_planes(int op, const uint16_t * src, int w, int h, size_t rs, uint16_t * dst, cudaStream_t st);
 
 }  // namespace sst

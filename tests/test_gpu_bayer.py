@@ -255,3 +255,38 @@ def test_stack_bayer_frames_device_and_host_inputs_agree(gpu):
         states.append([a.save_state()[0] for a in accs])
     for k in range(4):
         assert np.array_equal(states[0][k], states[1][k]), k
+
+
+def test_stack_bayer_frames_focus_weights(gpu, oracle):
+    """weighting = 2 on the Bayer pipeline: the focus map of the warped binned
+    luminance weights all four planes (1e-4 relative, FP32 Laplacians)."""
+    C, O = gpu, oracle
+    W_, H_, n = 192, 128, 4
+    pw, ph = W_ // 2, H_ // 2
+    frames, ref_raw, _ = _raw_sequence(n, W_, H_, 31)
+    scale = 1.0 / 4096
+    ref_bin = O.average_bayer_planes(ref_raw)
+    reg = C.c_ecch(C.default_options(method=C.IC, maxlevel=2, max_iterations=30, epsx=0.01, minimum_image_size=16))
+    reg.set_reference_image(ref_bin.astype(np.float32), scale=scale)
+    accs = [C.c_weigthed_average(pw, ph) for _ in range(4)]
+    out = C.stack_bayer_frames(reg, accs, frames, [C.TRANSLATION], scale, weighting=2)
+    m = O.model(C.TRANSLATION)
+    planes = np.stack([O.extract_bayer_planes(frames[i]) for i in range(n)])
+    for k in range(4):
+        S = np.zeros((ph, pw))
+        Wt = np.zeros((ph, pw))
+        for i in range(n):
+            st = O.set_params(m, O.identity(m), out["params"][i][:2].astype(np.float64))
+            dst, msk = O.stack_remap(m, st, planes[i, ..., k].astype(np.float64) * scale, pw, ph)
+            fw = O.focus_weights(m, st, O.average_bayer_planes(frames[i]).astype(np.float64) * scale, pw, ph)
+            wt = np.where(msk > 0, fw, 0.0)
+            S += wt * dst
+            Wt += wt
+        st_g, _ = accs[k].save_state()
+        Sg = st_g[0].astype(np.float64) + st_g[1]
+        Wg = st_g[2].astype(np.float64) + st_g[3]
+        ok = (Wt > 0) & (Wg > 0)
+        assert ((Wt > 0) == (Wg > 0)).mean() > 0.999
+        a_o, a_g = S[ok] / Wt[ok], Sg[ok] / Wg[ok]
+        rel = np.abs(a_g - a_o) / np.maximum(np.abs(a_o), 0.01 * float(a_o.max()))
+        assert rel.max() <= 1e-4, (k, rel.max())

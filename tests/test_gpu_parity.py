@@ -264,3 +264,40 @@ def test_failure_status_codes(gpu):
     assert out["status"][0] == C.FRAME_OK
     assert out["status"][1] in (C.FRAME_NAN, C.FRAME_LOW_RHO)
     assert out["status"][2] in (C.FRAME_EMPTY_MASK, C.FRAME_LOW_RHO)
+
+
+def test_pipeline_focus_weights_match_oracle(gpu, oracle):
+    """weighting = 2 (focus stacking): per-pixel W = (6 lap^2 + |grad|^2)^2 of the
+    warped frame, Gaussian sigma 3, times the remapped mask. The weights come
+    from FP32 5-point Laplacians (cancellation on smooth areas), so the
+    stacked values are held to 1e-4 relative here."""
+    C, O = gpu, oracle
+    w, h, n = 160, 120, 4
+    sc = synth.Scene(w, h, 0.3 * min(w, h))
+    frames, _, _ = synth.make_sequence_np(sc, n, seed=17, kind="config1", dtype=np.uint16, gain=64.0,
+                                          blur_range=(0.8, 2.0))
+    ref = synth.reference_np(sc) * 64.0
+    scale = 1.0 / 65535.0
+    opts = C.default_options(method=1, maxlevel=2, max_iterations=30, epsx=0.01, minimum_image_size=16)
+    reg = C.c_ecch(opts)
+    reg.set_reference_image(ref.astype(np.float32), scale=scale)
+    acc = C.c_weigthed_average(w, h)
+    out = C.stack_frames(reg, acc, frames, [3, 4], scale, weighting=2)
+    avg, mask = acc.compute()
+    m = O.model(4)
+    S = np.zeros((h, w))
+    W = np.zeros((h, w))
+    for i in range(n):
+        assert out["status"][i] == 0
+        st = _state_from_params(O, m, out["params"][i][:8])
+        img = frames[i].astype(np.float64) * scale
+        dst, msk = O.stack_remap(m, st, img, w, h)
+        fw = O.focus_weights(m, st, img, w, h)
+        wt = np.where(msk > 0, fw, 0.0)
+        S += wt * dst
+        W += wt
+    both = (mask > 0) & (W > 0)
+    assert ((mask > 0) == (W > 0)).mean() > 0.999
+    ref_avg = S[both] / W[both]
+    rel = np.abs(avg[both] - ref_avg) / np.maximum(np.abs(ref_avg), 0.01 * float(ref_avg.max()))
+    assert rel.max() <= 1e-4, rel.max()

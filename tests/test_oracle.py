@@ -419,3 +419,20 @@ def test_warp_residual_gradients_match_finite_differences(oracle):
     t3[7, 9] -= 1e-3
     fd_t = (oracle.warp_residual(m, st, img, t2)[0] - oracle.warp_residual(m, st, img, t3)[0]) / 2e-3
     assert abs(fd_t - gt[7, 9]) < 1e-6
+
+
+def test_focus_weights_known_answers(oracle):
+    m = oracle.model(oracle.TRANSLATION)
+    st = oracle.identity(m)
+    flat = np.full((30, 40), 7.0)
+    assert np.abs(oracle.focus_weights(m, st, flat, 40, 30)).max() < 1e-20     # no structure, no weight
+    y, x = np.mgrid[0:30, 0:40].astype(np.float64)
+    ramp = 0.5 * x                                  # |grad| = 0.5, lap = 0 away from the borders
+    wgt = oracle.focus_weights(m, st, ramp, 40, 30)
+    assert abs(wgt[15, 20] - 0.25 ** 2) < 1e-12
+    quad = 0.25 * x * x                             # lap = 0.5, grad = (0.5 x, 0)
+    e = (6 * 0.25 + (0.5 * x) ** 2) ** 2
+    raw = oracle.focus_weights(m, st, quad, 40, 30)
+    k = oracle.gaussian_kernel(3.0)
+    assert len(k) == 19
+    assert abs(raw[15, 20] - sum(k[i] * e[15, 20 + i - 9] for i in range(19))) < 1e-6 * raw[15, 20]
