@@ -1016,23 +1016,65 @@ __global__ void __launch_bounds__(256) k_correlation(CorrArgs a)
     const int tx0 = (t % tiles_x) * PW_TX, ty0 = (t / tiles_x) * PW_TY;
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
     const int yend = min(ty0 + PW_TY, lh);
-    const bool interior = !a.refM && rect_interior<FAM>(c, tx0, ty0, min(tx0 + PW_TX, lw) - 1, yend - 1, lw, lh);
+    // warm L2 with the source footprint of this CTA's next item (uniform tiles)
+    if( !a.roi && item + (int) gridDim.x < nitems ) {
+      const int nitem = item + gridDim.x;
+      const int nf = nitem / a.tiles, nt = nitem - nf * a.tiles;
+      const float * nw = a.fs[nf].wc;
+      const int nx0 = (nt % a.tiles_x) * PW_TX, ny0 = (nt / a.tiles_x) * PW_TY;
+      const int row = threadIdx.x >> 2;
+      if( row < PW_TY ) {
+        const int yy = min(ny0 + row, a.h - 1);
+        const int xx = min(nx0 + (threadIdx.x & 3) * 32, a.w - 1);
+        const float dx = fmaf(__ldg(nw + 0), (float) xx, fmaf(__ldg(nw + 1), (float) yy, __ldg(nw + 2)));
+        const float dy = fmaf(__ldg(nw + 3), (float) xx, fmaf(__ldg(nw + 4), (float) yy, __ldg(nw + 5)));
+        const int sx = clampi(xx + (int) __ldg(nw + 12) + (int) floorf(dx), 0, a.w - 1);
+        const int sy = clampi(yy + (int) __ldg(nw + 13) + (int) floorf(dy), 0, a.h - 1);
+        const float * pp = a.pyr + (size_t) nf * a.pyr_stride + (size_t) sy * a.w + sx;
+        asm volatile("prefetch.global.L2 [%0];" :: "l"(pp));
+      }
+    }
     float acc[NS] = { 0, 0, 0, 0, 0, 0 };
-    if( x < lw ) {
+    // per 32-column warp strip and 16-row chunk: chunks whose every tap is inside
+    // the level gather directly (no coverage, no border logic)
+    const int xs0 = tx0 + (threadIdx.x & (PW_TX - 1) & ~31);
+    const int xs1 = min(xs0 + 31, lw - 1);
+    for( int yc = ty0; yc < yend; yc += 16 ) {
+      const int yc1 = min(yc + 15, yend - 1);
+      const bool interior = !a.refM && xs0 < lw && rect_interior<FAM>(c, xs0, yc, xs1, yc1, lw, lh);
+      if( x >= lw ) continue;
+      if( interior ) {
 #pragma unroll 4
-      for( int y = ty0 + (threadIdx.x >> 7); y < yend; y += 2 ) {
-        const spos s = warp_pos<FAM>(c, x, y);
-        const size_t i = (size_t) y * lw + x;
-        bool ok = interior || mask_ok(coverage(lw, lh, s), 254);
-        if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
-        if( ok ) {
-          const float av = __ldg(refT + i) - tshift;
-          const float bv = (interior ? sample_replicate(img, lw, lh, s) : sample_constant0(img, lw, lh, s)) - tshift;
+        for( int y = yc + (threadIdx.x >> 7); y <= yc1; y += 2 ) {
+          const spos s = warp_pos<FAM>(c, x, y);
+          const float * r0 = img + (size_t) s.y0 * lw + s.x0;
+          const float v00 = __ldg(r0), v01 = __ldg(r0 + 1), v10 = __ldg(r0 + lw), v11 = __ldg(r0 + lw + 1);
+          const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+          const float av = __ldg(refT + (size_t) y * lw + x) - tshift;
+          const float bv = fmaf(s.fy, t1 - t0, t0) - tshift;
           acc[0] += av, acc[1] += bv;
           acc[2] = fmaf(av, av, acc[2]);
           acc[3] = fmaf(bv, bv, acc[3]);
           acc[4] = fmaf(av, bv, acc[4]);
           acc[5] += 1.f;
+        }
+      }
+      else {
+#pragma unroll 2
+        for( int y = yc + (threadIdx.x >> 7); y <= yc1; y += 2 ) {
+          const spos s = warp_pos<FAM>(c, x, y);
+          const size_t i = (size_t) y * lw + x;
+          bool ok = mask_ok(coverage(lw, lh, s), 254);
+          if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
+          if( ok ) {
+            const float av = __ldg(refT + i) - tshift;
+            const float bv = sample_constant0(img, lw, lh, s) - tshift;
+            acc[0] += av, acc[1] += bv;
+            acc[2] = fmaf(av, av, acc[2]);
+            acc[3] = fmaf(bv, bv, acc[3]);
+            acc[4] = fmaf(av, bv, acc[4]);
+            acc[5] += 1.f;
+          }
         }
       }
     }

@@ -100,6 +100,77 @@ __global__ void __launch_bounds__(256) k_convert_smooth(const uint8_t * src, int
   }
 }
 
+/* Fixed-radius form: the horizontal pass computes 4 outputs per thread from a
+ * register window filled by 128-bit shared-memory loads, the vertical pass 4
+ * rows per thread from a register column, so each output costs ~3 shared
+ * loads instead of 2 (2R + 1). */
+template<typename T, int R>
+__global__ void __launch_bounds__(256) k_convert_smooth_r(const uint8_t * src, int w, int h, size_t row_stride,
+    size_t frame_stride, float scale, const float * __restrict__ gk, float * dst, size_t dst_stride)
+{
+  constexpr int SW = (CS_TX + 2 * R + 3) & ~3, SH = CS_TY + 2 * R;   // row stride a multiple of 4 floats
+  constexpr int NW = (4 + 2 * R + 3) / 4;                           // float4 loads per 4 outputs
+  __shared__ __align__(16) float s_in[SH * SW];
+  __shared__ __align__(16) float s_h[SH * CS_TX];
+  __shared__ float g[2 * R + 1];
+  const uint8_t * fb = src + (size_t) blockIdx.z * frame_stride;
+  float * out = dst + (size_t) blockIdx.z * dst_stride;
+  const int tx0 = blockIdx.x * CS_TX, ty0 = blockIdx.y * CS_TY;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if( threadIdx.x <= 2 * R ) g[threadIdx.x] = gk[threadIdx.x];
+  for( int yy = wid; yy < SH; yy += 8 ) {
+    const int y = clampi(ty0 - R + yy, 0, h - 1);
+    const uint8_t * rowp = fb + (size_t) y * row_stride;
+#pragma unroll 4
+    for( int xx = lane; xx < SW; xx += 32 ) {
+      const int x = clampi(tx0 - R + xx, 0, w - 1);
+      s_in[yy * SW + xx] = (float) __ldg((const T *) rowp + x) * scale;
+    }
+  }
+  __syncthreads();
+  float gr[2 * R + 1];
+#pragma unroll
+  for( int i = 0; i <= 2 * R; ++i ) gr[i] = g[i];
+  // horizontal: (row, 4-output group) items
+  for( int q = threadIdx.x; q < SH * (CS_TX / 4); q += 256 ) {
+    const int yy = q / (CS_TX / 4), x4 = (q % (CS_TX / 4)) * 4;
+    float v[4 * NW];
+#pragma unroll
+    for( int k = 0; k < NW; ++k ) {
+      const float4 t = *reinterpret_cast<const float4 *>(s_in + yy * SW + x4 + 4 * k);
+      v[4 * k] = t.x, v[4 * k + 1] = t.y, v[4 * k + 2] = t.z, v[4 * k + 3] = t.w;
+    }
+    float o[4];
+#pragma unroll
+    for( int j = 0; j < 4; ++j ) {
+      float a = 0.f;
+#pragma unroll
+      for( int i = 0; i <= 2 * R; ++i ) a = fmaf(gr[i], v[j + i], a);
+      o[j] = a;
+    }
+    *reinterpret_cast<float4 *>(s_h + yy * CS_TX + x4) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+  __syncthreads();
+  // vertical: (4-row group, column) items
+  for( int q = threadIdx.x; q < (CS_TY / 4) * CS_TX; q += 256 ) {
+    const int xx = q % CS_TX, y4 = (q / CS_TX) * 4;
+    const int x = tx0 + xx;
+    float v[4 + 2 * R];
+#pragma unroll
+    for( int i = 0; i < 4 + 2 * R; ++i ) v[i] = s_h[(y4 + i) * CS_TX + xx];
+    if( x >= w ) continue;
+#pragma unroll
+    for( int j = 0; j < 4; ++j ) {
+      const int y = ty0 + y4 + j;
+      if( y >= h ) break;
+      float a = 0.f;
+#pragma unroll
+      for( int i = 0; i <= 2 * R; ++i ) a = fmaf(gr[i], v[j + i], a);
+      out[(size_t) y * w + x] = a;
+    }
+  }
+}
+
 cudaError_t launch_convert_smooth(const void * src, int depth, int n, int w, int h, size_t row_stride,
     size_t frame_stride, double scale, const float * gk, int ksize, float * dst, size_t dst_stride, cudaStream_t st)
 {
@@ -116,6 +187,18 @@ cudaError_t launch_convert_smooth(const void * src, int depth, int n, int w, int
     cudaFuncSetAttribute(k_convert_smooth<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_convert_smooth<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     attr = true;
+  }
+  if( R == 3 ) {   // sigma = 1 (the c_ecch default); 40 KB of static shared memory
+#define SST_CS_R(RV)                                                                                                   \
+    switch ( depth ) {                                                                                                 \
+    case SST_DEPTH_U8: k_convert_smooth_r<uint8_t, RV><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, dst, dst_stride); break; \
+    case SST_DEPTH_U16: k_convert_smooth_r<uint16_t, RV><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, dst, dst_stride); break; \
+    case SST_DEPTH_F32: k_convert_smooth_r<float, RV><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, dst, dst_stride); break; \
+    default: return cudaErrorInvalidValue;                                                                             \
+    }
+    SST_CS_R(3)
+#undef SST_CS_R
+    return cudaGetLastError();
   }
   switch ( depth ) {
   case SST_DEPTH_U8: k_convert_smooth<uint8_t><<<grid, 256, smem, st>>>(s, w, h, row_stride, frame_stride, (float) scale, gk, R, dst, dst_stride, nullptr); break;
@@ -461,7 +544,7 @@ cudaError_t launch_ref_stats(const float * img, const uint8_t * mask, int w, int
 
 /* mean over the interior of a pyramid level of the squared 5-point Laplacian:
  * per-tile {sum, count} partials, combined in order by k_finalize */
-constexpr int LE_TX = 64, LE_TY = 16;
+constexpr int LE_TX = 128, LE_TY = 32;   // 16 pixels per thread
 
 int lap_tiles(int w, int h)
 {
@@ -471,32 +554,35 @@ int lap_tiles(int w, int h)
 __global__ void __launch_bounds__(256) k_lap_energy(const float * pyr, size_t pyr_stride, size_t lvl_off, int w, int h,
     double * partials, int tiles)
 {
-  __shared__ double s_red[8 * 2];
+  __shared__ float s_red[8 * 2];
   const int f = blockIdx.y, t = blockIdx.x;
   const float * img = pyr + (size_t) f * pyr_stride + lvl_off;
   const int tiles_x = (w + LE_TX - 1) / LE_TX;
   const int tx0 = (t % tiles_x) * LE_TX, ty0 = (t / tiles_x) * LE_TY;
-  float acc[2] = { 0, 0 };
+  float s = 0.f, cnt = 0.f;
   const int x = tx0 + (threadIdx.x & (LE_TX - 1));
-  for( int k = 0; k < LE_TY / 4; ++k ) {
-    const int y = ty0 + (threadIdx.x >> 6) + 4 * k;
-    if( x >= 1 && x < w - 1 && y >= 1 && y < h - 1 ) {
-      const float * p = img + (size_t) y * w + x;
-      const float l = __ldg(p - 1) + __ldg(p + 1) + __ldg(p - w) + __ldg(p + w) - 4.f * __ldg(p);
-      acc[0] = fmaf(l, l, acc[0]);
-      acc[1] += 1.f;
+  if( x >= 1 && x < w - 1 ) {
+#pragma unroll 4
+    for( int k = 0; k < LE_TY / 2; ++k ) {
+      const int y = ty0 + (threadIdx.x >> 7) + 2 * k;
+      if( y >= 1 && y < h - 1 ) {
+        const float * p = img + (size_t) y * w + x;
+        const float l = (__ldg(p - 1) + __ldg(p + 1)) + (__ldg(p - w) + __ldg(p + w)) - 4.f * __ldg(p);
+        s = fmaf(l, l, s);
+        cnt += 1.f;
+      }
     }
   }
+  // FP32 within warps (16 values per thread, 32 lanes), FP64 across the 8 warps
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for( int k = 0; k < 2; ++k ) {
-    const double s = warp_sum((double) acc[k]);
-    if( lane == 0 ) s_red[wid * 2 + k] = s;
-  }
+  s = warp_sum(s);
+  cnt = warp_sum(cnt);
+  if( lane == 0 ) s_red[wid * 2] = s, s_red[wid * 2 + 1] = cnt;
   __syncthreads();
   if( threadIdx.x < 2 ) {
-    double s = 0;
-    for( int wv = 0; wv < 8; ++wv ) s += s_red[wv * 2 + threadIdx.x];
-    partials[((size_t) f * tiles + t) * 2 + threadIdx.x] = s;
+    double a = 0;
+    for( int wv = 0; wv < 8; ++wv ) a += (double) s_red[wv * 2 + threadIdx.x];
+    partials[((size_t) f * tiles + t) * 2 + threadIdx.x] = a;
   }
 }
 

@@ -78,6 +78,25 @@ __device__ __forceinline__ float tap(const uint8_t * fb, size_t rs, int sw, int 
 constexpr int SK_TX = 32, SK_TY = 8;          // remap utility tile
 constexpr int SA_TX = 64, SA_TY = 16;         // batched stack tile: 4 pixels per thread
 
+/* frames accumulated in plain FP32 per pixel before each compensated merge */
+constexpr int SA_FLUSH = 16;
+
+/* L2 prefetch of the source footprint of frame f's tile (rows ty0 - 2 ..
+ * ty0 + SA_TY + 1, both ends of each row): 40 threads, one line each */
+template<typename T>
+__device__ __forceinline__ void prefetch_footprint(const StackArgs & a, int f, int tx0, int ty0)
+{
+  if( threadIdx.x >= 2 * (SA_TY + 4) ) return;
+  const float * c = a.coeffs + (size_t) f * SST_NCOEF;
+  const int y = ty0 - 2 + (threadIdx.x >> 1), x = tx0 + (threadIdx.x & 1) * (SA_TX - 1);
+  const float dx = fmaf(__ldg(c + 0), (float) x, fmaf(__ldg(c + 1), (float) y, __ldg(c + 2)));
+  const float dy = fmaf(__ldg(c + 3), (float) x, fmaf(__ldg(c + 4), (float) y, __ldg(c + 5)));
+  const int sx = clampi(x + (int) __ldg(c + 12) + (int) floorf(fminf(fmaxf(dx, -1e6f), 1e6f)), 0, a.sw - 1);
+  const int sy = clampi(y + (int) __ldg(c + 13) + (int) floorf(fminf(fmaxf(dy, -1e6f), 1e6f)), 0, a.sh - 1);
+  const uint8_t * p = a.frames + (size_t) f * a.frame_stride + (size_t) sy * a.row_stride + (size_t) sx * sizeof(T);
+  asm volatile("prefetch.global.L2 [%0];" :: "l"(p));
+}
+
 template<int FAM, typename T>
 __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
 {
@@ -91,12 +110,16 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
   // window whose validity decides the tile's eroded mask (tile + 2 px halo, clipped)
   const int wx0 = max(tx0 - 2, 0), wy0 = max(ty0 - 2, 0);
   const int wx1 = min(tx0 + SA_TX + 1, a.dw - 1), wy1 = min(ty0 + SA_TY + 1, a.dh - 1);
-  float S[PPT], cS[PPT], Wt[PPT], cW[PPT];
+  // compensated running sums, and plain FP32 partials of up to SA_FLUSH frames
+  float S[PPT], cS[PPT], Wt[PPT], cW[PPT], pS[PPT], pW[PPT];
 #pragma unroll
-  for( int k = 0; k < PPT; ++k ) S[k] = cS[k] = Wt[k] = cW[k] = 0.f;
+  for( int k = 0; k < PPT; ++k ) S[k] = cS[k] = Wt[k] = cW[k] = pS[k] = pW[k] = 0.f;
+  int since = 0;                                // frames in the partials (uniform over the CTA)
+  if( a.n > 0 ) prefetch_footprint<T>(a, 0, tx0, ty0);
   for( int f = 0; f < a.n; ++f ) {
     const float wf = __ldg(a.weights + f);
     if( !(wf > 0.f) ) continue;                 // uniform over the CTA
+    if( f + 1 < a.n ) prefetch_footprint<T>(a, f + 1, tx0, ty0);
     float c[SST_NCOEF];
 #pragma unroll
     for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + i);
@@ -116,59 +139,71 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
             const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
             const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
             const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
-            kahan_add(S[k], cS[k], wp * val);
-            kahan_add(Wt[k], cW[k], wp);
+            pS[k] = fmaf(wp, val, pS[k]);
+            pW[k] += wp;
           }
         }
       }
-      continue;
     }
-    // remap(255-mask, LINEAR, CONSTANT 0) >= 255 over the tile + 2 px halo;
-    // positions outside the output count as 255 (erode border value)
-    for( int q = threadIdx.x; q < VW * VH; q += 256 ) {
-      const int qx = tx0 - 2 + q % VW, qy = ty0 - 2 + q / VW;
-      uint8_t v = 1;
-      if( qx >= 0 && qx < a.dw && qy >= 0 && qy < a.dh ) {
-        v = mask_ok(coverage(a.sw, a.sh, warp_pos<FAM>(c, qx, qy)), 255) ? 1 : 0;
+    else {
+      // remap(255-mask, LINEAR, CONSTANT 0) >= 255 over the tile + 2 px halo;
+      // positions outside the output count as 255 (erode border value)
+      for( int q = threadIdx.x; q < VW * VH; q += 256 ) {
+        const int qx = tx0 - 2 + q % VW, qy = ty0 - 2 + q / VW;
+        uint8_t v = 1;
+        if( qx >= 0 && qx < a.dw && qy >= 0 && qy < a.dh ) {
+          v = mask_ok(coverage(a.sw, a.sh, warp_pos<FAM>(c, qx, qy)), 255) ? 1 : 0;
+        }
+        s_v[q] = v;
       }
-      s_v[q] = v;
-    }
-    __syncthreads();
-    for( int q = threadIdx.x; q < SA_TX * VH; q += 256 ) {
-      const int xx = q % SA_TX, yy = q / SA_TX;
-      const uint8_t * p = s_v + yy * VW + xx;
-      s_h[yy * SA_TX + xx] = p[0] & p[1] & p[2] & p[3] & p[4];
-    }
-    __syncthreads();
-    if( x < a.dw ) {
+      __syncthreads();
+      for( int q = threadIdx.x; q < SA_TX * VH; q += 256 ) {
+        const int xx = q % SA_TX, yy = q / SA_TX;
+        const uint8_t * p = s_v + yy * VW + xx;
+        s_h[yy * SA_TX + xx] = p[0] & p[1] & p[2] & p[3] & p[4];
+      }
+      __syncthreads();
+      if( x < a.dw ) {
 #pragma unroll
-      for( int k = 0; k < PPT; ++k ) {
-        const int ly = ly0 + 4 * k, y = ty0 + ly;
-        if( y >= a.dh ) continue;
-        const uint8_t * p = s_h + ly * SA_TX + lx;
-        if( p[0] & p[SA_TX] & p[2 * SA_TX] & p[3 * SA_TX] & p[4 * SA_TX] ) {
-          const spos s = warp_pos<FAM>(c, x, y);
-          // the >= 255 test admits footprints with < 0.2 % of the weight outside the
-          // frame: those taps take the image border mode (base_remap's cv::remap)
-          const float v00 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
-          const float v01 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
-          const float v10 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
-          const float v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
-          const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-          const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
-          const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
-          kahan_add(S[k], cS[k], wp * val);
-          kahan_add(Wt[k], cW[k], wp);
+        for( int k = 0; k < PPT; ++k ) {
+          const int ly = ly0 + 4 * k, y = ty0 + ly;
+          if( y >= a.dh ) continue;
+          const uint8_t * p = s_h + ly * SA_TX + lx;
+          if( p[0] & p[SA_TX] & p[2 * SA_TX] & p[3 * SA_TX] & p[4 * SA_TX] ) {
+            const spos s = warp_pos<FAM>(c, x, y);
+            // the >= 255 test admits footprints with < 0.2 % of the weight outside the
+            // frame: those taps take the image border mode (base_remap's cv::remap)
+            const float v00 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
+            const float v01 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
+            const float v10 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
+            const float v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
+            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+            const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
+            const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
+            pS[k] = fmaf(wp, val, pS[k]);
+            pW[k] += wp;
+          }
         }
       }
+      __syncthreads();
     }
-    __syncthreads();
+    if( ++since == SA_FLUSH ) {
+#pragma unroll
+      for( int k = 0; k < PPT; ++k ) {
+        kahan_add(S[k], cS[k], pS[k]);
+        kahan_add(Wt[k], cW[k], pW[k]);
+        pS[k] = pW[k] = 0.f;
+      }
+      since = 0;
+    }
   }
   if( x < a.dw ) {
 #pragma unroll
     for( int k = 0; k < PPT; ++k ) {
       const int y = ty0 + ly0 + 4 * k;
       if( y >= a.dh ) continue;
+      kahan_add(S[k], cS[k], pS[k]);
+      kahan_add(Wt[k], cW[k], pW[k]);
       const size_t i = (size_t) y * a.dw + x;
       float gS = a.acc[i], gcS = a.acc[a.plane + i], gW = a.acc[2 * a.plane + i], gcW = a.acc[3 * a.plane + i];
       kahan_add(gS, gcS, S[k]);
