@@ -437,7 +437,7 @@ __device__ __forceinline__ void column_project(const float * P, float x, float *
  * level (warp-uniform corner test) the taps are gathered without the
  * coverage / mask / border logic. */
 template<int METHOD, int FAM, int JK, int M>
-__global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
+__global__ void __launch_bounds__(256, 5) k_pass_pointwise(PassArgs a)
 {
   constexpr int NS = M + 2;
   constexpr int NP = column_sums<JK, M>::N;
@@ -494,19 +494,27 @@ __global__ void __launch_bounds__(256) k_pass_pointwise(PassArgs a)
           rect_interior<FAM>(c, xs0, yc, xs1, yc1, a.w, a.h);
       if( x >= a.w ) continue;
       if( interior ) {
+        // every tap is inside the level: no clamps, 32-bit offsets, the pixel
+        // count known in advance, the row coordinate carried in FP32
+        const int y0r = yc + (threadIdx.x >> 7);
+        if( y0r <= yc1 ) cnt += (float) ((yc1 - y0r) / 2 + 1);
+        const int xI = x + (int) c[12], yI = (int) c[13];
+        const float fx = (float) x;
+        const float4 * tgp = a.refTG + (size_t) y0r * a.w + x;
+        float fy = (float) y0r;
 #pragma unroll 4
-        for( int y = yc + (threadIdx.x >> 7); y <= yc1; y += 2 ) {
-          const spos s = warp_pos<FAM>(c, x, y);
-          const size_t i = (size_t) y * a.w + x;
-          const float * r0 = img + (size_t) s.y0 * a.w + s.x0;
+        for( int y = y0r; y <= yc1; y += 2, fy += 2.f, tgp += 2 * a.w ) {
+          float dx, dy;
+          warp_disp<FAM>(c, fx, fy, dx, dy);
+          const float flx = floorf(dx), fly = floorf(dy);
+          const float ax = dx - flx, ay = dy - fly;
+          const float * r0 = img + ((y + yI + (int) fly) * a.w + xI + (int) flx);
           const float v00 = __ldg(r0), v01 = __ldg(r0 + 1), v10 = __ldg(r0 + a.w), v11 = __ldg(r0 + a.w + 1);
-          const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-          const float4 tg = __ldg(a.refTG + i);
-          const float r = fmaf(s.fy, t1 - t0, t0) - tg.x;
-          const float fy = (float) y;
+          const float t0 = fmaf(ax, v01 - v00, v00), t1 = fmaf(ax, v11 - v10, v10);
+          const float4 tg = __ldg(tgp);
+          const float r = fmaf(ay, t1 - t0, t0) - tg.x;
           const float u = tg.y * r, w = tg.z * r;
           rr = fmaf(r, r, rr);
-          cnt += 1.f;
           P[0] += u, P[1] += w;
           if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
           if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
