@@ -167,6 +167,7 @@ struct sst_ecch {
   DevBuf out_params, out_status, out_iters, out_eps, out_rho, out_weight, weff, coeffs;
   DevBuf res_params, res_status, res_rho, res_weight;   // whole-sequence results of sst_stack_frames
   DevBuf binned;                     // 2x2-binned luminance of a chunk of raw Bayer frames
+  DevBuf err;                        // device flag: a bounded wait for a staged tile gave up
   size_t part_stride = 0;
   int steps_cap = 0;
   int lap_t = 0;
@@ -183,7 +184,7 @@ struct sst_ecch {
     graphs.clear();
     DevBuf * bufs[] = { &ref, &grad, &refTG, &mask, &mask_e, &refsrc, &jc_id, &hpart, &gk_in, &gk_ref, &stage[0], &stage[1],
         &pyr, &fs, &part, &cnt, &lists, &counts, &lap, &init, &out_params, &out_status, &out_iters, &out_eps,
-        &out_rho, &out_weight, &weff, &coeffs, &res_params, &res_status, &res_rho, &res_weight, &binned };
+        &out_rho, &out_weight, &weff, &coeffs, &res_params, &res_status, &res_rho, &res_weight, &binned, &err };
     for( DevBuf * b : bufs ) b->release();
     for( auto & kv : H ) kv.second.release();
     if( ev_user ) cudaEventDestroy(ev_user);
@@ -470,7 +471,8 @@ static int ensure_capacity(sst_ecch * h, int n, int method, int num_passes, cons
   const int steps = 1 + num_passes * h->L * (h->o.max_iterations + 2);
   const int lap_level = h->L > 1 ? 1 : 0;
   const int lt = lap_tiles(h->lw[lap_level], h->lh[lap_level]);
-  const bool grow = n > h->cap || pstride > h->part_stride || steps > h->steps_cap || lt != h->lap_t;
+  const bool grow = n > h->cap || pstride > h->part_stride || steps > h->steps_cap || lt != h->lap_t ||
+      (size_t) std::max(n, h->cap) * h->pyr_px * sizeof(float) > h->pyr.n;   // a larger reference needs larger pyramids
   if( !grow ) return SST_OK;
   h->drop_graphs();
   const int cap = std::max(n, h->cap);
@@ -494,8 +496,24 @@ static int ensure_capacity(sst_ecch * h, int n, int method, int num_passes, cons
   SST_CK(h->out_weight.ensure((size_t) cap * sizeof(float)));
   SST_CK(h->weff.ensure((size_t) cap * sizeof(float)));
   SST_CK(h->coeffs.ensure((size_t) cap * SST_NCOEF * sizeof(float)));
+  if( !h->err.p ) {
+    SST_CK(h->err.ensure(sizeof(int)));
+    SST_CK(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->st));
+  }
   h->cap = cap;
   return SST_OK;
+}
+
+/* reports (and clears) a staged-tile wait that gave up during the last work */
+static int check_wait_flag(sst_ecch * h)
+{
+  if( !h->err.p ) return SST_OK;
+  int e = 0;
+  SST_CK(cudaMemcpyAsync(&e, h->err.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  SST_CK(cudaStreamSynchronize(h->st));
+  if( !e ) return SST_OK;
+  SST_CK(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->st));
+  return set_error(SST_ERR_TIMEOUT, "a bounded wait for a staged tile copy gave up; results are invalid");
 }
 
 /* The Gauss-Newton schedule of one batch: pass begin, per level a level
@@ -573,12 +591,17 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
       a.step = h->o.update_step_scale;
       a.max_it = max_it;
       a.scale_next = l > 0 ? (double) h->lw[l - 1] / (double) h->lw[l] : 0.0;
+      a.err = h->err.as<int>();
+      // IC / IC-LM: the level of every frame slot as a TMA tensor (footprints staged in shared memory)
+      CUtensorMap map;
+      const bool staged = (method == M_IC || method == M_ICLM) &&
+          encode_pass_level(h->pyr.as<float>() + h->loff[l], h->lw[l], h->lh[l], h->pyr_px, h->cap, &map);
       for( int it = 0; it <= max_it; ++it ) {
         a.list_in = lists + (size_t) (step + it) * h->cap;
         a.count_in = counts + step + it;
         a.list_out = lists + (size_t) (step + it + 1) * h->cap;
         a.count_out = counts + step + it + 1;
-        SST_CK_LAUNCH(launch_pass(method, a, -1, st));
+        SST_CK_LAUNCH(launch_pass(method, a, -1, st, staged ? &map : nullptr));
         SST_CK_LAUNCH(launch_solve(method, a, solve_grid, st));
         k += 2;
         if( host_driven ) {
@@ -816,7 +839,10 @@ static int align_common(sst_ecch * h, const void * frames, int depth, int n, int
     SST_TRY(copy_out(weight_out ? weight_out + f0 : nullptr, h->out_weight.p, (size_t) nc * sizeof(float), on_device, st));
     if( plain || !on_device ) SST_CK(cudaStreamSynchronize(st));
   }
-  if( !on_device ) SST_CK(cudaStreamSynchronize(st));
+  if( !on_device ) {
+    SST_CK(cudaStreamSynchronize(st));
+    SST_TRY(check_wait_flag(h));
+  }
   SST_TRY(release_to_user(h, stream));
   return SST_OK;
 }
@@ -1169,6 +1195,7 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
   SST_CK(cudaMemcpyAsync(stv.data(), h->res_status.p, (size_t) n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   SST_CK(cudaStreamSynchronize(st));
   for( int f = 0; f < n; ++f ) acc->frames += stv[f] == SST_FRAME_OK ? 1 : 0;
+  SST_TRY(check_wait_flag(h));
   SST_TRY(release_to_user(h, stream));
   return SST_OK;
 }
@@ -1281,6 +1308,7 @@ extern "C" int sst_stack_bayer_frames(sst_ecch * h, sst_weighted_average * const
   int added = 0;
   for( int f = 0; f < n; ++f ) added += stv[f] == SST_FRAME_OK ? 1 : 0;
   for( int k = 0; k < 4; ++k ) acc[k]->frames += added;
+  SST_TRY(check_wait_flag(h));
   SST_TRY(release_to_user(h, stream));
   return SST_OK;
 }

@@ -24,6 +24,7 @@
  */
 #include "sst_engine.cuh"
 #include "sst_kernels.cuh"
+#include "sst_tma.cuh"
 #include <float.h>
 
 namespace sst {
@@ -562,6 +563,211 @@ __global__ void __launch_bounds__(256, 5) k_pass_pointwise(PassArgs a)
   }
 }
 
+/* ------------------------------------------- TMA-staged pointwise pass */
+
+/* source footprint box of one 128 x 32 tile (floats): x origin a multiple of 4 */
+constexpr int PB_W = 144, PB_H = 40;
+
+struct ItemPlan {
+  int f, t;         // frame and tile of the item
+  int use;          // 1: every tap inside the level and inside the staged box
+  int bx0, by0;     // box origin in the level
+};
+
+/* Plans one work item (warp 0): frame, tile, coefficients (into s_c) and
+ * whether its footprint is staged. */
+template<int METHOD, int FAM>
+__device__ __forceinline__ void plan_item(const PassArgs & a, int item, float * s_c, ItemPlan * plan)
+{
+  const int lane = threadIdx.x & 31;
+  const int fi = item / a.tiles, t = item - fi * a.tiles;
+  const int f = __ldcg(a.list_in + fi);
+  const float * wc = a.fs[f].wc;
+  float c[16];
+#pragma unroll
+  for( int i = 0; i < 16; ++i ) c[i] = __ldcg(wc + i);
+  if( lane < 16 ) s_c[lane] = __ldcg(wc + lane);
+  const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
+  const int tx1 = min(tx0 + PW_TX, a.w) - 1, ty1 = min(ty0 + PW_TY, a.h) - 1;
+  int bx0, by0, bx1, by1;
+  bool use = rect_footprint<FAM>(c, tx0, ty0, tx1, ty1, a.w, a.h, bx0, by0, bx1, by1);
+  use = use && (METHOD == M_IC || !a.refM);
+  if( use ) {
+    bx0 = bx0 >= 0 ? bx0 & ~3 : -((-bx0 + 3) & ~3);
+    use = bx1 < bx0 + PB_W && by1 < by0 + PB_H;
+  }
+  if( lane == 0 ) {
+    plan->f = f, plan->t = t;
+    plan->use = use ? 1 : 0;
+    plan->bx0 = bx0, plan->by0 = by0;
+  }
+}
+
+/* The IC / IC-LM pass with each item's source footprint staged in shared
+ * memory by one TMA copy, double-buffered across the CTA's consecutive items:
+ * the gathers become shared-memory loads with no address arithmetic in
+ * 64 bits, and the next item's copy is in flight while this one computes.
+ * Items whose taps leave the level or the box take the global path. */
+template<int METHOD, int FAM, int JK, int M>
+__global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const __grid_constant__ CUtensorMap tmap)
+{
+  constexpr int NS = M + 2;
+  constexpr int NP = column_sums<JK, M>::N;
+  __shared__ __align__(128) float s_box[2][PB_H * PB_W];
+  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ float s_red[8 * NS];
+  __shared__ double s_tile[NS];
+  __shared__ float s_c[3][16];
+  __shared__ ItemPlan s_plan[3];
+
+  const int count = __ldcg(a.count_in);
+  const int nitems = count * a.tiles;
+  if( (int) blockIdx.x >= nitems ) return;          // uniform over the CTA
+  if( threadIdx.x == 0 ) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if( threadIdx.x < 32 ) plan_item<METHOD, FAM>(a, blockIdx.x, s_c[0], &s_plan[0]);
+  __syncthreads();
+  if( threadIdx.x == 0 && s_plan[0].use ) {
+    mbar_expect_tx(&s_bar[0], PB_W * PB_H * sizeof(float));
+    tma_load_3d(s_box[0], &tmap, s_plan[0].bx0, s_plan[0].by0, s_plan[0].f, &s_bar[0]);
+  }
+  uint32_t phases = 0u;
+  bool timed_out = false;
+  int slot = 0, b = 0;
+  for( int item = blockIdx.x; item < nitems; item += gridDim.x, b ^= 1 ) {
+    const int nitem = item + gridDim.x;
+    const int nslot = slot == 2 ? 0 : slot + 1;
+    if( threadIdx.x < 32 && nitem < nitems ) plan_item<METHOD, FAM>(a, nitem, s_c[nslot], &s_plan[nslot]);
+    __syncthreads();
+    if( threadIdx.x == 0 && nitem < nitems && s_plan[nslot].use ) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&s_bar[b ^ 1], PB_W * PB_H * sizeof(float));
+      tma_load_3d(s_box[b ^ 1], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, s_plan[nslot].f, &s_bar[b ^ 1]);
+    }
+    const ItemPlan pl = s_plan[slot];
+    float c[16];
+#pragma unroll
+    for( int i = 0; i < 16; ++i ) c[i] = s_c[slot][i];
+    slot = nslot;
+    const int f = pl.f, t = pl.t;
+    const float * img = a.pyr + (size_t) f * a.pyr_stride + a.lvl_off;
+    const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
+    const int x = tx0 + (threadIdx.x & (PW_TX - 1));
+    const int yend = min(ty0 + PW_TY, a.h);
+    float P[NP], rr = 0.f, cnt = 0.f;
+#pragma unroll
+    for( int k = 0; k < NP; ++k ) P[k] = 0.f;
+    if( pl.use ) {
+      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true;
+      phases ^= 1u << b;
+      if( x < a.w ) {
+        const float * box = s_box[b];
+        const int y0r = ty0 + (threadIdx.x >> 7);
+        if( y0r < yend ) cnt = (float) ((yend - 1 - y0r) / 2 + 1);
+        const int xI = x + (int) c[12] - pl.bx0, yI = (int) c[13] - pl.by0;
+        const float fx = (float) x;
+        const float4 * tgp = a.refTG + (size_t) y0r * a.w + x;
+        float fy = (float) y0r;
+#pragma unroll 4
+        for( int y = y0r; y < yend; y += 2, fy += 2.f, tgp += 2 * a.w ) {
+          float dx, dy;
+          warp_disp<FAM>(c, fx, fy, dx, dy);
+          const float flx = floorf(dx), fly = floorf(dy);
+          const float ax = dx - flx, ay = dy - fly;
+          // inside the box by construction (footprint test); the clamp only guards the array
+          const int o = min(max((y + yI + (int) fly) * PB_W + xI + (int) flx, 0), PB_W * PB_H - PB_W - 2);
+          const float v00 = box[o], v01 = box[o + 1], v10 = box[o + PB_W], v11 = box[o + PB_W + 1];
+          const float t0 = fmaf(ax, v01 - v00, v00), t1 = fmaf(ax, v11 - v10, v10);
+          const float4 tg = __ldg(tgp);
+          const float r = fmaf(ay, t1 - t0, t0) - tg.x;
+          const float u = tg.y * r, w = tg.z * r;
+          rr = fmaf(r, r, rr);
+          P[0] += u, P[1] += w;
+          if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
+          if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
+          if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fy * fy, w, P[4 < NP ? 4 : 0]);
+        }
+      }
+    }
+    else {
+      const int xs0 = tx0 + (threadIdx.x & (PW_TX - 1) & ~31);
+      const int xs1 = min(xs0 + 31, a.w - 1);
+      for( int yc = ty0; yc < yend; yc += 16 ) {
+        const int yc1 = min(yc + 15, yend - 1);
+        const bool interior = (METHOD == M_IC || !a.refM) && xs0 < a.w &&
+            rect_interior<FAM>(c, xs0, yc, xs1, yc1, a.w, a.h);
+        if( x >= a.w ) continue;
+        if( interior ) {
+          const int y0r = yc + (threadIdx.x >> 7);
+          if( y0r <= yc1 ) cnt += (float) ((yc1 - y0r) / 2 + 1);
+          const int xI = x + (int) c[12], yI = (int) c[13];
+          const float fx = (float) x;
+          const float4 * tgp = a.refTG + (size_t) y0r * a.w + x;
+          float fy = (float) y0r;
+#pragma unroll 4
+          for( int y = y0r; y <= yc1; y += 2, fy += 2.f, tgp += 2 * a.w ) {
+            float dx, dy;
+            warp_disp<FAM>(c, fx, fy, dx, dy);
+            const float flx = floorf(dx), fly = floorf(dy);
+            const float ax = dx - flx, ay = dy - fly;
+            const float * r0 = img + ((y + yI + (int) fly) * a.w + xI + (int) flx);
+            const float v00 = __ldg(r0), v01 = __ldg(r0 + 1), v10 = __ldg(r0 + a.w), v11 = __ldg(r0 + a.w + 1);
+            const float t0 = fmaf(ax, v01 - v00, v00), t1 = fmaf(ax, v11 - v10, v10);
+            const float4 tg = __ldg(tgp);
+            const float r = fmaf(ay, t1 - t0, t0) - tg.x;
+            const float u = tg.y * r, w = tg.z * r;
+            rr = fmaf(r, r, rr);
+            P[0] += u, P[1] += w;
+            if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
+            if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
+            if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fy * fy, w, P[4 < NP ? 4 : 0]);
+          }
+        }
+        else {
+#pragma unroll 2
+          for( int y = yc + (threadIdx.x >> 7); y <= yc1; y += 2 ) {
+            const spos s = warp_pos<FAM>(c, x, y);
+            const size_t i = (size_t) y * a.w + x;
+            bool ok;
+            if( METHOD == M_IC ) {
+              ok = mask_ok(coverage(a.w, a.h, s), 250);
+            }
+            else {
+              int rx, ry;
+              warp_nearest<FAM>(c, x, y, rx, ry);
+              ok = rx >= 0 && rx < a.w && ry >= 0 && ry < a.h;
+              if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
+            }
+            const float v = sample_replicate(img, a.w, a.h, s);
+            const float4 tg = __ldg(a.refTG + i);
+            const float r = ok ? v - tg.x : 0.f;
+            const float fy = (float) y;
+            const float u = tg.y * r, w = tg.z * r;
+            rr = fmaf(r, r, rr);
+            cnt += ok ? 1.f : 0.f;
+            P[0] += u, P[1] += w;
+            if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
+            if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
+            if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fy * fy, w, P[4 < NP ? 4 : 0]);
+          }
+        }
+      }
+    }
+    float acc[NS];
+#pragma unroll
+    for( int k = 0; k < NS; ++k ) acc[k] = 0.f;
+    if( x < a.w ) column_project<JK, M>(P, (float) x, acc);
+    acc[M] = rr;
+    acc[M + 1] = cnt;
+    block_reduce_d<NS>(acc, s_red, s_tile);
+    write_tile<NS>(a, f, t, s_tile);
+  }
+  if( timed_out && a.err ) atomicExch(a.err, 1);
+}
+
 /* -------------------------------------------------------- stencil passes */
 
 /* Gram-matrix entry (i, j) that holds pass sum k. FA: V = [J (M), g - s, f - s, 1],
@@ -835,9 +1041,15 @@ static int persistent_grid(K kernel)
 }
 
 template<int METHOD, int FAM, int JK, int M>
-static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st)
+static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st, const CUtensorMap * map)
 {
   if constexpr( METHOD == M_IC || METHOD == M_ICLM ) {
+    if( map && FAM != FAM_QUAD ) {
+      static int g = 0;
+      if( !g ) g = persistent_grid(k_pass_pointwise_tma<METHOD, FAM, JK, M>);
+      k_pass_pointwise_tma<METHOD, FAM, JK, M><<<grid > 0 ? grid : g, 256, 0, st>>>(a, *map);
+      return cudaGetLastError();
+    }
     static int g = 0;
     if( !g ) {
       g = persistent_grid(k_pass_pointwise<METHOD, FAM, JK, M>);
@@ -858,37 +1070,48 @@ static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st)
 }
 
 template<int METHOD>
-static cudaError_t launch_m(const PassArgs & a, int grid, cudaStream_t st)
+static cudaError_t launch_m(const PassArgs & a, int grid, cudaStream_t st, const CUtensorMap * map)
 {
   switch ( a.model.type ) {
-  case SST_MOTION_TRANSLATION: return launch_t<METHOD, FAM_AFFINE, J_TRANS, 2>(a, grid, st);
+  case SST_MOTION_TRANSLATION: return launch_t<METHOD, FAM_AFFINE, J_TRANS, 2>(a, grid, st, map);
   case SST_MOTION_EUCLIDEAN:
   case SST_MOTION_SCALED_EUCLIDEAN:
-    if( a.M == 3 ) return launch_t<METHOD, FAM_AFFINE, J_EUCL, 3>(a, grid, st);
-    return launch_t<METHOD, FAM_AFFINE, J_EUCL, 4>(a, grid, st);
-  case SST_MOTION_AFFINE: return launch_t<METHOD, FAM_AFFINE, J_AFFINE, 6>(a, grid, st);
+    if( a.M == 3 ) return launch_t<METHOD, FAM_AFFINE, J_EUCL, 3>(a, grid, st, map);
+    return launch_t<METHOD, FAM_AFFINE, J_EUCL, 4>(a, grid, st, map);
+  case SST_MOTION_AFFINE: return launch_t<METHOD, FAM_AFFINE, J_AFFINE, 6>(a, grid, st, map);
   case SST_MOTION_HOMOGRAPHY:
-  case SST_MOTION_EPIPOLAR_DEROTATION: return launch_t<METHOD, FAM_HOMOG, J_HOMOG, 8>(a, grid, st);
+  case SST_MOTION_EPIPOLAR_DEROTATION: return launch_t<METHOD, FAM_HOMOG, J_HOMOG, 8>(a, grid, st, map);
   case SST_MOTION_SEMI_QUADRATIC:
-    if( METHOD == M_FA || METHOD == M_LM ) return launch_t<(METHOD == M_FA ? M_FA : M_LM), FAM_QUAD, J_SEMIQ, 8>(a, grid, st);
+    if( METHOD == M_FA || METHOD == M_LM ) return launch_t<(METHOD == M_FA ? M_FA : M_LM), FAM_QUAD, J_SEMIQ, 8>(a, grid, st, map);
     return cudaErrorInvalidValue;
   case SST_MOTION_QUADRATIC:
-    if( METHOD == M_FA || METHOD == M_LM ) return launch_t<(METHOD == M_FA ? M_FA : M_LM), FAM_QUAD, J_QUAD, 12>(a, grid, st);
+    if( METHOD == M_FA || METHOD == M_LM ) return launch_t<(METHOD == M_FA ? M_FA : M_LM), FAM_QUAD, J_QUAD, 12>(a, grid, st, map);
     return cudaErrorInvalidValue;
   }
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_pass(int method, const PassArgs & a, int grid, cudaStream_t st)
+cudaError_t launch_pass(int method, const PassArgs & a, int grid, cudaStream_t st, const CUtensorMap * map)
 {
   if( a.roi && method != M_FA && method != M_LM ) return cudaErrorInvalidValue;
   switch ( method ) {
-  case M_IC: return launch_m<M_IC>(a, grid, st);
-  case M_ICLM: return launch_m<M_ICLM>(a, grid, st);
-  case M_FA: return launch_m<M_FA>(a, grid, st);
-  case M_LM: return launch_m<M_LM>(a, grid, st);
+  case M_IC: return launch_m<M_IC>(a, grid, st, map);
+  case M_ICLM: return launch_m<M_ICLM>(a, grid, st, map);
+  case M_FA: return launch_m<M_FA>(a, grid, st, nullptr);
+  case M_LM: return launch_m<M_LM>(a, grid, st, nullptr);
   }
   return cudaErrorInvalidValue;
+}
+
+/* the pyramid level of every frame slot as a 3-D tensor (x, y, frame) with
+ * the pointwise footprint box; false when the level's layout breaks the TMA
+ * rules (row and frame strides multiples of 16 bytes, aligned base) */
+bool encode_pass_level(const float * level0_of_slot0, int w, int h, size_t pyr_stride, int frames, CUtensorMap * map)
+{
+  const uint64_t dims[3] = { (uint64_t) w, (uint64_t) h, (uint64_t) frames };
+  const uint64_t strides[2] = { (uint64_t) w * sizeof(float), (uint64_t) pyr_stride * sizeof(float) };
+  const uint32_t box[3] = { (uint32_t) PB_W, (uint32_t) PB_H, 1 };
+  return encode_tensor_3d(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, level0_of_slot0, dims, strides, box);
 }
 
 /* ------------------------------------------------------ level / pass glue */

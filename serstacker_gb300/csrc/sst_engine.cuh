@@ -19,6 +19,7 @@
  * active frames' tile counts, rebuilt for every step by k_roi_scan.
  */
 #pragma once
+#include <cuda.h>            // CUtensorMap
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "sst_internal.cuh"
@@ -120,10 +121,11 @@ struct PassArgs {
   int lmax, level;
   const int * tile_prefix;  // per entry of list_in: tiles of the entries before it (k_roi_scan)
   const int * tile_total;   // tiles of the whole list
+  int * err;                // set to 1 when a bounded wait for a staged tile gave up
 };
 
-/* pointwise passes (IC, IC-LM, correlation): 128 x 64 pixel tiles, 256 threads */
-constexpr int PW_TX = 128, PW_TY = 64;
+/* pointwise passes (IC, IC-LM, correlation): 128 x 32 pixel tiles, 256 threads */
+constexpr int PW_TX = 128, PW_TY = 32;
 /* stencil passes (FA, LM): 64 x 16 pixel tiles + 2 px halo, 256 threads */
 constexpr int ST_TX = 64, ST_TY = 16;
 
@@ -134,7 +136,8 @@ inline int tiles_of(int w, int h, int tx, int ty, int * tiles_x)
 }
 
 /* kernel launchers (defined in the .cu files) */
-cudaError_t launch_pass(int method, const PassArgs & a, int grid, cudaStream_t st);
+cudaError_t launch_pass(int method, const PassArgs & a, int grid, cudaStream_t st, const CUtensorMap * map = nullptr);
+bool encode_pass_level(const float * level_of_slot0, int w, int h, size_t pyr_stride, int frames, CUtensorMap * map);
 __host__ __device__ int pass_num_sums(int method, int M);
 cudaError_t launch_solve(int method, const PassArgs & a, int grid, cudaStream_t st);
 

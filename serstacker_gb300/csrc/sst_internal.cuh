@@ -53,7 +53,7 @@ __device__ __forceinline__ void warp_disp(const float * __restrict__ c, float x,
   }
   else if( FAM == FAM_HOMOG ) {
     const float q = fmaf(c[6], x, c[7] * y);       // a20 x + a21 y
-    const float iw = __frcp_rn(1.0f + q);
+    const float iw = __fdividef(1.0f, 1.0f + q);   // approximate reciprocal: w is near 1, <= 2 ulp
     const float nx = fmaf(c[0], x, fmaf(c[1], y, c[2])) - q * (x + c[12]);
     const float ny = fmaf(c[3], x, fmaf(c[4], y, c[5])) - q * (y + c[13]);
     dx = nx * iw;

@@ -32,7 +32,7 @@ __device__ __forceinline__ void sd_pixel(const float * jc, float x, float y, flo
     J[3] = gy * x, J[4] = gy * y, J[5] = gy;
   }
   else if( JK == J_HOMOG ) {
-    const float den = __frcp_rn(fmaf(x, jc[6], fmaf(y, jc[7], 1.0f)));
+    const float den = __fdividef(1.0f, fmaf(x, jc[6], fmaf(y, jc[7], 1.0f)));
     const float hatX = -fmaf(x, jc[0], fmaf(y, jc[1], jc[2])) * den;
     const float hatY = -fmaf(x, jc[3], fmaf(y, jc[4], jc[5])) * den;
     const float ggx = gx * den, ggy = gy * den;

@@ -16,8 +16,10 @@
  * and accumulates every frame of the batch in registers (compensated) and
  * touches the accumulator planes once per batch: no atomics, deterministic.
  */
+#include <mutex>
 #include "sst_engine.cuh"
 #include "sst_stack.cuh"
+#include "sst_tma.cuh"
 
 namespace sst {
 
@@ -125,19 +127,26 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
     for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + i);
     const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
     if( rect_interior<FAM>(c, wx0, wy0, wx1, wy1, a.sw, a.sh) ) {
-      // every pixel of the window is valid and every tap is inside the frame
+      // every pixel of the window is valid and every tap is inside the frame:
+      // issue the taps of all PPT pixels before using any (one memory round trip)
       if( x < a.dw ) {
+        float v[PPT][4], fx[PPT], fy[PPT];
+#pragma unroll
+        for( int k = 0; k < PPT; ++k ) {
+          const int y = min(ty0 + ly0 + 4 * k, a.dh - 1);
+          const spos s = warp_pos<FAM>(c, x, y);
+          const T * r0 = (const T *) (fb + (size_t) s.y0 * a.row_stride) + s.x0;
+          const T * r1 = (const T *) ((const uint8_t *) r0 + a.row_stride);
+          v[k][0] = (float) __ldg(r0), v[k][1] = (float) __ldg(r0 + 1);
+          v[k][2] = (float) __ldg(r1), v[k][3] = (float) __ldg(r1 + 1);
+          fx[k] = s.fx, fy[k] = s.fy;
+        }
 #pragma unroll
         for( int k = 0; k < PPT; ++k ) {
           const int y = ty0 + ly0 + 4 * k;
           if( y < a.dh ) {
-            const spos s = warp_pos<FAM>(c, x, y);
-            const T * r0 = (const T *) (fb + (size_t) s.y0 * a.row_stride) + s.x0;
-            const T * r1 = (const T *) ((const uint8_t *) r0 + a.row_stride);
-            const float v00 = (float) __ldg(r0), v01 = (float) __ldg(r0 + 1);
-            const float v10 = (float) __ldg(r1), v11 = (float) __ldg(r1 + 1);
-            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-            const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
+            const float t0 = fmaf(fx[k], v[k][1] - v[k][0], v[k][0]), t1 = fmaf(fx[k], v[k][3] - v[k][2], v[k][2]);
+            const float val = fmaf(fy[k], t1 - t0, t0) * a.scale;
             const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
             pS[k] = fmaf(wp, val, pS[k]);
             pW[k] += wp;
@@ -215,10 +224,287 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
   }
 }
 
+/* ------------------------------------------- TMA-staged batched stack */
+
+/* source footprint box of one 64 x 16 output tile: TB_W x TB_H elements; its
+ * x origin is a multiple of 16 bytes (the TMA rule for the innermost coordinate) */
+constexpr int TB_W = 80, TB_H = 24;
+
+struct TilePlan {
+  int use;          // 1: the frame's tile is staged by TMA (window interior, footprint fits the box)
+  int bx0, by0;     // box origin in the frame
+  float w;          // frame weight
+};
+
+/* Plans frame f for this CTA's tile (warp 0): its weight, coefficients
+ * (into s_c), and whether its footprint is staged. */
+template<int FAM, typename T>
+__device__ __forceinline__ void plan_frame(const StackArgs & a, int f, int tx0, int ty0, int wx0, int wy0, int wx1,
+    int wy1, float * s_c, TilePlan * plan)
+{
+  constexpr int XA = 16 / (int) sizeof(T);
+  const int lane = threadIdx.x & 31;
+  float c[SST_NCOEF];
+#pragma unroll
+  for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + i);
+  if( lane < SST_NCOEF ) s_c[lane] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + lane);
+  const float wf = __ldg(a.weights + f);
+  bool use = wf > 0.f && rect_interior<FAM>(c, wx0, wy0, wx1, wy1, a.sw, a.sh);
+  int bx0, by0, bx1, by1;
+  const int tx1 = min(tx0 + SA_TX, a.dw) - 1, ty1 = min(ty0 + SA_TY, a.dh) - 1;
+  const bool in_tile = rect_footprint<FAM>(c, tx0, ty0, tx1, ty1, a.sw, a.sh, bx0, by0, bx1, by1);
+  if( use && in_tile ) {
+    bx0 = bx0 >= 0 ? bx0 - bx0 % XA : -((-bx0 + XA - 1) / XA) * XA;   // round down to the alignment
+    use = bx1 < bx0 + TB_W && by1 < by0 + TB_H;
+  }
+  else use = false;
+  if( lane == 0 ) {
+    plan->use = use ? 1 : 0;
+    plan->bx0 = bx0, plan->by0 = by0;
+    plan->w = wf;
+  }
+}
+
+/* The batched stack with the source footprint of each (frame, tile) staged
+ * in shared memory by one TMA copy, double-buffered: while the CTA warps and
+ * accumulates frame f from shared memory, the copy of frame f + 1 is in
+ * flight. Frames whose tile needs the validity / border logic, or whose
+ * footprint does not fit the box, take the global-memory paths. */
+template<int FAM, typename T>
+__global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, const __grid_constant__ CUtensorMap tmap)
+{
+  constexpr int VW = SA_TX + 4, VH = SA_TY + 4;
+  constexpr int PPT = SA_TX * SA_TY / 256;
+  __shared__ __align__(128) T s_box[2][TB_H * TB_W];
+  __shared__ __align__(8) uint64_t s_bar[2];
+  // plans and coefficients rotate over three slots: frame f + 1 is planned
+  // while slower warps may still read frame f's slot
+  __shared__ float s_c[3][SST_NCOEF];
+  __shared__ TilePlan s_plan[3];
+  __shared__ uint8_t s_v[VH * VW];
+  __shared__ uint8_t s_h[VH * SA_TX];
+  const int tx0 = blockIdx.x * SA_TX, ty0 = blockIdx.y * SA_TY;
+  const int lx = threadIdx.x % SA_TX, ly0 = threadIdx.x / SA_TX;
+  const int x = tx0 + lx;
+  const int wx0 = max(tx0 - 2, 0), wy0 = max(ty0 - 2, 0);
+  const int wx1 = min(tx0 + SA_TX + 1, a.dw - 1), wy1 = min(ty0 + SA_TY + 1, a.dh - 1);
+  float S[PPT], cS[PPT], Wt[PPT], cW[PPT], pS[PPT], pW[PPT];
+#pragma unroll
+  for( int k = 0; k < PPT; ++k ) S[k] = cS[k] = Wt[k] = cW[k] = pS[k] = pW[k] = 0.f;
+  uint32_t phases = 0u;                          // bit b: parity of the next completion of s_bar[b]
+  bool timed_out = false;
+  if( threadIdx.x == 0 ) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if( threadIdx.x < 32 && a.n > 0 ) plan_frame<FAM, T>(a, 0, tx0, ty0, wx0, wy0, wx1, wy1, s_c[0], &s_plan[0]);
+  __syncthreads();
+  if( threadIdx.x == 0 && a.n > 0 && s_plan[0].use ) {
+    mbar_expect_tx(&s_bar[0], TB_W * TB_H * sizeof(T));
+    tma_load_3d(s_box[0], &tmap, s_plan[0].bx0, s_plan[0].by0, 0, &s_bar[0]);
+  }
+  int since = 0;
+  int slot = 0;                                   // frame f's plan slot (f mod 3)
+  for( int f = 0; f < a.n; ++f ) {
+    const int b = f & 1, nb = b ^ 1;
+    const int nslot = slot == 2 ? 0 : slot + 1;
+    // plan frame f + 1; its box buffer was last read during frame f - 1, which every
+    // thread has finished at the barrier below
+    if( threadIdx.x < 32 && f + 1 < a.n )
+      plan_frame<FAM, T>(a, f + 1, tx0, ty0, wx0, wy0, wx1, wy1, s_c[nslot], &s_plan[nslot]);
+    __syncthreads();
+    if( threadIdx.x == 0 && f + 1 < a.n && s_plan[nslot].use ) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // order the generic reads of frame f - 1 before the copy
+      mbar_expect_tx(&s_bar[nb], TB_W * TB_H * sizeof(T));
+      tma_load_3d(s_box[nb], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, f + 1, &s_bar[nb]);
+    }
+    const TilePlan pl = s_plan[slot];
+    float c[SST_NCOEF];
+#pragma unroll
+    for( int i = 0; i < SST_NCOEF; ++i ) c[i] = s_c[slot][i];
+    slot = nslot;
+    const float wf = pl.w;
+    if( !(wf > 0.f) ) continue;                     // uniform over the CTA
+    const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
+    if( pl.use ) {
+      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true;
+      phases ^= 1u << b;
+      if( x < a.dw ) {
+        const T * box = s_box[b];
+#pragma unroll
+        for( int k = 0; k < PPT; ++k ) {
+          const int y = ty0 + ly0 + 4 * k;
+          if( y < a.dh ) {
+            const spos s = warp_pos<FAM>(c, x, y);
+            // inside the box by construction (footprint test); the clamp only guards the array
+            const int o = min(max((s.y0 - pl.by0) * TB_W + (s.x0 - pl.bx0), 0), TB_W * TB_H - TB_W - 2);
+            const float v00 = (float) box[o], v01 = (float) box[o + 1];
+            const float v10 = (float) box[o + TB_W], v11 = (float) box[o + TB_W + 1];
+            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+            const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
+            const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
+            pS[k] = fmaf(wp, val, pS[k]);
+            pW[k] += wp;
+          }
+        }
+      }
+    }
+    else if( rect_interior<FAM>(c, wx0, wy0, wx1, wy1, a.sw, a.sh) ) {
+      if( x < a.dw ) {
+#pragma unroll
+        for( int k = 0; k < PPT; ++k ) {
+          const int y = ty0 + ly0 + 4 * k;
+          if( y < a.dh ) {
+            const spos s = warp_pos<FAM>(c, x, y);
+            const T * r0 = (const T *) (fb + (size_t) s.y0 * a.row_stride) + s.x0;
+            const T * r1 = (const T *) ((const uint8_t *) r0 + a.row_stride);
+            const float v00 = (float) __ldg(r0), v01 = (float) __ldg(r0 + 1);
+            const float v10 = (float) __ldg(r1), v11 = (float) __ldg(r1 + 1);
+            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+            const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
+            const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
+            pS[k] = fmaf(wp, val, pS[k]);
+            pW[k] += wp;
+          }
+        }
+      }
+    }
+    else {
+      for( int q = threadIdx.x; q < VW * VH; q += 256 ) {
+        const int qx = tx0 - 2 + q % VW, qy = ty0 - 2 + q / VW;
+        uint8_t v = 1;
+        if( qx >= 0 && qx < a.dw && qy >= 0 && qy < a.dh ) {
+          v = mask_ok(coverage(a.sw, a.sh, warp_pos<FAM>(c, qx, qy)), 255) ? 1 : 0;
+        }
+        s_v[q] = v;
+      }
+      __syncthreads();
+      for( int q = threadIdx.x; q < SA_TX * VH; q += 256 ) {
+        const int xx = q % SA_TX, yy = q / SA_TX;
+        const uint8_t * p = s_v + yy * VW + xx;
+        s_h[yy * SA_TX + xx] = p[0] & p[1] & p[2] & p[3] & p[4];
+      }
+      __syncthreads();
+      if( x < a.dw ) {
+#pragma unroll
+        for( int k = 0; k < PPT; ++k ) {
+          const int ly = ly0 + 4 * k, y = ty0 + ly;
+          if( y >= a.dh ) continue;
+          const uint8_t * p = s_h + ly * SA_TX + lx;
+          if( p[0] & p[SA_TX] & p[2 * SA_TX] & p[3 * SA_TX] & p[4 * SA_TX] ) {
+            const spos s = warp_pos<FAM>(c, x, y);
+            const float v00 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
+            const float v01 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
+            const float v10 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
+            const float v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
+            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+            const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
+            const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
+            pS[k] = fmaf(wp, val, pS[k]);
+            pW[k] += wp;
+          }
+        }
+      }
+    }
+    if( ++since == SA_FLUSH ) {
+#pragma unroll
+      for( int k = 0; k < PPT; ++k ) {
+        kahan_add(S[k], cS[k], pS[k]);
+        kahan_add(Wt[k], cW[k], pW[k]);
+        pS[k] = pW[k] = 0.f;
+      }
+      since = 0;
+    }
+  }
+  if( timed_out && a.err ) atomicExch(a.err, 1);
+  if( x < a.dw ) {
+#pragma unroll
+    for( int k = 0; k < PPT; ++k ) {
+      const int y = ty0 + ly0 + 4 * k;
+      if( y >= a.dh ) continue;
+      kahan_add(S[k], cS[k], pS[k]);
+      kahan_add(Wt[k], cW[k], pW[k]);
+      const size_t i = (size_t) y * a.dw + x;
+      float gS = a.acc[i], gcS = a.acc[a.plane + i], gW = a.acc[2 * a.plane + i], gcW = a.acc[3 * a.plane + i];
+      kahan_add(gS, gcS, S[k]);
+      gcS += cS[k];
+      kahan_add(gW, gcW, Wt[k]);
+      gcW += cW[k];
+      a.acc[i] = gS, a.acc[a.plane + i] = gcS, a.acc[2 * a.plane + i] = gW, a.acc[3 * a.plane + i] = gcW;
+    }
+  }
+}
+
+/* cuTensorMapEncodeTiled through the runtime's driver entry point (no link to
+ * the driver library); nullptr when unavailable */
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn()
+{
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void * p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if( cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess )
+      fn = (EncodeTiledFn) p;
+    else cudaGetLastError();
+  });
+  return fn;
+}
+
+bool encode_tensor_3d(CUtensorMap * map, CUtensorMapDataType dt, int esz, const void * base, const uint64_t * dims,
+    const uint64_t * strides, const uint32_t * box)
+{
+  EncodeTiledFn fn = encode_fn();
+  if( !fn ) return false;
+  if( ((uintptr_t) base & 15) || (strides[0] & 15) || (strides[1] & 15) || ((size_t) box[0] * esz) % 16 ) return false;
+  const cuuint64_t d[3] = { dims[0], dims[1], dims[2] };
+  const cuuint64_t st[2] = { strides[0], strides[1] };
+  const cuuint32_t bx[3] = { box[0], box[1], box[2] };
+  const cuuint32_t estr[3] = { 1, 1, 1 };
+  return fn(map, dt, 3, (void *) base, d, st, bx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+/* The frames of a batch as a 3-D tensor (x, y, frame) with the footprint box;
+ * false when the layout does not meet the TMA rules (16-byte aligned base and
+ * strides) or the encoder is unavailable */
+static bool encode_frames(const StackArgs & a, int depth, CUtensorMap * map)
+{
+  CUtensorMapDataType dt;
+  int esz;
+  switch ( depth ) {
+  case SST_DEPTH_U8: dt = CU_TENSOR_MAP_DATA_TYPE_UINT8, esz = 1; break;
+  case SST_DEPTH_U16: dt = CU_TENSOR_MAP_DATA_TYPE_UINT16, esz = 2; break;
+  case SST_DEPTH_F32: dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32, esz = 4; break;
+  default: return false;
+  }
+  const uint64_t dims[3] = { (uint64_t) a.sw, (uint64_t) a.sh, (uint64_t) a.n };
+  const uint64_t strides[2] = { (uint64_t) a.row_stride, (uint64_t) a.frame_stride };
+  const uint32_t box[3] = { (uint32_t) TB_W, (uint32_t) TB_H, 1 };
+  return encode_tensor_3d(map, dt, esz, a.frames, dims, strides, box);
+}
+
 cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, cudaStream_t st)
 {
   dim3 grid((a.dw + SA_TX - 1) / SA_TX, (a.dh + SA_TY - 1) / SA_TY);
   const int fam = motion_family(motion);
+  CUtensorMap map;
+  if( fam != FAM_QUAD && a.n > 0 && encode_frames(a, depth, &map) ) {
+#define SST_LAUNCH_TMA(FAMV, TV) k_stack_add_warped_tma<FAMV, TV><<<grid, 256, 0, st>>>(a, map)
+    switch ( depth ) {
+    case SST_DEPTH_U8: if( fam == FAM_AFFINE ) SST_LAUNCH_TMA(FAM_AFFINE, uint8_t); else SST_LAUNCH_TMA(FAM_HOMOG, uint8_t); break;
+    case SST_DEPTH_U16: if( fam == FAM_AFFINE ) SST_LAUNCH_TMA(FAM_AFFINE, uint16_t); else SST_LAUNCH_TMA(FAM_HOMOG, uint16_t); break;
+    default: if( fam == FAM_AFFINE ) SST_LAUNCH_TMA(FAM_AFFINE, float); else SST_LAUNCH_TMA(FAM_HOMOG, float); break;
+    }
+#undef SST_LAUNCH_TMA
+    return cudaGetLastError();
+  }
 #define SST_LAUNCH_STACK(FAMV, TV) k_stack_add_warped<FAMV, TV><<<grid, 256, 0, st>>>(a)
   switch ( depth ) {
   case SST_DEPTH_U8:

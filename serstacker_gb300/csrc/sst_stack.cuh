@@ -21,6 +21,7 @@ struct StackArgs {
   size_t plane;             // floats per plane
   int border;               // image border mode of the remap (SST_BORDER_*)
   const float * wmap = nullptr;   // optional per-pixel weight maps (n x plane, output grid)
+  int * err = nullptr;            // optional: set to 1 when a bounded wait for a tile copy gave up
 };
 
 /* four Bayer planes of raw u16 mosaic frames, stacked into four accumulators */
