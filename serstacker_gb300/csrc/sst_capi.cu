@@ -631,7 +631,9 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
   c.counters = h->cnt.as<unsigned>();
   c.model = passes[num_passes - 1];
   c.min_rho = h->o.min_rho;
-  SST_CK_LAUNCH(launch_correlation(c, grid, st));
+  CUtensorMap cmap;
+  const bool cstaged = encode_pass_level(h->pyr.as<float>(), h->w, h->h, h->pyr_px, h->cap, &cmap);
+  SST_CK_LAUNCH(launch_correlation(c, grid, st, cstaged ? &cmap : nullptr));
   k += 2;
   if( kernels ) *kernels = k;
   return SST_OK;

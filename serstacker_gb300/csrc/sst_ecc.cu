@@ -1341,9 +1341,143 @@ __global__ void __launch_bounds__(256) k_correlation_finish(CorrArgs a)
   }
 }
 
-cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st)
+/* Correlation with each (frame, tile) footprint staged by TMA (uniform
+ * batches): same structure as the staged IC pass; items whose taps leave
+ * the level or the box, or with a reference mask, take the global path. */
+template<int FAM>
+__device__ __forceinline__ void plan_corr_item(const CorrArgs & a, int item, float * s_c, ItemPlan * plan)
 {
-  switch ( motion_family(a.model.type) ) {
+  const int lane = threadIdx.x & 31;
+  const int f = item / a.tiles, t = item - f * a.tiles;
+  const FrameState * F = a.fs + f;
+  const bool live = F->status == SST_FRAME_OK;
+  float c[16];
+#pragma unroll
+  for( int i = 0; i < 16; ++i ) c[i] = __ldcg(F->wc + i);
+  if( lane < 16 ) s_c[lane] = __ldcg(F->wc + lane);
+  const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
+  const int tx1 = min(tx0 + PW_TX, a.w) - 1, ty1 = min(ty0 + PW_TY, a.h) - 1;
+  int bx0, by0, bx1, by1;
+  bool use = rect_footprint<FAM>(c, tx0, ty0, tx1, ty1, a.w, a.h, bx0, by0, bx1, by1);
+  use = use && live && !a.refM;
+  if( use ) {
+    bx0 = bx0 >= 0 ? bx0 & ~3 : -((-bx0 + 3) & ~3);
+    use = bx1 < bx0 + PB_W && by1 < by0 + PB_H;
+  }
+  if( lane == 0 ) {
+    plan->f = live ? f : -1, plan->t = t;
+    plan->use = use ? 1 : 0;
+    plan->bx0 = bx0, plan->by0 = by0;
+  }
+}
+
+template<int FAM>
+__global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __grid_constant__ CUtensorMap tmap)
+{
+  constexpr int NS = 6;
+  __shared__ __align__(128) float s_box[2][PB_H * PB_W];
+  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ float s_red[8 * NS];
+  __shared__ double s_tile[NS];
+  __shared__ float s_c[3][16];
+  __shared__ ItemPlan s_plan[3];
+  const int nitems = a.n * a.tiles;
+  if( (int) blockIdx.x >= nitems ) return;          // uniform over the CTA
+  if( threadIdx.x == 0 ) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if( threadIdx.x < 32 ) plan_corr_item<FAM>(a, blockIdx.x, s_c[0], &s_plan[0]);
+  __syncthreads();
+  if( threadIdx.x == 0 && s_plan[0].use ) {
+    mbar_expect_tx(&s_bar[0], PB_W * PB_H * sizeof(float));
+    tma_load_3d(s_box[0], &tmap, s_plan[0].bx0, s_plan[0].by0, s_plan[0].f, &s_bar[0]);
+  }
+  uint32_t phases = 0u;
+  bool timed_out = false;
+  int slot = 0, b = 0;
+  for( int item = blockIdx.x; item < nitems; item += gridDim.x, b ^= 1 ) {
+    const int nitem = item + gridDim.x;
+    const int nslot = slot == 2 ? 0 : slot + 1;
+    if( threadIdx.x < 32 && nitem < nitems ) plan_corr_item<FAM>(a, nitem, s_c[nslot], &s_plan[nslot]);
+    __syncthreads();
+    if( threadIdx.x == 0 && nitem < nitems && s_plan[nslot].use ) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&s_bar[b ^ 1], PB_W * PB_H * sizeof(float));
+      tma_load_3d(s_box[b ^ 1], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, s_plan[nslot].f, &s_bar[b ^ 1]);
+    }
+    const ItemPlan pl = s_plan[slot];
+    float c[16];
+#pragma unroll
+    for( int i = 0; i < 16; ++i ) c[i] = s_c[slot][i];
+    slot = nslot;
+    if( pl.f < 0 ) continue;                        // frame already rejected: uniform over the CTA
+    const int f = pl.f, t = pl.t;
+    const float * img = a.pyr + (size_t) f * a.pyr_stride;
+    const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
+    const int x = tx0 + (threadIdx.x & (PW_TX - 1));
+    const int yend = min(ty0 + PW_TY, a.h);
+    float acc[NS] = { 0, 0, 0, 0, 0, 0 };
+    if( pl.use ) {
+      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true;
+      phases ^= 1u << b;
+      if( x < a.w ) {
+        const float * box = s_box[b];
+        const int y0r = ty0 + (threadIdx.x >> 7);
+        const int xI = x + (int) c[12] - pl.bx0, yI = (int) c[13] - pl.by0;
+        const float fx = (float) x;
+        float fy = (float) y0r;
+#pragma unroll 4
+        for( int y = y0r; y < yend; y += 2, fy += 2.f ) {
+          float dx, dy;
+          warp_disp<FAM>(c, fx, fy, dx, dy);
+          const float flx = floorf(dx), fly = floorf(dy);
+          const float ax = dx - flx, ay = dy - fly;
+          const int o = min(max((y + yI + (int) fly) * PB_W + xI + (int) flx, 0), PB_W * PB_H - PB_W - 2);
+          const float v00 = box[o], v01 = box[o + 1], v10 = box[o + PB_W], v11 = box[o + PB_W + 1];
+          const float t0 = fmaf(ax, v01 - v00, v00), t1 = fmaf(ax, v11 - v10, v10);
+          const float av = __ldg(a.refT + (size_t) y * a.w + x) - a.tshift;
+          const float bv = fmaf(ay, t1 - t0, t0) - a.tshift;
+          acc[0] += av, acc[1] += bv;
+          acc[2] = fmaf(av, av, acc[2]);
+          acc[3] = fmaf(bv, bv, acc[3]);
+          acc[4] = fmaf(av, bv, acc[4]);
+          acc[5] += 1.f;
+        }
+      }
+    }
+    else {
+      for( int y = ty0 + (threadIdx.x >> 7); y < yend && x < a.w; y += 2 ) {
+        const spos s = warp_pos<FAM>(c, x, y);
+        const size_t i = (size_t) y * a.w + x;
+        bool ok = mask_ok(coverage(a.w, a.h, s), 254);
+        if( a.refM ) ok = ok && __ldg(a.refM + i) != 0;
+        if( ok ) {
+          const float av = __ldg(a.refT + i) - a.tshift;
+          const float bv = sample_constant0(img, a.w, a.h, s) - a.tshift;
+          acc[0] += av, acc[1] += bv;
+          acc[2] = fmaf(av, av, acc[2]);
+          acc[3] = fmaf(bv, bv, acc[3]);
+          acc[4] = fmaf(av, bv, acc[4]);
+          acc[5] += 1.f;
+        }
+      }
+    }
+    block_reduce_d<NS>(acc, s_red, s_tile);
+    write_tile_at<NS>(a.partials + (size_t) f * a.part_stride, t, s_tile);
+  }
+  (void) timed_out;
+}
+
+cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st, const CUtensorMap * map)
+{
+  const int fam = motion_family(a.model.type);
+  if( map && !a.roi && fam != FAM_QUAD ) {
+    if( fam == FAM_AFFINE ) k_correlation_tma<FAM_AFFINE><<<grid, 256, 0, st>>>(a, *map);
+    else k_correlation_tma<FAM_HOMOG><<<grid, 256, 0, st>>>(a, *map);
+  }
+  else switch ( fam ) {
   case FAM_AFFINE: k_correlation<FAM_AFFINE><<<grid, 256, 0, st>>>(a); break;
   case FAM_HOMOG: k_correlation<FAM_HOMOG><<<grid, 256, 0, st>>>(a); break;
   default: k_correlation<FAM_QUAD><<<grid, 256, 0, st>>>(a); break;

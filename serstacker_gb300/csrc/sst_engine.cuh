@@ -184,7 +184,7 @@ struct CorrArgs {
   int lmax;
   const int * tile_prefix;       // n + 1 correlation tile offsets (all frames)
 };
-cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st);
+cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st, const CUtensorMap * map = nullptr);
 
 /* ROI batches: prefix sums of the active frames' tile counts for one step */
 cudaError_t launch_roi_scan(const int * list, const int * count, const RoiLevel * roi, int lmax, int level,
