@@ -326,7 +326,7 @@ def main():
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "alg_bytes_per_launch": 16.0 * WIDTH * HEIGHT * n,
             "traffic_note": "DRAM bytes of a level-0 launch with all frames active (ncu, scaled from 64 frames)",
-            "kernel": "k_pass_pointwise<IC> level 0 (1280x960), all frames x iterations",
+            "kernel": "k_pass_pointwise_tma<IC> level 0 (1280x960), all frames x iterations",
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
             "alg_bytes_model": "16 B per pixel and frame-iteration (warped source 4 + template 4 + gradients 8)",
             "level0_ms_per_step": lv_ms, "level0_frame_iterations": lv_fi}
@@ -548,7 +548,7 @@ def main_bayer(args, ws, rank, local):
             lv_ms, lv_bytes = t, ab
     achieved = lv_bytes / (lv_ms / 1000.0) / 1e9 if lv_ms > 0 else 0.0
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": f"k_pass_pointwise<IC> level 0 ({pw}x{ph}), all frames x iterations",
+            "traffic": None, "kernel": f"k_pass_pointwise_tma<IC> level 0 ({pw}x{ph}), all frames x iterations",
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
             "alg_bytes_model": "16 B per pixel and frame-iteration"}
     res = {k: v.cpu().numpy() for k, v in dev_out.items()}

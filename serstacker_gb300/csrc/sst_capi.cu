@@ -631,6 +631,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
   c.counters = h->cnt.as<unsigned>();
   c.model = passes[num_passes - 1];
   c.min_rho = h->o.min_rho;
+  c.err = h->err.as<int>();
   CUtensorMap cmap;
   const bool cstaged = encode_pass_level(h->pyr.as<float>(), h->w, h->h, h->pyr_px, h->cap, &cmap);
   SST_CK_LAUNCH(launch_correlation(c, grid, st, cstaged ? &cmap : nullptr));

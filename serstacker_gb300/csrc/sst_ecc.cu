@@ -619,6 +619,8 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
   __shared__ double s_tile[NS];
   __shared__ float s_c[3][16];
   __shared__ ItemPlan s_plan[3];
+  __shared__ uint32_t s_infl;             // copies in flight, kept by thread 0
+  __shared__ int s_gaveup[2];             // a wait gave up during an item of this buffer parity
 
   const int count = __ldcg(a.count_in);
   const int nitems = count * a.tiles;
@@ -626,6 +628,8 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
   if( threadIdx.x == 0 ) {
     mbar_init(&s_bar[0], 1);
     mbar_init(&s_bar[1], 1);
+    s_infl = 0u;
+    s_gaveup[0] = s_gaveup[1] = 0;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if( threadIdx.x < 32 ) plan_item<METHOD, FAM>(a, blockIdx.x, s_c[0], &s_plan[0]);
@@ -633,19 +637,25 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
   if( threadIdx.x == 0 && s_plan[0].use ) {
     mbar_expect_tx(&s_bar[0], PB_W * PB_H * sizeof(float));
     tma_load_3d(s_box[0], &tmap, s_plan[0].bx0, s_plan[0].by0, s_plan[0].f, &s_bar[0]);
+    inflight_issued(&s_infl, 0, 0u);
   }
   uint32_t phases = 0u;
-  bool timed_out = false;
+  bool timed_out = false, stop = false;
   int slot = 0, b = 0;
   for( int item = blockIdx.x; item < nitems; item += gridDim.x, b ^= 1 ) {
     const int nitem = item + gridDim.x;
     const int nslot = slot == 2 ? 0 : slot + 1;
     if( threadIdx.x < 32 && nitem < nitems ) plan_item<METHOD, FAM>(a, nitem, s_c[nslot], &s_plan[nslot]);
     __syncthreads();
-    if( threadIdx.x == 0 && nitem < nitems && s_plan[nslot].use ) {
+    // once a wait gave up no further copy is issued or consumed; the previous item's
+    // flag is read after the barrier and written again no earlier than the next item,
+    // so every thread sees the same value
+    stop = stop || s_gaveup[b ^ 1];
+    if( threadIdx.x == 0 && nitem < nitems && s_plan[nslot].use && !stop ) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_expect_tx(&s_bar[b ^ 1], PB_W * PB_H * sizeof(float));
       tma_load_3d(s_box[b ^ 1], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, s_plan[nslot].f, &s_bar[b ^ 1]);
+      inflight_issued(&s_infl, b ^ 1, (phases >> (b ^ 1)) & 1u);
     }
     const ItemPlan pl = s_plan[slot];
     float c[16];
@@ -660,8 +670,9 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
     float P[NP], rr = 0.f, cnt = 0.f;
 #pragma unroll
     for( int k = 0; k < NP; ++k ) P[k] = 0.f;
-    if( pl.use ) {
-      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true;
+    if( pl.use && !stop ) {
+      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true, s_gaveup[b] = 1;
+      else if( threadIdx.x == 0 ) inflight_landed(&s_infl, b);
       phases ^= 1u << b;
       if( x < a.w ) {
         const float * box = s_box[b];
@@ -765,6 +776,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
     block_reduce_d<NS>(acc, s_red, s_tile);
     write_tile<NS>(a, f, t, s_tile);
   }
+  if( threadIdx.x == 0 ) inflight_drain(&s_infl, s_bar);
   if( timed_out && a.err ) atomicExch(a.err, 1);
 }
 
@@ -1381,11 +1393,15 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
   __shared__ double s_tile[NS];
   __shared__ float s_c[3][16];
   __shared__ ItemPlan s_plan[3];
+  __shared__ uint32_t s_infl;             // copies in flight, kept by thread 0
+  __shared__ int s_gaveup[2];             // a wait gave up during an item of this buffer parity
   const int nitems = a.n * a.tiles;
   if( (int) blockIdx.x >= nitems ) return;          // uniform over the CTA
   if( threadIdx.x == 0 ) {
     mbar_init(&s_bar[0], 1);
     mbar_init(&s_bar[1], 1);
+    s_infl = 0u;
+    s_gaveup[0] = s_gaveup[1] = 0;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if( threadIdx.x < 32 ) plan_corr_item<FAM>(a, blockIdx.x, s_c[0], &s_plan[0]);
@@ -1393,19 +1409,25 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
   if( threadIdx.x == 0 && s_plan[0].use ) {
     mbar_expect_tx(&s_bar[0], PB_W * PB_H * sizeof(float));
     tma_load_3d(s_box[0], &tmap, s_plan[0].bx0, s_plan[0].by0, s_plan[0].f, &s_bar[0]);
+    inflight_issued(&s_infl, 0, 0u);
   }
   uint32_t phases = 0u;
-  bool timed_out = false;
+  bool timed_out = false, stop = false;
   int slot = 0, b = 0;
   for( int item = blockIdx.x; item < nitems; item += gridDim.x, b ^= 1 ) {
     const int nitem = item + gridDim.x;
     const int nslot = slot == 2 ? 0 : slot + 1;
     if( threadIdx.x < 32 && nitem < nitems ) plan_corr_item<FAM>(a, nitem, s_c[nslot], &s_plan[nslot]);
     __syncthreads();
-    if( threadIdx.x == 0 && nitem < nitems && s_plan[nslot].use ) {
+    // once a wait gave up no further copy is issued or consumed; the previous item's
+    // flag is read after the barrier and written again no earlier than the next item,
+    // so every thread sees the same value
+    stop = stop || s_gaveup[b ^ 1];
+    if( threadIdx.x == 0 && nitem < nitems && s_plan[nslot].use && !stop ) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_expect_tx(&s_bar[b ^ 1], PB_W * PB_H * sizeof(float));
       tma_load_3d(s_box[b ^ 1], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, s_plan[nslot].f, &s_bar[b ^ 1]);
+      inflight_issued(&s_infl, b ^ 1, (phases >> (b ^ 1)) & 1u);
     }
     const ItemPlan pl = s_plan[slot];
     float c[16];
@@ -1419,8 +1441,9 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
     const int x = tx0 + (threadIdx.x & (PW_TX - 1));
     const int yend = min(ty0 + PW_TY, a.h);
     float acc[NS] = { 0, 0, 0, 0, 0, 0 };
-    if( pl.use ) {
-      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true;
+    if( pl.use && !stop ) {
+      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true, s_gaveup[b] = 1;
+      else if( threadIdx.x == 0 ) inflight_landed(&s_infl, b);
       phases ^= 1u << b;
       if( x < a.w ) {
         const float * box = s_box[b];
@@ -1467,7 +1490,8 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
     block_reduce_d<NS>(acc, s_red, s_tile);
     write_tile_at<NS>(a.partials + (size_t) f * a.part_stride, t, s_tile);
   }
-  (void) timed_out;
+  if( threadIdx.x == 0 ) inflight_drain(&s_infl, s_bar);
+  if( timed_out && a.err ) atomicExch(a.err, 1);
 }
 
 cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st, const CUtensorMap * map)

@@ -183,6 +183,7 @@ struct CorrArgs {
   const RoiLevel * roi;          // ROI batches: per-frame level-0 geometry
   int lmax;
   const int * tile_prefix;       // n + 1 correlation tile offsets (all frames)
+  int * err;                     // set to 1 when a bounded wait for a staged tile gave up
 };
 cudaError_t launch_correlation(const CorrArgs & a, int grid, cudaStream_t st, const CUtensorMap * map = nullptr);
 

@@ -281,6 +281,8 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
   // while slower warps may still read frame f's slot
   __shared__ float s_c[3][SST_NCOEF];
   __shared__ TilePlan s_plan[3];
+  __shared__ uint32_t s_infl;             // copies in flight, kept by thread 0
+  __shared__ int s_gaveup[2];             // a wait gave up during a frame of this parity
   __shared__ uint8_t s_v[VH * VW];
   __shared__ uint8_t s_h[VH * SA_TX];
   const int tx0 = blockIdx.x * SA_TX, ty0 = blockIdx.y * SA_TY;
@@ -296,6 +298,8 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
   if( threadIdx.x == 0 ) {
     mbar_init(&s_bar[0], 1);
     mbar_init(&s_bar[1], 1);
+    s_infl = 0u;
+    s_gaveup[0] = s_gaveup[1] = 0;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if( threadIdx.x < 32 && a.n > 0 ) plan_frame<FAM, T>(a, 0, tx0, ty0, wx0, wy0, wx1, wy1, s_c[0], &s_plan[0]);
@@ -303,8 +307,10 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
   if( threadIdx.x == 0 && a.n > 0 && s_plan[0].use ) {
     mbar_expect_tx(&s_bar[0], TB_W * TB_H * sizeof(T));
     tma_load_3d(s_box[0], &tmap, s_plan[0].bx0, s_plan[0].by0, 0, &s_bar[0]);
+    inflight_issued(&s_infl, 0, 0u);
   }
   int since = 0;
+  bool stop = false;
   int slot = 0;                                   // frame f's plan slot (f mod 3)
   for( int f = 0; f < a.n; ++f ) {
     const int b = f & 1, nb = b ^ 1;
@@ -314,10 +320,15 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
     if( threadIdx.x < 32 && f + 1 < a.n )
       plan_frame<FAM, T>(a, f + 1, tx0, ty0, wx0, wy0, wx1, wy1, s_c[nslot], &s_plan[nslot]);
     __syncthreads();
-    if( threadIdx.x == 0 && f + 1 < a.n && s_plan[nslot].use ) {
+    // once a wait gave up no further copy is issued or consumed; frame f - 1's flag
+    // is read after the barrier and written again no earlier than frame f + 1, so
+    // every thread sees the same value
+    stop = stop || s_gaveup[(f + 1) & 1];
+    if( threadIdx.x == 0 && f + 1 < a.n && s_plan[nslot].use && !stop ) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // order the generic reads of frame f - 1 before the copy
       mbar_expect_tx(&s_bar[nb], TB_W * TB_H * sizeof(T));
       tma_load_3d(s_box[nb], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, f + 1, &s_bar[nb]);
+      inflight_issued(&s_infl, nb, (phases >> nb) & 1u);
     }
     const TilePlan pl = s_plan[slot];
     float c[SST_NCOEF];
@@ -327,8 +338,9 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
     const float wf = pl.w;
     if( !(wf > 0.f) ) continue;                     // uniform over the CTA
     const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
-    if( pl.use ) {
-      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true;
+    if( pl.use && !stop ) {
+      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true, s_gaveup[b] = 1;
+      else if( threadIdx.x == 0 ) inflight_landed(&s_infl, b);
       phases ^= 1u << b;
       if( x < a.dw ) {
         const T * box = s_box[b];
@@ -417,6 +429,7 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
       since = 0;
     }
   }
+  if( threadIdx.x == 0 ) inflight_drain(&s_infl, s_bar);
   if( timed_out && a.err ) atomicExch(a.err, 1);
   if( x < a.dw ) {
 #pragma unroll

@@ -48,6 +48,28 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t * bar, uint32_t parit
   return false;
 }
 
+/* Copies of a CTA's double buffer that the issuing thread started and has not
+ * seen land, kept in one shared word by that thread alone: bit b = a copy into
+ * buffer b is outstanding, bit 2 + b = the barrier parity it completes. A CTA
+ * that gave up on a wait drains them (bounded again) before it exits, so no
+ * copy writes into the shared memory of a finished CTA. */
+__device__ __forceinline__ void inflight_issued(uint32_t * w, int b, uint32_t parity)
+{
+  *w = (*w & ~(5u << b)) | (1u << b) | (parity << (b + 2));
+}
+
+__device__ __forceinline__ void inflight_landed(uint32_t * w, int b)
+{
+  *w &= ~(1u << b);
+}
+
+__device__ __forceinline__ void inflight_drain(uint32_t * w, uint64_t * bars)
+{
+  for( int b = 0; b < 2; ++b )
+    if( (*w >> b) & 1u ) mbar_wait_bounded(&bars[b], (*w >> (b + 2)) & 1u);
+  *w = 0u;
+}
+
 /* 3-D tile copy (x, y, frame) of the tensor map into shared memory, completion on bar */
 __device__ __forceinline__ void tma_load_3d(void * dst, const CUtensorMap * map, int x, int y, int z, uint64_t * bar)
 {

@@ -59,7 +59,7 @@ def test_forward_and_gradients_match_oracle(gpu, oracle):
         L, gp, gt, gu = oracle.warp_residual(m, st, frames[i].astype(np.float64), tmpl.astype(np.float64),
                                              flow[i].astype(np.float64))
         gt_sum += gt
-        assert abs(float(loss[i]) - L) <= 1e-5 * L
+        assert abs(float(loss[i].detach()) - L) <= 1e-5 * L
         g = p.grad[i].cpu().numpy().astype(np.float64)
         assert np.abs(g - gp).max() <= 1e-4 * np.abs(gp).max(), (i, g, gp)
         gug = fl.grad[i].cpu().numpy()
