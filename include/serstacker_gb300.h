@@ -183,6 +183,20 @@ int sst_ecch_align_plain(sst_ecch * h, const void * frames, int depth, int n, in
 int sst_ecch_level_stats(sst_ecch * h, int pass, int level, float * ms, double * frame_iterations,
     double * algorithmic_bytes);
 
+/* One level of the reference pyramid as the engine holds it: the converted,
+ * pre-smoothed (reference_smooth_sigma) and pyrDown'ed reference, lw x lh
+ * floats with packed rows (lw, lh: level 0 the image size, then
+ * ((prev + 1) / 2) & ~1). Replaces c_ecch::reference_image() (ecc2.h:281) at
+ * level 0 and c_ecc_align::reference_image() (ecc2.h:119) of the level's
+ * aligner. out is host memory, or device memory when on_device != 0. */
+int sst_ecch_reference_image(sst_ecch * h, int level, float * out, int on_device);
+
+/* One level of frame `frame`'s pyramid from the last registration call (the
+ * converted, pre-smoothed input_smooth_sigma image and its pyrDown levels).
+ * Replaces c_ecch::current_image() (ecc2.h:284) / c_ecc_align::current_image()
+ * (ecc2.h:122) for the frames of a batch. */
+int sst_ecch_current_image(sst_ecch * h, int frame, int level, float * out, int on_device);
+
 /* --------------------------------------------- weighted average accumulator */
 
 typedef struct sst_weighted_average sst_weighted_average;

@@ -130,6 +130,13 @@ public:
   int num_iterations() const { return _num_iterations; }
   double rho() const { return _rho; }
   int num_levels() const { return _h ? sst_ecch_num_levels(_h) : 0; }
+  /* pyramid level of the reference / of frame `frame` of the last batch into
+   * out (host memory, lw x lh floats) */
+  bool reference_image(int level, float * out) const { return _h && sst_ecch_reference_image(_h, level, out, 0) == SST_OK; }
+  bool current_image(int frame, int level, float * out) const
+  {
+    return _h && sst_ecch_current_image(_h, frame, level, out, 0) == SST_OK;
+  }
   sst_ecch * handle() const { return _h; }
 
   static int nparams(const sst_motion_model & m)

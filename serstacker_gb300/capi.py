@@ -80,6 +80,8 @@ def lib():
             "sst_ecch_align_plain": (i, [p, p, i, i, i, i, sz, sz, d, i, i, p, i, p, p, p, p, p, p, p]),
             "sst_set_chunk_frames": (i, [p, i]),
             "sst_ecch_level_stats": (i, [p, i, i, p, p, p]),
+            "sst_ecch_reference_image": (i, [p, i, p, i]),
+            "sst_ecch_current_image": (i, [p, i, i, p, i]),
             "sst_weighted_average_create": (i, [p, i, i]),
             "sst_weighted_average_destroy": (i, [p]),
             "sst_weighted_average_clear": (i, [p, p]),
@@ -190,6 +192,26 @@ class c_ecch:
         _check(lib().sst_ecch_set_reference_image(self._h, _ptr(img), depth, img.shape[1], img.shape[0],
                                                   img.strides[0], scale, _ptr(m), 0 if m is None else m.strides[0],
                                                   0, None), "set_reference_image")
+        self._ref_shape = img.shape[:2]
+
+    def level_shape(self, level: int):
+        """(height, width) of a pyramid level: c_ecch::compute_next_pyramid_layer_size per level."""
+        hh, ww = self._ref_shape
+        for _ in range(level):
+            hh, ww = ((hh + 1) // 2) & ~1, ((ww + 1) // 2) & ~1
+        return hh, ww
+
+    def reference_image(self, level: int = 0) -> np.ndarray:
+        """The engine's reference pyramid level (converted, pre-smoothed, pyrDown'ed)."""
+        out = np.empty(self.level_shape(level), np.float32)
+        _check(lib().sst_ecch_reference_image(self._h, level, _ptr(out), 0), "reference_image")
+        return out
+
+    def current_image(self, frame: int, level: int = 0) -> np.ndarray:
+        """Frame `frame`'s pyramid level from the last registration call."""
+        out = np.empty(self.level_shape(level), np.float32)
+        _check(lib().sst_ecch_current_image(self._h, frame, level, _ptr(out), 0), "current_image")
+        return out
 
     def num_levels(self) -> int:
         return lib().sst_ecch_num_levels(self._h)

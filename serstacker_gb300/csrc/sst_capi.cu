@@ -176,6 +176,7 @@ struct sst_ecch {
   bool prof_ready = false;
   int last_steps[3][32];
   int last_method = 0;
+  int last_n = 0;                 // frames whose pyramids the batch buffer holds
 
   ~sst_ecch()
   {
@@ -276,6 +277,52 @@ extern "C" int sst_set_chunk_frames(sst_ecch * h, int frames)
   return SST_OK;
 }
 
+/* the device word that TMA-staged kernels set when a bounded wait gives up */
+static int ensure_err(sst_ecch * h)
+{
+  if( !h->err.p ) {
+    SST_CK(h->err.ensure(sizeof(int)));
+    SST_CK(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->st));
+  }
+  return SST_OK;
+}
+
+/* reports (and clears) a staged-tile wait that gave up during the last work */
+static int check_wait_flag(sst_ecch * h)
+{
+  if( !h->err.p ) return SST_OK;
+  int e = 0;
+  SST_CK(cudaMemcpyAsync(&e, h->err.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  SST_CK(cudaStreamSynchronize(h->st));
+  if( !e ) return SST_OK;
+  SST_CK(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->st));
+  return set_error(SST_ERR_TIMEOUT, "a bounded wait for a staged tile copy gave up; results are invalid");
+}
+
+/* Pyramid of n frames (levels at loff[], frame stride dst_stride floats):
+ * convert + pre-smooth, then pyrDown per level. Levels 0 and 1 come from one
+ * fused pass when it applies (7-tap Gaussian, TMA-compatible layout). */
+static int build_pyramid(sst_ecch * h, const void * src, int depth, int n, size_t row_stride, size_t frame_stride,
+    double scale, const float * gk, int ks, float * pyr, size_t dst_stride, cudaStream_t st)
+{
+  int l0 = 1;
+  bool fused = false;
+  if( h->L > 1 ) {
+    SST_CK_LAUNCH(launch_convert_pyr1(src, depth, n, h->lw[0], h->lh[0], row_stride, frame_stride, scale, gk, ks, pyr,
+        pyr + h->loff[1], h->lw[1], h->lh[1], dst_stride, h->err.as<int>(), st, &fused));
+  }
+  if( fused ) l0 = 2;
+  else {
+    SST_CK_LAUNCH(launch_convert_smooth(src, depth, n, h->lw[0], h->lh[0], row_stride, frame_stride, scale, gk, ks, pyr,
+        dst_stride, st));
+  }
+  for( int l = l0; l < h->L; ++l ) {
+    SST_CK_LAUNCH(launch_pyrdown(pyr + h->loff[l - 1], h->lw[l - 1], h->lh[l - 1], dst_stride, pyr + h->loff[l], h->lw[l],
+        h->lh[l], dst_stride, n, st));
+  }
+  return SST_OK;
+}
+
 static int upload_image(DevBuf & dst, const void * src, size_t row_stride, int rows, int on_device, const void ** dptr,
     cudaStream_t st)
 {
@@ -338,12 +385,9 @@ extern "C" int sst_ecch_set_reference_image(sst_ecch * h, const void * image, in
   const void * src = nullptr;
   SST_TRY(upload_image(h->refsrc, image, row_stride, height, on_device, &src, st));
   float * ref = h->ref.as<float>();
-  SST_CK_LAUNCH(launch_convert_smooth(src, depth, 1, width, height, row_stride, 0, scale,
+  SST_TRY(ensure_err(h));
+  SST_TRY(build_pyramid(h, src, depth, 1, row_stride, row_stride * height, scale,
       ks_ref ? h->gk_ref.as<float>() : nullptr, ks_ref, ref, 0, st));
-  for( int l = 1; l < L; ++l ) {
-    SST_CK_LAUNCH(launch_pyrdown(ref + h->loff[l - 1], h->lw[l - 1], h->lh[l - 1], 0, ref + h->loff[l], h->lw[l],
-        h->lh[l], 0, 1, st));
-  }
 
   // masks: level 0 copy, nearest resize per level (c_ecch::downscale_image), 5x5 erosion
   h->has_mask = mask != nullptr;
@@ -384,6 +428,7 @@ extern "C" int sst_ecch_set_reference_image(sst_ecch * h, const void * image, in
     h->RMA[l] = m;
   }
   SST_CK(cudaStreamSynchronize(st));
+  SST_TRY(check_wait_flag(h));
   SST_TRY(release_to_user(h, stream));
   return SST_OK;
 }
@@ -496,24 +541,9 @@ static int ensure_capacity(sst_ecch * h, int n, int method, int num_passes, cons
   SST_CK(h->out_weight.ensure((size_t) cap * sizeof(float)));
   SST_CK(h->weff.ensure((size_t) cap * sizeof(float)));
   SST_CK(h->coeffs.ensure((size_t) cap * SST_NCOEF * sizeof(float)));
-  if( !h->err.p ) {
-    SST_CK(h->err.ensure(sizeof(int)));
-    SST_CK(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->st));
-  }
+  SST_TRY(ensure_err(h));
   h->cap = cap;
   return SST_OK;
-}
-
-/* reports (and clears) a staged-tile wait that gave up during the last work */
-static int check_wait_flag(sst_ecch * h)
-{
-  if( !h->err.p ) return SST_OK;
-  int e = 0;
-  SST_CK(cudaMemcpyAsync(&e, h->err.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-  SST_CK(cudaStreamSynchronize(h->st));
-  if( !e ) return SST_OK;
-  SST_CK(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->st));
-  return set_error(SST_ERR_TIMEOUT, "a bounded wait for a staged tile copy gave up; results are invalid");
 }
 
 /* The Gauss-Newton schedule of one batch: pass begin, per level a level
@@ -665,6 +695,29 @@ extern "C" int sst_ecch_level_stats(sst_ecch * h, int pass, int level, float * m
   return SST_OK;
 }
 
+/* one pyramid level (lw x lh floats, rows packed) to host or device memory */
+static int copy_level(sst_ecch * h, const float * level_base, int level, float * out, int on_device)
+{
+  const size_t bytes = (size_t) h->lw[level] * h->lh[level] * sizeof(float);
+  SST_CK(cudaMemcpyAsync(out, level_base, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->st));
+  SST_CK(cudaStreamSynchronize(h->st));
+  return SST_OK;
+}
+
+extern "C" int sst_ecch_reference_image(sst_ecch * h, int level, float * out, int on_device)
+{
+  if( !h || !out || level < 0 || level >= h->L || !h->ref.p )
+    return set_error(SST_ERR_INVALID_ARG, "sst_ecch_reference_image: invalid arguments");
+  return copy_level(h, h->ref.as<float>() + h->loff[level], level, out, on_device);
+}
+
+extern "C" int sst_ecch_current_image(sst_ecch * h, int frame, int level, float * out, int on_device)
+{
+  if( !h || !out || level < 0 || level >= h->L || frame < 0 || frame >= h->last_n || !h->pyr.p )
+    return set_error(SST_ERR_INVALID_ARG, "sst_ecch_current_image: invalid arguments");
+  return copy_level(h, h->pyr.as<float>() + (size_t) frame * h->pyr_px + h->loff[level], level, out, on_device);
+}
+
 static int validate_passes(const sst_ecch * h, int num_passes, const sst_motion_model * passes)
 {
   if( num_passes < 1 || num_passes > 3 || !passes ) return set_error(SST_ERR_INVALID_ARG, "1..3 motion passes are required");
@@ -696,12 +749,9 @@ static int register_device(sst_ecch * h, const void * d_frames, int depth, int n
   }
   // pyramid of every frame: convert + pre-smooth, pyrDown
   float * pyr = h->pyr.as<float>();
-  SST_CK_LAUNCH(launch_convert_smooth(d_frames, depth, n, h->w, h->h, row_stride, frame_stride, scale,
+  SST_TRY(build_pyramid(h, d_frames, depth, n, row_stride, frame_stride, scale,
       h->ks_in ? h->gk_in.as<float>() : nullptr, h->ks_in, pyr, h->pyr_px, st));
-  for( int l = 1; l < h->L; ++l ) {
-    SST_CK_LAUNCH(launch_pyrdown(pyr + h->loff[l - 1], h->lw[l - 1], h->lh[l - 1], h->pyr_px, pyr + h->loff[l], h->lw[l],
-        h->lh[l], h->pyr_px, n, st));
-  }
+  h->last_n = n;
   const int lap_level = h->L > 1 ? 1 : 0;
   SST_CK_LAUNCH(launch_lap_energy(pyr, h->pyr_px, h->loff[lap_level], h->lw[lap_level], h->lh[lap_level], n,
       h->lap.as<double>(), h->lap_t, st));

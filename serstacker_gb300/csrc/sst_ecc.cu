@@ -574,19 +574,19 @@ struct ItemPlan {
   int bx0, by0;     // box origin in the level
 };
 
-/* Plans one work item (warp 0): frame, tile, coefficients (into s_c) and
- * whether its footprint is staged. */
+/* Plans one work item (warp 0) from values loaded an item earlier, so that
+ * the plan waits on no memory: the item's frame f and, in lane l, coefficient
+ * l & 15 of that frame. Writes the coefficients (s_c) and whether the item's
+ * footprint is staged. */
 template<int METHOD, int FAM>
-__device__ __forceinline__ void plan_item(const PassArgs & a, int item, float * s_c, ItemPlan * plan)
+__device__ __forceinline__ void plan_item(const PassArgs & a, int item, int f, float cl, float * s_c, ItemPlan * plan)
 {
   const int lane = threadIdx.x & 31;
-  const int fi = item / a.tiles, t = item - fi * a.tiles;
-  const int f = __ldcg(a.list_in + fi);
-  const float * wc = a.fs[f].wc;
+  const int t = item - (item / a.tiles) * a.tiles;
   float c[16];
 #pragma unroll
-  for( int i = 0; i < 16; ++i ) c[i] = __ldcg(wc + i);
-  if( lane < 16 ) s_c[lane] = __ldcg(wc + lane);
+  for( int i = 0; i < 16; ++i ) c[i] = __shfl_sync(0xffffffffu, cl, i);
+  if( lane < 16 ) s_c[lane] = cl;
   const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
   const int tx1 = min(tx0 + PW_TX, a.w) - 1, ty1 = min(ty0 + PW_TY, a.h) - 1;
   int bx0, by0, bx1, by1;
@@ -603,6 +603,26 @@ __device__ __forceinline__ void plan_item(const PassArgs & a, int item, float * 
   }
 }
 
+/* frame of work item `item` (active-list entry item / tiles), or 0 past the end */
+__device__ __forceinline__ int item_frame(const PassArgs & a, int item, int nitems)
+{
+  return item < nitems ? __ldcg(a.list_in + item / a.tiles) : 0;
+}
+
+/* FP64 sum, in warp order, of the 8 warp sums of an item (lanes < NS of
+ * one warp) stored as that item's tile partials */
+template<int NS>
+__device__ __forceinline__ void store_item_sums(const PassArgs & a, int f, int t, const float * scratch)
+{
+  const int lane = threadIdx.x & 31;
+  if( lane < NS ) {
+    double s = 0;
+#pragma unroll
+    for( int wv = 0; wv < 8; ++wv ) s += (double) scratch[wv * NS + lane];
+    a.partials[(size_t) f * a.part_stride + (size_t) t * NS + lane] = s;
+  }
+}
+
 /* The IC / IC-LM pass with each item's source footprint staged in shared
  * memory by one TMA copy, double-buffered across the CTA's consecutive items:
  * the gathers become shared-memory loads with no address arithmetic in
@@ -615,8 +635,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
   constexpr int NP = column_sums<JK, M>::N;
   __shared__ __align__(128) float s_box[2][PB_H * PB_W];
   __shared__ __align__(8) uint64_t s_bar[2];
-  __shared__ float s_red[8 * NS];
-  __shared__ double s_tile[NS];
+  __shared__ float s_red[2][8 * NS];     // warp sums of the current and the previous item
   __shared__ float s_c[3][16];
   __shared__ ItemPlan s_plan[3];
   __shared__ uint32_t s_infl;             // copies in flight, kept by thread 0
@@ -632,7 +651,18 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
     s_gaveup[0] = s_gaveup[1] = 0;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  if( threadIdx.x < 32 ) plan_item<METHOD, FAM>(a, blockIdx.x, s_c[0], &s_plan[0]);
+  // warp 0 keeps the frame of the item after next (f2) and the frame and lane
+  // coefficient of the next item (f1, c1) in flight one item ahead of their use
+  int f1 = 0, f2 = 0;
+  float c1 = 0.f;
+  if( threadIdx.x < 32 ) {
+    const int lane = threadIdx.x & 31;
+    const int f0 = item_frame(a, blockIdx.x, nitems);
+    plan_item<METHOD, FAM>(a, blockIdx.x, f0, __ldcg(a.fs[f0].wc + (lane & 15)), s_c[0], &s_plan[0]);
+    f1 = item_frame(a, blockIdx.x + gridDim.x, nitems);
+    c1 = __ldcg(a.fs[f1].wc + (lane & 15));
+    f2 = item_frame(a, blockIdx.x + 2 * gridDim.x, nitems);
+  }
   __syncthreads();
   if( threadIdx.x == 0 && s_plan[0].use ) {
     mbar_expect_tx(&s_bar[0], PB_W * PB_H * sizeof(float));
@@ -642,10 +672,18 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
   uint32_t phases = 0u;
   bool timed_out = false, stop = false;
   int slot = 0, b = 0;
+  int pf = -1, pt = 0;                              // previous item (its sums wait in s_red[b ^ 1])
   for( int item = blockIdx.x; item < nitems; item += gridDim.x, b ^= 1 ) {
     const int nitem = item + gridDim.x;
     const int nslot = slot == 2 ? 0 : slot + 1;
-    if( threadIdx.x < 32 && nitem < nitems ) plan_item<METHOD, FAM>(a, nitem, s_c[nslot], &s_plan[nslot]);
+    if( threadIdx.x < 32 && nitem < nitems ) {
+      plan_item<METHOD, FAM>(a, nitem, f1, c1, s_c[nslot], &s_plan[nslot]);
+      if( nitem + gridDim.x < nitems ) c1 = __ldcg(a.fs[f2].wc + (threadIdx.x & 15));
+      f1 = f2;
+      f2 = item_frame(a, nitem + 2 * gridDim.x, nitems);
+    }
+    // orders: the next plan; the previous item's warp sums; the previous item's
+    // reads of the box buffer that the next copy overwrites
     __syncthreads();
     // once a wait gave up no further copy is issued or consumed; the previous item's
     // flag is read after the barrier and written again no earlier than the next item,
@@ -657,7 +695,9 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
       tma_load_3d(s_box[b ^ 1], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, s_plan[nslot].f, &s_bar[b ^ 1]);
       inflight_issued(&s_infl, b ^ 1, (phases >> (b ^ 1)) & 1u);
     }
+    if( pf >= 0 && (threadIdx.x >> 5) == 1 ) store_item_sums<NS>(a, pf, pt, s_red[b ^ 1]);
     const ItemPlan pl = s_plan[slot];
+    pf = pl.f, pt = pl.t;
     float c[16];
 #pragma unroll
     for( int i = 0; i < 16; ++i ) c[i] = s_c[slot][i];
@@ -678,18 +718,49 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
         const float * box = s_box[b];
         const int y0r = ty0 + (threadIdx.x >> 7);
         if( y0r < yend ) cnt = (float) ((yend - 1 - y0r) / 2 + 1);
-        const int xI = x + (int) c[12] - pl.bx0, yI = (int) c[13] - pl.by0;
-        const float fx = (float) x;
+        // The column's sample positions as functions of the tile-local row tr = y - ty0,
+        // in box coordinates: (Kx, Ky) is the integer offset of (x + Ix, ty0 + Iy) from
+        // the box origin, the warp's displacement is added to it. Box coordinates are
+        // positive (footprint test), so truncation is the floor.
+        const float fx = (float) x, fty0 = (float) ty0;
+        const float Kx = (float) (x + (int) c[12] - pl.bx0), Ky = (float) (ty0 + (int) c[13] - pl.by0);
+        float e0, e1, e2, e3, e4, e5, e6;
+        if( FAM == FAM_AFFINE ) {
+          e0 = Kx + fmaf(c[0], fx, fmaf(c[1], fty0, c[2]));      // X = e0 + c1 tr
+          e1 = Ky + fmaf(c[3], fx, fmaf(c[4], fty0, c[5]));      // Y = e1 + (1 + c4) tr
+          e2 = 1.0f + c[4];
+          e3 = e4 = e5 = e6 = 0.f;
+        }
+        else {
+          // denominator 1 + q0 + c7 tr; x numerator nx0 + nxs tr; y numerator
+          // ny0 + tr (nys - c7 tr) (the displacement form of warp_disp, expanded in tr)
+          const float X1 = fx + c[12], Y1 = fty0 + c[13];
+          const float q0 = fmaf(c[6], fx, c[7] * fty0);
+          e0 = 1.0f + q0;
+          e1 = fmaf(-q0, X1, fmaf(c[0], fx, fmaf(c[1], fty0, c[2])));
+          e2 = fmaf(-c[7], X1, c[1]);
+          e3 = fmaf(-q0, Y1, fmaf(c[3], fx, fmaf(c[4], fty0, c[5])));
+          e4 = fmaf(-c[7], Y1, c[4] - q0);
+          e5 = c[7], e6 = -c[7];
+        }
         const float4 * tgp = a.refTG + (size_t) y0r * a.w + x;
-        float fy = (float) y0r;
+        float tr = (float) (threadIdx.x >> 7);
 #pragma unroll 4
-        for( int y = y0r; y < yend; y += 2, fy += 2.f, tgp += 2 * a.w ) {
-          float dx, dy;
-          warp_disp<FAM>(c, fx, fy, dx, dy);
-          const float flx = floorf(dx), fly = floorf(dy);
-          const float ax = dx - flx, ay = dy - fly;
+        for( int y = y0r; y < yend; y += 2, tr += 2.f, tgp += 2 * a.w ) {
+          float X, Y;
+          if( FAM == FAM_AFFINE ) {
+            X = fmaf(c[1], tr, e0);
+            Y = fmaf(e2, tr, e1);
+          }
+          else {
+            const float iw = __fdividef(1.0f, fmaf(e5, tr, e0));
+            X = fmaf(fmaf(e2, tr, e1), iw, Kx);
+            Y = fmaf(fmaf(tr, fmaf(e6, tr, e4), e3), iw, Ky + tr);
+          }
+          const int ix = __float2int_rz(X), iy = __float2int_rz(Y);
+          const float ax = X - (float) ix, ay = Y - (float) iy;
           // inside the box by construction (footprint test); the clamp only guards the array
-          const int o = min(max((y + yI + (int) fly) * PB_W + xI + (int) flx, 0), PB_W * PB_H - PB_W - 2);
+          const int o = (int) min((unsigned) (iy * PB_W + ix), (unsigned) (PB_W * PB_H - PB_W - 2));
           const float v00 = box[o], v01 = box[o + 1], v10 = box[o + PB_W], v11 = box[o + PB_W + 1];
           const float t0 = fmaf(ax, v01 - v00, v00), t1 = fmaf(ax, v11 - v10, v10);
           const float4 tg = __ldg(tgp);
@@ -697,10 +768,14 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
           const float u = tg.y * r, w = tg.z * r;
           rr = fmaf(r, r, rr);
           P[0] += u, P[1] += w;
-          if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fy, u, P[2 < NP ? 2 : 0]);
-          if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fy, w, P[3 < NP ? 3 : 0]);
-          if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fy * fy, w, P[4 < NP ? 4 : 0]);
+          if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(tr, u, P[2 < NP ? 2 : 0]);
+          if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(tr, w, P[3 < NP ? 3 : 0]);
+          if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(tr * tr, w, P[4 < NP ? 4 : 0]);
         }
+        // row moments about y = 0 from the moments about y = ty0
+        if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fty0, fmaf(fty0, P[1], 2.0f * P[3 < NP ? 3 : 0]), P[4 < NP ? 4 : 0]);
+        if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(fty0, P[1], P[3 < NP ? 3 : 0]);
+        if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(fty0, P[0], P[2 < NP ? 2 : 0]);
       }
     }
     else {
@@ -773,9 +848,15 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
     if( x < a.w ) column_project<JK, M>(P, (float) x, acc);
     acc[M] = rr;
     acc[M + 1] = cnt;
-    block_reduce_d<NS>(acc, s_red, s_tile);
-    write_tile<NS>(a, f, t, s_tile);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for( int k = 0; k < NS; ++k ) {
+      const float sk = warp_sum(acc[k]);
+      if( lane == 0 ) s_red[b][wid * NS + k] = sk;
+    }
   }
+  __syncthreads();
+  if( pf >= 0 && (threadIdx.x >> 5) == 1 ) store_item_sums<NS>(a, pf, pt, s_red[b ^ 1]);
   if( threadIdx.x == 0 ) inflight_drain(&s_infl, s_bar);
   if( timed_out && a.err ) atomicExch(a.err, 1);
 }

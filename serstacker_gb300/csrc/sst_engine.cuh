@@ -221,6 +221,9 @@ cudaError_t launch_convert_smooth(const void * src, int depth, int n, int w, int
     size_t frame_stride, double scale, const float * gk, int ksize, float * dst, size_t dst_stride, cudaStream_t st);
 cudaError_t launch_pyrdown(const float * src, int sw, int sh, size_t src_stride, float * dst, int dw, int dh,
     size_t dst_stride, int n, cudaStream_t st);
+cudaError_t launch_convert_pyr1(const void * src, int depth, int n, int w, int h, size_t row_stride,
+    size_t frame_stride, double scale, const float * gk, int ksize, float * dst0, float * dst1, int dw, int dh,
+    size_t dst_stride, int * err, cudaStream_t st, bool * done);
 cudaError_t launch_resize_nearest_u8(const uint8_t * src, int sw, int sh, uint8_t * dst, int dw, int dh, cudaStream_t st);
 cudaError_t launch_ref_gradients(const float * img, const uint8_t * mask, int w, int h, float2 * grad, cudaStream_t st);
 cudaError_t launch_pack_reference(const float * img, const float2 * grad, size_t n, float4 * out, cudaStream_t st);

@@ -13,6 +13,7 @@
  * shared memory; each input pixel is read from HBM once per kernel.
  */
 #include "sst_engine.cuh"
+#include "sst_tma.cuh"
 
 namespace sst {
 
@@ -297,6 +298,301 @@ cudaError_t launch_pyrdown_ragged(const float * src, const RaggedImg * jobs, int
   dim3 grid((max_dw + PD_TX - 1) / PD_TX, (max_dh + PD_TY - 1) / PD_TY, n);
   k_pyrdown<<<grid, 256, 0, st>>>(src, 0, 0, 0, dst, 0, 0, 0, jobs);
   return cudaGetLastError();
+}
+
+/* ------------------------- fused convert + pre-smooth + first pyrDown */
+
+/* One CTA per 128 x 32 level-0 tile (and its 64 x 16 level-1 tile). One TMA
+ * copy stages the raw input window (tile + 2 + R rows above and below, and
+ * enough columns for the smoothed window). The window is converted to scaled
+ * FP32 once. The separable 7-tap Gaussian gives the smoothed window S: 36
+ * rows (level-0 y = ty0 - 2 ... ty0 + 33) by 136 columns (x = tx0 - 4 ...
+ * tx0 + 131, so the tile's own cells start on a 16-byte boundary). Its tile
+ * part is stored as level 0; the 5-tap pyrDown of S (rows first, as pyrDown)
+ * gives level 1. So level 0 is written once and never read back.
+ * Borders: out-of-image input cells take the nearest in-image cell
+ * (REPLICATE, as sepFilter2D). Out-of-image cells of S that pyrDown taps
+ * reach take the reflected cell (REFLECT_101, as pyrDown). */
+constexpr int FP_TX = 128, FP_TY = 32, FP_R = 3;
+constexpr int FP_SW = FP_TX + 8, FP_SH = FP_TY + 4;       // smoothed window
+constexpr int FP_IH = FP_SH + 2 * FP_R;                   // input rows
+
+template<typename T>
+struct fp_geom {
+  static constexpr int VEC = 16 / (int) sizeof(T);                          // elements per 16 bytes
+  static constexpr int XA = VEC >= 7 ? VEC : 8;                            // left margin: >= 4 + R, 16 B, 4 floats
+  static constexpr int IW = (XA + FP_SW + VEC - 1) / VEC * VEC;            // input row (16-byte multiple)
+  static constexpr size_t IN_BYTES = ((size_t) IW * FP_IH * sizeof(T) + 127) / 128 * 128;
+  static constexpr size_t F_BYTES = ((size_t) IW * FP_IH * sizeof(float) + 127) / 128 * 128;
+  static constexpr size_t H_BYTES = (size_t) FP_IH * FP_SW * sizeof(float);
+  static constexpr size_t SMEM = 128 + IN_BYTES + F_BYTES + H_BYTES + 16;
+  static_assert((size_t) FP_SH * FP_SW * sizeof(float) <= F_BYTES, "S aliases the converted window");
+  static_assert(XA % 4 == 0 && XA >= 4 + FP_R, "left margin");
+};
+
+/* eight consecutive elements (16-byte aligned for u16 / f32, 8-byte for u8) as floats */
+__device__ __forceinline__ void load8(const uint16_t * p, float (&v)[8])
+{
+  const uint4 q = *reinterpret_cast<const uint4 *>(p);
+  const uint32_t u[4] = { q.x, q.y, q.z, q.w };
+#pragma unroll
+  for( int k = 0; k < 4; ++k ) v[2 * k] = (float) (u[k] & 0xffffu), v[2 * k + 1] = (float) (u[k] >> 16);
+}
+
+__device__ __forceinline__ void load8(const uint8_t * p, float (&v)[8])
+{
+  const uint2 q = *reinterpret_cast<const uint2 *>(p);
+#pragma unroll
+  for( int k = 0; k < 4; ++k ) v[k] = (float) ((q.x >> (8 * k)) & 0xffu), v[4 + k] = (float) ((q.y >> (8 * k)) & 0xffu);
+}
+
+__device__ __forceinline__ void load8(const float * p, float (&v)[8])
+{
+  const float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 4);
+  v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+}
+
+__device__ __forceinline__ float4 pyr5(float4 a, float4 b, float4 c, float4 d, float4 e)
+{
+  float4 r;
+  r.x = (a.x + e.x) * 0.0625f + (b.x + d.x) * 0.25f + c.x * 0.375f;
+  r.y = (a.y + e.y) * 0.0625f + (b.y + d.y) * 0.25f + c.y * 0.375f;
+  r.z = (a.z + e.z) * 0.0625f + (b.z + d.z) * 0.25f + c.z * 0.375f;
+  r.w = (a.w + e.w) * 0.0625f + (b.w + d.w) * 0.25f + c.w * 0.375f;
+  return r;
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256, 3) k_convert_pyr1(const __grid_constant__ CUtensorMap tmap, int w, int h,
+    float scale, const float * __restrict__ gk, float * dst0, float * dst1, int dw, int dh, size_t dst_stride,
+    int * err)
+{
+  using G = fp_geom<T>;
+  constexpr int IW = G::IW;
+  extern __shared__ unsigned char fp_smem[];
+  unsigned char * base = (unsigned char *) (((uintptr_t) fp_smem + 127) & ~(uintptr_t) 127);
+  T * s_in = (T *) base;                                          // FP_IH x IW raw input
+  float * s_f = (float *) (base + G::IN_BYTES);                   // FP_IH x IW scaled FP32; then S: FP_SH x FP_SW
+  float * s_h = (float *) (base + G::IN_BYTES + G::F_BYTES);      // FP_IH x FP_SW horizontal pass; then pyrDown rows
+  float * s_S = s_f;
+  uint64_t * bar = (uint64_t *) (base + G::IN_BYTES + G::F_BYTES + G::H_BYTES);
+
+  const int tx0 = blockIdx.x * FP_TX, ty0 = blockIdx.y * FP_TY, z = blockIdx.z;
+  const int wx0 = tx0 - G::XA, wy0 = ty0 - 2 - FP_R;              // input window origin
+  if( threadIdx.x == 0 ) {
+    mbar_init(bar, 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if( threadIdx.x == 0 ) {
+    mbar_expect_tx(bar, IW * FP_IH * sizeof(T));
+    tma_load_3d(s_in, &tmap, wx0, wy0, z, bar);
+  }
+  float g[2 * FP_R + 1];
+#pragma unroll
+  for( int i = 0; i <= 2 * FP_R; ++i ) g[i] = __ldg(gk + i);
+  if( !mbar_wait_bounded(bar, 0) ) {
+    if( threadIdx.x == 0 ) mbar_wait_bounded(bar, 0);            // let the copy land before the CTA can exit
+    if( err ) atomicExch(err, 1);
+  }
+
+  // convert + scale; where the window leaves the image, each cell takes the
+  // nearest in-image cell (REPLICATE)
+  const bool edge_in = wx0 < 0 || wx0 + IW > w || wy0 < 0 || wy0 + FP_IH > h;
+  if( !edge_in ) {
+    for( int q = threadIdx.x; q < FP_IH * (IW / 8); q += 256 ) {
+      const int r = q / (IW / 8), c = (q - r * (IW / 8)) * 8;
+      float v[8];
+      load8(s_in + r * IW + c, v);
+      float * o = s_f + r * IW + c;
+      *reinterpret_cast<float4 *>(o) = make_float4(v[0] * scale, v[1] * scale, v[2] * scale, v[3] * scale);
+      *reinterpret_cast<float4 *>(o + 4) = make_float4(v[4] * scale, v[5] * scale, v[6] * scale, v[7] * scale);
+    }
+  }
+  else {
+    for( int q = threadIdx.x; q < FP_IH * IW; q += 256 ) {
+      const int r = q / IW, c = q - r * IW;
+      const int rs = clampi(wy0 + r, 0, h - 1) - wy0, cs = clampi(wx0 + c, 0, w - 1) - wx0;
+      s_f[q] = (float) s_in[rs * IW + cs] * scale;
+    }
+  }
+  __syncthreads();
+
+  // horizontal Gaussian: S column c (x = tx0 - 4 + c) reads converted columns
+  // c + XA - 7 ... c + XA - 1; four columns per item from three 16-byte loads
+  for( int q = threadIdx.x; q < FP_IH * (FP_SW / 4); q += 256 ) {
+    const int r = q / (FP_SW / 4), c0 = (q - r * (FP_SW / 4)) * 4;
+    const float * p = s_f + r * IW + c0 + G::XA - 8;
+    float v[12];
+#pragma unroll
+    for( int k = 0; k < 3; ++k ) {
+      const float4 t = *reinterpret_cast<const float4 *>(p + 4 * k);
+      v[4 * k] = t.x, v[4 * k + 1] = t.y, v[4 * k + 2] = t.z, v[4 * k + 3] = t.w;
+    }
+    float o[4];
+#pragma unroll
+    for( int j = 0; j < 4; ++j ) {
+      float a = 0.f;
+#pragma unroll
+      for( int i = 0; i <= 2 * FP_R; ++i ) a = fmaf(g[i], v[j + 1 + i], a);
+      o[j] = a;
+    }
+    *reinterpret_cast<float4 *>(s_h + r * FP_SW + c0) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+  __syncthreads();
+
+  // vertical Gaussian: S row s (y = ty0 - 2 + s) reads rows s ... s + 2R of the
+  // horizontal pass; 4 rows x 4 columns per item (S overwrites the converted window)
+  for( int q = threadIdx.x; q < (FP_SH / 4) * (FP_SW / 4); q += 256 ) {
+    const int rg = q / (FP_SW / 4), c0 = (q - rg * (FP_SW / 4)) * 4, s0 = rg * 4;
+    float4 v[4 + 2 * FP_R];
+#pragma unroll
+    for( int i = 0; i < 4 + 2 * FP_R; ++i ) v[i] = *reinterpret_cast<const float4 *>(s_h + (s0 + i) * FP_SW + c0);
+#pragma unroll
+    for( int j = 0; j < 4; ++j ) {
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for( int i = 0; i <= 2 * FP_R; ++i ) {
+        a.x = fmaf(g[i], v[j + i].x, a.x), a.y = fmaf(g[i], v[j + i].y, a.y);
+        a.z = fmaf(g[i], v[j + i].z, a.z), a.w = fmaf(g[i], v[j + i].w, a.w);
+      }
+      *reinterpret_cast<float4 *>(s_S + (s0 + j) * FP_SW + c0) = a;
+    }
+  }
+  __syncthreads();
+
+  // level 0: the tile's cells of S (rows 2 ... 33, columns 4 ... 131)
+  float * out0 = dst0 + (size_t) z * dst_stride;
+  const bool vec0 = (w & 3) == 0;
+  for( int q = threadIdx.x; q < FP_TY * (FP_TX / 4); q += 256 ) {
+    const int i = q / (FP_TX / 4), k = q - i * (FP_TX / 4);
+    const int y = ty0 + i, x = tx0 + 4 * k;
+    if( y >= h || x >= w ) continue;
+    const float4 v = *reinterpret_cast<const float4 *>(s_S + (i + 2) * FP_SW + 4 + 4 * k);
+    float * o = out0 + (size_t) y * w + x;
+    if( vec0 && x + 3 < w ) *reinterpret_cast<float4 *>(o) = v;
+    else {
+      o[0] = v.x;
+      if( x + 1 < w ) o[1] = v.y;
+      if( x + 2 < w ) o[2] = v.z;
+      if( x + 3 < w ) o[3] = v.w;
+    }
+  }
+
+  // REFLECT_101 the cells of S that pyrDown taps reach outside the image
+  // (x in {-2, -1, w, w + 1}, then y likewise), from in-image cells of S
+  const bool edge_s = tx0 == 0 || ty0 == 0 || tx0 + FP_TX + 4 > w || ty0 + FP_TY + 2 > h;
+  if( edge_s ) {
+    for( int q = threadIdx.x; q < FP_SH * 4; q += 256 ) {
+      const int s = q >> 2, k = q & 3;
+      const int x = k < 2 ? k - 2 : w + k - 2, c = x - (tx0 - 4);
+      if( c >= 0 && c < FP_SW ) s_S[s * FP_SW + c] = s_S[s * FP_SW + clampi(reflect101(x, w) - (tx0 - 4), 0, FP_SW - 1)];
+    }
+    __syncthreads();
+    for( int q = threadIdx.x; q < 4 * FP_SW; q += 256 ) {
+      const int k = q / FP_SW, c = q - k * FP_SW;
+      const int y = k < 2 ? k - 2 : h + k - 2, s = y - (ty0 - 2);
+      if( s >= 0 && s < FP_SH ) s_S[s * FP_SW + c] = s_S[clampi(reflect101(y, h) - (ty0 - 2), 0, FP_SH - 1) * FP_SW + c];
+    }
+  }
+  __syncthreads();
+
+  // pyrDown [1 4 6 4 1] / 16, rows first (as pyrDown): level-1 column j
+  // (x = tx0 + 2j) reads S columns 2j + 2 ... 2j + 6; four columns per item
+  constexpr int TX1 = FP_TX / 2, TY1 = FP_TY / 2;
+  float * s_p = s_h;                                              // FP_SH x TX1
+  for( int q = threadIdx.x; q < FP_SH * (TX1 / 4); q += 256 ) {
+    const int s = q / (TX1 / 4), k = q - s * (TX1 / 4);
+    const float * p = s_S + s * FP_SW + 8 * k;
+    float v[16];
+#pragma unroll
+    for( int m = 0; m < 4; ++m ) {
+      const float4 t = *reinterpret_cast<const float4 *>(p + 4 * m);
+      v[4 * m] = t.x, v[4 * m + 1] = t.y, v[4 * m + 2] = t.z, v[4 * m + 3] = t.w;
+    }
+    float o[4];
+#pragma unroll
+    for( int m = 0; m < 4; ++m ) {
+      const float * a = v + 2 * m + 2;
+      o[m] = (a[0] + a[4]) * 0.0625f + (a[1] + a[3]) * 0.25f + a[2] * 0.375f;
+    }
+    *reinterpret_cast<float4 *>(s_p + s * TX1 + 4 * k) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+  __syncthreads();
+  // then columns: level-1 row i (y = ty0 + 2i) reads rows 2i ... 2i + 4
+  float * out1 = dst1 + (size_t) z * dst_stride;
+  const bool vec1 = (dw & 3) == 0;
+  for( int q = threadIdx.x; q < TY1 * (TX1 / 4); q += 256 ) {
+    const int i = q / (TX1 / 4), k = q - i * (TX1 / 4);
+    const int y1 = ty0 / 2 + i, x1 = tx0 / 2 + 4 * k;
+    if( y1 >= dh || x1 >= dw ) continue;
+    const float * p = s_p + (2 * i) * TX1 + 4 * k;
+    const float4 o = pyr5(*reinterpret_cast<const float4 *>(p), *reinterpret_cast<const float4 *>(p + TX1),
+        *reinterpret_cast<const float4 *>(p + 2 * TX1), *reinterpret_cast<const float4 *>(p + 3 * TX1),
+        *reinterpret_cast<const float4 *>(p + 4 * TX1));
+    float * d = out1 + (size_t) y1 * dw + x1;
+    if( vec1 && x1 + 3 < dw ) *reinterpret_cast<float4 *>(d) = o;
+    else {
+      d[0] = o.x;
+      if( x1 + 1 < dw ) d[1] = o.y;
+      if( x1 + 2 < dw ) d[2] = o.z;
+      if( x1 + 3 < dw ) d[3] = o.w;
+    }
+  }
+}
+
+template<typename T>
+static cudaError_t launch_fp(const CUtensorMap & map, int n, int w, int h, float scale, const float * gk, float * dst0,
+    float * dst1, int dw, int dh, size_t dst_stride, int * err, cudaStream_t st)
+{
+  static bool attr = false;
+  if( !attr ) {
+    cudaError_t e = cudaFuncSetAttribute(k_convert_pyr1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) fp_geom<T>::SMEM);
+    if( e != cudaSuccess ) return e;
+    attr = true;
+  }
+  dim3 grid((w + FP_TX - 1) / FP_TX, (h + FP_TY - 1) / FP_TY, n);
+  k_convert_pyr1<T><<<grid, 256, fp_geom<T>::SMEM, st>>>(map, w, h, scale, gk, dst0, dst1, dw, dh, dst_stride, err);
+  return cudaGetLastError();
+}
+
+/* Level 0 and level 1 of n frames in one pass when the pre-smoothing is the
+ * 7-tap Gaussian and the frames meet the TMA layout rules; *done = false
+ * (nothing launched) otherwise, and the caller builds the levels separately. */
+cudaError_t launch_convert_pyr1(const void * src, int depth, int n, int w, int h, size_t row_stride,
+    size_t frame_stride, double scale, const float * gk, int ksize, float * dst0, float * dst1, int dw, int dh,
+    size_t dst_stride, int * err, cudaStream_t st, bool * done)
+{
+  *done = false;
+  if( !gk || ksize != 2 * FP_R + 1 || w < 8 || h < 8 || n < 1 || n > 65535 || 2 * dw > w + 1 || 2 * dh > h + 1 )
+    return cudaSuccess;
+  CUtensorMap map;
+  const uint64_t dims[3] = { (uint64_t) w, (uint64_t) h, (uint64_t) n };
+  const uint64_t strides[2] = { (uint64_t) row_stride, (uint64_t) (n > 1 ? frame_stride : row_stride * h) };
+  cudaError_t e = cudaSuccess;
+  switch ( depth ) {
+  case SST_DEPTH_U8: {
+    const uint32_t box[3] = { (uint32_t) fp_geom<uint8_t>::IW, (uint32_t) FP_IH, 1 };
+    if( !encode_tensor_3d(&map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, src, dims, strides, box) ) return cudaSuccess;
+    e = launch_fp<uint8_t>(map, n, w, h, (float) scale, gk, dst0, dst1, dw, dh, dst_stride, err, st);
+    break;
+  }
+  case SST_DEPTH_U16: {
+    const uint32_t box[3] = { (uint32_t) fp_geom<uint16_t>::IW, (uint32_t) FP_IH, 1 };
+    if( !encode_tensor_3d(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, src, dims, strides, box) ) return cudaSuccess;
+    e = launch_fp<uint16_t>(map, n, w, h, (float) scale, gk, dst0, dst1, dw, dh, dst_stride, err, st);
+    break;
+  }
+  case SST_DEPTH_F32: {
+    const uint32_t box[3] = { (uint32_t) fp_geom<float>::IW, (uint32_t) FP_IH, 1 };
+    if( !encode_tensor_3d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src, dims, strides, box) ) return cudaSuccess;
+    e = launch_fp<float>(map, n, w, h, (float) scale, gk, dst0, dst1, dw, dh, dst_stride, err, st);
+    break;
+  }
+  default: return cudaSuccess;
+  }
+  if( e == cudaSuccess ) *done = true;
+  return e;
 }
 
 /* Sum of each image of a ragged job list (one CTA per image, fixed-order
