@@ -116,6 +116,20 @@ __device__ __forceinline__ bool rect_interior(const float * __restrict__ c, int 
   return __all_sync(0xffffffffu, ok);
 }
 
+/* rect_interior's test for one output position (one thread): both bilinear
+ * taps inside the w x h source with the 0.01 px margin, and w > 0 */
+template<int FAM>
+__device__ __forceinline__ bool point_interior(const float * __restrict__ c, int x, int y, int w, int h)
+{
+  if( FAM == FAM_QUAD ) return false;
+  float dx, dy;
+  warp_disp<FAM>(c, (float) x, (float) y, dx, dy);
+  const float X = (float) (x + (int) c[12]) + dx, Y = (float) (y + (int) c[13]) + dy;
+  bool ok = X >= 0.01f && X <= (float) (w - 2) - 0.01f && Y >= 0.01f && Y <= (float) (h - 2) - 0.01f;
+  if( FAM == FAM_HOMOG ) ok = ok && (1.0f + fmaf(c[6], (float) x, c[7] * (float) y)) > 0.f;
+  return ok;
+}
+
 /* Source footprint of the rectangle [x0, x1] x [y0, y1]: whether every
  * bilinear tap is inside a w x h source (as rect_interior) and the integer
  * box [bx0, bx1] x [by0, by1] that holds every tap (0.01 px margin against

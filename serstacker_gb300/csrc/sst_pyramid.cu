@@ -325,7 +325,7 @@ struct fp_geom {
   static constexpr size_t IN_BYTES = ((size_t) IW * FP_IH * sizeof(T) + 127) / 128 * 128;
   static constexpr size_t F_BYTES = ((size_t) IW * FP_IH * sizeof(float) + 127) / 128 * 128;
   static constexpr size_t H_BYTES = (size_t) FP_IH * FP_SW * sizeof(float);
-  static constexpr size_t SMEM = 128 + IN_BYTES + F_BYTES + H_BYTES + 16;
+  static constexpr size_t SMEM = 128 + 2 * IN_BYTES + F_BYTES + H_BYTES + 32;   // two input windows
   static_assert((size_t) FP_SH * FP_SW * sizeof(float) <= F_BYTES, "S aliases the converted window");
   static_assert(XA % 4 == 0 && XA >= 4 + FP_R, "left margin");
 };
@@ -362,197 +362,240 @@ __device__ __forceinline__ float4 pyr5(float4 a, float4 b, float4 c, float4 d, f
   return r;
 }
 
+/* Persistent: each CTA walks (frame, tile) items frame-major, and the input
+ * window of its next item is copied into the second buffer while the current
+ * item computes. */
 template<typename T>
 __global__ void __launch_bounds__(256, 3) k_convert_pyr1(const __grid_constant__ CUtensorMap tmap, int w, int h,
-    float scale, const float * __restrict__ gk, float * dst0, float * dst1, int dw, int dh, size_t dst_stride,
-    int * err)
+    int gx, int gy, int n, float scale, const float * __restrict__ gk, float * dst0, float * dst1, int dw, int dh,
+    size_t dst_stride, int * err)
 {
   using G = fp_geom<T>;
   constexpr int IW = G::IW;
+  constexpr int IN_ELEMS = (int) (G::IN_BYTES / sizeof(T));
   extern __shared__ unsigned char fp_smem[];
   unsigned char * base = (unsigned char *) (((uintptr_t) fp_smem + 127) & ~(uintptr_t) 127);
-  T * s_in = (T *) base;                                          // FP_IH x IW raw input
-  float * s_f = (float *) (base + G::IN_BYTES);                   // FP_IH x IW scaled FP32; then S: FP_SH x FP_SW
-  float * s_h = (float *) (base + G::IN_BYTES + G::F_BYTES);      // FP_IH x FP_SW horizontal pass; then pyrDown rows
+  T * s_in0 = (T *) base;                                         // two FP_IH x IW raw input windows
+  float * s_f = (float *) (base + 2 * G::IN_BYTES);               // FP_IH x IW scaled FP32; then S: FP_SH x FP_SW
+  float * s_h = (float *) (base + 2 * G::IN_BYTES + G::F_BYTES);  // FP_IH x FP_SW horizontal pass; then pyrDown rows
   float * s_S = s_f;
-  uint64_t * bar = (uint64_t *) (base + G::IN_BYTES + G::F_BYTES + G::H_BYTES);
+  uint64_t * bar = (uint64_t *) (base + 2 * G::IN_BYTES + G::F_BYTES + G::H_BYTES);
+  uint32_t * s_infl = (uint32_t *) (bar + 2);                     // copies in flight, kept by thread 0
+  int * s_gaveup = (int *) (s_infl + 1);                          // [2]: a wait gave up on this buffer
 
-  const int tx0 = blockIdx.x * FP_TX, ty0 = blockIdx.y * FP_TY, z = blockIdx.z;
-  const int wx0 = tx0 - G::XA, wy0 = ty0 - 2 - FP_R;              // input window origin
+  const int per_frame = gx * gy, items = per_frame * n;
+  if( (int) blockIdx.x >= items ) return;                         // uniform over the CTA
   if( threadIdx.x == 0 ) {
-    mbar_init(bar, 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    *s_infl = 0u;
+    s_gaveup[0] = s_gaveup[1] = 0;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
   if( threadIdx.x == 0 ) {
-    mbar_expect_tx(bar, IW * FP_IH * sizeof(T));
-    tma_load_3d(s_in, &tmap, wx0, wy0, z, bar);
+    const int z = blockIdx.x / per_frame, rem = blockIdx.x - z * per_frame, by = rem / gx, bx = rem - by * gx;
+    mbar_expect_tx(&bar[0], IW * FP_IH * sizeof(T));
+    tma_load_3d(s_in0, &tmap, bx * FP_TX - G::XA, by * FP_TY - 2 - FP_R, z, &bar[0]);
+    inflight_issued(s_infl, 0, 0u);
   }
   float g[2 * FP_R + 1];
 #pragma unroll
   for( int i = 0; i <= 2 * FP_R; ++i ) g[i] = __ldg(gk + i);
-  if( !mbar_wait_bounded(bar, 0) ) {
-    if( threadIdx.x == 0 ) mbar_wait_bounded(bar, 0);            // let the copy land before the CTA can exit
-    if( err ) atomicExch(err, 1);
-  }
+  uint32_t phases = 0u;
+  bool timed_out = false, stop = false;
+  int b = 0;
+  for( int item = blockIdx.x; item < items; item += gridDim.x, b ^= 1 ) {
+    // the next item's window goes into the other buffer, last read by the
+    // convert pass two items ago (every thread is past the barrier after it);
+    // the previous item's wait flag was written before that item's barriers
+    stop = stop || s_gaveup[b ^ 1];
+    const int nitem = item + gridDim.x;
+    if( threadIdx.x == 0 && nitem < items && !stop ) {
+      const int z = nitem / per_frame, rem = nitem - z * per_frame, by = rem / gx, bx = rem - by * gx;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&bar[b ^ 1], IW * FP_IH * sizeof(T));
+      tma_load_3d(s_in0 + (b ^ 1) * IN_ELEMS, &tmap, bx * FP_TX - G::XA, by * FP_TY - 2 - FP_R, z, &bar[b ^ 1]);
+      inflight_issued(s_infl, b ^ 1, (phases >> (b ^ 1)) & 1u);
+    }
+    const int z = item / per_frame, rem = item - z * per_frame, by = rem / gx, bx = rem - by * gx;
+    const int tx0 = bx * FP_TX, ty0 = by * FP_TY;
+    const int wx0 = tx0 - G::XA, wy0 = ty0 - 2 - FP_R;            // input window origin
+    const T * s_in = s_in0 + b * IN_ELEMS;
+    if( !stop ) {
+      if( !mbar_wait_bounded(&bar[b], (phases >> b) & 1u) ) timed_out = true, s_gaveup[b] = 1;
+      else if( threadIdx.x == 0 ) inflight_landed(s_infl, b);
+      phases ^= 1u << b;
+    }
 
-  // convert + scale; where the window leaves the image, each cell takes the
-  // nearest in-image cell (REPLICATE)
-  const bool edge_in = wx0 < 0 || wx0 + IW > w || wy0 < 0 || wy0 + FP_IH > h;
-  if( !edge_in ) {
-    for( int q = threadIdx.x; q < FP_IH * (IW / 8); q += 256 ) {
-      const int r = q / (IW / 8), c = (q - r * (IW / 8)) * 8;
-      float v[8];
-      load8(s_in + r * IW + c, v);
-      float * o = s_f + r * IW + c;
-      *reinterpret_cast<float4 *>(o) = make_float4(v[0] * scale, v[1] * scale, v[2] * scale, v[3] * scale);
-      *reinterpret_cast<float4 *>(o + 4) = make_float4(v[4] * scale, v[5] * scale, v[6] * scale, v[7] * scale);
-    }
-  }
-  else {
-    for( int q = threadIdx.x; q < FP_IH * IW; q += 256 ) {
-      const int r = q / IW, c = q - r * IW;
-      const int rs = clampi(wy0 + r, 0, h - 1) - wy0, cs = clampi(wx0 + c, 0, w - 1) - wx0;
-      s_f[q] = (float) s_in[rs * IW + cs] * scale;
-    }
-  }
-  __syncthreads();
-
-  // horizontal Gaussian: S column c (x = tx0 - 4 + c) reads converted columns
-  // c + XA - 7 ... c + XA - 1; four columns per item from three 16-byte loads
-  for( int q = threadIdx.x; q < FP_IH * (FP_SW / 4); q += 256 ) {
-    const int r = q / (FP_SW / 4), c0 = (q - r * (FP_SW / 4)) * 4;
-    const float * p = s_f + r * IW + c0 + G::XA - 8;
-    float v[12];
-#pragma unroll
-    for( int k = 0; k < 3; ++k ) {
-      const float4 t = *reinterpret_cast<const float4 *>(p + 4 * k);
-      v[4 * k] = t.x, v[4 * k + 1] = t.y, v[4 * k + 2] = t.z, v[4 * k + 3] = t.w;
-    }
-    float o[4];
-#pragma unroll
-    for( int j = 0; j < 4; ++j ) {
-      float a = 0.f;
-#pragma unroll
-      for( int i = 0; i <= 2 * FP_R; ++i ) a = fmaf(g[i], v[j + 1 + i], a);
-      o[j] = a;
-    }
-    *reinterpret_cast<float4 *>(s_h + r * FP_SW + c0) = make_float4(o[0], o[1], o[2], o[3]);
-  }
-  __syncthreads();
-
-  // vertical Gaussian: S row s (y = ty0 - 2 + s) reads rows s ... s + 2R of the
-  // horizontal pass; 4 rows x 4 columns per item (S overwrites the converted window)
-  for( int q = threadIdx.x; q < (FP_SH / 4) * (FP_SW / 4); q += 256 ) {
-    const int rg = q / (FP_SW / 4), c0 = (q - rg * (FP_SW / 4)) * 4, s0 = rg * 4;
-    float4 v[4 + 2 * FP_R];
-#pragma unroll
-    for( int i = 0; i < 4 + 2 * FP_R; ++i ) v[i] = *reinterpret_cast<const float4 *>(s_h + (s0 + i) * FP_SW + c0);
-#pragma unroll
-    for( int j = 0; j < 4; ++j ) {
-      float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-      for( int i = 0; i <= 2 * FP_R; ++i ) {
-        a.x = fmaf(g[i], v[j + i].x, a.x), a.y = fmaf(g[i], v[j + i].y, a.y);
-        a.z = fmaf(g[i], v[j + i].z, a.z), a.w = fmaf(g[i], v[j + i].w, a.w);
+    // convert + scale; where the window leaves the image, each cell takes the
+    // nearest in-image cell (REPLICATE)
+    const bool edge_in = wx0 < 0 || wx0 + IW > w || wy0 < 0 || wy0 + FP_IH > h;
+    if( !edge_in ) {
+      for( int q = threadIdx.x; q < FP_IH * (IW / 8); q += 256 ) {
+        const int r = q / (IW / 8), c = (q - r * (IW / 8)) * 8;
+        float v[8];
+        load8(s_in + r * IW + c, v);
+        float * o = s_f + r * IW + c;
+        *reinterpret_cast<float4 *>(o) = make_float4(v[0] * scale, v[1] * scale, v[2] * scale, v[3] * scale);
+        *reinterpret_cast<float4 *>(o + 4) = make_float4(v[4] * scale, v[5] * scale, v[6] * scale, v[7] * scale);
       }
-      *reinterpret_cast<float4 *>(s_S + (s0 + j) * FP_SW + c0) = a;
     }
-  }
-  __syncthreads();
-
-  // level 0: the tile's cells of S (rows 2 ... 33, columns 4 ... 131)
-  float * out0 = dst0 + (size_t) z * dst_stride;
-  const bool vec0 = (w & 3) == 0;
-  for( int q = threadIdx.x; q < FP_TY * (FP_TX / 4); q += 256 ) {
-    const int i = q / (FP_TX / 4), k = q - i * (FP_TX / 4);
-    const int y = ty0 + i, x = tx0 + 4 * k;
-    if( y >= h || x >= w ) continue;
-    const float4 v = *reinterpret_cast<const float4 *>(s_S + (i + 2) * FP_SW + 4 + 4 * k);
-    float * o = out0 + (size_t) y * w + x;
-    if( vec0 && x + 3 < w ) *reinterpret_cast<float4 *>(o) = v;
     else {
-      o[0] = v.x;
-      if( x + 1 < w ) o[1] = v.y;
-      if( x + 2 < w ) o[2] = v.z;
-      if( x + 3 < w ) o[3] = v.w;
-    }
-  }
-
-  // REFLECT_101 the cells of S that pyrDown taps reach outside the image
-  // (x in {-2, -1, w, w + 1}, then y likewise), from in-image cells of S
-  const bool edge_s = tx0 == 0 || ty0 == 0 || tx0 + FP_TX + 4 > w || ty0 + FP_TY + 2 > h;
-  if( edge_s ) {
-    for( int q = threadIdx.x; q < FP_SH * 4; q += 256 ) {
-      const int s = q >> 2, k = q & 3;
-      const int x = k < 2 ? k - 2 : w + k - 2, c = x - (tx0 - 4);
-      if( c >= 0 && c < FP_SW ) s_S[s * FP_SW + c] = s_S[s * FP_SW + clampi(reflect101(x, w) - (tx0 - 4), 0, FP_SW - 1)];
+      for( int q = threadIdx.x; q < FP_IH * IW; q += 256 ) {
+        const int r = q / IW, c = q - r * IW;
+        const int rs = clampi(wy0 + r, 0, h - 1) - wy0, cs = clampi(wx0 + c, 0, w - 1) - wx0;
+        s_f[q] = (float) s_in[rs * IW + cs] * scale;
+      }
     }
     __syncthreads();
-    for( int q = threadIdx.x; q < 4 * FP_SW; q += 256 ) {
-      const int k = q / FP_SW, c = q - k * FP_SW;
-      const int y = k < 2 ? k - 2 : h + k - 2, s = y - (ty0 - 2);
-      if( s >= 0 && s < FP_SH ) s_S[s * FP_SW + c] = s_S[clampi(reflect101(y, h) - (ty0 - 2), 0, FP_SH - 1) * FP_SW + c];
-    }
-  }
-  __syncthreads();
 
-  // pyrDown [1 4 6 4 1] / 16, rows first (as pyrDown): level-1 column j
-  // (x = tx0 + 2j) reads S columns 2j + 2 ... 2j + 6; four columns per item
-  constexpr int TX1 = FP_TX / 2, TY1 = FP_TY / 2;
-  float * s_p = s_h;                                              // FP_SH x TX1
-  for( int q = threadIdx.x; q < FP_SH * (TX1 / 4); q += 256 ) {
-    const int s = q / (TX1 / 4), k = q - s * (TX1 / 4);
-    const float * p = s_S + s * FP_SW + 8 * k;
-    float v[16];
-#pragma unroll
-    for( int m = 0; m < 4; ++m ) {
-      const float4 t = *reinterpret_cast<const float4 *>(p + 4 * m);
-      v[4 * m] = t.x, v[4 * m + 1] = t.y, v[4 * m + 2] = t.z, v[4 * m + 3] = t.w;
+    // horizontal Gaussian: S column c (x = tx0 - 4 + c) reads converted columns
+    // c + XA - 7 ... c + XA - 1; four columns per item from three 16-byte loads
+    for( int q = threadIdx.x; q < FP_IH * (FP_SW / 4); q += 256 ) {
+      const int r = q / (FP_SW / 4), c0 = (q - r * (FP_SW / 4)) * 4;
+      const float * p = s_f + r * IW + c0 + G::XA - 8;
+      float v[12];
+  #pragma unroll
+      for( int k = 0; k < 3; ++k ) {
+        const float4 t = *reinterpret_cast<const float4 *>(p + 4 * k);
+        v[4 * k] = t.x, v[4 * k + 1] = t.y, v[4 * k + 2] = t.z, v[4 * k + 3] = t.w;
+      }
+      float o[4];
+  #pragma unroll
+      for( int j = 0; j < 4; ++j ) {
+        float a = 0.f;
+  #pragma unroll
+        for( int i = 0; i <= 2 * FP_R; ++i ) a = fmaf(g[i], v[j + 1 + i], a);
+        o[j] = a;
+      }
+      *reinterpret_cast<float4 *>(s_h + r * FP_SW + c0) = make_float4(o[0], o[1], o[2], o[3]);
     }
-    float o[4];
-#pragma unroll
-    for( int m = 0; m < 4; ++m ) {
-      const float * a = v + 2 * m + 2;
-      o[m] = (a[0] + a[4]) * 0.0625f + (a[1] + a[3]) * 0.25f + a[2] * 0.375f;
+    __syncthreads();
+
+    // vertical Gaussian: S row s (y = ty0 - 2 + s) reads rows s ... s + 2R of the
+    // horizontal pass; 4 rows x 4 columns per item (S overwrites the converted window)
+    for( int q = threadIdx.x; q < (FP_SH / 4) * (FP_SW / 4); q += 256 ) {
+      const int rg = q / (FP_SW / 4), c0 = (q - rg * (FP_SW / 4)) * 4, s0 = rg * 4;
+      float4 v[4 + 2 * FP_R];
+  #pragma unroll
+      for( int i = 0; i < 4 + 2 * FP_R; ++i ) v[i] = *reinterpret_cast<const float4 *>(s_h + (s0 + i) * FP_SW + c0);
+  #pragma unroll
+      for( int j = 0; j < 4; ++j ) {
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+  #pragma unroll
+        for( int i = 0; i <= 2 * FP_R; ++i ) {
+          a.x = fmaf(g[i], v[j + i].x, a.x), a.y = fmaf(g[i], v[j + i].y, a.y);
+          a.z = fmaf(g[i], v[j + i].z, a.z), a.w = fmaf(g[i], v[j + i].w, a.w);
+        }
+        *reinterpret_cast<float4 *>(s_S + (s0 + j) * FP_SW + c0) = a;
+      }
     }
-    *reinterpret_cast<float4 *>(s_p + s * TX1 + 4 * k) = make_float4(o[0], o[1], o[2], o[3]);
+    __syncthreads();
+
+    // level 0: the tile's cells of S (rows 2 ... 33, columns 4 ... 131)
+    float * out0 = dst0 + (size_t) z * dst_stride;
+    const bool vec0 = (w & 3) == 0;
+    for( int q = threadIdx.x; q < FP_TY * (FP_TX / 4); q += 256 ) {
+      const int i = q / (FP_TX / 4), k = q - i * (FP_TX / 4);
+      const int y = ty0 + i, x = tx0 + 4 * k;
+      if( y >= h || x >= w ) continue;
+      const float4 v = *reinterpret_cast<const float4 *>(s_S + (i + 2) * FP_SW + 4 + 4 * k);
+      float * o = out0 + (size_t) y * w + x;
+      if( vec0 && x + 3 < w ) *reinterpret_cast<float4 *>(o) = v;
+      else {
+        o[0] = v.x;
+        if( x + 1 < w ) o[1] = v.y;
+        if( x + 2 < w ) o[2] = v.z;
+        if( x + 3 < w ) o[3] = v.w;
+      }
+    }
+
+    // REFLECT_101 the cells of S that pyrDown taps reach outside the image
+    // (x in {-2, -1, w, w + 1}, then y likewise), from in-image cells of S
+    const bool edge_s = tx0 == 0 || ty0 == 0 || tx0 + FP_TX + 4 > w || ty0 + FP_TY + 2 > h;
+    if( edge_s ) {
+      for( int q = threadIdx.x; q < FP_SH * 4; q += 256 ) {
+        const int s = q >> 2, k = q & 3;
+        const int x = k < 2 ? k - 2 : w + k - 2, c = x - (tx0 - 4);
+        if( c >= 0 && c < FP_SW ) s_S[s * FP_SW + c] = s_S[s * FP_SW + clampi(reflect101(x, w) - (tx0 - 4), 0, FP_SW - 1)];
+      }
+      __syncthreads();
+      for( int q = threadIdx.x; q < 4 * FP_SW; q += 256 ) {
+        const int k = q / FP_SW, c = q - k * FP_SW;
+        const int y = k < 2 ? k - 2 : h + k - 2, s = y - (ty0 - 2);
+        if( s >= 0 && s < FP_SH ) s_S[s * FP_SW + c] = s_S[clampi(reflect101(y, h) - (ty0 - 2), 0, FP_SH - 1) * FP_SW + c];
+      }
+    }
+    __syncthreads();
+
+    // pyrDown [1 4 6 4 1] / 16, rows first (as pyrDown): level-1 column j
+    // (x = tx0 + 2j) reads S columns 2j + 2 ... 2j + 6; four columns per item
+    constexpr int TX1 = FP_TX / 2, TY1 = FP_TY / 2;
+    float * s_p = s_h;                                              // FP_SH x TX1
+    for( int q = threadIdx.x; q < FP_SH * (TX1 / 4); q += 256 ) {
+      const int s = q / (TX1 / 4), k = q - s * (TX1 / 4);
+      const float * p = s_S + s * FP_SW + 8 * k;
+      float v[16];
+  #pragma unroll
+      for( int m = 0; m < 4; ++m ) {
+        const float4 t = *reinterpret_cast<const float4 *>(p + 4 * m);
+        v[4 * m] = t.x, v[4 * m + 1] = t.y, v[4 * m + 2] = t.z, v[4 * m + 3] = t.w;
+      }
+      float o[4];
+  #pragma unroll
+      for( int m = 0; m < 4; ++m ) {
+        const float * a = v + 2 * m + 2;
+        o[m] = (a[0] + a[4]) * 0.0625f + (a[1] + a[3]) * 0.25f + a[2] * 0.375f;
+      }
+      *reinterpret_cast<float4 *>(s_p + s * TX1 + 4 * k) = make_float4(o[0], o[1], o[2], o[3]);
+    }
+    __syncthreads();
+    // then columns: level-1 row i (y = ty0 + 2i) reads rows 2i ... 2i + 4
+    float * out1 = dst1 + (size_t) z * dst_stride;
+    const bool vec1 = (dw & 3) == 0;
+    for( int q = threadIdx.x; q < TY1 * (TX1 / 4); q += 256 ) {
+      const int i = q / (TX1 / 4), k = q - i * (TX1 / 4);
+      const int y1 = ty0 / 2 + i, x1 = tx0 / 2 + 4 * k;
+      if( y1 >= dh || x1 >= dw ) continue;
+      const float * p = s_p + (2 * i) * TX1 + 4 * k;
+      const float4 o = pyr5(*reinterpret_cast<const float4 *>(p), *reinterpret_cast<const float4 *>(p + TX1),
+          *reinterpret_cast<const float4 *>(p + 2 * TX1), *reinterpret_cast<const float4 *>(p + 3 * TX1),
+          *reinterpret_cast<const float4 *>(p + 4 * TX1));
+      float * d = out1 + (size_t) y1 * dw + x1;
+      if( vec1 && x1 + 3 < dw ) *reinterpret_cast<float4 *>(d) = o;
+      else {
+        d[0] = o.x;
+        if( x1 + 1 < dw ) d[1] = o.y;
+        if( x1 + 2 < dw ) d[2] = o.z;
+        if( x1 + 3 < dw ) d[3] = o.w;
+      }
+    }
   }
-  __syncthreads();
-  // then columns: level-1 row i (y = ty0 + 2i) reads rows 2i ... 2i + 4
-  float * out1 = dst1 + (size_t) z * dst_stride;
-  const bool vec1 = (dw & 3) == 0;
-  for( int q = threadIdx.x; q < TY1 * (TX1 / 4); q += 256 ) {
-    const int i = q / (TX1 / 4), k = q - i * (TX1 / 4);
-    const int y1 = ty0 / 2 + i, x1 = tx0 / 2 + 4 * k;
-    if( y1 >= dh || x1 >= dw ) continue;
-    const float * p = s_p + (2 * i) * TX1 + 4 * k;
-    const float4 o = pyr5(*reinterpret_cast<const float4 *>(p), *reinterpret_cast<const float4 *>(p + TX1),
-        *reinterpret_cast<const float4 *>(p + 2 * TX1), *reinterpret_cast<const float4 *>(p + 3 * TX1),
-        *reinterpret_cast<const float4 *>(p + 4 * TX1));
-    float * d = out1 + (size_t) y1 * dw + x1;
-    if( vec1 && x1 + 3 < dw ) *reinterpret_cast<float4 *>(d) = o;
-    else {
-      d[0] = o.x;
-      if( x1 + 1 < dw ) d[1] = o.y;
-      if( x1 + 2 < dw ) d[2] = o.z;
-      if( x1 + 3 < dw ) d[3] = o.w;
-    }
-  }
+  if( threadIdx.x == 0 ) inflight_drain(s_infl, bar);
+  if( timed_out && err ) atomicExch(err, 1);
 }
 
 template<typename T>
 static cudaError_t launch_fp(const CUtensorMap & map, int n, int w, int h, float scale, const float * gk, float * dst0,
     float * dst1, int dw, int dh, size_t dst_stride, int * err, cudaStream_t st)
 {
-  static bool attr = false;
-  if( !attr ) {
+  static int slots = 0;                       // resident CTAs on the device
+  if( !slots ) {
     cudaError_t e = cudaFuncSetAttribute(k_convert_pyr1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) fp_geom<T>::SMEM);
     if( e != cudaSuccess ) return e;
-    attr = true;
+    int dev = 0, sms = 0, per_sm = 0;
+    if( (e = cudaGetDevice(&dev)) != cudaSuccess ) return e;
+    if( (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ) return e;
+    if( (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_convert_pyr1<T>, 256, fp_geom<T>::SMEM)) != cudaSuccess )
+      return e;
+    slots = sms * (per_sm > 0 ? per_sm : 1);
   }
-  dim3 grid((w + FP_TX - 1) / FP_TX, (h + FP_TY - 1) / FP_TY, n);
-  k_convert_pyr1<T><<<grid, 256, fp_geom<T>::SMEM, st>>>(map, w, h, scale, gk, dst0, dst1, dw, dh, dst_stride, err);
+  const int gx = (w + FP_TX - 1) / FP_TX, gy = (h + FP_TY - 1) / FP_TY;
+  const long long items = (long long) gx * gy * n;
+  if( items > (1ll << 30) ) return cudaErrorInvalidValue;
+  const int grid = (int) (items < slots ? items : slots);
+  k_convert_pyr1<T><<<grid, 256, fp_geom<T>::SMEM, st>>>(map, w, h, gx, gy, n, scale, gk, dst0, dst1, dw, dh, dst_stride, err);
   return cudaGetLastError();
 }
 

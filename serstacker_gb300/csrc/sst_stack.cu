@@ -231,35 +231,69 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
 constexpr int TB_W = 80, TB_H = 24;
 
 struct TilePlan {
-  int use;          // 1: the frame's tile is staged by TMA (window interior, footprint fits the box)
+  int use;          // 1: the frame's tile footprint is staged by TMA (it fits the box)
+  int interior;     // 1: every pixel of the validity window is valid and every tap inside the frame
   int bx0, by0;     // box origin in the frame
   float w;          // frame weight
 };
 
-/* Plans frame f for this CTA's tile (warp 0): its weight, coefficients
- * (into s_c), and whether its footprint is staged. */
+/* Plans frame f for this CTA's tile (warp 0) from values loaded a frame
+ * earlier, so that the plan waits on no memory: coefficient l & 15 of the
+ * frame in lane l (cl) and its weight. Lanes 0-3 test the corners of the
+ * validity window (tile + 2 px halo, as rect_interior), lanes 4-7 the corners
+ * of the tile for its source footprint (as rect_footprint). */
 template<int FAM, typename T>
-__device__ __forceinline__ void plan_frame(const StackArgs & a, int f, int tx0, int ty0, int wx0, int wy0, int wx1,
-    int wy1, float * s_c, TilePlan * plan)
+__device__ __forceinline__ void plan_frame(const StackArgs & a, float cl, float wf, int tx0, int ty0, int wx0,
+    int wy0, int wx1, int wy1, float * s_c, TilePlan * plan)
 {
   constexpr int XA = 16 / (int) sizeof(T);
   const int lane = threadIdx.x & 31;
   float c[SST_NCOEF];
 #pragma unroll
-  for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + i);
-  if( lane < SST_NCOEF ) s_c[lane] = __ldg(a.coeffs + (size_t) f * SST_NCOEF + lane);
-  const float wf = __ldg(a.weights + f);
-  bool use = wf > 0.f && rect_interior<FAM>(c, wx0, wy0, wx1, wy1, a.sw, a.sh);
-  int bx0, by0, bx1, by1;
+  for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __shfl_sync(0xffffffffu, cl, i);
+  if( lane < SST_NCOEF ) s_c[lane] = cl;
   const int tx1 = min(tx0 + SA_TX, a.dw) - 1, ty1 = min(ty0 + SA_TY, a.dh) - 1;
-  const bool in_tile = rect_footprint<FAM>(c, tx0, ty0, tx1, ty1, a.sw, a.sh, bx0, by0, bx1, by1);
-  if( use && in_tile ) {
+  float X = 0.f, Y = 0.f;
+  bool ok = true, fin = true;
+  if( FAM == FAM_QUAD ) ok = fin = false;
+  else if( lane < 8 ) {
+    const bool win = lane < 4;
+    const int x = (lane & 1) ? (win ? wx1 : tx1) : (win ? wx0 : tx0);
+    const int y = (lane & 2) ? (win ? wy1 : ty1) : (win ? wy0 : ty0);
+    float dx, dy;
+    warp_disp<FAM>(c, (float) x, (float) y, dx, dy);
+    X = (float) (x + (int) c[12]) + dx, Y = (float) (y + (int) c[13]) + dy;
+    ok = X >= 0.01f && X <= (float) (a.sw - 2) - 0.01f && Y >= 0.01f && Y <= (float) (a.sh - 2) - 0.01f;
+    fin = fabsf(X) < 1e6f && fabsf(Y) < 1e6f;
+    if( FAM == FAM_HOMOG ) {
+      const bool pos = (1.0f + fmaf(c[6], (float) x, c[7] * (float) y)) > 0.f;
+      ok = ok && pos, fin = fin && pos;
+    }
+  }
+  const unsigned okm = __ballot_sync(0xffffffffu, ok), finm = __ballot_sync(0xffffffffu, fin);
+  // interior: every window pixel valid, every tap inside; boxable: the tile's
+  // taps lie in the bounding box of its mapped corners (w > 0 on the tile)
+  const bool interior = (okm & 0xFu) == 0xFu, boxable = (finm & 0xF0u) == 0xF0u;
+  // footprint box of the tile: min / max over lanes 4-7
+  float mnx = X, mxx = X, mny = Y, mxy = Y;
+#pragma unroll
+  for( int m = 1; m < 4; m <<= 1 ) {
+    mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, m)), mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, m));
+    mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, m)), mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, m));
+  }
+  mnx = __shfl_sync(0xffffffffu, mnx, 4), mxx = __shfl_sync(0xffffffffu, mxx, 4);
+  mny = __shfl_sync(0xffffffffu, mny, 4), mxy = __shfl_sync(0xffffffffu, mxy, 4);
+  bool use = wf > 0.f && boxable;
+  int bx0 = 0, by0 = 0;
+  if( use ) {
+    bx0 = (int) floorf(mnx - 0.01f), by0 = (int) floorf(mny - 0.01f);
+    const int bx1 = (int) floorf(mxx + 0.01f) + 1, by1 = (int) floorf(mxy + 0.01f) + 1;
     bx0 = bx0 >= 0 ? bx0 - bx0 % XA : -((-bx0 + XA - 1) / XA) * XA;   // round down to the alignment
     use = bx1 < bx0 + TB_W && by1 < by0 + TB_H;
   }
-  else use = false;
   if( lane == 0 ) {
     plan->use = use ? 1 : 0;
+    plan->interior = interior ? 1 : 0;
     plan->bx0 = bx0, plan->by0 = by0;
     plan->w = wf;
   }
@@ -268,7 +302,8 @@ __device__ __forceinline__ void plan_frame(const StackArgs & a, int f, int tx0, 
 /* The batched stack with the source footprint of each (frame, tile) staged
  * in shared memory by one TMA copy, double-buffered: while the CTA warps and
  * accumulates frame f from shared memory, the copy of frame f + 1 is in
- * flight. Frames whose tile needs the validity / border logic, or whose
+ * flight, and warp 0 has frame f + 2's coefficients in flight for the plan
+ * after. Frames whose tile needs the validity / border logic, or whose
  * footprint does not fit the box, take the global-memory paths. */
 template<int FAM, typename T>
 __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, const __grid_constant__ CUtensorMap tmap)
@@ -279,12 +314,13 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
   __shared__ __align__(8) uint64_t s_bar[2];
   // plans and coefficients rotate over three slots: frame f + 1 is planned
   // while slower warps may still read frame f's slot
-  __shared__ float s_c[3][SST_NCOEF];
+  __shared__ __align__(16) float s_c[3][SST_NCOEF];
   __shared__ TilePlan s_plan[3];
   __shared__ uint32_t s_infl;             // copies in flight, kept by thread 0
   __shared__ int s_gaveup[2];             // a wait gave up during a frame of this parity
   __shared__ uint8_t s_v[VH * VW];
   __shared__ uint8_t s_h[VH * SA_TX];
+  __shared__ uint8_t s_seg[VH * 4];       // window row segments with full coverage throughout
   const int tx0 = blockIdx.x * SA_TX, ty0 = blockIdx.y * SA_TY;
   const int lx = threadIdx.x % SA_TX, ly0 = threadIdx.x / SA_TX;
   const int x = tx0 + lx;
@@ -302,7 +338,13 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
     s_gaveup[0] = s_gaveup[1] = 0;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  if( threadIdx.x < 32 && a.n > 0 ) plan_frame<FAM, T>(a, 0, tx0, ty0, wx0, wy0, wx1, wy1, s_c[0], &s_plan[0]);
+  // warp 0: frame f + 1's lane coefficient and weight, loaded during frame f - 1
+  float cl1 = 0.f, w1 = 0.f;
+  if( threadIdx.x < 32 && a.n > 0 ) {
+    const int lane = threadIdx.x & 15;
+    plan_frame<FAM, T>(a, __ldg(a.coeffs + lane), __ldg(a.weights), tx0, ty0, wx0, wy0, wx1, wy1, s_c[0], &s_plan[0]);
+    if( a.n > 1 ) cl1 = __ldg(a.coeffs + SST_NCOEF + lane), w1 = __ldg(a.weights + 1);
+  }
   __syncthreads();
   if( threadIdx.x == 0 && a.n > 0 && s_plan[0].use ) {
     mbar_expect_tx(&s_bar[0], TB_W * TB_H * sizeof(T));
@@ -317,8 +359,13 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
     const int nslot = slot == 2 ? 0 : slot + 1;
     // plan frame f + 1; its box buffer was last read during frame f - 1, which every
     // thread has finished at the barrier below
-    if( threadIdx.x < 32 && f + 1 < a.n )
-      plan_frame<FAM, T>(a, f + 1, tx0, ty0, wx0, wy0, wx1, wy1, s_c[nslot], &s_plan[nslot]);
+    if( threadIdx.x < 32 && f + 1 < a.n ) {
+      plan_frame<FAM, T>(a, cl1, w1, tx0, ty0, wx0, wy0, wx1, wy1, s_c[nslot], &s_plan[nslot]);
+      if( f + 2 < a.n ) {
+        cl1 = __ldg(a.coeffs + (size_t) (f + 2) * SST_NCOEF + (threadIdx.x & 15));
+        w1 = __ldg(a.weights + f + 2);
+      }
+    }
     __syncthreads();
     // once a wait gave up no further copy is issued or consumed; frame f - 1's flag
     // is read after the barrier and written again no earlier than frame f + 1, so
@@ -338,23 +385,58 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
     const float wf = pl.w;
     if( !(wf > 0.f) ) continue;                     // uniform over the CTA
     const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
-    if( pl.use && !stop ) {
+    const bool staged = pl.use && !stop;
+    if( staged ) {
       if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true, s_gaveup[b] = 1;
       else if( threadIdx.x == 0 ) inflight_landed(&s_infl, b);
       phases ^= 1u << b;
+    }
+    if( staged && pl.interior ) {
       if( x < a.dw ) {
         const T * box = s_box[b];
+        // the column's displacements as functions of t = y - (ty0 + ly0) (rows 4k apart):
+        // affine d = e + c t; projective (the displacement form of warp_disp) numerators
+        // and denominator expanded in t. The integer offset of (x + Ix, y + Iy) from the
+        // box origin is added to the floor of the displacement.
+        const float fx = (float) x, fy0 = (float) (ty0 + ly0);
+        const int obase = (ty0 + ly0 + (int) c[13] - pl.by0) * TB_W + x + (int) c[12] - pl.bx0;
+        float e0, e1, e2 = 0.f, e3 = 0.f, e4 = 0.f;
+        if( FAM == FAM_AFFINE ) {
+          e0 = fmaf(c[0], fx, fmaf(c[1], fy0, c[2]));
+          e1 = fmaf(c[3], fx, fmaf(c[4], fy0, c[5]));
+        }
+        else {
+          const float X1 = fx + c[12], Y1 = fy0 + c[13];
+          const float q0 = fmaf(c[6], fx, c[7] * fy0);
+          e0 = 1.0f + q0;
+          e1 = fmaf(-q0, X1, fmaf(c[0], fx, fmaf(c[1], fy0, c[2])));
+          e2 = fmaf(-c[7], X1, c[1]);
+          e3 = fmaf(-q0, Y1, fmaf(c[3], fx, fmaf(c[4], fy0, c[5])));
+          e4 = fmaf(-c[7], Y1, c[4] - q0);
+        }
 #pragma unroll
         for( int k = 0; k < PPT; ++k ) {
           const int y = ty0 + ly0 + 4 * k;
           if( y < a.dh ) {
-            const spos s = warp_pos<FAM>(c, x, y);
+            const float t = (float) (4 * k);
+            float dx, dy;
+            if( FAM == FAM_AFFINE ) {
+              dx = fmaf(c[1], t, e0);
+              dy = fmaf(c[4], t, e1);
+            }
+            else {
+              const float iw = __fdividef(1.0f, fmaf(c[7], t, e0));
+              dx = fmaf(e2, t, e1) * iw;
+              dy = fmaf(t, fmaf(-c[7], t, e4), e3) * iw;
+            }
+            const int ix = __float2int_rd(dx), iy = __float2int_rd(dy);
+            const float fxr = dx - (float) ix, fyr = dy - (float) iy;
             // inside the box by construction (footprint test); the clamp only guards the array
-            const int o = min(max((s.y0 - pl.by0) * TB_W + (s.x0 - pl.bx0), 0), TB_W * TB_H - TB_W - 2);
+            const int o = (int) min((unsigned) (obase + 4 * k * TB_W + iy * TB_W + ix), (unsigned) (TB_W * TB_H - TB_W - 2));
             const float v00 = (float) box[o], v01 = (float) box[o + 1];
             const float v10 = (float) box[o + TB_W], v11 = (float) box[o + TB_W + 1];
-            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-            const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
+            const float t0 = fmaf(fxr, v01 - v00, v00), t1 = fmaf(fxr, v11 - v10, v10);
+            const float val = fmaf(fyr, t1 - t0, t0) * a.scale;
             const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
             pS[k] = fmaf(wp, val, pS[k]);
             pW[k] += wp;
@@ -362,7 +444,7 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
         }
       }
     }
-    else if( rect_interior<FAM>(c, wx0, wy0, wx1, wy1, a.sw, a.sh) ) {
+    else if( pl.interior ) {
       if( x < a.dw ) {
 #pragma unroll
         for( int k = 0; k < PPT; ++k ) {
@@ -383,10 +465,26 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
       }
     }
     else {
+      // validity of the window positions (tile + 2 px halo): each row in four
+      // segments; a segment whose end positions map strictly inside the frame
+      // (the rect_interior test: a projective map with w > 0 keeps a segment a
+      // segment) has full coverage throughout, the others are evaluated per position
+      if( threadIdx.x < VH * 4 ) {
+        const int r = threadIdx.x >> 2, sg = threadIdx.x & 3;
+        const int qy = ty0 - 2 + r;
+        bool all = true;
+        if( qy >= 0 && qy < a.dh ) {
+          const int qa = max(tx0 - 2 + sg * (VW / 4), 0), qb = min(tx0 - 2 + (sg + 1) * (VW / 4) - 1, a.dw - 1);
+          if( qa <= qb ) all = point_interior<FAM>(c, qa, qy, a.sw, a.sh) && point_interior<FAM>(c, qb, qy, a.sw, a.sh);
+        }
+        s_seg[threadIdx.x] = all ? 1 : 0;
+      }
+      __syncthreads();
       for( int q = threadIdx.x; q < VW * VH; q += 256 ) {
-        const int qx = tx0 - 2 + q % VW, qy = ty0 - 2 + q / VW;
+        const int r = q / VW, cc = q - r * VW;
+        const int qx = tx0 - 2 + cc, qy = ty0 - 2 + r;
         uint8_t v = 1;
-        if( qx >= 0 && qx < a.dw && qy >= 0 && qy < a.dh ) {
+        if( !s_seg[r * 4 + cc / (VW / 4)] && qx >= 0 && qx < a.dw && qy >= 0 && qy < a.dh ) {
           v = mask_ok(coverage(a.sw, a.sh, warp_pos<FAM>(c, qx, qy)), 255) ? 1 : 0;
         }
         s_v[q] = v;
@@ -406,10 +504,20 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
           const uint8_t * p = s_h + ly * SA_TX + lx;
           if( p[0] & p[SA_TX] & p[2 * SA_TX] & p[3 * SA_TX] & p[4 * SA_TX] ) {
             const spos s = warp_pos<FAM>(c, x, y);
-            const float v00 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
-            const float v01 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
-            const float v10 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
-            const float v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
+            float v00, v01, v10, v11;
+            if( staged && s.x0 >= 0 && s.x0 < a.sw - 1 && s.y0 >= 0 && s.y0 < a.sh - 1 ) {
+              // taps inside the frame: from the staged box (it holds every tap of the tile)
+              const T * box = s_box[b];
+              const int o = min(max((s.y0 - pl.by0) * TB_W + (s.x0 - pl.bx0), 0), TB_W * TB_H - TB_W - 2);
+              v00 = (float) box[o], v01 = (float) box[o + 1], v10 = (float) box[o + TB_W], v11 = (float) box[o + TB_W + 1];
+            }
+            else {
+              // < 0.2 % of the weight may fall outside: those taps take the border mode
+              v00 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
+              v01 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
+              v10 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
+              v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
+            }
             const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
             const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
             const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
