@@ -925,13 +925,15 @@ extern "C" int sst_ecch_align_plain(sst_ecch * h, const void * frames, int depth
 struct sst_weighted_average {
   int w = 0, h = 0;
   DevBuf acc, coeffs, weff, src, wsrc;
+  DevBuf part;                         // partial sums of the frame chunks of one batch
+  DevBuf err;                          // set on the device when a bounded tile-copy wait gave up
   DevBuf focus_e, focus_w, gk_focus;   // focus weighting: energy maps, blurred maps, Gaussian taps
   int gk_n = 0;
   int frames = 0;
   size_t plane() const { return (size_t) w * h; }
   ~sst_weighted_average()
   {
-    acc.release(), coeffs.release(), weff.release(), src.release(), wsrc.release();
+    acc.release(), coeffs.release(), weff.release(), src.release(), wsrc.release(), part.release(), err.release();
     focus_e.release(), focus_w.release(), gk_focus.release();
   }
 };
@@ -1044,8 +1046,29 @@ static int add_warped_device(sst_weighted_average * a, const void * d_frames, in
   s.acc = a->acc.as<float>();
   s.plane = a->plane();
   s.border = border;
+  // a tile's frames may be split over up to four CTAs (partial sums merged in order)
+  constexpr int kChunks = 4;
+  SST_CK(a->part.ensure((size_t) (kChunks - 1) * 4 * a->plane() * sizeof(float)));
+  s.part = a->part.as<float>(), s.max_chunks = kChunks;
+  if( !a->err.p ) {
+    SST_CK(a->err.ensure(sizeof(int)));
+    SST_CK(cudaMemsetAsync(a->err.p, 0, sizeof(int), st));
+  }
+  s.err = a->err.as<int>();
   SST_CK_LAUNCH(launch_stack_add_warped(s, m.type, depth, st));
   return SST_OK;
+}
+
+/* reports (and clears) a tile-copy wait of the stacking kernels that gave up */
+static int check_acc_wait_flag(sst_weighted_average * a, cudaStream_t st)
+{
+  if( !a->err.p ) return SST_OK;
+  int e = 0;
+  SST_CK(cudaMemcpyAsync(&e, a->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SST_CK(cudaStreamSynchronize(st));
+  if( !e ) return SST_OK;
+  SST_CK(cudaMemsetAsync(a->err.p, 0, sizeof(int), st));
+  return set_error(SST_ERR_TIMEOUT, "a bounded wait for a staged tile copy gave up; the accumulator is invalid");
 }
 
 extern "C" int sst_weighted_average_add_warped_batch(sst_weighted_average * a, const void * frames, int depth, int n,
@@ -1103,6 +1126,7 @@ extern "C" int sst_weighted_average_compute(sst_weighted_average * a, float * av
   if( a->frames < 1 ) return set_error(SST_ERR_STATE, "no frames accumulated");
   cudaStream_t st = (cudaStream_t) stream;
   const size_t N = a->plane();
+  SST_TRY(check_acc_wait_flag(a, st));
   if( on_device ) {
     SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, avg, mask, nullptr, st));
     return SST_OK;
@@ -1162,6 +1186,7 @@ extern "C" int sst_weighted_average_save_state(sst_weighted_average * a, float *
   cudaStream_t st = (cudaStream_t) stream;
   SST_CK(cudaMemcpyAsync(state4, a->acc.p, 4 * a->plane() * sizeof(float), cudaMemcpyDeviceToHost, st));
   SST_CK(cudaStreamSynchronize(st));
+  SST_TRY(check_acc_wait_flag(a, st));
   if( frames ) *frames = a->frames;
   return SST_OK;
 }

@@ -230,6 +230,45 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
  * x origin is a multiple of 16 bytes (the TMA rule for the innermost coordinate) */
 constexpr int TB_W = 80, TB_H = 24;
 
+/* Work item L of the batched stack grid: (tile, frame chunk). The tiles of
+ * the outer ring come first (their frames often need the validity / border
+ * path, so their CTAs run longest), then the inner tiles; the chunks of a tile
+ * are consecutive items. */
+__device__ __forceinline__ void stack_item(int L, int tx, int ty, int chunks, int & tile, int & chunk)
+{
+  const int ring = (tx > 2 && ty > 2) ? 2 * tx + 2 * (ty - 2) : 0;
+  if( L < ring * chunks ) {
+    const int r = L / chunks;
+    chunk = L - r * chunks;
+    if( r < tx ) tile = r;                                          // top row
+    else if( r < 2 * tx ) tile = (ty - 1) * tx + (r - tx);          // bottom row
+    else if( r < 2 * tx + ty - 2 ) tile = (1 + r - 2 * tx) * tx;    // left column
+    else tile = (1 + r - 2 * tx - (ty - 2)) * tx + tx - 1;         // right column
+    return;
+  }
+  const int q = (L - ring * chunks) / chunks;
+  chunk = (L - ring * chunks) - q * chunks;
+  if( !ring ) { tile = q; return; }
+  tile = (1 + q / (tx - 2)) * tx + 1 + q % (tx - 2);
+}
+
+/* adds the partial sums of chunks 1 .. K - 1 into the accumulator, in chunk
+ * order (the same compensated update the chunk-0 CTAs made) */
+__global__ void k_stack_merge_chunks(float * acc, const float * part, size_t plane, int parts)
+{
+  const size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if( i >= plane ) return;
+  float gS = acc[i], gcS = acc[plane + i], gW = acc[2 * plane + i], gcW = acc[3 * plane + i];
+  for( int j = 0; j < parts; ++j ) {
+    const float * P = part + (size_t) j * 4 * plane;
+    kahan_add(gS, gcS, P[i]);
+    gcS += P[plane + i];
+    kahan_add(gW, gcW, P[2 * plane + i]);
+    gcW += P[3 * plane + i];
+  }
+  acc[i] = gS, acc[plane + i] = gcS, acc[2 * plane + i] = gW, acc[3 * plane + i] = gcW;
+}
+
 struct TilePlan {
   int use;          // 1: the frame's tile footprint is staged by TMA (it fits the box)
   int interior;     // 1: every pixel of the validity window is valid and every tap inside the frame
@@ -306,7 +345,7 @@ __device__ __forceinline__ void plan_frame(const StackArgs & a, float cl, float 
  * after. Frames whose tile needs the validity / border logic, or whose
  * footprint does not fit the box, take the global-memory paths. */
 template<int FAM, typename T>
-__global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, const __grid_constant__ CUtensorMap tmap)
+__global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, const __grid_constant__ CUtensorMap tmap, int chunks)
 {
   constexpr int VW = SA_TX + 4, VH = SA_TY + 4;
   constexpr int PPT = SA_TX * SA_TY / 256;
@@ -321,7 +360,12 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
   __shared__ uint8_t s_v[VH * VW];
   __shared__ uint8_t s_h[VH * SA_TX];
   __shared__ uint8_t s_seg[VH * 4];       // window row segments with full coverage throughout
-  const int tx0 = blockIdx.x * SA_TX, ty0 = blockIdx.y * SA_TY;
+  int tile, chunk;
+  stack_item((int) blockIdx.x, (a.dw + SA_TX - 1) / SA_TX, (a.dh + SA_TY - 1) / SA_TY, chunks, tile, chunk);
+  const int tiles_x = (a.dw + SA_TX - 1) / SA_TX;
+  const int tx0 = (tile % tiles_x) * SA_TX, ty0 = (tile / tiles_x) * SA_TY;
+  // this CTA's frames [f0, f0 + nf)
+  const int f0 = (int) ((long long) chunk * a.n / chunks), nf = (int) ((long long) (chunk + 1) * a.n / chunks) - f0;
   const int lx = threadIdx.x % SA_TX, ly0 = threadIdx.x / SA_TX;
   const int x = tx0 + lx;
   const int wx0 = max(tx0 - 2, 0), wy0 = max(ty0 - 2, 0);
@@ -340,28 +384,30 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
   }
   // warp 0: frame f + 1's lane coefficient and weight, loaded during frame f - 1
   float cl1 = 0.f, w1 = 0.f;
-  if( threadIdx.x < 32 && a.n > 0 ) {
+  if( threadIdx.x < 32 && nf > 0 ) {
     const int lane = threadIdx.x & 15;
-    plan_frame<FAM, T>(a, __ldg(a.coeffs + lane), __ldg(a.weights), tx0, ty0, wx0, wy0, wx1, wy1, s_c[0], &s_plan[0]);
-    if( a.n > 1 ) cl1 = __ldg(a.coeffs + SST_NCOEF + lane), w1 = __ldg(a.weights + 1);
+    plan_frame<FAM, T>(a, __ldg(a.coeffs + (size_t) f0 * SST_NCOEF + lane), __ldg(a.weights + f0), tx0, ty0, wx0, wy0,
+        wx1, wy1, s_c[0], &s_plan[0]);
+    if( nf > 1 ) cl1 = __ldg(a.coeffs + (size_t) (f0 + 1) * SST_NCOEF + lane), w1 = __ldg(a.weights + f0 + 1);
   }
   __syncthreads();
-  if( threadIdx.x == 0 && a.n > 0 && s_plan[0].use ) {
+  if( threadIdx.x == 0 && nf > 0 && s_plan[0].use ) {
     mbar_expect_tx(&s_bar[0], TB_W * TB_H * sizeof(T));
-    tma_load_3d(s_box[0], &tmap, s_plan[0].bx0, s_plan[0].by0, 0, &s_bar[0]);
+    tma_load_3d(s_box[0], &tmap, s_plan[0].bx0, s_plan[0].by0, f0, &s_bar[0]);
     inflight_issued(&s_infl, 0, 0u);
   }
   int since = 0;
   bool stop = false;
-  int slot = 0;                                   // frame f's plan slot (f mod 3)
-  for( int f = 0; f < a.n; ++f ) {
-    const int b = f & 1, nb = b ^ 1;
+  int slot = 0;                                   // frame f's plan slot (j mod 3)
+  for( int j = 0; j < nf; ++j ) {
+    const int f = f0 + j;
+    const int b = j & 1, nb = b ^ 1;
     const int nslot = slot == 2 ? 0 : slot + 1;
     // plan frame f + 1; its box buffer was last read during frame f - 1, which every
     // thread has finished at the barrier below
-    if( threadIdx.x < 32 && f + 1 < a.n ) {
+    if( threadIdx.x < 32 && j + 1 < nf ) {
       plan_frame<FAM, T>(a, cl1, w1, tx0, ty0, wx0, wy0, wx1, wy1, s_c[nslot], &s_plan[nslot]);
-      if( f + 2 < a.n ) {
+      if( j + 2 < nf ) {
         cl1 = __ldg(a.coeffs + (size_t) (f + 2) * SST_NCOEF + (threadIdx.x & 15));
         w1 = __ldg(a.weights + f + 2);
       }
@@ -370,8 +416,8 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
     // once a wait gave up no further copy is issued or consumed; frame f - 1's flag
     // is read after the barrier and written again no earlier than frame f + 1, so
     // every thread sees the same value
-    stop = stop || s_gaveup[(f + 1) & 1];
-    if( threadIdx.x == 0 && f + 1 < a.n && s_plan[nslot].use && !stop ) {
+    stop = stop || s_gaveup[(j + 1) & 1];
+    if( threadIdx.x == 0 && j + 1 < nf && s_plan[nslot].use && !stop ) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // order the generic reads of frame f - 1 before the copy
       mbar_expect_tx(&s_bar[nb], TB_W * TB_H * sizeof(T));
       tma_load_3d(s_box[nb], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, f + 1, &s_bar[nb]);
@@ -547,6 +593,12 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
       kahan_add(S[k], cS[k], pS[k]);
       kahan_add(Wt[k], cW[k], pW[k]);
       const size_t i = (size_t) y * a.dw + x;
+      if( chunk > 0 ) {
+        // a later chunk's partial sums; merged in chunk order after the launch
+        float * P = a.part + (size_t) (chunk - 1) * 4 * a.plane;
+        P[i] = S[k], P[a.plane + i] = cS[k], P[2 * a.plane + i] = Wt[k], P[3 * a.plane + i] = cW[k];
+        continue;
+      }
       float gS = a.acc[i], gcS = a.acc[a.plane + i], gW = a.acc[2 * a.plane + i], gcW = a.acc[3 * a.plane + i];
       kahan_add(gS, gcS, S[k]);
       gcS += cS[k];
@@ -617,13 +669,34 @@ cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, 
   const int fam = motion_family(motion);
   CUtensorMap map;
   if( fam != FAM_QUAD && a.n > 0 && encode_frames(a, depth, &map) ) {
-#define SST_LAUNCH_TMA(FAMV, TV) k_stack_add_warped_tma<FAMV, TV><<<grid, 256, 0, st>>>(a, map)
+    // frame chunks: enough (tile, chunk) CTAs for about four per resident slot,
+    // at least 32 frames per chunk, within the caller's scratch
+    static int slots = 0;
+    if( !slots ) {
+      int dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      slots = 4 * (sms > 0 ? sms : 1);
+    }
+    const int tiles = (int) (grid.x * grid.y);
+    int chunks = 1;
+    if( a.part && a.max_chunks > 1 ) {
+      chunks = (4 * slots + tiles - 1) / tiles;
+      chunks = chunks < a.max_chunks ? chunks : a.max_chunks;
+      chunks = chunks < a.n / 32 ? chunks : a.n / 32;
+      chunks = chunks > 1 ? chunks : 1;
+    }
+    const unsigned items = (unsigned) tiles * (unsigned) chunks;
+#define SST_LAUNCH_TMA(FAMV, TV) k_stack_add_warped_tma<FAMV, TV><<<items, 256, 0, st>>>(a, map, chunks)
     switch ( depth ) {
     case SST_DEPTH_U8: if( fam == FAM_AFFINE ) SST_LAUNCH_TMA(FAM_AFFINE, uint8_t); else SST_LAUNCH_TMA(FAM_HOMOG, uint8_t); break;
     case SST_DEPTH_U16: if( fam == FAM_AFFINE ) SST_LAUNCH_TMA(FAM_AFFINE, uint16_t); else SST_LAUNCH_TMA(FAM_HOMOG, uint16_t); break;
     default: if( fam == FAM_AFFINE ) SST_LAUNCH_TMA(FAM_AFFINE, float); else SST_LAUNCH_TMA(FAM_HOMOG, float); break;
     }
 #undef SST_LAUNCH_TMA
+    cudaError_t e = cudaGetLastError();
+    if( e != cudaSuccess || chunks == 1 ) return e;
+    k_stack_merge_chunks<<<(unsigned) ((a.plane + 255) / 256), 256, 0, st>>>(a.acc, a.part, a.plane, chunks - 1);
     return cudaGetLastError();
   }
 #define SST_LAUNCH_STACK(FAMV, TV) k_stack_add_warped<FAMV, TV><<<grid, 256, 0, st>>>(a)

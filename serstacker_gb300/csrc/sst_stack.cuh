@@ -22,6 +22,10 @@ struct StackArgs {
   int border;               // image border mode of the remap (SST_BORDER_*)
   const float * wmap = nullptr;   // optional per-pixel weight maps (n x plane, output grid)
   int * err = nullptr;            // optional: set to 1 when a bounded wait for a tile copy gave up
+  // optional scratch for frame chunks: (max_chunks - 1) x 4 planes of partial
+  // sums, so that one tile's frames can be split over several CTAs
+  float * part = nullptr;
+  int max_chunks = 1;
 };
 
 /* four Bayer planes of raw u16 mosaic frames, stacked into four accumulators */
