@@ -58,12 +58,7 @@ __device__ void combine_partials(const double * P, int tiles, int NS, double * t
 template<int NS>
 __device__ __forceinline__ void block_reduce_d(const float (&acc)[NS], float * scratch, double * out)
 {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for( int k = 0; k < NS; ++k ) {
-    const float s = warp_sum(acc[k]);
-    if( lane == 0 ) scratch[wid * NS + k] = s;
-  }
+  warp_sums_to<NS>(acc, scratch + (threadIdx.x >> 5) * NS);
   __syncthreads();
   for( int k = threadIdx.x; k < NS; k += 256 ) {
     double t = 0;
@@ -848,12 +843,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
     if( x < a.w ) column_project<JK, M>(P, (float) x, acc);
     acc[M] = rr;
     acc[M + 1] = cnt;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for( int k = 0; k < NS; ++k ) {
-      const float sk = warp_sum(acc[k]);
-      if( lane == 0 ) s_red[b][wid * NS + k] = sk;
-    }
+    warp_sums_to<NS>(acc, &s_red[b][(threadIdx.x >> 5) * NS]);
   }
   __syncthreads();
   if( pf >= 0 && (threadIdx.x >> 5) == 1 ) store_item_sums<NS>(a, pf, pt, s_red[b ^ 1]);
@@ -1529,16 +1519,42 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
       if( x < a.w ) {
         const float * box = s_box[b];
         const int y0r = ty0 + (threadIdx.x >> 7);
-        const int xI = x + (int) c[12] - pl.bx0, yI = (int) c[13] - pl.by0;
-        const float fx = (float) x;
-        float fy = (float) y0r;
+        // sample positions in box coordinates as functions of the tile-local row
+        // (as in the IC pass): positive by the footprint test, so truncation floors
+        const float fx = (float) x, fty0 = (float) ty0;
+        const float Kx = (float) (x + (int) c[12] - pl.bx0), Ky = (float) (ty0 + (int) c[13] - pl.by0);
+        float e0, e1, e2, e3 = 0.f, e4 = 0.f, e5 = 0.f, e6 = 0.f;
+        if( FAM == FAM_AFFINE ) {
+          e0 = Kx + fmaf(c[0], fx, fmaf(c[1], fty0, c[2]));
+          e1 = Ky + fmaf(c[3], fx, fmaf(c[4], fty0, c[5]));
+          e2 = 1.0f + c[4];
+        }
+        else {
+          const float X1 = fx + c[12], Y1 = fty0 + c[13];
+          const float q0 = fmaf(c[6], fx, c[7] * fty0);
+          e0 = 1.0f + q0;
+          e1 = fmaf(-q0, X1, fmaf(c[0], fx, fmaf(c[1], fty0, c[2])));
+          e2 = fmaf(-c[7], X1, c[1]);
+          e3 = fmaf(-q0, Y1, fmaf(c[3], fx, fmaf(c[4], fty0, c[5])));
+          e4 = fmaf(-c[7], Y1, c[4] - q0);
+          e5 = c[7], e6 = -c[7];
+        }
+        float tr = (float) (threadIdx.x >> 7);
 #pragma unroll 4
-        for( int y = y0r; y < yend; y += 2, fy += 2.f ) {
-          float dx, dy;
-          warp_disp<FAM>(c, fx, fy, dx, dy);
-          const float flx = floorf(dx), fly = floorf(dy);
-          const float ax = dx - flx, ay = dy - fly;
-          const int o = min(max((y + yI + (int) fly) * PB_W + xI + (int) flx, 0), PB_W * PB_H - PB_W - 2);
+        for( int y = y0r; y < yend; y += 2, tr += 2.f ) {
+          float X, Y;
+          if( FAM == FAM_AFFINE ) {
+            X = fmaf(c[1], tr, e0);
+            Y = fmaf(e2, tr, e1);
+          }
+          else {
+            const float iw = __fdividef(1.0f, fmaf(e5, tr, e0));
+            X = fmaf(fmaf(e2, tr, e1), iw, Kx);
+            Y = fmaf(fmaf(tr, fmaf(e6, tr, e4), e3), iw, Ky + tr);
+          }
+          const int ix = __float2int_rz(X), iy = __float2int_rz(Y);
+          const float ax = X - (float) ix, ay = Y - (float) iy;
+          const int o = (int) min((unsigned) (iy * PB_W + ix), (unsigned) (PB_W * PB_H - PB_W - 2));
           const float v00 = box[o], v01 = box[o + 1], v10 = box[o + PB_W], v11 = box[o + PB_W + 1];
           const float t0 = fmaf(ax, v01 - v00, v00), t1 = fmaf(ax, v11 - v10, v10);
           const float av = __ldg(a.refT + (size_t) y * a.w + x) - a.tshift;

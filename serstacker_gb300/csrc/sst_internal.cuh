@@ -256,6 +256,39 @@ __device__ __forceinline__ float warp_sum(float v)
   return v;
 }
 
+/* Warp sums of NS values per lane, written to out[0 .. NS) by the lanes that
+ * hold them. Each stage halves the vector: the lanes with the stage's lane bit
+ * set keep the upper half and add their partner's upper half, the others the
+ * lower half, so NS sums cost about NS + 5 shuffles instead of 5 NS. After
+ * the halving stages lane L holds sum (L >> (5 - log2 N)) mod N (N = NS
+ * rounded up to a power of two); the remaining lane bits are a plain butterfly. */
+template<int NS>
+__device__ __forceinline__ void warp_sums_to(const float (&v)[NS], float * out)
+{
+  constexpr int N = NS <= 1 ? 1 : NS <= 2 ? 2 : NS <= 4 ? 4 : NS <= 8 ? 8 : NS <= 16 ? 16 : 32;
+  constexpr int LOGN = N == 1 ? 0 : N == 2 ? 1 : N == 4 ? 2 : N == 8 ? 3 : N == 16 ? 4 : 5;
+  const int lane = threadIdx.x & 31;
+  float w[N];
+#pragma unroll
+  for( int i = 0; i < N; ++i ) w[i] = i < NS ? v[i < NS ? i : 0] : 0.f;
+#pragma unroll
+  for( int t = 0; t < LOGN; ++t ) {
+    const int H = N >> (t + 1), off = 16 >> t;
+    const bool up = (lane & off) != 0;
+#pragma unroll
+    for( int i = 0; i < H; ++i ) {
+      const float send = up ? w[i] : w[i + H];
+      const float keep = up ? w[i + H] : w[i];
+      w[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+  }
+  float s = w[0];
+#pragma unroll
+  for( int off = 16 >> LOGN; off > 0; off >>= 1 ) s += __shfl_xor_sync(0xffffffffu, s, off);
+  const int idx = (lane >> (5 - LOGN)) & (N - 1);
+  if( (lane & ((32 >> LOGN) - 1)) == 0 && idx < NS ) out[idx] = s;
+}
+
 __device__ __forceinline__ double warp_sum(double v)
 {
 #pragma unroll
