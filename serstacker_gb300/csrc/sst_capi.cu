@@ -106,7 +106,9 @@ extern "C" int sst_device_count(void)
 
 extern "C" long long sst_kernel_launch_count(int reset)
 {
-  return reset ? g_launches.exchange(0) : g_launches.load();
+  // host launches plus the iterations of the graph level loops (counted on the device)
+  const long long loops = sst::loop_launches(reset != 0);
+  return (reset ? g_launches.exchange(0) : g_launches.load()) + loops;
 }
 
 extern "C" void sst_ecch_options_default(sst_ecch_options * o)
@@ -143,6 +145,7 @@ struct GraphEntry {
 struct sst_ecch {
   sst_ecch_options o;
   cudaStream_t st = nullptr, st_copy = nullptr;
+  cudaStream_t st_body = nullptr;   // captures the bodies of the level loops
   cudaEvent_t ev_user = nullptr, ev_done = nullptr, ev_copy[2] = { nullptr, nullptr }, ev_free[2] = { nullptr, nullptr };
   int num_sms = 0;
 
@@ -168,6 +171,8 @@ struct sst_ecch {
   DevBuf res_params, res_status, res_rho, res_weight;   // whole-sequence results of sst_stack_frames
   DevBuf binned;                     // 2x2-binned luminance of a chunk of raw Bayer frames
   DevBuf err;                        // device flag: a bounded wait for a staged tile gave up
+  DevBuf loopst;                     // per pass and level: loop cursor and the two list counts
+  int loops_ok = 1;                  // graph WHILE loops usable (cleared when building one fails)
   size_t part_stride = 0;
   int steps_cap = 0;
   int lap_t = 0;
@@ -185,7 +190,7 @@ struct sst_ecch {
     graphs.clear();
     DevBuf * bufs[] = { &ref, &grad, &refTG, &mask, &mask_e, &refsrc, &jc_id, &hpart, &gk_in, &gk_ref, &stage[0], &stage[1],
         &pyr, &fs, &part, &cnt, &lists, &counts, &lap, &init, &out_params, &out_status, &out_iters, &out_eps,
-        &out_rho, &out_weight, &weff, &coeffs, &res_params, &res_status, &res_rho, &res_weight, &binned, &err };
+        &out_rho, &out_weight, &weff, &coeffs, &res_params, &res_status, &res_rho, &res_weight, &binned, &err, &loopst };
     for( DevBuf * b : bufs ) b->release();
     for( auto & kv : H ) kv.second.release();
     if( ev_user ) cudaEventDestroy(ev_user);
@@ -196,6 +201,7 @@ struct sst_ecch {
     }
     if( st ) cudaStreamDestroy(st);
     if( st_copy ) cudaStreamDestroy(st_copy);
+    if( st_body ) cudaStreamDestroy(st_body);
   }
 
   void drop_graphs()
@@ -210,6 +216,7 @@ static int ensure_streams(sst_ecch * h)
   if( h->st ) return SST_OK;
   SST_CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
   SST_CK(cudaStreamCreateWithFlags(&h->st_copy, cudaStreamNonBlocking));
+  SST_CK(cudaStreamCreateWithFlags(&h->st_body, cudaStreamNonBlocking));
   SST_CK(cudaEventCreateWithFlags(&h->ev_user, cudaEventDisableTiming));
   SST_CK(cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming));
   for( int i = 0; i < 2; ++i ) {
@@ -546,12 +553,44 @@ static int ensure_capacity(sst_ecch * h, int n, int method, int num_passes, cons
   return SST_OK;
 }
 
+/* Adds a WHILE node after the work captured so far on st (a capture must be
+ * active) and captures its body on the engine's body stream: body(stream,
+ * handle) enqueues one iteration; the loop runs while the handle, 1 at each
+ * graph launch, stays non-zero. The capture on st continues after the node. */
+template<typename Body>
+static int add_level_loop(sst_ecch * h, cudaStream_t st, Body body)
+{
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t * deps = nullptr;
+  size_t nd = 0;
+  SST_CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+  if( cs != cudaStreamCaptureStatusActive ) return set_error(SST_ERR_STATE, "level loop outside a graph capture");
+  cudaGraphConditionalHandle hc;
+  SST_CK(cudaGraphConditionalHandleCreate(&hc, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams p = { cudaGraphNodeTypeConditional };   // the rest zero-initialised
+  p.conditional.handle = hc;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  SST_CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+  SST_CK(cudaStreamBeginCaptureToGraph(h->st_body, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+      cudaStreamCaptureModeThreadLocal));
+  const int r = body(h->st_body, hc);
+  cudaGraph_t out = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(h->st_body, &out);
+  if( r != SST_OK ) return r;
+  SST_CK(e);
+  SST_CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return SST_OK;
+}
+
 /* The Gauss-Newton schedule of one batch: pass begin, per level a level
  * begin and max_iterations + 1 pass launches, then the correlation. In
  * host-driven mode every step is followed by a synchronisation and an early
  * exit when no frame is left (the plain one-frame-per-launch form). */
 static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, const sst_motion_model * passes,
-    bool have_init, bool host_driven, long long * kernels)
+    bool have_init, bool host_driven, long long * kernels, bool loops = false)
 {
   cudaStream_t st = h->st;
   const int L = h->L;
@@ -578,11 +617,15 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
     for( int l = L - 1; l >= 0; --l ) {
       SST_CK(record_prof(h->prof[k_pass][l][0], st, host_driven));
       h->last_steps[k_pass][l] = step;
+      // graph loops: [cursor, count A, count B] of this pass and level; list A is the
+      // level's first list slot, list B the second, the step counts the history
+      int * lp = loops ? h->loopst.as<int>() + 4 * (k_pass * 32 + l) : nullptr;
+      if( loops ) SST_CK(cudaMemsetAsync(lp, 0, 4 * sizeof(int), st));
       LevelBeginArgs lb;
       memset(&lb, 0, sizeof(lb));
       lb.fs = fs, lb.n = n, lb.model = m, lb.method = method;
       lb.list_out = lists + (size_t) step * h->cap;
-      lb.count_out = counts + step;
+      lb.count_out = loops ? lp + 1 : counts + step;
       lb.level_is_first = l == L - 1;
       SST_CK_LAUNCH(launch_level_begin(lb, st));
       ++k;
@@ -626,7 +669,24 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
       CUtensorMap map;
       const bool staged = (method == M_IC || method == M_ICLM) &&
           encode_pass_level(h->pyr.as<float>() + h->loff[l], h->lw[l], h->lh[l], h->pyr_px, h->cap, &map);
-      for( int it = 0; it <= max_it; ++it ) {
+      if( loops ) {
+        a.list_in = lists + (size_t) step * h->cap;
+        a.count_in = lp + 1;
+        a.list_out = lists + (size_t) (step + 1) * h->cap;
+        a.count_out = lp + 2;
+        LevelLoopArgs la;
+        la.cursor = lp, la.list_a = lists + (size_t) step * h->cap, la.count_a = lp + 1;
+        la.list_b = lists + (size_t) (step + 1) * h->cap, la.count_b = lp + 2;
+        la.hist = counts + step, la.max_it = max_it;
+        SST_TRY(add_level_loop(h, st, [&](cudaStream_t sb, cudaGraphConditionalHandle hc) -> int {
+          la.handle = hc;
+          SST_CK(launch_pass(method, a, -1, sb, staged ? &map : nullptr));
+          SST_CK(launch_solve(method, a, solve_grid, sb));
+          SST_CK(launch_level_advance(la, sb));
+          return SST_OK;
+        }));
+      }
+      for( int it = 0; !loops && it <= max_it; ++it ) {
         a.list_in = lists + (size_t) (step + it) * h->cap;
         a.count_in = counts + step + it;
         a.list_out = lists + (size_t) (step + it + 1) * h->cap;
@@ -776,24 +836,34 @@ static int register_device(sst_ecch * h, const void * d_frames, int depth, int n
     GraphEntry * ge = nullptr;
     for( auto & g : h->graphs ) if( g.key == key ) ge = &g;
     if( !ge ) {
-      cudaGraph_t graph = nullptr;
-      SST_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      long long kk = 0;
-      const long long before = g_launches.load();
-      const int r = enqueue_schedule(h, n, method, num_passes, passes, init_states_host != nullptr, false, &kk);
-      g_launches.store(before);
-      cudaError_t e = cudaStreamEndCapture(st, &graph);
-      if( r != SST_OK ) {
-        if( graph ) cudaGraphDestroy(graph);
-        return r;
-      }
-      if( e != cudaSuccess ) return set_error(SST_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+      // levels as graph WHILE loops (no launches for iterations no frame needs);
+      // the unrolled schedule when such a graph cannot be built
+      if( h->loops_ok ) SST_CK(h->loopst.ensure((size_t) 3 * 32 * 4 * sizeof(int)));
       GraphEntry g;
       g.key = key;
-      g.kernels = kk;
-      e = cudaGraphInstantiate(&g.exec, graph, 0);
-      cudaGraphDestroy(graph);
-      if( e != cudaSuccess ) return set_error(SST_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+      for( int attempt = h->loops_ok ? 0 : 1; attempt < 2; ++attempt ) {
+        const bool loops = attempt == 0;
+        cudaGraph_t graph = nullptr;
+        SST_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        long long kk = 0;
+        const long long before = g_launches.load();
+        const int r = enqueue_schedule(h, n, method, num_passes, passes, init_states_host != nullptr, false, &kk, loops);
+        g_launches.store(before);
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if( r == SST_OK && e == cudaSuccess ) e = cudaGraphInstantiate(&g.exec, graph, 0);
+        if( graph ) cudaGraphDestroy(graph);
+        if( r == SST_OK && e == cudaSuccess ) {
+          g.kernels = kk;
+          break;
+        }
+        cudaGetLastError();
+        if( loops ) {
+          h->loops_ok = 0;
+          continue;
+        }
+        if( r != SST_OK ) return r;
+        return set_error(SST_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+      }
       h->graphs.push_back(g);
       ge = &h->graphs.back();
     }

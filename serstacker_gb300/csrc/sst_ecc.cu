@@ -1251,6 +1251,52 @@ cudaError_t launch_level_begin(const LevelBeginArgs & a, cudaStream_t st)
   return cudaGetLastError();
 }
 
+/* launches of the level loops' kernels (pass, solve, advance), counted on the device */
+__device__ unsigned long long g_loop_launches = 0;
+
+/* End of one iteration of a level run as a graph WHILE loop: records the
+ * active count the next iteration starts with, moves list B (the solve's
+ * output) to list A (the next pass's input), clears B and keeps the loop
+ * going while frames remain and iterations are left (the unrolled schedule's
+ * max_iterations + 1 passes). */
+__global__ void __launch_bounds__(1024) k_level_advance(LevelLoopArgs a)
+{
+  const int it = *a.cursor;
+  const int cb = *a.count_b;
+  for( int i = threadIdx.x; i < cb; i += blockDim.x ) a.list_a[i] = a.list_b[i];
+  __syncthreads();                                   // every thread has read the counts
+  if( threadIdx.x == 0 ) {
+    if( it == 0 ) a.hist[0] = *a.count_a;
+    a.hist[it + 1] = cb;
+    *a.count_a = cb;
+    *a.count_b = 0;
+    *a.cursor = it + 1;
+    g_loop_launches += 3;
+    cudaGraphSetConditional(a.handle, (cb > 0 && it + 1 <= a.max_it) ? 1u : 0u);
+  }
+}
+
+cudaError_t launch_level_advance(const LevelLoopArgs & a, cudaStream_t st)
+{
+  k_level_advance<<<1, 1024, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+long long loop_launches(bool reset)
+{
+  unsigned long long v = 0;
+  if( cudaDeviceSynchronize() != cudaSuccess ) {
+    cudaGetLastError();
+    return 0;
+  }
+  if( cudaMemcpyFromSymbol(&v, g_loop_launches, sizeof(v)) != cudaSuccess ) return 0;
+  if( reset ) {
+    const unsigned long long z = 0;
+    cudaMemcpyToSymbol(g_loop_launches, &z, sizeof(z));
+  }
+  return (long long) v;
+}
+
 /* c_ecch::align prologue (ecc2.cc:1133-1151): start state of the pass, then
  * scale_transfrom to the coarsest level. */
 __global__ void k_pass_begin(PassBeginArgs a)

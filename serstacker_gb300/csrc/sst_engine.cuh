@@ -154,6 +154,22 @@ struct LevelBeginArgs {
 };
 cudaError_t launch_level_begin(const LevelBeginArgs & a, cudaStream_t st);
 
+/* One level's Gauss-Newton iterations as a graph WHILE loop: the pass reads
+ * list A, the solve appends to list B, and the advance kernel moves B to A. */
+struct LevelLoopArgs {
+  int * cursor;             // iterations done at this level
+  int * list_a;             // active frames of the next pass
+  int * count_a;
+  const int * list_b;       // frames the solve kept iterating
+  int * count_b;
+  int * hist;               // per iteration: active frames at its start (step history)
+  int max_it;
+  cudaGraphConditionalHandle handle;
+};
+cudaError_t launch_level_advance(const LevelLoopArgs & a, cudaStream_t st);
+/* kernel launches made by the level loops since the last reset (3 per iteration) */
+long long loop_launches(bool reset);
+
 struct PassBeginArgs {
   FrameState * fs;
   int n;
