@@ -230,6 +230,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form leg (profiling runs)")
+    ap.add_argument("--unrolled-schedule", action="store_true",
+                    help="level iterations as the unrolled launch schedule instead of graph WHILE loops "
+                         "(per-kernel profilers do not profile kernels of graphs with conditional nodes)")
     ap.add_argument("--workload", choices=["mono", "bayer", "roi", "flow"], default="mono",
                     help="mono: the headline 1280x960 sequence; bayer: raw RGGB 3096x2080 frames; "
                          "roi: uneven-ROI crops (--frames crops)")
@@ -269,6 +272,7 @@ def main():
     opts = C.default_options(method=C.IC, maxlevel=4, max_iterations=50, epsx=0.01, minimum_image_size=16,
                              min_rho=0.8)
     reg = C.c_ecch(opts)
+    reg.set_level_loops(not args.unrolled_schedule)
     reg.set_reference_image(ref, scale=SCALE)
     acc = C.c_weigthed_average(WIDTH, HEIGHT)
     passes = [C.AFFINE, C.HOMOGRAPHY]
@@ -503,6 +507,7 @@ def main_bayer(args, ws, rank, local):
     opts = C.default_options(method=C.IC, maxlevel=4, max_iterations=50, epsx=0.01, minimum_image_size=16,
                              min_rho=0.8)
     reg = C.c_ecch(opts)
+    reg.set_level_loops(not args.unrolled_schedule)
     reg.set_reference_image(ref_bin.astype(np.float32), scale=BAYER_SCALE)
     accs = [C.c_weigthed_average(pw, ph) for _ in range(4)]
     passes = [C.TRANSLATION]

@@ -285,6 +285,14 @@ int sst_stack_bayer_frames(sst_ecch * reg, sst_weighted_average * const * acc, c
 /* Frames per chunk used by sst_stack_frames (default 256). */
 int sst_set_chunk_frames(sst_ecch * h, int frames);
 
+/* Level iterations as CUDA graph WHILE loops (enable = 1, the default): each
+ * pyramid level runs only the Gauss-Newton iterations some frame still needs.
+ * enable = 0 selects the unrolled schedule (max_iterations + 1 pass / solve
+ * launches per level, empty ones exit at once); the results are identical.
+ * Kernel profilers do not profile single kernels of graphs that hold
+ * conditional nodes, so per-kernel profiles use the unrolled schedule. */
+int sst_ecch_set_level_loops(sst_ecch * h, int enable);
+
 /* Number of kernels the library launched since the last call of this
  * function (graph replays count every kernel node they run). */
 long long sst_kernel_launch_count(int reset);

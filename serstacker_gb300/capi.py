@@ -79,6 +79,7 @@ def lib():
             "sst_ecch_align_batch": (i, [p, p, i, i, i, i, sz, sz, d, i, i, p, i, p, p, p, p, p, p, p]),
             "sst_ecch_align_plain": (i, [p, p, i, i, i, i, sz, sz, d, i, i, p, i, p, p, p, p, p, p, p]),
             "sst_set_chunk_frames": (i, [p, i]),
+            "sst_ecch_set_level_loops": (i, [p, i]),
             "sst_ecch_level_stats": (i, [p, i, i, p, p, p]),
             "sst_ecch_reference_image": (i, [p, i, p, i]),
             "sst_ecch_current_image": (i, [p, i, i, p, i]),
@@ -218,6 +219,10 @@ class c_ecch:
 
     def set_chunk_frames(self, n: int):
         _check(lib().sst_set_chunk_frames(self._h, n), "set_chunk_frames")
+
+    def set_level_loops(self, enable: bool):
+        """Level iterations as graph WHILE loops (default) or the unrolled schedule."""
+        _check(lib().sst_ecch_set_level_loops(self._h, 1 if enable else 0), "set_level_loops")
 
     def level_stats(self, pass_index: int, level: int):
         """(ms, frame_iterations, algorithmic_bytes) of the last call at one pass / level."""

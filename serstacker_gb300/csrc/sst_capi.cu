@@ -173,6 +173,7 @@ struct sst_ecch {
   DevBuf err;                        // device flag: a bounded wait for a staged tile gave up
   DevBuf loopst;                     // per pass and level: loop cursor and the two list counts
   int loops_ok = 1;                  // graph WHILE loops usable (cleared when building one fails)
+  bool loops_enabled = true;         // sst_ecch_set_level_loops
   size_t part_stride = 0;
   int steps_cap = 0;
   int lap_t = 0;
@@ -281,6 +282,13 @@ extern "C" int sst_set_chunk_frames(sst_ecch * h, int frames)
 {
   if( !h || frames < 1 ) return set_error(SST_ERR_INVALID_ARG, "invalid chunk size");
   h->chunk = frames;
+  return SST_OK;
+}
+
+extern "C" int sst_ecch_set_level_loops(sst_ecch * h, int enable)
+{
+  if( !h ) return set_error(SST_ERR_INVALID_ARG, "NULL engine");
+  h->loops_enabled = enable != 0;
   return SST_OK;
 }
 
@@ -828,7 +836,8 @@ static int register_device(sst_ecch * h, const void * d_frames, int depth, int n
     SST_TRY(enqueue_schedule(h, n, method, num_passes, passes, init_states_host != nullptr, true, &kk));
   }
   else {
-    std::vector<long long> key = { n, method, num_passes, init_states_host ? 1 : 0, h->o.max_iterations };
+    const bool want_loops = h->loops_ok && h->loops_enabled;
+    std::vector<long long> key = { n, method, num_passes, init_states_host ? 1 : 0, h->o.max_iterations, want_loops };
     for( int k = 0; k < num_passes; ++k ) {
       key.push_back(passes[k].type);
       key.push_back(passes[k].fix_scale);
@@ -838,10 +847,10 @@ static int register_device(sst_ecch * h, const void * d_frames, int depth, int n
     if( !ge ) {
       // levels as graph WHILE loops (no launches for iterations no frame needs);
       // the unrolled schedule when such a graph cannot be built
-      if( h->loops_ok ) SST_CK(h->loopst.ensure((size_t) 3 * 32 * 4 * sizeof(int)));
+      if( want_loops ) SST_CK(h->loopst.ensure((size_t) 3 * 32 * 4 * sizeof(int)));
       GraphEntry g;
       g.key = key;
-      for( int attempt = h->loops_ok ? 0 : 1; attempt < 2; ++attempt ) {
+      for( int attempt = want_loops ? 0 : 1; attempt < 2; ++attempt ) {
         const bool loops = attempt == 0;
         cudaGraph_t graph = nullptr;
         SST_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));

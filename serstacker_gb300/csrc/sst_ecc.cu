@@ -740,7 +740,8 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
         }
         const float4 * tgp = a.refTG + (size_t) y0r * a.w + x;
         float tr = (float) (threadIdx.x >> 7);
-#pragma unroll 4
+        // the projective loop keeps fewer samples in flight (registers)
+#pragma unroll (FAM == FAM_AFFINE ? 4 : 2)
         for( int y = y0r; y < yend; y += 2, tr += 2.f, tgp += 2 * a.w ) {
           float X, Y;
           if( FAM == FAM_AFFINE ) {

@@ -113,6 +113,27 @@ def test_batch_equals_plain_bitwise(gpu):
         assert np.array_equal(a["params"][2:4], c["params"]), method
 
 
+def test_level_loops_equal_unrolled_schedule_bitwise(gpu):
+    """Graph WHILE loops per level against the unrolled launch schedule: the
+    same results and the same per-level frame-iteration counts, bit for bit,
+    for every method and a two-pass run."""
+    C = gpu
+    w, h, n = 160, 128, 6
+    ref, frames, _ = _sequence(n, w, h, seed=5)
+    for method, passes in ((1, [3, 4]), (3, [3]), (0, [3]), (2, [6])):
+        out, its = [], []
+        for loops in (True, False):
+            reg = C.c_ecch(C.default_options(method=method, maxlevel=3, max_iterations=30, epsx=0.01,
+                                             minimum_image_size=16))
+            reg.set_level_loops(loops)
+            reg.set_reference_image(ref.astype(np.float32))
+            out.append(reg.align(frames, passes))
+            its.append([reg.level_stats(k, l)[1] for k in range(len(passes)) for l in range(reg.num_levels())])
+        for key in ("params", "iterations", "status"):
+            assert np.array_equal(out[0][key], out[1][key]), (method, key)
+        assert its[0] == its[1], (method, its)
+
+
 @pytest.mark.parametrize("data", ["scene", "noise"])
 def test_stack_matches_fp64(gpu, oracle, data):
     """Batched warp + weighted stack vs FP64 sums with the same parameters.
