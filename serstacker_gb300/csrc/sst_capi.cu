@@ -510,10 +510,19 @@ static cudaError_t record_prof(cudaEvent_t e, cudaStream_t st, bool host_driven)
   return host_driven ? cudaEventRecord(e, st) : cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
 }
 
+/* tile width of the staged IC / IC-LM pass at a level: 64 on levels at most
+ * 384 px wide (fewer idle columns in the last tile), PW_TX otherwise */
+static int pointwise_tile_w(const sst_ecch * h, int l)
+{
+  return h->lw[l] <= 384 ? 64 : PW_TX;
+}
+
+/* tiles of a level's pass; for IC / IC-LM the staged pass's tiling, which has at
+ * least as many tiles as the PW_TX-wide one of the unstaged pass */
 static int level_tiles(const sst_ecch * h, int l, int method, int * tiles_x)
 {
   if( method == M_FA || method == M_LM ) return tiles_of(h->lw[l], h->lh[l], ST_TX, ST_TY, tiles_x);
-  return tiles_of(h->lw[l], h->lh[l], PW_TX, PW_TY, tiles_x);
+  return tiles_of(h->lw[l], h->lh[l], pointwise_tile_w(h, l), PW_TY, tiles_x);
 }
 
 static int ensure_capacity(sst_ecch * h, int n, int method, int num_passes, const sst_motion_model * passes)
@@ -673,10 +682,16 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
       a.max_it = max_it;
       a.scale_next = l > 0 ? (double) h->lw[l - 1] / (double) h->lw[l] : 0.0;
       a.err = h->err.as<int>();
-      // IC / IC-LM: the level of every frame slot as a TMA tensor (footprints staged in shared memory)
+      // IC / IC-LM: the level of every frame slot as a TMA tensor (footprints staged in shared
+      // memory); the unstaged pass keeps PW_TX-wide tiles
       CUtensorMap map;
+      const int tw = pointwise_tile_w(h, l);
       const bool staged = (method == M_IC || method == M_ICLM) &&
-          encode_pass_level(h->pyr.as<float>() + h->loff[l], h->lw[l], h->lh[l], h->pyr_px, h->cap, &map);
+          encode_pass_level(h->pyr.as<float>() + h->loff[l], h->lw[l], h->lh[l], h->pyr_px, h->cap, &map, tw);
+      if( method == M_IC || method == M_ICLM ) {
+        a.tile_w = staged ? tw : PW_TX;
+        a.tiles = tiles_of(h->lw[l], h->lh[l], a.tile_w, PW_TY, &a.tiles_x);
+      }
       if( loops ) {
         a.list_in = lists + (size_t) step * h->cap;
         a.count_in = lp + 1;

@@ -573,23 +573,24 @@ struct ItemPlan {
  * the plan waits on no memory: the item's frame f and, in lane l, coefficient
  * l & 15 of that frame. Writes the coefficients (s_c) and whether the item's
  * footprint is staged. */
-template<int METHOD, int FAM>
+template<int METHOD, int FAM, int TXS>
 __device__ __forceinline__ void plan_item(const PassArgs & a, int item, int f, float cl, float * s_c, ItemPlan * plan)
 {
+  constexpr int BW = TXS + 16;
   const int lane = threadIdx.x & 31;
   const int t = item - (item / a.tiles) * a.tiles;
   float c[16];
 #pragma unroll
   for( int i = 0; i < 16; ++i ) c[i] = __shfl_sync(0xffffffffu, cl, i);
   if( lane < 16 ) s_c[lane] = cl;
-  const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
-  const int tx1 = min(tx0 + PW_TX, a.w) - 1, ty1 = min(ty0 + PW_TY, a.h) - 1;
+  const int tx0 = (t % a.tiles_x) * TXS, ty0 = (t / a.tiles_x) * PW_TY;
+  const int tx1 = min(tx0 + TXS, a.w) - 1, ty1 = min(ty0 + PW_TY, a.h) - 1;
   int bx0, by0, bx1, by1;
   bool use = rect_footprint<FAM>(c, tx0, ty0, tx1, ty1, a.w, a.h, bx0, by0, bx1, by1);
   use = use && (METHOD == M_IC || !a.refM);
   if( use ) {
     bx0 = bx0 >= 0 ? bx0 & ~3 : -((-bx0 + 3) & ~3);
-    use = bx1 < bx0 + PB_W && by1 < by0 + PB_H;
+    use = bx1 < bx0 + BW && by1 < by0 + PB_H;
   }
   if( lane == 0 ) {
     plan->f = f, plan->t = t;
@@ -623,11 +624,14 @@ __device__ __forceinline__ void store_item_sums(const PassArgs & a, int f, int t
  * the gathers become shared-memory loads with no address arithmetic in
  * 64 bits, and the next item's copy is in flight while this one computes.
  * Items whose taps leave the level or the box take the global path. */
-template<int METHOD, int FAM, int JK, int M>
+template<int METHOD, int FAM, int JK, int M, int TXS>
 __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const __grid_constant__ CUtensorMap tmap)
 {
   constexpr int NS = M + 2;
   constexpr int NP = column_sums<JK, M>::N;
+  constexpr int PB_W = TXS + 16;                    // footprint box width (tile + 16 px)
+  constexpr int RS = 256 / TXS;                     // rows between a thread's samples
+  constexpr int RSH = TXS == 128 ? 7 : 6;           // log2 TXS
   __shared__ __align__(128) float s_box[2][PB_H * PB_W];
   __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ float s_red[2][8 * NS];     // warp sums of the current and the previous item
@@ -653,7 +657,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
   if( threadIdx.x < 32 ) {
     const int lane = threadIdx.x & 31;
     const int f0 = item_frame(a, blockIdx.x, nitems);
-    plan_item<METHOD, FAM>(a, blockIdx.x, f0, __ldcg(a.fs[f0].wc + (lane & 15)), s_c[0], &s_plan[0]);
+    plan_item<METHOD, FAM, TXS>(a, blockIdx.x, f0, __ldcg(a.fs[f0].wc + (lane & 15)), s_c[0], &s_plan[0]);
     f1 = item_frame(a, blockIdx.x + gridDim.x, nitems);
     c1 = __ldcg(a.fs[f1].wc + (lane & 15));
     f2 = item_frame(a, blockIdx.x + 2 * gridDim.x, nitems);
@@ -672,7 +676,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
     const int nitem = item + gridDim.x;
     const int nslot = slot == 2 ? 0 : slot + 1;
     if( threadIdx.x < 32 && nitem < nitems ) {
-      plan_item<METHOD, FAM>(a, nitem, f1, c1, s_c[nslot], &s_plan[nslot]);
+      plan_item<METHOD, FAM, TXS>(a, nitem, f1, c1, s_c[nslot], &s_plan[nslot]);
       if( nitem + gridDim.x < nitems ) c1 = __ldcg(a.fs[f2].wc + (threadIdx.x & 15));
       f1 = f2;
       f2 = item_frame(a, nitem + 2 * gridDim.x, nitems);
@@ -699,8 +703,8 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
     slot = nslot;
     const int f = pl.f, t = pl.t;
     const float * img = a.pyr + (size_t) f * a.pyr_stride + a.lvl_off;
-    const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
-    const int x = tx0 + (threadIdx.x & (PW_TX - 1));
+    const int tx0 = (t % a.tiles_x) * TXS, ty0 = (t / a.tiles_x) * PW_TY;
+    const int x = tx0 + (threadIdx.x & (TXS - 1));
     const int yend = min(ty0 + PW_TY, a.h);
     float P[NP], rr = 0.f, cnt = 0.f;
 #pragma unroll
@@ -711,8 +715,8 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
       phases ^= 1u << b;
       if( x < a.w ) {
         const float * box = s_box[b];
-        const int y0r = ty0 + (threadIdx.x >> 7);
-        if( y0r < yend ) cnt = (float) ((yend - 1 - y0r) / 2 + 1);
+        const int y0r = ty0 + (threadIdx.x >> RSH);
+        if( y0r < yend ) cnt = (float) ((yend - 1 - y0r) / RS + 1);
         // The column's sample positions as functions of the tile-local row tr = y - ty0,
         // in box coordinates: (Kx, Ky) is the integer offset of (x + Ix, ty0 + Iy) from
         // the box origin, the warp's displacement is added to it. Box coordinates are
@@ -739,10 +743,10 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
           e5 = c[7], e6 = -c[7];
         }
         const float4 * tgp = a.refTG + (size_t) y0r * a.w + x;
-        float tr = (float) (threadIdx.x >> 7);
+        float tr = (float) (threadIdx.x >> RSH);
         // the projective loop keeps fewer samples in flight (registers)
 #pragma unroll (FAM == FAM_AFFINE ? 4 : 2)
-        for( int y = y0r; y < yend; y += 2, tr += 2.f, tgp += 2 * a.w ) {
+        for( int y = y0r; y < yend; y += RS, tr += (float) RS, tgp += RS * a.w ) {
           float X, Y;
           if( FAM == FAM_AFFINE ) {
             X = fmaf(c[1], tr, e0);
@@ -775,7 +779,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
       }
     }
     else {
-      const int xs0 = tx0 + (threadIdx.x & (PW_TX - 1) & ~31);
+      const int xs0 = tx0 + (threadIdx.x & (TXS - 1) & ~31);
       const int xs1 = min(xs0 + 31, a.w - 1);
       for( int yc = ty0; yc < yend; yc += 16 ) {
         const int yc1 = min(yc + 15, yend - 1);
@@ -783,14 +787,14 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
             rect_interior<FAM>(c, xs0, yc, xs1, yc1, a.w, a.h);
         if( x >= a.w ) continue;
         if( interior ) {
-          const int y0r = yc + (threadIdx.x >> 7);
-          if( y0r <= yc1 ) cnt += (float) ((yc1 - y0r) / 2 + 1);
+          const int y0r = yc + (threadIdx.x >> RSH);
+          if( y0r <= yc1 ) cnt += (float) ((yc1 - y0r) / RS + 1);
           const int xI = x + (int) c[12], yI = (int) c[13];
           const float fx = (float) x;
           const float4 * tgp = a.refTG + (size_t) y0r * a.w + x;
           float fy = (float) y0r;
 #pragma unroll 4
-          for( int y = y0r; y <= yc1; y += 2, fy += 2.f, tgp += 2 * a.w ) {
+          for( int y = y0r; y <= yc1; y += RS, fy += (float) RS, tgp += RS * a.w ) {
             float dx, dy;
             warp_disp<FAM>(c, fx, fy, dx, dy);
             const float flx = floorf(dx), fly = floorf(dy);
@@ -810,7 +814,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
         }
         else {
 #pragma unroll 2
-          for( int y = yc + (threadIdx.x >> 7); y <= yc1; y += 2 ) {
+          for( int y = yc + (threadIdx.x >> RSH); y <= yc1; y += RS ) {
             const spos s = warp_pos<FAM>(c, x, y);
             const size_t i = (size_t) y * a.w + x;
             bool ok;
@@ -1129,9 +1133,16 @@ static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st, const
 {
   if constexpr( METHOD == M_IC || METHOD == M_ICLM ) {
     if( map && FAM != FAM_QUAD ) {
-      static int g = 0;
-      if( !g ) g = persistent_grid(k_pass_pointwise_tma<METHOD, FAM, JK, M>);
-      k_pass_pointwise_tma<METHOD, FAM, JK, M><<<grid > 0 ? grid : g, 256, 0, st>>>(a, *map);
+      if( a.tile_w == 64 ) {
+        static int g = 0;
+        if( !g ) g = persistent_grid(k_pass_pointwise_tma<METHOD, FAM, JK, M, 64>);
+        k_pass_pointwise_tma<METHOD, FAM, JK, M, 64><<<grid > 0 ? grid : g, 256, 0, st>>>(a, *map);
+      }
+      else {
+        static int g = 0;
+        if( !g ) g = persistent_grid(k_pass_pointwise_tma<METHOD, FAM, JK, M, PW_TX>);
+        k_pass_pointwise_tma<METHOD, FAM, JK, M, PW_TX><<<grid > 0 ? grid : g, 256, 0, st>>>(a, *map);
+      }
       return cudaGetLastError();
     }
     static int g = 0;
@@ -1190,11 +1201,12 @@ cudaError_t launch_pass(int method, const PassArgs & a, int grid, cudaStream_t s
 /* the pyramid level of every frame slot as a 3-D tensor (x, y, frame) with
  * the pointwise footprint box; false when the level's layout breaks the TMA
  * rules (row and frame strides multiples of 16 bytes, aligned base) */
-bool encode_pass_level(const float * level0_of_slot0, int w, int h, size_t pyr_stride, int frames, CUtensorMap * map)
+bool encode_pass_level(const float * level0_of_slot0, int w, int h, size_t pyr_stride, int frames, CUtensorMap * map,
+    int tile_w)
 {
   const uint64_t dims[3] = { (uint64_t) w, (uint64_t) h, (uint64_t) frames };
   const uint64_t strides[2] = { (uint64_t) w * sizeof(float), (uint64_t) pyr_stride * sizeof(float) };
-  const uint32_t box[3] = { (uint32_t) PB_W, (uint32_t) PB_H, 1 };
+  const uint32_t box[3] = { (uint32_t) (tile_w + 16), (uint32_t) PB_H, 1 };
   return encode_tensor_3d(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, level0_of_slot0, dims, strides, box);
 }
 

@@ -122,6 +122,7 @@ struct PassArgs {
   const int * tile_prefix;  // per entry of list_in: tiles of the entries before it (k_roi_scan)
   const int * tile_total;   // tiles of the whole list
   int * err;                // set to 1 when a bounded wait for a staged tile gave up
+  int tile_w;               // staged IC / IC-LM pass: tile width (PW_TX, or 64 on narrow levels)
 };
 
 /* pointwise passes (IC, IC-LM, correlation): 128 x 32 pixel tiles, 256 threads */
@@ -137,7 +138,8 @@ inline int tiles_of(int w, int h, int tx, int ty, int * tiles_x)
 
 /* kernel launchers (defined in the .cu files) */
 cudaError_t launch_pass(int method, const PassArgs & a, int grid, cudaStream_t st, const CUtensorMap * map = nullptr);
-bool encode_pass_level(const float * level_of_slot0, int w, int h, size_t pyr_stride, int frames, CUtensorMap * map);
+bool encode_pass_level(const float * level_of_slot0, int w, int h, size_t pyr_stride, int frames, CUtensorMap * map,
+    int tile_w = PW_TX);
 __host__ __device__ int pass_num_sums(int method, int M);
 cudaError_t launch_solve(int method, const PassArgs & a, int grid, cudaStream_t st);
 
