@@ -1487,16 +1487,17 @@ __global__ void __launch_bounds__(256) k_correlation_finish(CorrArgs a)
  * batches): same structure as the staged IC pass; items whose taps leave
  * the level or the box, or with a reference mask, take the global path. */
 template<int FAM>
-__device__ __forceinline__ void plan_corr_item(const CorrArgs & a, int item, float * s_c, ItemPlan * plan)
+__device__ __forceinline__ void plan_corr_item(const CorrArgs & a, int item, int status, float cl, float * s_c,
+    ItemPlan * plan)
 {
+  // values loaded an item earlier: the frame's status and, in lane l, its coefficient l & 15
   const int lane = threadIdx.x & 31;
   const int f = item / a.tiles, t = item - f * a.tiles;
-  const FrameState * F = a.fs + f;
-  const bool live = F->status == SST_FRAME_OK;
+  const bool live = status == SST_FRAME_OK;
   float c[16];
 #pragma unroll
-  for( int i = 0; i < 16; ++i ) c[i] = __ldcg(F->wc + i);
-  if( lane < 16 ) s_c[lane] = __ldcg(F->wc + lane);
+  for( int i = 0; i < 16; ++i ) c[i] = __shfl_sync(0xffffffffu, cl, i);
+  if( lane < 16 ) s_c[lane] = cl;
   const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
   const int tx1 = min(tx0 + PW_TX, a.w) - 1, ty1 = min(ty0 + PW_TY, a.h) - 1;
   int bx0, by0, bx1, by1;
@@ -1519,8 +1520,7 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
   constexpr int NS = 6;
   __shared__ __align__(128) float s_box[2][PB_H * PB_W];
   __shared__ __align__(8) uint64_t s_bar[2];
-  __shared__ float s_red[8 * NS];
-  __shared__ double s_tile[NS];
+  __shared__ float s_red[2][8 * NS];     // warp sums of the current and the previous item
   __shared__ float s_c[3][16];
   __shared__ ItemPlan s_plan[3];
   __shared__ uint32_t s_infl;             // copies in flight, kept by thread 0
@@ -1534,7 +1534,19 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
     s_gaveup[0] = s_gaveup[1] = 0;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  if( threadIdx.x < 32 ) plan_corr_item<FAM>(a, blockIdx.x, s_c[0], &s_plan[0]);
+  // warp 0 keeps the next item's frame status and lane coefficient in flight
+  int st1 = 0;
+  float c1 = 0.f;
+  if( threadIdx.x < 32 ) {
+    const int lane = threadIdx.x & 31;
+    const FrameState * F0 = a.fs + blockIdx.x / a.tiles;
+    plan_corr_item<FAM>(a, blockIdx.x, __ldcg(&F0->status), __ldcg(F0->wc + (lane & 15)), s_c[0], &s_plan[0]);
+    const int it1 = blockIdx.x + gridDim.x;
+    if( it1 < nitems ) {
+      const FrameState * F1 = a.fs + it1 / a.tiles;
+      st1 = __ldcg(&F1->status), c1 = __ldcg(F1->wc + (lane & 15));
+    }
+  }
   __syncthreads();
   if( threadIdx.x == 0 && s_plan[0].use ) {
     mbar_expect_tx(&s_bar[0], PB_W * PB_H * sizeof(float));
@@ -1544,10 +1556,20 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
   uint32_t phases = 0u;
   bool timed_out = false, stop = false;
   int slot = 0, b = 0;
+  int pf = -1, pt = 0;                              // previous item (its sums wait in s_red[b ^ 1])
   for( int item = blockIdx.x; item < nitems; item += gridDim.x, b ^= 1 ) {
     const int nitem = item + gridDim.x;
     const int nslot = slot == 2 ? 0 : slot + 1;
-    if( threadIdx.x < 32 && nitem < nitems ) plan_corr_item<FAM>(a, nitem, s_c[nslot], &s_plan[nslot]);
+    if( threadIdx.x < 32 && nitem < nitems ) {
+      plan_corr_item<FAM>(a, nitem, st1, c1, s_c[nslot], &s_plan[nslot]);
+      const int it2 = nitem + gridDim.x;
+      if( it2 < nitems ) {
+        const FrameState * F2 = a.fs + it2 / a.tiles;
+        st1 = __ldcg(&F2->status), c1 = __ldcg(F2->wc + (threadIdx.x & 15));
+      }
+    }
+    // orders: the next plan; the previous item's warp sums; the previous item's
+    // reads of the box buffer that the next copy overwrites
     __syncthreads();
     // once a wait gave up no further copy is issued or consumed; the previous item's
     // flag is read after the barrier and written again no earlier than the next item,
@@ -1559,7 +1581,18 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
       tma_load_3d(s_box[b ^ 1], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, s_plan[nslot].f, &s_bar[b ^ 1]);
       inflight_issued(&s_infl, b ^ 1, (phases >> (b ^ 1)) & 1u);
     }
+    if( pf >= 0 && (threadIdx.x >> 5) == 1 ) {
+      // FP64 sum, in warp order, of the previous item's 8 warp sums: its tile partials
+      const int lane = threadIdx.x & 31;
+      if( lane < NS ) {
+        double sum = 0;
+#pragma unroll
+        for( int wv = 0; wv < 8; ++wv ) sum += (double) s_red[b ^ 1][wv * NS + lane];
+        a.partials[(size_t) pf * a.part_stride + (size_t) pt * NS + lane] = sum;
+      }
+    }
     const ItemPlan pl = s_plan[slot];
+    pf = pl.f, pt = pl.t;
     float c[16];
 #pragma unroll
     for( int i = 0; i < 16; ++i ) c[i] = s_c[slot][i];
@@ -1643,8 +1676,17 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
         }
       }
     }
-    block_reduce_d<NS>(acc, s_red, s_tile);
-    write_tile_at<NS>(a.partials + (size_t) f * a.part_stride, t, s_tile);
+    warp_sums_to<NS>(acc, &s_red[b][(threadIdx.x >> 5) * NS]);
+  }
+  __syncthreads();
+  if( pf >= 0 && (threadIdx.x >> 5) == 1 ) {
+    const int lane = threadIdx.x & 31;
+    if( lane < NS ) {
+      double sum = 0;
+#pragma unroll
+      for( int wv = 0; wv < 8; ++wv ) sum += (double) s_red[b ^ 1][wv * NS + lane];
+      a.partials[(size_t) pf * a.part_stride + (size_t) pt * NS + lane] = sum;
+    }
   }
   if( threadIdx.x == 0 ) inflight_drain(&s_infl, s_bar);
   if( timed_out && a.err ) atomicExch(a.err, 1);
