@@ -624,8 +624,9 @@ __device__ __forceinline__ void store_item_sums(const PassArgs & a, int f, int t
  * the gathers become shared-memory loads with no address arithmetic in
  * 64 bits, and the next item's copy is in flight while this one computes.
  * Items whose taps leave the level or the box take the global path. */
+// (the projective pass needs more registers per thread: three CTAs per SM)
 template<int METHOD, int FAM, int JK, int M, int TXS>
-__global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const __grid_constant__ CUtensorMap tmap)
+__global__ void __launch_bounds__(256, FAM == FAM_HOMOG ? 3 : 4) k_pass_pointwise_tma(PassArgs a, const __grid_constant__ CUtensorMap tmap)
 {
   constexpr int NS = M + 2;
   constexpr int NP = column_sums<JK, M>::N;
@@ -744,8 +745,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_pointwise_tma(PassArgs a, const
         }
         const float4 * tgp = a.refTG + (size_t) y0r * a.w + x;
         float tr = (float) (threadIdx.x >> RSH);
-        // the projective loop keeps fewer samples in flight (registers)
-#pragma unroll (FAM == FAM_AFFINE ? 4 : 2)
+#pragma unroll 4
         for( int y = y0r; y < yend; y += RS, tr += (float) RS, tgp += RS * a.w ) {
           float X, Y;
           if( FAM == FAM_AFFINE ) {
