@@ -565,7 +565,8 @@ constexpr int PB_W = 144, PB_H = 40;
 
 struct ItemPlan {
   int f, t;         // frame and tile of the item
-  int use;          // 1: every tap inside the level and inside the staged box
+  int use;          // 1: the footprint box is staged (every tap of the tile lies in it)
+  int inside;       // 1: every tap inside the level as well (no per-pixel border test)
   int bx0, by0;     // box origin in the level
 };
 
@@ -586,7 +587,8 @@ __device__ __forceinline__ void plan_item(const PassArgs & a, int item, int f, f
   const int tx0 = (t % a.tiles_x) * TXS, ty0 = (t / a.tiles_x) * PW_TY;
   const int tx1 = min(tx0 + TXS, a.w) - 1, ty1 = min(ty0 + PW_TY, a.h) - 1;
   int bx0, by0, bx1, by1;
-  bool use = rect_footprint<FAM>(c, tx0, ty0, tx1, ty1, a.w, a.h, bx0, by0, bx1, by1);
+  bool inside;
+  bool use = rect_box<FAM>(c, tx0, ty0, tx1, ty1, a.w, a.h, bx0, by0, bx1, by1, inside);
   use = use && (METHOD == M_IC || !a.refM);
   if( use ) {
     bx0 = bx0 >= 0 ? bx0 & ~3 : -((-bx0 + 3) & ~3);
@@ -595,6 +597,7 @@ __device__ __forceinline__ void plan_item(const PassArgs & a, int item, int f, f
   if( lane == 0 ) {
     plan->f = f, plan->t = t;
     plan->use = use ? 1 : 0;
+    plan->inside = inside ? 1 : 0;
     plan->bx0 = bx0, plan->by0 = by0;
   }
 }
@@ -717,7 +720,6 @@ __global__ void __launch_bounds__(256, FAM == FAM_HOMOG ? 3 : 4) k_pass_pointwis
       if( x < a.w ) {
         const float * box = s_box[b];
         const int y0r = ty0 + (threadIdx.x >> RSH);
-        if( y0r < yend ) cnt = (float) ((yend - 1 - y0r) / RS + 1);
         // The column's sample positions as functions of the tile-local row tr = y - ty0,
         // in box coordinates: (Kx, Ky) is the integer offset of (x + Ix, ty0 + Iy) from
         // the box origin, the warp's displacement is added to it. Box coordinates are
@@ -745,6 +747,8 @@ __global__ void __launch_bounds__(256, FAM == FAM_HOMOG ? 3 : 4) k_pass_pointwis
         }
         const float4 * tgp = a.refTG + (size_t) y0r * a.w + x;
         float tr = (float) (threadIdx.x >> RSH);
+        if( pl.inside ) {
+          if( y0r < yend ) cnt = (float) ((yend - 1 - y0r) / RS + 1);
 #pragma unroll 4
         for( int y = y0r; y < yend; y += RS, tr += (float) RS, tgp += RS * a.w ) {
           float X, Y;
@@ -771,6 +775,55 @@ __global__ void __launch_bounds__(256, FAM == FAM_HOMOG ? 3 : 4) k_pass_pointwis
           if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(tr, u, P[2 < NP ? 2 : 0]);
           if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(tr, w, P[3 < NP ? 3 : 0]);
           if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(tr * tr, w, P[4 < NP ? 4 : 0]);
+        }
+        }
+        else {
+          // tile at the level's border: samples whose four taps lie inside the level
+          // read the box (full coverage, the same value as the global path); the
+          // others take the global path's validity test and border mode
+#pragma unroll 2
+          for( int y = y0r; y < yend; y += RS, tr += (float) RS, tgp += RS * a.w ) {
+            float X, Y;
+            if( FAM == FAM_AFFINE ) {
+              X = fmaf(c[1], tr, e0);
+              Y = fmaf(e2, tr, e1);
+            }
+            else {
+              const float iw = __fdividef(1.0f, fmaf(e5, tr, e0));
+              X = fmaf(fmaf(e2, tr, e1), iw, Kx);
+              Y = fmaf(fmaf(tr, fmaf(e6, tr, e4), e3), iw, Ky + tr);
+            }
+            const int ix = __float2int_rz(X), iy = __float2int_rz(Y);
+            float v;
+            bool ok;
+            if( (unsigned) (ix + pl.bx0) <= (unsigned) (a.w - 2) && (unsigned) (iy + pl.by0) <= (unsigned) (a.h - 2) ) {
+              const float ax = X - (float) ix, ay = Y - (float) iy;
+              const int o = (int) min((unsigned) (iy * PB_W + ix), (unsigned) (PB_W * PB_H - PB_W - 2));
+              const float v00 = box[o], v01 = box[o + 1], v10 = box[o + PB_W], v11 = box[o + PB_W + 1];
+              const float t0 = fmaf(ax, v01 - v00, v00), t1 = fmaf(ax, v11 - v10, v10);
+              v = fmaf(ay, t1 - t0, t0);
+              ok = true;
+            }
+            else {
+              const spos sp = warp_pos<FAM>(c, x, y);
+              if( METHOD == M_IC ) ok = mask_ok(coverage(a.w, a.h, sp), 250);
+              else {
+                int rx, ry;
+                warp_nearest<FAM>(c, x, y, rx, ry);
+                ok = rx >= 0 && rx < a.w && ry >= 0 && ry < a.h;
+              }
+              v = sample_replicate(img, a.w, a.h, sp);
+            }
+            const float4 tg = __ldg(tgp);
+            const float r = ok ? v - tg.x : 0.f;
+            const float u = tg.y * r, w = tg.z * r;
+            rr = fmaf(r, r, rr);
+            cnt += ok ? 1.f : 0.f;
+            P[0] += u, P[1] += w;
+            if( NP > 2 ) P[2 < NP ? 2 : 0] = fmaf(tr, u, P[2 < NP ? 2 : 0]);
+            if( NP > 3 ) P[3 < NP ? 3 : 0] = fmaf(tr, w, P[3 < NP ? 3 : 0]);
+            if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(tr * tr, w, P[4 < NP ? 4 : 0]);
+          }
         }
         // row moments about y = 0 from the moments about y = ty0
         if( NP > 4 ) P[4 < NP ? 4 : 0] = fmaf(fty0, fmaf(fty0, P[1], 2.0f * P[3 < NP ? 3 : 0]), P[4 < NP ? 4 : 0]);
@@ -1501,7 +1554,8 @@ __device__ __forceinline__ void plan_corr_item(const CorrArgs & a, int item, int
   const int tx0 = (t % a.tiles_x) * PW_TX, ty0 = (t / a.tiles_x) * PW_TY;
   const int tx1 = min(tx0 + PW_TX, a.w) - 1, ty1 = min(ty0 + PW_TY, a.h) - 1;
   int bx0, by0, bx1, by1;
-  bool use = rect_footprint<FAM>(c, tx0, ty0, tx1, ty1, a.w, a.h, bx0, by0, bx1, by1);
+  bool inside;
+  bool use = rect_box<FAM>(c, tx0, ty0, tx1, ty1, a.w, a.h, bx0, by0, bx1, by1, inside);
   use = use && live && !a.refM;
   if( use ) {
     bx0 = bx0 >= 0 ? bx0 & ~3 : -((-bx0 + 3) & ~3);
@@ -1510,6 +1564,7 @@ __device__ __forceinline__ void plan_corr_item(const CorrArgs & a, int item, int
   if( lane == 0 ) {
     plan->f = live ? f : -1, plan->t = t;
     plan->use = use ? 1 : 0;
+    plan->inside = inside ? 1 : 0;
     plan->bx0 = bx0, plan->by0 = by0;
   }
 }
@@ -1632,6 +1687,7 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
           e5 = c[7], e6 = -c[7];
         }
         float tr = (float) (threadIdx.x >> 7);
+        if( pl.inside ) {
 #pragma unroll 4
         for( int y = y0r; y < yend; y += 2, tr += 2.f ) {
           float X, Y;
@@ -1656,6 +1712,50 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
           acc[3] = fmaf(bv, bv, acc[3]);
           acc[4] = fmaf(av, bv, acc[4]);
           acc[5] += 1.f;
+        }
+        }
+        else {
+          // tile at the level's border: samples whose four taps lie inside the level
+          // read the box (full coverage, the same value as the global path); the
+          // others take the global path's coverage test and constant border
+#pragma unroll 2
+          for( int y = y0r; y < yend; y += 2, tr += 2.f ) {
+            float X, Y;
+            if( FAM == FAM_AFFINE ) {
+              X = fmaf(c[1], tr, e0);
+              Y = fmaf(e2, tr, e1);
+            }
+            else {
+              const float iw = __fdividef(1.0f, fmaf(e5, tr, e0));
+              X = fmaf(fmaf(e2, tr, e1), iw, Kx);
+              Y = fmaf(fmaf(tr, fmaf(e6, tr, e4), e3), iw, Ky + tr);
+            }
+            const int ix = __float2int_rz(X), iy = __float2int_rz(Y);
+            float v;
+            bool ok;
+            if( (unsigned) (ix + pl.bx0) <= (unsigned) (a.w - 2) && (unsigned) (iy + pl.by0) <= (unsigned) (a.h - 2) ) {
+              const float ax = X - (float) ix, ay = Y - (float) iy;
+              const int o = (int) min((unsigned) (iy * PB_W + ix), (unsigned) (PB_W * PB_H - PB_W - 2));
+              const float v00 = box[o], v01 = box[o + 1], v10 = box[o + PB_W], v11 = box[o + PB_W + 1];
+              const float t0 = fmaf(ax, v01 - v00, v00), t1 = fmaf(ax, v11 - v10, v10);
+              v = fmaf(ay, t1 - t0, t0);
+              ok = true;
+            }
+            else {
+              const spos sp = warp_pos<FAM>(c, x, y);
+              ok = mask_ok(coverage(a.w, a.h, sp), 254);
+              v = ok ? sample_constant0(img, a.w, a.h, sp) : 0.f;
+            }
+            if( ok ) {
+              const float av = __ldg(a.refT + (size_t) y * a.w + x) - a.tshift;
+              const float bv = v - a.tshift;
+              acc[0] += av, acc[1] += bv;
+              acc[2] = fmaf(av, av, acc[2]);
+              acc[3] = fmaf(bv, bv, acc[3]);
+              acc[4] = fmaf(av, bv, acc[4]);
+              acc[5] += 1.f;
+            }
+          }
         }
       }
     }

@@ -164,6 +164,50 @@ __device__ __forceinline__ bool rect_footprint(const float * __restrict__ c, int
   return ok;
 }
 
+/* Bounding box of the mapped corners of [x0, x1] x [y0, y1] (0.01 px margin),
+ * which holds every bilinear tap of the rectangle when the corners map to
+ * finite positions with w > 0 (the return value), whether or not they lie
+ * inside the w x h source; `inside` is rect_footprint's test (every tap
+ * inside the source). Warp-uniform results. */
+template<int FAM>
+__device__ __forceinline__ bool rect_box(const float * __restrict__ c, int x0, int y0, int x1, int y1, int w, int h,
+    int & bx0, int & by0, int & bx1, int & by1, bool & inside)
+{
+  inside = false;
+  if( FAM == FAM_QUAD ) return false;
+  const int lane = threadIdx.x & 31;
+  float X = 0.f, Y = 0.f;
+  bool ok = true, fin = true;
+  if( lane < 4 ) {
+    const int x = (lane & 1) ? x1 : x0, y = (lane & 2) ? y1 : y0;
+    float dx, dy;
+    warp_disp<FAM>(c, (float) x, (float) y, dx, dy);
+    X = (float) (x + (int) c[12]) + dx, Y = (float) (y + (int) c[13]) + dy;
+    ok = X >= 0.01f && X <= (float) (w - 2) - 0.01f && Y >= 0.01f && Y <= (float) (h - 2) - 0.01f;
+    fin = fabsf(X) < 1e6f && fabsf(Y) < 1e6f;
+    if( FAM == FAM_HOMOG ) {
+      const bool pos = (1.0f + fmaf(c[6], (float) x, c[7] * (float) y)) > 0.f;
+      ok = ok && pos, fin = fin && pos;
+    }
+  }
+  inside = __all_sync(0xffffffffu, ok);
+  const bool boxable = __all_sync(0xffffffffu, fin);
+  float mnx = X, mxx = X, mny = Y, mxy = Y;
+#pragma unroll
+  for( int k = 1; k < 4; ++k ) {
+    const float xs = __shfl_sync(0xffffffffu, X, k), ys = __shfl_sync(0xffffffffu, Y, k);
+    mnx = fminf(mnx, xs), mxx = fmaxf(mxx, xs), mny = fminf(mny, ys), mxy = fmaxf(mxy, ys);
+  }
+  mnx = __shfl_sync(0xffffffffu, mnx, 0), mxx = __shfl_sync(0xffffffffu, mxx, 0);
+  mny = __shfl_sync(0xffffffffu, mny, 0), mxy = __shfl_sync(0xffffffffu, mxy, 0);
+  if( boxable ) {
+    bx0 = (int) floorf(mnx - 0.01f), bx1 = (int) floorf(mxx + 0.01f) + 1;
+    by0 = (int) floorf(mny - 0.01f), by1 = (int) floorf(mxy + 0.01f) + 1;
+  }
+  else bx0 = by0 = bx1 = by1 = 0;
+  return boxable;
+}
+
 /* nearest source pixel of output pixel (x, y) (cvRound of the map, INTER_NEAREST) */
 template<int FAM>
 __device__ __forceinline__ void warp_nearest(const float * __restrict__ c, int x, int y, int & rx, int & ry)
