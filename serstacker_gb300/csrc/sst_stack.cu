@@ -349,12 +349,13 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
 {
   constexpr int VW = SA_TX + 4, VH = SA_TY + 4;
   constexpr int PPT = SA_TX * SA_TY / 256;
-  __shared__ __align__(128) T s_box[2][TB_H * TB_W];
-  __shared__ __align__(8) uint64_t s_bar[2];
-  // plans and coefficients rotate over three slots: frame f + 1 is planned
-  // while slower warps may still read frame f's slot
-  __shared__ __align__(16) float s_c[3][SST_NCOEF];
-  __shared__ TilePlan s_plan[3];
+  // three box buffers: frame f + 2's copy is issued while frame f computes;
+  // plans and coefficients rotate over four slots: frame f + 2 is planned while
+  // slower warps may still read frame f - 1's slot
+  __shared__ __align__(128) T s_box[3][TB_H * TB_W];
+  __shared__ __align__(8) uint64_t s_bar[3];
+  __shared__ __align__(16) float s_c[4][SST_NCOEF];
+  __shared__ TilePlan s_plan[4];
   __shared__ uint32_t s_infl;             // copies in flight, kept by thread 0
   __shared__ int s_gaveup[2];             // a wait gave up during a frame of this parity
   __shared__ uint8_t s_v[VH * VW];
@@ -378,38 +379,43 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
   if( threadIdx.x == 0 ) {
     mbar_init(&s_bar[0], 1);
     mbar_init(&s_bar[1], 1);
+    mbar_init(&s_bar[2], 1);
     s_infl = 0u;
     s_gaveup[0] = s_gaveup[1] = 0;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  // warp 0: frame f + 1's lane coefficient and weight, loaded during frame f - 1
-  float cl1 = 0.f, w1 = 0.f;
+  // warp 0: frame f + 2's lane coefficient and weight, loaded during frame f - 1
+  float cl2 = 0.f, w2 = 0.f;
   if( threadIdx.x < 32 && nf > 0 ) {
     const int lane = threadIdx.x & 15;
     plan_frame<FAM, T>(a, __ldg(a.coeffs + (size_t) f0 * SST_NCOEF + lane), __ldg(a.weights + f0), tx0, ty0, wx0, wy0,
         wx1, wy1, s_c[0], &s_plan[0]);
-    if( nf > 1 ) cl1 = __ldg(a.coeffs + (size_t) (f0 + 1) * SST_NCOEF + lane), w1 = __ldg(a.weights + f0 + 1);
+    if( nf > 1 )
+      plan_frame<FAM, T>(a, __ldg(a.coeffs + (size_t) (f0 + 1) * SST_NCOEF + lane), __ldg(a.weights + f0 + 1), tx0, ty0,
+          wx0, wy0, wx1, wy1, s_c[1], &s_plan[1]);
+    if( nf > 2 ) cl2 = __ldg(a.coeffs + (size_t) (f0 + 2) * SST_NCOEF + lane), w2 = __ldg(a.weights + f0 + 2);
   }
   __syncthreads();
-  if( threadIdx.x == 0 && nf > 0 && s_plan[0].use ) {
-    mbar_expect_tx(&s_bar[0], TB_W * TB_H * sizeof(T));
-    tma_load_3d(s_box[0], &tmap, s_plan[0].bx0, s_plan[0].by0, f0, &s_bar[0]);
-    inflight_issued(&s_infl, 0, 0u);
+  if( threadIdx.x == 0 ) {
+    for( int q = 0; q < 2 && q < nf; ++q ) {
+      if( !s_plan[q].use ) continue;
+      mbar_expect_tx(&s_bar[q], TB_W * TB_H * sizeof(T));
+      tma_load_3d(s_box[q], &tmap, s_plan[q].bx0, s_plan[q].by0, f0 + q, &s_bar[q]);
+      inflight_issued(&s_infl, q, 0u);
+    }
   }
   int since = 0;
   bool stop = false;
-  int slot = 0;                                   // frame f's plan slot (j mod 3)
   for( int j = 0; j < nf; ++j ) {
     const int f = f0 + j;
-    const int b = j & 1, nb = b ^ 1;
-    const int nslot = slot == 2 ? 0 : slot + 1;
-    // plan frame f + 1; its box buffer was last read during frame f - 1, which every
-    // thread has finished at the barrier below
-    if( threadIdx.x < 32 && j + 1 < nf ) {
-      plan_frame<FAM, T>(a, cl1, w1, tx0, ty0, wx0, wy0, wx1, wy1, s_c[nslot], &s_plan[nslot]);
-      if( j + 2 < nf ) {
-        cl1 = __ldg(a.coeffs + (size_t) (f + 2) * SST_NCOEF + (threadIdx.x & 15));
-        w1 = __ldg(a.weights + f + 2);
+    const int b = j % 3;                            // frame f's box buffer
+    const int slot = j & 3;                         // frame f's plan slot
+    // plan frame f + 2 (slot (j + 2) mod 4, last read during frame f - 2)
+    if( threadIdx.x < 32 && j + 2 < nf ) {
+      plan_frame<FAM, T>(a, cl2, w2, tx0, ty0, wx0, wy0, wx1, wy1, s_c[(j + 2) & 3], &s_plan[(j + 2) & 3]);
+      if( j + 3 < nf ) {
+        cl2 = __ldg(a.coeffs + (size_t) (f + 3) * SST_NCOEF + (threadIdx.x & 15));
+        w2 = __ldg(a.weights + f + 3);
       }
     }
     __syncthreads();
@@ -417,23 +423,25 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
     // is read after the barrier and written again no earlier than frame f + 1, so
     // every thread sees the same value
     stop = stop || s_gaveup[(j + 1) & 1];
-    if( threadIdx.x == 0 && j + 1 < nf && s_plan[nslot].use && !stop ) {
+    if( threadIdx.x == 0 && j + 2 < nf && s_plan[(j + 2) & 3].use && !stop ) {
+      // frame f + 2's box goes into the buffer frame f - 1 used: every thread has
+      // finished frame f - 1 at the barrier above
+      const int nb = (j + 2) % 3;
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // order the generic reads of frame f - 1 before the copy
       mbar_expect_tx(&s_bar[nb], TB_W * TB_H * sizeof(T));
-      tma_load_3d(s_box[nb], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, f + 1, &s_bar[nb]);
+      tma_load_3d(s_box[nb], &tmap, s_plan[(j + 2) & 3].bx0, s_plan[(j + 2) & 3].by0, f + 2, &s_bar[nb]);
       inflight_issued(&s_infl, nb, (phases >> nb) & 1u);
     }
     const TilePlan pl = s_plan[slot];
     float c[SST_NCOEF];
 #pragma unroll
     for( int i = 0; i < SST_NCOEF; ++i ) c[i] = s_c[slot][i];
-    slot = nslot;
     const float wf = pl.w;
     if( !(wf > 0.f) ) continue;                     // uniform over the CTA
     const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
     const bool staged = pl.use && !stop;
     if( staged ) {
-      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true, s_gaveup[b] = 1;
+      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true, s_gaveup[j & 1] = 1;
       else if( threadIdx.x == 0 ) inflight_landed(&s_infl, b);
       phases ^= 1u << b;
     }
@@ -583,7 +591,7 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
       since = 0;
     }
   }
-  if( threadIdx.x == 0 ) inflight_drain(&s_infl, s_bar);
+  if( threadIdx.x == 0 ) inflight_drain(&s_infl, s_bar, 3);
   if( timed_out && a.err ) atomicExch(a.err, 1);
   if( x < a.dw ) {
 #pragma unroll

@@ -48,14 +48,15 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t * bar, uint32_t parit
   return false;
 }
 
-/* Copies of a CTA's double buffer that the issuing thread started and has not
- * seen land, kept in one shared word by that thread alone: bit b = a copy into
- * buffer b is outstanding, bit 2 + b = the barrier parity it completes. A CTA
- * that gave up on a wait drains them (bounded again) before it exits, so no
- * copy writes into the shared memory of a finished CTA. */
+/* Copies of a CTA's multi-buffer (up to 8 buffers) that the issuing thread
+ * started and has not seen land, kept in one shared word by that thread
+ * alone: bit b = a copy into buffer b is outstanding, bit 8 + b = the barrier
+ * parity it completes. A CTA that gave up on a wait drains them (bounded
+ * again) before it exits, so no copy writes into the shared memory of a
+ * finished CTA. */
 __device__ __forceinline__ void inflight_issued(uint32_t * w, int b, uint32_t parity)
 {
-  *w = (*w & ~(5u << b)) | (1u << b) | (parity << (b + 2));
+  *w = (*w & ~(0x101u << b)) | (1u << b) | (parity << (b + 8));
 }
 
 __device__ __forceinline__ void inflight_landed(uint32_t * w, int b)
@@ -63,10 +64,10 @@ __device__ __forceinline__ void inflight_landed(uint32_t * w, int b)
   *w &= ~(1u << b);
 }
 
-__device__ __forceinline__ void inflight_drain(uint32_t * w, uint64_t * bars)
+__device__ __forceinline__ void inflight_drain(uint32_t * w, uint64_t * bars, int nbuf = 2)
 {
-  for( int b = 0; b < 2; ++b )
-    if( (*w >> b) & 1u ) mbar_wait_bounded(&bars[b], (*w >> (b + 2)) & 1u);
+  for( int b = 0; b < nbuf; ++b )
+    if( (*w >> b) & 1u ) mbar_wait_bounded(&bars[b], (*w >> (b + 8)) & 1u);
   *w = 0u;
 }
 
