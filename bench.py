@@ -222,7 +222,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--frames", type=int, default=2000)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--chunk", type=int, default=256, help="frames per streamed chunk in the e2e leg")
+    ap.add_argument("--chunk", type=int, default=512,
+                    help="frames per streamed chunk in the e2e leg (a quarter of it for the raw Bayer frames)")
     ap.add_argument("--ref-sample", type=int, default=6, help="frames per step of the --impl reference arm")
     ap.add_argument("--cpu-sample", type=int, default=160,
                     help="frames of the cpu_baseline sample (about 10 s of the oracle on 16 cores)")
@@ -572,7 +573,9 @@ def main_bayer(args, ws, rank, local):
         mask_host = torch.zeros((ph, pw), dtype=torch.uint8, pin_memory=True)
 
         def step_e2e():
-            step(host.data_ptr(), True, True, pinned, args.chunk)
+            # raw frames are 5x the mono frame: a quarter of the mono chunk keeps the
+            # first, unoverlapped copy short
+            step(host.data_ptr(), True, True, pinned, max(32, args.chunk // 4))
             for k, a in enumerate(accs):
                 C.lib().sst_weighted_average_compute(a.handle, avg_host[k].data_ptr(),
                                                      mask_host.data_ptr() if k == 0 else None, 0, None)

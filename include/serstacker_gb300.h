@@ -282,7 +282,8 @@ int sst_stack_bayer_frames(sst_ecch * reg, sst_weighted_average * const * acc, c
     int num_passes, const sst_motion_model * passes, int border, int weighting,
     float * params_out, int32_t * status_out, float * rho_out, float * weight_out, void * stream);
 
-/* Frames per chunk used by sst_stack_frames (default 256). */
+/* Frames per chunk used by sst_stack_frames (default 512): each chunk's host-to-device
+ * copy overlaps the previous chunk's registration and stacking. */
 int sst_set_chunk_frames(sst_ecch * h, int frames);
 
 /* Level iterations as CUDA graph WHILE loops (enable = 1, the default): each

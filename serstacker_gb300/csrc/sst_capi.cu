@@ -164,7 +164,7 @@ struct sst_ecch {
 
   // batch
   int cap = 0;
-  int chunk = 256;
+  int chunk = 512;
   DevBuf stage[2];
   DevBuf pyr, fs, part, cnt, lists, counts, lap, init;
   DevBuf out_params, out_status, out_iters, out_eps, out_rho, out_weight, weff, coeffs;
