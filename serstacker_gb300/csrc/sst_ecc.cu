@@ -1266,54 +1266,40 @@ bool encode_pass_level(const float * level0_of_slot0, int w, int h, size_t pyr_s
 /* ------------------------------------------------------ level / pass glue */
 
 /* c_ecch per-level align() prologue: reset the per-level solver state and
- * list every frame still registering (block-wide ordered compaction). */
-__global__ void k_level_begin(LevelBeginArgs a)
+ * list every frame still registering. One thread per frame over the whole
+ * grid (the FP64 state work spreads over the SMs); frames are appended with
+ * one atomic per warp, in no particular order (nothing depends on the order
+ * of an active list). *count_out is zero before the launch. */
+__global__ void __launch_bounds__(128) k_level_begin(LevelBeginArgs a)
 {
-  __shared__ int s_base;
-  __shared__ int s_warp[32];
-  if( threadIdx.x == 0 ) s_base = 0;
-  __syncthreads();
-  for( int f0 = 0; f0 < a.n; f0 += blockDim.x ) {
-    const int f = f0 + threadIdx.x;
-    bool alive = false;
-    if( f < a.n ) {
-      FrameState * F = a.fs + f;
-      alive = F->status == SST_FRAME_OK;
-      if( a.roi && a.roi[(size_t) f * a.lmax + a.level].w == 0 ) alive = false;   // no such level
-      F->n = 0;
-      F->phase = PH_START;
-      F->converged = 0;
-      F->level_ok = 0;
-      F->err = 0;
-      F->rmsold = FLT_MAX;
-      F->eps = FLT_MAX;
-      F->dpe = 0;
-      F->lambda = a.method == M_LM ? 0.1 : 0.001;
-      set_eval(F, a.model, F->state);
-    }
-    const unsigned b = __ballot_sync(0xffffffffu, alive);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if( lane == 0 ) s_warp[wid] = __popc(b);
-    __syncthreads();
-    if( threadIdx.x == 0 ) {
-      int run = s_base;
-      for( int w = 0; w < (int) (blockDim.x >> 5); ++w ) {
-        const int c = s_warp[w];
-        s_warp[w] = run;
-        run += c;
-      }
-      s_base = run;
-    }
-    __syncthreads();
-    if( alive ) a.list_out[s_warp[wid] + __popc(b & ((1u << lane) - 1u))] = f;
-    __syncthreads();
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  bool alive = false;
+  if( f < a.n ) {
+    FrameState * F = a.fs + f;
+    alive = F->status == SST_FRAME_OK;
+    if( a.roi && a.roi[(size_t) f * a.lmax + a.level].w == 0 ) alive = false;   // no such level
+    F->n = 0;
+    F->phase = PH_START;
+    F->converged = 0;
+    F->level_ok = 0;
+    F->err = 0;
+    F->rmsold = FLT_MAX;
+    F->eps = FLT_MAX;
+    F->dpe = 0;
+    F->lambda = a.method == M_LM ? 0.1 : 0.001;
+    set_eval(F, a.model, F->state);
   }
-  if( threadIdx.x == 0 ) *a.count_out = s_base;
+  const unsigned b = __ballot_sync(0xffffffffu, alive);
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if( lane == 0 && b ) base = atomicAdd(a.count_out, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if( alive ) a.list_out[base + __popc(b & ((1u << lane) - 1u))] = f;
 }
 
 cudaError_t launch_level_begin(const LevelBeginArgs & a, cudaStream_t st)
 {
-  k_level_begin<<<1, 1024, 0, st>>>(a);
+  k_level_begin<<<(unsigned) (a.n > 0 ? (a.n + 127) / 128 : 1), 128, 0, st>>>(a);
   return cudaGetLastError();
 }
 
