@@ -39,10 +39,17 @@ SCALE = 1.0 / 65535.0
 SEED = 1001
 
 
+# sst_stack_frames weighting modes
+WEIGHTING = {0: "unweighted", 1: "Laplacian-energy frame weights",
+             2: "focus-stacking per-pixel weights (6 lap^2 + |grad|^2)^2, Gaussian sigma 3",
+             3: "local-variance per-pixel weights (kradius 2, dscale 1, uscale 3)"}
+_weighting = 1
+
+
 def workload_cfg(frames: int):
     return {
         "workload": f"{frames} x {WIDTH}x{HEIGHT} u16 frames; c_ecch 4 levels, inverse-compositional ECC, "
-                    "affine then homography; rho>=0.8 gate; Laplacian-energy frame weights; "
+                    f"affine then homography; rho>=0.8 gate; {WEIGHTING[_weighting]}; "
                     "compensated FP32 weighted average",
         "frames": frames, "width": WIDTH, "height": HEIGHT, "levels": 4, "method": "INVERSE_COMPOSITIONAL",
         "passes": ["AFFINE", "HOMOGRAPHY"], "epsx": 0.01, "max_iterations": 50,
@@ -240,7 +247,14 @@ def main():
     ap.add_argument("--roi-method", choices=["fa", "lm"], default="fa")
     ap.add_argument("--roi-sample", type=int, default=8, help="crops checked against the oracle")
     ap.add_argument("--flow-sample", type=int, default=32, help="frames checked against the oracle (flow)")
+    ap.add_argument("--weighting", type=int, choices=sorted(WEIGHTING), default=1,
+                    help="stacking weights of the mono / bayer workloads (1, the Laplacian-energy frame weight, "
+                         "is the headline; the oracle's cpu_baseline implements only that one)")
     args = ap.parse_args()
+    global _weighting
+    _weighting = args.weighting
+    if args.weighting != 1:
+        args.no_cpu_baseline = True
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -285,7 +299,7 @@ def main():
     def step_device():
         acc.clear()
         reg.set_chunk_frames(n)
-        C.stack_frames(reg, acc, frames, passes, SCALE, weighting=1, on_device=True, n=n, width=WIDTH,
+        C.stack_frames(reg, acc, frames, passes, SCALE, weighting=_weighting, on_device=True, n=n, width=WIDTH,
                        height=HEIGHT, depth=C.DEPTH_U16, row_stride=WIDTH * 2, frame_stride=frame_bytes,
                        outputs=dev_out)
 
@@ -394,7 +408,7 @@ def run_e2e(args, ws, n, frames, reg, acc, passes, frame_bytes):
     def step_e2e():
         acc.clear()
         reg.set_chunk_frames(args.chunk)
-        C.stack_frames(reg, acc, host_frames.data_ptr(), passes, SCALE, weighting=1, on_device=True, n=n,
+        C.stack_frames(reg, acc, host_frames.data_ptr(), passes, SCALE, weighting=_weighting, on_device=True, n=n,
                        width=WIDTH, height=HEIGHT, depth=C.DEPTH_U16, row_stride=WIDTH * 2,
                        frame_stride=frame_bytes, outputs=pinned_out, host_input=True)
         C.lib().sst_weighted_average_compute(acc.handle, avg_host.data_ptr(), mask_host.data_ptr(), 0, None)
@@ -445,7 +459,7 @@ def bayer_cfg(frames: int):
     return {
         "workload": f"{frames} x {BAYER_W}x{BAYER_H} raw RGGB u16 12-bit frames (peak 1500 ADU, Poisson + read "
                     "noise); translation-only inverse-compositional c_ecch (4 levels) on the 2x2-binned "
-                    f"luminance ({BAYER_W // 2}x{BAYER_H // 2}); rho>=0.8 gate; Laplacian-energy frame weights; "
+                    f"luminance ({BAYER_W // 2}x{BAYER_H // 2}); rho>=0.8 gate; {WEIGHTING[_weighting]}; "
                     "the four Bayer planes warped and stacked with compensated FP32 sums",
         "frames": frames, "width": BAYER_W, "height": BAYER_H, "levels": 4, "method": "INVERSE_COMPOSITIONAL",
         "passes": ["TRANSLATION"], "epsx": 0.01, "max_iterations": 50,
@@ -521,7 +535,7 @@ def main_bayer(args, ws, rank, local):
         for a in accs:
             a.clear()
         reg.set_chunk_frames(chunk)
-        C.stack_bayer_frames(reg, accs, ptr, passes, BAYER_SCALE, weighting=1, on_device=on_device, n=n,
+        C.stack_bayer_frames(reg, accs, ptr, passes, BAYER_SCALE, weighting=_weighting, on_device=on_device, n=n,
                              width=BAYER_W, height=BAYER_H, row_stride=BAYER_W * 2, frame_stride=frame_bytes,
                              outputs=outputs, host_input=host_input)
 

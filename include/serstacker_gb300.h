@@ -249,6 +249,42 @@ int sst_weighted_average_accumulated_frames(const sst_weighted_average * h);
 int sst_weighted_average_save_state(sst_weighted_average * h, float * state4, int32_t * frames, void * stream);
 int sst_weighted_average_load_state(sst_weighted_average * h, const float * state4, int32_t frames, void * stream);
 
+/* ------------------------------------------------ local-variance weights */
+
+/* c_local_variance_map_options (c_local_variance_sharpness_measure.h:17-23):
+ * kernel radius of the morphological gradient, pyrDown steps before it
+ * (dscale) and INTER_AREA halvings of the map after it (uscale). The
+ * channel option is the frame itself (mono frames; the Bayer pipeline uses
+ * the 2x2-binned luminance). */
+typedef struct sst_local_variance_options {
+  int kradius;   /* 2; values below 1 act as 1; at most 16 */
+  int dscale;    /* 1 */
+  int uscale;    /* 3 */
+} sst_local_variance_options;
+
+void sst_local_variance_options_default(sst_local_variance_options * opts);
+
+typedef struct sst_local_variance sst_local_variance;
+
+/* c_local_variance_sharpness_measure (create_map, ..._measure.cc:252-262) */
+int sst_local_variance_create(sst_local_variance ** out, const sst_local_variance_options * opts);
+int sst_local_variance_destroy(sst_local_variance * h);
+
+/* compute_local_variance_map (c_local_variance_sharpness_measure.cc:
+ * 193-249) of n frames converted to FP32 by `scale`, with depthScale 20 (the
+ * CV_32F frames of the stacking pipeline): `maps` receives n width x height
+ * FP32 maps (may be NULL), `q` the n frame qualities Q (may be NULL). A
+ * frame whose morphological gradient sums to zero has no map in the
+ * reference: its q is 0 and its map is zero here. The map is always
+ * returned at the frame's size: where the reference returns a reduced map
+ * (dscale 0 with uscale > 0), it is upscaled with INTER_LINEAR here. */
+int sst_local_variance_compute(sst_local_variance * h, const void * frames, int depth, int n, int width, int height,
+    size_t row_stride, size_t frame_stride, double scale, int on_device, float * maps, double * q, void * stream);
+
+/* c_frame_accumulation_options::sharpness_measure of the stacking pipeline:
+ * the options of sst_stack_frames' weighting 3 (defaults until set). */
+int sst_weighted_average_set_local_variance(sst_weighted_average * h, const sst_local_variance_options * opts);
+
 /* ------------------------------------------------------- stacking pipeline */
 
 /* The per-frame body of the stacking pipeline for n frames
@@ -258,7 +294,13 @@ int sst_weighted_average_load_state(sst_weighted_average * h, const float * stat
  * 1265-1340), weight it and add it to `acc`. `weighting`: 0 none; 1 the
  * frame's Laplacian-energy sharpness; 2 focus stacking: per pixel
  * W = (6 lap^2 + |grad|^2)^2 of the warped frame (5-point Laplacian and
- * central differences, BORDER_REPLICATE) blurred by a Gaussian of sigma 3. Host frames are streamed to the
+ * central differences, BORDER_REPLICATE) blurred by a Gaussian of sigma 3;
+ * 3 local-variance maps (compute_weights, c_image_stacking_pipeline.cc:
+ * 2013-2020): the frame's sst_local_variance_compute map (options of
+ * sst_weighted_average_set_local_variance) warped like the frame (bilinear,
+ * BORDER_CONSTANT 0) and multiplied by the remapped mask
+ * (c_image_stacking_pipeline.cc:1653-1658, 1704-1713); kradius <= 0 disables
+ * the maps (weight 1), as weights_required does. Host frames are streamed to the
  * device in chunks whose copies overlap the registration of the previous
  * chunk. Outputs follow `on_device` and may be NULL. */
 int sst_stack_frames(sst_ecch * reg, sst_weighted_average * acc, const void * frames, int depth, int n,

@@ -27,7 +27,7 @@ BORDER_CONSTANT, BORDER_REPLICATE, BORDER_REFLECT, BORDER_REFLECT101 = 0, 1, 2, 
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(_HERE, f) for f in ("sst_oracle.cc", "sst_oracle_model.cc", "sst_oracle.h")]
+    srcs = [os.path.join(_HERE, f) for f in sorted(os.listdir(_HERE)) if f.endswith((".cc", ".h")) or f == "Makefile"]
     if force or not os.path.exists(_LIB_PATH) or any(
             os.path.getmtime(s) > os.path.getmtime(_LIB_PATH) for s in srcs):
         subprocess.check_call(["make", "-s", "-C", _HERE])
@@ -105,6 +105,9 @@ def lib():
             "orc_warp_residual": (d, [p, p, p, p, p, i, i, p, p, p]),
             "orc_focus_weights": (None, [p, p, p, i, i, i, i, p]),
             "orc_laplacian_energy": (d, [p, i, i]),
+            "orc_resize_linear": (None, [p, i, i, p, i, i]),
+            "orc_local_variance_size": (i, [i, i, i, i, p, p]),
+            "orc_local_variance_map": (i, [p, i, i, i, i, i, d, p, p, p, p]),
             "orc_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
             "orc_set_num_threads": (None, [i]),
             "orc_get_num_threads": (i, []),
@@ -425,6 +428,35 @@ def focus_weights(m: Model, state, src, dw, dh):
     out = np.empty((dh, dw))
     lib().orc_focus_weights(C.byref(m), _ptr(s), _ptr(a), a.shape[1], a.shape[0], dw, dh, _ptr(out))
     return out
+
+
+def resize_linear(img, dw, dh):
+    """cv::resize INTER_LINEAR"""
+    a = _f64(img)
+    out = np.empty((dh, dw))
+    lib().orc_resize_linear(_ptr(a), a.shape[1], a.shape[0], _ptr(out), dw, dh)
+    return out
+
+
+def local_variance_size(w, h, dscale=1, uscale=3):
+    """(width, height) of the map compute_local_variance_map returns"""
+    mw, mh = C.c_int(), C.c_int()
+    lib().orc_local_variance_size(w, h, dscale, uscale, C.byref(mw), C.byref(mh))
+    return mw.value, mh.value
+
+
+def local_variance_map(img, kradius=2, dscale=1, uscale=3, depth_scale=20.0):
+    """compute_local_variance_map -> (map or None, Q); depth_scale 20 is the
+    CV_32F case (20 * maxval(CV_32F) / maxval(depth))"""
+    a = _f64(img)
+    h, w = a.shape
+    out = np.empty((h, w))
+    mw, mh, q = C.c_int(), C.c_int(), C.c_double()
+    ok = lib().orc_local_variance_map(_ptr(a), w, h, kradius, dscale, uscale, depth_scale, _ptr(out),
+                                      C.byref(mw), C.byref(mh), C.byref(q))
+    if not ok:
+        return None, 0.0
+    return out.ravel()[:mw.value * mh.value].reshape(mh.value, mw.value).copy(), q.value
 
 
 def warp_residual(m: Model, state, img, tmpl, flow=None):

@@ -181,6 +181,22 @@ double orc_warp_residual(const orc_model * m, const double * state, const double
  * interior of a level image */
 double orc_laplacian_energy(const double * img, int w, int h);
 
+/* cv::resize INTER_LINEAR geometry (equal sizes copy) */
+void orc_resize_linear(const double * src, int sw, int sh, double * dst, int dw, int dh);
+
+/* size of the map compute_local_variance_map returns for a w x h image;
+ * returns 1 when the map is upscaled to the image's size */
+int orc_local_variance_size(int w, int h, int dscale, int uscale, int * mw, int * mh);
+
+/* compute_local_variance_map: morphological gradient G (square of radius
+ * max(1, kradius), BORDER_REPLICATE) of the image pyrDown'ed dscale times;
+ * map = ds^3 G^3, INTER_AREA-reduced uscale halvings, plus 0.05 Q with
+ * Q = ds^3 sum G^4 / sum G, INTER_LINEAR-upscaled to the image's size when the
+ * gradient's size differs from it. Returns 0 (no map, q = 0) when sum G is
+ * not positive, else 1 with the map (*mw x *mh, at most w x h) and q. */
+int orc_local_variance_map(const double * img, int w, int h, int kradius, int dscale, int uscale,
+    double depth_scale, double * map, int * mw, int * mh, double * q);
+
 /* whole pipeline for the CPU baseline: register (ecch passes) + rho gate +
  * final warp + weighted stack of n frames. */
 typedef struct orc_pipeline_opts {

@@ -121,6 +121,11 @@ def lib():
             "sst_bayer_average_accumulated_frames": (i, [p]),
             "sst_bayer_average_save_state": (i, [p, p, p, p]),
             "sst_bayer_average_load_state": (i, [p, p, C.c_int32, p]),
+            "sst_local_variance_options_default": (None, [p]),
+            "sst_local_variance_create": (i, [p, p]),
+            "sst_local_variance_destroy": (i, [p]),
+            "sst_local_variance_compute": (i, [p, p, i, i, i, i, sz, sz, d, i, p, p, p]),
+            "sst_weighted_average_set_local_variance": (i, [p, p]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(_lib, name)
@@ -400,6 +405,47 @@ class c_roi_batch:
         return ms.value, fi.value, px.value, ab.value
 
 
+class LocalVarianceOptions(C.Structure):
+    """c_local_variance_map_options (c_local_variance_sharpness_measure.h:17-23)"""
+    _fields_ = [("kradius", C.c_int), ("dscale", C.c_int), ("uscale", C.c_int)]
+
+
+def local_variance_options(**kw) -> LocalVarianceOptions:
+    o = LocalVarianceOptions()
+    lib().sst_local_variance_options_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class c_local_variance_sharpness_measure:
+    """c_local_variance_sharpness_measure::create_map over the C ABI."""
+
+    def __init__(self, options: Optional[LocalVarianceOptions] = None, **kw):
+        self.options = options if options is not None else local_variance_options(**kw)
+        self._h = C.c_void_p()
+        _check(lib().sst_local_variance_create(C.byref(self._h), C.byref(self.options)), "sst_local_variance_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_local_variance_destroy(h)
+            self._h = C.c_void_p()
+
+    def create_maps(self, frames: np.ndarray, scale: float = 1.0):
+        """frames (n, h, w) or (h, w) -> (maps (n, h, w) float32, q (n,) float64)"""
+        f = np.ascontiguousarray(frames)
+        if f.ndim == 2:
+            f = f[None]
+        n, h, w = f.shape
+        maps = np.zeros((n, h, w), np.float32)
+        q = np.zeros(n, np.float64)
+        _check(lib().sst_local_variance_compute(self._h, _ptr(f), _NP_DEPTH[f.dtype], n, w, h, f.strides[1],
+                                                 f.strides[0], scale, 0, _ptr(maps), _ptr(q), None),
+               "sst_local_variance_compute")
+        return maps, q
+
+
 class c_weigthed_average:
     """c_weigthed_average (c_frame_accumulation.h:39-63) over the C ABI."""
 
@@ -420,6 +466,11 @@ class c_weigthed_average:
 
     def clear(self):
         _check(lib().sst_weighted_average_clear(self._h, None), "clear")
+
+    def set_local_variance(self, options: Optional[LocalVarianceOptions] = None, **kw):
+        """sharpness-map options of stack_frames(weighting=3)"""
+        o = options if options is not None else local_variance_options(**kw)
+        _check(lib().sst_weighted_average_set_local_variance(self._h, C.byref(o)), "set_local_variance")
 
     def add(self, src: np.ndarray, weights: Optional[np.ndarray] = None, scale: float = 1.0):
         s = np.ascontiguousarray(src)

@@ -1023,12 +1023,15 @@ struct sst_weighted_average {
   DevBuf err;                          // set on the device when a bounded tile-copy wait gave up
   DevBuf focus_e, focus_w, gk_focus;   // focus weighting: energy maps, blurred maps, Gaussian taps
   int gk_n = 0;
+  sst_local_variance * lv = nullptr;   // local-variance weighting (created on first use)
+  sst_local_variance_options lvo = { 2, 1, 3 };
   int frames = 0;
   size_t plane() const { return (size_t) w * h; }
   ~sst_weighted_average()
   {
     acc.release(), coeffs.release(), weff.release(), src.release(), wsrc.release(), part.release(), err.release();
     focus_e.release(), focus_w.release(), gk_focus.release();
+    sst_local_variance_destroy(lv);
   }
 };
 
@@ -1053,6 +1056,40 @@ static int focus_maps(sst_weighted_average * a, const void * d_frames, int depth
   SST_CK_LAUNCH(launch_convert_smooth(a->focus_e.p, SST_DEPTH_F32, n, a->w, a->h, (size_t) a->w * sizeof(float),
       plane * sizeof(float), 1.0, a->gk_focus.as<float>(), a->gk_n, a->focus_w.as<float>(), plane, st));
   *maps = a->focus_w.as<float>();
+  return SST_OK;
+}
+
+int sst_internal_lv_create(sst_local_variance ** out, const sst_local_variance_options * o);   // sst_weights.cu
+int sst_internal_lv_build(sst_local_variance * L, const void * d_frames, int depth, int n, int w, int h,
+    size_t row_stride, size_t frame_stride, double scale, cudaStream_t st);
+int sst_internal_lv_warp(sst_local_variance * L, int motion, const float * coeffs, int dw, int dh, float * out,
+    cudaStream_t st);
+
+/* local-variance weighting: each frame's compute_local_variance_map warped
+ * to the accumulator's grid (bilinear, BORDER_CONSTANT 0); no maps (weight 1)
+ * when kradius <= 0, as weights_required (c_image_stacking_pipeline.cc:
+ * 2005-2011) */
+static int lv_maps(sst_weighted_average * a, const void * d_frames, int depth, int n, int sw, int sh,
+    size_t row_stride, size_t frame_stride, double scale, int motion, const float * coeffs, const float ** maps,
+    cudaStream_t st)
+{
+  *maps = nullptr;
+  if( a->lvo.kradius <= 0 ) return SST_OK;
+  if( !a->lv ) SST_TRY(sst_internal_lv_create(&a->lv, &a->lvo));
+  SST_CK(a->focus_w.ensure((size_t) n * a->plane() * sizeof(float)));
+  SST_TRY(sst_internal_lv_build(a->lv, d_frames, depth, n, sw, sh, row_stride, frame_stride, scale, st));
+  SST_TRY(sst_internal_lv_warp(a->lv, motion, coeffs, a->w, a->h, a->focus_w.as<float>(), st));
+  *maps = a->focus_w.as<float>();
+  return SST_OK;
+}
+
+extern "C" int sst_weighted_average_set_local_variance(sst_weighted_average * h, const sst_local_variance_options * o)
+{
+  if( !h || !o ) return set_error(SST_ERR_INVALID_ARG, "sst_weighted_average_set_local_variance: NULL argument");
+  if( o->kradius > 16 ) return set_error(SST_ERR_UNSUPPORTED, "local variance map: kradius above 16 is not supported");
+  h->lvo = *o;
+  sst_local_variance_destroy(h->lv);   // re-created with the new options on first use
+  h->lv = nullptr;
   return SST_OK;
 }
 
@@ -1119,14 +1156,16 @@ extern "C" int sst_weighted_average_add(sst_weighted_average * a, const void * s
 
 static int add_warped_device(sst_weighted_average * a, const void * d_frames, int depth, int n, int sw, int sh,
     size_t row_stride, size_t frame_stride, double scale, const sst_motion_model & m, const float * d_params,
-    const int32_t * d_status, const float * d_weights, int border, cudaStream_t st, bool focus = false)
+    const int32_t * d_status, const float * d_weights, int border, cudaStream_t st, int wmode = 0)
 {
   SST_CK(a->coeffs.ensure((size_t) n * SST_NCOEF * sizeof(float)));
   SST_CK(a->weff.ensure((size_t) n * sizeof(float)));
   SST_CK_LAUNCH(launch_coeffs_from_params(m, d_params, n, a->coeffs.as<float>(), st));
   SST_CK_LAUNCH(launch_effective_weights(d_weights, d_status, n, a->weff.as<float>(), st));
   const float * maps = nullptr;
-  if( focus ) SST_TRY(focus_maps(a, d_frames, depth, n, sw, sh, row_stride, frame_stride, scale, m.type,
+  if( wmode == 2 ) SST_TRY(focus_maps(a, d_frames, depth, n, sw, sh, row_stride, frame_stride, scale, m.type,
+      a->coeffs.as<float>(), &maps, st));
+  if( wmode == 3 ) SST_TRY(lv_maps(a, d_frames, depth, n, sw, sh, row_stride, frame_stride, scale, m.type,
       a->coeffs.as<float>(), &maps, st));
   StackArgs s;
   s.wmap = maps;
@@ -1308,7 +1347,7 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
     return set_error(SST_ERR_UNSUPPORTED, "unsupported border mode %d", border);
   if( h->L == 0 ) return set_error(SST_ERR_STATE, "c_ecch: no reference image was set");
   if( n < 1 ) return set_error(SST_ERR_INVALID_ARG, "n must be >= 1");
-  if( weighting < 0 || weighting > 2 ) return set_error(SST_ERR_INVALID_ARG, "weighting must be 0, 1 or 2");
+  if( weighting < 0 || weighting > 3 ) return set_error(SST_ERR_INVALID_ARG, "weighting must be 0, 1, 2 or 3");
   if( width != h->w || height != h->h || acc->w != h->w || acc->h != h->h )
     return set_error(SST_ERR_INVALID_ARG, "frame, reference and accumulator sizes must match");
   if( depth_bytes(depth) == 0 ) return set_error(SST_ERR_INVALID_ARG, "unsupported depth %d", depth);
@@ -1351,7 +1390,7 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
     SST_TRY(register_device(h, d_frames, depth, nc, row_stride, frame_stride, scale, num_passes, passes, nullptr, false));
     SST_TRY(add_warped_device(acc, d_frames, depth, nc, width, height, row_stride, frame_stride, scale, last,
         h->out_params.as<float>(), h->out_status.as<int32_t>(), weighting == 1 ? h->out_weight.as<float>() : nullptr,
-        border, st, weighting == 2));
+        border, st, weighting));
     if( !on_device ) SST_CK(cudaEventRecord(h->ev_free[buf], st));
     SST_TRY(copy_out(h->res_params.as<float>() + (size_t) f0 * 12, h->out_params.p, (size_t) nc * 12 * sizeof(float), 1, st));
     SST_TRY(copy_out(h->res_status.as<int32_t>() + f0, h->out_status.p, (size_t) nc * sizeof(int32_t), 1, st));
@@ -1392,7 +1431,7 @@ extern "C" int sst_stack_bayer_frames(sst_ecch * h, sst_weighted_average * const
   if( n < 1 ) return set_error(SST_ERR_INVALID_ARG, "n must be >= 1");
   if( (width & 1) || (height & 1) )
     return set_error(SST_ERR_INVALID_ARG, "Can not average raw bayer planes for uneven image size %dx%d", width, height);
-  if( weighting < 0 || weighting > 2 ) return set_error(SST_ERR_INVALID_ARG, "weighting must be 0, 1 or 2");
+  if( weighting < 0 || weighting > 3 ) return set_error(SST_ERR_INVALID_ARG, "weighting must be 0, 1, 2 or 3");
   const int pw = width / 2, ph = height / 2;
   if( pw != h->w || ph != h->h )
     return set_error(SST_ERR_INVALID_ARG, "the reference must be the binned size (width/2 x height/2)");
@@ -1450,6 +1489,11 @@ extern "C" int sst_stack_bayer_frames(sst_ecch * h, sst_weighted_average * const
     if( weighting == 2 ) {
       // focus weights of the warped binned luminance, shared by the four planes
       SST_TRY(focus_maps(a0, h->binned.p, SST_DEPTH_U16, nc, pw, ph, (size_t) pw * 2, bin_frame, scale, last.type,
+          a0->coeffs.as<float>(), &maps, st));
+    }
+    if( weighting == 3 ) {
+      // local-variance maps of the binned luminance, shared by the four planes
+      SST_TRY(lv_maps(a0, h->binned.p, SST_DEPTH_U16, nc, pw, ph, (size_t) pw * 2, bin_frame, scale, last.type,
           a0->coeffs.as<float>(), &maps, st));
     }
     BayerPlanesArgs b;

@@ -436,3 +436,60 @@ def test_focus_weights_known_answers(oracle):
     k = oracle.gaussian_kernel(3.0)
     assert len(k) == 19
     assert abs(raw[15, 20] - sum(k[i] * e[15, 20 + i - 9] for i in range(19))) < 1e-6 * raw[15, 20]
+
+
+def test_resize_linear_known_answers(oracle):
+    # cv::resize INTER_LINEAR of [0, 1] to 4: f = (d + 0.5) / 2 - 0.5, clamped at both ends
+    out = oracle.resize_linear(np.array([[0.0, 1.0]]), 4, 1)
+    assert np.allclose(out, [[0.0, 0.25, 0.75, 1.0]], atol=1e-15)
+    img = np.arange(12.0).reshape(3, 4)
+    assert np.array_equal(oracle.resize_linear(img, 4, 3), img)           # equal sizes copy
+    # linear data stays linear away from the clamped ends
+    ramp = np.tile(np.arange(8.0), (2, 1))
+    up = oracle.resize_linear(ramp, 16, 2)
+    assert np.allclose(up[0, 1:15], (np.arange(1, 15) + 0.5) / 2 - 0.5, atol=1e-12)
+
+
+def test_local_variance_map_sizes_follow_the_reference(oracle):
+    assert oracle.local_variance_size(1280, 960, 1, 3) == (1280, 960)    # upscaled back to the frame
+    assert oracle.local_variance_size(1280, 960, 0, 0) == (1280, 960)
+    assert oracle.local_variance_size(1280, 960, 0, 3) == (160, 120)     # the reference keeps the reduced map
+    assert oracle.local_variance_size(16, 10, 0, 3) == (8, 5)            # dscaleSize stops before a side < 4
+    assert oracle.local_variance_size(3, 9, 2, 0) == (3, 9)              # pdownscale keeps images below 4
+
+
+def test_local_variance_map_known_answers(oracle):
+    # no structure: no map and Q = 0
+    m, q = oracle.local_variance_map(np.full((30, 40), 3.0))
+    assert m is None and q == 0.0
+    # vertical step a -> b at x = 20, radius 2: G = |b - a| on columns 18..21, 0 elsewhere
+    a, b, ds = 0.25, 0.75, 20.0
+    img = np.full((30, 40), a)
+    img[:, 20:] = b
+    m, q = oracle.local_variance_map(img, kradius=2, dscale=0, uscale=0, depth_scale=ds)
+    d3 = (ds * (b - a)) ** 3
+    assert abs(q - d3) < 1e-12 * d3                          # Q = ds^3 sum G^4 / sum G
+    want = np.full((30, 40), 0.05 * d3)
+    want[:, 18:22] += d3
+    assert np.allclose(m, want, rtol=1e-14, atol=0)
+    # radius 0 acts as 1: columns 19..20
+    m1, _ = oracle.local_variance_map(img, kradius=0, dscale=0, uscale=0, depth_scale=ds)
+    assert np.allclose(m1[0, 18:22], [0.05 * d3, 1.05 * d3, 1.05 * d3, 0.05 * d3])
+
+
+def test_local_variance_map_is_scale_invariant_and_area_reduced(oracle):
+    rng = np.random.default_rng(7)
+    img = rng.random((96, 128))
+    m1, q1 = oracle.local_variance_map(img)
+    m2, q2 = oracle.local_variance_map(img * 7.0, depth_scale=20.0 / 7.0)
+    assert m1.shape == (96, 128)
+    assert abs(q1 - q2) < 1e-12 * q1 and np.abs(m1 - m2).max() < 1e-12 * m1.max()
+    # dscale 0, uscale 1: the reference returns the INTER_AREA-halved map + 0.05 Q
+    m3, q3 = oracle.local_variance_map(img, kradius=1, dscale=0, uscale=1, depth_scale=1.0)
+    assert m3.shape == (48, 64)
+    p = np.pad(img, 1, mode="edge")
+    win = np.lib.stride_tricks.sliding_window_view(p, (3, 3))
+    g = win.max(axis=(2, 3)) - win.min(axis=(2, 3))
+    assert abs(q3 - (g ** 4).sum() / g.sum()) < 1e-12 * q3
+    want = (g ** 3).reshape(48, 2, 64, 2).mean(axis=(1, 3)) + 0.05 * q3
+    assert np.abs(m3 - want).max() < 1e-12 * want.max()
