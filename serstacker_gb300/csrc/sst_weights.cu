@@ -55,11 +55,13 @@ struct Taps {
   int K;
 };
 
-/* INTER_LINEAR taps along one axis: destination d reads sources i0[d] and
- * min(i0[d] + 1, m - 1) with weights 1 - fr[d], fr[d] */
-struct LinTaps {
-  const int * i0;
-  const float * fr;
+/* INTER_LINEAR taps along one axis of the full-resolution grid: position p
+ * reads small-map cells i0(p) and min(i0(p) + 1, m - 1) with weights
+ * 1 - fr(p), fr(p). t[p + 1] = { i0(p), fr(p), i0(p + 1), fr(p + 1) } for
+ * p = -1 ... full - 1 (a bilinear remap tap pair p, p + 1 in one load); the
+ * entries outside the grid repeat the edge with zero fractions. */
+struct LinTab {
+  const float4 * t;
   int m;
 };
 
@@ -112,6 +114,182 @@ __global__ void __launch_bounds__(256) k_lv_down(const uint8_t * src, int sw, in
   }
 }
 
+/* tile sums of G and G^4 (FP64 across the warps) to part[2 tile] */
+__device__ __forceinline__ void store_tile_sums(float sg, float sg4, double * part)
+{
+  __shared__ double s_red[2][8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double a = sg, b = sg4;
+#pragma unroll
+  for( int o = 16; o > 0; o >>= 1 ) a += __shfl_xor_sync(0xffffffffu, a, o), b += __shfl_xor_sync(0xffffffffu, b, o);
+  if( lane == 0 ) s_red[0][wid] = a, s_red[1][wid] = b;
+  __syncthreads();
+  if( threadIdx.x == 0 ) {
+    double ta = 0, tb = 0;
+    for( int i = 0; i < 8; ++i ) ta += s_red[0][i], tb += s_red[1][i];
+    const size_t t = ((size_t) blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    part[2 * t] = ta, part[2 * t + 1] = tb;
+  }
+}
+
+/* INTER_AREA reduction by whole fx x fy cells that tile a 64 x 16 tile
+ * (fx | 64, fy | 16, the gradient's size a multiple of both): the tile
+ * kernel writes the small map's cell means instead of P (fx = 0: P). */
+struct AreaFuse {
+  int fx, fy, mw, mh;
+  float inv_area;
+  float * small;
+};
+
+/* One 64 x 16 gradient tile with its radius-R halo (REPLICATE) for the
+ * common radii, every staging load of a thread issued before its first use.
+ * DOWN: the gradient's level is pyrDown of the raw frame (dscale 1): the raw
+ * window under the clamped halo rows / columns (REFLECT_101 at the frame's
+ * edges) is converted, reduced rows first, then columns, into the level
+ * window. Otherwise the level window is read directly (the raw frame x scale
+ * at dscale 0, or an FP32 pyramid level with scale 1). */
+template<typename T, int R, bool DOWN>
+__global__ void __launch_bounds__(256) k_lv_tile(const uint8_t * src, int sw, int sh, size_t rs, size_t fs, float scale,
+    int gw, int gh, float ds3, float * p3, double * part, AreaFuse af)
+{
+  constexpr int LW = GR_TX + 2 * R, LH = GR_TY + 2 * R;                      // level window
+  constexpr int RW = DOWN ? 2 * LW + 3 : LW, RH = DOWN ? 2 * LH + 3 : LH;    // staged source window
+  constexpr int NS = RW * RH, PER = (NS + 255) / 256;
+  constexpr int NH = DOWN ? RH * LW : 1, NL = DOWN ? LH * LW : 1, NM = DOWN ? 1 : 2 * LH * GR_TX;
+  static_assert(!DOWN || NS >= 2 * LH * GR_TX, "the row extrema reuse the source window");
+  static_assert((DOWN ? NH : NS) >= GR_TX * GR_TY, "the fused cells reuse a staging buffer");
+  __shared__ __align__(16) float s_src[NS];
+  __shared__ __align__(16) float s_h[NH];
+  __shared__ __align__(16) float s_lvl[NL];
+  __shared__ __align__(16) float s_m2[NM];
+  const float * lvl = DOWN ? s_lvl : s_src;
+  float * s_mx = DOWN ? s_src : s_m2;
+  float * s_mn = s_mx + LH * GR_TX;
+  float * s_p = DOWN ? s_h : s_src;          // the tile's P for the fused INTER_AREA cells (free by then)
+  const uint8_t * fb = src + (size_t) blockIdx.z * fs;
+  const int tx0 = blockIdx.x * GR_TX, ty0 = blockIdx.y * GR_TY;
+  // first clamped level column / row of the window
+  const int cx0 = max(tx0 - R, 0), cy0 = max(ty0 - R, 0);
+  {
+    // window origin in the source; a window inside the source needs no border rule
+    const int ox = DOWN ? 2 * cx0 - 2 : tx0 - R, oy = DOWN ? 2 * cy0 - 2 : ty0 - R;
+    const bool inside = ox >= 0 && oy >= 0 && ox + RW <= sw && oy + RH <= sh;
+    const T * base = (const T *) (fb + (size_t) max(oy, 0) * rs) + max(ox, 0);
+    float v[PER];
+#pragma unroll
+    for( int k = 0; k < PER; ++k ) {
+      const int i = threadIdx.x + 256 * k;
+      if( i < NS ) {
+        const int yy = i / RW, xx = i - yy * RW;
+        if( inside ) {
+          v[k] = (float) __ldg((const T *) ((const uint8_t *) base + (size_t) yy * rs) + xx);
+        }
+        else {
+          int sx, sy;
+          if( DOWN ) sx = reflect101(ox + xx, sw), sy = reflect101(oy + yy, sh);
+          else sx = clampi(ox + xx, 0, sw - 1), sy = clampi(oy + yy, 0, sh - 1);
+          v[k] = (float) __ldg((const T *) (fb + (size_t) sy * rs) + sx);
+        }
+      }
+    }
+#pragma unroll
+    for( int k = 0; k < PER; ++k ) {
+      const int i = threadIdx.x + 256 * k;
+      if( i < NS ) s_src[i] = v[k] * scale;
+    }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int NCL = (LW + 31) / 32;   // level-window columns per lane
+  if( DOWN ) {
+    // rows first: every staged row at the LW clamped level columns; the
+    // lane's staged-column offsets are fixed over the rows
+    int off[NCL];
+#pragma unroll
+    for( int k = 0; k < NCL; ++k ) off[k] = 2 * (clampi(tx0 - R + lane + 32 * k, 0, gw - 1) - cx0);
+    for( int yy = wid; yy < RH; yy += 8 ) {
+#pragma unroll
+      for( int k = 0; k < NCL; ++k ) {
+        const int c = lane + 32 * k;
+        if( c < LW ) {
+          const float * p = s_src + yy * RW + off[k];
+          s_h[yy * LW + c] = (p[0] + p[4]) * 0.0625f + (p[1] + p[3]) * 0.25f + p[2] * 0.375f;
+        }
+      }
+    }
+    __syncthreads();
+    for( int yy = wid; yy < LH; yy += 8 ) {
+      const float * row = s_h + 2 * (clampi(ty0 - R + yy, 0, gh - 1) - cy0) * LW;
+#pragma unroll
+      for( int k = 0; k < NCL; ++k ) {
+        const int c = lane + 32 * k;
+        if( c < LW ) {
+          const float * p = row + c;
+          s_lvl[yy * LW + c] = (p[0] + p[4 * LW]) * 0.0625f + (p[LW] + p[3 * LW]) * 0.25f + p[2 * LW] * 0.375f;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // dilate / erode along rows over 2R + 1 columns
+  for( int yy = wid; yy < LH; yy += 8 ) {
+#pragma unroll
+    for( int k = 0; k < GR_TX / 32; ++k ) {
+      const int xx = lane + 32 * k;
+      const float * p = lvl + yy * LW + xx;
+      float mx = p[0], mn = p[0];
+#pragma unroll
+      for( int j = 1; j <= 2 * R; ++j ) mx = fmaxf(mx, p[j]), mn = fminf(mn, p[j]);
+      s_mx[yy * GR_TX + xx] = mx, s_mn[yy * GR_TX + xx] = mn;
+    }
+  }
+  __syncthreads();
+  float sg = 0.f, sg4 = 0.f;
+  float * out = p3 + (size_t) blockIdx.z * gw * gh;
+#pragma unroll
+  for( int r2 = 0; r2 < GR_TY / 8; ++r2 ) {
+    const int yy = wid + 8 * r2, y = ty0 + yy;
+#pragma unroll
+    for( int k = 0; k < GR_TX / 32; ++k ) {
+      const int xx = lane + 32 * k, x = tx0 + xx;
+      if( y < gh && x < gw ) {
+        float mx = s_mx[yy * GR_TX + xx], mn = s_mn[yy * GR_TX + xx];
+#pragma unroll
+        for( int j = 1; j <= 2 * R; ++j ) mx = fmaxf(mx, s_mx[(yy + j) * GR_TX + xx]), mn = fminf(mn, s_mn[(yy + j) * GR_TX + xx]);
+        const float g = mx - mn;
+        const float g3 = g * g * g;
+        if( af.fx ) s_p[yy * GR_TX + xx] = g3 * ds3;
+        else out[(size_t) y * gw + x] = g3 * ds3;
+        sg += g;
+        sg4 = fmaf(g3, g, sg4);
+      }
+    }
+  }
+  store_tile_sums(sg, sg4, part);   // ends with a barrier: s_p is complete
+  if( af.fx ) {
+    // cell sums along rows (into the free extrema buffer), then along columns
+    const int ncx = GR_TX / af.fx, ncy = GR_TY / af.fy;
+    float * s_q = s_mx;
+    for( int i = threadIdx.x; i < GR_TY * ncx; i += 256 ) {
+      const int yy = i / ncx, c = i - yy * ncx;
+      const float * p = s_p + yy * GR_TX + c * af.fx;
+      float a = 0.f;
+      for( int j = 0; j < af.fx; ++j ) a += p[j];
+      s_q[i] = a;
+    }
+    __syncthreads();
+    for( int i = threadIdx.x; i < ncy * ncx; i += 256 ) {
+      const int cy = i / ncx, c = i - cy * ncx;
+      const int X = tx0 / af.fx + c, Y = ty0 / af.fy + cy;
+      if( X < af.mw && Y < af.mh ) {
+        float a = 0.f;
+        for( int j = 0; j < af.fy; ++j ) a += s_q[(cy * af.fy + j) * ncx + c];
+        af.small[(size_t) blockIdx.z * af.mw * af.mh + (size_t) Y * af.mw + X] = a * af.inv_area;
+      }
+    }
+  }
+}
+
 /* Morphological gradient of one 64 x 16 tile: the window (tile + r on every
  * side, coordinates clamped) is staged in shared memory, row maxima / minima
  * over 2r + 1 columns, then column maxima / minima over 2r + 1 rows.
@@ -125,7 +303,6 @@ __global__ void __launch_bounds__(256) k_lv_gradient(const float * src, int w, i
   float * s_in = s_mem;
   float * s_mx = s_in + SH * SW;
   float * s_mn = s_mx + SH * GR_TX;
-  __shared__ double s_red[2][8];
   const size_t plane = (size_t) w * h;
   const float * in = src + (size_t) blockIdx.z * plane;
   const int tx0 = blockIdx.x * GR_TX, ty0 = blockIdx.y * GR_TY;
@@ -166,17 +343,7 @@ __global__ void __launch_bounds__(256) k_lv_gradient(const float * src, int w, i
       }
     }
   }
-  double a = sg, b = sg4;
-#pragma unroll
-  for( int o = 16; o > 0; o >>= 1 ) a += __shfl_xor_sync(0xffffffffu, a, o), b += __shfl_xor_sync(0xffffffffu, b, o);
-  if( lane == 0 ) s_red[0][wid] = a, s_red[1][wid] = b;
-  __syncthreads();
-  if( threadIdx.x == 0 ) {
-    double ta = 0, tb = 0;
-    for( int i = 0; i < 8; ++i ) ta += s_red[0][i], tb += s_red[1][i];
-    const size_t t = ((size_t) blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    part[2 * t] = ta, part[2 * t + 1] = tb;
-  }
+  store_tile_sums(sg, sg4, part);
 }
 
 /* per frame (one warp each, fixed summation order): W = sum G,
@@ -208,11 +375,12 @@ __global__ void __launch_bounds__(256) k_lv_area(const float * src, int sw, int 
   if( x >= dw || y >= dh ) return;
   const float * s = src + (size_t) blockIdx.z * sw * sh;
   float acc = 0.f;
+#pragma unroll 2
   for( int j = 0; j < ty.K; ++j ) {
     const float wy = __ldg(ty.w + y * ty.K + j);
-    if( wy == 0.f ) continue;
     const float * row = s + (size_t) __ldg(ty.idx + y * ty.K + j) * sw;
     float r = 0.f;
+#pragma unroll 4
     for( int i = 0; i < tx.K; ++i ) r = fmaf(__ldg(tx.w + x * tx.K + i), __ldg(row + __ldg(tx.idx + x * tx.K + i)), r);
     acc = fmaf(wy, r, acc);
   }
@@ -221,20 +389,19 @@ __global__ void __launch_bounds__(256) k_lv_area(const float * src, int sw, int 
 
 /* the full-resolution map at source pixel (px, py): the INTER_LINEAR upscale
  * of the small map plus 0.05 Q */
-__device__ __forceinline__ float lv_at(const float * sm, LinTaps ux, LinTaps uy, float addq, int px, int py)
+__device__ __forceinline__ float lv_at(const float * sm, LinTab ux, LinTab uy, float addq, int px, int py)
 {
-  const int y0 = __ldg(uy.i0 + py), y1 = min(y0 + 1, uy.m - 1);
-  const int x0 = __ldg(ux.i0 + px), x1 = min(x0 + 1, ux.m - 1);
-  const float b = __ldg(uy.fr + py), a = __ldg(ux.fr + px);
+  const float4 ty = __ldg(uy.t + py + 1), tx = __ldg(ux.t + px + 1);
+  const int y0 = (int) ty.x, y1 = min(y0 + 1, uy.m - 1), x0 = (int) tx.x, x1 = min(x0 + 1, ux.m - 1);
   const float * r0 = sm + (size_t) y0 * ux.m;
   const float * r1 = sm + (size_t) y1 * ux.m;
-  const float t0 = (1.f - a) * __ldg(r0 + x0) + a * __ldg(r0 + x1);
-  const float t1 = (1.f - a) * __ldg(r1 + x0) + a * __ldg(r1 + x1);
-  return (1.f - b) * t0 + b * t1 + addq;
+  const float t0 = (1.f - tx.y) * __ldg(r0 + x0) + tx.y * __ldg(r0 + x1);
+  const float t1 = (1.f - tx.y) * __ldg(r1 + x0) + tx.y * __ldg(r1 + x1);
+  return (1.f - ty.y) * t0 + ty.y * t1 + addq;
 }
 
 /* source-grid maps (w x h per frame); frames without a map are zero */
-__global__ void __launch_bounds__(256) k_lv_expand(const float * small, LinTaps ux, LinTaps uy, const float * addq,
+__global__ void __launch_bounds__(256) k_lv_expand(const float * small, LinTab ux, LinTab uy, const float * addq,
     const int * has, int w, int h, float * out)
 {
   const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -244,33 +411,76 @@ __global__ void __launch_bounds__(256) k_lv_expand(const float * small, LinTaps 
   out[(size_t) f * w * h + (size_t) y * w + x] = __ldg(has + f) ? lv_at(sm, ux, uy, __ldg(addq + f), x, y) : 0.f;
 }
 
+/* Weights of the small-map cells c, c + 1, c + 2 (c = i0 of the first
+ * position, cells clamped to the map) for the bilinear remap tap pair p, p + 1
+ * with weights b0, b1 (zero outside the grid) composed with the INTER_LINEAR
+ * upscale: tap p spreads over cells i0(p), i0(p) + 1, tap p + 1 over
+ * i0(p + 1) = i0(p) + d (d = 0 or 1, the upscale never skips a cell). */
+__device__ __forceinline__ void lin_pair(float4 t, float b0, float b1, float & w0, float & w1, float & w2)
+{
+  const bool same = t.z == t.x;
+  const float a0 = b0 * (1.f - t.y), a1 = b0 * t.y, c0 = b1 * (1.f - t.w), c1 = b1 * t.w;
+  w0 = same ? a0 + c0 : a0;
+  w1 = same ? a1 + c1 : a1 + c0;
+  w2 = same ? 0.f : c1;
+}
+
 /* output-grid stacking weights: the source-grid map sampled bilinearly at the
  * frame's warp of each output pixel, zero outside the frame
- * (BORDER_CONSTANT); a frame without a map weighs 1 everywhere */
+ * (BORDER_CONSTANT); a frame without a map weighs 1 everywhere. The
+ * composition bilinear(remap) o bilinear(upscale) is separable: per axis the
+ * two remap taps give weights over three consecutive small-map cells. */
+constexpr int WP_ROWS = 4;   // output rows per thread of the warp-weight kernel (32 x 32 tiles)
+
 template<int FAM>
-__global__ void __launch_bounds__(256) k_lv_warp(const float * small, LinTaps ux, LinTaps uy, const float * addq,
+__global__ void __launch_bounds__(256) k_lv_warp(const float * small, LinTab ux, LinTab uy, const float * addq,
     const int * has, const float * coeffs, int w, int h, int dw, int dh, float * out)
 {
-  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
-  if( x >= dw || y >= dh ) return;
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), yb = blockIdx.y * (8 * WP_ROWS) + (threadIdx.x >> 5);
+  if( x >= dw || yb >= dh ) return;
   const int f = blockIdx.z;
-  float * o = out + (size_t) f * dw * dh + (size_t) y * dw + x;
-  if( !__ldg(has + f) ) {
-    *o = 1.f;
-    return;
-  }
-  float c[SST_NCOEF];
-#pragma unroll
-  for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __ldg(coeffs + (size_t) f * SST_NCOEF + i);
-  const spos s = warp_pos<FAM>(c, x, y);
-  const float * sm = small + (size_t) f * ux.m * uy.m;
+  // the frame's flag, 0.05 Q and warp coefficients in one round of loads
+  const int hf = __ldg(has + f);
   const float aq = __ldg(addq + f);
-  auto v = [&](int px, int py) {
-    return ((unsigned) px < (unsigned) w && (unsigned) py < (unsigned) h) ? lv_at(sm, ux, uy, aq, px, py) : 0.f;
-  };
-  const float v00 = v(s.x0, s.y0), v01 = v(s.x0 + 1, s.y0), v10 = v(s.x0, s.y0 + 1), v11 = v(s.x0 + 1, s.y0 + 1);
-  const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-  *o = fmaf(s.fy, t1 - t0, t0);
+  float c[SST_NCOEF];
+  const float4 * c4 = reinterpret_cast<const float4 *>(coeffs + (size_t) f * SST_NCOEF);
+#pragma unroll
+  for( int i = 0; i < SST_NCOEF / 4; ++i ) {
+    const float4 v = __ldg(c4 + i);
+    c[4 * i] = v.x, c[4 * i + 1] = v.y, c[4 * i + 2] = v.z, c[4 * i + 3] = v.w;
+  }
+  float * o = out + (size_t) f * dw * dh + x;
+  const float * sm = small + (size_t) f * ux.m * uy.m;
+  const int m = ux.m;
+#pragma unroll
+  for( int k = 0; k < WP_ROWS; ++k ) {
+    const int y = min(yb + 8 * k, dh - 1);   // rows past the grid recompute the last one, unstored
+    float res = 1.f;
+    if( hf ) {
+      res = 0.f;
+      const spos s = warp_pos<FAM>(c, x, y);
+      if( s.x0 >= -1 && s.x0 <= w - 1 && s.y0 >= -1 && s.y0 <= h - 1 ) {
+        const float bx0 = s.x0 >= 0 ? 1.f - s.fx : 0.f, bx1 = s.x0 + 1 <= w - 1 ? s.fx : 0.f;
+        const float by0 = s.y0 >= 0 ? 1.f - s.fy : 0.f, by1 = s.y0 + 1 <= h - 1 ? s.fy : 0.f;
+        const float4 tx = __ldg(ux.t + s.x0 + 1), ty = __ldg(uy.t + s.y0 + 1);
+        float wx0, wx1, wx2, wy0, wy1, wy2;
+        lin_pair(tx, bx0, bx1, wx0, wx1, wx2);
+        lin_pair(ty, by0, by1, wy0, wy1, wy2);
+        const int cx = (int) tx.x, cx1 = min(cx + 1, m - 1), cx2 = min(cx + 2, m - 1);
+        const int ry = (int) ty.x, ry1 = min(ry + 1, uy.m - 1), ry2 = min(ry + 2, uy.m - 1);
+        auto row = [&](int r) {
+          const float * p = sm + (size_t) r * m;
+          float v = wx0 * __ldg(p + cx) + wx1 * __ldg(p + cx1);
+          if( wx2 != 0.f ) v = fmaf(wx2, __ldg(p + cx2), v);
+          return v;
+        };
+        float v = wy0 * row(ry) + wy1 * row(ry1);
+        if( wy2 != 0.f ) v = fmaf(wy2, row(ry2), v);
+        res = fmaf(aq, (bx0 + bx1) * (by0 + by1), v);
+      }
+    }
+    if( yb + 8 * k < dh ) o[(size_t) y * dw] = res;
+  }
 }
 
 }  // namespace lvm
@@ -308,10 +518,11 @@ void area_axis(int ssize, int dsize, std::vector<int> & idx, std::vector<float> 
 }
 
 /* INTER_LINEAR geometry: destination d samples f = (d + 0.5) ssize / dsize - 0.5,
- * clamped to the first / last source with a zero fraction */
-void linear_axis(int ssize, int dsize, std::vector<int> & i0, std::vector<float> & fr)
+ * clamped to the first / last source with a zero fraction; packed as the
+ * LinTab pairs { i0(p), fr(p), i0(p + 1), fr(p + 1) }, p = -1 ... dsize - 1 */
+std::vector<float4> linear_axis(int ssize, int dsize)
 {
-  i0.resize(dsize), fr.resize(dsize);
+  std::vector<float> i0(dsize + 2), fr(dsize + 2, 0.f);
   const double s = (double) ssize / dsize;
   for( int d = 0; d < dsize; ++d ) {
     const double f = (d + 0.5) * s - 0.5;
@@ -319,8 +530,12 @@ void linear_axis(int ssize, int dsize, std::vector<int> & i0, std::vector<float>
     double a = f - si;
     if( si < 0 ) si = 0, a = 0;
     if( si >= ssize - 1 ) si = ssize - 1, a = 0;
-    i0[d] = si, fr[d] = (float) a;
+    i0[d + 1] = (float) si, fr[d + 1] = (float) a;
   }
+  i0[0] = i0[1], i0[dsize + 1] = i0[dsize];   // outside the grid: the edge cell, zero fraction
+  std::vector<float4> t(dsize + 1);
+  for( int p = -1; p < dsize; ++p ) t[p + 1] = make_float4(i0[p + 1], fr[p + 1], i0[p + 2], fr[p + 2]);
+  return t;
 }
 
 /* dscaleSize (c_local_variance_sharpness_measure.cc:15-25) */
@@ -374,20 +589,21 @@ struct sst_local_variance {
   // pyrDowns) and small map (mw x mh)
   int w = 0, h = 0, gw = 0, gh = 0, nlev = 0, mw = 0, mh = 0, tiles = 0;
   int n = 0;                              // frames of the last batch
+  bool area_fused = false;                // the last batch's INTER_AREA cells came from the tile kernel
   DevBuf lv[2], p3, small, part, q, addq, has, stage, maps;
   DevBuf ax_i, ax_w, ay_i, ay_w;          // INTER_AREA taps (gradient grid -> small map)
-  DevBuf ux_i, ux_f, uy_i, uy_f;          // INTER_LINEAR taps (small map -> frame grid)
+  DevBuf ux, uy;                          // INTER_LINEAR tap pairs (small map -> frame grid)
   int ax_k = 0, ay_k = 0;
   int tab_key[4] = { -1, -1, -1, -1 };
   ~sst_local_variance()
   {
     for( DevBuf * b : { &lv[0], &lv[1], &p3, &small, &part, &q, &addq, &has, &stage, &maps, &ax_i, &ax_w, &ay_i, &ay_w,
-             &ux_i, &ux_f, &uy_i, &uy_f } )
+             &ux, &uy } )
       b->release();
   }
   const float * small_map() const { return (mw == gw && mh == gh) ? p3.as<float>() : small.as<float>(); }
-  LinTaps lx() const { return LinTaps { ux_i.as<int>(), ux_f.as<float>(), mw }; }
-  LinTaps ly() const { return LinTaps { uy_i.as<int>(), uy_f.as<float>(), mh }; }
+  LinTab lx() const { return LinTab { ux.as<float4>(), mw }; }
+  LinTab ly() const { return LinTab { uy.as<float4>(), mh }; }
 };
 
 namespace {
@@ -423,12 +639,9 @@ int lv_tables(sst_local_variance * L, cudaStream_t st)
     SST_LCK(upload(L->ay_i, i, st));
     SST_LCK(upload(L->ay_w, f, st));
   }
-  linear_axis(L->mw, L->w, i, f);
-  SST_LCK(upload(L->ux_i, i, st));
-  SST_LCK(upload(L->ux_f, f, st));
-  linear_axis(L->mh, L->h, i, f);
-  SST_LCK(upload(L->uy_i, i, st));
-  SST_LCK(upload(L->uy_f, f, st));
+  const std::vector<float4> tx = linear_axis(L->mw, L->w), ty = linear_axis(L->mh, L->h);
+  SST_LCK(upload(L->ux, tx, st));
+  SST_LCK(upload(L->uy, ty, st));
   // pageable sources: the copies have read them when the stream reaches here
   SST_LCK(cudaStreamSynchronize(st));
   memcpy(L->tab_key, key, sizeof(key));
@@ -448,59 +661,115 @@ int sst_internal_lv_build(sst_local_variance * L, const void * d_frames, int dep
   L->n = n;
   SST_TRY_L(lv_tables(L, st));
   const size_t gplane = (size_t) L->gw * L->gh;
-  SST_LCK(L->p3.ensure((size_t) n * gplane * sizeof(float)));
   SST_LCK(L->part.ensure((size_t) n * L->tiles * 2 * sizeof(double)));
   SST_LCK(L->q.ensure((size_t) n * sizeof(double)));
   SST_LCK(L->addq.ensure((size_t) n * sizeof(float)));
   SST_LCK(L->has.ensure((size_t) n * sizeof(int)));
-  // step 1: scaled FP32 at the gradient's resolution
-  const float * lvl = nullptr;
-  if( L->nlev == 0 ) {
-    SST_LCK(L->lv[0].ensure((size_t) n * w * h * sizeof(float)));
-    SST_LLAUNCH(launch_convert_smooth(d_frames, depth, n, w, h, row_stride, frame_stride, scale, nullptr, 0,
-        L->lv[0].as<float>(), (size_t) w * h, st));
-    lvl = L->lv[0].as<float>();
+  // steps 1-2: the gradient's level, P = ds^3 G^3 and the tile sums; radii up
+  // to 3 (4 without a reduction) in one staged tile kernel straight from the
+  // raw frames at dscale 0 and 1
+  const double ds = 20.0, ds3 = ds * ds * ds;
+  const dim3 ggrid((L->gw + GR_TX - 1) / GR_TX, (L->gh + GR_TY - 1) / GR_TY, n);
+  const uint8_t * s = (const uint8_t *) d_frames;
+  const float sc = (float) scale;
+  float * p3 = nullptr;
+  double * part = L->part.as<double>();
+#define SST_LV_TILE(TV, RV, DV, SRC, SW, SH, RS, FS, SC)                                                       \
+  k_lv_tile<TV, RV, DV><<<ggrid, 256, 0, st>>>(SRC, SW, SH, RS, FS, SC, L->gw, L->gh, (float) ds3, p3, part, af)
+#define SST_LV_TILE_R(TV, DV, SRC, SW, SH, RS, FS, SC)                                                         \
+  switch ( r ) {                                                                                               \
+  case 1: SST_LV_TILE(TV, 1, DV, SRC, SW, SH, RS, FS, SC); break;                                              \
+  case 2: SST_LV_TILE(TV, 2, DV, SRC, SW, SH, RS, FS, SC); break;                                              \
+  case 3: SST_LV_TILE(TV, 3, DV, SRC, SW, SH, RS, FS, SC); break;                                              \
+  default: SST_LV_TILE(TV, 4, false, SRC, SW, SH, RS, FS, SC); break;                                          \
+  }
+#define SST_LV_TILE_T(DV)                                                                                      \
+  switch ( depth ) {                                                                                           \
+  case SST_DEPTH_U8: SST_LV_TILE_R(uint8_t, DV, s, w, h, row_stride, frame_stride, sc); break;                \
+  case SST_DEPTH_U16: SST_LV_TILE_R(uint16_t, DV, s, w, h, row_stride, frame_stride, sc); break;              \
+  case SST_DEPTH_F32: SST_LV_TILE_R(float, DV, s, w, h, row_stride, frame_stride, sc); break;                 \
+  default: return lfail(SST_ERR_INVALID_ARG, "unsupported depth");                                             \
+  }
+  const bool fused = (L->nlev == 0 && r <= 4) || (L->nlev == 1 && r <= 3);
+  // INTER_AREA folded into the tile kernel when its cells tile the 64 x 16 tiles
+  AreaFuse af = { 0, 0, L->mw, L->mh, 0.f, nullptr };
+  const bool area = L->mw != L->gw || L->mh != L->gh;
+  if( area && r <= 4 && L->gw % L->mw == 0 && L->gh % L->mh == 0 && GR_TX % (L->gw / L->mw) == 0 &&
+      GR_TY % (L->gh / L->mh) == 0 ) {
+    SST_LCK(L->small.ensure((size_t) n * L->mw * L->mh * sizeof(float)));
+    af.fx = L->gw / L->mw, af.fy = L->gh / L->mh;
+    af.inv_area = (float) (1.0 / ((double) af.fx * af.fy));
+    af.small = L->small.as<float>();
+  }
+  L->area_fused = af.fx != 0;
+  if( !L->area_fused ) {
+    SST_LCK(L->p3.ensure((size_t) n * gplane * sizeof(float)));
+    p3 = L->p3.as<float>();
+  }
+  if( fused ) {
+    if( L->nlev == 0 ) {
+      SST_LV_TILE_T(false)
+    }
+    else {
+      SST_LV_TILE_T(true)
+    }
+    SST_LCK(cudaGetLastError());
+    sst_internal_count_launches(1);
   }
   else {
-    int cw = (w + 1) / 2, ch = (h + 1) / 2;
-    SST_LCK(L->lv[0].ensure((size_t) n * cw * ch * sizeof(float)));
-    dim3 grid((cw + DN_TX - 1) / DN_TX, (ch + DN_TY - 1) / DN_TY, n);
-    const uint8_t * s = (const uint8_t *) d_frames;
-    const float sc = (float) scale;
-    switch ( depth ) {
-    case SST_DEPTH_U8: k_lv_down<uint8_t><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, sc, L->lv[0].as<float>(), cw, ch); break;
-    case SST_DEPTH_U16: k_lv_down<uint16_t><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, sc, L->lv[0].as<float>(), cw, ch); break;
-    case SST_DEPTH_F32: k_lv_down<float><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, sc, L->lv[0].as<float>(), cw, ch); break;
-    default: return lfail(SST_ERR_INVALID_ARG, "unsupported depth");
+    // step 1: scaled FP32 at the gradient's resolution
+    const float * lvl = nullptr;
+    if( L->nlev == 0 ) {
+      SST_LCK(L->lv[0].ensure((size_t) n * w * h * sizeof(float)));
+      SST_LLAUNCH(launch_convert_smooth(d_frames, depth, n, w, h, row_stride, frame_stride, scale, nullptr, 0,
+          L->lv[0].as<float>(), (size_t) w * h, st));
+      lvl = L->lv[0].as<float>();
+    }
+    else {
+      int cw = (w + 1) / 2, ch = (h + 1) / 2;
+      SST_LCK(L->lv[0].ensure((size_t) n * cw * ch * sizeof(float)));
+      dim3 grid((cw + DN_TX - 1) / DN_TX, (ch + DN_TY - 1) / DN_TY, n);
+      switch ( depth ) {
+      case SST_DEPTH_U8: k_lv_down<uint8_t><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, sc, L->lv[0].as<float>(), cw, ch); break;
+      case SST_DEPTH_U16: k_lv_down<uint16_t><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, sc, L->lv[0].as<float>(), cw, ch); break;
+      case SST_DEPTH_F32: k_lv_down<float><<<grid, 256, 0, st>>>(s, w, h, row_stride, frame_stride, sc, L->lv[0].as<float>(), cw, ch); break;
+      default: return lfail(SST_ERR_INVALID_ARG, "unsupported depth");
+      }
+      SST_LCK(cudaGetLastError());
+      sst_internal_count_launches(1);
+      int b = 0;
+      for( int l = 1; l < L->nlev; ++l ) {
+        const int nw = (cw + 1) / 2, nh = (ch + 1) / 2;
+        SST_LCK(L->lv[b ^ 1].ensure((size_t) n * nw * nh * sizeof(float)));
+        SST_LLAUNCH(launch_pyrdown(L->lv[b].as<float>(), cw, ch, (size_t) cw * ch, L->lv[b ^ 1].as<float>(), nw, nh,
+            (size_t) nw * nh, n, st));
+        b ^= 1, cw = nw, ch = nh;
+      }
+      lvl = L->lv[b].as<float>();
+    }
+    // step 2
+    if( r <= 4 ) {
+      const uint8_t * ls = (const uint8_t *) lvl;
+      const size_t lrs = (size_t) L->gw * sizeof(float), lfs = (size_t) L->gw * L->gh * sizeof(float);
+      SST_LV_TILE_R(float, false, ls, L->gw, L->gh, lrs, lfs, 1.f)
+    }
+    else {
+      const size_t smem = ((size_t) (GR_TY + 2 * r) * (GR_TX + 2 * r) + 2 * (size_t) (GR_TY + 2 * r) * GR_TX) * sizeof(float);
+      k_lv_gradient<<<ggrid, 256, smem, st>>>(lvl, L->gw, L->gh, r, (float) ds3, p3, part);
     }
     SST_LCK(cudaGetLastError());
     sst_internal_count_launches(1);
-    int b = 0;
-    for( int l = 1; l < L->nlev; ++l ) {
-      const int nw = (cw + 1) / 2, nh = (ch + 1) / 2;
-      SST_LCK(L->lv[b ^ 1].ensure((size_t) n * nw * nh * sizeof(float)));
-      SST_LLAUNCH(launch_pyrdown(L->lv[b].as<float>(), cw, ch, (size_t) cw * ch, L->lv[b ^ 1].as<float>(), nw, nh,
-          (size_t) nw * nh, n, st));
-      b ^= 1, cw = nw, ch = nh;
-    }
-    lvl = L->lv[b].as<float>();
   }
-  // step 2: gradient, P = ds^3 G^3, tile sums
-  const double ds = 20.0, ds3 = ds * ds * ds;
-  {
-    dim3 grid((L->gw + GR_TX - 1) / GR_TX, (L->gh + GR_TY - 1) / GR_TY, n);
-    const size_t smem = ((size_t) (GR_TY + 2 * r) * (GR_TX + 2 * r) + 2 * (size_t) (GR_TY + 2 * r) * GR_TX) * sizeof(float);
-    k_lv_gradient<<<grid, 256, smem, st>>>(lvl, L->gw, L->gh, r, (float) ds3, L->p3.as<float>(), L->part.as<double>());
-    SST_LCK(cudaGetLastError());
-    sst_internal_count_launches(1);
-  }
+#undef SST_LV_TILE_T
+#undef SST_LV_TILE_R
+#undef SST_LV_TILE
   // step 3: W and Q per frame
   k_lv_finish<<<(n + 7) / 8, 256, 0, st>>>(L->part.as<double>(), L->tiles, n, ds3, L->q.as<double>(),
       L->addq.as<float>(), L->has.as<int>());
   SST_LCK(cudaGetLastError());
   sst_internal_count_launches(1);
   // step 4: INTER_AREA reduction
-  if( L->mw != L->gw || L->mh != L->gh ) {
+  if( (L->mw != L->gw || L->mh != L->gh) && !L->area_fused ) {
     SST_LCK(L->small.ensure((size_t) n * L->mw * L->mh * sizeof(float)));
     dim3 grid((L->mw + 31) / 32, (L->mh + 7) / 8, n);
     k_lv_area<<<grid, 256, 0, st>>>(L->p3.as<float>(), L->gw, L->gh, L->small.as<float>(), L->mw, L->mh,
@@ -516,7 +785,7 @@ int sst_internal_lv_build(sst_local_variance * L, const void * d_frames, int dep
 int sst_internal_lv_warp(sst_local_variance * L, int motion, const float * coeffs, int dw, int dh, float * out,
     cudaStream_t st)
 {
-  dim3 grid((dw + 31) / 32, (dh + 7) / 8, L->n);
+  dim3 grid((dw + 31) / 32, (dh + 8 * WP_ROWS - 1) / (8 * WP_ROWS), L->n);
   const int fam = motion_family(motion);
 #define SST_LV_WARP(FAMV) k_lv_warp<FAMV><<<grid, 256, 0, st>>>(L->small_map(), L->lx(), L->ly(), L->addq.as<float>(), \
       L->has.as<int>(), coeffs, L->w, L->h, dw, dh, out)

@@ -35,12 +35,17 @@ _SCALE = {np.uint8: 1.0 / 255, np.uint16: 1.0 / 65535, np.float32: 1.0}
 
 
 @pytest.mark.parametrize("w,h,dtype,kradius,dscale,uscale", [
-    (1280, 960, np.uint16, 2, 1, 3),     # the stacking defaults at the headline frame size
+    (1280, 960, np.uint16, 2, 1, 3),     # the stacking defaults at the headline frame size (8 x 8 cells folded)
     (333, 277, np.float32, 1, 2, 2),     # two pyrDowns, non-integer INTER_AREA factors
     (160, 120, np.uint8, 3, 0, 0),       # full resolution, no reduction
     (100, 75, np.float32, 2, 1, 0),      # pyrDown only, INTER_LINEAR back
     (61, 47, np.uint16, 2, 1, 3),        # partial tiles, dscaleSize stops early
-    (200, 150, np.float32, 16, 1, 1),    # the largest supported radius
+    (200, 150, np.float32, 16, 1, 1),    # the largest supported radius (general two-kernel path)
+    (150, 97, np.uint8, 1, 1, 2),        # fused pyrDown + gradient, radius 1
+    (257, 129, np.uint16, 3, 1, 2),      # fused pyrDown + gradient, radius 3
+    (130, 66, np.uint16, 4, 1, 0),       # pyrDown kernel, then the staged gradient of radius 4
+    (96, 40, np.float32, 4, 0, 0),       # staged gradient of radius 4 on the frame itself
+    (1024, 512, np.uint16, 1, 1, 4),     # 16 x 16 INTER_AREA cells folded into the gradient tiles
 ])
 def test_local_variance_maps_match_oracle(gpu, oracle, w, h, dtype, kradius, dscale, uscale):
     frames = np.stack([_image(w, h, dtype, seed=w + k) for k in range(2)])
