@@ -6,8 +6,8 @@
  * Follows compute_local_variance_map
  * (core/proc/sharpness_measure/c_local_variance_sharpness_measure.cc:193-249)
  * and its helpers dscaleSize (:15-25), pdownscale (:28-52),
- * _compute_sharpness_map (:125-160) and upscale_local_variance_map
- * (:172-181), with OpenCV's morphological gradient (dilate - erode over a
+ * _compute_sharpness_map (:131-165) and upscale_local_variance_map
+ * (:175-184), with OpenCV's morphological gradient (dilate - erode over a
  * square, BORDER_REPLICATE), INTER_AREA and INTER_LINEAR resize geometry.
  */
 #include <math.h>

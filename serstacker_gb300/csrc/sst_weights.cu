@@ -10,11 +10,11 @@
  *      the raw frame;
  *   2. G = dilate - erode over the (2r+1)^2 square (cv::MORPH_GRADIENT,
  *      BORDER_REPLICATE) and P = ds^3 G^3 (_compute_sharpness_map,
- *      :125-160), with per-tile FP64 sums of G and G^4;
+ *      :131-165), with per-tile FP64 sums of G and G^4;
  *   3. per frame W = sum G, Q = ds^3 sum G^4 / W; W <= 0 means no map;
  *   4. INTER_AREA reduction of P by uscale halvings (dscaleSize, :15-25);
  *   5. + 0.05 Q and the INTER_LINEAR upscale to the frame's size
- *      (upscale_local_variance_map, :172-181).
+ *      (upscale_local_variance_map, :175-184).
  * Step 5 is never materialised for stacking: the stacking weight of an
  * output pixel is the map sampled bilinearly (BORDER_CONSTANT 0) at the
  * frame's warp of that pixel (c_image_stacking_pipeline.cc:1653-1658), and
