@@ -32,6 +32,7 @@ extern "C" {
 #define SST_ERR_STATE          -4
 #define SST_ERR_NOMEM          -5
 #define SST_ERR_TIMEOUT        -6
+#define SST_ERR_IO             -7
 
 /* per-frame registration status */
 #define SST_FRAME_OK              0
@@ -67,6 +68,9 @@ extern "C" {
 #define SST_DEPTH_U8   0
 #define SST_DEPTH_U16  2
 #define SST_DEPTH_F32  5
+/* reported by SER files only (no compute entry point takes them) */
+#define SST_DEPTH_S32  4
+#define SST_DEPTH_F64  6
 
 /* COLORID Bayer patterns (core/io/debayer.h:19-34) */
 #define SST_COLORID_BAYER_RGGB  8
@@ -339,6 +343,58 @@ int sst_ecch_set_level_loops(sst_ecch * h, int enable);
 /* Number of kernels the library launched since the last call of this
  * function (graph replays count every kernel node they run). */
 long long sst_kernel_launch_count(int reset);
+
+/* ------------------------------------------------------------ SER input */
+
+/* c_ser_file's header (core/io/c_ser_file.h:40-62) as read by c_ser_reader::open
+ * (c_ser_file.cc:259-385). data_little_endian is the reference's inverted
+ * reading of the LittleEndian field (1 when the field is 0). depth is an
+ * SST_DEPTH_* code (SST_DEPTH_S32 for 17..32 bits, SST_DEPTH_F32 / _F64 for
+ * -32 / -64), channels 3 for RGB / BGR, else 1. */
+typedef struct sst_ser_info {
+  int32_t luid, color_id, data_little_endian;
+  int32_t width, height, bits_per_plane, frames;
+  int32_t channels, bytes_per_plane, depth, has_timestamps;
+  char observer[41], instrument[41], telescope[41];
+  uint64_t date_time, date_time_utc;
+} sst_ser_info;
+
+typedef struct sst_ser_reader sst_ser_reader;
+
+/* c_ser_reader::open: validates the header (file id, image size, pixel
+ * format, color id) and reads the timestamp trailer when the file holds one;
+ * the read position is frame 0. SST_ERR_IO for file errors, SST_ERR_UNSUPPORTED
+ * for files the reference rejects. */
+int sst_ser_open(sst_ser_reader ** out, const char * path);
+int sst_ser_close(sst_ser_reader * r);
+int sst_ser_get_info(const sst_ser_reader * r, sst_ser_info * info);
+
+/* c_ser_file::timestamps: copies up to n timestamps, returns how many
+ * (SST_ERR_STATE when the file has none) */
+int sst_ser_timestamps(const sst_ser_reader * r, uint64_t * ts, int n);
+
+/* c_ser_reader::curpos / seek (negative frames seek to 0; frames past the
+ * end are rejected unless equal to the current position) */
+int sst_ser_curpos(const sst_ser_reader * r);
+int sst_ser_seek(sst_ser_reader * r, int frame);
+
+/* c_ser_reader::read for up to n frames from the current position into host
+ * memory, frame_stride bytes apart (0: packed); pixel data stored in the other
+ * byte order than the host's is swapped. *frames_read receives the count
+ * (0 at the end of the file). */
+int sst_ser_read(sst_ser_reader * r, int n, void * dst, size_t frame_stride, int * frames_read);
+
+/* The stacking loop over frames [first, first + count) of a SER file (count
+ * < 0: to the end): frames are read in chunks of `chunk` frames (0: 256) into
+ * pinned host buffers, the next chunk from the file while the GPU registers
+ * and stacks the current one, scaled by 1 / 2^bits_per_plane as
+ * read_input_frame does (c_image_processing_pipeline.cc:1180-1190), and
+ * handed to sst_stack_frames (mono: acc[0]) or sst_stack_bayer_frames
+ * (RGGB-family 16-bit Bayer: acc[0..3]). Outputs as those calls, for the
+ * count frames (host memory). */
+int sst_stack_ser(sst_ecch * reg, sst_weighted_average * const * acc, sst_ser_reader * ser, int first, int count,
+    int chunk, int num_passes, const sst_motion_model * passes, int border, int weighting,
+    float * params_out, int32_t * status_out, float * rho_out, float * weight_out, void * stream);
 
 /* ----------------------------------------------------------- utilities */
 

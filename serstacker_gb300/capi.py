@@ -126,6 +126,14 @@ def lib():
             "sst_local_variance_destroy": (i, [p]),
             "sst_local_variance_compute": (i, [p, p, i, i, i, i, sz, sz, d, i, p, p, p]),
             "sst_weighted_average_set_local_variance": (i, [p, p]),
+            "sst_ser_open": (i, [p, C.c_char_p]),
+            "sst_ser_close": (i, [p]),
+            "sst_ser_get_info": (i, [p, p]),
+            "sst_ser_timestamps": (i, [p, p, i]),
+            "sst_ser_curpos": (i, [p]),
+            "sst_ser_seek": (i, [p, i]),
+            "sst_ser_read": (i, [p, i, p, sz, p]),
+            "sst_stack_ser": (i, [p, p, p, i, i, i, i, p, i, i, p, p, p, p, p]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(_lib, name)
@@ -647,6 +655,88 @@ def stack_bayer_frames(reg: c_ecch, accs: Sequence[c_weigthed_average], frames, 
                                         dev, len(passes), models, border, weighting, _ptr(outputs["params"]),
                                         _ptr(outputs["status"]), _ptr(outputs["rho"]), _ptr(outputs["weight"]),
                                         None), "sst_stack_bayer_frames")
+    return outputs
+
+
+class SerInfo(C.Structure):
+    """sst_ser_info: the SER header as c_ser_reader reads it (c_ser_file.h:40-62)"""
+    _fields_ = [("luid", C.c_int32), ("color_id", C.c_int32), ("data_little_endian", C.c_int32),
+                ("width", C.c_int32), ("height", C.c_int32), ("bits_per_plane", C.c_int32), ("frames", C.c_int32),
+                ("channels", C.c_int32), ("bytes_per_plane", C.c_int32), ("depth", C.c_int32),
+                ("has_timestamps", C.c_int32), ("observer", C.c_char * 41), ("instrument", C.c_char * 41),
+                ("telescope", C.c_char * 41), ("date_time", C.c_uint64), ("date_time_utc", C.c_uint64)]
+
+
+_SER_DTYPE = {1: np.uint8, 2: np.uint16}
+
+
+class c_ser_reader:
+    """c_ser_reader (core/io/c_ser_file.h:130-190) over the C ABI."""
+
+    def __init__(self, path: str):
+        self._h = C.c_void_p()
+        _check(lib().sst_ser_open(C.byref(self._h), os.fsencode(path)), "sst_ser_open")
+        self.info = SerInfo()
+        _check(lib().sst_ser_get_info(self._h, C.byref(self.info)), "sst_ser_get_info")
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_ser_close(h)
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def dtype(self):
+        if self.info.depth == DEPTH_F32:
+            return np.float32
+        if self.info.bits_per_plane == -64:
+            return np.float64
+        if self.info.bytes_per_plane == 4:
+            return np.int32
+        return _SER_DTYPE[self.info.bytes_per_plane]
+
+    def curpos(self) -> int:
+        return lib().sst_ser_curpos(self._h)
+
+    def seek(self, frame: int):
+        _check(lib().sst_ser_seek(self._h, frame), "sst_ser_seek")
+
+    def read(self, n: int = 1) -> np.ndarray:
+        """up to n frames from the current position: (m, h, w[, channels])"""
+        i = self.info
+        shape = (n, i.height, i.width) + ((i.channels,) if i.channels > 1 else ())
+        out = np.zeros(shape, self.dtype())
+        got = C.c_int()
+        _check(lib().sst_ser_read(self._h, n, _ptr(out), 0, C.byref(got)), "sst_ser_read")
+        return out[:got.value]
+
+    def timestamps(self) -> np.ndarray:
+        ts = np.zeros(self.info.frames, np.uint64)
+        m = lib().sst_ser_timestamps(self._h, _ptr(ts), len(ts))
+        if m < 0:
+            _check(m, "sst_ser_timestamps")
+        return ts[:m]
+
+
+def stack_ser(reg: c_ecch, accs, ser: c_ser_reader, passes: Sequence[int], first: int = 0, count: int = -1,
+              chunk: int = 0, weighting: int = 1, border: int = BORDER_REFLECT101):
+    """sst_stack_ser: register + stack frames of a SER file (accs: one
+    accumulator for mono files, four for Bayer files)."""
+    accs = list(accs) if isinstance(accs, (list, tuple)) else [accs]
+    n = ser.info.frames - first if count < 0 else min(count, ser.info.frames - first)
+    handles = (C.c_void_p * len(accs))(*[a.handle.value for a in accs])
+    models = (MotionModel * len(passes))(*[motion(t) for t in passes])
+    outputs = {"params": np.zeros((n, 12), np.float32), "status": np.zeros(n, np.int32),
+               "rho": np.zeros(n, np.float32), "weight": np.zeros(n, np.float32)}
+    _check(lib().sst_stack_ser(reg.handle, handles, ser.handle, first, count, chunk, len(passes), models, border,
+                               weighting, _ptr(outputs["params"]), _ptr(outputs["status"]), _ptr(outputs["rho"]),
+                               _ptr(outputs["weight"]), None), "sst_stack_ser")
     return outputs
 
 
