@@ -346,8 +346,8 @@ long long sst_kernel_launch_count(int reset);
 
 /* ------------------------------------------------------------ SER input */
 
-/* c_ser_file's header (core/io/c_ser_file.h:40-62) as read by c_ser_reader::open
- * (c_ser_file.cc:259-385). data_little_endian is the reference's inverted
+/* c_ser_file's header (core/io/c_ser_file.h:42-56) as read by c_ser_reader::open
+ * (c_ser_file.cc:272-411). data_little_endian is the reference's inverted
  * reading of the LittleEndian field (1 when the field is 0). depth is an
  * SST_DEPTH_* code (SST_DEPTH_S32 for 17..32 bits, SST_DEPTH_F32 / _F64 for
  * -32 / -64), channels 3 for RGB / BGR, else 1. */

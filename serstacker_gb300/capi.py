@@ -659,7 +659,7 @@ def stack_bayer_frames(reg: c_ecch, accs: Sequence[c_weigthed_average], frames, 
 
 
 class SerInfo(C.Structure):
-    """sst_ser_info: the SER header as c_ser_reader reads it (c_ser_file.h:40-62)"""
+    """sst_ser_info: the SER header as c_ser_reader reads it (c_ser_file.h:42-56)"""
     _fields_ = [("luid", C.c_int32), ("color_id", C.c_int32), ("data_little_endian", C.c_int32),
                 ("width", C.c_int32), ("height", C.c_int32), ("bits_per_plane", C.c_int32), ("frames", C.c_int32),
                 ("channels", C.c_int32), ("bytes_per_plane", C.c_int32), ("depth", C.c_int32),
@@ -671,7 +671,7 @@ _SER_DTYPE = {1: np.uint8, 2: np.uint16}
 
 
 class c_ser_reader:
-    """c_ser_reader (core/io/c_ser_file.h:130-190) over the C ABI."""
+    """c_ser_reader (core/io/c_ser_file.h:136-174) over the C ABI."""
 
     def __init__(self, path: str):
         self._h = C.c_void_p()

@@ -2,11 +2,11 @@
  * sst_ser.cpp -- SER v3 frame sequences (the stacking pipeline's usual
  * input) read straight into the registration + stacking path.
  *
- * The reader follows c_ser_reader (core/io/c_ser_file.h:130-190,
- * core/io/c_ser_file.cc:259-530): the 178-byte LUCAM-RECORDER header (always
+ * The reader follows c_ser_reader (core/io/c_ser_file.h:136-174,
+ * core/io/c_ser_file.cc:272-532): the 178-byte LUCAM-RECORDER header (always
  * little-endian), the reference's reading of the LittleEndian field (0 means
  * little-endian pixel data: "well-known bug with endiannes in ser file
- * format", c_ser_file.cc:296-297), its bits-per-plane extension (-32 / -64
+ * format", c_ser_file.cc:304-305), its bits-per-plane extension (-32 / -64
  * for float / double, 17..32 for int32), the accepted color ids, the optional
  * trailer of per-frame 64-bit timestamps, and seek / read positions.
  *

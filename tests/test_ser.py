@@ -1,6 +1,6 @@
 """SER v3 input through the C ABI on the CPU: sst_ser_* against files written
 by tests/ser_files.py. Covers c_ser_reader's header checks, the inverted
-LittleEndian field (0 = little-endian pixel data, c_ser_file.cc:296-297), the
+LittleEndian field (0 = little-endian pixel data, c_ser_file.cc:304-305), the
 bits-per-plane extension (-32, -64, 17..32), timestamps, seek / curpos and
 truncated files. Byte-for-byte: every read is compared exactly."""
 import ctypes as C
