@@ -7,6 +7,9 @@
  *   sst_gb300::c_ecch_options      core/proc/image_registration/ecc2.h:158-172
  *   sst_gb300::c_ecch              core/proc/image_registration/ecc2.h:193-308
  *   sst_gb300::c_weigthed_average  core/average/c_frame_accumulation.h:39-63
+ *   sst_gb300::c_local_variance_map_options, c_local_variance_sharpness_measure
+ *                                  core/proc/sharpness_measure/c_local_variance_sharpness_measure.h:17-23
+ *   sst_gb300::c_ser_reader        core/io/c_ser_file.h:136-174
  * Images are passed as `image_view` (pointer, size, OpenCV depth code,
  * stride) instead of cv::Mat, so this header needs no OpenCV; define
  * SST_GB300_WITH_OPENCV before including it to get cv::Mat overloads.
@@ -230,6 +233,18 @@ public:
     return sst_weighted_average_reinitialize(_h, avg.data(), accw.data(), 0, nullptr) == SST_OK;
   }
 
+  /* c_frame_accumulation_options::sharpness_measure: the map options of the
+   * stacking pipeline's local-variance weights (sst_stack_frames weighting 3) */
+  bool set_sharpness_measure(int kradius, int dscale, int uscale)
+  {
+    if( !_h ) return false;
+    const sst_local_variance_options o = { kradius, dscale, uscale };
+    return sst_weighted_average_set_local_variance(_h, &o) == SST_OK;
+  }
+
+  /* the accumulator must exist before its options can be set */
+  bool create(int width, int height) { return ensure(width, height); }
+
   void clear() { if( _h ) sst_weighted_average_clear(_h, nullptr); }
   int accumulated_frames() const { return _h ? sst_weighted_average_accumulated_frames(_h) : 0; }
   int width() const { return _w; }
@@ -247,6 +262,120 @@ private:
   }
   sst_weighted_average * _h = nullptr;
   int _w = 0, _hh = 0;
+};
+
+/* c_local_variance_map_options (c_local_variance_sharpness_measure.h:17-23) */
+struct c_local_variance_map_options {
+  int kradius = 2;
+  int dscale = 1;
+  int uscale = 3;
+};
+
+/* c_local_variance_sharpness_measure::create_map on the GPU: the map of a
+ * host image converted to FP32 by `scale` (depthScale 20, the stacking
+ * pipeline's CV_32F frames), returned at the image's size, and its quality Q */
+class c_local_variance_sharpness_measure {
+public:
+  explicit c_local_variance_sharpness_measure(const c_local_variance_map_options & o = c_local_variance_map_options())
+  {
+    const sst_local_variance_options so = { o.kradius, o.dscale, o.uscale };
+    if( sst_local_variance_create(&_h, &so) != SST_OK ) _h = nullptr;
+  }
+  ~c_local_variance_sharpness_measure() { if( _h ) sst_local_variance_destroy(_h); }
+  c_local_variance_sharpness_measure(const c_local_variance_sharpness_measure &) = delete;
+  c_local_variance_sharpness_measure & operator=(const c_local_variance_sharpness_measure &) = delete;
+
+  bool create_map(const image_view & image, std::vector<float> & map, double * q = nullptr, double scale = 1.0)
+  {
+    if( !_h || image.empty() ) return false;
+    map.resize((size_t) image.width * image.height);
+    double qq = 0;
+    const bool ok = sst_local_variance_compute(_h, image.data, image.depth, 1, image.width, image.height, image.stride,
+        image.stride * image.height, scale, 0, map.data(), &qq, nullptr) == SST_OK;
+    if( q ) *q = qq;
+    return ok;
+  }
+
+  sst_local_variance * handle() const { return _h; }
+
+private:
+  sst_local_variance * _h = nullptr;
+};
+
+/* c_ser_reader (core/io/c_ser_file.h:136-174): header accessors, seek /
+ * curpos and frame reads into a host buffer (pixel data byte-swapped to the
+ * host's order). read() fills `frame` with one frame of frame_size() bytes. */
+class c_ser_reader {
+public:
+  c_ser_reader() = default;
+  explicit c_ser_reader(const std::string & filename) { open(filename); }
+  ~c_ser_reader() { close(); }
+  c_ser_reader(const c_ser_reader &) = delete;
+  c_ser_reader & operator=(const c_ser_reader &) = delete;
+
+  bool open(const std::string & filename)
+  {
+    close();
+    if( sst_ser_open(&_h, filename.c_str()) != SST_OK ) return false;
+    sst_ser_get_info(_h, &_info);
+    return true;
+  }
+  void close()
+  {
+    if( _h ) sst_ser_close(_h);
+    _h = nullptr;
+  }
+  bool is_open() const { return _h != nullptr; }
+
+  int image_width() const { return _info.width; }
+  int image_height() const { return _info.height; }
+  int bits_per_plane() const { return _info.bits_per_plane; }
+  int bytes_per_plane() const { return _info.bytes_per_plane; }
+  int color_id() const { return _info.color_id; }
+  int channels() const { return _info.channels; }
+  int num_frames() const { return _info.frames; }
+  int depth() const { return _info.depth; }
+  const char * observer() const { return _info.observer; }
+  const char * instrument() const { return _info.instrument; }
+  const char * telescope() const { return _info.telescope; }
+  size_t frame_size() const { return (size_t) _info.width * _info.height * _info.channels * _info.bytes_per_plane; }
+  const sst_ser_info & info() const { return _info; }
+
+  std::vector<uint64_t> timestamps() const
+  {
+    std::vector<uint64_t> ts;
+    if( _h && _info.has_timestamps ) {
+      ts.resize(_info.frames);
+      sst_ser_timestamps(_h, ts.data(), _info.frames);
+    }
+    return ts;
+  }
+
+  int curpos() const { return _h ? sst_ser_curpos(_h) : -1; }
+  bool seek(int frame_index) { return _h && sst_ser_seek(_h, frame_index) == SST_OK; }
+
+  bool read(std::vector<uint8_t> & frame)
+  {
+    if( !_h ) return false;
+    frame.resize(frame_size());
+    int got = 0;
+    return sst_ser_read(_h, 1, frame.data(), 0, &got) == SST_OK && got == 1;
+  }
+#ifdef SST_GB300_WITH_OPENCV
+  bool read(cv::Mat & image)
+  {
+    if( !_h || _info.depth < 0 ) return false;
+    image.create(_info.height, _info.width, CV_MAKETYPE(_info.depth, _info.channels));
+    int got = 0;
+    return sst_ser_read(_h, 1, image.data, 0, &got) == SST_OK && got == 1;
+  }
+#endif
+
+  sst_ser_reader * handle() const { return _h; }
+
+private:
+  sst_ser_reader * _h = nullptr;
+  sst_ser_info _info {};
 };
 
 }  // namespace sst_gb300

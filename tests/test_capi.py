@@ -73,10 +73,26 @@ int main() {
   sst_gb300::image_transform t(SST_MOTION_HOMOGRAPHY);
   e.set_image_transform(&t);
   if( sst_gb300::c_ecch::nparams(t.model) != 8 ) return 3;
+  sst_gb300::c_local_variance_map_options lo;
+  if( lo.kradius != 2 || lo.dscale != 1 || lo.uscale != 3 ) return 4;
+  sst_gb300::c_ser_reader ser(SER_PATH);
+  if( !ser.is_open() || ser.image_width() != 6 || ser.image_height() != 4 || ser.num_frames() != 3 ) return 5;
+  if( ser.bits_per_plane() != 12 || ser.depth() != SST_DEPTH_U16 || ser.frame_size() != 48 ) return 6;
+  std::vector<uint8_t> f;
+  if( !ser.seek(2) || !ser.read(f) || ser.curpos() != 3 ) return 7;
+  const uint16_t * px = (const uint16_t *) f.data();
+  for( int i = 0; i < 24; ++i ) if( px[i] != 2 * 1000 + i ) return 8;
+  if( ser.read(f) ) return 9;          // past the last frame
+  std::vector<uint64_t> ts = ser.timestamps();
+  if( ts.size() != 3 || ts[1] != 11 ) return 10;
   std::printf("ok %s\n", sst_version());
   return 0;
 }
-''')
+'''.replace("SER_PATH", '"' + str(tmp_path / "t.ser") + '"'))
+    import numpy as np
+    from ser_files import write_ser
+    frames = (np.arange(3)[:, None, None] * 1000 + np.arange(24).reshape(4, 6)).astype(np.uint16)
+    write_ser(tmp_path / "t.ser", frames, bits=12, timestamps=[10, 11, 12])
     libdir = os.path.dirname(capi.LIB_PATH)
     exe = tmp_path / "t"
     subprocess.check_call([gxx, "-std=c++17", "-I", os.path.join(root, "include"), str(src), "-o", str(exe),
