@@ -800,6 +800,7 @@ int sst_internal_lv_warp(sst_local_variance * L, int motion, const float * coeff
 
 int sst_internal_lv_create(sst_local_variance ** out, const sst_local_variance_options * o)
 {
+  if( o && o->kradius > LV_RMAX ) return lfail(SST_ERR_UNSUPPORTED, "local variance map: kradius above 16 is not supported");
   sst_local_variance * L = new (std::nothrow) sst_local_variance;
   if( !L ) return lfail(SST_ERR_NOMEM, "out of host memory");
   if( o ) L->o = *o;

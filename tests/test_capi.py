@@ -100,3 +100,23 @@ int main() {
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
     assert out.stdout.startswith("ok")
+
+
+def test_local_variance_host_checks(capi):
+    """option defaults and argument checks of sst_local_variance_* (no GPU work)"""
+    import ctypes as C
+    o = capi.local_variance_options()
+    assert (o.kradius, o.dscale, o.uscale) == (2, 1, 3)
+    h = C.c_void_p()
+    assert capi.lib().sst_local_variance_create(C.byref(h), C.byref(capi.local_variance_options(kradius=17))) == -3
+    assert not h.value
+    assert capi.lib().sst_local_variance_create(C.byref(h), C.byref(capi.local_variance_options(kradius=16))) == 0
+    try:
+        buf = (C.c_uint16 * 64)()
+        lib = capi.lib()
+        assert lib.sst_local_variance_compute(h, None, capi.DEPTH_U16, 1, 8, 8, 16, 128, 1.0, 0, None, None, None) == -1
+        assert lib.sst_local_variance_compute(h, buf, capi.DEPTH_U16, 0, 8, 8, 16, 128, 1.0, 0, None, None, None) == -1
+        assert lib.sst_local_variance_compute(h, buf, 3, 1, 8, 8, 16, 128, 1.0, 0, None, None, None) == -1
+        assert lib.sst_local_variance_compute(h, buf, capi.DEPTH_U16, 2, 8, 8, 8, 128, 1.0, 0, None, None, None) == -1
+    finally:
+        capi.lib().sst_local_variance_destroy(h)
