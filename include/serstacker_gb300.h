@@ -384,6 +384,19 @@ int sst_ser_seek(sst_ser_reader * r, int frame);
  * (0 at the end of the file). */
 int sst_ser_read(sst_ser_reader * r, int n, void * dst, size_t frame_stride, int * frames_read);
 
+/* c_ser_writer (core/io/c_ser_file.h:183-213, c_ser_file.cc:544-712):
+ * create() writes the header of an empty file (LittleEndian field 0 on a
+ * little-endian host, as the reference writes it); write() appends n frames
+ * of the file's format from host memory (frame_stride 0: packed) with their
+ * timestamps (NULL: UINT64_MAX each, the reference's default); the first
+ * frame's timestamp becomes DateTime and DateTime_UTC. close() patches
+ * FrameCount and appends the little-endian timestamp trailer. */
+typedef struct sst_ser_writer sst_ser_writer;
+int sst_ser_writer_create(sst_ser_writer ** out, const char * path, int width, int height, int color_id,
+    int bits_per_plane);
+int sst_ser_write(sst_ser_writer * w, const void * frames, int n, size_t frame_stride, const uint64_t * timestamps);
+int sst_ser_writer_close(sst_ser_writer * w);
+
 /* The stacking loop over frames [first, first + count) of a SER file (count
  * < 0: to the end): frames are read in chunks of `chunk` frames (0: 256) into
  * pinned host buffers, the next chunk from the file while the GPU registers

@@ -10,6 +10,7 @@
  *   sst_gb300::c_local_variance_map_options, c_local_variance_sharpness_measure
  *                                  core/proc/sharpness_measure/c_local_variance_sharpness_measure.h:17-23
  *   sst_gb300::c_ser_reader        core/io/c_ser_file.h:136-174
+ *   sst_gb300::c_ser_writer        core/io/c_ser_file.h:183-213
  * Images are passed as `image_view` (pointer, size, OpenCV depth code,
  * stride) instead of cv::Mat, so this header needs no OpenCV; define
  * SST_GB300_WITH_OPENCV before including it to get cv::Mat overloads.
@@ -376,6 +377,32 @@ public:
 private:
   sst_ser_reader * _h = nullptr;
   sst_ser_info _info {};
+};
+
+/* c_ser_writer (core/io/c_ser_file.h:183-213): create, write frames of the
+ * file's format with their timestamps, close (FrameCount and the trailer). */
+class c_ser_writer {
+public:
+  ~c_ser_writer() { close(); }
+  bool create(const std::string & filename, int image_width, int image_height, int color_id, int bits_per_plane)
+  {
+    close();
+    return sst_ser_writer_create(&_h, filename.c_str(), image_width, image_height, color_id, bits_per_plane) == SST_OK;
+  }
+  bool is_open() const { return _h != nullptr; }
+  bool write(const void * frame, uint64_t ts = UINT64_MAX) { return _h && sst_ser_write(_h, frame, 1, 0, &ts) == SST_OK; }
+#ifdef SST_GB300_WITH_OPENCV
+  bool write(const cv::Mat & image, uint64_t ts = UINT64_MAX) { return image.isContinuous() && write(image.data, ts); }
+#endif
+  bool close()
+  {
+    const bool ok = !_h || sst_ser_writer_close(_h) == SST_OK;
+    _h = nullptr;
+    return ok;
+  }
+
+private:
+  sst_ser_writer * _h = nullptr;
 };
 
 }  // namespace sst_gb300

@@ -134,6 +134,9 @@ def lib():
             "sst_ser_seek": (i, [p, i]),
             "sst_ser_read": (i, [p, i, p, sz, p]),
             "sst_stack_ser": (i, [p, p, p, i, i, i, i, p, i, i, p, p, p, p, p]),
+            "sst_ser_writer_create": (i, [p, C.c_char_p, i, i, i, i]),
+            "sst_ser_write": (i, [p, p, i, sz, p]),
+            "sst_ser_writer_close": (i, [p]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(_lib, name)
@@ -722,6 +725,36 @@ class c_ser_reader:
         if m < 0:
             _check(m, "sst_ser_timestamps")
         return ts[:m]
+
+
+class c_ser_writer:
+    """c_ser_writer (core/io/c_ser_file.h:183-213) over the C ABI."""
+
+    def __init__(self, path: str, width: int, height: int, color_id: int = 0, bits_per_plane: int = 16):
+        self._h = C.c_void_p()
+        _check(lib().sst_ser_writer_create(C.byref(self._h), os.fsencode(path), width, height, color_id,
+                                           bits_per_plane), "sst_ser_writer_create")
+
+    def write(self, frames: np.ndarray, timestamps=None):
+        """appends frames (n, h, w[, c]) in the file's format, with n timestamps or none"""
+        f = np.ascontiguousarray(frames)
+        n = f.shape[0]
+        ts = None if timestamps is None else np.ascontiguousarray(timestamps, np.uint64)
+        if ts is not None and ts.size != n:
+            raise ValueError("one timestamp per frame")
+        _check(lib().sst_ser_write(self._h, _ptr(f), n, 0, _ptr(ts)), "sst_ser_write")
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            self._h = C.c_void_p()
+            _check(_lib.sst_ser_writer_close(h), "sst_ser_writer_close")
+
+    def __del__(self):
+        try:
+            self.close()
+        except SSTError:
+            pass
 
 
 def stack_ser(reg: c_ecch, accs, ser: c_ser_reader, passes: Sequence[int], first: int = 0, count: int = -1,

@@ -392,3 +392,109 @@ extern "C" int sst_stack_ser(sst_ecch * reg, sst_weighted_average * const * acc,
   }
   return SST_OK;
 }
+
+/* ------------------------------------------------------------- SER output */
+
+struct sst_ser_writer {
+  int fd = -1;
+  uint8_t header[kHeaderBytes] = {};
+  int32_t frames = 0;
+  uint64_t date_time = 0;
+  size_t frame_bytes = 0;
+  std::vector<uint64_t> timestamps;
+};
+
+namespace {
+
+void put32(uint8_t * p, int32_t v)
+{
+  for( int i = 0; i < 4; ++i ) p[i] = (uint8_t) ((uint32_t) v >> (8 * i));
+}
+
+void put64(uint8_t * p, uint64_t v)
+{
+  for( int i = 0; i < 8; ++i ) p[i] = (uint8_t) (v >> (8 * i));
+}
+
+bool write_at(int fd, const void * src, size_t bytes, off_t offset)
+{
+  const uint8_t * s = (const uint8_t *) src;
+  while ( bytes > 0 ) {
+    const ssize_t r = pwrite(fd, s, bytes, offset);
+    if( r < 0 ) {
+      if( errno == EINTR ) continue;
+      return false;
+    }
+    s += r, bytes -= (size_t) r, offset += r;
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" int sst_ser_writer_create(sst_ser_writer ** out, const char * path, int width, int height, int color_id,
+    int bits_per_plane)
+{
+  if( !out || !path ) return ser_fail(SST_ERR_INVALID_ARG, "sst_ser_writer_create: NULL argument");
+  *out = nullptr;
+  if( width < 1 || height < 1 || plane_bytes(bits_per_plane) == 0 )
+    return ser_fail(SST_ERR_INVALID_ARG, "unsupported image size or PixelDepthPerPlane");
+  if( !color_id_supported(color_id) ) return ser_fail(SST_ERR_INVALID_ARG, "invalid ColorId " + std::to_string(color_id));
+  sst_ser_writer * w = new (std::nothrow) sst_ser_writer;
+  if( !w ) return ser_fail(SST_ERR_NOMEM, "out of host memory");
+  memcpy(w->header, "LUCAM-RECORDER", 14);
+  put32(w->header + 18, color_id);
+  // LittleEndian written as the reference's writer does: 0 on a little-endian
+  // host, which its reader (and this one) takes as little-endian data
+  put32(w->header + 22, host_little_endian() ? 0 : 1);
+  put32(w->header + 26, width);
+  put32(w->header + 30, height);
+  put32(w->header + 34, bits_per_plane);
+  const int channels = (color_id == 100 || color_id == 101) ? 3 : 1;
+  w->frame_bytes = (size_t) width * height * channels * plane_bytes(bits_per_plane);
+  w->fd = open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
+  if( w->fd < 0 || !write_at(w->fd, w->header, kHeaderBytes, 0) ) {
+    const std::string msg = std::string("create('") + path + "') fails: " + strerror(errno);
+    if( w->fd >= 0 ) close(w->fd);
+    delete w;
+    return ser_fail(SST_ERR_IO, msg);
+  }
+  *out = w;
+  return SST_OK;
+}
+
+extern "C" int sst_ser_write(sst_ser_writer * w, const void * frames, int n, size_t frame_stride,
+    const uint64_t * timestamps)
+{
+  if( !w || (!frames && n > 0) || n < 0 ) return ser_fail(SST_ERR_INVALID_ARG, "sst_ser_write: invalid argument");
+  if( frame_stride == 0 ) frame_stride = w->frame_bytes;
+  if( frame_stride < w->frame_bytes ) return ser_fail(SST_ERR_INVALID_ARG, "frame_stride below the frame size");
+  const uint8_t * s = (const uint8_t *) frames;
+  for( int k = 0; k < n; ++k ) {
+    const off_t at = (off_t) (kHeaderBytes + (size_t) w->frames * w->frame_bytes);
+    if( !write_at(w->fd, s + (size_t) k * frame_stride, w->frame_bytes, at) )
+      return ser_fail(SST_ERR_IO, std::string("write(frame) fails: ") + strerror(errno));
+    const uint64_t ts = timestamps ? timestamps[k] : UINT64_MAX;
+    if( w->frames == 0 ) w->date_time = ts;   // DateTime and DateTime_UTC of the first frame
+    w->timestamps.push_back(ts);
+    ++w->frames;
+  }
+  return SST_OK;
+}
+
+extern "C" int sst_ser_writer_close(sst_ser_writer * w)
+{
+  if( !w ) return SST_OK;
+  int rc = SST_OK;
+  put32(w->header + 38, w->frames);
+  put64(w->header + 162, w->date_time);
+  put64(w->header + 170, w->date_time);
+  std::vector<uint8_t> ts(w->timestamps.size() * 8);
+  for( size_t i = 0; i < w->timestamps.size(); ++i ) put64(ts.data() + 8 * i, w->timestamps[i]);
+  if( !write_at(w->fd, w->header, kHeaderBytes, 0) ||
+      !write_at(w->fd, ts.data(), ts.size(), (off_t) (kHeaderBytes + (size_t) w->frames * w->frame_bytes)) )
+    rc = ser_fail(SST_ERR_IO, std::string("write(SER header / timestamps) fails: ") + strerror(errno));
+  if( close(w->fd) != 0 && rc == SST_OK ) rc = ser_fail(SST_ERR_IO, std::string("close fails: ") + strerror(errno));
+  delete w;
+  return rc;
+}

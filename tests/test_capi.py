@@ -85,10 +85,14 @@ int main() {
   if( ser.read(f) ) return 9;          // past the last frame
   std::vector<uint64_t> ts = ser.timestamps();
   if( ts.size() != 3 || ts[1] != 11 ) return 10;
+  sst_gb300::c_ser_writer wr;
+  if( !wr.create(SER_OUT, 6, 4, 0, 12) || !wr.write(f.data(), 77) || !wr.close() ) return 11;
+  sst_gb300::c_ser_reader back(SER_OUT);
+  if( back.num_frames() != 1 || back.timestamps()[0] != 77 ) return 12;
   std::printf("ok %s\n", sst_version());
   return 0;
 }
-'''.replace("SER_PATH", '"' + str(tmp_path / "t.ser") + '"'))
+'''.replace("SER_PATH", '"' + str(tmp_path / "t.ser") + '"').replace("SER_OUT", '"' + str(tmp_path / "o.ser") + '"'))
     import numpy as np
     from ser_files import write_ser
     frames = (np.arange(3)[:, None, None] * 1000 + np.arange(24).reshape(4, 6)).astype(np.uint16)

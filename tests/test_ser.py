@@ -152,3 +152,33 @@ def test_large_reads_split_over_threads(capi, tmp_path, le_field):
     t = capi.c_ser_reader(str(write_ser(tmp_path / "l.ser", fr[:40], frames_count=80)))
     with pytest.raises(capi.SSTError):
         t.read(80)                                            # truncated: a piece past the end fails
+
+
+def test_writer_round_trip_and_layout(capi, tmp_path):
+    """c_ser_writer: the file equals the reference writer's layout (header with
+    LittleEndian 0, FrameCount and DateTime of the first frame, frames, then
+    the little-endian timestamps) and reads back exactly"""
+    fr = _frames(4, 5, 7, np.uint16, 8)
+    ts = np.array([5, 6, 7, 8], np.uint64) << np.uint64(33)
+    w = capi.c_ser_writer(str(tmp_path / "w.ser"), 7, 5, 0, 12)
+    w.write(fr[:1], ts[:1])
+    w.write(fr[1:], ts[1:])
+    w.close()
+    want = write_ser(tmp_path / "ref.ser", fr, bits=12, timestamps=ts, date_time=int(ts[0]), date_time_utc=int(ts[0]))
+    assert (tmp_path / "w.ser").read_bytes() == want.read_bytes()
+    r = capi.c_ser_reader(str(tmp_path / "w.ser"))
+    assert r.info.frames == 4 and np.array_equal(r.read(4), fr) and np.array_equal(r.timestamps(), ts)
+
+
+def test_writer_defaults_and_checks(capi, tmp_path):
+    rgb = _frames(2, 3, 4 * 3, np.uint8, 9).reshape(2, 3, 4, 3)
+    w = capi.c_ser_writer(str(tmp_path / "x.ser"), 4, 3, 100, 8)
+    w.write(rgb)                                   # no timestamps: UINT64_MAX each
+    w.close()
+    r = capi.c_ser_reader(str(tmp_path / "x.ser"))
+    assert r.info.channels == 3 and np.array_equal(r.read(2), rgb)
+    assert np.array_equal(r.timestamps(), np.full(2, np.iinfo(np.uint64).max, np.uint64))
+    assert r.info.date_time == np.iinfo(np.uint64).max
+    for args in ((0, 3, 0, 16), (4, 3, 5, 16), (4, 3, 0, 40)):
+        with pytest.raises(capi.SSTError):
+            capi.c_ser_writer(str(tmp_path / "y.ser"), *args)
