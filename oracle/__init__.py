@@ -108,6 +108,7 @@ def lib():
             "orc_resize_linear": (None, [p, i, i, p, i, i]),
             "orc_local_variance_size": (i, [i, i, i, i, p, p]),
             "orc_local_variance_map": (i, [p, i, i, i, i, i, d, p, p, p, p]),
+            "orc_average_pyramid_inpaint": (None, [p, p, i, i, i, p, p]),
             "orc_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
             "orc_set_num_threads": (None, [i]),
             "orc_get_num_threads": (i, []),
@@ -457,6 +458,17 @@ def local_variance_map(img, kradius=2, dscale=1, uscale=3, depth_scale=20.0):
     if not ok:
         return None, 0.0
     return out.ravel()[:mw.value * mh.value].reshape(mh.value, mw.value).copy(), q.value
+
+
+def average_pyramid_inpaint(img, mask, max_levels=100):
+    """average_pyramid_inpaint -> (image, mask)"""
+    a = _f64(img)
+    m = np.ascontiguousarray(mask, np.uint8)
+    h, w = a.shape
+    out = np.empty((h, w))
+    om = np.empty((h, w), np.uint8)
+    lib().orc_average_pyramid_inpaint(_ptr(a), _ptr(m), w, h, max_levels, _ptr(out), _ptr(om))
+    return out, om
 
 
 def warp_residual(m: Model, state, img, tmpl, flow=None):

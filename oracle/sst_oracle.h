@@ -194,6 +194,13 @@ int orc_local_variance_size(int w, int h, int dscale, int uscale, int * mw, int 
  * Q = ds^3 sum G^4 / sum G, INTER_LINEAR-upscaled to the image's size when the
  * gradient's size differs from it. Returns 0 (no map, q = 0) when sum G is
  * not positive, else 1 with the map (*mw x *mh, at most w x h) and q. */
+/* average_pyramid_inpaint of a single-channel image with a u8 mask
+ * (non-zero = valid): holes filled from 3 x 3 means over a downstrike /
+ * upject pyramid of at most max_levels levels; the output mask is 255 where
+ * a value was found */
+void orc_average_pyramid_inpaint(const double * src, const uint8_t * mask, int w, int h, int max_levels,
+    double * dst, uint8_t * dstmask);
+
 int orc_local_variance_map(const double * img, int w, int h, int kradius, int dscale, int uscale,
     double depth_scale, double * map, int * mw, int * mh, double * q);
 

@@ -493,3 +493,37 @@ def test_local_variance_map_is_scale_invariant_and_area_reduced(oracle):
     assert abs(q3 - (g ** 4).sum() / g.sum()) < 1e-12 * q3
     want = (g ** 3).reshape(48, 2, 64, 2).mean(axis=(1, 3)) + 0.05 * q3
     assert np.abs(m3 - want).max() < 1e-12 * want.max()
+
+
+def test_average_pyramid_inpaint_known_answers(oracle):
+    rng = np.random.default_rng(3)
+    img = rng.random((24, 20))
+    full = np.full((24, 20), 255, np.uint8)
+    out, om = oracle.average_pyramid_inpaint(img, full)
+    assert np.array_equal(out, img) and np.array_equal(om, full)            # nothing to fill: a copy
+    # nothing to fill from: zeros, yet every pixel comes back valid, since
+    # upject_even marks each copied position valid whether or not its value was
+    out, om = oracle.average_pyramid_inpaint(img, np.zeros_like(full))
+    assert not out.any() and om.min() == 255
+    # a 3 x 3 image with its centre missing: the centre becomes the mean of its 8 neighbours
+    s = np.arange(9.0).reshape(3, 3) ** 2
+    m = np.full((3, 3), 255, np.uint8)
+    m[1, 1] = 0
+    out, om = oracle.average_pyramid_inpaint(s, m)
+    assert abs(out[1, 1] - (s.sum() - s[1, 1]) / 8) < 1e-12 and om.min() == 255
+    assert np.array_equal(np.delete(out.ravel(), 4), np.delete(s.ravel(), 4))
+    # a constant image keeps its value over a large hole; a linear ramp over a one-pixel hole
+    c = np.full((40, 33), 2.5)
+    m = np.full((40, 33), 255, np.uint8)
+    m[5:30, 3:25] = 0
+    out, om = oracle.average_pyramid_inpaint(c, m)
+    assert np.abs(out - 2.5).max() < 1e-12 and om.min() == 255
+    y, x = np.mgrid[0:17, 0:19].astype(np.float64)
+    ramp = 0.5 * x - 0.25 * y
+    m = np.full((17, 19), 255, np.uint8)
+    m[8, 9] = 0
+    out, _ = oracle.average_pyramid_inpaint(ramp, m)
+    assert abs(out[8, 9] - ramp[8, 9]) < 1e-12
+    # no pyramid levels: the holes stay empty
+    out, om = oracle.average_pyramid_inpaint(ramp, m, max_levels=0)
+    assert out[8, 9] == 0 and om[8, 9] == 0 and om.sum() == 255 * (17 * 19 - 1)
