@@ -398,7 +398,8 @@ int sst_ser_write(sst_ser_writer * w, const void * frames, int n, size_t frame_s
 int sst_ser_writer_close(sst_ser_writer * w);
 
 /* The stacking loop over frames [first, first + count) of a SER file (count
- * < 0: to the end): frames are read in chunks of `chunk` frames (0: 256) into
+ * < 0: to the end): frames are read in chunks of `chunk` frames (0: 256; at
+ * most 512 MB of frames per chunk) into
  * pinned host buffers, the next chunk from the file while the GPU registers
  * and stacks the current one, scaled by 1 / 2^bits_per_plane as
  * read_input_frame does (c_image_processing_pipeline.cc:1180-1190), and

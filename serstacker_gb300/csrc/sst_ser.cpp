@@ -351,6 +351,8 @@ extern "C" int sst_stack_ser(sst_ecch * reg, sst_weighted_average * const * acc,
   count = std::min(count, in.frames - first);
   if( count == 0 ) return SST_OK;
   if( chunk <= 0 ) chunk = 256;
+  // each of the two pinned buffers holds at most 512 MB of frames
+  chunk = std::min(chunk, (int) std::max<size_t>(1, ((size_t) 512 << 20) / ser->frame_bytes));
   chunk = std::min(chunk, count);
   // read_input_frame: integer frames are scaled by 1 / 2^bpp
   const double scale = in.depth == SST_DEPTH_F32 ? 1.0 : 1.0 / (double) (1u << in.bits_per_plane);

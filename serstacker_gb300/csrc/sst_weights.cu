@@ -594,7 +594,7 @@ struct sst_local_variance {
   DevBuf ax_i, ax_w, ay_i, ay_w;          // INTER_AREA taps (gradient grid -> small map)
   DevBuf ux, uy;                          // INTER_LINEAR tap pairs (small map -> frame grid)
   int ax_k = 0, ay_k = 0;
-  int tab_key[4] = { -1, -1, -1, -1 };
+  int tab_key[6] = { -1, -1, -1, -1, -1, -1 };   // w, h, gw, gh, mw, mh of the uploaded tap tables
   ~sst_local_variance()
   {
     for( DevBuf * b : { &lv[0], &lv[1], &p3, &small, &part, &q, &addq, &has, &stage, &maps, &ax_i, &ax_w, &ay_i, &ay_w,
@@ -627,7 +627,7 @@ void lv_geometry(sst_local_variance * L, int w, int h)
 
 int lv_tables(sst_local_variance * L, cudaStream_t st)
 {
-  const int key[4] = { L->w * 65536 + L->h, L->gw * 65536 + L->gh, L->mw * 65536 + L->mh, 0 };
+  const int key[6] = { L->w, L->h, L->gw, L->gh, L->mw, L->mh };
   if( !memcmp(key, L->tab_key, sizeof(key)) ) return SST_OK;
   std::vector<int> i;
   std::vector<float> f;
