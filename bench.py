@@ -247,6 +247,10 @@ def main():
     ap.add_argument("--roi-method", choices=["fa", "lm"], default="fa")
     ap.add_argument("--roi-sample", type=int, default=8, help="crops checked against the oracle")
     ap.add_argument("--flow-sample", type=int, default=32, help="frames checked against the oracle (flow)")
+    ap.add_argument("--ser-file", action="store_true",
+                    help="mono workload: also write the frames to a SER file and time sst_stack_ser on it")
+    ap.add_argument("--ser-dir", default="/tmp", help="directory of the --ser-file leg's temporary file")
+    ap.add_argument("--ser-chunk", type=int, default=256, help="frames per file chunk of the --ser-file leg")
     ap.add_argument("--weighting", type=int, choices=sorted(WEIGHTING), default=1,
                     help="stacking weights of the mono / bayer workloads (1, the Laplacian-energy frame weight, "
                          "is the headline; the oracle's cpu_baseline implements only that one)")
@@ -359,6 +363,7 @@ def main():
         e2e = run_e2e(args, ws, n, frames, reg, acc, passes, frame_bytes)
     plain_fps = run_plain(args, n, frames, ref, opts, passes) if not args.no_plain else None
     pn = min(args.plain_frames, n)
+    ser_leg = run_ser_file(args, n, frames, ref, opts, passes) if args.ser_file and rank == 0 else None
 
     # ---------------------------------------------------------- CPU baseline
     cpu = None
@@ -386,6 +391,8 @@ def main():
                 "accuracy": {"warp_rms_vs_truth_px_median": med_rms, "warp_rms_vs_truth_px_max": max_rms,
                              "frames_ok": int((res["status"] == 0).sum())},
                 "levels": level_table}
+        if ser_leg is not None:
+            line["ser_file"] = ser_leg
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -427,6 +434,49 @@ def run_e2e(args, ws, n, frames, reg, acc, passes, frame_bytes):
     return {"value": ws * n / (e2e_ms / 1000.0), "unit": "frames/s", "h2d_bytes_per_step": n * frame_bytes,
             "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
             "api": "sst_stack_frames (host pinned) + sst_weighted_average_compute"}
+
+
+def run_ser_file(args, n, frames, ref, opts, passes):
+    """The workload written to a SER file (16-bit mono, read back from the page
+    cache) and stacked by sst_stack_ser: file reads into pinned chunks overlap
+    registration + stacking. Frames are scaled by 1 / 2^16 as read_input_frame
+    does, so the reference is set with that scale. Returns the leg's figures."""
+    import torch
+    from serstacker_gb300 import capi as C
+    path = os.path.join(args.ser_dir, f"sst_bench_{os.getpid()}.ser")
+    host = frames.cpu().numpy().view(np.uint16)
+    w = C.c_ser_writer(path, WIDTH, HEIGHT, 0, 16)
+    try:
+        w.write(host)
+        w.close()
+        del host
+        reg_s = C.c_ecch(opts)
+        reg_s.set_reference_image(ref, scale=1.0 / 65536)
+        acc_s = C.c_weigthed_average(WIDTH, HEIGHT)
+        passes_s = list(passes)
+
+        def step():
+            acc_s.clear()
+            ser = C.c_ser_reader(path)
+            out = C.stack_ser(reg_s, acc_s, ser, passes_s, chunk=args.ser_chunk, weighting=_weighting)
+            ser.close()
+            return out
+
+        for _ in range(max(1, args.warmup)):
+            out = step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            out = step()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    finally:
+        w.close()
+        if os.path.exists(path):
+            os.remove(path)
+    return {"value": n / (ms / 1000.0), "unit": "frames/s", "ms_per_step": ms, "file_bytes": 178 + n * WIDTH * HEIGHT * 2
+            + n * 8, "chunk": args.ser_chunk, "frames_ok": int((out["status"] == 0).sum()),
+            "api": "sst_stack_ser (16-bit mono SER file in the page cache)"}
 
 
 def run_plain(args, n, frames, ref, opts, passes):
