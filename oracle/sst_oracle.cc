@@ -1,7 +1,7 @@
 /*
  * sst_oracle.cc -- FP64 restatement of the ECC / c_ecch / stacking hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the parity checker and the timed CPU baseline.
+ * TEST INFRASTRUCTURE ONLY: the oracle of the parity tests and the timed CPU baseline.
  * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use it.
  *
  * Reference anchors (core/proc/image_registration/ecc2.cc unless stated):

@@ -2,7 +2,7 @@
  * sst_oracle.h -- FP64 CPU restatement of SerStacker's frame registration +
  * stacking hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the parity checker for the
+ * TEST INFRASTRUCTURE ONLY. This library is the oracle of the parity tests of the
  * CUDA path and the timed CPU baseline; the product never links, loads or
  * calls it. It restates the algorithms of the reference files
  *   core/proc/image_registration/ecc2.cc

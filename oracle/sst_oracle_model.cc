@@ -1,7 +1,7 @@
 /*
  * sst_oracle_model.cc -- FP64 restatement of the c_image_transform family.
  *
- * TEST INFRASTRUCTURE ONLY (parity checker, never part of the product).
+ * TEST INFRASTRUCTURE ONLY (the oracle of the parity tests, never part of the product).
  *
  * Follows core/proc/image_registration/c_image_transform.cc:
  *   translation    :   80-269   (create_remap 150-170, eps 136-139, SD 262-269)

@@ -1,6 +1,6 @@
 /*
  * sst_oracle_post.cc -- FP64 restatement of the stacking pipeline's
- * post-stack hole filling (test infrastructure only: the checker for a GPU
+ * post-stack hole filling (test infrastructure only: the oracle for a GPU
  * implementation, never shipped).
  *
  * average_pyramid_inpaint (core/proc/inpaint/average_pyramid_inpaint.cc:

@@ -1,7 +1,7 @@
 /*
  * sst_oracle_weights.cc -- FP64 restatement of the local-variance sharpness
  * map used as per-pixel stacking weights. Test infrastructure only: this is
- * the checker of the CUDA weight maps, never the thing measured or shipped.
+ * the oracle of the CUDA weight maps, never the thing measured or shipped.
  *
  * Follows compute_local_variance_map
  * (core/proc/sharpness_measure/c_local_variance_sharpness_measure.cc:193-249)
