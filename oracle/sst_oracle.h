@@ -10,6 +10,8 @@
  *   core/proc/image_registration/c_frame_registration.cc
  *   core/average/c_frame_accumulation.cc
  *   core/io/debayer.cc
+ *   core/proc/sharpness_measure/c_local_variance_sharpness_measure.cc
+ *   core/proc/inpaint/average_pyramid_inpaint.cc, core/proc/downstrike.cc
  * in double precision. OpenCV primitives the reference calls (sepFilter2D,
  * pyrDown, remap, meanStdDev, erode, resize NEAREST, Cholesky solve) are
  * re-implemented from their documented semantics; bilinear sampling is exact
