@@ -1,7 +1,9 @@
 """ctypes binding of the C ABI in ``include/serstacker_gb300.h``.
 
 Thin Python classes with the reference's names (``c_ecch``,
-``c_weigthed_average``) over ``libsst_gb300.so``. Host numpy buffers are
+``c_weigthed_average``, ``c_bayer_average``, ``c_eccflow``,
+``c_local_variance_sharpness_measure``, ``c_ser_reader``, ``c_ser_writer``)
+over ``libsst_gb300.so``. Host numpy buffers are
 passed with ``on_device=0``; device buffers (e.g. torch CUDA tensors) with
 ``on_device=1`` and their ``data_ptr()``. Errors raise ``SSTError`` carrying
 ``sst_last_error()``. There is no CPU fallback: if the library cannot be
@@ -25,6 +27,7 @@ FA, IC, LM, ICLM = range(4)
 BORDER_CONSTANT, BORDER_REPLICATE, BORDER_REFLECT, BORDER_REFLECT101 = 0, 1, 2, 4
 COLORID_BAYER_RGGB, COLORID_BAYER_GRBG, COLORID_BAYER_GBRG, COLORID_BAYER_BGGR = 8, 9, 10, 11
 DEPTH_U8, DEPTH_U16, DEPTH_F32 = 0, 2, 5
+DEPTH_S32, DEPTH_F64 = 4, 6           # reported by SER files only
 
 _NP_DEPTH = {np.dtype(np.uint8): DEPTH_U8, np.dtype(np.uint16): DEPTH_U16, np.dtype(np.float32): DEPTH_F32}
 
@@ -698,9 +701,9 @@ class c_ser_reader:
     def dtype(self):
         if self.info.depth == DEPTH_F32:
             return np.float32
-        if self.info.bits_per_plane == -64:
+        if self.info.depth == DEPTH_F64:
             return np.float64
-        if self.info.bytes_per_plane == 4:
+        if self.info.depth == DEPTH_S32:
             return np.int32
         return _SER_DTYPE[self.info.bytes_per_plane]
 
