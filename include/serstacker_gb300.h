@@ -289,6 +289,19 @@ int sst_local_variance_compute(sst_local_variance * h, const void * frames, int 
  * the options of sst_stack_frames' weighting 3 (defaults until set). */
 int sst_weighted_average_set_local_variance(sst_weighted_average * h, const sst_local_variance_options * opts);
 
+/* ------------------------------------------------------ post-stack steps */
+
+/* average_pyramid_inpaint (core/proc/inpaint/average_pyramid_inpaint.cc:
+ * 18-126), applied by the stacking pipeline to the accumulated image and its
+ * mask (c_image_stacking_pipeline.cc:763-767, max_levels 100): holes (mask 0)
+ * are filled from 3 x 3 means over a downstrike / upject pyramid of at most
+ * max_levels levels. dst / dst_mask receive the filled image and its mask
+ * (255 where a value was found; a mask without holes is returned as it is).
+ * Strides in bytes (0: packed). */
+int sst_average_pyramid_inpaint(const float * src, size_t src_stride, const uint8_t * mask, size_t mask_stride,
+    int width, int height, int max_levels, float * dst, size_t dst_stride, uint8_t * dst_mask,
+    size_t dst_mask_stride, int on_device, void * stream);
+
 /* ------------------------------------------------------- stacking pipeline */
 
 /* The per-frame body of the stacking pipeline for n frames

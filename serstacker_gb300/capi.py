@@ -140,6 +140,7 @@ def lib():
             "sst_ser_writer_create": (i, [p, C.c_char_p, i, i, i, i]),
             "sst_ser_write": (i, [p, p, i, sz, p]),
             "sst_ser_writer_close": (i, [p]),
+            "sst_average_pyramid_inpaint": (i, [p, sz, p, sz, i, i, i, p, sz, p, sz, i, p]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(_lib, name)
@@ -774,6 +775,19 @@ def stack_ser(reg: c_ecch, accs, ser: c_ser_reader, passes: Sequence[int], first
                                weighting, _ptr(outputs["params"]), _ptr(outputs["status"]), _ptr(outputs["rho"]),
                                _ptr(outputs["weight"]), None), "sst_stack_ser")
     return outputs
+
+
+def average_pyramid_inpaint(image: np.ndarray, mask: np.ndarray, max_levels: int = 100):
+    """average_pyramid_inpaint of a float32 image and its u8 mask -> (image, mask)"""
+    img = np.ascontiguousarray(image, np.float32)
+    msk = np.ascontiguousarray(mask, np.uint8)
+    h, w = img.shape
+    out = np.zeros((h, w), np.float32)
+    om = np.zeros((h, w), np.uint8)
+    _check(lib().sst_average_pyramid_inpaint(_ptr(img), img.strides[0], _ptr(msk), msk.strides[0], w, h, max_levels,
+                                             _ptr(out), out.strides[0], _ptr(om), om.strides[0], 0, None),
+           "sst_average_pyramid_inpaint")
+    return out, om
 
 
 def remap(src: np.ndarray, motion_type: int, params, dst_shape=None, border=BORDER_REFLECT101, scale=1.0):

@@ -124,3 +124,17 @@ def test_local_variance_host_checks(capi):
         assert lib.sst_local_variance_compute(h, buf, capi.DEPTH_U16, 2, 8, 8, 8, 128, 1.0, 0, None, None, None) == -1
     finally:
         capi.lib().sst_local_variance_destroy(h)
+
+
+def test_inpaint_argument_checks(capi):
+    """sst_average_pyramid_inpaint rejects bad arguments before any GPU work"""
+    import ctypes as C
+    lib = capi.lib()
+    img = (C.c_float * 16)()
+    msk = (C.c_uint8 * 16)()
+    out = (C.c_float * 16)()
+    om = (C.c_uint8 * 16)()
+    assert lib.sst_average_pyramid_inpaint(None, 0, msk, 0, 4, 4, 100, out, 0, om, 0, 0, None) == -1
+    assert lib.sst_average_pyramid_inpaint(img, 0, msk, 0, 0, 4, 100, out, 0, om, 0, 0, None) == -1
+    assert lib.sst_average_pyramid_inpaint(img, 8, msk, 0, 4, 4, 100, out, 0, om, 0, 0, None) == -1   # stride < row
+    assert lib.sst_average_pyramid_inpaint(img, 18, msk, 0, 4, 4, 100, out, 0, om, 0, 0, None) == -1  # unaligned

@@ -1,0 +1,64 @@
+"""Post-stack hole filling on the GPU (sst_average_pyramid_inpaint) against
+the FP64 oracle of average_pyramid_inpaint (average_pyramid_inpaint.cc:
+18-126). Tolerance: 2e-6 of the image's largest magnitude (FP32 3 x 3 means
+over the pyramid against FP64); masks exact."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-6
+
+
+def _case(h, w, kind, seed):
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    img = (1000 + 300 * np.sin(x / 9) * np.cos(y / 13) + rng.standard_normal((h, w))).astype(np.float32)
+    if kind == "ring":          # the master frame's uncovered border and a hole in the middle
+        r = np.hypot(x - w / 2, y - h / 2)
+        mask = ((r < 0.42 * (w + h)) & (r > 30)).astype(np.uint8) * 255
+    elif kind == "blobs":
+        mask = np.full((h, w), 255, np.uint8)
+        mask[20:90, 40:200] = 0
+        mask[150:, 300:] = 0
+        mask[:, :3] = 0
+    elif kind == "sparse":
+        mask = (rng.random((h, w)) > 0.97).astype(np.uint8) * 255
+    elif kind == "frac":        # mask values other than 0 / 255 weigh the means
+        mask = (rng.integers(1, 256, (h, w)) * (rng.random((h, w)) > 0.5)).astype(np.uint8)
+    elif kind == "none":
+        mask = np.full((h, w), 255, np.uint8)
+    elif kind == "empty":
+        mask = np.zeros((h, w), np.uint8)
+    else:
+        mask = (rng.random((h, w)) > 0.5).astype(np.uint8) * 255
+    return img, mask
+
+
+@pytest.mark.parametrize("h,w,kind", [
+    (960, 1280, "ring"), (277, 333, "blobs"), (64, 64, "sparse"), (129, 65, "frac"), (300, 200, "none"),
+    (33, 47, "empty"), (1, 17, "rand"), (2, 2, "rand"), (5, 1, "rand"), (31, 2, "rand")])
+@pytest.mark.parametrize("max_levels", [100, 3, 0])
+def test_inpaint_matches_oracle(gpu, oracle, h, w, kind, max_levels):
+    img, mask = _case(h, w, kind, seed=h * 7 + w)
+    got, gm = gpu.average_pyramid_inpaint(img, mask, max_levels)
+    want, wm = oracle.average_pyramid_inpaint(img.astype(np.float64), mask, max_levels)
+    assert np.array_equal(gm, wm)
+    err = np.abs(got.astype(np.float64) - want).max()
+    assert err <= TOL * max(np.abs(want).max(), 1.0), err
+
+
+def test_inpaint_device_buffers(gpu, oracle):
+    import torch
+    C = gpu
+    img, mask = _case(130, 170, "blobs", 4)
+    s = torch.from_numpy(img).cuda()
+    m = torch.from_numpy(mask).cuda()
+    d = torch.zeros_like(s)
+    dm = torch.zeros_like(m)
+    C._check(C.lib().sst_average_pyramid_inpaint(s.data_ptr(), 170 * 4, m.data_ptr(), 170, 170, 130, 100,
+                                                 d.data_ptr(), 170 * 4, dm.data_ptr(), 170, 1, None), "inpaint")
+    torch.cuda.synchronize()
+    want, wm = oracle.average_pyramid_inpaint(img.astype(np.float64), mask, 100)
+    assert np.array_equal(dm.cpu().numpy(), wm)
+    assert np.abs(d.cpu().numpy().astype(np.float64) - want).max() <= TOL * np.abs(want).max()
