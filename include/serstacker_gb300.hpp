@@ -11,6 +11,7 @@
  *                                  core/proc/sharpness_measure/c_local_variance_sharpness_measure.h:17-23
  *   sst_gb300::c_ser_reader        core/io/c_ser_file.h:136-174
  *   sst_gb300::c_ser_writer        core/io/c_ser_file.h:183-213
+ *   sst_gb300::average_pyramid_inpaint  core/proc/inpaint/average_pyramid_inpaint.h:14-20
  * Images are passed as `image_view` (pointer, size, OpenCV depth code,
  * stride) instead of cv::Mat, so this header needs no OpenCV; define
  * SST_GB300_WITH_OPENCV before including it to get cv::Mat overloads.
@@ -264,6 +265,23 @@ private:
   sst_weighted_average * _h = nullptr;
   int _w = 0, _hh = 0;
 };
+
+/* average_pyramid_inpaint (core/proc/inpaint/average_pyramid_inpaint.h:14-20)
+ * on the GPU for a host image and mask of width x height (packed rows), in
+ * place: the stacking pipeline's fill of the master frame's holes */
+inline bool average_pyramid_inpaint(std::vector<float> & image, std::vector<uint8_t> & mask, int width, int height,
+    int max_levels = 100)
+{
+  if( image.size() != (size_t) width * height || mask.size() != image.size() ) return false;
+  std::vector<float> out(image.size());
+  std::vector<uint8_t> om(mask.size());
+  if( sst_average_pyramid_inpaint(image.data(), 0, mask.data(), 0, width, height, max_levels, out.data(), 0,
+          om.data(), 0, 0, nullptr) != SST_OK )
+    return false;
+  image.swap(out);
+  mask.swap(om);
+  return true;
+}
 
 /* c_local_variance_map_options (c_local_variance_sharpness_measure.h:17-23) */
 struct c_local_variance_map_options {
