@@ -11,7 +11,7 @@
  *                                  core/proc/sharpness_measure/c_local_variance_sharpness_measure.h:17-23
  *   sst_gb300::c_ser_reader        core/io/c_ser_file.h:136-174
  *   sst_gb300::c_ser_writer        core/io/c_ser_file.h:183-213
- *   sst_gb300::average_pyramid_inpaint  core/proc/inpaint/average_pyramid_inpaint.h:14-20
+ *   sst_gb300::average_pyramid_inpaint  core/proc/inpaint/average_pyramid_inpaint.h:14-18
  * Images are passed as `image_view` (pointer, size, OpenCV depth code,
  * stride) instead of cv::Mat, so this header needs no OpenCV; define
  * SST_GB300_WITH_OPENCV before including it to get cv::Mat overloads.
@@ -266,7 +266,7 @@ private:
   int _w = 0, _hh = 0;
 };
 
-/* average_pyramid_inpaint (core/proc/inpaint/average_pyramid_inpaint.h:14-20)
+/* average_pyramid_inpaint (core/proc/inpaint/average_pyramid_inpaint.h:14-18)
  * on the GPU for a host image and mask of width x height (packed rows), in
  * place: the stacking pipeline's fill of the master frame's holes */
 inline bool average_pyramid_inpaint(std::vector<float> & image, std::vector<uint8_t> & mask, int width, int height,
