@@ -289,6 +289,20 @@ int sst_local_variance_compute(sst_local_variance * h, const void * frames, int 
  * the options of sst_stack_frames' weighting 3 (defaults until set). */
 int sst_weighted_average_set_local_variance(sst_weighted_average * h, const sst_local_variance_options * opts);
 
+/* ---------------------------------------------------- input calibration */
+
+/* read_input_frame's dark / flat calibration of raw frames
+ * (c_image_processing_pipeline.cc:1124-1162), for n device frames into n
+ * device FP32 frames: x = raw * scale (1 / 2^bpp), minus dark (when not
+ * NULL), then x * 5 / flat (when not NULL): the reference passes the image
+ * depth, CV_32F = 5, as cv::divide's scale argument. dark / flat are device
+ * FP32 planes of the frame size. Strides in bytes (0: packed for dark, flat
+ * and out). Enqueued on `stream`; the output feeds sst_stack_frames as
+ * SST_DEPTH_F32 frames with scale 1. */
+int sst_calibrate_frames(const void * frames, int depth, int n, int width, int height, size_t row_stride,
+    size_t frame_stride, double scale, const float * dark, size_t dark_stride, const float * flat, size_t flat_stride,
+    float * out, size_t out_row_stride, size_t out_frame_stride, void * stream);
+
 /* ------------------------------------------------------ post-stack steps */
 
 /* average_pyramid_inpaint (core/proc/inpaint/average_pyramid_inpaint.cc:

@@ -141,6 +141,7 @@ def lib():
             "sst_ser_write": (i, [p, p, i, sz, p]),
             "sst_ser_writer_close": (i, [p]),
             "sst_average_pyramid_inpaint": (i, [p, sz, p, sz, i, i, i, p, sz, p, sz, i, p]),
+            "sst_calibrate_frames": (i, [p, i, i, i, i, sz, sz, d, p, sz, p, sz, p, sz, sz, p]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(_lib, name)
@@ -775,6 +776,21 @@ def stack_ser(reg: c_ecch, accs, ser: c_ser_reader, passes: Sequence[int], first
                                weighting, _ptr(outputs["params"]), _ptr(outputs["status"]), _ptr(outputs["rho"]),
                                _ptr(outputs["weight"]), None), "sst_stack_ser")
     return outputs
+
+
+def calibrate_frames(frames, scale: float, dark=None, flat=None):
+    """sst_calibrate_frames on torch CUDA tensors: frames (n, h, w) u8 / int16
+    (u16 bits) / f32, dark and flat (h, w) f32 or None -> (n, h, w) f32"""
+    import torch
+    n, h, w = frames.shape
+    depth = {torch.uint8: DEPTH_U8, torch.int16: DEPTH_U16, torch.float32: DEPTH_F32}[frames.dtype]
+    es = frames.element_size()
+    out = torch.empty((n, h, w), dtype=torch.float32, device=frames.device)
+    _check(lib().sst_calibrate_frames(frames.data_ptr(), depth, n, w, h, frames.stride(1) * es, frames.stride(0) * es,
+                                      scale, None if dark is None else dark.data_ptr(), 0,
+                                      None if flat is None else flat.data_ptr(), 0, out.data_ptr(), 0, 0, None),
+           "sst_calibrate_frames")
+    return out
 
 
 def average_pyramid_inpaint(image: np.ndarray, mask: np.ndarray, max_levels: int = 100):

@@ -138,3 +138,13 @@ def test_inpaint_argument_checks(capi):
     assert lib.sst_average_pyramid_inpaint(img, 0, msk, 0, 0, 4, 100, out, 0, om, 0, 0, None) == -1
     assert lib.sst_average_pyramid_inpaint(img, 8, msk, 0, 4, 4, 100, out, 0, om, 0, 0, None) == -1   # stride < row
     assert lib.sst_average_pyramid_inpaint(img, 18, msk, 0, 4, 4, 100, out, 0, om, 0, 0, None) == -1  # unaligned
+
+
+def test_calibration_argument_checks(capi):
+    """sst_calibrate_frames rejects bad arguments before any GPU work"""
+    lib = capi.lib()
+    assert lib.sst_calibrate_frames(None, capi.DEPTH_U16, 1, 8, 8, 16, 128, 1.0, None, 0, None, 0, 1, 0, 0, None) == -1
+    assert lib.sst_calibrate_frames(1, capi.DEPTH_U16, 0, 8, 8, 16, 128, 1.0, None, 0, None, 0, 1, 0, 0, None) == -1
+    assert lib.sst_calibrate_frames(1, 3, 1, 8, 8, 16, 128, 1.0, None, 0, None, 0, 1, 0, 0, None) == -1
+    assert lib.sst_calibrate_frames(1, capi.DEPTH_U16, 2, 8, 8, 16, 100, 1.0, None, 0, None, 0, 1, 0, 0, None) == -1
+    assert lib.sst_calibrate_frames(1, capi.DEPTH_U16, 1, 8, 8, 15, 128, 1.0, None, 0, None, 0, 1, 0, 0, None) == -1

@@ -1,7 +1,13 @@
-"""Post-stack hole filling on the GPU (sst_average_pyramid_inpaint) against
-the FP64 oracle of average_pyramid_inpaint (average_pyramid_inpaint.cc:
-18-126). Tolerance: 2e-6 of the image's largest magnitude (FP32 3 x 3 means
-over the pyramid against FP64); masks exact."""
+"""The steps on either side of the stacking loop, on the GPU.
+
+Post-stack hole filling (sst_average_pyramid_inpaint) against the FP64
+oracle of average_pyramid_inpaint (average_pyramid_inpaint.cc:18-126):
+2e-6 of the image's largest magnitude (FP32 3 x 3 means over the pyramid
+against FP64), masks exact.
+
+Dark / flat calibration of raw frames (sst_calibrate_frames,
+c_image_processing_pipeline.cc:1124-1162) against the same sequence of
+rounded FP32 operations in numpy: bitwise."""
 import numpy as np
 import pytest
 
@@ -62,3 +68,28 @@ def test_inpaint_device_buffers(gpu, oracle):
     want, wm = oracle.average_pyramid_inpaint(img.astype(np.float64), mask, 100)
     assert np.array_equal(dm.cpu().numpy(), wm)
     assert np.abs(d.cpu().numpy().astype(np.float64) - want).max() <= TOL * np.abs(want).max()
+
+
+@pytest.mark.parametrize("dtype,scale", [(np.uint16, 1.0 / 4096), (np.uint8, 1.0 / 256), (np.float32, 1.0)])
+@pytest.mark.parametrize("use_dark,use_flat", [(True, True), (True, False), (False, True), (False, False)])
+def test_calibration_is_the_reference_sequence_in_fp32(gpu, dtype, scale, use_dark, use_flat):
+    import torch
+    rng = np.random.default_rng(11)
+    n, h, w = 3, 37, 70
+    if dtype == np.float32:
+        raw = rng.random((n, h, w)).astype(np.float32)
+        t = torch.from_numpy(raw).cuda()
+    else:
+        raw = rng.integers(0, 4096 if dtype == np.uint16 else 256, (n, h, w)).astype(dtype)
+        t = torch.from_numpy(raw.view(np.int16) if dtype == np.uint16 else raw).cuda()
+    dark = (rng.random((h, w)) * 0.05).astype(np.float32)
+    flat = (0.5 + rng.random((h, w))).astype(np.float32)
+    out = gpu.calibrate_frames(t, scale, torch.from_numpy(dark).cuda() if use_dark else None,
+                               torch.from_numpy(flat).cuda() if use_flat else None).cpu().numpy()
+    want = raw.astype(np.float32) * np.float32(scale)
+    if use_dark:
+        want = want - dark
+    if use_flat:
+        want = (want * np.float32(5)) / flat
+    assert want.dtype == np.float32
+    assert np.array_equal(out, want)
