@@ -292,7 +292,7 @@ int sst_weighted_average_set_local_variance(sst_weighted_average * h, const sst_
 /* ---------------------------------------------------- input calibration */
 
 /* read_input_frame's dark / flat calibration of raw frames
- * (c_image_processing_pipeline.cc:1124-1162), for n device frames into n
+ * (c_image_stacking_pipeline_base.cc:142-183), for n device frames into n
  * device FP32 frames: x = raw * scale (1 / 2^bpp), minus dark (when not
  * NULL), then x * 5 / flat (when not NULL): the reference passes the image
  * depth, CV_32F = 5, as cv::divide's scale argument. dark / flat are device
@@ -429,7 +429,7 @@ int sst_ser_writer_close(sst_ser_writer * w);
  * most 512 MB of frames per chunk) into
  * pinned host buffers, the next chunk from the file while the GPU registers
  * and stacks the current one, scaled by 1 / 2^bits_per_plane as
- * read_input_frame does (c_image_processing_pipeline.cc:1180-1190), and
+ * read_input_frame does (c_image_stacking_pipeline_base.cc:270-275), and
  * handed to sst_stack_frames (mono: acc[0]) or sst_stack_bayer_frames
  * (RGGB-family 16-bit Bayer: acc[0..3]). Outputs as those calls, for the
  * count frames (host memory). */
@@ -631,11 +631,11 @@ int sst_state_merge(float * dst, const float * src, int groups, size_t plane);
  * accumulators with OpenCV and never runs on a GPU.
  *
  * It exists for callers that cannot let the library call cudaMalloc:
- *   - code that issues the call while its stream is being captured into a
- *     CUDA graph (cudaMalloc is not allowed during capture);
- *   - hosts that own all device memory through their own pool or arena;
+ *   - hosts that own all device memory through their own pool or arena (an
+ *     allocation behind their back breaks their accounting, or fails once
+ *     the pool has reserved the device);
  *   - real-time capture loops that cannot afford cudaMalloc's implicit
- *     device synchronisation.
+ *     device-wide synchronisation.
  * It warps, weights and accumulates n device-resident frames exactly like
  * sst_weighted_average_add_warped_batch (same kernels), but allocates
  * nothing: the per-frame scratch (warp coefficients and effective weights)
@@ -650,11 +650,16 @@ int sst_state_merge(float * dst, const float * src, int groups, size_t plane);
  * weights (n entries each) may be NULL. n > SST_NOALLOC_MAX_FRAMES is
  * rejected with SST_ERR_INVALID_ARG.
  *
- * The first call on each device looks up the scratch array's device address
- * (cudaGetSymbolAddress) with that device current: make that first call
- * before capturing a stream. All calls share the one array: calls whose work
- * can overlap on the GPU (e.g. on unordered streams) race and must not be
- * issued concurrently. */
+ * The call returns once its work on `stream` has finished: it clears a
+ * device word before the launch and reads it back after it. If a bounded
+ * wait of the stacking kernel for a staged tile copy gave up, the call
+ * returns SST_ERR_TIMEOUT and acc_state is invalid (rebuild it).
+ *
+ * The first call on each device looks up the device addresses of the
+ * scratch array and of that word (cudaGetSymbolAddress) with that device
+ * current: make that first call before capturing any stream. All calls share
+ * the one array: calls whose work can overlap on the GPU (e.g. on unordered
+ * streams) race and must not be issued concurrently. */
 int sst_weighted_average_add_warped_batch_noalloc(const void * frames, int depth, int n,
     int src_width, int src_height, size_t row_stride, size_t frame_stride, double scale,
     const sst_motion_model * model, const float * params, const int32_t * status, const float * weights,

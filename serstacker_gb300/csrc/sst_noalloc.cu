@@ -4,10 +4,10 @@
  * sst_weighted_average_add_warped_batch() keeps its per-frame scratch (the
  * FP32 warp coefficients and the effective frame weights) in buffers the
  * accumulator object allocates with cudaMalloc. Some callers cannot allow
- * that: code that runs while a CUDA stream is being captured into a graph
- * (cudaMalloc is not permitted during capture), hosts that own every byte of
- * device memory through their own pool or arena, and real-time capture loops
- * that must not pay cudaMalloc's implicit device synchronisation. For them,
+ * that: hosts that own every byte of device memory through their own pool or
+ * arena (a cudaMalloc behind their back breaks their accounting, or fails
+ * when the pool has reserved the device), and real-time capture loops that
+ * must not pay cudaMalloc's implicit device-wide synchronisation. For them,
  * sst_weighted_average_add_warped_batch_noalloc() runs the same kernels with
  * that scratch placed in a fixed file-scope device array, and the caller
  * passes the accumulator planes it owns.
@@ -16,7 +16,11 @@
  * that loads the library, until the process exits. Every call shares it:
  * calls whose work overlaps on the GPU (different streams, no ordering) race
  * on it and must not be issued. Each call writes the scratch entries of its
- * n frames before reading them, so nothing has to start at zero.
+ * n frames before reading them, so nothing there has to start at zero. The
+ * one word that must start at zero, the flag the stacking kernel raises when
+ * a bounded wait for a staged tile copy gives up, is cleared on the stream
+ * before each launch and read back after it: the call returns once its work
+ * on the stream has finished, with SST_ERR_TIMEOUT if the flag was raised.
  */
 #include <mutex>
 
@@ -29,10 +33,13 @@ namespace {
 
 /* per frame: SST_NCOEF warp coefficients and one effective weight */
 static __device__ __align__(256) float g_noalloc_scratch[SST_NOALLOC_MAX_FRAMES * (SST_NCOEF + 1)];
+/* raised (set to 1) by the stacking kernel when a bounded tile-copy wait gives up */
+static __device__ __align__(16) int g_noalloc_wait_flag;
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 float * g_noalloc_ptr[kMaxDevices] = { nullptr };
+int * g_noalloc_flag_ptr[kMaxDevices] = { nullptr };
 
 /* errors are reported through sst_last_error(), like every other entry point */
 int fail(int code, const char * msg)
@@ -40,9 +47,9 @@ int fail(int code, const char * msg)
   return sst_internal_error(code, msg);
 }
 
-/* Device address of the scratch array on the current device: looked up once
- * per device, with that device current. */
-int scratch_address(float ** out)
+/* Device addresses of the scratch array and the wait flag on the current
+ * device: looked up once per device, with that device current. */
+int scratch_address(float ** out, int ** flag)
 {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -53,9 +60,14 @@ int scratch_address(float ** out)
     void * p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if( e != cudaSuccess ) return fail(SST_ERR_CUDA, cudaGetErrorString(e));
+    void * q = nullptr;
+    e = cudaGetSymbolAddress(&q, g_noalloc_wait_flag);
+    if( e != cudaSuccess ) return fail(SST_ERR_CUDA, cudaGetErrorString(e));
     g_noalloc_ptr[dev] = (float *) p;
+    g_noalloc_flag_ptr[dev] = (int *) q;
   }
   *out = g_noalloc_ptr[dev];
+  *flag = g_noalloc_flag_ptr[dev];
   return SST_OK;
 }
 
@@ -83,7 +95,8 @@ extern "C" int sst_weighted_average_add_warped_batch_noalloc(const void * frames
     return fail(SST_ERR_UNSUPPORTED, "unsupported border mode");
 
   float * scratch = nullptr;
-  const int r = scratch_address(&scratch);
+  int * wait_flag = nullptr;
+  const int r = scratch_address(&scratch, &wait_flag);
   if( r != SST_OK ) return r;
   float * coeffs = scratch;
   float * weff = scratch + (size_t) SST_NOALLOC_MAX_FRAMES * SST_NCOEF;
@@ -103,7 +116,17 @@ extern "C" int sst_weighted_average_add_warped_batch_noalloc(const void * frames
   s.acc = acc_state;
   s.plane = (size_t) dst_width * dst_height;
   s.border = border;
-  e = sst::launch_stack_add_warped(s, model->type, depth, st);
+  s.err = wait_flag;
+  e = cudaMemsetAsync(wait_flag, 0, sizeof(int), st);
+  if( e == cudaSuccess ) e = sst::launch_stack_add_warped(s, model->type, depth, st);
   if( e != cudaSuccess ) return fail(SST_ERR_CUDA, cudaGetErrorString(e));
+  int raised = 0;
+  e = cudaMemcpyAsync(&raised, wait_flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if( e == cudaSuccess ) e = cudaStreamSynchronize(st);
+  if( e != cudaSuccess ) return fail(SST_ERR_CUDA, cudaGetErrorString(e));
+  if( raised ) {
+    return fail(SST_ERR_TIMEOUT,
+        "a bounded wait for a staged tile copy gave up; acc_state is invalid and must be rebuilt");
+  }
   return SST_OK;
 }
