@@ -190,6 +190,48 @@ def cpu_reference_rate(frames_host: np.ndarray, ref: np.ndarray, sample: int, th
     return sample / dt, dt
 
 
+def accuracy_vs_oracle(frames_host: np.ndarray, ref: np.ndarray, opts, passes, threads: int):
+    """Registration and stack of `frames_host` through sst_stack_frames against
+    the FP64 oracle pipeline (outside every timed region): per-frame warp RMS
+    vs the oracle's warp, the stack arithmetic error (the GPU's transforms and
+    weights summed in FP64) and the end-to-end stack error, both as maxima
+    over the settled pixels (oracle.stack_compare_region)."""
+    import oracle as O
+    from serstacker_gb300 import capi as C
+    O.build()
+    O.set_num_threads(threads)
+    k = frames_host.shape[0]
+    reg = C.c_ecch(opts)
+    reg.set_reference_image(ref, scale=SCALE)
+    acc = C.c_weigthed_average(WIDTH, HEIGHT)
+    out = C.stack_frames(reg, acc, frames_host, passes, SCALE, weighting=1)
+    avg, _ = acc.compute()
+    po = O.pipeline_opts(passes=(O.AFFINE, O.HOMOGRAPHY), method=O.IC, maxlevel=4, max_iterations=50, epsx=0.01,
+                         min_rho=0.8, minimum_image_size=16)
+    states, status, rho, S, W = O.register_and_stack(po, ref.astype(np.float64) * SCALE, frames_host, SCALE)
+    m = O.model(O.HOMOGRAPHY)
+    rms = []
+    for i in range(k):
+        if status[i] != 0 or out["status"][i] != 0:
+            continue
+        s_g = O.set_params(m, O.identity(m), out["params"][i][:8].astype(np.float64))
+        xa, ya = O.warp_grid(m, s_g, WIDTH, HEIGHT)
+        xb, yb = O.warp_grid(m, states[i], WIDTH, HEIGHT)
+        rms.append(math.sqrt(float(((xa - xb) ** 2 + (ya - yb) ** 2)[::8, ::8].mean())))
+    rep = O.stack_error_report(frames_host, SCALE, O.HOMOGRAPHY, out["params"], out["status"], out["weight"], avg,
+                               states, status, S, W)
+    return {"frames": k, "status_equal": bool(np.array_equal(out["status"], status)),
+            "warp_rms_vs_oracle_px_median": float(np.median(rms)) if rms else None,
+            "warp_rms_vs_oracle_px_max": float(np.max(rms)) if rms else None,
+            "stack_arith_rel_err_max": rep["arith_max"],
+            "stack_rel_err_vs_oracle_max": rep["e2e_max"],
+            "stack_rel_err_vs_oracle_median": rep["e2e_median"],
+            "stack_err_of_registration_bound": rep["e2e_bound_frac"],
+            "note": "stack_arith: the GPU stack vs FP64 sums with the GPU's transforms and weights; "
+                    "stack_rel_err_vs_oracle: vs the oracle pipeline's own registration and weights "
+                    "(relative to max(|value|, 1% of the image maximum), settled pixels only)"}
+
+
 def run_reference_arm(args, ws, rank):
     """--impl reference: the reference path's CPU implementation, timed per step."""
     if rank != 0:
@@ -236,6 +278,8 @@ def main():
                     help="frames of the cpu_baseline sample (about 10 s of the oracle on 16 cores)")
     ap.add_argument("--plain-frames", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--accuracy-frames", type=int, default=48,
+                    help="frames of the workload checked against the FP64 oracle (0: skip)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form leg (profiling runs)")
     ap.add_argument("--unrolled-schedule", action="store_true",
@@ -377,6 +421,12 @@ def main():
         cpu = {"value": rate, "unit": "frames/s", "cores": threads, "kind": "port",
                "sample": f"{cs} frames of the workload (oracle FP64 pipeline, OpenMP, {dt:.1f} s)"}
 
+    acc_oracle = None
+    if rank == 0 and args.accuracy_frames > 0 and _weighting == 1:
+        ka = min(args.accuracy_frames, n)
+        acc_oracle = accuracy_vs_oracle(frames[:ka].cpu().numpy().view(np.uint16), ref, opts, passes,
+                                        os.cpu_count() or 1)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -389,7 +439,7 @@ def main():
                     "form": "one frame per call, one launch per Gauss-Newton step, host sync per step"},
                 "batched_over_plain": None if plain_fps is None else value / ws / plain_fps,
                 "accuracy": {"warp_rms_vs_truth_px_median": med_rms, "warp_rms_vs_truth_px_max": max_rms,
-                             "frames_ok": int((res["status"] == 0).sum())},
+                             "frames_ok": int((res["status"] == 0).sum()), "vs_oracle": acc_oracle},
                 "levels": level_table}
         if ser_leg is not None:
             line["ser_file"] = ser_leg
@@ -560,13 +610,12 @@ def make_bayer_workload(n: int, device):
 def main_bayer(args, ws, rank, local):
     import torch
     from serstacker_gb300 import capi as C
-    import oracle as O
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
     C.lib()
     n = args.frames
     frames, ref_raw, Hs = make_bayer_workload(n, device)
-    ref_bin = O.average_bayer_planes(ref_raw)
+    ref_bin = C.bayer_planes(ref_raw, average=True)   # sst_average_bayer_planes_u16
     pw, ph = BAYER_W // 2, BAYER_H // 2
     frame_bytes = BAYER_W * BAYER_H * 2
     opts = C.default_options(method=C.IC, maxlevel=4, max_iterations=50, epsx=0.01, minimum_image_size=16,

@@ -11,6 +11,7 @@ tests in ``tests/test_oracle.py``.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -520,3 +521,127 @@ def set_num_threads(n: int):
 
 def get_num_threads() -> int:
     return lib().orc_get_num_threads()
+
+
+def stack_compare_region(models_states, dw, dh, sw, sh, delta=0.05):
+    """Pixels of a dw x dh stack whose per-frame validity is settled.
+
+    The stacked mask of a frame is its remapped coverage (>= 255 of 255, i.e.
+    coverage >= 0.998) eroded 5 x 5 (c_frame_registration.cc:1315-1340).
+    A registration that differs by up to 0.02 px can flip a pixel whose 5 x 5
+    window maps within that distance of the source frame's edge, which moves
+    that pixel's stacked value by a whole frame's share. A pixel is kept
+    when, for every frame (motion model, oracle state), the warped positions
+    of its clipped 5 x 5 window lie all at least `delta` px inside the source
+    frame [0, sw - 1] x [0, sh - 1] or at least one of them `delta` px
+    outside it. models_states: iterable of (Model, state) of accepted frames.
+    """
+    from scipy.ndimage import maximum_filter, minimum_filter
+    keep = np.ones((dh, dw), bool)
+    for m, s in models_states:
+        X, Y = warp_grid(m, s, dw, dh)
+        x0, x1 = minimum_filter(X, 5, mode="nearest"), maximum_filter(X, 5, mode="nearest")
+        y0, y1 = minimum_filter(Y, 5, mode="nearest"), maximum_filter(Y, 5, mode="nearest")
+        inside = (x0 >= delta) & (x1 <= sw - 1 - delta) & (y0 >= delta) & (y1 <= sh - 1 - delta)
+        outside = (x0 <= -delta) | (x1 >= sw - 1 + delta) | (y0 <= -delta) | (y1 >= sh - 1 + delta)
+        keep &= inside | outside
+    return keep
+
+
+def stack_rel_err(avg, ref_avg, floor_frac=0.01):
+    """|avg - ref| / max(|ref|, floor_frac * max |ref|) elementwise (the floor
+    keeps the black sky of the synthetic scenes from dividing by ~0)."""
+    ref_avg = np.asarray(ref_avg, np.float64)
+    den = np.maximum(np.abs(ref_avg), floor_frac * float(np.abs(ref_avg).max()))
+    return np.abs(np.asarray(avg, np.float64) - ref_avg) / den
+
+
+def stack_error_report(frames, frame_scale, motion, gpu_params, gpu_status, gpu_weights, gpu_avg, orc_states,
+                       orc_status, orc_S, orc_W, input_sigma=1.0, laplacian_weights=True, border=BORDER_REFLECT101,
+                       arith_tol=1e-5, floor_frac=0.01):
+    """Errors of a GPU stack against the FP64 oracle, split by cause.
+
+    arith   : the GPU stack against FP64 sums of the same frames warped with
+              the GPU's own transforms and weighted by the GPU's own frame
+              weights: the error of the warp + accumulate arithmetic alone.
+    e2e     : the GPU stack against the oracle pipeline's stack (its own
+              registration and FP64 Laplacian-energy weights).
+    e2e_bound_frac : the largest ratio of the end-to-end error to the error
+              the registration differences explain. For pixel p the bound is
+                arith_tol * den(p)
+                + 2 * sum_f w_f * g_f(p) * sqrt(2) * d_f / sum_f w_f
+                + 2 * sum_f w_f * |I_f(p) - avg(p)| * dw_f / sum_f w_f
+              with d_f the largest displacement between the GPU's and the
+              oracle's warp of frame f over the image, g_f(p) the largest
+              forward difference of source frame f over the 5 x 5 source
+              pixels around the oracle's sample position of p (within a
+              bilinear cell the interpolant's slope along x or y is a blend
+              of two such differences, so a sample moved by d < 1 px changes
+              by at most sqrt(2) d g_f), and dw_f the relative difference of
+              the two frame weights (the derivative of the weighted mean by
+              w_f is (I_f - avg) / sum w). The factor 2 covers second-order
+              terms. A value <= 1 means the whole end-to-end difference is
+              accounted for.
+    Every maximum is over the pixels that stack_compare_region keeps (of the
+    oracle's transforms for e2e, of the GPU's for arith) where both stacks
+    have weight. Relative errors use stack_rel_err's floor.
+    """
+    from scipy.ndimage import maximum_filter
+    n, h, w = frames.shape
+    m = model(motion)
+    orc_avg = np.where(orc_W > 0, orc_S / np.where(orc_W > 0, orc_W, 1.0), 0.0)
+    S_g = np.zeros((h, w))
+    W_g = np.zeros((h, w))
+    G = np.zeros((h, w))
+    T = np.zeros((h, w))
+    Wb = np.zeros((h, w))
+    ms_g, ms_o = [], []
+    warp_rms, disp_max, dw_max = 0.0, 0.0, 0.0
+    for i in range(n):
+        img = frames[i].astype(np.float64) * frame_scale
+        if gpu_status[i] == 0:
+            s_g = set_params(m, identity(m), np.asarray(gpu_params[i][:nparams(m)], np.float64))
+            ms_g.append((m, s_g))
+            dst, msk = stack_remap(m, s_g, img, w, h, border)
+            wt = np.where(msk > 0, float(gpu_weights[i]), 0.0)
+            S_g += wt * dst
+            W_g += wt
+        if orc_status[i] != 0:
+            continue
+        s_o = orc_states[i]
+        ms_o.append((m, s_o))
+        if gpu_status[i] != 0:
+            continue
+        xa, ya = warp_grid(m, s_g, w, h)
+        xb, yb = warp_grid(m, s_o, w, h)
+        d2 = (xa - xb) ** 2 + (ya - yb) ** 2
+        d_f = math.sqrt(float(d2.max()))
+        warp_rms = max(warp_rms, math.sqrt(float(d2.mean())))
+        disp_max = max(disp_max, d_f)
+        dst_o, msk_o = stack_remap(m, s_o, img, w, h, border)
+        w_o = laplacian_energy(pyrdown(smooth(img, input_sigma))) if laplacian_weights else 1.0
+        dw_f = abs(float(gpu_weights[i]) / w_o - 1.0)
+        dw_max = max(dw_max, dw_f)
+        gx = np.zeros((h, w))
+        gy = np.zeros((h, w))
+        gx[:, :-1] = np.abs(np.diff(img, axis=1))
+        gy[:-1, :] = np.abs(np.diff(img, axis=0))
+        gs = maximum_filter(np.maximum(gx, gy), 5, mode="nearest")
+        xi = np.clip(np.floor(xb), 0, w - 1).astype(np.int64)
+        yi = np.clip(np.floor(yb), 0, h - 1).astype(np.int64)
+        g = gs[yi, xi]
+        wt = np.where(msk_o > 0, w_o, 0.0)
+        G += wt * g * math.sqrt(2.0) * d_f
+        T += wt * np.abs(dst_o - orc_avg) * dw_f
+        Wb += wt
+    keep_g = stack_compare_region(ms_g, w, h, w, h) & (W_g > 0)
+    keep_o = stack_compare_region(ms_o, w, h, w, h) & (orc_W > 0) & (Wb > 0)
+    arith = stack_rel_err(gpu_avg[keep_g], S_g[keep_g] / W_g[keep_g], floor_frac)
+    e2e = stack_rel_err(gpu_avg[keep_o], orc_avg[keep_o], floor_frac)
+    den = np.maximum(np.abs(orc_avg[keep_o]), floor_frac * float(np.abs(orc_avg[keep_o]).max()))
+    bound = arith_tol * den + 2.0 * (G[keep_o] + T[keep_o]) / Wb[keep_o]
+    frac = np.abs(gpu_avg[keep_o].astype(np.float64) - orc_avg[keep_o]) / bound
+    return {"arith_max": float(arith.max()), "arith_median": float(np.median(arith)),
+            "e2e_max": float(e2e.max()), "e2e_median": float(np.median(e2e)),
+            "e2e_bound_frac": float(frac.max()), "warp_rms_max": warp_rms, "warp_disp_max": disp_max,
+            "weight_rel_diff_max": dw_max, "region_frac": float(keep_o.mean())}

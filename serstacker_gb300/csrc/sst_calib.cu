@@ -1,7 +1,8 @@
 /*
  * sst_calib.cu -- the dark / flat calibration read_input_frame applies to
- * every raw frame before registration (c_image_processing_pipeline.cc:
- * 1124-1162):
+ * every raw frame before registration (read_input_frame,
+ * c_image_stacking_pipeline_base.cc:142-183; the dark branch converts with
+ * 1 / 2^bpp first, the flat branch converts if the dark branch did not):
  *   x = raw * scale                      convertTo(CV_32F, 1 / 2^bpp)
  *   x = x - dark                         cv::subtract(image, darkbayer)
  *   x = x * 5 / flat                     cv::divide(image, flatbayer, image, image.depth())

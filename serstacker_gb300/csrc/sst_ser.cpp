@@ -14,7 +14,8 @@
  * a reader thread fills one pinned chunk buffer from the file while the GPU
  * registers and stacks the previous one. Frames are scaled by
  * 1 / 2^bits_per_plane, the stacking pipeline's conversion of integer input
- * (read_input_frame, c_image_processing_pipeline.cc:1180-1190).
+ * (read_input_frame, c_image_stacking_pipeline_base.cc:270-275: integer
+ * frames are converted with 1 / 2^bpp even without dark or flat frames).
  */
 #include <errno.h>
 #include <fcntl.h>

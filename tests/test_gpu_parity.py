@@ -247,12 +247,14 @@ def test_pipeline_matches_oracle(gpu, oracle):
         rms = _grid_rms(O, m, states[i], _state_from_params(O, m, out["params"][i][:8]), w, h)
         assert rms <= WARP_RMS_TOL, (i, rms)
         assert out["rho"][i] == pytest.approx(rho[i], abs=1e-4)
-    both = (mask > 0) & (W > 0)
     assert ((mask > 0) == (W > 0)).mean() > 0.995
-    ref_avg = S[both] / W[both]
-    rel = np.abs(avg[both] - ref_avg) / np.maximum(np.abs(ref_avg), 1e-3)
-    # registration differences within 0.02 px move edge pixels; compare where both agree closely
-    assert np.median(rel) < 1e-4
+    # the stack arithmetic (the GPU's own transforms and weights against FP64
+    # sums) to 1e-5 at every settled pixel; the end-to-end difference from the
+    # oracle pipeline within what the two registrations' differences explain
+    rep = O.stack_error_report(frames, scale, O.HOMOGRAPHY, out["params"], out["status"], out["weight"], avg,
+                               states, status, S, W)
+    assert rep["arith_max"] <= STACK_REL_TOL, rep
+    assert rep["e2e_bound_frac"] <= 1.0, rep
 
 
 def test_checkpoint_resume_is_bitwise(gpu):

@@ -6,7 +6,7 @@ oracle of average_pyramid_inpaint (average_pyramid_inpaint.cc:18-126):
 against FP64), masks exact.
 
 Dark / flat calibration of raw frames (sst_calibrate_frames,
-c_image_processing_pipeline.cc:1124-1162) against the same sequence of
+c_image_stacking_pipeline_base.cc:142-183) against the same sequence of
 rounded FP32 operations in numpy: bitwise."""
 import numpy as np
 import pytest

@@ -527,3 +527,44 @@ def test_average_pyramid_inpaint_known_answers(oracle):
     # no pyramid levels: the holes stay empty
     out, om = oracle.average_pyramid_inpaint(ramp, m, max_levels=0)
     assert out[8, 9] == 0 and om[8, 9] == 0 and om.sum() == 255 * (17 * 19 - 1)
+
+
+def test_stack_error_report_separates_arithmetic_from_registration(oracle):
+    """The checker of the end-to-end stack comparisons: a stack built in FP64
+    from transforms moved by a few thousandths of a pixel has no arithmetic
+    error against its own transforms, an end-to-end error well above 1e-5 at
+    the disk's rim, and that error stays inside the registration bound."""
+    from serstacker_gb300 import synth
+    O = oracle
+    w, h, n = 128, 96, 3
+    sc = synth.Scene(w, h, 30.0)
+    frames, _, _ = synth.make_sequence_np(sc, n, seed=5, kind="config1", dtype=np.uint16, gain=64.0,
+                                          blur_range=(0.8, 2.0))
+    scale = 1.0 / 65535.0
+    ref = synth.reference_np(sc) * 64.0 * scale
+    po = O.pipeline_opts(passes=(O.AFFINE, O.HOMOGRAPHY), method=O.IC, maxlevel=2, max_iterations=30, epsx=0.01,
+                         min_rho=0.0, minimum_image_size=16)
+    states, status, rho, S, W = O.register_and_stack(po, ref, frames, scale)
+    m = O.model(O.HOMOGRAPHY)
+    params = np.zeros((n, 12), np.float32)
+    weights = np.zeros(n, np.float32)
+    S2 = np.zeros((h, w))
+    W2 = np.zeros((h, w))
+    for i in range(n):
+        p = O.get_params(m, states[i]).copy()
+        p[2] += 0.003 * (i + 1)
+        p[5] -= 0.002
+        params[i, :8] = p
+        img = frames[i].astype(np.float64) * scale
+        weights[i] = O.laplacian_energy(O.pyrdown(O.smooth(img, 1.0)))
+        st = O.set_params(m, O.identity(m), params[i, :8].astype(np.float64))
+        dst, msk = O.stack_remap(m, st, img, w, h)
+        wt = np.where(msk > 0, float(weights[i]), 0.0)
+        S2 += wt * dst
+        W2 += wt
+    avg = np.where(W2 > 0, S2 / np.where(W2 > 0, W2, 1), 0).astype(np.float32)
+    rep = O.stack_error_report(frames, scale, O.HOMOGRAPHY, params, status, weights, avg, states, status, S, W)
+    assert rep["arith_max"] < 1e-6, rep
+    assert rep["e2e_max"] > 1e-5, rep
+    assert rep["e2e_bound_frac"] <= 1.0, rep
+    assert 0.005 < rep["warp_disp_max"] < 0.02, rep
