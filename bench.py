@@ -12,8 +12,9 @@ sequence through sst_stack_frames.
   e2e   : the same call with pinned HOST frames (H2D inside the timed region)
           plus the D2H of every result and of the stacked image
 
---impl reference times the CPU restatement of the reference path (the FP64
-oracle, OpenMP over all host cores) on a bounded sample of the same workload.
+--impl reference times the CPU restatement of the reference path (FP32, the
+reference's sequence of full-image passes, OpenMP static row partitions over
+all host cores; oracle/sst_refcpu.cc) on a bounded sample of the same workload.
 Multi-GPU runs (torchrun) are replicas: each rank stacks its own sequence.
 """
 from __future__ import annotations
@@ -177,17 +178,55 @@ def warp_rms_vs_truth(params: np.ndarray, Hs: np.ndarray, status: np.ndarray, st
     return float(np.median(out)) if out else None, float(np.max(out)) if out else None
 
 
+CPU_BASELINE_DESC = ("FP32 reference-semantics CPU restatement (oracle/sst_refcpu.cc: the reference's sequence of "
+                     "full-image passes per frame, -O3 -ffast-math, OpenMP static row partitions over all host cores)")
+
+
 def cpu_reference_rate(frames_host: np.ndarray, ref: np.ndarray, sample: int, threads: int):
-    """Oracle (CPU restatement of the reference path) on `sample` frames: frames/s."""
+    """The FP32 reference-semantics CPU restatement of the path (register +
+    warp + running-mean stack) on `sample` frames: frames/s."""
     import oracle as O
     O.set_num_threads(threads)
     po = O.pipeline_opts(passes=(O.AFFINE, O.HOMOGRAPHY), method=O.IC, maxlevel=4, max_iterations=50, epsx=0.01,
                          min_rho=0.8, minimum_image_size=16)
     sub = frames_host[:sample]
+    r = (ref.astype(np.float64) * SCALE).astype(np.float32)
     t0 = time.perf_counter()
-    O.register_and_stack(po, ref.astype(np.float64) * SCALE, sub, SCALE)
+    O.refcpu_register_and_stack(po, r, sub, SCALE)
     dt = time.perf_counter() - t0
     return sample / dt, dt
+
+
+def run_reference_arm(args, ws, rank):
+    """--impl reference: the reference path's CPU implementation, timed per step."""
+    if rank != 0:
+        return
+    import oracle as O
+    O.build()
+    from serstacker_gb300 import synth
+    threads = os.cpu_count() or 1
+    sample = args.ref_sample
+    sc = synth.scene_config1()
+    frames, _, _ = synth.make_sequence_np(sc, sample, SEED, kind="config1", dtype=np.uint16, gain=GAIN,
+                                          blur_range=(0.8, 2.5))
+    ref = synth.reference_np(sc) * GAIN
+    for _ in range(min(args.warmup, 1)):
+        cpu_reference_rate(frames, ref, min(4, sample), threads)
+    rates = []
+    t_all = 0.0
+    for _ in range(args.steps):
+        r, dt = cpu_reference_rate(frames, ref, sample, threads)
+        rates.append(r)
+        t_all += dt
+    v = float(np.median(rates))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_all / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_cfg(args.frames),
+            "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample} frames of the workload per step; {CPU_BASELINE_DESC}"},
+            "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 def accuracy_vs_oracle(frames_host: np.ndarray, ref: np.ndarray, opts, passes, threads: int):
@@ -232,38 +271,6 @@ def accuracy_vs_oracle(frames_host: np.ndarray, ref: np.ndarray, opts, passes, t
                     "(relative to max(|value|, 1% of the image maximum), settled pixels only)"}
 
 
-def run_reference_arm(args, ws, rank):
-    """--impl reference: the reference path's CPU implementation, timed per step."""
-    if rank != 0:
-        return
-    import oracle as O
-    O.build()
-    from serstacker_gb300 import synth
-    threads = os.cpu_count() or 1
-    sample = args.ref_sample
-    sc = synth.scene_config1()
-    frames, _, _ = synth.make_sequence_np(sc, sample, SEED, kind="config1", dtype=np.uint16, gain=GAIN,
-                                          blur_range=(0.8, 2.5))
-    ref = synth.reference_np(sc) * GAIN
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_reference_rate(frames, ref, min(2, sample), threads)
-    rates = []
-    t_all = 0.0
-    for _ in range(args.steps):
-        r, dt = cpu_reference_rate(frames, ref, sample, threads)
-        rates.append(r)
-        t_all += dt
-    v = float(np.median(rates))
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t_all / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_cfg(args.frames),
-            "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
-                             "sample": f"{sample} frames of the workload per step (oracle pipeline, FP64, OpenMP)"},
-            "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -273,9 +280,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--chunk", type=int, default=512,
                     help="frames per streamed chunk in the e2e leg (a quarter of it for the raw Bayer frames)")
-    ap.add_argument("--ref-sample", type=int, default=6, help="frames per step of the --impl reference arm")
-    ap.add_argument("--cpu-sample", type=int, default=160,
-                    help="frames of the cpu_baseline sample (about 10 s of the oracle on 16 cores)")
+    ap.add_argument("--ref-sample", type=int, default=128, help="frames per step of the --impl reference arm")
+    ap.add_argument("--cpu-sample", type=int, default=1024,
+                    help="frames of the cpu_baseline sample (the FP32 CPU restatement on all host cores)")
     ap.add_argument("--plain-frames", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy-frames", type=int, default=48,
@@ -419,7 +426,7 @@ def main():
         sub = frames[:cs].cpu().numpy().view(np.uint16)
         rate, dt = cpu_reference_rate(sub, ref, cs, threads)
         cpu = {"value": rate, "unit": "frames/s", "cores": threads, "kind": "port",
-               "sample": f"{cs} frames of the workload (oracle FP64 pipeline, OpenMP, {dt:.1f} s)"}
+               "sample": f"{cs} frames of the workload ({dt:.1f} s); {CPU_BASELINE_DESC}"}
 
     acc_oracle = None
     if rank == 0 and args.accuracy_frames > 0 and _weighting == 1:
@@ -431,7 +438,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {**workload_cfg(n), "parallelism": f"replicas x{ws}"},
+                "config": workload_cfg(n), "parallelism": f"replicas x{ws}",
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
                 "clocks": clk, "gpu_launches": launches,
                 "plain": None if plain_fps is None else {

@@ -621,6 +621,143 @@ int sst_bayer_average_load_state(sst_bayer_average * h, const float * state12, i
  * the reference, whose stacking runs in one process. */
 int sst_state_merge(float * dst, const float * src, int groups, size_t plane);
 
+/* ------------------------------------------------------ frame registration */
+
+/* color_channel_gray of color_channel_type (core/proc/extract_channel.h:31):
+ * the registration channel of mono frames, which is the frame itself */
+#define SST_COLOR_CHANNEL_GRAY 104
+
+/* c_ecc_registration_options (core/proc/image_registration/
+ * c_frame_registration.h:47-63), same fields and defaults */
+typedef struct sst_ecc_registration_options {
+  double scale;                     /* 0.5: ECC on scaleImage(frame): pyrDown at 0.5, INTER_AREA otherwise */
+  double eps;                       /* 0.2: c_ecch epsx */
+  double min_rho;                   /* 0.8: correlation gate after alignment */
+  double input_smooth_sigma;        /* 1 */
+  double reference_smooth_sigma;    /* 1 */
+  double update_step_scale;         /* 1.5 */
+  double normalization_noise;       /* 0.01 */
+  int32_t se_radius;                /* 5 (planetary-disk masks only) */
+  int32_t ecc_method;               /* SST_ECC_LM */
+  int32_t max_iterations;           /* 50 */
+  int32_t ecch_max_level;           /* 0 */
+  int32_t ecch_minimum_image_size;  /* 16 */
+  int32_t normalization_scale;      /* 0: ecc_normalize off; > 0: its pyramid level */
+  int32_t ecch_estimate_translation_first;   /* 1 */
+  int32_t replace_planetary_disk_with_mask;  /* 0; 1 is not supported */
+} sst_ecc_registration_options;
+
+/* c_eccflow_registration_options (c_frame_registration.h:88-100) */
+typedef struct sst_eccflow_registration_options {
+  double update_multiplier;         /* 1.5 */
+  double input_smooth_sigma;        /* 0 */
+  double reference_smooth_sigma;    /* 0 */
+  double noise_level;               /* -1 */
+  double scale_factor;              /* 0.75 */
+  int32_t max_iterations;           /* 3 */
+  int32_t support_scale;            /* 4 */
+  int32_t min_image_size;           /* -1 */
+  int32_t max_pyramid_level;        /* -1 */
+  int32_t downscale_method;         /* SST_ECCFLOW_DOWNSCALE_RECURSIVE_RESIZE */
+  int32_t reserved;
+} sst_eccflow_registration_options;
+
+/* c_image_registration_options (c_frame_registration.h:119-137). The
+ * reference's defaults enable feature registration (AKAZE / ORB matching),
+ * which is not part of this library: set enable_feature_registration = 0
+ * and enable ECC and / or eccflow registration. */
+typedef struct sst_image_registration_options {
+  int32_t motion_type;              /* SST_MOTION_AFFINE */
+  int32_t ecc_registration_channel; /* SST_COLOR_CHANNEL_GRAY (frames are mono) */
+  int32_t interpolation;            /* ECC_INTER_LINEAR (1) */
+  int32_t border_mode;              /* SST_BORDER_REFLECT101 */
+  double border_value;              /* 0 */
+  sst_ecc_registration_options ecc;
+  sst_eccflow_registration_options eccflow;
+  int32_t enable_feature_registration;               /* 1 in the reference; must be 0 */
+  int32_t enable_ecc_registration;                   /* 0 */
+  int32_t enable_eccflow_registration;               /* 0 */
+  int32_t accumulate_and_compensate_turbulent_flow;  /* 0; 1 is not supported */
+} sst_image_registration_options;
+
+/* The reference defaults of the three option structs. */
+void sst_image_registration_options_default(sst_image_registration_options * opts);
+
+typedef struct sst_frame_registration sst_frame_registration;
+
+/* c_frame_registration (c_frame_registration.h:210-356) with ECC and / or
+ * eccflow registration of mono frames. */
+int sst_frame_registration_create(sst_frame_registration ** out, const sst_image_registration_options * opts);
+int sst_frame_registration_destroy(sst_frame_registration * h);
+
+/* c_frame_registration::setup_reference_frame(reference_image, reference_mask)
+ * (c_frame_registration.cc:565-719): the ECC reference is
+ * scaleImage(reference, ecc.scale) (pyrDown at 0.5, INTER_AREA otherwise; the
+ * mask pyrDown'ed / resized, then >= 250; c_frame_registration.cc:230-250),
+ * ecc_normalize'd when normalization_scale > 0 and normalization_noise > 0
+ * (ecc2.cc:385-397), and handed to c_ecch; the eccflow reference is the
+ * full-size image. Values are multiplied by `scale`. mask may be NULL (u8,
+ * 0 = invalid); masks are not supported with eccflow registration. */
+int sst_frame_registration_setup_reference_frame(sst_frame_registration * h, const void * image, int depth,
+    int width, int height, size_t row_stride, double scale, const uint8_t * mask, size_t mask_stride,
+    int on_device, void * stream);
+
+/* c_frame_registration::register_frame (c_frame_registration.cc:721-964)
+ * for n frames of the reference's size, registered together: each frame's
+ * ECC image (scaleImage, ecc_normalize) is aligned by the batched c_ecch
+ * engine, first as a translation with the gate rho >= 0.75 min_rho when
+ * ecch_estimate_translation_first applies (motion_type not TRANSLATION,
+ * ecch_max_level != 0), then with motion_type and the gate rho >= min_rho;
+ * the result is scaled back by 1 / ecc.scale. With eccflow registration the
+ * transform's remap at full size is refined by c_eccflow::compute.
+ *   params_out     n x 12 floats: motion_type's parameter vector at full size
+ *   status_out     SST_FRAME_* (SST_FRAME_LOW_RHO for either gate)
+ *   rho_out        the last correlation computed for the frame
+ *   iterations_out Gauss-Newton iterations over both passes and all levels
+ *   rmap_out       n x height x width x 2 floats (interleaved x, y as
+ *                  cv::Mat2f): the current remap (current_remap(),
+ *                  c_frame_registration.h:308); may be NULL
+ * Frames and outputs are host or device memory per on_device; outputs may be NULL. */
+int sst_frame_registration_register_frames(sst_frame_registration * h, const void * frames, int depth, int n,
+    int width, int height, size_t row_stride, size_t frame_stride, double scale, int on_device,
+    float * params_out, int32_t * status_out, float * rho_out, int32_t * iterations_out, float * rmap_out,
+    void * stream);
+
+/* Frames registered per engine launch (default 256). */
+int sst_frame_registration_set_chunk_frames(sst_frame_registration * h, int frames);
+
+/* Size of the ECC images (the reference size scaled by scaleImage). */
+int sst_frame_registration_ecc_size(const sst_frame_registration * h, int * width, int * height);
+
+/* The ECC image (after scaleImage and ecc_normalize) of the reference
+ * (frame = -1, with its ECC mask when mask_out is not NULL) or of frame
+ * `frame` of the last chunk registered; out is ecc width x height floats. */
+int sst_frame_registration_ecc_image(sst_frame_registration * h, int frame, float * out, uint8_t * mask_out,
+    int on_device);
+
+/* c_frame_registration::base_remap / custom_remap with a dense remap
+ * (c_frame_registration.cc:1265-1386): dst (f32, dst_width x dst_height) =
+ * cv::remap(src * scale, rmap, INTER_LINEAR, border, border_value); dst_mask
+ * (u8) = remap of src_mask (all 255 when NULL) with LINEAR / BORDER_CONSTANT
+ * 0, compared >= 255 and eroded 5 x 5. rmap is dst_width x dst_height x 2
+ * floats. Either output may be NULL. Buffers are host or device memory per
+ * on_device (packed dst rows). */
+int sst_remap_rmap(const void * src, int depth, int src_width, int src_height, size_t row_stride, double scale,
+    const float * rmap, int dst_width, int dst_height, int border, double border_value, const uint8_t * src_mask,
+    size_t mask_stride, float * dst, uint8_t * dst_mask, int on_device, void * stream);
+
+/* c_image_transform::scale_transfrom(factor) (c_image_transform.h:101;
+ * per-model overrides c_image_transform.cc:130-1781) on a parameter vector
+ * of `model`, in place (host memory). */
+int sst_image_transform_scale(const sst_motion_model * model, float * params, double factor);
+
+/* c_image_transform::create_remap(size, map) (c_image_transform.cc:150-170,
+ * 525-555, 926-946, 1207-1223, 1531-1547, 1783-1798): rmap (width x height x
+ * 2 floats, interleaved x, y) = W(x, y; params). Host or device memory per
+ * on_device. */
+int sst_image_transform_create_remap(const sst_motion_model * model, const float * params, int width, int height,
+    float * rmap, int on_device, void * stream);
+
 /* ------------------------------------------------ allocation-free stacking */
 
 /* Largest batch the allocation-free entry point accepts. */

@@ -6,7 +6,14 @@
  * replace (paths relative to the SerStacker source tree):
  *   sst_gb300::c_ecch_options      core/proc/image_registration/ecc2.h:158-172
  *   sst_gb300::c_ecch              core/proc/image_registration/ecc2.h:193-308
+ *   sst_gb300::image_transform     core/proc/image_registration/c_image_transform.h:42-117
+ *                                  (parameters, scale_transfrom, create_remap)
+ *   sst_gb300::c_eccflow           core/proc/image_registration/ecc2.h:548-662
+ *   sst_gb300::c_ecc_registration_options, c_eccflow_registration_options,
+ *   c_image_registration_options, c_frame_registration
+ *                                  core/proc/image_registration/c_frame_registration.h:47-356
  *   sst_gb300::c_weigthed_average  core/average/c_frame_accumulation.h:39-63
+ *   sst_gb300::c_bayer_average     core/average/c_frame_accumulation.h:222-262
  *   sst_gb300::c_local_variance_map_options, c_local_variance_sharpness_measure
  *                                  core/proc/sharpness_measure/c_local_variance_sharpness_measure.h:17-23
  *   sst_gb300::c_ser_reader        core/io/c_ser_file.h:136-174
@@ -61,7 +68,10 @@ struct c_ecch_options {
   int maxlevel = 0;
 };
 
-/* The motion model and its parameter vector (c_image_transform::parameters()). */
+/* The motion model and its parameter vector: the c_image_transform object of
+ * create_image_transform() (image_transform.cc:32-60) with its
+ * parameters() / set_parameters(), scale_transfrom() and create_remap()
+ * (c_image_transform.h:42-117). An empty parameter vector is the identity. */
 struct image_transform {
   sst_motion_model model { SST_MOTION_AFFINE, 0, 0, 0 };
   std::vector<float> parameters;
@@ -70,6 +80,68 @@ struct image_transform {
   {
     model.type = motion_type;
     model.fix_scale = motion_type == SST_MOTION_EUCLIDEAN ? 1 : 0;
+  }
+
+  int num_parameters() const
+  {
+    switch ( model.type ) {
+    case SST_MOTION_TRANSLATION: return 2;
+    case SST_MOTION_EUCLIDEAN:
+    case SST_MOTION_SCALED_EUCLIDEAN:
+      return (model.fix_translation ? 0 : 2) + (model.fix_rotation ? 0 : 1) + (model.fix_scale ? 0 : 1);
+    case SST_MOTION_AFFINE: return 6;
+    case SST_MOTION_QUADRATIC: return 12;
+    default: return 8;
+    }
+  }
+
+  /* c_image_transform::set_parameters / parameters */
+  void set_parameters(const std::vector<float> & p) { parameters = p; }
+  std::vector<float> get_parameters() const
+  {
+    float p[12] = { 0 };
+    fill(p);
+    return std::vector<float>(p, p + num_parameters());
+  }
+
+  /* c_image_transform::scale_transfrom(factor) */
+  bool scale_transfrom(double factor)
+  {
+    float p[12] = { 0 };
+    fill(p);
+    if( sst_image_transform_scale(&model, p, factor) != SST_OK ) return false;
+    parameters.assign(p, p + num_parameters());
+    return true;
+  }
+
+  /* c_image_transform::create_remap(size, map): width x height x 2 floats */
+  bool create_remap(int width, int height, std::vector<float> & map) const
+  {
+    float p[12] = { 0 };
+    fill(p);
+    map.resize((size_t) width * height * 2);
+    return sst_image_transform_create_remap(&model, p, width, height, map.data(), 0, nullptr) == SST_OK;
+  }
+
+  /* the parameter vector, the identity when none is set */
+  void fill(float * p) const
+  {
+    if( !parameters.empty() ) {
+      for( size_t i = 0; i < parameters.size() && i < 12; ++i ) p[i] = parameters[i];
+      return;
+    }
+    switch ( model.type ) {
+    case SST_MOTION_EUCLIDEAN:
+    case SST_MOTION_SCALED_EUCLIDEAN:
+      if( !model.fix_scale ) p[(model.fix_translation ? 0 : 2) + (model.fix_rotation ? 0 : 1)] = 1;
+      break;
+    case SST_MOTION_AFFINE:
+    case SST_MOTION_HOMOGRAPHY:
+    case SST_MOTION_EPIPOLAR_DEROTATION: p[0] = 1, p[4] = 1; break;
+    case SST_MOTION_SEMI_QUADRATIC: p[0] = 1, p[5] = 1; break;
+    case SST_MOTION_QUADRATIC: p[0] = 1, p[7] = 1; break;
+    default: break;
+    }
   }
 };
 
@@ -95,8 +167,31 @@ public:
   bool set_reference_image(const image_view & img, const image_view & mask = image_view(), double scale = 1.0)
   {
     if( !_h ) return false;
-    return sst_ecch_set_reference_image(_h, img.data, img.depth, img.width, img.height, img.stride, scale,
-        (const uint8_t *) mask.data, mask.stride, 0, nullptr) == SST_OK;
+    if( sst_ecch_set_reference_image(_h, img.data, img.depth, img.width, img.height, img.stride, scale,
+            (const uint8_t *) mask.data, mask.stride, 0, nullptr) != SST_OK )
+      return false;
+    _ref_w = img.width, _ref_h = img.height;
+    return true;
+  }
+
+  /* c_ecch::set_current_image(current_image) (ecc2.cc:1060-1120): the frame
+   * the next align() registers (kept by reference, as a view) */
+  bool set_current_image(const image_view & img, double scale = 1.0)
+  {
+    if( img.empty() ) return false;
+    _current = img;
+    _current_scale = scale;
+    return true;
+  }
+
+  /* c_ecch::align() (ecc2.cc:1133-1176) of the current image */
+  bool align() { return !_current.empty() && align(_current, _current_scale); }
+
+  /* c_ecch::create_remap(map) (ecc2.h:300): the attached transform's remap at
+   * the reference size, width x height x 2 floats */
+  bool create_remap(std::vector<float> & map) const
+  {
+    return _transform && _ref_w > 0 && _transform->create_remap(_ref_w, _ref_h, map);
   }
 
   /* c_ecch::align(current_image, current_mask) (ecc2.cc:1123-1176): updates the
@@ -180,6 +275,9 @@ private:
   double _min_rho = 0;
   sst_ecch * _h = nullptr;
   image_transform * _transform = nullptr;
+  image_view _current;
+  double _current_scale = 1.0;
+  int _ref_w = 0, _ref_h = 0;
   double _eps = -1, _rho = -1;
   int _num_iterations = -1;
 };
@@ -421,6 +519,345 @@ public:
 
 private:
   sst_ser_writer * _h = nullptr;
+};
+
+/* c_eccflow_options (ecc2.h:515-527) */
+struct c_eccflow_options {
+  double update_multiplier = 1.5;
+  double scale_factor = 0.5;
+  double noise_level = -1;
+  double input_smooth_sigma = 0;
+  double reference_smooth_sigma = 0;
+  int max_iterations = 1;
+  int support_scale = 5;
+  int min_image_size = 4;
+  int max_pyramid_level = -1;
+  int downscale_method = SST_ECCFLOW_DOWNSCALE_RECURSIVE_RESIZE;
+};
+
+/* c_eccflow (ecc2.h:548-662) on the GPU: set_reference_image(reference),
+ * compute(current, rmap) refining rmap (width x height x 2 floats, the
+ * identity when empty) in place. */
+class c_eccflow {
+public:
+  c_eccflow() { create(); }
+  explicit c_eccflow(const c_eccflow_options & o) : _opts(o) { create(); }
+  ~c_eccflow() { if( _h ) sst_eccflow_destroy(_h); }
+  c_eccflow(const c_eccflow &) = delete;
+  c_eccflow & operator=(const c_eccflow &) = delete;
+
+  const c_eccflow_options & options() const { return _opts; }
+  void set_options(const c_eccflow_options & o) { _opts = o; create(); }
+
+  /* c_eccflow::set_reference_image (ecc2.cc:2489-2672) */
+  bool set_reference_image(const image_view & img, double scale = 1.0)
+  {
+    if( !_h || img.empty() ) return false;
+    if( sst_eccflow_set_reference_image(_h, img.data, img.depth, img.width, img.height, img.stride, scale, 0, nullptr) !=
+        SST_OK )
+      return false;
+    _w = img.width, _hh = img.height;
+    return true;
+  }
+
+  /* c_eccflow::compute(current, rmap) (ecc2.cc:2856-2865) */
+  bool compute(const image_view & current, std::vector<float> & rmap, double scale = 1.0)
+  {
+    if( !_h || current.width != _w || current.height != _hh ) return false;
+    const size_t n = (size_t) _w * _hh * 2;
+    const bool have_init = rmap.size() == n;
+    std::vector<float> out(n);
+    if( sst_eccflow_compute_batch(_h, current.data, current.depth, 1, current.stride, current.stride * current.height,
+            scale, 0, have_init ? rmap.data() : nullptr, out.data(), nullptr) != SST_OK )
+      return false;
+    rmap.swap(out);
+    return true;
+  }
+
+  int num_levels() const { return _h ? sst_eccflow_num_levels(_h) : 0; }
+  sst_eccflow * handle() const { return _h; }
+
+private:
+  void create()
+  {
+    if( _h ) sst_eccflow_destroy(_h), _h = nullptr;
+    sst_eccflow_options o;
+    sst_eccflow_options_default(&o);
+    o.update_multiplier = _opts.update_multiplier;
+    o.scale_factor = _opts.scale_factor;
+    o.noise_level = _opts.noise_level;
+    o.input_smooth_sigma = _opts.input_smooth_sigma;
+    o.reference_smooth_sigma = _opts.reference_smooth_sigma;
+    o.max_iterations = _opts.max_iterations;
+    o.support_scale = _opts.support_scale;
+    o.min_image_size = _opts.min_image_size;
+    o.max_pyramid_level = _opts.max_pyramid_level;
+    o.downscale = _opts.downscale_method;
+    if( sst_eccflow_create(&_h, &o) != SST_OK ) _h = nullptr;
+  }
+  c_eccflow_options _opts;
+  sst_eccflow * _h = nullptr;
+  int _w = 0, _hh = 0;
+};
+
+/* c_ecc_registration_options (c_frame_registration.h:47-63) */
+struct c_ecc_registration_options {
+  double scale = 0.5;
+  double eps = 0.2;
+  double min_rho = 0.8;
+  double input_smooth_sigma = 1.0;
+  double reference_smooth_sigma = 1.0;
+  double update_step_scale = 1.5;
+  int se_radius = 5;
+  int ecc_method = SST_ECC_LM;
+  int max_iterations = 50;
+  int ecch_max_level = 0;
+  int ecch_minimum_image_size = 16;
+  double normalization_noise = 0.01;
+  int normalization_scale = 0;
+  bool ecch_estimate_translation_first = true;
+  bool replace_planetary_disk_with_mask = false;
+};
+
+/* c_eccflow_registration_options (c_frame_registration.h:88-100) */
+struct c_eccflow_registration_options {
+  double update_multiplier = 1.5;
+  double input_smooth_sigma = 0;
+  double reference_smooth_sigma = 0;
+  double noise_level = -1;
+  double scale_factor = 0.75;
+  int max_iterations = 3;
+  int support_scale = 4;
+  int min_image_size = -1;
+  int max_pyramid_level = -1;
+  int downscale_method = SST_ECCFLOW_DOWNSCALE_RECURSIVE_RESIZE;
+};
+
+/* c_image_registration_options (c_frame_registration.h:119-137). The
+ * reference enables feature registration by default; this library has no
+ * feature registration, so create() fails unless it is switched off. */
+struct c_image_registration_options {
+  int motion_type = SST_MOTION_AFFINE;
+  int ecc_registration_channel = SST_COLOR_CHANNEL_GRAY;
+  int interpolation = 1;                       // ECC_INTER_LINEAR
+  int border_mode = SST_BORDER_REFLECT101;
+  double border_value = 0;
+  c_ecc_registration_options ecc;
+  c_eccflow_registration_options eccflow;
+  bool enable_feature_registration = true;
+  bool enable_ecc_registration = false;
+  bool enable_eccflow_registration = false;
+  bool accumulate_and_compensate_turbulent_flow = false;
+};
+
+/* c_image_registration_status (c_frame_registration.h:185-207), the fields
+ * the GPU path fills */
+struct c_image_registration_status {
+  double rho = -1;
+  int num_iterations = 0;
+  int frame_status = SST_FRAME_OK;
+};
+
+/* c_frame_registration (c_frame_registration.h:210-356) on the GPU for mono
+ * frames: setup_reference_frame, register_frame (ECC with ecc.scale,
+ * ecc_normalize and the translation estimate, then eccflow), remap /
+ * custom_remap by the current remap, current_remap, image_transform, status.
+ * register_frames registers a whole batch in one engine schedule. */
+class c_frame_registration {
+public:
+  c_frame_registration() = default;
+  explicit c_frame_registration(const c_image_registration_options & o) : _opts(o) {}
+  ~c_frame_registration() { if( _h ) sst_frame_registration_destroy(_h); }
+  c_frame_registration(const c_frame_registration &) = delete;
+  c_frame_registration & operator=(const c_frame_registration &) = delete;
+
+  const c_image_registration_options & options() const { return _opts; }
+  c_image_registration_options & options() { return _opts; }
+
+  /* setup_reference_frame(reference_image, reference_mask) (c_frame_registration.cc:565-719) */
+  bool setup_reference_frame(const image_view & reference_image, const image_view & reference_mask = image_view(),
+      double scale = 1.0)
+  {
+    if( !create() || reference_image.empty() ) return false;
+    if( sst_frame_registration_setup_reference_frame(_h, reference_image.data, reference_image.depth,
+            reference_image.width, reference_image.height, reference_image.stride, scale,
+            (const uint8_t *) reference_mask.data, reference_mask.stride, 0, nullptr) != SST_OK )
+      return false;
+    _w = reference_image.width, _hh = reference_image.height;
+    return true;
+  }
+
+  /* register_frame(current_image, current_mask, dst, dstmask)
+   * (c_frame_registration.cc:721-964): false when registration fails (the
+   * status says why); dst / dst_mask (optional, reference-size f32 / u8)
+   * receive remap() of the frame */
+  bool register_frame(const image_view & current_image, std::vector<float> * dst = nullptr,
+      std::vector<uint8_t> * dst_mask = nullptr, double scale = 1.0)
+  {
+    if( !_h || current_image.width != _w || current_image.height != _hh ) return false;
+    float params[12] = { 0 };
+    int32_t status = 0, iters = 0;
+    float rho = 0;
+    _remap.resize((size_t) _w * _hh * 2);
+    if( sst_frame_registration_register_frames(_h, current_image.data, current_image.depth, 1, _w, _hh,
+            current_image.stride, current_image.stride * _hh, scale, 0, params, &status, &rho, &iters, _remap.data(),
+            nullptr) != SST_OK )
+      return false;
+    _transform.parameters.assign(params, params + _transform.num_parameters());
+    _status.rho = rho, _status.num_iterations = iters, _status.frame_status = status;
+    if( status != SST_FRAME_OK ) return false;
+    if( dst || dst_mask ) return remap(current_image, dst, image_view(), dst_mask, scale);
+    return true;
+  }
+
+  /* register_frames: n frames (host, frame_stride bytes apart) in one batch;
+   * params n x 12, status / rho per frame */
+  bool register_frames(const void * frames, int depth, int n, size_t row_stride, size_t frame_stride,
+      std::vector<float> & params, std::vector<int32_t> & status, std::vector<float> & rho, double scale = 1.0)
+  {
+    if( !_h ) return false;
+    params.assign((size_t) n * 12, 0.f);
+    status.assign(n, 0);
+    rho.assign(n, 0.f);
+    return sst_frame_registration_register_frames(_h, frames, depth, n, _w, _hh, row_stride, frame_stride, scale, 0,
+        params.data(), status.data(), rho.data(), nullptr, nullptr, nullptr) == SST_OK;
+  }
+
+  /* remap(src, dst, src_mask, dst_mask) (c_frame_registration.cc:1386-1400):
+   * base_remap with the current remap, the options' border */
+  bool remap(const image_view & src, std::vector<float> * dst, const image_view & src_mask = image_view(),
+      std::vector<uint8_t> * dst_mask = nullptr, double scale = 1.0) const
+  {
+    return custom_remap(_remap, src, dst, src_mask, dst_mask, scale);
+  }
+
+  /* custom_remap(rmap, src, dst, src_mask, dst_mask) (c_frame_registration.cc:1342-1384) */
+  bool custom_remap(const std::vector<float> & rmap, const image_view & src, std::vector<float> * dst,
+      const image_view & src_mask = image_view(), std::vector<uint8_t> * dst_mask = nullptr, double scale = 1.0) const
+  {
+    if( rmap.size() != (size_t) _w * _hh * 2 || src.empty() ) return false;
+    if( dst ) dst->resize((size_t) _w * _hh);
+    if( dst_mask ) dst_mask->resize((size_t) _w * _hh);
+    return sst_remap_rmap(src.data, src.depth, src.width, src.height, src.stride, scale, rmap.data(), _w, _hh,
+        _opts.border_mode, _opts.border_value, (const uint8_t *) src_mask.data, src_mask.stride,
+        dst ? dst->data() : nullptr, dst_mask ? dst_mask->data() : nullptr, 0, nullptr) == SST_OK;
+  }
+
+  /* current_remap() (c_frame_registration.h:308): width x height x 2 floats */
+  const std::vector<float> & current_remap() const { return _remap; }
+  const image_transform & image_transform_ref() const { return _transform; }
+  const c_image_registration_status & status() const { return _status; }
+  sst_frame_registration * handle() const { return _h; }
+
+private:
+  bool create()
+  {
+    if( _h ) sst_frame_registration_destroy(_h), _h = nullptr;
+    sst_image_registration_options o;
+    sst_image_registration_options_default(&o);
+    o.motion_type = _opts.motion_type;
+    o.ecc_registration_channel = _opts.ecc_registration_channel;
+    o.interpolation = _opts.interpolation;
+    o.border_mode = _opts.border_mode;
+    o.border_value = _opts.border_value;
+    const c_ecc_registration_options & e = _opts.ecc;
+    o.ecc.scale = e.scale, o.ecc.eps = e.eps, o.ecc.min_rho = e.min_rho;
+    o.ecc.input_smooth_sigma = e.input_smooth_sigma, o.ecc.reference_smooth_sigma = e.reference_smooth_sigma;
+    o.ecc.update_step_scale = e.update_step_scale, o.ecc.normalization_noise = e.normalization_noise;
+    o.ecc.se_radius = e.se_radius, o.ecc.ecc_method = e.ecc_method, o.ecc.max_iterations = e.max_iterations;
+    o.ecc.ecch_max_level = e.ecch_max_level, o.ecc.ecch_minimum_image_size = e.ecch_minimum_image_size;
+    o.ecc.normalization_scale = e.normalization_scale;
+    o.ecc.ecch_estimate_translation_first = e.ecch_estimate_translation_first;
+    o.ecc.replace_planetary_disk_with_mask = e.replace_planetary_disk_with_mask;
+    const c_eccflow_registration_options & f = _opts.eccflow;
+    o.eccflow.update_multiplier = f.update_multiplier, o.eccflow.input_smooth_sigma = f.input_smooth_sigma;
+    o.eccflow.reference_smooth_sigma = f.reference_smooth_sigma, o.eccflow.noise_level = f.noise_level;
+    o.eccflow.scale_factor = f.scale_factor, o.eccflow.max_iterations = f.max_iterations;
+    o.eccflow.support_scale = f.support_scale, o.eccflow.min_image_size = f.min_image_size;
+    o.eccflow.max_pyramid_level = f.max_pyramid_level, o.eccflow.downscale_method = f.downscale_method;
+    o.enable_feature_registration = _opts.enable_feature_registration;
+    o.enable_ecc_registration = _opts.enable_ecc_registration;
+    o.enable_eccflow_registration = _opts.enable_eccflow_registration;
+    o.accumulate_and_compensate_turbulent_flow = _opts.accumulate_and_compensate_turbulent_flow;
+    _transform = image_transform(_opts.motion_type);
+    return sst_frame_registration_create(&_h, &o) == SST_OK;
+  }
+
+  c_image_registration_options _opts;
+  sst_frame_registration * _h = nullptr;
+  image_transform _transform;
+  std::vector<float> _remap;
+  c_image_registration_status _status;
+  int _w = 0, _hh = 0;
+};
+
+/* c_bayer_average (c_frame_accumulation.h:222-262) on the GPU: the pattern
+ * of set_bayer_pattern, the frame's transform in place of set_remap's map
+ * (set_remap with a transform; clear_remap for no registration), add of raw
+ * mosaic frames, compute of the B, G, R planes. */
+class c_bayer_average {
+public:
+  c_bayer_average() = default;
+  ~c_bayer_average() { if( _h ) sst_bayer_average_destroy(_h); }
+  c_bayer_average(const c_bayer_average &) = delete;
+  c_bayer_average & operator=(const c_bayer_average &) = delete;
+
+  /* c_bayer_average::set_bayer_pattern (c_frame_accumulation.cc:1138-1144) */
+  void set_bayer_pattern(int colorid) { _colorid = colorid; }
+  int bayer_pattern() const { return _colorid; }
+
+  /* c_bayer_average::set_remap (c_frame_accumulation.cc:1151-1159) */
+  void set_remap(const image_transform & t) { _transform = t, _have_transform = true; }
+  void clear_remap() { _have_transform = false; }
+
+  /* c_bayer_average::add(src, weights) (c_frame_accumulation.cc:1175-1203)
+   * for one raw frame (u16 or f32, values times `scale`) with a frame weight */
+  bool add(const image_view & src, float weight = 1.f, double scale = 1.0)
+  {
+    if( !ensure(src.width, src.height) ) return false;
+    float p[12] = { 0 };
+    if( _have_transform ) _transform.fill(p);
+    int32_t st = SST_FRAME_OK;
+    return sst_bayer_average_add_batch(_h, src.data, src.depth, 1, src.stride, src.stride * src.height, scale, 0,
+        _have_transform ? &_transform.model : nullptr, _have_transform ? p : nullptr, &st, &weight, nullptr) == SST_OK;
+  }
+
+  /* c_bayer_average::compute (c_frame_accumulation.cc:1205-1238): avg width x
+   * height x 3 (B, G, R), mask u8 */
+  bool compute(std::vector<float> & avg, std::vector<uint8_t> & mask) const
+  {
+    if( !_h ) return false;
+    avg.resize((size_t) _w * _hh * 3);
+    mask.resize((size_t) _w * _hh);
+    return sst_bayer_average_compute(_h, avg.data(), mask.data(), nullptr, 0, nullptr) == SST_OK;
+  }
+
+  /* c_bayer_average::get_acc_counters (c_frame_accumulation.cc:1240-1250) */
+  bool get_acc_counters(std::vector<float> & accw) const
+  {
+    if( !_h ) return false;
+    accw.resize((size_t) _w * _hh * 3);
+    return sst_bayer_average_compute(_h, nullptr, nullptr, accw.data(), 0, nullptr) == SST_OK;
+  }
+
+  void clear() { if( _h ) sst_bayer_average_clear(_h, nullptr); }
+  int accumulated_frames() const { return _h ? sst_bayer_average_accumulated_frames(_h) : 0; }
+  sst_bayer_average * handle() const { return _h; }
+
+private:
+  bool ensure(int w, int h)
+  {
+    if( _h && w == _w && h == _hh ) return true;
+    if( _h ) return false;
+    if( sst_bayer_average_create(&_h, w, h, _colorid) != SST_OK ) return false;
+    _w = w, _hh = h;
+    return true;
+  }
+  sst_bayer_average * _h = nullptr;
+  int _colorid = SST_COLORID_BAYER_RGGB;
+  image_transform _transform;
+  bool _have_transform = false;
+  int _w = 0, _hh = 0;
 };
 
 }  // namespace sst_gb300

@@ -31,7 +31,7 @@ def build(force: bool = False) -> str:
     srcs = [os.path.join(_HERE, f) for f in sorted(os.listdir(_HERE)) if f.endswith((".cc", ".h")) or f == "Makefile"]
     if force or not os.path.exists(_LIB_PATH) or any(
             os.path.getmtime(s) > os.path.getmtime(_LIB_PATH) for s in srcs):
-        subprocess.check_call(["make", "-s", "-C", _HERE])
+        subprocess.check_call(["make", "-s", "-j8", "-C", _HERE])
     return _LIB_PATH
 
 
@@ -60,6 +60,15 @@ class EcchOpts(C.Structure):
 class PipelineOpts(C.Structure):
     _fields_ = [("ecch", EcchOpts), ("num_passes", C.c_int), ("pass_motion", C.c_int * 3),
                 ("min_rho", C.c_double), ("border_mode", C.c_int), ("use_laplacian_weights", C.c_int)]
+
+
+class RegistrationOpts(C.Structure):
+    """c_ecc_registration_options (c_frame_registration.h:47-63) + motion type."""
+    _fields_ = [("motion_type", C.c_int), ("method", C.c_int), ("scale", C.c_double), ("eps", C.c_double),
+                ("min_rho", C.c_double), ("input_smooth_sigma", C.c_double), ("reference_smooth_sigma", C.c_double),
+                ("update_step_scale", C.c_double), ("max_iterations", C.c_int), ("ecch_max_level", C.c_int),
+                ("ecch_minimum_image_size", C.c_int), ("normalization_scale", C.c_int),
+                ("normalization_noise", C.c_double), ("estimate_translation_first", C.c_int)]
 
 
 _lib = None
@@ -111,6 +120,14 @@ def lib():
             "orc_local_variance_map": (i, [p, i, i, i, i, i, d, p, p, p, p]),
             "orc_average_pyramid_inpaint": (None, [p, p, i, i, i, p, p]),
             "orc_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
+            "orc_pyrdown_border": (None, [p, i, i, p, i, i, i]),
+            "orc_pyrup": (None, [p, i, i, p, i, i]),
+            "orc_mask_pyrdown_ge250": (None, [p, i, i, p, i, i]),
+            "orc_scale_image_size": (None, [i, i, d, p, p]),
+            "orc_scale_image": (None, [p, p, i, i, d, p, p]),
+            "orc_ecc_normalize": (None, [p, p, i, i, i, p]),
+            "orc_register_frame": (i, [p, p, p, i, i, p, p, p, p]),
+            "ref_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
             "orc_set_num_threads": (None, [i]),
             "orc_get_num_threads": (i, []),
         }
@@ -645,3 +662,95 @@ def stack_error_report(frames, frame_scale, motion, gpu_params, gpu_status, gpu_
             "e2e_max": float(e2e.max()), "e2e_median": float(np.median(e2e)),
             "e2e_bound_frac": float(frac.max()), "warp_rms_max": warp_rms, "warp_disp_max": disp_max,
             "weight_rel_diff_max": dw_max, "region_frac": float(keep_o.mean())}
+
+
+def pyrdown_border(img, border, dw=None, dh=None):
+    """cv::pyrDown(src, dst, Size(), border): size ((w + 1) / 2, (h + 1) / 2)."""
+    a = _f64(img)
+    h, w = a.shape
+    if dw is None:
+        dw, dh = (w + 1) // 2, (h + 1) // 2
+    out = np.empty((dh, dw))
+    lib().orc_pyrdown_border(_ptr(a), w, h, _ptr(out), dw, dh, border)
+    return out
+
+
+def pyrup(img, dw, dh):
+    a = _f64(img)
+    out = np.empty((dh, dw))
+    lib().orc_pyrup(_ptr(a), a.shape[1], a.shape[0], _ptr(out), dw, dh)
+    return out
+
+
+def mask_pyrdown_ge250(mask):
+    m = _u8(mask)
+    h, w = m.shape
+    out = np.empty(((h + 1) // 2, (w + 1) // 2), np.uint8)
+    lib().orc_mask_pyrdown_ge250(_ptr(m), w, h, _ptr(out), out.shape[1], out.shape[0])
+    return out
+
+
+def scale_image_size(w, h, scale):
+    dw, dh = C.c_int(), C.c_int()
+    lib().orc_scale_image_size(w, h, scale, C.byref(dw), C.byref(dh))
+    return dw.value, dh.value
+
+
+def scale_image(img, scale, mask=None):
+    """scaleImage (c_frame_registration.cc:230-250) -> (image, mask or None)."""
+    a = _f64(img)
+    h, w = a.shape
+    dw, dh = scale_image_size(w, h, scale)
+    out = np.empty((dh, dw))
+    mo = np.empty((dh, dw), np.uint8) if mask is not None else None
+    lib().orc_scale_image(_ptr(a), _ptr(_u8(mask)), w, h, scale, _ptr(out), _ptr(mo))
+    return out, mo
+
+
+def ecc_normalize(img, lvl, mask=None):
+    a = _f64(img)
+    out = np.empty_like(a)
+    lib().orc_ecc_normalize(_ptr(a), _ptr(_u8(mask)), a.shape[1], a.shape[0], lvl, _ptr(out))
+    return out
+
+
+def registration_opts(motion_type=AFFINE, method=LM, scale=0.5, eps=0.2, min_rho=0.8, input_smooth_sigma=1.0,
+                      reference_smooth_sigma=1.0, update_step_scale=1.5, max_iterations=50, ecch_max_level=0,
+                      ecch_minimum_image_size=16, normalization_scale=0, normalization_noise=0.01,
+                      estimate_translation_first=1) -> RegistrationOpts:
+    """Defaults of c_ecc_registration_options (c_frame_registration.h:47-63) and
+    c_image_registration_options::motion_type (:121)."""
+    return RegistrationOpts(motion_type, method, scale, eps, min_rho, input_smooth_sigma, reference_smooth_sigma,
+                            update_step_scale, max_iterations, ecch_max_level, ecch_minimum_image_size,
+                            normalization_scale, normalization_noise, estimate_translation_first)
+
+
+def register_frame(o: RegistrationOpts, ref, cur, ref_mask=None):
+    """setup_reference_frame + register_frame (ECC part) -> (status, state, rho, iterations)."""
+    r, c = _f64(ref), _f64(cur)
+    h, w = r.shape
+    st = np.zeros(16)
+    rho, it = C.c_double(), C.c_int()
+    status = lib().orc_register_frame(C.byref(o), _ptr(r), _ptr(_u8(ref_mask)), w, h, _ptr(c), _ptr(st),
+                                      C.byref(rho), C.byref(it))
+    return status, st, rho.value, it.value
+
+
+def refcpu_register_and_stack(o: PipelineOpts, ref, frames, frame_scale):
+    """The FP32 reference-semantics CPU restatement (sst_refcpu.cc, the timed
+    CPU baseline): register_frame with c_ecch over the motion passes, the
+    correlation gate, base_remap and the FP32 running weighted mean, with the
+    reference's sequence of full-image passes. Returns (states, status, rho,
+    mean, weight sum)."""
+    r = np.ascontiguousarray(ref, dtype=np.float32)
+    fr = np.ascontiguousarray(frames, dtype=np.uint16)
+    n = fr.shape[0]
+    h, w = r.shape
+    states = np.zeros((n, 16))
+    status = np.zeros(n, np.int32)
+    rho = np.zeros(n)
+    acc = np.zeros((h, w), np.float32)
+    accw = np.zeros((h, w), np.float32)
+    lib().ref_register_and_stack(C.byref(o), _ptr(r), w, h, _ptr(fr), n, frame_scale, _ptr(states), _ptr(status),
+                                 _ptr(rho), _ptr(acc), _ptr(accw))
+    return states, status, rho, acc, accw

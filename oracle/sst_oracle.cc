@@ -842,6 +842,30 @@ extern "C" int orc_ecch_align(const orc_model * m, double * state, const orc_ecc
   return ecch_align_pyr(m, state, o, R, C, iters, eps);
 }
 
+/* c_ecch::align(current) after set_reference_image(reference, reference_mask)
+ * (ecc2.cc:984-1176) on w x h images, then compute_correlation of the
+ * result against the level-0 reference and its mask
+ * (c_frame_registration.cc:837-839); rho may be NULL */
+extern "C" int orc_ecch_align_pyramids(const orc_model * m, double * state, const orc_ecch_opts * o,
+    const double * ref, const uint8_t * ref_mask, const double * cur, int w, int h, int * iters, double * eps,
+    double * rho)
+{
+  const int lv = orc_ecch_num_levels(w, h, o);
+  std::vector<pyr_level> R, C;
+  build_pyramid(ref, ref_mask, w, h, o->reference_smooth_sigma, lv, false, R);
+  build_pyramid(cur, nullptr, w, h, o->input_smooth_sigma, lv, true, C);
+  int it = 0;
+  double e = 0;
+  ecch_align_pyr(m, state, o, R, C, &it, &e);
+  if( iters ) *iters = it;
+  if( eps ) *eps = e;
+  if( rho ) {
+    *rho = orc_correlation(C[0].img.data(), nullptr, w, h, R[0].img.data(), R[0].mask.empty() ? nullptr : R[0].mask.data(),
+        w, h, m, state);
+  }
+  return 1;
+}
+
 /* compute_correlation(current, current_mask, reference, reference_mask, rmap)
  * (ecc2.cc:65-137): remap LINEAR / BORDER_CONSTANT, mask >= 254 */
 extern "C" double orc_correlation(const double * cur, const uint8_t * cur_mask, int cw, int ch,

@@ -223,6 +223,33 @@ int orc_register_and_stack(const orc_pipeline_opts * o,
     double * out_states /* n x 16 */, int * out_status, double * out_rho,
     double * acc, double * accw);
 
+/* c_ecch::align + compute_correlation on w x h images (see sst_oracle.cc) */
+int orc_ecch_align_pyramids(const orc_model * m, double * state, const orc_ecch_opts * o,
+    const double * ref, const uint8_t * ref_mask, const double * cur, int w, int h, int * iters, double * eps,
+    double * rho);
+
+/* c_ecc_registration_options (c_frame_registration.h:47-63) with the
+ * motion type of c_image_registration_options (:119-137) */
+typedef struct orc_registration_opts {
+  int motion_type;
+  int method;
+  double scale, eps, min_rho, input_smooth_sigma, reference_smooth_sigma, update_step_scale;
+  int max_iterations, ecch_max_level, ecch_minimum_image_size;
+  int normalization_scale;
+  double normalization_noise;
+  int estimate_translation_first;
+} orc_registration_opts;
+
+void orc_pyrdown_border(const double * src, int w, int h, double * dst, int dw, int dh, int border);
+void orc_pyrup(const double * src, int sw, int sh, double * dst, int dw, int dh);
+void orc_mask_pyrdown_ge250(const uint8_t * src, int w, int h, uint8_t * dst, int dw, int dh);
+void orc_scale_image_size(int w, int h, double scale, int * dw, int * dh);
+void orc_scale_image(const double * src, const uint8_t * mask, int w, int h, double scale, double * dst,
+    uint8_t * dst_mask);
+void orc_ecc_normalize(const double * src, const uint8_t * mask, int w, int h, int lvl, double * dst);
+int orc_register_frame(const orc_registration_opts * o, const double * ref, const uint8_t * ref_mask,
+    int w, int h, const double * cur, double * state, double * rho, int * iters);
+
 void orc_set_num_threads(int n);
 int  orc_get_num_threads(void);
 

@@ -21,6 +21,7 @@ from . import build as _build
 
 # status / enums (serstacker_gb300.h)
 SST_OK = 0
+ERR_INVALID_ARG, ERR_CUDA, ERR_UNSUPPORTED, ERR_STATE, ERR_NOMEM, ERR_TIMEOUT, ERR_IO = -1, -2, -3, -4, -5, -6, -7
 FRAME_OK, FRAME_SINGULAR, FRAME_EMPTY_MASK, FRAME_LOW_RHO, FRAME_NAN, FRAME_NOT_INVERTIBLE = range(6)
 TRANSLATION, EUCLIDEAN, SCALED_EUCLIDEAN, AFFINE, HOMOGRAPHY, SEMI_QUADRATIC, QUADRATIC, EPIPOLAR = range(8)
 FA, IC, LM, ICLM = range(4)
@@ -57,6 +58,33 @@ class EcchOptions(C.Structure):
                 ("update_step_scale", C.c_double), ("method", C.c_int32), ("interpolation", C.c_int32),
                 ("max_iterations", C.c_int32), ("minimum_image_size", C.c_int32), ("maxlevel", C.c_int32),
                 ("min_rho", C.c_double), ("ic_jacobian_at_identity", C.c_int32), ("reserved", C.c_int32)]
+
+
+class EccRegistrationOptions(C.Structure):
+    """c_ecc_registration_options (c_frame_registration.h:47-63)."""
+    _fields_ = [("scale", C.c_double), ("eps", C.c_double), ("min_rho", C.c_double),
+                ("input_smooth_sigma", C.c_double), ("reference_smooth_sigma", C.c_double),
+                ("update_step_scale", C.c_double), ("normalization_noise", C.c_double), ("se_radius", C.c_int32),
+                ("ecc_method", C.c_int32), ("max_iterations", C.c_int32), ("ecch_max_level", C.c_int32),
+                ("ecch_minimum_image_size", C.c_int32), ("normalization_scale", C.c_int32),
+                ("ecch_estimate_translation_first", C.c_int32), ("replace_planetary_disk_with_mask", C.c_int32)]
+
+
+class EccflowRegistrationOptions(C.Structure):
+    """c_eccflow_registration_options (c_frame_registration.h:88-100)."""
+    _fields_ = [("update_multiplier", C.c_double), ("input_smooth_sigma", C.c_double),
+                ("reference_smooth_sigma", C.c_double), ("noise_level", C.c_double), ("scale_factor", C.c_double),
+                ("max_iterations", C.c_int32), ("support_scale", C.c_int32), ("min_image_size", C.c_int32),
+                ("max_pyramid_level", C.c_int32), ("downscale_method", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ImageRegistrationOptions(C.Structure):
+    """c_image_registration_options (c_frame_registration.h:119-137)."""
+    _fields_ = [("motion_type", C.c_int32), ("ecc_registration_channel", C.c_int32), ("interpolation", C.c_int32),
+                ("border_mode", C.c_int32), ("border_value", C.c_double), ("ecc", EccRegistrationOptions),
+                ("eccflow", EccflowRegistrationOptions), ("enable_feature_registration", C.c_int32),
+                ("enable_ecc_registration", C.c_int32), ("enable_eccflow_registration", C.c_int32),
+                ("accumulate_and_compensate_turbulent_flow", C.c_int32)]
 
 
 _lib = None
@@ -142,6 +170,17 @@ def lib():
             "sst_ser_writer_close": (i, [p]),
             "sst_average_pyramid_inpaint": (i, [p, sz, p, sz, i, i, i, p, sz, p, sz, i, p]),
             "sst_calibrate_frames": (i, [p, i, i, i, i, sz, sz, d, p, sz, p, sz, p, sz, sz, p]),
+            "sst_image_registration_options_default": (None, [p]),
+            "sst_frame_registration_create": (i, [p, p]),
+            "sst_frame_registration_destroy": (i, [p]),
+            "sst_frame_registration_setup_reference_frame": (i, [p, p, i, i, i, sz, d, p, sz, i, p]),
+            "sst_frame_registration_register_frames": (i, [p, p, i, i, i, i, sz, sz, d, i, p, p, p, p, p, p]),
+            "sst_frame_registration_set_chunk_frames": (i, [p, i]),
+            "sst_frame_registration_ecc_size": (i, [p, p, p]),
+            "sst_frame_registration_ecc_image": (i, [p, i, p, p, i]),
+            "sst_remap_rmap": (i, [p, i, i, i, sz, d, p, i, i, i, d, p, sz, p, p, i, p]),
+            "sst_image_transform_scale": (i, [p, p, d]),
+            "sst_image_transform_create_remap": (i, [p, p, i, i, p, i, p]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(_lib, name)
@@ -837,3 +876,119 @@ def bayer_planes(raw: np.ndarray, average: bool = False):
         _check(lib().sst_extract_bayer_planes_u16(d.data_ptr(), w, h, r.strides[0], out.data_ptr(), None), "bayer")
     torch.cuda.synchronize()
     return out.cpu().numpy().view(np.uint16)
+
+
+# ------------------------------------------------------------ frame registration
+
+def image_registration_options(ecc=None, eccflow=None, **kw) -> ImageRegistrationOptions:
+    """The reference defaults (sst_image_registration_options_default), then
+    `kw` on the top level, `ecc` / `eccflow` dicts on the nested options.
+    Feature registration is switched off and ECC registration on unless kw says
+    otherwise."""
+    o = ImageRegistrationOptions()
+    lib().sst_image_registration_options_default(C.byref(o))
+    o.enable_feature_registration = 0
+    o.enable_ecc_registration = 1
+    for k, v in kw.items():
+        setattr(o, k, v)
+    for k, v in (ecc or {}).items():
+        setattr(o.ecc, k, v)
+    for k, v in (eccflow or {}).items():
+        setattr(o.eccflow, k, v)
+    return o
+
+
+class c_frame_registration:
+    """c_frame_registration (c_frame_registration.h:210-356) over the C ABI."""
+
+    def __init__(self, options: Optional[ImageRegistrationOptions] = None, **kw):
+        self.options = options if options is not None else image_registration_options(**kw)
+        self._h = C.c_void_p()
+        _check(lib().sst_frame_registration_create(C.byref(self._h), C.byref(self.options)),
+               "sst_frame_registration_create")
+        self.width = self.height = 0
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().sst_frame_registration_destroy(self._h)
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def setup_reference_frame(self, image: np.ndarray, mask: Optional[np.ndarray] = None, scale: float = 1.0):
+        a = np.ascontiguousarray(image)
+        m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+        _check(lib().sst_frame_registration_setup_reference_frame(
+            self._h, _ptr(a), _NP_DEPTH[a.dtype], a.shape[1], a.shape[0], a.strides[0], scale, _ptr(m),
+            0 if m is None else m.strides[0], 0, None), "setup_reference_frame")
+        self.height, self.width = a.shape
+
+    def register_frames(self, frames: np.ndarray, scale: float = 1.0, rmap: bool = False):
+        fr = np.ascontiguousarray(frames)
+        if fr.ndim == 2:
+            fr = fr[None]
+        n, hh, ww = fr.shape
+        out = {"params": np.zeros((n, 12), np.float32), "status": np.zeros(n, np.int32),
+               "rho": np.zeros(n, np.float32), "iterations": np.zeros(n, np.int32),
+               "rmap": np.zeros((n, hh, ww, 2), np.float32) if rmap else None}
+        _check(lib().sst_frame_registration_register_frames(
+            self._h, _ptr(fr), _NP_DEPTH[fr.dtype], n, ww, hh, fr.strides[1], fr.strides[0], scale, 0,
+            _ptr(out["params"]), _ptr(out["status"]), _ptr(out["rho"]), _ptr(out["iterations"]), _ptr(out["rmap"]),
+            None), "register_frames")
+        return out
+
+    def set_chunk_frames(self, n: int):
+        _check(lib().sst_frame_registration_set_chunk_frames(self._h, n), "set_chunk_frames")
+
+    def ecc_size(self):
+        w, h = C.c_int(), C.c_int()
+        _check(lib().sst_frame_registration_ecc_size(self._h, C.byref(w), C.byref(h)), "ecc_size")
+        return w.value, h.value
+
+    def ecc_image(self, frame: int = -1, with_mask: bool = False):
+        w, h = self.ecc_size()
+        out = np.zeros((h, w), np.float32)
+        m = np.zeros((h, w), np.uint8) if with_mask else None
+        _check(lib().sst_frame_registration_ecc_image(self._h, frame, _ptr(out), _ptr(m), 0), "ecc_image")
+        return (out, m) if with_mask else out
+
+
+def remap_rmap(src: np.ndarray, rmap: np.ndarray, border: int = BORDER_REFLECT101, border_value: float = 0.0,
+               src_mask=None, scale: float = 1.0):
+    """sst_remap_rmap on host arrays: (dst, dst_mask)."""
+    s = np.ascontiguousarray(src)
+    rm = np.ascontiguousarray(rmap, np.float32)
+    dh, dw = rm.shape[:2]
+    msk = None if src_mask is None else np.ascontiguousarray(src_mask, np.uint8)
+    dst = np.zeros((dh, dw), np.float32)
+    dmask = np.zeros((dh, dw), np.uint8)
+    _check(lib().sst_remap_rmap(_ptr(s), _NP_DEPTH[s.dtype], s.shape[1], s.shape[0], s.strides[0], scale, _ptr(rm),
+                                dw, dh, border, border_value, _ptr(msk), 0 if msk is None else msk.strides[0],
+                                _ptr(dst), _ptr(dmask), 0, None), "sst_remap_rmap")
+    return dst, dmask
+
+
+def create_remap(motion_type: int, params, width: int, height: int) -> np.ndarray:
+    """sst_image_transform_create_remap: (height, width, 2) map of W(x, y; params)."""
+    m = motion(motion_type)
+    p = np.zeros(12, np.float32)
+    pp = np.asarray(params, np.float32).ravel()
+    p[:pp.size] = pp
+    out = np.zeros((height, width, 2), np.float32)
+    _check(lib().sst_image_transform_create_remap(C.byref(m), _ptr(p), width, height, _ptr(out), 0, None),
+           "create_remap")
+    return out
+
+
+def scale_transform(motion_type: int, params, factor: float) -> np.ndarray:
+    """sst_image_transform_scale: scale_transfrom(factor) of a parameter vector."""
+    m = motion(motion_type)
+    p = np.zeros(12, np.float32)
+    pp = np.asarray(params, np.float32).ravel()
+    p[:pp.size] = pp
+    _check(lib().sst_image_transform_scale(C.byref(m), _ptr(p), factor), "scale_transform")
+    return p[:nparams(motion_type)]

@@ -183,6 +183,7 @@ struct sst_ecch {
   int last_steps[3][32];
   int last_method = 0;
   int last_n = 0;                 // frames whose pyramids the batch buffer holds
+  double gate[3] = { 0, 0, 0 };   // correlation gate after pass k < last (0: none)
 
   ~sst_ecch()
   {
@@ -282,6 +283,15 @@ extern "C" int sst_set_chunk_frames(sst_ecch * h, int frames)
 {
   if( !h || frames < 1 ) return set_error(SST_ERR_INVALID_ARG, "invalid chunk size");
   h->chunk = frames;
+  return SST_OK;
+}
+
+/* correlation gates after passes 0 .. num - 1 of the following registrations
+ * (0: none); used by the frame-registration glue (sst_registration.cu) */
+int sst_internal_ecch_set_pass_gates(sst_ecch * h, int num, const double * gates)
+{
+  if( !h || num < 0 || num > 3 ) return set_error(SST_ERR_INVALID_ARG, "invalid pass gates");
+  for( int k = 0; k < 3; ++k ) h->gate[k] = k < num && gates ? gates[k] : 0.0;
   return SST_OK;
 }
 
@@ -602,6 +612,35 @@ static int add_level_loop(sst_ecch * h, cudaStream_t st, Body body)
   return SST_OK;
 }
 
+/* compute_correlation of every frame still registering against the level-0
+ * reference under the model's current state, and the gate rho >= min_rho
+ * (min_rho <= 0: rho only) */
+static int enqueue_correlation(sst_ecch * h, int n, const sst_motion_model & model, double min_rho, cudaStream_t st)
+{
+  const int grid = std::max(1, h->num_sms) * 4;
+  CorrArgs c;
+  memset(&c, 0, sizeof(c));
+  c.pyr = h->pyr.as<float>();
+  c.pyr_stride = h->pyr_px;
+  c.w = h->w, c.h = h->h;
+  c.tiles = tiles_of(h->w, h->h, PW_TX, PW_TY, &c.tiles_x);
+  c.refT = h->ref.as<float>();
+  c.refM = h->has_mask ? h->mask.as<uint8_t>() : nullptr;
+  c.tshift = h->tshift[0];
+  c.fs = h->fs.as<FrameState>();
+  c.n = n;
+  c.partials = h->part.as<double>();
+  c.part_stride = h->part_stride;
+  c.counters = h->cnt.as<unsigned>();
+  c.model = model;
+  c.min_rho = min_rho;
+  c.err = h->err.as<int>();
+  CUtensorMap cmap;
+  const bool cstaged = encode_pass_level(h->pyr.as<float>(), h->w, h->h, h->pyr_px, h->cap, &cmap);
+  SST_CK_LAUNCH(launch_correlation(c, grid, st, cstaged ? &cmap : nullptr));
+  return SST_OK;
+}
+
 /* The Gauss-Newton schedule of one batch: pass begin, per level a level
  * begin and max_iterations + 1 pass launches, then the correlation. In
  * host-driven mode every step is followed by a synchronisation and an early
@@ -727,27 +766,14 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
       SST_CK(record_prof(h->prof[k_pass][l][1], st, host_driven));
       step += max_it + 2;
     }
+    // an intermediate correlation gate (register_frame's translation estimate,
+    // c_frame_registration.cc:825-834): frames below it stop registering
+    if( k_pass + 1 < num_passes && h->gate[k_pass] > 0 ) {
+      SST_TRY(enqueue_correlation(h, n, m, h->gate[k_pass], st));
+      k += 2;
+    }
   }
-  CorrArgs c;
-  memset(&c, 0, sizeof(c));
-  c.pyr = h->pyr.as<float>();
-  c.pyr_stride = h->pyr_px;
-  c.w = h->w, c.h = h->h;
-  c.tiles = tiles_of(h->w, h->h, PW_TX, PW_TY, &c.tiles_x);
-  c.refT = h->ref.as<float>();
-  c.refM = h->has_mask ? h->mask.as<uint8_t>() : nullptr;
-  c.tshift = h->tshift[0];
-  c.fs = fs;
-  c.n = n;
-  c.partials = h->part.as<double>();
-  c.part_stride = h->part_stride;
-  c.counters = h->cnt.as<unsigned>();
-  c.model = passes[num_passes - 1];
-  c.min_rho = h->o.min_rho;
-  c.err = h->err.as<int>();
-  CUtensorMap cmap;
-  const bool cstaged = encode_pass_level(h->pyr.as<float>(), h->w, h->h, h->pyr_px, h->cap, &cmap);
-  SST_CK_LAUNCH(launch_correlation(c, grid, st, cstaged ? &cmap : nullptr));
+  SST_TRY(enqueue_correlation(h, n, passes[num_passes - 1], h->o.min_rho, st));
   k += 2;
   if( kernels ) *kernels = k;
   return SST_OK;
@@ -856,6 +882,9 @@ static int register_device(sst_ecch * h, const void * d_frames, int depth, int n
     for( int k = 0; k < num_passes; ++k ) {
       key.push_back(passes[k].type);
       key.push_back(passes[k].fix_scale);
+      long long g;
+      memcpy(&g, &h->gate[k], sizeof(g));
+      key.push_back(g);
     }
     GraphEntry * ge = nullptr;
     for( auto & g : h->graphs ) if( g.key == key ) ge = &g;

@@ -53,7 +53,8 @@ def test_kernel_launch_counter(capi):
 
 def test_cpp_dropin_header_compiles_and_links(capi, tmp_path):
     """The C++ drop-in classes (include/serstacker_gb300.hpp) compile against the C ABI
-    and run their host-only parts (option defaults, handle creation) without a GPU."""
+    and run their host-only parts (option defaults, handle creation, the
+    rejection of feature registration, scale_transfrom) without a GPU."""
     import os
     import shutil
     import subprocess
@@ -89,6 +90,25 @@ int main() {
   if( !wr.create(SER_OUT, 6, 4, 0, 12) || !wr.write(f.data(), 77) || !wr.close() ) return 11;
   sst_gb300::c_ser_reader back(SER_OUT);
   if( back.num_frames() != 1 || back.timestamps()[0] != 77 ) return 12;
+  sst_gb300::c_image_registration_options ro;
+  if( ro.ecc.scale != 0.5 || ro.ecc.eps != 0.2 || ro.ecc.ecc_method != SST_ECC_LM || ro.ecc.update_step_scale != 1.5 ||
+      ro.ecc.ecch_max_level != 0 || !ro.ecc.ecch_estimate_translation_first || ro.eccflow.scale_factor != 0.75 ||
+      ro.eccflow.support_scale != 4 || ro.motion_type != SST_MOTION_AFFINE || !ro.enable_feature_registration )
+    return 13;
+  sst_gb300::c_frame_registration fr(ro);
+  std::vector<float> ref(64 * 48, 1.f);
+  if( fr.setup_reference_frame(sst_gb300::image_view(ref.data(), 64, 48, SST_DEPTH_F32, 64 * 4)) ) return 14;
+  if( sst_gb300::last_error().find("feature registration") == std::string::npos ) return 15;
+  sst_gb300::image_transform ht(SST_MOTION_HOMOGRAPHY);
+  ht.parameters = { 1.f, 0.f, 3.f, 0.f, 1.f, -2.f, 1e-5f, 0.f };
+  if( !ht.scale_transfrom(2.0) || ht.parameters[2] != 6.f || ht.parameters[5] != -4.f || ht.parameters[6] != 5e-6f )
+    return 16;
+  if( sizeof(sst_image_registration_options) != 192 ) return 17;
+  sst_gb300::c_bayer_average ba;
+  ba.set_bayer_pattern(SST_COLORID_BAYER_GRBG);
+  if( ba.bayer_pattern() != SST_COLORID_BAYER_GRBG ) return 18;
+  sst_gb300::c_eccflow_options fo;
+  if( fo.support_scale != 5 || fo.scale_factor != 0.5 ) return 19;
   std::printf("ok %s\n", sst_version());
   return 0;
 }
@@ -148,3 +168,53 @@ def test_calibration_argument_checks(capi):
     assert lib.sst_calibrate_frames(1, 3, 1, 8, 8, 16, 128, 1.0, None, 0, None, 0, 1, 0, 0, None) == -1
     assert lib.sst_calibrate_frames(1, capi.DEPTH_U16, 2, 8, 8, 16, 100, 1.0, None, 0, None, 0, 1, 0, 0, None) == -1
     assert lib.sst_calibrate_frames(1, capi.DEPTH_U16, 1, 8, 8, 15, 128, 1.0, None, 0, None, 0, 1, 0, 0, None) == -1
+
+
+def test_registration_options_mirror_the_c_struct(capi):
+    """The ctypes mirror of sst_image_registration_options has the C layout
+    (192 bytes, checked in the compiled C++ test too) and the reference
+    defaults of c_frame_registration.h:47-137."""
+    import ctypes
+    assert ctypes.sizeof(capi.ImageRegistrationOptions) == 192
+    o = capi.ImageRegistrationOptions()
+    capi.lib().sst_image_registration_options_default(ctypes.byref(o))
+    assert (o.motion_type, o.ecc_registration_channel, o.interpolation, o.border_mode) == (3, 104, 1, 4)
+    assert (o.ecc.scale, o.ecc.eps, o.ecc.min_rho, o.ecc.update_step_scale) == (0.5, 0.2, 0.8, 1.5)
+    assert (o.ecc.ecc_method, o.ecc.max_iterations, o.ecc.ecch_max_level, o.ecc.ecch_minimum_image_size) == (2, 50, 0, 16)
+    assert (o.ecc.normalization_scale, o.ecc.ecch_estimate_translation_first, o.ecc.se_radius) == (0, 1, 5)
+    assert (o.eccflow.update_multiplier, o.eccflow.scale_factor, o.eccflow.max_iterations) == (1.5, 0.75, 3)
+    assert (o.eccflow.support_scale, o.eccflow.min_image_size, o.eccflow.max_pyramid_level) == (4, -1, -1)
+    assert (o.enable_feature_registration, o.enable_ecc_registration, o.enable_eccflow_registration) == (1, 0, 0)
+
+
+def test_frame_registration_rejects_unsupported_options(capi):
+    import ctypes
+    h = ctypes.c_void_p()
+    o = capi.ImageRegistrationOptions()
+    capi.lib().sst_image_registration_options_default(ctypes.byref(o))
+    assert capi.lib().sst_frame_registration_create(ctypes.byref(h), ctypes.byref(o)) == capi.ERR_UNSUPPORTED
+    assert "feature registration" in capi.last_error()
+    o.enable_feature_registration = 0
+    assert capi.lib().sst_frame_registration_create(ctypes.byref(h), ctypes.byref(o)) == capi.ERR_INVALID_ARG
+    o.enable_ecc_registration = 1
+    o.ecc.replace_planetary_disk_with_mask = 1
+    assert capi.lib().sst_frame_registration_create(ctypes.byref(h), ctypes.byref(o)) == capi.ERR_UNSUPPORTED
+    o.ecc.replace_planetary_disk_with_mask = 0
+    assert capi.lib().sst_frame_registration_create(ctypes.byref(h), ctypes.byref(o)) == 0
+    assert capi.lib().sst_frame_registration_register_frames(h, ctypes.c_void_p(1), 2, 1, 64, 48, 128, 128 * 48, 1.0,
+                                                             0, None, None, None, None, None, None) == capi.ERR_STATE
+    capi.lib().sst_frame_registration_destroy(h)
+
+
+def test_scale_transform_matches_oracle(capi, oracle):
+    """sst_image_transform_scale (scale_transfrom) against the oracle's for
+    every model."""
+    import numpy as np
+    O = oracle
+    rng = np.random.default_rng(3)
+    for t in (0, 1, 2, 3, 4, 5, 6):
+        m = O.model(t)
+        p = O.get_params(m, O.identity(m)) + rng.normal(0, 1e-3, O.nparams(m))
+        want = O.get_params(m, O.scale(m, O.set_params(m, O.identity(m), p), 0.5))
+        got = capi.scale_transform(t, p, 0.5)
+        assert np.allclose(got, want, rtol=1e-6, atol=1e-6), t

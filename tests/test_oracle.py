@@ -568,3 +568,127 @@ def test_stack_error_report_separates_arithmetic_from_registration(oracle):
     assert rep["e2e_max"] > 1e-5, rep
     assert rep["e2e_bound_frac"] <= 1.0, rep
     assert 0.005 < rep["warp_disp_max"] < 0.02, rep
+
+
+def test_pyrup_known_answers(oracle):
+    """cv::pyrUp: zero insertion + 4 x [1 4 6 4 1] / 16, BORDER_REFLECT_101 on the
+    2w grid, a 2w - 1 destination keeps the first 2w - 1 samples."""
+    O = oracle
+    assert np.allclose(O.pyrup(np.full((5, 7), 3.25), 14, 10), 3.25)
+    assert np.allclose(O.pyrup(np.full((5, 7), 3.25), 13, 9), 3.25)
+    s = np.zeros((1, 8))
+    s[0, 3] = 1.0
+    up = O.pyrup(np.repeat(s, 4, axis=0), 16, 8)[3]
+    assert np.allclose(up[4:9], [1 / 8, 1 / 2, 6 / 8, 1 / 2, 1 / 8]) and np.allclose(up[:4], 0) and np.allclose(up[9:], 0)
+    r = np.arange(1.0, 9.0)[None].repeat(4, axis=0)          # right edge: reflect on the 2w grid
+    up = O.pyrup(r, 16, 8)[0]
+    assert np.isclose(up[14], (7 + 7 * 8) / 8) and np.isclose(up[15], 8.0)
+    assert np.isclose(up[0], (2 + 6 * 1 + 2) / 8)
+    up_odd = O.pyrup(r, 15, 8)[0]
+    assert np.allclose(up_odd, up[:15])
+    ramp = np.add.outer(np.arange(6.0) * 0.5, np.arange(9.0) * 2.0)
+    assert np.allclose(O.pyrup(ramp, 18, 12)[2:-2, 2:-2],
+                       np.add.outer(np.arange(12.0) * 0.25, np.arange(18.0))[2:-2, 2:-2])
+
+
+def test_pyrdown_border_and_mask_threshold(oracle):
+    O = oracle
+    a = np.arange(30, dtype=np.float64).reshape(5, 6)
+    rep = O.pyrdown_border(a, O.BORDER_REPLICATE)
+    r101 = O.pyrdown_border(a, O.BORDER_REFLECT101)
+    assert rep.shape == (3, 3) and r101.shape == (3, 3)
+    k = np.array([1, 4, 6, 4, 1]) / 16.0
+
+    def ref(border):
+        idx = lambda p, n: (min(max(p, 0), n - 1) if border == O.BORDER_REPLICATE else
+                            (abs(p) if p < 0 else (2 * (n - 1) - p if p >= n else p)))
+        out = np.zeros((3, 3))
+        for y in range(3):
+            for x in range(3):
+                out[y, x] = sum(k[j] * k[i] * a[idx(2 * y + j - 2, 5), idx(2 * x + i - 2, 6)]
+                                for j in range(5) for i in range(5))
+        return out
+    assert np.allclose(rep, ref(O.BORDER_REPLICATE)) and np.allclose(r101, ref(O.BORDER_REFLECT101))
+    # u8 pyrDown ((sum + 128) >> 8) then >= 250: one zero pixel under a tap of weight
+    # 1 or 4 keeps the output, weight 6 or more clears it
+    for (j, i), keep in [((0, 0), True), ((0, 1), True), ((0, 2), False), ((1, 1), False), ((2, 2), False)]:
+        m = np.full((12, 12), 255, np.uint8)
+        m[4 + j - 2, 4 + i - 2] = 0       # tap (j, i) of output (2, 2), weight k_j k_i of 1 4 6 4 1
+        out = O.mask_pyrdown_ge250(m)
+        assert (out[2, 2] == 255) == keep, (j, i)
+        assert (out == 0).sum() <= 5
+
+
+def test_ecc_normalize_known_answers(oracle):
+    """ecc_normalize removes the pyramid background: zero on constant images,
+    zero on linear ramps away from the border, zero outside the mask."""
+    O = oracle
+    assert np.allclose(O.ecc_normalize(np.full((40, 56), 7.0), 2), 0)
+    ramp = np.add.outer(np.arange(48.0) * 0.3, np.arange(64.0) * 0.7)
+    nz = O.ecc_normalize(ramp, 2)
+    assert np.abs(nz[12:-12, 12:-12]).max() < 1e-12
+    rng = np.random.default_rng(3)
+    img = rng.random((33, 47))
+    mask = (rng.random((33, 47)) > 0.2).astype(np.uint8) * 255
+    out = O.ecc_normalize(img, 1, mask)
+    assert np.all(out[mask == 0] == 0)
+    assert np.allclose(out[mask > 0], (img - O.ecc_normalize(img, 1) * 0 - (img - O.ecc_normalize(img, 1)))[mask > 0])
+
+
+def test_register_frame_scaled_recovers_warps(oracle):
+    """register_frame with the reference's defaults (scale 0.5: registration on
+    the pyrDown'ed images, the transform scaled back; eps tightened to 0.01) and
+    with translation-first on a 3-level IC pyramid (step 1: the default step
+    of 1.5 overshoots) recovers exactly rendered warps; a frame of noise is
+    rejected by the correlation gate."""
+    from serstacker_gb300 import synth
+    O = oracle
+    w, h = 192, 144
+    sc = synth.Scene(w, h, 45.0, band_period=16.0)
+    ref = synth.reference_np(sc)
+    m = O.model(O.AFFINE)
+    H = np.array([[1.002, -0.004, 2.6], [0.003, 0.999, -1.7], [0, 0, 1.0]])
+    cur = synth.render_frame_np(sc, H)
+    for kw in (dict(eps=0.01), dict(method=O.IC, ecch_max_level=3, eps=0.01, update_step_scale=1.0),
+               dict(method=O.IC, ecch_max_level=3, eps=0.01, update_step_scale=1.0, normalization_scale=2, scale=1.0)):
+        o = O.registration_opts(**kw)
+        status, st, rho, it = O.register_frame(o, ref, cur)
+        assert status == 0 and rho > 0.99, (kw, status, rho)
+        gx, gy = O.warp_grid(m, st, w, h)
+        yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+        tx = H[0, 0] * xx + H[0, 1] * yy + H[0, 2]
+        ty = H[1, 0] * xx + H[1, 1] * yy + H[1, 2]
+        rms = np.sqrt(np.mean((gx - tx) ** 2 + (gy - ty) ** 2))
+        assert rms < 0.02, (kw, rms)
+    noise = np.random.default_rng(4).random((h, w)) * 200
+    status, _, rho, _ = O.register_frame(O.registration_opts(method=O.IC, ecch_max_level=3), ref, noise)
+    assert status == 3 and rho < 0.6
+
+
+def test_fp32_baseline_restatement_matches_oracle(oracle):
+    """The timed CPU baseline (oracle/sst_refcpu.cc: FP32 images, the
+    reference's sequence of full-image passes, FP32 running mean) registers
+    like the FP64 oracle (0.02 px) and stacks within FP32 running-mean error."""
+    from serstacker_gb300 import synth
+    O = oracle
+    w, h, n = 192, 144, 3
+    sc = synth.Scene(w, h, 0.28 * min(w, h))
+    frames, _, _ = synth.make_sequence_np(sc, n, seed=12, kind="config1", dtype=np.uint16, gain=64.0,
+                                          blur_range=(0.8, 2.0))
+    scale = 1.0 / 65535.0
+    ref = synth.reference_np(sc) * 64.0 * scale
+    po = O.pipeline_opts(passes=(O.AFFINE, O.HOMOGRAPHY), method=O.IC, maxlevel=3, max_iterations=40, epsx=0.01,
+                         min_rho=0.5, minimum_image_size=16)
+    st_o, s_o, r_o, S, W = O.register_and_stack(po, ref, frames, scale)
+    st_r, s_r, r_r, A, Wr = O.refcpu_register_and_stack(po, ref, frames, scale)
+    assert np.array_equal(s_o, s_r)
+    m = O.model(O.HOMOGRAPHY)
+    for i in range(n):
+        xa, ya = O.warp_grid(m, st_o[i], w, h)
+        xb, yb = O.warp_grid(m, st_r[i], w, h)
+        assert np.sqrt(((xa - xb) ** 2 + (ya - yb) ** 2).mean()) < 0.02
+        assert abs(r_o[i] - r_r[i]) < 1e-4
+    assert ((W > 0) == (Wr > 0)).mean() > 0.995
+    both = (W > 0) & (Wr > 0)
+    rel = O.stack_rel_err(A[both], S[both] / W[both])
+    assert np.median(rel) < 1e-4
