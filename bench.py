@@ -285,6 +285,7 @@ def main():
                     help="frames of the cpu_baseline sample (the FP32 CPU restatement on all host cores)")
     ap.add_argument("--plain-frames", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no autotuner)")
     ap.add_argument("--accuracy-frames", type=int, default=48,
                     help="frames of the workload checked against the FP64 oracle (0: skip)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
@@ -292,9 +293,10 @@ def main():
     ap.add_argument("--unrolled-schedule", action="store_true",
                     help="level iterations as the unrolled launch schedule instead of graph WHILE loops "
                          "(per-kernel profilers do not profile kernels of graphs with conditional nodes)")
-    ap.add_argument("--workload", choices=["mono", "bayer", "roi", "flow"], default="mono",
+    ap.add_argument("--workload", choices=["mono", "bayer", "roi", "flow", "config0"], default="mono",
                     help="mono: the headline 1280x960 sequence; bayer: raw RGGB 3096x2080 frames; "
-                         "roi: uneven-ROI crops (--frames crops)")
+                         "roi: uneven-ROI crops (--frames crops); flow: c_eccflow on 1024^2 frames; "
+                         "config0: 64 u8 640x480 frames, plain FA euclidean")
     ap.add_argument("--roi-method", choices=["fa", "lm"], default="fa")
     ap.add_argument("--roi-sample", type=int, default=8, help="crops checked against the oracle")
     ap.add_argument("--flow-sample", type=int, default=32, help="frames checked against the oracle (flow)")
@@ -324,8 +326,9 @@ def main():
             import torch.distributed as dist
             dist.destroy_process_group()
         return
-    if args.workload in ("bayer", "roi", "flow"):
-        {"bayer": main_bayer, "roi": main_roi, "flow": main_flow}[args.workload](args, ws, rank, local)
+    if args.workload in ("bayer", "roi", "flow", "config0"):
+        {"bayer": main_bayer, "roi": main_roi, "flow": main_flow, "config0": main_config0}[args.workload](
+            args, ws, rank, local)
         if ws > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
@@ -350,6 +353,13 @@ def main():
                "status": torch.zeros(n, dtype=torch.int32, device=device),
                "rho": torch.zeros(n, dtype=torch.float32, device=device),
                "weight": torch.zeros(n, dtype=torch.float32, device=device)}
+    tuning = None
+    if not args.no_tune:
+        # launch shapes chosen by the project's autotuner on a sample of these frames
+        # (outside every timed region; cached per device and workload)
+        from serstacker_gb300 import autotune
+        tuning = autotune.tune_stack_frames(reg, acc, frames, n, WIDTH, HEIGHT, C.DEPTH_U16, WIDTH * 2, frame_bytes,
+                                            passes, SCALE, weighting=_weighting, sample=512)
 
     def step_device():
         acc.clear()
@@ -438,7 +448,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": workload_cfg(n), "parallelism": f"replicas x{ws}",
+                "config": workload_cfg(n), "parallelism": f"replicas x{ws}", "tuning": tuning,
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
                 "clocks": clk, "gpu_launches": launches,
                 "plain": None if plain_fps is None else {
@@ -554,6 +564,154 @@ def run_plain(args, n, frames, ref, opts, passes):
                          scale=SCALE)
     torch.cuda.synchronize()
     return pn / (time.perf_counter() - t0)
+
+
+# ------------------------------------------------------------------ config-0 workload
+
+C0_W, C0_H = 640, 480
+
+
+def config0_cfg(n: int):
+    return {
+        "workload": f"{n} x {C0_W}x{C0_H} u8 frames (banded disk of radius 180 px, euclidean warps tx, ty ~ "
+                    "U(-8, 8) px and theta ~ N(0, 0.5 deg) about (0, 0), Poisson peak 200 + read noise 2); plain "
+                    "forward-additive ECC, EUCLIDEAN (fixed scale: the reference's eps never converges, every "
+                    "frame runs max_iterations 30), one pyramid level; bilinear remap; unweighted FP32 average",
+        "frames": n, "width": C0_W, "height": C0_H, "levels": 1, "method": "FORWARD_ADDITIVE",
+        "passes": ["EUCLIDEAN"], "max_iterations": 30,
+        "l2": f"inputs ({n} x 0.31 MB) fit in L2; the step is latency-bound, not HBM-bound",
+    }
+
+
+def main_config0(args, ws_, rank, local):
+    """BASELINE's CPU-runnable case: 64 u8 640x480 frames, FA euclidean, one
+    level, unweighted stack, through sst_stack_frames."""
+    import torch
+    from serstacker_gb300 import capi as C
+    from serstacker_gb300 import synth
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    C.lib()
+    n = args.frames if args.frames != 2000 else 64
+    sc = synth.scene_config0()
+    fr, Hs, _ = synth.make_sequence_torch(sc, n, SEED, kind="config0", gain=1.0, blur_range=None, device=device,
+                                          maxval=255)
+    frames = fr.to(torch.uint8)
+    del fr
+    ref = synth.reference_np(sc).astype(np.float32)
+    opts = C.default_options(method=C.FA, maxlevel=0, max_iterations=30, epsx=0.2, minimum_image_size=16,
+                             min_rho=0.0)
+    reg = C.c_ecch(opts)
+    reg.set_level_loops(not args.unrolled_schedule)
+    reg.set_reference_image(ref, scale=1.0)
+    acc = C.c_weigthed_average(C0_W, C0_H)
+    passes = [C.EUCLIDEAN]
+    dev_out = {"params": torch.zeros((n, 12), dtype=torch.float32, device=device),
+               "status": torch.zeros(n, dtype=torch.int32, device=device),
+               "rho": torch.zeros(n, dtype=torch.float32, device=device),
+               "weight": torch.zeros(n, dtype=torch.float32, device=device)}
+
+    def step(ptr, on_device, host_input, outputs):
+        acc.clear()
+        reg.set_chunk_frames(n)
+        C.stack_frames(reg, acc, ptr, passes, 1.0, weighting=0, on_device=on_device, n=n, width=C0_W, height=C0_H,
+                       depth=C.DEPTH_U8, row_stride=C0_W, frame_stride=C0_W * C0_H, outputs=outputs,
+                       host_input=host_input)
+
+    for _ in range(args.warmup):
+        step(frames, True, False, dev_out)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(ws_)
+    torch.cuda.synchronize()
+    C.kernel_launch_count(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step(frames, True, False, dev_out)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(ws_)
+    launches = C.kernel_launch_count()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, ws_)
+    clk = clocks.stop()
+    value = ws_ * n / (ms / 1000.0)
+    t0_ms, fi0, ab0 = reg.level_stats(0, 0)
+    peak, peak_kind = measured_peaks()
+    achieved = ab0 / (t0_ms / 1000.0) / 1e9 if t0_ms > 0 else 0.0
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "k_pass_stencil<FA, EUCLIDEAN> (the single level), all frames x iterations",
+            "alg_bytes_model": "8 B per pixel and frame-iteration (warped source 4 + template 4)",
+            "peak_source": peak_kind, "level0_ms_per_step": t0_ms, "frame_iterations": fi0}
+    res = {k: v.cpu().numpy() for k, v in dev_out.items()}
+
+    # e2e: pinned host frames through the same call, results and the stack read back
+    host = torch.empty((n, C0_H, C0_W), dtype=torch.uint8, pin_memory=True)
+    host.copy_(frames)
+    pout = {k: torch.zeros_like(v, device="cpu").pin_memory() for k, v in dev_out.items()}
+    avg_host = torch.zeros((C0_H, C0_W), dtype=torch.float32, pin_memory=True)
+    mask_host = torch.zeros((C0_H, C0_W), dtype=torch.uint8, pin_memory=True)
+
+    def step_e2e():
+        step(host.data_ptr(), True, True, pout)
+        C.lib().sst_weighted_average_compute(acc.handle, avg_host.data_ptr(), mask_host.data_ptr(), 0, None)
+
+    for _ in range(max(1, args.warmup)):
+        step_e2e()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000.0 / args.steps, ws_)
+    e2e = {"value": ws_ * n / (e2e_ms / 1000.0), "unit": "frames/s", "h2d_bytes_per_step": n * C0_W * C0_H,
+           "d2h_bytes_per_step": n * 16 * 4 + C0_W * C0_H * 5, "ms_per_step": e2e_ms,
+           "api": "sst_stack_frames (host pinned) + sst_weighted_average_compute"}
+
+    # plain one-frame-per-launch form
+    sub = frames[:min(args.plain_frames, n)].cpu().numpy()
+    reg_p = C.c_ecch(opts)
+    reg_p.set_reference_image(ref, scale=1.0)
+    acc_p = C.c_weigthed_average(C0_W, C0_H)
+    reg_p.align(sub[:1], passes, plain=True)
+    torch.cuda.synchronize()
+    tp = time.perf_counter()
+    for i in range(sub.shape[0]):
+        o = reg_p.align(sub[i:i + 1], passes, plain=True)
+        acc_p.add_warped(sub[i:i + 1], C.EUCLIDEAN, o["params"], status=o["status"])
+    torch.cuda.synchronize()
+    plain_fps = sub.shape[0] / (time.perf_counter() - tp)
+
+    acc_o = None
+    if rank == 0 and args.accuracy_frames > 0:
+        import oracle as O
+        O.build()
+        O.set_num_threads(os.cpu_count() or 1)
+        k = min(8, n)
+        host_np = frames[:k].cpu().numpy()
+        m = O.model(O.EUCLIDEAN)
+        oo = O.ecch_opts(method=O.FA, maxlevel=0, max_iterations=30, epsx=0.2, minimum_image_size=16)
+        rms, its = [], []
+        for i in range(k):
+            st, it, _ = O.ecch_align(m, O.identity(m), ref.astype(np.float64), host_np[i].astype(np.float64), oo)
+            s_g = O.set_params(m, O.identity(m), res["params"][i][:3].astype(np.float64))
+            xa, ya = O.warp_grid(m, s_g, C0_W, C0_H)
+            xb, yb = O.warp_grid(m, st, C0_W, C0_H)
+            rms.append(math.sqrt(float(((xa - xb) ** 2 + (ya - yb) ** 2)[::8, ::8].mean())))
+            its.append(it)
+        acc_o = {"frames": k, "warp_rms_vs_oracle_px_max": max(rms), "oracle_iterations": sorted(set(its))}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws_, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {**config0_cfg(n), "parallelism": f"replicas x{ws_}"}, "e2e": e2e, "roofline": roof,
+                "cpu_baseline": None, "clocks": clk, "gpu_launches": launches,
+                "plain": {"value": plain_fps, "unit": "frames/s", "frames": int(sub.shape[0])},
+                "batched_over_plain": value / ws_ / plain_fps,
+                "accuracy": {"gpu_iterations_per_frame": fi0 / n, "frames_ok": int((res["status"] == 0).sum()),
+                             "vs_oracle": acc_o}}
+        print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------ Bayer workload

@@ -367,6 +367,38 @@ int sst_set_chunk_frames(sst_ecch * h, int frames);
  * conditional nodes, so per-kernel profiles use the unrolled schedule. */
 int sst_ecch_set_level_loops(sst_ecch * h, int enable);
 
+/* Launch shapes of the engine and the accumulator, chosen by the project's
+ * autotuner (serstacker_gb300/autotune.py) per device and workload; a zero
+ * field keeps the default. No counterpart in the reference (CPU code).
+ *   pass_ctas_per_sm     CTAs per SM of the persistent Gauss-Newton pass
+ *                        launches (0: the kernel's occupancy); results are
+ *                        bitwise identical for every value
+ *   pass_tile_w[c]       tile width of the staged IC / IC-LM pass on levels
+ *                        of width class c (<= 192, <= 384, <= 768, wider
+ *                        px): 64 or 128 (0: 64 up to 384 px, else 128); the
+ *                        tile sums group differently, so results differ at
+ *                        the rounding level
+ *   corr_ctas_per_sm     CTAs per SM of the correlation launches (0: 4);
+ *                        bitwise identical
+ *   stack_max_chunks     CTAs a stack tile's frames may split over (0: 4);
+ *                        the chunks' compensated partial sums are merged in
+ *                        order (rounding-level differences)
+ *   stack_items_per_slot (tile, chunk) CTAs aimed at per resident CTA slot
+ *                        when splitting (0: 4) */
+typedef struct sst_tuning {
+  int32_t pass_ctas_per_sm;
+  int32_t pass_tile_w[4];
+  int32_t corr_ctas_per_sm;
+  int32_t stack_max_chunks;
+  int32_t stack_items_per_slot;
+} sst_tuning;
+
+/* the engine's fields (pass and correlation shapes); graphs are rebuilt */
+int sst_ecch_set_tuning(sst_ecch * h, const sst_tuning * t);
+int sst_ecch_get_tuning(const sst_ecch * h, sst_tuning * t);
+/* the accumulator's fields (stack chunks) */
+int sst_weighted_average_set_tuning(sst_weighted_average * h, const sst_tuning * t);
+
 /* Number of kernels the library launched since the last call of this
  * function (graph replays count every kernel node they run). */
 long long sst_kernel_launch_count(int reset);
@@ -490,9 +522,16 @@ int sst_eccflow_destroy(sst_eccflow * h);
 
 /* c_eccflow::set_reference_image(reference) (ecc2.cc:2489-2672): the
  * reference pyramid, its gradients and the per-level 2x2 systems D. Values
- * are multiplied by `scale`. Masks are not supported. */
+ * are multiplied by `scale`. No mask (see _masked below). */
 int sst_eccflow_set_reference_image(sst_eccflow * h, const void * image, int depth, int width, int height,
     size_t row_stride, double scale, int on_device, void * stream);
+
+/* set_reference_image(reference, reference_mask) (ecc2.cc:2489-2672): as
+ * sst_eccflow_set_reference_image, with a u8 reference mask (0 = invalid;
+ * NULL: none). Each level's mask is the INTER_NEAREST resize of the mask of
+ * the level its image comes from (downscale, ecc2.cc:2431-2456). */
+int sst_eccflow_set_reference_image_masked(sst_eccflow * h, const void * image, int depth, int width, int height,
+    size_t row_stride, double scale, const uint8_t * mask, size_t mask_stride, int on_device, void * stream);
 
 /* number of pyramid levels of the current reference */
 int sst_eccflow_num_levels(const sst_eccflow * h);
@@ -504,6 +543,16 @@ int sst_eccflow_num_levels(const sst_eccflow * h);
  * Buffers are host or device memory per on_device. */
 int sst_eccflow_compute_batch(sst_eccflow * h, const void * frames, int depth, int n, size_t row_stride,
     size_t frame_stride, double scale, int on_device, const float * init_rmap, float * rmap_out, void * stream);
+
+/* c_eccflow::compute(current, rmap, current_mask) for n frames with their u8
+ * masks (n masks of the reference's size, mask_frame_stride bytes apart;
+ * NULL: none): in every update the current mask is remapped INTER_NEAREST
+ * (BORDER_CONSTANT 0) by the flow and ANDed with the reference mask, and the
+ * update terms It gx, It gy are zero where that is 0 (compute_uv,
+ * ecc2.cc:2253-2335). */
+int sst_eccflow_compute_batch_masked(sst_eccflow * h, const void * frames, int depth, int n, size_t row_stride,
+    size_t frame_stride, double scale, const uint8_t * masks, size_t mask_row_stride, size_t mask_frame_stride,
+    int on_device, const float * init_rmap, float * rmap_out, void * stream);
 
 /* -------------------------------------------- differentiable warp residual */
 
@@ -696,8 +745,8 @@ int sst_frame_registration_destroy(sst_frame_registration * h);
  * mask pyrDown'ed / resized, then >= 250; c_frame_registration.cc:230-250),
  * ecc_normalize'd when normalization_scale > 0 and normalization_noise > 0
  * (ecc2.cc:385-397), and handed to c_ecch; the eccflow reference is the
- * full-size image. Values are multiplied by `scale`. mask may be NULL (u8,
- * 0 = invalid); masks are not supported with eccflow registration. */
+ * full-size image and mask. Values are multiplied by `scale`. mask may be
+ * NULL (u8, 0 = invalid). */
 int sst_frame_registration_setup_reference_frame(sst_frame_registration * h, const void * image, int depth,
     int width, int height, size_t row_stride, double scale, const uint8_t * mask, size_t mask_stride,
     int on_device, void * stream);

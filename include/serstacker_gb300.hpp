@@ -549,26 +549,28 @@ public:
   const c_eccflow_options & options() const { return _opts; }
   void set_options(const c_eccflow_options & o) { _opts = o; create(); }
 
-  /* c_eccflow::set_reference_image (ecc2.cc:2489-2672) */
-  bool set_reference_image(const image_view & img, double scale = 1.0)
+  /* c_eccflow::set_reference_image(reference, reference_mask) (ecc2.cc:2489-2672) */
+  bool set_reference_image(const image_view & img, const image_view & mask = image_view(), double scale = 1.0)
   {
     if( !_h || img.empty() ) return false;
-    if( sst_eccflow_set_reference_image(_h, img.data, img.depth, img.width, img.height, img.stride, scale, 0, nullptr) !=
-        SST_OK )
+    if( sst_eccflow_set_reference_image_masked(_h, img.data, img.depth, img.width, img.height, img.stride, scale,
+            (const uint8_t *) mask.data, mask.stride, 0, nullptr) != SST_OK )
       return false;
     _w = img.width, _hh = img.height;
     return true;
   }
 
-  /* c_eccflow::compute(current, rmap) (ecc2.cc:2856-2865) */
-  bool compute(const image_view & current, std::vector<float> & rmap, double scale = 1.0)
+  /* c_eccflow::compute(current, rmap, current_mask) (ecc2.cc:2856-2865) */
+  bool compute(const image_view & current, std::vector<float> & rmap, const image_view & mask = image_view(),
+      double scale = 1.0)
   {
     if( !_h || current.width != _w || current.height != _hh ) return false;
     const size_t n = (size_t) _w * _hh * 2;
     const bool have_init = rmap.size() == n;
     std::vector<float> out(n);
-    if( sst_eccflow_compute_batch(_h, current.data, current.depth, 1, current.stride, current.stride * current.height,
-            scale, 0, have_init ? rmap.data() : nullptr, out.data(), nullptr) != SST_OK )
+    if( sst_eccflow_compute_batch_masked(_h, current.data, current.depth, 1, current.stride,
+            current.stride * current.height, scale, (const uint8_t *) mask.data, mask.stride,
+            mask.stride * current.height, 0, have_init ? rmap.data() : nullptr, out.data(), nullptr) != SST_OK )
       return false;
     rmap.swap(out);
     return true;

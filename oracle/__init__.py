@@ -128,6 +128,7 @@ def lib():
             "orc_ecc_normalize": (None, [p, p, i, i, i, p]),
             "orc_register_frame": (i, [p, p, p, i, i, p, p, p, p]),
             "ref_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
+            "orc_eccflow_masked": (i, [p, p, p, p, p, i, i, p, p]),
             "orc_set_num_threads": (None, [i]),
             "orc_get_num_threads": (i, []),
         }
@@ -431,13 +432,14 @@ def eccflow_levels(w, h, o: FlowOpts):
     return list(zip(ws[:n].tolist(), hs[:n].tolist()))
 
 
-def eccflow(o: FlowOpts, ref, cur, init_flow=None):
-    """c_eccflow: reference + current -> flow (h, w, 2) (rmap = identity + flow)"""
+def eccflow(o: FlowOpts, ref, cur, init_flow=None, ref_mask=None, cur_mask=None):
+    """c_eccflow: reference + current (+ masks) -> flow (h, w, 2) (rmap = identity + flow)"""
     r, c = _f64(ref), _f64(cur)
     h, w = r.shape
     init = None if init_flow is None else _f64(init_flow)
     out = np.empty((h, w, 2))
-    lib().orc_eccflow(C.byref(o), _ptr(r), _ptr(c), w, h, _ptr(init), _ptr(out))
+    lib().orc_eccflow_masked(C.byref(o), _ptr(r), _ptr(_u8(ref_mask)), _ptr(c), _ptr(_u8(cur_mask)), w, h,
+                             _ptr(init), _ptr(out))
     return out
 
 

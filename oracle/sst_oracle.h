@@ -164,6 +164,9 @@ int orc_eccflow_levels(int w, int h, const orc_flow_opts * o, int * ws, int * hs
  * flow (h x w x 2, interleaved u, v); init_flow may be NULL (zero start) */
 int orc_eccflow(const orc_flow_opts * o, const double * ref, const double * cur, int w, int h,
     const double * init_flow, double * flow);
+/* the same with reference / current masks (u8, 0 = invalid; either may be NULL) */
+int orc_eccflow_masked(const orc_flow_opts * o, const double * ref, const uint8_t * ref_mask,
+    const double * cur, const uint8_t * cur_mask, int w, int h, const double * init_flow, double * flow);
 
 /* focus-stacking weights of a frame warped to the dw x dh grid:
  * W = (6 lap^2 + |grad|^2)^2 blurred by a Gaussian of sigma 3 */

@@ -122,6 +122,7 @@ void avgdown(const double * src, int w, int h, int support_scale, std::vector<do
 struct level {
   int w, h;
   std::vector<double> ref, cur, Ix, Iy;
+  std::vector<uint8_t> rmask, cmask;
   int dw, dh;
   std::vector<double> D;   // dw x dh x 4: a00, a01, a11, mult / (|det| + reg)
 };
@@ -176,6 +177,19 @@ extern "C" int orc_eccflow_levels(int w, int h, const orc_flow_opts * o, int * w
 extern "C" int orc_eccflow(const orc_flow_opts * o, const double * ref, const double * cur, int w, int h,
     const double * init_flow, double * flow)
 {
+  return orc_eccflow_masked(o, ref, nullptr, cur, nullptr, w, h, init_flow, flow);
+}
+
+/* c_eccflow with masks: each level's reference and current masks are the
+ * INTER_NEAREST resizes of the masks of the level the image comes from
+ * (downscale, ecc2.cc:2431-2456); in an update, the current mask is
+ * remapped INTER_NEAREST (cvRound, BORDER_CONSTANT 0) by the flow and ANDed
+ * with the reference mask, and It gx, It gy are zero where that fails
+ * (compute_uv, ecc2.cc:2253-2335). The reference gradients and D ignore the
+ * masks, as in the reference (ecc2.cc:2604-2605). */
+extern "C" int orc_eccflow_masked(const orc_flow_opts * o, const double * ref, const uint8_t * ref_mask,
+    const double * cur, const uint8_t * cur_mask, int w, int h, const double * init_flow, double * flow)
+{
   int ws[64], hs[64];
   const int L = orc_eccflow_levels(w, h, o, ws, hs, 64);
   const int min_size = std::max(4, o->min_image_size);
@@ -188,9 +202,13 @@ extern "C" int orc_eccflow(const orc_flow_opts * o, const double * ref, const do
     e.w = ws[l], e.h = hs[l];
     e.ref.resize((size_t) e.w * e.h);
     e.cur.resize((size_t) e.w * e.h);
+    if( ref_mask ) e.rmask.resize(e.ref.size());
+    if( cur_mask ) e.cmask.resize(e.ref.size());
     if( l == 0 ) {
       memcpy(e.ref.data(), ref, sizeof(double) * e.ref.size());
       memcpy(e.cur.data(), cur, sizeof(double) * e.cur.size());
+      if( ref_mask ) memcpy(e.rmask.data(), ref_mask, e.rmask.size());
+      if( cur_mask ) memcpy(e.cmask.data(), cur_mask, e.cmask.size());
     }
     else {
       const bool from0 = o->downscale == 1 ||
@@ -198,6 +216,8 @@ extern "C" int orc_eccflow(const orc_flow_opts * o, const double * ref, const do
       const level & s = from0 ? P[0] : P[l - 1];
       downscale(o, s.ref.data(), s.w, s.h, e.ref.data(), e.w, e.h);
       downscale(o, s.cur.data(), s.w, s.h, e.cur.data(), e.w, e.h);
+      if( ref_mask ) orc_resize_nearest_u8(s.rmask.data(), s.w, s.h, e.rmask.data(), e.w, e.h);
+      if( cur_mask ) orc_resize_nearest_u8(s.cmask.data(), s.w, s.h, e.cmask.data(), e.w, e.h);
     }
     e.Ix.resize(e.ref.size());
     e.Iy.resize(e.ref.size());
@@ -250,6 +270,15 @@ extern "C" int orc_eccflow(const orc_flow_opts * o, const double * ref, const do
       for( int y = 0; y < e.h; ++y ) {
         for( int x = 0; x < e.w; ++x ) {
           const size_t i = (size_t) y * e.w + x;
+          bool ok = e.rmask.empty() || e.rmask[i] != 0;
+          if( ok && !e.cmask.empty() ) {
+            const double X = nearbyint(x + u[i]), Y = nearbyint(y + v[i]);
+            ok = X >= 0 && X < e.w && Y >= 0 && Y < e.h && e.cmask[(size_t) Y * e.w + (size_t) X] != 0;
+          }
+          if( !ok ) {
+            bx[i] = by[i] = 0;
+            continue;
+          }
           const double W = orc_sample_bilinear(e.cur.data(), e.w, e.h, x + u[i], y + v[i], ORC_BORDER_REPLICATE, 0);
           const double It = e.ref[i] - W;
           bx[i] = It * e.Ix[i], by[i] = It * e.Iy[i];

@@ -60,6 +60,28 @@ class EcchOptions(C.Structure):
                 ("min_rho", C.c_double), ("ic_jacobian_at_identity", C.c_int32), ("reserved", C.c_int32)]
 
 
+class Tuning(C.Structure):
+    """sst_tuning: launch shapes of the engine and the accumulator (0 = default)."""
+    _fields_ = [("pass_ctas_per_sm", C.c_int32), ("pass_tile_w", C.c_int32 * 4), ("corr_ctas_per_sm", C.c_int32),
+                ("stack_max_chunks", C.c_int32), ("stack_items_per_slot", C.c_int32)]
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "Tuning":
+        t = cls()
+        for k, v in (d or {}).items():
+            if k == "pass_tile_w":
+                for i, x in enumerate(v):
+                    t.pass_tile_w[i] = int(x)
+            else:
+                setattr(t, k, int(v))
+        return t
+
+    def to_dict(self) -> dict:
+        return {"pass_ctas_per_sm": self.pass_ctas_per_sm, "pass_tile_w": list(self.pass_tile_w),
+                "corr_ctas_per_sm": self.corr_ctas_per_sm, "stack_max_chunks": self.stack_max_chunks,
+                "stack_items_per_slot": self.stack_items_per_slot}
+
+
 class EccRegistrationOptions(C.Structure):
     """c_ecc_registration_options (c_frame_registration.h:47-63)."""
     _fields_ = [("scale", C.c_double), ("eps", C.c_double), ("min_rho", C.c_double),
@@ -139,6 +161,8 @@ def lib():
             "sst_eccflow_set_reference_image": (i, [p, p, i, i, i, sz, d, i, p]),
             "sst_eccflow_num_levels": (i, [p]),
             "sst_eccflow_compute_batch": (i, [p, p, i, i, sz, sz, d, i, p, p, p]),
+            "sst_eccflow_set_reference_image_masked": (i, [p, p, i, i, i, sz, d, p, sz, i, p]),
+            "sst_eccflow_compute_batch_masked": (i, [p, p, i, i, sz, sz, d, p, sz, sz, i, p, p, p]),
             "sst_roi_batch_create": (i, [p, p]),
             "sst_roi_batch_destroy": (i, [p]),
             "sst_roi_batch_align": (i, [p, i, p, p, p, i, d, i, i, p, p, p, p, p, p, p, p]),
@@ -170,6 +194,9 @@ def lib():
             "sst_ser_writer_close": (i, [p]),
             "sst_average_pyramid_inpaint": (i, [p, sz, p, sz, i, i, i, p, sz, p, sz, i, p]),
             "sst_calibrate_frames": (i, [p, i, i, i, i, sz, sz, d, p, sz, p, sz, p, sz, sz, p]),
+            "sst_ecch_set_tuning": (i, [p, p]),
+            "sst_ecch_get_tuning": (i, [p, p]),
+            "sst_weighted_average_set_tuning": (i, [p, p]),
             "sst_image_registration_options_default": (None, [p]),
             "sst_frame_registration_create": (i, [p, p]),
             "sst_frame_registration_destroy": (i, [p]),
@@ -277,6 +304,15 @@ class c_ecch:
     def num_levels(self) -> int:
         return lib().sst_ecch_num_levels(self._h)
 
+    def set_tuning(self, tuning):
+        t = tuning if isinstance(tuning, Tuning) else Tuning.from_dict(tuning)
+        _check(lib().sst_ecch_set_tuning(self._h, C.byref(t)), "sst_ecch_set_tuning")
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        _check(lib().sst_ecch_get_tuning(self._h, C.byref(t)), "sst_ecch_get_tuning")
+        return t.to_dict()
+
     def set_chunk_frames(self, n: int):
         _check(lib().sst_set_chunk_frames(self._h, n), "set_chunk_frames")
 
@@ -354,25 +390,30 @@ class c_eccflow:
     def handle(self):
         return self._h
 
-    def set_reference_image(self, img: np.ndarray, scale: float = 1.0):
+    def set_reference_image(self, img: np.ndarray, scale: float = 1.0, mask: Optional[np.ndarray] = None):
         a = np.ascontiguousarray(img)
-        _check(lib().sst_eccflow_set_reference_image(self._h, _ptr(a), _NP_DEPTH[a.dtype], a.shape[1], a.shape[0],
-                                                      a.strides[0], scale, 0, None), "set_reference_image")
+        m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+        _check(lib().sst_eccflow_set_reference_image_masked(
+            self._h, _ptr(a), _NP_DEPTH[a.dtype], a.shape[1], a.shape[0], a.strides[0], scale, _ptr(m),
+            0 if m is None else m.strides[0], 0, None), "set_reference_image")
         self.shape = a.shape
 
     def num_levels(self) -> int:
         return lib().sst_eccflow_num_levels(self._h)
 
-    def compute(self, frames: np.ndarray, init_rmap=None, scale: float = 1.0):
-        """frames (n, h, w) -> rmaps (n, h, w, 2) = identity + flow"""
+    def compute(self, frames: np.ndarray, init_rmap=None, scale: float = 1.0, masks: Optional[np.ndarray] = None):
+        """frames (n, h, w) (+ masks (n, h, w) u8) -> rmaps (n, h, w, 2) = identity + flow"""
         fr = np.ascontiguousarray(frames)
         if fr.ndim == 2:
             fr = fr[None]
         n, hh, ww = fr.shape
         out = np.zeros((n, hh, ww, 2), np.float32)
         init = None if init_rmap is None else np.ascontiguousarray(init_rmap, np.float32).reshape(n, hh, ww, 2)
-        _check(lib().sst_eccflow_compute_batch(self._h, _ptr(fr), _NP_DEPTH[fr.dtype], n, fr.strides[1], fr.strides[0],
-                                               scale, 0, _ptr(init), _ptr(out), None), "sst_eccflow_compute_batch")
+        m = None if masks is None else np.ascontiguousarray(masks, np.uint8).reshape(n, hh, ww)
+        _check(lib().sst_eccflow_compute_batch_masked(
+            self._h, _ptr(fr), _NP_DEPTH[fr.dtype], n, fr.strides[1], fr.strides[0], scale, _ptr(m),
+            0 if m is None else m.strides[1], 0 if m is None else m.strides[0], 0, _ptr(init), _ptr(out), None),
+            "sst_eccflow_compute_batch")
         return out
 
     def compute_device(self, frames, n, depth, row_stride, frame_stride, rmap_out, init_rmap=None, scale=1.0):
@@ -521,6 +562,10 @@ class c_weigthed_average:
 
     def clear(self):
         _check(lib().sst_weighted_average_clear(self._h, None), "clear")
+
+    def set_tuning(self, tuning):
+        t = tuning if isinstance(tuning, Tuning) else Tuning.from_dict(tuning)
+        _check(lib().sst_weighted_average_set_tuning(self._h, C.byref(t)), "sst_weighted_average_set_tuning")
 
     def set_local_variance(self, options: Optional[LocalVarianceOptions] = None, **kw):
         """sharpness-map options of stack_frames(weighting=3)"""

@@ -184,6 +184,7 @@ struct sst_ecch {
   int last_method = 0;
   int last_n = 0;                 // frames whose pyramids the batch buffer holds
   double gate[3] = { 0, 0, 0 };   // correlation gate after pass k < last (0: none)
+  sst_tuning tune {};             // launch shapes (zero fields: the defaults)
 
   ~sst_ecch()
   {
@@ -292,6 +293,36 @@ int sst_internal_ecch_set_pass_gates(sst_ecch * h, int num, const double * gates
 {
   if( !h || num < 0 || num > 3 ) return set_error(SST_ERR_INVALID_ARG, "invalid pass gates");
   for( int k = 0; k < 3; ++k ) h->gate[k] = k < num && gates ? gates[k] : 0.0;
+  return SST_OK;
+}
+
+static int check_tuning(const sst_tuning * t)
+{
+  if( !t ) return set_error(SST_ERR_INVALID_ARG, "NULL tuning");
+  if( t->pass_ctas_per_sm < 0 || t->pass_ctas_per_sm > 16 || t->corr_ctas_per_sm < 0 || t->corr_ctas_per_sm > 16 )
+    return set_error(SST_ERR_INVALID_ARG, "CTAs per SM out of range 0..16");
+  for( int c = 0; c < 4; ++c ) {
+    if( t->pass_tile_w[c] != 0 && t->pass_tile_w[c] != 64 && t->pass_tile_w[c] != PW_TX )
+      return set_error(SST_ERR_INVALID_ARG, "pass tile width must be 0, 64 or %d", PW_TX);
+  }
+  if( t->stack_max_chunks < 0 || t->stack_max_chunks > 16 || t->stack_items_per_slot < 0 || t->stack_items_per_slot > 64 )
+    return set_error(SST_ERR_INVALID_ARG, "stack chunk settings out of range");
+  return SST_OK;
+}
+
+extern "C" int sst_ecch_set_tuning(sst_ecch * h, const sst_tuning * t)
+{
+  if( !h ) return set_error(SST_ERR_INVALID_ARG, "NULL engine");
+  SST_TRY(check_tuning(t));
+  h->tune = *t;
+  h->drop_graphs();
+  return SST_OK;
+}
+
+extern "C" int sst_ecch_get_tuning(const sst_ecch * h, sst_tuning * t)
+{
+  if( !h || !t ) return set_error(SST_ERR_INVALID_ARG, "NULL argument");
+  *t = h->tune;
   return SST_OK;
 }
 
@@ -520,11 +551,27 @@ static cudaError_t record_prof(cudaEvent_t e, cudaStream_t st, bool host_driven)
   return host_driven ? cudaEventRecord(e, st) : cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
 }
 
-/* tile width of the staged IC / IC-LM pass at a level: 64 on levels at most
- * 384 px wide (fewer idle columns in the last tile), PW_TX otherwise */
+/* the level-width class of the tuning tables: <= 192, <= 384, <= 768, wider */
+static int width_class(int w)
+{
+  return w <= 192 ? 0 : w <= 384 ? 1 : w <= 768 ? 2 : 3;
+}
+
+/* tile width of the staged IC / IC-LM pass at a level: the tuned width of the
+ * level's width class, else 64 on levels at most 384 px wide (fewer idle
+ * columns in the last tile) and PW_TX on wider ones */
 static int pointwise_tile_w(const sst_ecch * h, int l)
 {
+  const int t = h->tune.pass_tile_w[width_class(h->lw[l])];
+  if( t == 64 || t == PW_TX ) return t;
   return h->lw[l] <= 384 ? 64 : PW_TX;
+}
+
+/* grid of the Gauss-Newton pass launches: tuned CTAs per SM, else the
+ * kernel's occupancy (-1) */
+static int pass_grid(const sst_ecch * h)
+{
+  return h->tune.pass_ctas_per_sm > 0 ? std::max(1, h->num_sms) * h->tune.pass_ctas_per_sm : -1;
 }
 
 /* tiles of a level's pass; for IC / IC-LM the staged pass's tiling, which has at
@@ -617,7 +664,7 @@ static int add_level_loop(sst_ecch * h, cudaStream_t st, Body body)
  * (min_rho <= 0: rho only) */
 static int enqueue_correlation(sst_ecch * h, int n, const sst_motion_model & model, double min_rho, cudaStream_t st)
 {
-  const int grid = std::max(1, h->num_sms) * 4;
+  const int grid = std::max(1, h->num_sms) * (h->tune.corr_ctas_per_sm > 0 ? h->tune.corr_ctas_per_sm : 4);
   CorrArgs c;
   memset(&c, 0, sizeof(c));
   c.pyr = h->pyr.as<float>();
@@ -651,7 +698,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
   cudaStream_t st = h->st;
   const int L = h->L;
   const int max_it = h->o.max_iterations;
-  const int grid = std::max(1, h->num_sms) * 4;
+  const int pgrid = pass_grid(h);
   const int solve_grid = std::max(1, std::min((n + 7) / 8, std::max(1, h->num_sms) * 8));
   long long k = 0;
   SST_CK(cudaMemsetAsync(h->counts.p, 0, (size_t) h->steps_cap * sizeof(int), st));
@@ -742,7 +789,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
         la.hist = counts + step, la.max_it = max_it;
         SST_TRY(add_level_loop(h, st, [&](cudaStream_t sb, cudaGraphConditionalHandle hc) -> int {
           la.handle = hc;
-          SST_CK(launch_pass(method, a, -1, sb, staged ? &map : nullptr));
+          SST_CK(launch_pass(method, a, pgrid, sb, staged ? &map : nullptr));
           SST_CK(launch_solve(method, a, solve_grid, sb));
           SST_CK(launch_level_advance(la, sb));
           return SST_OK;
@@ -753,7 +800,7 @@ static int enqueue_schedule(sst_ecch * h, int n, int method, int num_passes, con
         a.count_in = counts + step + it;
         a.list_out = lists + (size_t) (step + it + 1) * h->cap;
         a.count_out = counts + step + it + 1;
-        SST_CK_LAUNCH(launch_pass(method, a, -1, st, staged ? &map : nullptr));
+        SST_CK_LAUNCH(launch_pass(method, a, pgrid, st, staged ? &map : nullptr));
         SST_CK_LAUNCH(launch_solve(method, a, solve_grid, st));
         k += 2;
         if( host_driven ) {
@@ -886,6 +933,9 @@ static int register_device(sst_ecch * h, const void * d_frames, int depth, int n
       memcpy(&g, &h->gate[k], sizeof(g));
       key.push_back(g);
     }
+    key.push_back(h->tune.pass_ctas_per_sm);
+    key.push_back(h->tune.corr_ctas_per_sm);
+    for( int c = 0; c < 4; ++c ) key.push_back(h->tune.pass_tile_w[c]);
     GraphEntry * ge = nullptr;
     for( auto & g : h->graphs ) if( g.key == key ) ge = &g;
     if( !ge ) {
@@ -1055,6 +1105,8 @@ struct sst_weighted_average {
   sst_local_variance * lv = nullptr;   // local-variance weighting (created on first use)
   sst_local_variance_options lvo = { 2, 1, 3 };
   int frames = 0;
+  int max_chunks = 4;                  // a tile's frames split over at most this many CTAs
+  int items_per_slot = 4;              // (tile, chunk) CTAs aimed at per resident CTA slot
   size_t plane() const { return (size_t) w * h; }
   ~sst_weighted_average()
   {
@@ -1138,6 +1190,15 @@ extern "C" int sst_weighted_average_create(sst_weighted_average ** out, int widt
   return SST_OK;
 }
 
+extern "C" int sst_weighted_average_set_tuning(sst_weighted_average * a, const sst_tuning * t)
+{
+  if( !a ) return set_error(SST_ERR_INVALID_ARG, "NULL accumulator");
+  SST_TRY(check_tuning(t));
+  a->max_chunks = t->stack_max_chunks > 0 ? t->stack_max_chunks : 4;
+  a->items_per_slot = t->stack_items_per_slot > 0 ? t->stack_items_per_slot : 4;
+  return SST_OK;
+}
+
 extern "C" int sst_weighted_average_destroy(sst_weighted_average * a)
 {
   delete a;
@@ -1209,9 +1270,10 @@ static int add_warped_device(sst_weighted_average * a, const void * d_frames, in
   s.plane = a->plane();
   s.border = border;
   // a tile's frames may be split over up to four CTAs (partial sums merged in order)
-  constexpr int kChunks = 4;
-  SST_CK(a->part.ensure((size_t) (kChunks - 1) * 4 * a->plane() * sizeof(float)));
-  s.part = a->part.as<float>(), s.max_chunks = kChunks;
+  const int kChunks = a->max_chunks;
+  if( kChunks > 1 ) SST_CK(a->part.ensure((size_t) (kChunks - 1) * 4 * a->plane() * sizeof(float)));
+  s.part = kChunks > 1 ? a->part.as<float>() : nullptr, s.max_chunks = kChunks;
+  s.items_per_slot = a->items_per_slot;
   if( !a->err.p ) {
     SST_CK(a->err.ensure(sizeof(int)));
     SST_CK(cudaMemsetAsync(a->err.p, 0, sizeof(int), st));

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) k_resample(const float * src, int sw, siz
 template<int MODE>
 __global__ void __launch_bounds__(256) k_flow_area(const float4 * __restrict__ tg, const float * cur, size_t cur_frame,
     const float2 * uv, size_t uv_frame, int w, int h, TapAxis tx, TapAxis ty, int dw, int dh, float * out,
-    size_t out_frame)
+    size_t out_frame, const uint8_t * rmask = nullptr, const uint8_t * cmask = nullptr, size_t cmask_frame = 0)
 {
   constexpr int NC = MODE == 0 ? 3 : 2;
   const int lane = threadIdx.x & 31;
@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(256) k_flow_area(const float4 * __restrict__ t
   const int X = cell % dw, Y = cell / dw;
   const float * img = MODE == 1 ? cur + (size_t) blockIdx.z * cur_frame : nullptr;
   const float2 * fl = MODE == 1 ? uv + (size_t) blockIdx.z * uv_frame : nullptr;
+  const uint8_t * cm = MODE == 1 && cmask ? cmask + (size_t) blockIdx.z * cmask_frame : nullptr;
   float acc[NC];
 #pragma unroll
   for( int c = 0; c < NC; ++c ) acc[c] = 0.f;
@@ -117,6 +118,14 @@ __global__ void __launch_bounds__(256) k_flow_area(const float4 * __restrict__ t
     else {
       const float2 f = fl[p];
       const float sx = (float) x + f.x, sy = (float) y + f.y;
+      // masks (compute_uv, ecc2.cc:2253-2281): the current mask remapped
+      // INTER_NEAREST (cvRound) with BORDER_CONSTANT 0, ANDed with the
+      // reference mask; It gx, It gy are zero where either is 0
+      if( rmask && !__ldg(rmask + p) ) continue;
+      if( cm ) {
+        const int nx = __float2int_rn(fminf(fmaxf(sx, -1e8f), 1e8f)), ny = __float2int_rn(fminf(fmaxf(sy, -1e8f), 1e8f));
+        if( nx < 0 || nx >= w || ny < 0 || ny >= h || !__ldg(cm + (size_t) ny * w + nx) ) continue;
+      }
       // cv::remap INTER_LINEAR, BORDER_REPLICATE
       const float fx0 = floorf(fminf(fmaxf(sx, -1e8f), 1e8f)), fy0 = floorf(fminf(fmaxf(sy, -1e8f), 1e8f));
       const float ax = sx - fx0, ay = sy - fy0;
@@ -186,6 +195,16 @@ __global__ void k_flow_solve(const float * avg, size_t avg_frame, const float4 *
   duv[(size_t) blockIdx.z * duv_frame + i] = make_float2((float) u, (float) v);
 }
 
+/* cv::resize INTER_NEAREST of u8 masks: source floor(d * ssize / dsize), grid.z = frame */
+__global__ void k_resize_nearest_u8_batch(const uint8_t * src, int sw, int sh, size_t src_frame, uint8_t * dst, int dw,
+    int dh, size_t dst_frame)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if( x >= dw ) return;
+  const int sx = min((int) floor(x * ((double) sw / dw)), sw - 1), sy = min((int) floor(y * ((double) sh / dh)), sh - 1);
+  dst[(size_t) blockIdx.z * dst_frame + (size_t) y * dw + x] = src[(size_t) blockIdx.z * src_frame + (size_t) sy * sw + sx];
+}
+
 /* rmap <-> flow (ecc_remap_to_optflow / ecc_flow_to_remap, ecc2.cc:400-500) */
 __global__ void k_flow_grid(const float2 * src, float2 * dst, int w, int h, size_t frame, float sign)
 {
@@ -221,13 +240,15 @@ struct sst_eccflow {
   std::vector<Tabs> down, area, up, next;
   DevBuf ref, tg, Dm, tmp;              // reference pyramid, {T, gx, gy}, D, tensor averages
   DevBuf cur, uv[2], avg, duv, in;      // batch buffers
+  DevBuf rmask, cmask, min_;            // reference mask pyramid; current mask pyramids; staged host masks
+  bool has_rmask = false;
   size_t cap = 0;
 
   ~sst_eccflow()
   {
     for( auto * v : { &down, &area, &up, &next } )
       for( auto & t : *v ) t.ix.release(), t.wx.release(), t.iy.release(), t.wy.release();
-    DevBuf * bufs[] = { &ref, &tg, &Dm, &tmp, &cur, &uv[0], &uv[1], &avg, &duv, &in };
+    DevBuf * bufs[] = { &ref, &tg, &Dm, &tmp, &cur, &uv[0], &uv[1], &avg, &duv, &in, &rmask, &cmask, &min_ };
     for( DevBuf * b : bufs ) b->release();
     if( ev_user ) cudaEventDestroy(ev_user);
     if( ev_done ) cudaEventDestroy(ev_done);
@@ -251,6 +272,12 @@ static int ffail(int code, const std::string & msg)
   do {                                                                                         \
     SST_FCK(call);                                                                             \
     ++launches;                                                                                \
+  } while ( 0 )
+
+#define SST_TRYF(expr)                                                                         \
+  do {                                                                                         \
+    int r_ = (expr);                                                                           \
+    if( r_ != SST_OK ) return r_;                                                              \
   } while ( 0 )
 
 static int upload_tabs(sst_eccflow::Tabs & t, HostTaps hx, HostTaps hy, cudaStream_t st)
@@ -351,10 +378,30 @@ static void flow_levels(sst_eccflow * f, int w, int h)
   }
 }
 
+/* the mask pyramid of `n` masks whose level 0 is in place: every coarser
+ * level the INTER_NEAREST resize of its downscale source level */
+static int mask_pyramid(sst_eccflow * f, uint8_t * m, int n, cudaStream_t st, int & launches)
+{
+  for( int l = 1; l < f->L; ++l ) {
+    const int s = f->from0[l] ? 0 : l - 1;
+    SST_FLAUNCH((k_resize_nearest_u8_batch<<<dim3((f->lw[l] + 127) / 128, f->lh[l], n), 128, 0, st>>>(m + f->loff[s],
+        f->lw[s], f->lh[s], f->pyr_px, m + f->loff[l], f->lw[l], f->lh[l], f->pyr_px), cudaGetLastError()));
+  }
+  return SST_OK;
+}
+
 extern "C" int sst_eccflow_set_reference_image(sst_eccflow * f, const void * img, int depth, int width, int height,
     size_t row_stride, double scale, int on_device, void * stream)
 {
+  return sst_eccflow_set_reference_image_masked(f, img, depth, width, height, row_stride, scale, nullptr, 0, on_device,
+      stream);
+}
+
+extern "C" int sst_eccflow_set_reference_image_masked(sst_eccflow * f, const void * img, int depth, int width,
+    int height, size_t row_stride, double scale, const uint8_t * mask, size_t mask_stride, int on_device, void * stream)
+{
   if( !f || !img ) return ffail(SST_ERR_INVALID_ARG, "sst_eccflow_set_reference_image: NULL argument");
+  if( mask && mask_stride < (size_t) width ) return ffail(SST_ERR_INVALID_ARG, "mask_stride too small");
   const int bytes = depth_bytes(depth);
   if( !bytes || width < 4 || height < 4 || row_stride < (size_t) width * bytes )
     return ffail(SST_ERR_INVALID_ARG, "sst_eccflow_set_reference_image: invalid image");
@@ -421,6 +468,13 @@ extern "C" int sst_eccflow_set_reference_image(sst_eccflow * f, const void * img
     SST_FLAUNCH((k_flow_tensor<<<(cells + 127) / 128, 128, 0, st>>>(avg, f->dw[l], f->dh[l], (float) o.update_multiplier,
         reg, f->Dm.as<float4>() + f->doff[l]), cudaGetLastError()));
   }
+  f->has_rmask = mask != nullptr;
+  if( mask ) {
+    SST_FCK(f->rmask.ensure(f->pyr_px));
+    SST_FCK(cudaMemcpy2DAsync(f->rmask.p, width, mask, mask_stride, width, height,
+        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    SST_TRYF(mask_pyramid(f, f->rmask.as<uint8_t>(), 1, st, launches));
+  }
   SST_FCK(cudaEventRecord(f->ev_done, st));
   SST_FCK(cudaStreamWaitEvent((cudaStream_t) stream, f->ev_done, 0));
   if( !on_device ) SST_FCK(cudaStreamSynchronize(st));
@@ -431,7 +485,17 @@ extern "C" int sst_eccflow_set_reference_image(sst_eccflow * f, const void * img
 extern "C" int sst_eccflow_compute_batch(sst_eccflow * f, const void * frames, int depth, int n, size_t row_stride,
     size_t frame_stride, double scale, int on_device, const float * init_rmap, float * rmap_out, void * stream)
 {
+  return sst_eccflow_compute_batch_masked(f, frames, depth, n, row_stride, frame_stride, scale, nullptr, 0, 0,
+      on_device, init_rmap, rmap_out, stream);
+}
+
+extern "C" int sst_eccflow_compute_batch_masked(sst_eccflow * f, const void * frames, int depth, int n,
+    size_t row_stride, size_t frame_stride, double scale, const uint8_t * masks, size_t mask_row_stride,
+    size_t mask_frame_stride, int on_device, const float * init_rmap, float * rmap_out, void * stream)
+{
   if( !f || !frames || !rmap_out ) return ffail(SST_ERR_INVALID_ARG, "sst_eccflow_compute_batch: NULL argument");
+  if( masks && (mask_row_stride < (size_t) f->w || mask_frame_stride < mask_row_stride * f->h) )
+    return ffail(SST_ERR_INVALID_ARG, "invalid mask strides");
   if( f->L == 0 ) return ffail(SST_ERR_STATE, "c_eccflow: no reference image was set");
   if( n < 1 || n > 65535 ) return ffail(SST_ERR_INVALID_ARG, "n must be 1..65535");
   const int bytes = depth_bytes(depth);
@@ -473,6 +537,23 @@ extern "C" int sst_eccflow_compute_batch(sst_eccflow * f, const void * frames, i
         f->lw[s], f->pyr_px, cur + f->loff[l], f->lw[l], f->lh[l], f->pyr_px, f->down[l].ax(), f->down[l].ay(), 1.f,
         1.f, 0), cudaGetLastError()));
   }
+  // current mask pyramids (setup_input_image: INTER_NEAREST per level)
+  uint8_t * cmask = nullptr;
+  if( masks ) {
+    SST_FCK(f->cmask.ensure((size_t) n * f->pyr_px));
+    cmask = f->cmask.as<uint8_t>();
+    const uint8_t * msrc = masks;
+    if( !on_device ) {
+      SST_FCK(f->min_.ensure(mask_frame_stride * n));
+      SST_FCK(cudaMemcpyAsync(f->min_.p, masks, mask_frame_stride * n, cudaMemcpyHostToDevice, st));
+      msrc = f->min_.as<uint8_t>();
+    }
+    for( int i = 0; i < n; ++i ) {
+      SST_FCK(cudaMemcpy2DAsync(cmask + (size_t) i * f->pyr_px, f->w, msrc + (size_t) i * mask_frame_stride,
+          mask_row_stride, f->w, f->h, cudaMemcpyDeviceToDevice, st));
+    }
+    SST_TRYF(mask_pyramid(f, cmask, n, st, launches));
+  }
   // initial flow at the coarsest level
   const int Lc = f->L - 1;
   int a = 0;                                     // uv[a] holds the flow of the current level
@@ -513,7 +594,8 @@ extern "C" int sst_eccflow_compute_batch(sst_eccflow * f, const void * frames, i
     for( int it = 0; it < o.max_iterations; ++it ) {
       SST_FLAUNCH((k_flow_area<1><<<dim3((cells + 7) / 8, 1, n), 256, 0, st>>>(f->tg.as<float4>() + f->loff[l],
           cur + f->loff[l], f->pyr_px, u, plane, f->lw[l], f->lh[l], f->area[l].ax(), f->area[l].ay(), f->dw[l],
-          f->dh[l], f->avg.as<float>(), f->max_cells * 2), cudaGetLastError()));
+          f->dh[l], f->avg.as<float>(), f->max_cells * 2, f->has_rmask ? f->rmask.as<uint8_t>() + f->loff[l] : nullptr,
+          cmask ? cmask + f->loff[l] : nullptr, f->pyr_px), cudaGetLastError()));
       SST_FLAUNCH((k_flow_solve<<<dim3((cells + 127) / 128, 1, n), 128, 0, st>>>(f->avg.as<float>(), f->max_cells * 2,
           f->Dm.as<float4>() + f->doff[l], f->dw[l], f->dh[l], f->duv.as<float2>(), f->max_cells), cudaGetLastError()));
       SST_FLAUNCH((k_resample<2><<<dim3((f->lw[l] + 31) / 32, (f->lh[l] + 7) / 8, n), 256, 0, st>>>(

@@ -483,7 +483,6 @@ extern "C" int sst_frame_registration_setup_reference_frame(sst_frame_registrati
   if( width < 8 || height < 8 ) return fail(SST_ERR_INVALID_ARG, "reference image too small");
   if( row_stride < (size_t) width * depth_bytes(depth) ) return fail(SST_ERR_INVALID_ARG, "row_stride too small");
   if( mask && mask_stride < (size_t) width ) return fail(SST_ERR_INVALID_ARG, "mask_stride too small");
-  if( mask && h->flow ) return fail(SST_ERR_UNSUPPORTED, "reference masks with eccflow registration are not supported");
   SST_RTRY(ensure_stream(h));
   SST_RCK(cudaEventRecord(h->ev_user, (cudaStream_t) stream));
   SST_RCK(cudaStreamWaitEvent(h->st, h->ev_user, 0));
@@ -566,7 +565,9 @@ extern "C" int sst_frame_registration_setup_reference_frame(sst_frame_registrati
         1.0, emask, emask ? (size_t) h->ew : 0, 1, h->st));
   }
   if( h->flow ) {
-    SST_RTRY(sst_eccflow_set_reference_image(h->flow, src, depth, width, height, row_stride, scale, 1, h->st));
+    // the eccflow reference: the full-size image and mask (c_frame_registration.cc:680-687)
+    SST_RTRY(sst_eccflow_set_reference_image_masked(h->flow, src, depth, width, height, row_stride, scale, dmask,
+        mask_stride, 1, h->st));
   }
   SST_RCK(cudaStreamSynchronize(st));
   SST_RCK(cudaEventRecord(h->ev_done, st));

@@ -677,8 +677,8 @@ cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, 
   const int fam = motion_family(motion);
   CUtensorMap map;
   if( fam != FAM_QUAD && a.n > 0 && encode_frames(a, depth, &map) ) {
-    // frame chunks: enough (tile, chunk) CTAs for about four per resident slot,
-    // at least 32 frames per chunk, within the caller's scratch
+    // frame chunks: enough (tile, chunk) CTAs for about items_per_slot per
+    // resident slot, at least 32 frames per chunk, within the caller's scratch
     static int slots = 0;
     if( !slots ) {
       int dev = 0, sms = 0;
@@ -689,7 +689,7 @@ cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, 
     const int tiles = (int) (grid.x * grid.y);
     int chunks = 1;
     if( a.part && a.max_chunks > 1 ) {
-      chunks = (4 * slots + tiles - 1) / tiles;
+      chunks = (a.items_per_slot * slots + tiles - 1) / tiles;
       chunks = chunks < a.max_chunks ? chunks : a.max_chunks;
       chunks = chunks < a.n / 32 ? chunks : a.n / 32;
       chunks = chunks > 1 ? chunks : 1;

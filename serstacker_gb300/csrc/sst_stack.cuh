@@ -26,6 +26,7 @@ struct StackArgs {
   // sums, so that one tile's frames can be split over several CTAs
   float * part = nullptr;
   int max_chunks = 1;
+  int items_per_slot = 4;         // (tile, chunk) CTAs aimed at per resident CTA slot
 };
 
 /* four Bayer planes of raw u16 mosaic frames, stacked into four accumulators */

@@ -218,3 +218,14 @@ def test_scale_transform_matches_oracle(capi, oracle):
         want = O.get_params(m, O.scale(m, O.set_params(m, O.identity(m), p), 0.5))
         got = capi.scale_transform(t, p, 0.5)
         assert np.allclose(got, want, rtol=1e-6, atol=1e-6), t
+
+
+def test_tuning_values_are_checked(capi):
+    import ctypes
+    C = capi
+    reg = C.c_ecch(C.default_options())
+    reg.set_tuning({"pass_ctas_per_sm": 2, "pass_tile_w": [64, 128, 0, 0]})
+    assert reg.get_tuning()["pass_tile_w"] == [64, 128, 0, 0]
+    for bad in ({"pass_tile_w": [32, 0, 0, 0]}, {"pass_ctas_per_sm": -1}, {"stack_max_chunks": 99}):
+        t = C.Tuning.from_dict(bad)
+        assert C.lib().sst_ecch_set_tuning(reg.handle, ctypes.byref(t)) == C.ERR_INVALID_ARG

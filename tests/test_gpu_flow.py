@@ -91,3 +91,32 @@ def test_eccflow_identical_frames_give_identity(gpu):
     fl.set_reference_image(ref)
     rm = fl.compute(np.stack([ref, ref]))
     assert np.abs(_flow(rm[0])).max() < 1e-5 and np.abs(_flow(rm[1])).max() < 1e-5
+
+
+@pytest.mark.parametrize("ref_masked,cur_masked", [(True, False), (False, True), (True, True)])
+def test_eccflow_masks_match_oracle(gpu, oracle, ref_masked, cur_masked):
+    """Masks (set_reference_image(reference, mask), compute(current, rmap,
+    mask)): per level INTER_NEAREST mask pyramids; in each update the current
+    mask remapped INTER_NEAREST by the flow and ANDed with the reference mask
+    zeroes It gx, It gy (ecc2.cc:2253-2335)."""
+    C, O = gpu, oracle
+    w, h = 160, 112
+    ref, frames, _ = _scene(w, h, 21, n=2)
+    rng = np.random.default_rng(4)
+    rmask = np.full((h, w), 255, np.uint8)
+    rmask[20:60, 30:90] = 0
+    rmask[rng.integers(0, h, 200), rng.integers(0, w, 200)] = 0
+    cmasks = np.full((2, h, w), 255, np.uint8)
+    cmasks[:, :, :12] = 0
+    cmasks[1, 70:, 100:] = 0
+    kw = dict(scale_factor=0.5, support_scale=3, max_iterations=2, min_image_size=8)
+    fl = C.c_eccflow(C.eccflow_options(**kw))
+    fl.set_reference_image(ref, mask=rmask if ref_masked else None)
+    rm = fl.compute(frames, masks=cmasks if cur_masked else None)
+    oo = O.flow_opts(**kw)
+    for i in range(2):
+        f_o = O.eccflow(oo, ref.astype(np.float64), frames[i].astype(np.float64),
+                        ref_mask=rmask if ref_masked else None, cur_mask=cmasks[i] if cur_masked else None)
+        d = _flow(rm[i]) - f_o
+        rms = float(np.sqrt(np.mean(d ** 2)))
+        assert rms <= RMS_TOL and np.abs(d).max() <= MAX_TOL, (i, rms, np.abs(d).max())

@@ -692,3 +692,29 @@ def test_fp32_baseline_restatement_matches_oracle(oracle):
     both = (W > 0) & (Wr > 0)
     rel = O.stack_rel_err(A[both], S[both] / W[both])
     assert np.median(rel) < 1e-4
+
+
+def test_eccflow_masks_known_answers(oracle):
+    """c_eccflow masks: an all-valid reference mask changes nothing; an empty
+    one stops every update (the flow stays at its start); half a reference
+    mask changes the flow."""
+    O = oracle
+    rng = np.random.default_rng(2)
+    h, w = 64, 80
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    ref = 10 + 4 * np.sin(x / 3.1) * np.cos(y / 2.3) + np.sin((x + y) / 5.0)
+    cur = 10 + 4 * np.sin((x - 0.6) / 3.1) * np.cos((y + 0.4) / 2.3) + np.sin((x + y - 0.2) / 5.0)
+    o = O.flow_opts(support_scale=2, max_iterations=2, scale_factor=0.5, min_image_size=8)
+    base = O.eccflow(o, ref, cur)
+    assert np.array_equal(O.eccflow(o, ref, cur, ref_mask=np.full((h, w), 255, np.uint8)), base)
+    assert np.array_equal(O.eccflow(o, ref, cur, ref_mask=np.zeros((h, w), np.uint8)), np.zeros((h, w, 2)))
+    init = np.stack([np.full((h, w), 0.3), np.full((h, w), -0.2)], axis=-1)
+    assert np.allclose(O.eccflow(o, ref, cur, init_flow=init, ref_mask=np.zeros((h, w), np.uint8)), init)
+    # an all-valid current mask still drops samples whose nearest source pixel lies
+    # outside the frame: the flow changes, but only from the border inwards
+    full = O.eccflow(o, ref, cur, cur_mask=np.full((h, w), 255, np.uint8))
+    assert np.abs(full - base).max() > 0
+    m = np.full((h, w), 255, np.uint8)
+    m[:, : w // 2] = 0
+    half = O.eccflow(o, ref, cur, ref_mask=m)
+    assert np.abs(half - base).max() > 1e-3
