@@ -289,6 +289,45 @@ int sst_local_variance_compute(sst_local_variance * h, const void * frames, int 
  * the options of sst_stack_frames' weighting 3 (defaults until set). */
 int sst_weighted_average_set_local_variance(sst_weighted_average * h, const sst_local_variance_options * opts);
 
+/* ------------------------------------------------------------ LPG weights */
+
+/* c_lpg_options (core/proc/sharpness_measure/c_lpg_sharpness_measure.h:
+ * 22-28): k weighs the Laplacian against the gradient (alpha = k / (k + 1),
+ * beta = 1 / (k + 1)), p the power of the map (0 and 1: none), dscale the
+ * pyrDowns before the 5 x 5 operators, uscale the total pyrDowns of the map
+ * before it is upscaled back. */
+typedef struct sst_lpg_options {
+  double k;
+  double p;
+  int32_t dscale;
+  int32_t uscale;
+} sst_lpg_options;
+
+/* the reference defaults: k 2, p 2, dscale 2, uscale 6 */
+void sst_lpg_options_default(sst_lpg_options * opts);
+
+typedef struct sst_lpg sst_lpg;
+
+/* c_lpg_sharpness_measure (c_lpg_sharpness_measure.h:44-80); opts NULL:
+ * the defaults */
+int sst_lpg_create(sst_lpg ** out, const sst_lpg_options * opts);
+int sst_lpg_destroy(sst_lpg * h);
+
+/* lpg() (core/proc/lpg.cc:223-291) of n mono frames: the map
+ * alpha lap^2 + beta |grad|^2 + 1e-9 of the 5 x 5 noise-robust Laplacian and
+ * extended Sobel gradient (lpg.cc:60-131) after dscale pyrDowns
+ * (BORDER_REFLECT_101) of the frames converted to [0, 1] by their depth's
+ * maximum and multiplied by 1 / (1 + dscale); then (uscale - dscale) further
+ * pyrDowns, times (uscale - dscale), to the power p, and pyrUps back to the
+ * frame size. `maps` (may be NULL) receives n packed width x height FP32 maps,
+ * `metrics` (may be NULL) the n means of the maps over the nonzero pixels of
+ * `masks` (NULL: all pixels). Frames, masks and maps are device pointers
+ * when on_device, else host. SST_ERR_INVALID_ARG when the map would be
+ * smaller than 5 x 5 after dscale. */
+int sst_lpg_compute(sst_lpg * h, const void * frames, int depth, int n, int width, int height, size_t row_stride,
+    size_t frame_stride, const uint8_t * masks, size_t mask_row_stride, size_t mask_frame_stride, int on_device,
+    float * maps, double * metrics, void * stream);
+
 /* ---------------------------------------------------- input calibration */
 
 /* read_input_frame's dark / flat calibration of raw frames
@@ -302,6 +341,19 @@ int sst_weighted_average_set_local_variance(sst_weighted_average * h, const sst_
 int sst_calibrate_frames(const void * frames, int depth, int n, int width, int height, size_t row_stride,
     size_t frame_stride, double scale, const float * dark, size_t dark_stride, const float * flat, size_t flat_stride,
     float * out, size_t out_row_stride, size_t out_frame_stride, void * stream);
+
+/* nninterpolation (core/debayer.cc:828-1161), read_input_frame's
+ * DEBAYER_NN2 (c_image_stacking_pipeline_base.cc:220-235): n device Bayer
+ * frames (u8, u16 or f32; even width and height) into n device 3-channel BGR
+ * frames of the same depth. colorid is the pattern: 8 RGGB, 9 GRBG, 10 GBRG,
+ * 11 BGGR. At each pixel its own colour is copied; a green pixel takes red
+ * and blue as the means of its two horizontal or vertical neighbours; a red
+ * or blue pixel takes green as the mean of its 4 edge neighbours and the
+ * other colour as the mean of its 4 diagonal neighbours (BORDER_REFLECT_101;
+ * integer types round the means half up). Strides in bytes (dst rows hold
+ * 3 * width elements). */
+int sst_debayer_nn2(const void * frames, int depth, int n, int width, int height, size_t row_stride,
+    size_t frame_stride, int colorid, void * dst, size_t dst_row_stride, size_t dst_frame_stride, void * stream);
 
 /* ------------------------------------------------------ post-stack steps */
 

@@ -129,6 +129,9 @@ def lib():
             "orc_register_frame": (i, [p, p, p, i, i, p, p, p, p]),
             "ref_register_and_stack": (i, [p, p, i, i, p, i, d, p, p, p, p, p]),
             "orc_eccflow_masked": (i, [p, p, p, p, p, i, i, p, p]),
+            "orc_lpg": (i, [p, p, i, i, d, d, i, i, p, p]),
+            "orc_debayer_nn2_u16": (i, [p, i, i, i, p]),
+            "orc_debayer_nn2_f32": (i, [p, i, i, i, p]),
             "orc_set_num_threads": (None, [i]),
             "orc_get_num_threads": (i, []),
         }
@@ -756,3 +759,32 @@ def refcpu_register_and_stack(o: PipelineOpts, ref, frames, frame_scale):
     lib().ref_register_and_stack(C.byref(o), _ptr(r), w, h, _ptr(fr), n, frame_scale, _ptr(states), _ptr(status),
                                  _ptr(rho), _ptr(acc), _ptr(accw))
     return states, status, rho, acc, accw
+
+
+def lpg(img, k=2.0, p=2.0, dscale=2, uscale=6, mask=None):
+    """lpg() (core/proc/lpg.cc:223-291) of an image already scaled like the
+    reference's convertTo(1 / maxval): (map, metric); c_lpg_options defaults."""
+    a = _f64(img)
+    h, w = a.shape
+    out = np.empty((h, w))
+    met = C.c_double()
+    r = lib().orc_lpg(_ptr(a), _ptr(_u8(mask)), w, h, k, p, dscale, uscale, _ptr(out), C.byref(met))
+    if r != 0:
+        raise ValueError("lpg: the map is smaller than 5 x 5")
+    return out, met.value
+
+
+def debayer_nn2(raw, colorid=8):
+    """debayer NN2 (core/io/debayer.cc:828-1161): (h, w, 3) B, G, R of a u16 or f32 mosaic."""
+    a = np.ascontiguousarray(raw)
+    h, w = a.shape
+    if a.dtype == np.uint16:
+        out = np.empty((h, w, 3), np.uint16)
+        r = lib().orc_debayer_nn2_u16(_ptr(a), w, h, colorid, _ptr(out))
+    else:
+        a = np.ascontiguousarray(a, np.float32)
+        out = np.empty((h, w, 3), np.float32)
+        r = lib().orc_debayer_nn2_f32(_ptr(a), w, h, colorid, _ptr(out))
+    if r != 0:
+        raise ValueError("debayer_nn2: odd size or not a Bayer pattern")
+    return out

@@ -253,6 +253,15 @@ void orc_ecc_normalize(const double * src, const uint8_t * mask, int w, int h, i
 int orc_register_frame(const orc_registration_opts * o, const double * ref, const uint8_t * ref_mask,
     int w, int h, const double * cur, double * state, double * rho, int * iters);
 
+/* lpg() (core/proc/lpg.cc:223-291) of a mono image already scaled to
+ * [0, 1] (integer input / maxval); map w x h, metric = mean(map) (masked) */
+int orc_lpg(const double * img, const uint8_t * mask, int w, int h, double k, double p, int dscale, int uscale,
+    double * map, double * metric);
+
+/* debayer NN2 (core/io/debayer.cc:828-1161): BGR interleaved output */
+int orc_debayer_nn2_u16(const uint16_t * src, int w, int h, int colorid, uint16_t * dst);
+int orc_debayer_nn2_f32(const float * src, int w, int h, int colorid, float * dst);
+
 void orc_set_num_threads(int n);
 int  orc_get_num_threads(void);
 

@@ -260,3 +260,77 @@ extern "C" int orc_register_frame(const orc_registration_opts * o, const double 
   if( scaled ) orc_model_scale(&m, state, 1.0 / o->scale);
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* debayer NN2 (core/io/debayer.cc:828-1161, _debayer_nn2_interpolation): per
+ * pixel, its own colour as it is; green at a red or blue site the mean of the
+ * 4 cross neighbours; at a green site the colour of its row neighbours the
+ * mean of those 2, the other colour the mean of the 2 column neighbours; red
+ * at a blue site (and blue at a red one) the mean of the 4 diagonal
+ * neighbours. Neighbours outside the frame reflect (BORDER_REFLECT_101: row
+ * -1 is row 1, column w is column w - 2). Integer frames round the means
+ * half up ((sum + n / 2) / n in integer arithmetic), float ones do not.
+ * Output: B, G, R interleaved. colorid: 8 RGGB, 9 GRBG, 10 GBRG, 11 BGGR. */
+namespace {
+
+/* colour (0 B, 1 G, 2 R) of mosaic position (x, y) */
+int bayer_color(int colorid, int x, int y)
+{
+  static const int pat[4][4] = {
+    { 2, 1, 1, 0 },   // RGGB, index (y & 1) * 2 + (x & 1)
+    { 1, 2, 0, 1 },   // GRBG
+    { 1, 0, 2, 1 },   // GBRG
+    { 0, 1, 1, 2 },   // BGGR
+  };
+  return pat[colorid - 8][(y & 1) * 2 + (x & 1)];
+}
+
+/* sums in the accumulation type A (int64 for integer frames, float for
+ * float ones, added left to right in the order N W E S / NW NE SW SE / W E /
+ * N S as the reference adds them) */
+template<class T, class A>
+void nn2(const T * src, int w, int h, int colorid, T * dst, bool integral)
+{
+  auto at = [&](int x, int y) -> A {
+    x = x < 0 ? -x : (x >= w ? 2 * (w - 1) - x : x);
+    y = y < 0 ? -y : (y >= h ? 2 * (h - 1) - y : y);
+    return (A) src[(size_t) y * w + x];
+  };
+  auto mean = [&](A s, int n) -> T {
+    if( integral ) return (T) (((long long) s + n / 2) / n);
+    return (T) (s / (A) n);
+  };
+  for( int y = 0; y < h; ++y ) {
+    for( int x = 0; x < w; ++x ) {
+      const int own = bayer_color(colorid, x, y);
+      T out[3];
+      for( int ch = 0; ch < 3; ++ch ) {
+        if( ch == own ) out[ch] = (T) at(x, y);
+        else if( ch == 1 ) out[ch] = mean(at(x, y - 1) + at(x - 1, y) + at(x + 1, y) + at(x, y + 1), 4);
+        else if( own == 1 ) {
+          if( bayer_color(colorid, x + 1, y) == ch ) out[ch] = mean(at(x - 1, y) + at(x + 1, y), 2);
+          else out[ch] = mean(at(x, y - 1) + at(x, y + 1), 2);
+        }
+        else out[ch] = mean(at(x - 1, y - 1) + at(x + 1, y - 1) + at(x - 1, y + 1) + at(x + 1, y + 1), 4);
+      }
+      T * d = dst + ((size_t) y * w + x) * 3;
+      d[0] = out[0], d[1] = out[1], d[2] = out[2];
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int orc_debayer_nn2_u16(const uint16_t * src, int w, int h, int colorid, uint16_t * dst)
+{
+  if( (w & 1) || (h & 1) || colorid < 8 || colorid > 11 ) return -1;
+  nn2<uint16_t, long long>(src, w, h, colorid, dst, true);
+  return 0;
+}
+
+extern "C" int orc_debayer_nn2_f32(const float * src, int w, int h, int colorid, float * dst)
+{
+  if( (w & 1) || (h & 1) || colorid < 8 || colorid > 11 ) return -1;
+  nn2<float, float>(src, w, h, colorid, dst, false);
+  return 0;
+}

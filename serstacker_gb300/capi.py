@@ -194,6 +194,11 @@ def lib():
             "sst_ser_writer_close": (i, [p]),
             "sst_average_pyramid_inpaint": (i, [p, sz, p, sz, i, i, i, p, sz, p, sz, i, p]),
             "sst_calibrate_frames": (i, [p, i, i, i, i, sz, sz, d, p, sz, p, sz, p, sz, sz, p]),
+            "sst_debayer_nn2": (i, [p, i, i, i, i, sz, sz, i, p, sz, sz, p]),
+            "sst_lpg_options_default": (None, [p]),
+            "sst_lpg_create": (i, [p, p]),
+            "sst_lpg_destroy": (i, [p]),
+            "sst_lpg_compute": (i, [p, p, i, i, i, i, sz, sz, p, sz, sz, i, p, p, p]),
             "sst_ecch_set_tuning": (i, [p, p]),
             "sst_ecch_get_tuning": (i, [p, p]),
             "sst_weighted_average_set_tuning": (i, [p, p]),
@@ -542,6 +547,53 @@ class c_local_variance_sharpness_measure:
         return maps, q
 
 
+class LpgOptions(C.Structure):
+    """c_lpg_options (c_lpg_sharpness_measure.h:22-28)"""
+    _fields_ = [("k", C.c_double), ("p", C.c_double), ("dscale", C.c_int32), ("uscale", C.c_int32)]
+
+
+def lpg_options(**kw) -> LpgOptions:
+    o = LpgOptions()
+    lib().sst_lpg_options_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class c_lpg_sharpness_measure:
+    """c_lpg_sharpness_measure (c_lpg_sharpness_measure.h:44-80) over the C
+    ABI: lpg() maps and metrics of batches of mono frames."""
+
+    def __init__(self, options: Optional[LpgOptions] = None, **kw):
+        self.options = options if options is not None else lpg_options(**kw)
+        self._h = C.c_void_p()
+        _check(lib().sst_lpg_create(C.byref(self._h), C.byref(self.options)), "sst_lpg_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_lpg_destroy(h)
+            self._h = C.c_void_p()
+
+    def compute(self, frames: np.ndarray, masks: Optional[np.ndarray] = None):
+        """frames (n, h, w) or (h, w) u8 / u16 / f32, masks of the same shape
+        (u8, nonzero = valid) or None -> (maps (n, h, w) float32, metrics (n,)
+        float64)"""
+        f = np.ascontiguousarray(frames)
+        if f.ndim == 2:
+            f = f[None]
+        n, h, w = f.shape
+        mk = None
+        if masks is not None:
+            mk = np.ascontiguousarray(masks, dtype=np.uint8).reshape(n, h, w)
+        maps = np.zeros((n, h, w), np.float32)
+        metrics = np.zeros(n, np.float64)
+        _check(lib().sst_lpg_compute(self._h, _ptr(f), _NP_DEPTH[f.dtype], n, w, h, f.strides[1], f.strides[0],
+                                     None if mk is None else _ptr(mk), w, w * h, 0, _ptr(maps), _ptr(metrics), None),
+               "sst_lpg_compute")
+        return maps, metrics
+
+
 class c_weigthed_average:
     """c_weigthed_average (c_frame_accumulation.h:39-63) over the C ABI."""
 
@@ -875,6 +927,23 @@ def calibrate_frames(frames, scale: float, dark=None, flat=None):
                                       None if flat is None else flat.data_ptr(), 0, out.data_ptr(), 0, 0, None),
            "sst_calibrate_frames")
     return out
+
+
+def debayer_nn2(raw, colorid: int):
+    """sst_debayer_nn2: raw (n, h, w) or (h, w) Bayer frames, numpy u8 / u16 /
+    f32 -> (n, h, w, 3) BGR frames of the same dtype (through device
+    buffers)"""
+    import torch
+    r = np.ascontiguousarray(raw)
+    if r.ndim == 2:
+        r = r[None]
+    n, h, w = r.shape
+    dev = torch.from_numpy(r.view(np.int16) if r.dtype == np.uint16 else r).cuda()
+    out = torch.empty((n, h, w, 3), dtype=dev.dtype, device=dev.device)
+    _check(lib().sst_debayer_nn2(dev.data_ptr(), _NP_DEPTH[r.dtype], n, w, h, w * r.itemsize, w * h * r.itemsize,
+                                 colorid, out.data_ptr(), 0, 0, None), "sst_debayer_nn2")
+    res = out.cpu().numpy()
+    return res.view(np.uint16) if r.dtype == np.uint16 else res
 
 
 def average_pyramid_inpaint(image: np.ndarray, mask: np.ndarray, max_levels: int = 100):

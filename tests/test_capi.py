@@ -229,3 +229,35 @@ def test_tuning_values_are_checked(capi):
     for bad in ({"pass_tile_w": [32, 0, 0, 0]}, {"pass_ctas_per_sm": -1}, {"stack_max_chunks": 99}):
         t = C.Tuning.from_dict(bad)
         assert C.lib().sst_ecch_set_tuning(reg.handle, ctypes.byref(t)) == C.ERR_INVALID_ARG
+
+
+def test_lpg_host_checks(capi):
+    """c_lpg_options defaults and the argument checks of sst_lpg_* (no GPU work)"""
+    import ctypes as C
+    o = capi.lpg_options()
+    assert (o.k, o.p, o.dscale, o.uscale) == (2.0, 2.0, 2, 6)
+    lib = capi.lib()
+    h = C.c_void_p()
+    assert lib.sst_lpg_create(C.byref(h), C.byref(capi.lpg_options(dscale=-1))) == -1
+    assert not h.value
+    assert lib.sst_lpg_create(C.byref(h), None) == 0
+    try:
+        buf = (C.c_uint16 * 144)()
+        assert lib.sst_lpg_compute(h, None, capi.DEPTH_U16, 1, 12, 12, 24, 288, None, 0, 0, 0, None, None, None) == -1
+        assert lib.sst_lpg_compute(h, buf, 3, 1, 12, 12, 24, 288, None, 0, 0, 0, None, None, None) == -1
+        assert lib.sst_lpg_compute(h, buf, capi.DEPTH_U16, 1, 12, 12, 12, 288, None, 0, 0, 0, None, None, None) == -1
+        # two pyrDowns of 12 x 12 leave 3 x 3: too small for the 5 x 5 operators
+        assert lib.sst_lpg_compute(h, buf, capi.DEPTH_U16, 1, 12, 12, 24, 288, None, 0, 0, 0, None, None, None) == -1
+        assert "5 x 5" in capi.last_error()
+    finally:
+        lib.sst_lpg_destroy(h)
+
+
+def test_debayer_nn2_argument_checks(capi):
+    """sst_debayer_nn2 rejects bad arguments before any GPU work"""
+    lib = capi.lib()
+    assert lib.sst_debayer_nn2(None, capi.DEPTH_U16, 1, 8, 8, 16, 128, 8, 1, 0, 0, None) == -1
+    assert lib.sst_debayer_nn2(1, capi.DEPTH_U16, 1, 8, 8, 16, 128, 7, 1, 0, 0, None) == -1    # not a Bayer pattern
+    assert lib.sst_debayer_nn2(1, capi.DEPTH_U16, 1, 9, 8, 18, 144, 8, 1, 0, 0, None) == -1    # odd width
+    assert lib.sst_debayer_nn2(1, capi.DEPTH_U16, 1, 8, 8, 14, 128, 8, 1, 0, 0, None) == -1    # short rows
+    assert lib.sst_debayer_nn2(1, 6, 1, 8, 8, 64, 512, 8, 1, 0, 0, None) == -1                 # f64

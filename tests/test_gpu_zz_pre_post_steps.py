@@ -93,3 +93,22 @@ def test_calibration_is_the_reference_sequence_in_fp32(gpu, dtype, scale, use_da
         want = (want * np.float32(5)) / flat
     assert want.dtype == np.float32
     assert np.array_equal(out, want)
+
+
+@pytest.mark.parametrize("colorid", [8, 9, 10, 11])
+@pytest.mark.parametrize("dtype", [np.uint16, np.float32])
+def test_debayer_nn2_bit_exact(gpu, oracle, colorid, dtype):
+    """read_input_frame's DEBAYER_NN2 (nninterpolation, core/debayer.cc:
+    828-1161) of raw Bayer frames against the oracle: bitwise."""
+    C, O = gpu, oracle
+    rng = np.random.default_rng(colorid)
+    n, h, w = 3, 62, 90
+    if dtype == np.uint16:
+        raw = rng.integers(0, 65536, (n, h, w)).astype(np.uint16)
+    else:
+        raw = rng.random((n, h, w)).astype(np.float32)
+    got = C.debayer_nn2(raw, colorid)
+    for i in range(n):
+        want = O.debayer_nn2(raw[i], colorid)
+        assert got[i].dtype == want.dtype
+        assert np.array_equal(got[i].view(np.uint8), want.view(np.uint8)), i

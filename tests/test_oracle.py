@@ -718,3 +718,66 @@ def test_eccflow_masks_known_answers(oracle):
     m[:, : w // 2] = 0
     half = O.eccflow(o, ref, cur, ref_mask=m)
     assert np.abs(half - base).max() > 1e-3
+
+
+def test_lpg_known_answers(oracle):
+    """lpg() (core/proc/lpg.cc:223-291): a flat image gives the map eps
+    (1e-9) scaled by (uscale - dscale) and raised to p; a ramp a x has no
+    Laplacian and the extended-Sobel gradient 56 a, so with no scaling and
+    p = 1 the map is beta (100 / 36)^2 (56 a)^2 + eps everywhere (the edge
+    rows and columns copy their inner neighbours)."""
+    O = oracle
+    m, met = O.lpg(np.full((40, 56), 0.3))
+    assert np.allclose(m, (4 * 1e-9) ** 2, rtol=1e-9) and np.isclose(met, (4e-9) ** 2, rtol=1e-9)
+    a, k = 0.01, 2.0
+    ramp = np.tile(np.arange(56) * a, (40, 1))
+    m, met = O.lpg(ramp, k=k, p=1.0, dscale=0, uscale=0)
+    want = 1.0 / (k + 1) * (100.0 / 36.0) ** 2 * (56 * a) ** 2 + 1e-9
+    assert np.allclose(m, want, rtol=1e-12) and np.isclose(met, want, rtol=1e-12)
+    # the map has the image's size for every dscale / uscale, and the metric is its (masked) mean
+    img = np.random.default_rng(3).random((100, 140))
+    for ds, us in ((0, 0), (1, 3), (2, 6), (3, 3)):
+        m, met = O.lpg(img, dscale=ds, uscale=us)
+        assert m.shape == img.shape and np.isclose(met, m.mean())
+    mask = np.zeros((100, 140), np.uint8)
+    mask[20:60, 30:90] = 255
+    m, met = O.lpg(img, mask=mask)
+    assert np.isclose(met, m[mask > 0].mean())
+
+
+def test_debayer_nn2_known_answers(oracle):
+    """debayer NN2 (core/io/debayer.cc:828-1161) against a direct restatement
+    of the reference's per-position formulas on an RGGB mosaic, including the
+    reflected first / last rows and columns and the integer rounding; the
+    other patterns are the RGGB rule on the mosaic shifted by their cell
+    offset."""
+    O = oracle
+    rng = np.random.default_rng(6)
+    h, w = 6, 8
+    raw = rng.integers(0, 4096, size=(h, w)).astype(np.uint16)
+    out = O.debayer_nn2(raw, 8)
+    r = lambda v: 2 * (h - 1) - v if v >= h else abs(v)
+    c = lambda v: 2 * (w - 1) - v if v >= w else abs(v)
+    s = lambda x, y: int(raw[r(y), c(x)])
+    for y in range(h):
+        for x in range(w):
+            q = (s(x, y - 1) + s(x - 1, y) + s(x + 1, y) + s(x, y + 1) + 2) // 4
+            d = (s(x - 1, y - 1) + s(x + 1, y - 1) + s(x - 1, y + 1) + s(x + 1, y + 1) + 2) // 4
+            hz = (s(x - 1, y) + s(x + 1, y) + 1) // 2
+            vt = (s(x, y - 1) + s(x, y + 1) + 1) // 2
+            if y % 2 == 0 and x % 2 == 0:      # R
+                want = (d, q, s(x, y))
+            elif y % 2 == 0:                   # G in an R row: R horizontal, B vertical
+                want = (vt, s(x, y), hz)
+            elif x % 2 == 0:                   # G in a B row: B horizontal, R vertical
+                want = (hz, s(x, y), vt)
+            else:                              # B
+                want = (s(x, y), q, d)
+            assert tuple(out[y, x]) == want, (x, y, tuple(out[y, x]), want)
+    big = rng.integers(0, 4096, size=(12, 16)).astype(np.uint16)
+    for cid, (dy, dx) in ((9, (0, 1)), (10, (1, 0)), (11, (1, 1))):
+        a = O.debayer_nn2(big, cid)
+        b = O.debayer_nn2(big[dy:dy + 10, dx:dx + 14], 8)
+        assert np.array_equal(a[dy + 1:dy + 9, dx + 1:dx + 13], b[1:9, 1:13]), cid
+    fl = rng.random((6, 8)).astype(np.float32)
+    assert np.array_equal(O.debayer_nn2(fl, 8)[..., 2][0::2, 0::2], fl[0::2, 0::2])
