@@ -368,6 +368,137 @@ int sst_average_pyramid_inpaint(const float * src, size_t src_stride, const uint
     int width, int height, int max_levels, float * dst, size_t dst_stride, uint8_t * dst_mask,
     size_t dst_mask_stride, int on_device, void * stream);
 
+/* ------------------------------------------------------ other accumulators */
+
+/* cv::getOptimalDFTSize: the smallest 2^a 3^b 5^c >= n */
+int sst_optimal_dft_size(int n);
+
+typedef struct sst_fft_average sst_fft_average;
+
+/* c_frame_accumulation_with_fft (core/average/c_frame_accumulation.cc:
+ * 704-900). Frames are padded with BORDER_REFLECT to the optimal DFT size
+ * (fftGetOptimalSize, core/proc/fft.cc:17-57, centred), transformed, and
+ * their spectra averaged with per-bin weights max(s, (|F|^2 s)^3),
+ * s = 1 / (DFT area)^2 (fftPower, c_frame_accumulation.cc:940-980); the
+ * average is the inverse transform of the weighted mean spectrum, cropped
+ * to the frame. Mono frames of an already optimal size get their weights
+ * like the others (the reference leaves them empty there and fails). */
+int sst_fft_average_create(sst_fft_average ** out);
+int sst_fft_average_destroy(sst_fft_average * h);
+int sst_fft_average_clear(sst_fft_average * h);
+int sst_fft_average_accumulated_frames(const sst_fft_average * h);
+/* the DFT size of the accumulated frames (0 x 0 before the first add) */
+int sst_fft_average_size(const sst_fft_average * h, int * fft_width, int * fft_height);
+
+/* add n frames (u8 / u16 / f32, `channels` interleaved channels, values
+ * times `scale`); every frame of one accumulator has the same size and
+ * channels. Host or device frames per on_device. */
+int sst_fft_average_add(sst_fft_average * h, const void * frames, int depth, int n, int width, int height, int channels,
+    size_t row_stride, size_t frame_stride, double scale, int on_device, void * stream);
+
+/* avg (width x height x channels FP32, interleaved) and mask (u8, all 255 as
+ * the reference returns it); either may be NULL; strides 0 = packed. */
+int sst_fft_average_compute(sst_fft_average * h, float * avg, size_t avg_row_stride, uint8_t * mask,
+    size_t mask_row_stride, int on_device, void * stream);
+
+typedef struct sst_canvas_average sst_canvas_average;
+
+/* c_canvas_average (c_frame_accumulation.cc:264-450); canvas_width /
+ * canvas_height: setCanvasSize (0 = none). The canvas is max(requested,
+ * 3/2 of the first frame) on each side. */
+int sst_canvas_average_create(sst_canvas_average ** out, int canvas_width, int canvas_height);
+int sst_canvas_average_destroy(sst_canvas_average * h);
+int sst_canvas_average_clear(sst_canvas_average * h);
+int sst_canvas_average_set_canvas_size(sst_canvas_average * h, int canvas_width, int canvas_height);
+
+/* canvas size, last_bbox (x, y, width, height) and accumulated_frames; any
+ * pointer may be NULL */
+int sst_canvas_average_state(const sst_canvas_average * h, int * canvas_width, int * canvas_height, int * last_bbox,
+    int * accumulated_frames);
+
+/* c_canvas_average::add(image, weights_or_mask, rmap, new_canvas_bbox): the
+ * first frame is centred on the new canvas; later frames without rmap and
+ * bbox (bbox NULL or of zero size) land on the last box; with both, the box
+ * is clipped to the canvas, the canvas contents shift by 64 px when the box
+ * comes within 32 px of an edge (maintainCanvasBoundaries), and the image
+ * remapped by rmap (bbox width x height x 2 floats, interleaved x, y;
+ * LINEAR / BORDER_REPLICATE) with its weights (u8 mask: NEAREST, f32:
+ * LINEAR; BORDER_CONSTANT 0; NULL: weight 1) updates the running mean
+ * A += (I - A) w / W, W += w (_weighted_average_update, :20-129, FP32). A box
+ * clipped by the canvas is counted but not added, as in the reference.
+ * SST_ERR_INVALID_ARG for an empty box. */
+int sst_canvas_average_add(sst_canvas_average * h, const void * image, int depth, int width, int height, int channels,
+    size_t row_stride, double scale, const void * weights, int weights_depth, size_t weights_stride,
+    const float * rmap, const int32_t * bbox, int on_device, void * stream);
+
+/* c_canvas_average::compute(avg, mask, dscale, -1, rbbox): the canvas (or
+ * the part inside rbbox, when given with a nonzero size) times dscale,
+ * interleaved FP32, and mask = 255 where the weight sum is > 0. out_bbox
+ * (may be NULL) receives the box returned. */
+int sst_canvas_average_compute(sst_canvas_average * h, float * avg, size_t avg_row_stride, uint8_t * mask,
+    size_t mask_row_stride, double dscale, const int32_t * rbbox, int32_t * out_bbox, int on_device, void * stream);
+
+/* c_canvas_average::counter(): the weight plane (canvas size, FP32) */
+int sst_canvas_average_counter(sst_canvas_average * h, float * W, size_t row_stride, int on_device, void * stream);
+
+/* c_laplacian_pyramid_focus_stacking::fusing_policy
+ * (c_frame_accumulation.h:153-156) */
+#define SST_FOCUS_SELECT_MAX_ENERGY  0
+#define SST_FOCUS_WEIGHTED_AVERAGE   1
+
+/* c_laplacian_pyramid_focus_stacking::options (c_frame_accumulation.h:
+ * 158-164): fusing_policy, inpaint_mask_holes (fill the mask holes of each
+ * frame first), avgchannel (weighted_average: one weight from the channel
+ * sum), kradius / ksigma (the Gaussian that smooths the energies:
+ * getGaussianKernel(2 kradius + 1, ksigma); ksigma <= 0 takes the documented
+ * default sigma 0.3 ((ksize - 1) / 2 - 1) + 0.8; none when both are 0) */
+typedef struct sst_focus_stack_options {
+  int32_t fusing_policy;
+  int32_t inpaint_mask_holes;
+  int32_t avgchannel;
+  int32_t kradius;
+  double ksigma;
+} sst_focus_stack_options;
+
+/* the reference defaults: select_max_energy, inpaint 1, avgchannel 1, no smoothing */
+void sst_focus_stack_options_default(sst_focus_stack_options * opts);
+
+typedef struct sst_focus_stack sst_focus_stack;
+
+/* c_laplacian_pyramid_focus_stacking (c_frame_accumulation.cc:464-688);
+ * opts NULL: the defaults */
+int sst_focus_stack_create(sst_focus_stack ** out, const sst_focus_stack_options * opts);
+int sst_focus_stack_destroy(sst_focus_stack * h);
+int sst_focus_stack_clear(sst_focus_stack * h);
+int sst_focus_stack_accumulated_frames(const sst_focus_stack * h);
+/* the smoothing kernel's taps (k may be NULL to ask for *n; 0 taps: none) */
+int sst_focus_stack_kernel(const sst_focus_stack * h, float * k, int * n);
+
+/* add(src, mask) for n frames (u8 / u16 / f32 times `scale`, 1..4
+ * interleaved channels, the same size for every frame): the Laplacian
+ * pyramid (build_laplacian_pyramid, core/proc/laplacian_pyramid.cc:45-96,
+ * minimum size 8) of each frame, after linear_interpolation_inpaint of its
+ * mask holes when inpaint_mask_holes; the levels zeroed where the frame's
+ * u8 mask pyramid is below 255; folded into the accumulated pyramid in
+ * frame order. masks may be NULL. */
+int sst_focus_stack_add(sst_focus_stack * h, const void * frames, int depth, int n, int width, int height, int channels,
+    size_t row_stride, size_t frame_stride, double scale, const uint8_t * masks, size_t mask_row_stride,
+    size_t mask_frame_stride, int on_device, void * stream);
+
+/* compute(avg): reconstruct_laplacian_pyramid of the fused pyramid
+ * (weighted_average: of acc / wwp), interleaved FP32 (stride 0 = packed) */
+int sst_focus_stack_compute(sst_focus_stack * h, float * avg, size_t avg_row_stride, int on_device, void * stream);
+
+/* linear_interpolation_inpaint(image, mask) (core/proc/inpaint/
+ * linear_interpolation_inpaint.cc): the holes (mask 0) of an interleaved
+ * FP32 image of 1..4 channels filled in place from the nearest valid pixels
+ * of their row and column (a run of holes between s and e takes
+ * sv + (x - s) (ev - sv) / run length; the two directions mix as
+ * (h dv + v dh) / (dh + dv) with the distances dh, dv), repeated until no
+ * hole gains a value. Strides in bytes (0: packed). */
+int sst_linear_interpolation_inpaint(float * image, size_t row_stride, int width, int height, int channels,
+    const uint8_t * mask, size_t mask_stride, int on_device, void * stream);
+
 /* ------------------------------------------------------- stacking pipeline */
 
 /* The per-frame body of the stacking pipeline for n frames

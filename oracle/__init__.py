@@ -132,6 +132,11 @@ def lib():
             "orc_lpg": (i, [p, p, i, i, d, d, i, i, p, p]),
             "orc_debayer_nn2_u16": (i, [p, i, i, i, p]),
             "orc_debayer_nn2_f32": (i, [p, i, i, i, p]),
+            "orc_optimal_dft_size": (i, [i]),
+            "orc_linear_inpaint": (None, [p, p, i, i, i]),
+            "orc_fft_average": (i, [p, i, i, i, i, p]),
+            "orc_focus_stack": (i, [p, p, i, i, i, i, i, i, i, p, i, p]),
+            "orc_canvas_average": (i, [p, i, i, i, i, i, p, p, p, p, p, p, p, p]),
             "orc_set_num_threads": (None, [i]),
             "orc_get_num_threads": (i, []),
         }
@@ -788,3 +793,79 @@ def debayer_nn2(raw, colorid=8):
     if r != 0:
         raise ValueError("debayer_nn2: odd size or not a Bayer pattern")
     return out
+
+
+def optimal_dft_size(n):
+    """cv::getOptimalDFTSize: the smallest 2^a 3^b 5^c >= n"""
+    return lib().orc_optimal_dft_size(int(n))
+
+
+def _hwc(frames):
+    a = np.ascontiguousarray(frames, np.float64)
+    if a.ndim == 3:
+        a = a[..., None]
+    return a
+
+
+def fft_average(frames):
+    """c_frame_accumulation_with_fft (c_frame_accumulation.cc:704-900) of n
+    frames (n, h, w) or (n, h, w, cn) -> the average, same layout as a frame"""
+    a = _hwc(frames)
+    n, h, w, cn = a.shape
+    out = np.empty((h, w, cn))
+    if lib().orc_fft_average(_ptr(a), n, w, h, cn, _ptr(out)) != 0:
+        raise ValueError("fft_average: invalid arguments")
+    return out[..., 0] if np.ndim(frames) == 3 else out
+
+
+def focus_stack(frames, masks=None, policy=0, inpaint=True, avgchannel=True, G=None):
+    """c_laplacian_pyramid_focus_stacking (c_frame_accumulation.cc:464-688):
+    policy 0 select_max_energy, 1 weighted_average; G the energy smoothing
+    kernel (None: no smoothing) -> the fused image"""
+    a = _hwc(frames)
+    n, h, w, cn = a.shape
+    m = None if masks is None else np.ascontiguousarray(masks, np.uint8)
+    g = None if G is None else np.ascontiguousarray(G, np.float64)
+    out = np.empty((h, w, cn))
+    r = lib().orc_focus_stack(_ptr(a), _ptr(m), n, w, h, cn, policy, int(inpaint), int(avgchannel), _ptr(g),
+                              0 if g is None else len(g), _ptr(out))
+    if r < 0:
+        raise ValueError("focus_stack: invalid arguments")
+    return out[..., 0] if np.ndim(frames) == 3 else out
+
+
+def canvas_average(frames, weights=None, boxes=None, rmaps=None, canvas=(0, 0)):
+    """c_canvas_average (c_frame_accumulation.cc:264-450) over a sequence.
+    weights: None, u8 masks or f64 weights (n, h, w); boxes (n, 4) x, y, w, h
+    (w 0: no remap); rmaps: list of (bh, bw, 2) maps (None where no remap).
+    Returns (acc (CH, CW[, cn]), W (CH, CW), status (n,), last bbox)."""
+    a = _hwc(frames)
+    n, h, w, cn = a.shape
+    wk, wp = 0, None
+    if weights is not None:
+        if np.asarray(weights).dtype == np.uint8:
+            wk, wp = 1, np.ascontiguousarray(weights, np.uint8)
+        else:
+            wk, wp = 2, np.ascontiguousarray(weights, np.float64)
+    bx = np.zeros((n, 4), np.int32) if boxes is None else np.ascontiguousarray(boxes, np.int32)
+    parts = [np.asarray(r, np.float64).reshape(-1) for r in (rmaps or []) if r is not None]
+    rm = np.ascontiguousarray(np.concatenate(parts)) if parts else np.zeros(2)
+    cv = np.array([canvas[0], canvas[1]], np.int32)
+    CW, CH = max(canvas[0], 3 * w // 2), max(canvas[1], 3 * h // 2)
+    acc = np.zeros((CH, CW, cn))
+    W = np.zeros((CH, CW))
+    st = np.zeros(n, np.int32)
+    last = np.zeros(4, np.int32)
+    lib().orc_canvas_average(_ptr(a), n, w, h, cn, wk, _ptr(wp), _ptr(bx), _ptr(rm), _ptr(cv), _ptr(acc), _ptr(W),
+                             _ptr(st), _ptr(last))
+    return (acc[..., 0] if np.ndim(frames) == 3 else acc), W, st, last
+
+
+def linear_inpaint(image, mask):
+    """linear_interpolation_inpaint (core/proc/inpaint/linear_interpolation_inpaint.cc)
+    of (h, w) or (h, w, cn) with a u8 mask (0 = hole) -> the filled image"""
+    a = _hwc(np.asarray(image)[None])[0].copy()
+    h, w, cn = a.shape
+    m = np.ascontiguousarray(mask, np.uint8)
+    lib().orc_linear_inpaint(_ptr(a), _ptr(m), w, h, cn)
+    return a[..., 0] if np.ndim(image) == 2 else a

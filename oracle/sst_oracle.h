@@ -262,6 +262,15 @@ int orc_lpg(const double * img, const uint8_t * mask, int w, int h, double k, do
 int orc_debayer_nn2_u16(const uint16_t * src, int w, int h, int colorid, uint16_t * dst);
 int orc_debayer_nn2_f32(const float * src, int w, int h, int colorid, float * dst);
 
+/* other accumulators (sst_oracle_accum.cc) */
+int orc_optimal_dft_size(int n);
+void orc_linear_inpaint(double * image, const uint8_t * mask, int w, int h, int cn);
+int orc_fft_average(const double * frames, int n, int w, int h, int cn, double * avg);
+int orc_focus_stack(const double * frames, const uint8_t * masks, int n, int w, int h, int cn, int policy,
+    int inpaint, int avgchannel, const double * G, int gk, double * avg);
+int orc_canvas_average(const double * frames, int n, int w, int h, int cn, int wkind, const void * weights,
+    const int * boxes, const double * rmaps, int * canvas, double * acc, double * W, int * status, int * last);
+
 void orc_set_num_threads(int n);
 int  orc_get_num_threads(void);
 

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libsst_gb300.so")
-SOURCES = ["sst_capi.cu", "sst_ecc.cu", "sst_pyramid.cu", "sst_stack.cu", "sst_noalloc.cu", "sst_bayer.cu", "sst_replicas.cu", "sst_roi.cu", "sst_flow.cu", "sst_adjoint.cu", "sst_weights.cu", "sst_inpaint.cu", "sst_calib.cu", "sst_registration.cu", "sst_lpg.cu", "sst_ser.cpp"]
+SOURCES = ["sst_capi.cu", "sst_ecc.cu", "sst_pyramid.cu", "sst_stack.cu", "sst_noalloc.cu", "sst_bayer.cu", "sst_replicas.cu", "sst_roi.cu", "sst_flow.cu", "sst_adjoint.cu", "sst_weights.cu", "sst_inpaint.cu", "sst_calib.cu", "sst_registration.cu", "sst_lpg.cu", "sst_accum.cu", "sst_focus.cu", "sst_ser.cpp"]
 HEADERS = ["sst_internal.cuh", "sst_model.cuh", "sst_engine.cuh", "sst_stack.cuh", "sst_host.h", "sst_kernels.cuh", "sst_tma.cuh", "sst_taps.h", "sst_resample.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -63,7 +63,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
     tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcufft", "-lcudart"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
     return LIB

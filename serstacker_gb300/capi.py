@@ -196,6 +196,31 @@ def lib():
             "sst_calibrate_frames": (i, [p, i, i, i, i, sz, sz, d, p, sz, p, sz, p, sz, sz, p]),
             "sst_debayer_nn2": (i, [p, i, i, i, i, sz, sz, i, p, sz, sz, p]),
             "sst_lpg_options_default": (None, [p]),
+            "sst_optimal_dft_size": (i, [i]),
+            "sst_focus_stack_options_default": (None, [p]),
+            "sst_focus_stack_create": (i, [p, p]),
+            "sst_focus_stack_destroy": (i, [p]),
+            "sst_focus_stack_clear": (i, [p]),
+            "sst_focus_stack_accumulated_frames": (i, [p]),
+            "sst_focus_stack_kernel": (i, [p, p, p]),
+            "sst_focus_stack_add": (i, [p, p, i, i, i, i, i, sz, sz, d, p, sz, sz, i, p]),
+            "sst_focus_stack_compute": (i, [p, p, sz, i, p]),
+            "sst_linear_interpolation_inpaint": (i, [p, sz, i, i, i, p, sz, i, p]),
+            "sst_fft_average_create": (i, [p]),
+            "sst_fft_average_destroy": (i, [p]),
+            "sst_fft_average_clear": (i, [p]),
+            "sst_fft_average_accumulated_frames": (i, [p]),
+            "sst_fft_average_size": (i, [p, p, p]),
+            "sst_fft_average_add": (i, [p, p, i, i, i, i, i, sz, sz, d, i, p]),
+            "sst_fft_average_compute": (i, [p, p, sz, p, sz, i, p]),
+            "sst_canvas_average_create": (i, [p, i, i]),
+            "sst_canvas_average_destroy": (i, [p]),
+            "sst_canvas_average_clear": (i, [p]),
+            "sst_canvas_average_set_canvas_size": (i, [p, i, i]),
+            "sst_canvas_average_state": (i, [p, p, p, p, p]),
+            "sst_canvas_average_add": (i, [p, p, i, i, i, i, sz, d, p, i, sz, p, p, i, p]),
+            "sst_canvas_average_compute": (i, [p, p, sz, p, sz, d, p, p, i, p]),
+            "sst_canvas_average_counter": (i, [p, p, sz, i, p]),
             "sst_lpg_create": (i, [p, p]),
             "sst_lpg_destroy": (i, [p]),
             "sst_lpg_compute": (i, [p, p, i, i, i, i, sz, sz, p, sz, sz, i, p, p, p]),
@@ -592,6 +617,209 @@ class c_lpg_sharpness_measure:
                                      None if mk is None else _ptr(mk), w, w * h, 0, _ptr(maps), _ptr(metrics), None),
                "sst_lpg_compute")
         return maps, metrics
+
+
+def _hwc(a):
+    """(h, w) or (h, w, cn) -> contiguous array and (h, w, cn)"""
+    a = np.ascontiguousarray(a)
+    h, w = a.shape[:2]
+    return a, h, w, (a.shape[2] if a.ndim == 3 else 1)
+
+
+class c_frame_accumulation_with_fft:
+    """c_frame_accumulation_with_fft (c_frame_accumulation.h:168-199) over the
+    C ABI: frames (h, w) or (h, w, cn) u8 / u16 / f32."""
+
+    def __init__(self):
+        self._h = C.c_void_p()
+        _check(lib().sst_fft_average_create(C.byref(self._h)), "sst_fft_average_create")
+        self._cn, self._shape = 1, None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_fft_average_destroy(h)
+            self._h = C.c_void_p()
+
+    def add(self, frame, scale: float = 1.0):
+        """one frame (h, w) or (h, w, cn)"""
+        a, h, w, cn = _hwc(frame)
+        self.add_batch(a.reshape(1, h, w, cn), scale)
+
+    def add_batch(self, frames, scale: float = 1.0):
+        """frames (n, h, w) or (n, h, w, cn)"""
+        f = np.ascontiguousarray(frames)
+        n, h, w = f.shape[:3]
+        cn = f.shape[3] if f.ndim == 4 else 1
+        _check(lib().sst_fft_average_add(self._h, _ptr(f), _NP_DEPTH[f.dtype], n, w, h, cn, f.strides[1],
+                                         f.strides[0], scale, 0, None), "sst_fft_average_add")
+        self._cn, self._shape = cn, (h, w)
+
+    def compute(self):
+        if not self.accumulated_frames():
+            raise SSTError("c_frame_accumulation_with_fft: accumulator is empty")
+        cn = self._cn
+        h, w = self._shape
+        avg = np.zeros((h, w, cn), np.float32)
+        mask = np.zeros((h, w), np.uint8)
+        _check(lib().sst_fft_average_compute(self._h, _ptr(avg), 0, _ptr(mask), 0, 0, None), "sst_fft_average_compute")
+        return (avg[..., 0] if cn == 1 else avg), mask
+
+    def fft_size(self):
+        fw, fh = C.c_int(), C.c_int()
+        _check(lib().sst_fft_average_size(self._h, C.byref(fw), C.byref(fh)), "sst_fft_average_size")
+        return fw.value, fh.value
+
+    def accumulated_frames(self) -> int:
+        return lib().sst_fft_average_accumulated_frames(self._h)
+
+    def clear(self):
+        _check(lib().sst_fft_average_clear(self._h), "clear")
+
+
+def fft_average(frames, scale: float = 1.0):
+    """c_frame_accumulation_with_fft over a batch: frames (n, h, w) or
+    (n, h, w, cn) -> (avg, mask)"""
+    acc = c_frame_accumulation_with_fft()
+    acc.add_batch(frames, scale)
+    return acc.compute()
+
+
+SELECT_MAX_ENERGY, WEIGHTED_AVERAGE = 0, 1
+
+
+class FocusStackOptions(C.Structure):
+    """c_laplacian_pyramid_focus_stacking::options (c_frame_accumulation.h:158-164)"""
+    _fields_ = [("fusing_policy", C.c_int32), ("inpaint_mask_holes", C.c_int32), ("avgchannel", C.c_int32),
+                ("kradius", C.c_int32), ("ksigma", C.c_double)]
+
+
+def focus_stack_options(**kw) -> FocusStackOptions:
+    o = FocusStackOptions()
+    lib().sst_focus_stack_options_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class c_laplacian_pyramid_focus_stacking:
+    """c_laplacian_pyramid_focus_stacking (c_frame_accumulation.h:149-191)
+    over the C ABI: frames (h, w) or (h, w, cn)."""
+
+    def __init__(self, options: Optional[FocusStackOptions] = None, **kw):
+        self.options = options if options is not None else focus_stack_options(**kw)
+        self._h = C.c_void_p()
+        _check(lib().sst_focus_stack_create(C.byref(self._h), C.byref(self.options)), "sst_focus_stack_create")
+        self._cn, self._shape = 1, None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_focus_stack_destroy(h)
+            self._h = C.c_void_p()
+
+    def add(self, frame, mask=None, scale: float = 1.0):
+        a, h, w, cn = _hwc(frame)
+        self.add_batch(a.reshape(1, h, w, cn), None if mask is None else np.asarray(mask)[None], scale)
+
+    def add_batch(self, frames, masks=None, scale: float = 1.0):
+        """frames (n, h, w) or (n, h, w, cn); masks (n, h, w) u8 or None"""
+        f = np.ascontiguousarray(frames)
+        n, h, w = f.shape[:3]
+        cn = f.shape[3] if f.ndim == 4 else 1
+        m = None if masks is None else np.ascontiguousarray(masks, np.uint8).reshape(n, h, w)
+        _check(lib().sst_focus_stack_add(self._h, _ptr(f), _NP_DEPTH[f.dtype], n, w, h, cn, f.strides[1], f.strides[0],
+                                         scale, _ptr(m), w, w * h, 0, None), "sst_focus_stack_add")
+        self._cn, self._shape = cn, (h, w)
+
+    def compute(self):
+        h, w = self._shape
+        avg = np.zeros((h, w, self._cn), np.float32)
+        _check(lib().sst_focus_stack_compute(self._h, _ptr(avg), 0, 0, None), "sst_focus_stack_compute")
+        return avg[..., 0] if self._cn == 1 else avg
+
+    def kernel(self):
+        n = C.c_int()
+        _check(lib().sst_focus_stack_kernel(self._h, None, C.byref(n)), "kernel")
+        k = np.zeros(n.value, np.float32)
+        if n.value:
+            _check(lib().sst_focus_stack_kernel(self._h, _ptr(k), C.byref(n)), "kernel")
+        return k
+
+    def accumulated_frames(self) -> int:
+        return lib().sst_focus_stack_accumulated_frames(self._h)
+
+    def clear(self):
+        _check(lib().sst_focus_stack_clear(self._h), "clear")
+
+
+def linear_interpolation_inpaint(image, mask):
+    """sst_linear_interpolation_inpaint: image (h, w) or (h, w, cn) f32, u8
+    mask (0 = hole) -> the filled image"""
+    a, h, w, cn = _hwc(np.asarray(image, np.float32))
+    a = a.copy()
+    m = np.ascontiguousarray(mask, np.uint8)
+    _check(lib().sst_linear_interpolation_inpaint(_ptr(a), a.strides[0], w, h, cn, _ptr(m), m.strides[0], 0, None),
+           "sst_linear_interpolation_inpaint")
+    return a
+
+
+class c_canvas_average:
+    """c_canvas_average (c_frame_accumulation.h:65-146) over the C ABI."""
+
+    def __init__(self, canvas_size=(0, 0)):
+        self._h = C.c_void_p()
+        _check(lib().sst_canvas_average_create(C.byref(self._h), int(canvas_size[0]), int(canvas_size[1])),
+               "sst_canvas_average_create")
+        self._cn = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.sst_canvas_average_destroy(h)
+            self._h = C.c_void_p()
+
+    def set_canvas_size(self, size):
+        _check(lib().sst_canvas_average_set_canvas_size(self._h, int(size[0]), int(size[1])), "set_canvas_size")
+
+    def add(self, image, weights=None, rmap=None, bbox=None, scale: float = 1.0):
+        """image (h, w[, cn]); weights None, u8 mask or f32 (h, w); rmap
+        (bh, bw, 2) f32 with bbox (x, y, bw, bh)"""
+        a, h, w, cn = _hwc(image)
+        self._cn = cn
+        wt = None if weights is None else np.ascontiguousarray(weights)
+        wd = 0 if wt is None else _NP_DEPTH[wt.dtype]
+        rm = None if rmap is None else np.ascontiguousarray(rmap, np.float32)
+        bb = None if bbox is None else np.ascontiguousarray(bbox, np.int32)
+        _check(lib().sst_canvas_average_add(self._h, _ptr(a), _NP_DEPTH[a.dtype], w, h, cn, a.strides[0], scale,
+                                            _ptr(wt), wd, 0 if wt is None else wt.strides[0], _ptr(rm), _ptr(bb), 0,
+                                            None), "sst_canvas_average_add")
+
+    def state(self):
+        cw, ch, fr = C.c_int(), C.c_int(), C.c_int()
+        bb = np.zeros(4, np.int32)
+        _check(lib().sst_canvas_average_state(self._h, C.byref(cw), C.byref(ch), _ptr(bb), C.byref(fr)), "state")
+        return (cw.value, ch.value), bb, fr.value
+
+    def compute(self, dscale: float = 1.0, rbbox=None):
+        (cw, ch), _, _ = self.state()
+        rb = None if rbbox is None else np.ascontiguousarray(rbbox, np.int32)
+        bw, bh = (cw, ch) if rb is None else (int(rb[2]), int(rb[3]))
+        bw, bh = min(bw, cw), min(bh, ch)
+        cn = self._cn or 1
+        avg = np.zeros((bh, bw, cn), np.float32)
+        mask = np.zeros((bh, bw), np.uint8)
+        ob = np.zeros(4, np.int32)
+        _check(lib().sst_canvas_average_compute(self._h, _ptr(avg), avg.strides[0], _ptr(mask), mask.strides[0], dscale,
+                                                _ptr(rb), _ptr(ob), 0, None), "sst_canvas_average_compute")
+        avg, mask = avg[:ob[3], :ob[2]], mask[:ob[3], :ob[2]]
+        return (avg[..., 0] if cn == 1 else avg), mask
+
+    def counter(self):
+        (cw, ch), _, _ = self.state()
+        W = np.zeros((ch, cw), np.float32)
+        _check(lib().sst_canvas_average_counter(self._h, _ptr(W), 0, 0, None), "counter")
+        return W
 
 
 class c_weigthed_average:

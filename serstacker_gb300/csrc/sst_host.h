@@ -33,6 +33,15 @@ struct DevBuf {
   template<class T> T * as() const { return (T *) p; }
 };
 
+/* a temporary device allocation released when it goes out of scope (cudaFree
+ * waits for the work that may still use it) */
+struct ScopedBuf : DevBuf {
+  ScopedBuf() = default;
+  ScopedBuf(const ScopedBuf &) = delete;
+  ScopedBuf & operator=(const ScopedBuf &) = delete;
+  ~ScopedBuf() { release(); }
+};
+
 inline int depth_bytes(int depth)
 {
   switch ( depth ) {

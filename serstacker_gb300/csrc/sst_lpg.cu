@@ -236,7 +236,7 @@ extern "C" int sst_lpg_compute(sst_lpg * L, const void * frames, int depth, int 
   const size_t plane = (size_t) width * height;
   SST_LCK(L->buf[0].ensure((size_t) n * plane * sizeof(float)));
   SST_LCK(L->buf[1].ensure((size_t) n * plane * sizeof(float)));
-  DevBuf tf;
+  ScopedBuf tf;
   const void * src = frames;
   if( !on_device ) {
     SST_LCK(tf.ensure(frame_stride * n));

@@ -261,3 +261,37 @@ def test_debayer_nn2_argument_checks(capi):
     assert lib.sst_debayer_nn2(1, capi.DEPTH_U16, 1, 9, 8, 18, 144, 8, 1, 0, 0, None) == -1    # odd width
     assert lib.sst_debayer_nn2(1, capi.DEPTH_U16, 1, 8, 8, 14, 128, 8, 1, 0, 0, None) == -1    # short rows
     assert lib.sst_debayer_nn2(1, 6, 1, 8, 8, 64, 512, 8, 1, 0, 0, None) == -1                 # f64
+
+
+def test_accumulator_host_checks(capi):
+    """defaults and argument checks of the FFT, canvas and focus-stacking
+    accumulators (no GPU work)"""
+    import ctypes as C
+    lib = capi.lib()
+    assert [lib.sst_optimal_dft_size(n) for n in (1, 7, 29, 960, 1021)] == [1, 8, 30, 960, 1024]
+    o = capi.focus_stack_options()
+    assert (o.fusing_policy, o.inpaint_mask_holes, o.avgchannel, o.kradius, o.ksigma) == (0, 1, 1, 0, 0.0)
+    h = C.c_void_p()
+    assert lib.sst_focus_stack_create(C.byref(h), C.byref(capi.focus_stack_options(fusing_policy=7))) == -1
+    assert lib.sst_focus_stack_create(C.byref(h), C.byref(capi.focus_stack_options(kradius=-1))) == -1
+    assert not h.value
+    buf = (C.c_float * 64)()
+    f = C.c_void_p()
+    assert lib.sst_fft_average_create(C.byref(f)) == 0
+    try:
+        assert lib.sst_fft_average_add(f, None, capi.DEPTH_F32, 1, 8, 8, 1, 32, 256, 1.0, 0, None) == -1
+        assert lib.sst_fft_average_add(f, buf, capi.DEPTH_F32, 1, 8, 8, 5, 160, 1280, 1.0, 0, None) == -1
+        assert lib.sst_fft_average_add(f, buf, capi.DEPTH_F32, 1, 8, 8, 1, 16, 256, 1.0, 0, None) == -1
+        assert lib.sst_fft_average_compute(f, buf, 0, None, 0, 0, None) == -4      # empty: SST_ERR_STATE
+    finally:
+        lib.sst_fft_average_destroy(f)
+    c = C.c_void_p()
+    assert lib.sst_canvas_average_create(C.byref(c), 0, 0) == 0
+    try:
+        assert lib.sst_canvas_average_add(c, buf, capi.DEPTH_F32, 8, 8, 1, 16, 1.0, None, 0, 0, None, None, 0,
+                                          None) == -1
+        assert lib.sst_canvas_average_add(c, buf, capi.DEPTH_F32, 8, 8, 1, 32, 1.0, buf, 2, 32, None, None, 0,
+                                          None) == -1    # u16 weights
+        assert lib.sst_canvas_average_compute(c, buf, 0, None, 0, 1.0, None, None, 0, None) == -4
+    finally:
+        lib.sst_canvas_average_destroy(c)

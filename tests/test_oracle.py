@@ -781,3 +781,95 @@ def test_debayer_nn2_known_answers(oracle):
         assert np.array_equal(a[dy + 1:dy + 9, dx + 1:dx + 13], b[1:9, 1:13]), cid
     fl = rng.random((6, 8)).astype(np.float32)
     assert np.array_equal(O.debayer_nn2(fl, 8)[..., 2][0::2, 0::2], fl[0::2, 0::2])
+
+
+def test_optimal_dft_size_known_answers(oracle):
+    O = oracle
+    for n, m in [(1, 1), (7, 8), (11, 12), (13, 15), (17, 18), (29, 30), (37, 40), (960, 960), (1021, 1024),
+                 (1280, 1280), (2049, 2160)]:
+        assert O.optimal_dft_size(n) == m, n
+
+
+def test_fft_average_known_answers(oracle):
+    """c_frame_accumulation_with_fft: one frame or identical frames give the
+    frame back; two constant frames c, d give (c^7 + d^7) / (c^6 + d^6), the
+    DC bins weighted by (|F|^2 / area^2)^3 = c^6 and d^6 (the other bins are
+    zero in both)"""
+    O = oracle
+    rng = np.random.default_rng(3)
+    f = rng.random((29, 37))
+    assert np.abs(O.fft_average(f[None]) - f).max() < 1e-10
+    assert np.abs(O.fft_average(np.stack([f, f, f])) - f).max() < 1e-10
+    c, d = 0.6, 0.9
+    frames = np.stack([np.full((30, 40), c), np.full((30, 40), d)])
+    want = (c ** 7 + d ** 7) / (c ** 6 + d ** 6)
+    assert np.abs(O.fft_average(frames) - want).max() < 1e-10
+    col = rng.random((2, 17, 23, 3))
+    out = O.fft_average(np.stack([col[0], col[0]]))
+    assert out.shape == (17, 23, 3) and np.abs(out - col[0]).max() < 1e-10
+
+
+def test_linear_inpaint_known_answers(oracle):
+    """linear_interpolation_inpaint: a run of holes between s and e takes
+    sv + (x - s) (ev - sv) / (run length) (the slope over the run length, as
+    the reference computes it), a single hole its right / lower neighbour;
+    both directions mix as (h dv + v dh) / (dh + dv)"""
+    O = oracle
+    row = np.array([[1.0, 0.0, 0.0, 4.0]])
+    out = O.linear_inpaint(row, np.array([[255, 0, 0, 255]], np.uint8))
+    assert np.allclose(out, [[1.0, 2.5, 4.0, 4.0]])
+    img = np.arange(9, dtype=np.float64).reshape(3, 3) ** 2
+    m = np.full((3, 3), 255, np.uint8)
+    m[1, 1] = 0
+    out = O.linear_inpaint(img, m)
+    assert out[1, 1] == pytest.approx((img[1, 2] + img[2, 1]) / 2)
+    # an all-hole row and column: filled in a second sweep from the first one's values
+    img = np.random.default_rng(1).random((6, 7))
+    m = np.full((6, 7), 255, np.uint8)
+    m[2, :] = 0
+    m[:, 3] = 0
+    out = O.linear_inpaint(img, m)
+    assert np.isfinite(out).all()
+    assert np.array_equal(out[m > 0], img[m > 0])
+
+
+def test_focus_stack_known_answers(oracle):
+    """c_laplacian_pyramid_focus_stacking: one frame, or identical frames,
+    reconstruct the frame (both fusing policies)"""
+    O = oracle
+    rng = np.random.default_rng(4)
+    f = rng.random((70, 90))
+    for policy in (0, 1):
+        assert np.abs(O.focus_stack(f[None], policy=policy) - f).max() < 1e-10
+        assert np.abs(O.focus_stack(np.stack([f, f, f]), policy=policy) - f).max() < 1e-10
+    c = rng.random((50, 66, 3))
+    for policy in (0, 1):
+        assert np.abs(O.focus_stack(np.stack([c, c]), policy=policy) - c).max() < 1e-10
+
+
+def test_canvas_average_known_answers(oracle):
+    """c_canvas_average: the first frame is centred on a 3/2-size canvas; a
+    frame without remap lands on the last box; an identity remap places the
+    frame at its box; a box within 32 px of the left edge shifts the canvas
+    contents 64 px right (when the shifted copy is not empty)"""
+    O = oracle
+    rng = np.random.default_rng(6)
+    n, h, w = 3, 40, 60
+    fr = rng.random((n, h, w))
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    rm = np.stack([xx, yy], axis=-1)
+    boxes = np.zeros((n, 4), np.int32)
+    boxes[2] = (20, 12, w, h)
+    acc, W, st, last = O.canvas_average(fr, boxes=boxes, rmaps=[None, None, rm])
+    assert acc.shape == (60, 90) and list(st) == [0, 0, 0] and list(last) == [20, 12, w, h]
+    # frames 0 and 1 at (15, 10); frame 2 at (20, 12): the 90 x 60 canvas is too
+    # small for the 64 px shift in y, so nothing moves
+    assert W[10, 15] == 2 and W[12, 20] == 3 and W[51, 79] == 1 and W.sum() == 3 * w * h
+    assert acc[10, 15] == pytest.approx((fr[0, 0, 0] + fr[1, 0, 0]) / 2)
+    assert acc[51, 79] == pytest.approx(fr[2, 39, 59])
+    assert acc[12, 20] == pytest.approx((fr[0, 2, 5] + fr[1, 2, 5] + fr[2, 0, 0]) / 3)
+    acc3, W3, st3, last3 = O.canvas_average(fr[:2], boxes=np.array([[0, 0, 0, 0], [10, 50, w, h]], np.int32),
+                                            rmaps=[None, rm], canvas=(300, 200))
+    assert acc3.shape == (200, 300) and list(st3) == [0, 0] and list(last3) == [74, 50, w, h]
+    assert np.all(W3[80:120, 184:244] == 1) and np.all(W3[50:90, 74:134] == 1) and W3.sum() == 2 * w * h
+    assert np.allclose(acc3[80:120, 184:244], fr[0]) and np.allclose(acc3[50:90, 74:134], fr[1])
