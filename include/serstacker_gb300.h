@@ -1020,9 +1020,11 @@ int sst_image_transform_create_remap(const sst_motion_model * model, const float
  * rejected with SST_ERR_INVALID_ARG.
  *
  * The call returns once its work on `stream` has finished: it clears a
- * device word before the launch and reads it back after it. If a bounded
- * wait of the stacking kernel for a staged tile copy gave up, the call
- * returns SST_ERR_TIMEOUT and acc_state is invalid (rebuild it).
+ * device error word before the launch and reads it back after it, and
+ * returns SST_ERR_TIMEOUT (acc_state invalid: rebuild it) if a stacking
+ * kernel raised it. The batched stacking kernels read the frames directly
+ * and hold no waits, so none raises it today; the word stays the kernels'
+ * error channel.
  *
  * The first call on each device looks up the device addresses of the
  * scratch array and of that word (cudaGetSymbolAddress) with that device

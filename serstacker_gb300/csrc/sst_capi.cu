@@ -1099,7 +1099,7 @@ struct sst_weighted_average {
   int w = 0, h = 0;
   DevBuf acc, coeffs, weff, src, wsrc;
   DevBuf part;                         // partial sums of the frame chunks of one batch
-  DevBuf err;                          // set on the device when a bounded tile-copy wait gave up
+  DevBuf err;                          // the stacking kernels' error flag (StackArgs::err)
   DevBuf focus_e, focus_w, gk_focus;   // focus weighting: energy maps, blurred maps, Gaussian taps
   int gk_n = 0;
   sst_local_variance * lv = nullptr;   // local-variance weighting (created on first use)
@@ -1283,7 +1283,7 @@ static int add_warped_device(sst_weighted_average * a, const void * d_frames, in
   return SST_OK;
 }
 
-/* reports (and clears) a tile-copy wait of the stacking kernels that gave up */
+/* reports (and clears) the stacking kernels' error flag */
 static int check_acc_wait_flag(sst_weighted_average * a, cudaStream_t st)
 {
   if( !a->err.p ) return SST_OK;
@@ -1292,7 +1292,7 @@ static int check_acc_wait_flag(sst_weighted_average * a, cudaStream_t st)
   SST_CK(cudaStreamSynchronize(st));
   if( !e ) return SST_OK;
   SST_CK(cudaMemsetAsync(a->err.p, 0, sizeof(int), st));
-  return set_error(SST_ERR_TIMEOUT, "a bounded wait for a staged tile copy gave up; the accumulator is invalid");
+  return set_error(SST_ERR_TIMEOUT, "a stacking kernel raised its error flag; the accumulator is invalid");
 }
 
 extern "C" int sst_weighted_average_add_warped_batch(sst_weighted_average * a, const void * frames, int depth, int n,

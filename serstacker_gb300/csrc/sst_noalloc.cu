@@ -17,10 +17,11 @@
  * calls whose work overlaps on the GPU (different streams, no ordering) race
  * on it and must not be issued. Each call writes the scratch entries of its
  * n frames before reading them, so nothing there has to start at zero. The
- * one word that must start at zero, the flag the stacking kernel raises when
- * a bounded wait for a staged tile copy gives up, is cleared on the stream
- * before each launch and read back after it: the call returns once its work
- * on the stream has finished, with SST_ERR_TIMEOUT if the flag was raised.
+ * one word that must start at zero, the stacking kernels' error flag
+ * (StackArgs::err), is cleared on the stream before each launch and read back
+ * after it: the call returns once its work on the stream has finished, with
+ * SST_ERR_TIMEOUT if the flag was raised. (The batched kernels read the
+ * frames directly and hold no bounded waits, so none raises it today.)
  */
 #include <mutex>
 
@@ -33,7 +34,7 @@ namespace {
 
 /* per frame: SST_NCOEF warp coefficients and one effective weight */
 static __device__ __align__(256) float g_noalloc_scratch[SST_NOALLOC_MAX_FRAMES * (SST_NCOEF + 1)];
-/* raised (set to 1) by the stacking kernel when a bounded tile-copy wait gives up */
+/* the stacking kernels' error flag (StackArgs::err), raised by setting it to 1 */
 static __device__ __align__(16) int g_noalloc_wait_flag;
 
 constexpr int kMaxDevices = 64;
@@ -126,7 +127,7 @@ extern "C" int sst_weighted_average_add_warped_batch_noalloc(const void * frames
   if( e != cudaSuccess ) return fail(SST_ERR_CUDA, cudaGetErrorString(e));
   if( raised ) {
     return fail(SST_ERR_TIMEOUT,
-        "a bounded wait for a staged tile copy gave up; acc_state is invalid and must be rebuilt");
+        "the stacking kernel raised its error flag; acc_state is invalid and must be rebuilt");
   }
   return SST_OK;
 }

@@ -13,8 +13,9 @@
  * Accumulator layout in HBM: four planar FP32 planes of width x height:
  * S (sum of w*I), cS (its Kahan-Babuska compensation), W (sum of w), cW.
  * The batched kernel assigns each output pixel to one thread, which warps
- * and accumulates every frame of the batch in registers (compensated) and
- * touches the accumulator planes once per batch: no atomics, deterministic.
+ * and accumulates the frames of its chunk (partial sums in registers,
+ * compensated sums in thread-private shared slots) and touches the
+ * accumulator planes once per batch: no atomics, deterministic.
  */
 #include <mutex>
 #include "sst_engine.cuh"
@@ -226,10 +227,6 @@ __global__ void __launch_bounds__(256) k_stack_add_warped(StackArgs a)
 
 /* ------------------------------------------- TMA-staged batched stack */
 
-/* source footprint box of one 64 x 16 output tile: TB_W x TB_H elements; its
- * x origin is a multiple of 16 bytes (the TMA rule for the innermost coordinate) */
-constexpr int TB_W = 80, TB_H = 24;
-
 /* Work item L of the batched stack grid: (tile, frame chunk). The tiles of
  * the outer ring come first (their frames often need the validity / border
  * path, so their CTAs run longest), then the inner tiles; the chunks of a tile
@@ -269,210 +266,125 @@ __global__ void k_stack_merge_chunks(float * acc, const float * part, size_t pla
   acc[i] = gS, acc[plane + i] = gcS, acc[2 * plane + i] = gW, acc[3 * plane + i] = gcW;
 }
 
-struct TilePlan {
-  int use;          // 1: the frame's tile footprint is staged by TMA (it fits the box)
-  int interior;     // 1: every pixel of the validity window is valid and every tap inside the frame
-  int bx0, by0;     // box origin in the frame
-  float w;          // frame weight
-};
-
-/* Plans frame f for this CTA's tile (warp 0) from values loaded a frame
- * earlier, so that the plan waits on no memory: coefficient l & 15 of the
- * frame in lane l (cl) and its weight. Lanes 0-3 test the corners of the
- * validity window (tile + 2 px halo, as rect_interior), lanes 4-7 the corners
- * of the tile for its source footprint (as rect_footprint). */
-template<int FAM, typename T>
-__device__ __forceinline__ void plan_frame(const StackArgs & a, float cl, float wf, int tx0, int ty0, int wx0,
-    int wy0, int wx1, int wy1, float * s_c, TilePlan * plan)
+/* Eroded validity of output pixel (x, y) for the projective family: the
+ * reference's mask is remap(255, LINEAR, BORDER_CONSTANT 0) >= 255 eroded
+ * 5 x 5 (window clipped to the output). The set of output positions whose
+ * sample has full in-image coverage is convex (the coverage wx(X) wy(Y) is
+ * log-concave in the source position, so its superlevel set is convex, and
+ * its preimage under a projective map with w > 0 is convex), so the window
+ * is valid exactly when its four corners are. */
+template<int FAM>
+__device__ __forceinline__ bool window_valid(const float * c, int x, int y, int dw, int dh, int sw, int sh)
 {
-  constexpr int XA = 16 / (int) sizeof(T);
-  const int lane = threadIdx.x & 31;
-  float c[SST_NCOEF];
-#pragma unroll
-  for( int i = 0; i < SST_NCOEF; ++i ) c[i] = __shfl_sync(0xffffffffu, cl, i);
-  if( lane < SST_NCOEF ) s_c[lane] = cl;
-  const int tx1 = min(tx0 + SA_TX, a.dw) - 1, ty1 = min(ty0 + SA_TY, a.dh) - 1;
-  float X = 0.f, Y = 0.f;
-  bool ok = true, fin = true;
-  if( FAM == FAM_QUAD ) ok = fin = false;
-  else if( lane < 8 ) {
-    const bool win = lane < 4;
-    const int x = (lane & 1) ? (win ? wx1 : tx1) : (win ? wx0 : tx0);
-    const int y = (lane & 2) ? (win ? wy1 : ty1) : (win ? wy0 : ty0);
-    float dx, dy;
-    warp_disp<FAM>(c, (float) x, (float) y, dx, dy);
-    X = (float) (x + (int) c[12]) + dx, Y = (float) (y + (int) c[13]) + dy;
-    ok = X >= 0.01f && X <= (float) (a.sw - 2) - 0.01f && Y >= 0.01f && Y <= (float) (a.sh - 2) - 0.01f;
-    fin = fabsf(X) < 1e6f && fabsf(Y) < 1e6f;
-    if( FAM == FAM_HOMOG ) {
-      const bool pos = (1.0f + fmaf(c[6], (float) x, c[7] * (float) y)) > 0.f;
-      ok = ok && pos, fin = fin && pos;
-    }
-  }
-  const unsigned okm = __ballot_sync(0xffffffffu, ok), finm = __ballot_sync(0xffffffffu, fin);
-  // interior: every window pixel valid, every tap inside; boxable: the tile's
-  // taps lie in the bounding box of its mapped corners (w > 0 on the tile)
-  const bool interior = (okm & 0xFu) == 0xFu, boxable = (finm & 0xF0u) == 0xF0u;
-  // footprint box of the tile: min / max over lanes 4-7
-  float mnx = X, mxx = X, mny = Y, mxy = Y;
-#pragma unroll
-  for( int m = 1; m < 4; m <<= 1 ) {
-    mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, m)), mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, m));
-    mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, m)), mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, m));
-  }
-  mnx = __shfl_sync(0xffffffffu, mnx, 4), mxx = __shfl_sync(0xffffffffu, mxx, 4);
-  mny = __shfl_sync(0xffffffffu, mny, 4), mxy = __shfl_sync(0xffffffffu, mxy, 4);
-  bool use = wf > 0.f && boxable;
-  int bx0 = 0, by0 = 0;
-  if( use ) {
-    bx0 = (int) floorf(mnx - 0.01f), by0 = (int) floorf(mny - 0.01f);
-    const int bx1 = (int) floorf(mxx + 0.01f) + 1, by1 = (int) floorf(mxy + 0.01f) + 1;
-    bx0 = bx0 >= 0 ? bx0 - bx0 % XA : -((-bx0 + XA - 1) / XA) * XA;   // round down to the alignment
-    use = bx1 < bx0 + TB_W && by1 < by0 + TB_H;
-  }
-  if( lane == 0 ) {
-    plan->use = use ? 1 : 0;
-    plan->interior = interior ? 1 : 0;
-    plan->bx0 = bx0, plan->by0 = by0;
-    plan->w = wf;
-  }
+  const int xa = max(x - 2, 0), xb = min(x + 2, dw - 1), ya = max(y - 2, 0), yb = min(y + 2, dh - 1);
+  return mask_ok(coverage(sw, sh, warp_pos<FAM>(c, xa, ya)), 255) &&
+      mask_ok(coverage(sw, sh, warp_pos<FAM>(c, xb, ya)), 255) &&
+      mask_ok(coverage(sw, sh, warp_pos<FAM>(c, xa, yb)), 255) &&
+      mask_ok(coverage(sw, sh, warp_pos<FAM>(c, xb, yb)), 255);
 }
 
-/* The batched stack with the source footprint of each (frame, tile) staged
- * in shared memory by one TMA copy, double-buffered: while the CTA warps and
- * accumulates frame f from shared memory, the copy of frame f + 1 is in
- * flight, and warp 0 has frame f + 2's coefficients in flight for the plan
- * after. Frames whose tile needs the validity / border logic, or whose
- * footprint does not fit the box, take the global-memory paths. */
-template<int FAM, typename T>
-__global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, const __grid_constant__ CUtensorMap tmap, int chunks)
+/* The batched stack for the affine and projective families, one output
+ * pixel column of SA_PPT consecutive rows per thread, every warp on its own:
+ * no shared memory and no barrier inside the frame loop. Each warp tests
+ * its own 5 x 5 window region (the rect_interior test: every window pixel
+ * valid, every tap inside the frame) for 8 frames at once, one corner and
+ * frame per lane; inside, its pixels sample the frame
+ * directly with positions stepped along the column and 32-bit element
+ * offsets; otherwise each pixel tests its window by its four corners
+ * (window_valid) and samples with the border mode. Partial sums of SA_FLUSH
+ * frames go into compensated sums; chunk > 0 writes its sums to the scratch
+ * planes for k_stack_merge_chunks. WMAP: per-pixel weight maps. */
+constexpr int SA_PPT = 4, SA_GRP = 4;
+
+template<int FAM, typename T, bool WMAP>
+__global__ void __launch_bounds__(256, 4) k_stack_add_streamed(StackArgs a, int chunks)
 {
-  constexpr int VW = SA_TX + 4, VH = SA_TY + 4;
-  constexpr int PPT = SA_TX * SA_TY / 256;
-  // three box buffers: frame f + 2's copy is issued while frame f computes;
-  // plans and coefficients rotate over four slots: frame f + 2 is planned while
-  // slower warps may still read frame f - 1's slot
-  __shared__ __align__(128) T s_box[3][TB_H * TB_W];
-  __shared__ __align__(8) uint64_t s_bar[3];
-  __shared__ __align__(16) float s_c[4][SST_NCOEF];
-  __shared__ TilePlan s_plan[4];
-  __shared__ uint32_t s_infl;             // copies in flight, kept by thread 0
-  __shared__ int s_gaveup[2];             // a wait gave up during a frame of this parity
-  __shared__ uint8_t s_v[VH * VW];
-  __shared__ uint8_t s_h[VH * SA_TX];
-  __shared__ uint8_t s_seg[VH * 4];       // window row segments with full coverage throughout
   int tile, chunk;
-  stack_item((int) blockIdx.x, (a.dw + SA_TX - 1) / SA_TX, (a.dh + SA_TY - 1) / SA_TY, chunks, tile, chunk);
   const int tiles_x = (a.dw + SA_TX - 1) / SA_TX;
+  stack_item((int) blockIdx.x, tiles_x, (a.dh + SA_TY - 1) / SA_TY, chunks, tile, chunk);
   const int tx0 = (tile % tiles_x) * SA_TX, ty0 = (tile / tiles_x) * SA_TY;
-  // this CTA's frames [f0, f0 + nf)
   const int f0 = (int) ((long long) chunk * a.n / chunks), nf = (int) ((long long) (chunk + 1) * a.n / chunks) - f0;
-  const int lx = threadIdx.x % SA_TX, ly0 = threadIdx.x / SA_TX;
+  const int lx = threadIdx.x % SA_TX, yb = ty0 + (threadIdx.x / SA_TX) * SA_PPT;
   const int x = tx0 + lx;
-  const int wx0 = max(tx0 - 2, 0), wy0 = max(ty0 - 2, 0);
-  const int wx1 = min(tx0 + SA_TX + 1, a.dw - 1), wy1 = min(ty0 + SA_TY + 1, a.dh - 1);
-  float S[PPT], cS[PPT], Wt[PPT], cW[PPT], pS[PPT], pW[PPT];
+  // this warp's pixels: 32 columns x SA_PPT rows; its 5 x 5 window region, clipped
+  const int xw = tx0 + (lx & ~31);
+  const int wx0 = max(xw - 2, 0), wx1 = min(xw + 33, a.dw - 1);
+  const int wy0 = max(yb - 2, 0), wy1 = min(yb + SA_PPT + 1, a.dh - 1);
+  const bool active = xw < a.dw && yb < a.dh;           // warp-uniform
+  const bool xin = x < a.dw;
+  const bool rows_in = yb + SA_PPT <= a.dh;             // warp-uniform: every row of the column exists
+  const int rse = (int) (a.row_stride / sizeof(T));     // row stride in elements
+  // compensated sums in thread-private shared slots [sum][pixel][thread]; partials in registers
+  __shared__ float s_acc[4][SA_PPT][256];
+  float pS[SA_PPT], pW[SA_PPT];
 #pragma unroll
-  for( int k = 0; k < PPT; ++k ) S[k] = cS[k] = Wt[k] = cW[k] = pS[k] = pW[k] = 0.f;
-  uint32_t phases = 0u;                          // bit b: parity of the next completion of s_bar[b]
-  bool timed_out = false;
-  if( threadIdx.x == 0 ) {
-    mbar_init(&s_bar[0], 1);
-    mbar_init(&s_bar[1], 1);
-    mbar_init(&s_bar[2], 1);
-    s_infl = 0u;
-    s_gaveup[0] = s_gaveup[1] = 0;
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  // warp 0: frame f + 2's lane coefficient and weight, loaded during frame f - 1
-  float cl2 = 0.f, w2 = 0.f;
-  if( threadIdx.x < 32 && nf > 0 ) {
-    const int lane = threadIdx.x & 15;
-    plan_frame<FAM, T>(a, __ldg(a.coeffs + (size_t) f0 * SST_NCOEF + lane), __ldg(a.weights + f0), tx0, ty0, wx0, wy0,
-        wx1, wy1, s_c[0], &s_plan[0]);
-    if( nf > 1 )
-      plan_frame<FAM, T>(a, __ldg(a.coeffs + (size_t) (f0 + 1) * SST_NCOEF + lane), __ldg(a.weights + f0 + 1), tx0, ty0,
-          wx0, wy0, wx1, wy1, s_c[1], &s_plan[1]);
-    if( nf > 2 ) cl2 = __ldg(a.coeffs + (size_t) (f0 + 2) * SST_NCOEF + lane), w2 = __ldg(a.weights + f0 + 2);
-  }
-  __syncthreads();
-  if( threadIdx.x == 0 ) {
-    for( int q = 0; q < 2 && q < nf; ++q ) {
-      if( !s_plan[q].use ) continue;
-      mbar_expect_tx(&s_bar[q], TB_W * TB_H * sizeof(T));
-      tma_load_3d(s_box[q], &tmap, s_plan[q].bx0, s_plan[q].by0, f0 + q, &s_bar[q]);
-      inflight_issued(&s_infl, q, 0u);
-    }
+  for( int k = 0; k < SA_PPT; ++k ) {
+    pS[k] = pW[k] = 0.f;
+    s_acc[0][k][threadIdx.x] = s_acc[1][k][threadIdx.x] = s_acc[2][k][threadIdx.x] = s_acc[3][k][threadIdx.x] = 0.f;
   }
   int since = 0;
-  bool stop = false;
-  for( int j = 0; j < nf; ++j ) {
+  const float fxc = (float) x, fyb = (float) yb;
+  const float sc = a.scale;
+  const int lane = threadIdx.x & 31;
+  unsigned inner8 = 0u;                           // rect_interior of the window region, 8 frames at a time
+  for( int j = 0; j < nf && active; ++j ) {
     const int f = f0 + j;
-    const int b = j % 3;                            // frame f's box buffer
-    const int slot = j & 3;                         // frame f's plan slot
-    // plan frame f + 2 (slot (j + 2) mod 4, last read during frame f - 2)
-    if( threadIdx.x < 32 && j + 2 < nf ) {
-      plan_frame<FAM, T>(a, cl2, w2, tx0, ty0, wx0, wy0, wx1, wy1, s_c[(j + 2) & 3], &s_plan[(j + 2) & 3]);
-      if( j + 3 < nf ) {
-        cl2 = __ldg(a.coeffs + (size_t) (f + 3) * SST_NCOEF + (threadIdx.x & 15));
-        w2 = __ldg(a.weights + f + 3);
+    if( (j & 7) == 0 ) {
+      // lane l tests corner l & 3 of the window region for frame f + (l >> 2)
+      const int fl = f + (lane >> 2);
+      bool ok = false;
+      if( fl < f0 + nf && FAM != FAM_QUAD ) {
+        const float4 * cq = (const float4 *) (a.coeffs + (size_t) fl * SST_NCOEF);
+        const float4 r0 = __ldg(cq), r1 = __ldg(cq + 1), r3 = __ldg(cq + 3);
+        float cc[SST_NCOEF];
+        cc[0] = r0.x, cc[1] = r0.y, cc[2] = r0.z, cc[3] = r0.w, cc[4] = r1.x, cc[5] = r1.y, cc[6] = r1.z, cc[7] = r1.w;
+        cc[8] = cc[9] = cc[10] = cc[11] = 0.f;
+        cc[12] = r3.x, cc[13] = r3.y, cc[14] = r3.z, cc[15] = r3.w;
+        const int qx = (lane & 1) ? wx1 : wx0, qy = (lane & 2) ? wy1 : wy0;
+        ok = point_interior<FAM>(cc, qx, qy, a.sw, a.sh);
       }
+      inner8 = __ballot_sync(0xffffffffu, ok);
     }
-    __syncthreads();
-    // once a wait gave up no further copy is issued or consumed; frame f - 1's flag
-    // is read after the barrier and written again no earlier than frame f + 1, so
-    // every thread sees the same value
-    stop = stop || s_gaveup[(j + 1) & 1];
-    if( threadIdx.x == 0 && j + 2 < nf && s_plan[(j + 2) & 3].use && !stop ) {
-      // frame f + 2's box goes into the buffer frame f - 1 used: every thread has
-      // finished frame f - 1 at the barrier above
-      const int nb = (j + 2) % 3;
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // order the generic reads of frame f - 1 before the copy
-      mbar_expect_tx(&s_bar[nb], TB_W * TB_H * sizeof(T));
-      tma_load_3d(s_box[nb], &tmap, s_plan[(j + 2) & 3].bx0, s_plan[(j + 2) & 3].by0, f + 2, &s_bar[nb]);
-      inflight_issued(&s_infl, nb, (phases >> nb) & 1u);
-    }
-    const TilePlan pl = s_plan[slot];
+    const bool inner = ((inner8 >> (4 * (j & 7))) & 0xFu) == 0xFu;
+    const float wf = __ldg(a.weights + f);
+    if( !(wf > 0.f) ) continue;                   // uniform over the CTA
+    const float4 * cp = (const float4 *) (a.coeffs + (size_t) f * SST_NCOEF);
+    const float4 q0 = __ldg(cp), q1 = __ldg(cp + 1), q3 = __ldg(cp + 3);
     float c[SST_NCOEF];
-#pragma unroll
-    for( int i = 0; i < SST_NCOEF; ++i ) c[i] = s_c[slot][i];
-    const float wf = pl.w;
-    if( !(wf > 0.f) ) continue;                     // uniform over the CTA
-    const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
-    const bool staged = pl.use && !stop;
-    if( staged ) {
-      if( !mbar_wait_bounded(&s_bar[b], (phases >> b) & 1u) ) timed_out = true, s_gaveup[j & 1] = 1;
-      else if( threadIdx.x == 0 ) inflight_landed(&s_infl, b);
-      phases ^= 1u << b;
-    }
-    if( staged && pl.interior ) {
-      if( x < a.dw ) {
-        const T * box = s_box[b];
-        // the column's displacements as functions of t = y - (ty0 + ly0) (rows 4k apart):
-        // affine d = e + c t; projective (the displacement form of warp_disp) numerators
-        // and denominator expanded in t. The integer offset of (x + Ix, y + Iy) from the
-        // box origin is added to the floor of the displacement.
-        const float fx = (float) x, fy0 = (float) (ty0 + ly0);
-        const int obase = (ty0 + ly0 + (int) c[13] - pl.by0) * TB_W + x + (int) c[12] - pl.bx0;
+    c[0] = q0.x, c[1] = q0.y, c[2] = q0.z, c[3] = q0.w, c[4] = q1.x, c[5] = q1.y, c[6] = q1.z, c[7] = q1.w;
+    c[8] = c[9] = c[10] = c[11] = 0.f;
+    c[12] = q3.x, c[13] = q3.y, c[14] = q3.z, c[15] = q3.w;
+    const T * fb = (const T *) (a.frames + (size_t) f * a.frame_stride);
+    if( inner ) {
+      if( xin ) {
+        // displacements along the column as functions of t = y - yb (as warp_disp)
+        const int Ix = (int) c[12], Iy = (int) c[13];
         float e0, e1, e2 = 0.f, e3 = 0.f, e4 = 0.f;
         if( FAM == FAM_AFFINE ) {
-          e0 = fmaf(c[0], fx, fmaf(c[1], fy0, c[2]));
-          e1 = fmaf(c[3], fx, fmaf(c[4], fy0, c[5]));
+          e0 = fmaf(c[0], fxc, fmaf(c[1], fyb, c[2]));
+          e1 = fmaf(c[3], fxc, fmaf(c[4], fyb, c[5]));
         }
         else {
-          const float X1 = fx + c[12], Y1 = fy0 + c[13];
-          const float q0 = fmaf(c[6], fx, c[7] * fy0);
-          e0 = 1.0f + q0;
-          e1 = fmaf(-q0, X1, fmaf(c[0], fx, fmaf(c[1], fy0, c[2])));
+          const float X1 = fxc + c[12], Y1 = fyb + c[13];
+          const float qq = fmaf(c[6], fxc, c[7] * fyb);
+          e0 = 1.0f + qq;
+          e1 = fmaf(-qq, X1, fmaf(c[0], fxc, fmaf(c[1], fyb, c[2])));
           e2 = fmaf(-c[7], X1, c[1]);
-          e3 = fmaf(-q0, Y1, fmaf(c[3], fx, fmaf(c[4], fy0, c[5])));
-          e4 = fmaf(-c[7], Y1, c[4] - q0);
+          e3 = fmaf(-qq, Y1, fmaf(c[3], fxc, fmaf(c[4], fyb, c[5])));
+          e4 = fmaf(-c[7], Y1, c[4] - qq);
         }
+        // element offset of (x + Ix, yb + Iy); rows past the output's last one
+        // sample its last row (inside the tested window)
+        const int obase = (yb + Iy) * rse + x + Ix;
+        const float wsc = wf * sc;
+        // SA_GRP pixels' taps in flight at a time
 #pragma unroll
-        for( int k = 0; k < PPT; ++k ) {
-          const int y = ty0 + ly0 + 4 * k;
-          if( y < a.dh ) {
-            const float t = (float) (4 * k);
+        for( int g = 0; g < SA_PPT; g += SA_GRP ) {
+          float v[SA_GRP][4], fx[SA_GRP], fy[SA_GRP];
+#pragma unroll
+          for( int q = 0; q < SA_GRP; ++q ) {
+            const int k = g + q;
+            const float t = (float) k;
             float dx, dy;
             if( FAM == FAM_AFFINE ) {
               dx = fmaf(c[1], t, e0);
@@ -483,135 +395,94 @@ __global__ void __launch_bounds__(256, 4) k_stack_add_warped_tma(StackArgs a, co
               dx = fmaf(e2, t, e1) * iw;
               dy = fmaf(t, fmaf(-c[7], t, e4), e3) * iw;
             }
-            const int ix = __float2int_rd(dx), iy = __float2int_rd(dy);
-            const float fxr = dx - (float) ix, fyr = dy - (float) iy;
-            // inside the box by construction (footprint test); the clamp only guards the array
-            const int o = (int) min((unsigned) (obase + 4 * k * TB_W + iy * TB_W + ix), (unsigned) (TB_W * TB_H - TB_W - 2));
-            const float v00 = (float) box[o], v01 = (float) box[o + 1];
-            const float v10 = (float) box[o + TB_W], v11 = (float) box[o + TB_W + 1];
-            const float t0 = fmaf(fxr, v01 - v00, v00), t1 = fmaf(fxr, v11 - v10, v10);
-            const float val = fmaf(fyr, t1 - t0, t0) * a.scale;
-            const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
-            pS[k] = fmaf(wp, val, pS[k]);
-            pW[k] += wp;
+            const float ix = floorf(dx), iy = floorf(dy);
+            fx[q] = dx - ix, fy[q] = dy - iy;
+            const int kk = rows_in ? k : min(yb + k, a.dh - 1) - yb;
+            const T * r0 = fb + (obase + (kk + (int) iy) * rse + (int) ix);
+            v[q][0] = (float) __ldg(r0), v[q][1] = (float) __ldg(r0 + 1);
+            v[q][2] = (float) __ldg(r0 + rse), v[q][3] = (float) __ldg(r0 + rse + 1);
+          }
+#pragma unroll
+          for( int q = 0; q < SA_GRP; ++q ) {
+            const int k = g + q;
+            if( rows_in || yb + k < a.dh ) {
+              const float t0 = fmaf(fx[q], v[q][1] - v[q][0], v[q][0]), t1 = fmaf(fx[q], v[q][3] - v[q][2], v[q][2]);
+              const float val = fmaf(fy[q], t1 - t0, t0);
+              if( WMAP ) {
+                const float wp = wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) (yb + k) * a.dw + x);
+                pS[k] = fmaf(wp, val * sc, pS[k]);
+                pW[k] += wp;
+              }
+              else {
+                pS[k] = fmaf(wsc, val, pS[k]);
+                pW[k] += wf;
+              }
+            }
           }
         }
       }
     }
-    else if( pl.interior ) {
-      if( x < a.dw ) {
+    else if( xin ) {
 #pragma unroll
-        for( int k = 0; k < PPT; ++k ) {
-          const int y = ty0 + ly0 + 4 * k;
-          if( y < a.dh ) {
-            const spos s = warp_pos<FAM>(c, x, y);
-            const T * r0 = (const T *) (fb + (size_t) s.y0 * a.row_stride) + s.x0;
-            const T * r1 = (const T *) ((const uint8_t *) r0 + a.row_stride);
-            const float v00 = (float) __ldg(r0), v01 = (float) __ldg(r0 + 1);
-            const float v10 = (float) __ldg(r1), v11 = (float) __ldg(r1 + 1);
-            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-            const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
-            const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
-            pS[k] = fmaf(wp, val, pS[k]);
-            pW[k] += wp;
+      for( int k = 0; k < SA_PPT; ++k ) {
+        const int y = yb + k;
+        if( y < a.dh && window_valid<FAM>(c, x, y, a.dw, a.dh, a.sw, a.sh) ) {
+          const spos s = warp_pos<FAM>(c, x, y);
+          float v00, v01, v10, v11;
+          if( s.x0 >= 0 && s.x0 < a.sw - 1 && s.y0 >= 0 && s.y0 < a.sh - 1 ) {
+            const T * r0 = fb + (s.y0 * rse + s.x0);
+            v00 = (float) __ldg(r0), v01 = (float) __ldg(r0 + 1), v10 = (float) __ldg(r0 + rse), v11 = (float) __ldg(r0 + rse + 1);
           }
-        }
-      }
-    }
-    else {
-      // validity of the window positions (tile + 2 px halo): each row in four
-      // segments; a segment whose end positions map strictly inside the frame
-      // (the rect_interior test: a projective map with w > 0 keeps a segment a
-      // segment) has full coverage throughout, the others are evaluated per position
-      if( threadIdx.x < VH * 4 ) {
-        const int r = threadIdx.x >> 2, sg = threadIdx.x & 3;
-        const int qy = ty0 - 2 + r;
-        bool all = true;
-        if( qy >= 0 && qy < a.dh ) {
-          const int qa = max(tx0 - 2 + sg * (VW / 4), 0), qb = min(tx0 - 2 + (sg + 1) * (VW / 4) - 1, a.dw - 1);
-          if( qa <= qb ) all = point_interior<FAM>(c, qa, qy, a.sw, a.sh) && point_interior<FAM>(c, qb, qy, a.sw, a.sh);
-        }
-        s_seg[threadIdx.x] = all ? 1 : 0;
-      }
-      __syncthreads();
-      for( int q = threadIdx.x; q < VW * VH; q += 256 ) {
-        const int r = q / VW, cc = q - r * VW;
-        const int qx = tx0 - 2 + cc, qy = ty0 - 2 + r;
-        uint8_t v = 1;
-        if( !s_seg[r * 4 + cc / (VW / 4)] && qx >= 0 && qx < a.dw && qy >= 0 && qy < a.dh ) {
-          v = mask_ok(coverage(a.sw, a.sh, warp_pos<FAM>(c, qx, qy)), 255) ? 1 : 0;
-        }
-        s_v[q] = v;
-      }
-      __syncthreads();
-      for( int q = threadIdx.x; q < SA_TX * VH; q += 256 ) {
-        const int xx = q % SA_TX, yy = q / SA_TX;
-        const uint8_t * p = s_v + yy * VW + xx;
-        s_h[yy * SA_TX + xx] = p[0] & p[1] & p[2] & p[3] & p[4];
-      }
-      __syncthreads();
-      if( x < a.dw ) {
-#pragma unroll
-        for( int k = 0; k < PPT; ++k ) {
-          const int ly = ly0 + 4 * k, y = ty0 + ly;
-          if( y >= a.dh ) continue;
-          const uint8_t * p = s_h + ly * SA_TX + lx;
-          if( p[0] & p[SA_TX] & p[2 * SA_TX] & p[3 * SA_TX] & p[4 * SA_TX] ) {
-            const spos s = warp_pos<FAM>(c, x, y);
-            float v00, v01, v10, v11;
-            if( staged && s.x0 >= 0 && s.x0 < a.sw - 1 && s.y0 >= 0 && s.y0 < a.sh - 1 ) {
-              // taps inside the frame: from the staged box (it holds every tap of the tile)
-              const T * box = s_box[b];
-              const int o = min(max((s.y0 - pl.by0) * TB_W + (s.x0 - pl.bx0), 0), TB_W * TB_H - TB_W - 2);
-              v00 = (float) box[o], v01 = (float) box[o + 1], v10 = (float) box[o + TB_W], v11 = (float) box[o + TB_W + 1];
-            }
-            else {
-              // < 0.2 % of the weight may fall outside: those taps take the border mode
-              v00 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
-              v01 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
-              v10 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
-              v11 = tap<T>(fb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
-            }
-            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
-            const float val = fmaf(s.fy, t1 - t0, t0) * a.scale;
-            const float wp = a.wmap ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
-            pS[k] = fmaf(wp, val, pS[k]);
-            pW[k] += wp;
+          else {
+            // < 0.2 % of the weight may fall outside: those taps take the image border mode
+            const uint8_t * fbb = (const uint8_t *) fb;
+            v00 = tap<T>(fbb, a.row_stride, a.sw, a.sh, s.x0, s.y0, a.border);
+            v01 = tap<T>(fbb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0, a.border);
+            v10 = tap<T>(fbb, a.row_stride, a.sw, a.sh, s.x0, s.y0 + 1, a.border);
+            v11 = tap<T>(fbb, a.row_stride, a.sw, a.sh, s.x0 + 1, s.y0 + 1, a.border);
           }
+          const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+          const float val = fmaf(s.fy, t1 - t0, t0) * sc;
+          const float wp = WMAP ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.dw + x) : wf;
+          pS[k] = fmaf(wp, val, pS[k]);
+          pW[k] += wp;
         }
       }
     }
     if( ++since == SA_FLUSH ) {
 #pragma unroll
-      for( int k = 0; k < PPT; ++k ) {
-        kahan_add(S[k], cS[k], pS[k]);
-        kahan_add(Wt[k], cW[k], pW[k]);
+      for( int k = 0; k < SA_PPT; ++k ) {
+        float S = s_acc[0][k][threadIdx.x], cS = s_acc[1][k][threadIdx.x];
+        float Wt = s_acc[2][k][threadIdx.x], cW = s_acc[3][k][threadIdx.x];
+        kahan_add(S, cS, pS[k]);
+        kahan_add(Wt, cW, pW[k]);
+        s_acc[0][k][threadIdx.x] = S, s_acc[1][k][threadIdx.x] = cS;
+        s_acc[2][k][threadIdx.x] = Wt, s_acc[3][k][threadIdx.x] = cW;
         pS[k] = pW[k] = 0.f;
       }
       since = 0;
     }
   }
-  if( threadIdx.x == 0 ) inflight_drain(&s_infl, s_bar, 3);
-  if( timed_out && a.err ) atomicExch(a.err, 1);
-  if( x < a.dw ) {
+  if( xin ) {
 #pragma unroll
-    for( int k = 0; k < PPT; ++k ) {
-      const int y = ty0 + ly0 + 4 * k;
+    for( int k = 0; k < SA_PPT; ++k ) {
+      const int y = yb + k;
       if( y >= a.dh ) continue;
-      kahan_add(S[k], cS[k], pS[k]);
-      kahan_add(Wt[k], cW[k], pW[k]);
+      float S = s_acc[0][k][threadIdx.x], cS = s_acc[1][k][threadIdx.x];
+      float Wt = s_acc[2][k][threadIdx.x], cW = s_acc[3][k][threadIdx.x];
+      kahan_add(S, cS, pS[k]);
+      kahan_add(Wt, cW, pW[k]);
       const size_t i = (size_t) y * a.dw + x;
       if( chunk > 0 ) {
-        // a later chunk's partial sums; merged in chunk order after the launch
         float * P = a.part + (size_t) (chunk - 1) * 4 * a.plane;
-        P[i] = S[k], P[a.plane + i] = cS[k], P[2 * a.plane + i] = Wt[k], P[3 * a.plane + i] = cW[k];
+        P[i] = S, P[a.plane + i] = cS, P[2 * a.plane + i] = Wt, P[3 * a.plane + i] = cW;
         continue;
       }
       float gS = a.acc[i], gcS = a.acc[a.plane + i], gW = a.acc[2 * a.plane + i], gcW = a.acc[3 * a.plane + i];
-      kahan_add(gS, gcS, S[k]);
-      gcS += cS[k];
-      kahan_add(gW, gcW, Wt[k]);
-      gcW += cW[k];
+      kahan_add(gS, gcS, S);
+      gcS += cS;
+      kahan_add(gW, gcW, Wt);
+      gcW += cW;
       a.acc[i] = gS, a.acc[a.plane + i] = gcS, a.acc[2 * a.plane + i] = gW, a.acc[3 * a.plane + i] = gcW;
     }
   }
@@ -652,31 +523,12 @@ bool encode_tensor_3d(CUtensorMap * map, CUtensorMapDataType dt, int esz, const 
       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-/* The frames of a batch as a 3-D tensor (x, y, frame) with the footprint box;
- * false when the layout does not meet the TMA rules (16-byte aligned base and
- * strides) or the encoder is unavailable */
-static bool encode_frames(const StackArgs & a, int depth, CUtensorMap * map)
-{
-  CUtensorMapDataType dt;
-  int esz;
-  switch ( depth ) {
-  case SST_DEPTH_U8: dt = CU_TENSOR_MAP_DATA_TYPE_UINT8, esz = 1; break;
-  case SST_DEPTH_U16: dt = CU_TENSOR_MAP_DATA_TYPE_UINT16, esz = 2; break;
-  case SST_DEPTH_F32: dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32, esz = 4; break;
-  default: return false;
-  }
-  const uint64_t dims[3] = { (uint64_t) a.sw, (uint64_t) a.sh, (uint64_t) a.n };
-  const uint64_t strides[2] = { (uint64_t) a.row_stride, (uint64_t) a.frame_stride };
-  const uint32_t box[3] = { (uint32_t) TB_W, (uint32_t) TB_H, 1 };
-  return encode_tensor_3d(map, dt, esz, a.frames, dims, strides, box);
-}
-
 cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, cudaStream_t st)
 {
   dim3 grid((a.dw + SA_TX - 1) / SA_TX, (a.dh + SA_TY - 1) / SA_TY);
   const int fam = motion_family(motion);
-  CUtensorMap map;
-  if( fam != FAM_QUAD && a.n > 0 && encode_frames(a, depth, &map) ) {
+  const size_t esz = depth == SST_DEPTH_U8 ? 1 : depth == SST_DEPTH_U16 ? 2 : 4;
+  if( fam != FAM_QUAD && a.n > 0 && a.row_stride % esz == 0 && a.row_stride / esz * (size_t) (a.sh + 1) < (1u << 31) ) {
     // frame chunks: enough (tile, chunk) CTAs for about items_per_slot per
     // resident slot, at least 32 frames per chunk, within the caller's scratch
     static int slots = 0;
@@ -684,7 +536,7 @@ cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, 
       int dev = 0, sms = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      slots = 4 * (sms > 0 ? sms : 1);
+      slots = 4 * (sms > 0 ? sms : 1);   // k_stack_add_streamed: 4 CTAs per SM
     }
     const int tiles = (int) (grid.x * grid.y);
     int chunks = 1;
@@ -695,11 +547,19 @@ cudaError_t launch_stack_add_warped(const StackArgs & a, int motion, int depth, 
       chunks = chunks > 1 ? chunks : 1;
     }
     const unsigned items = (unsigned) tiles * (unsigned) chunks;
-#define SST_LAUNCH_TMA(FAMV, TV) k_stack_add_warped_tma<FAMV, TV><<<items, 256, 0, st>>>(a, map, chunks)
+#define SST_LAUNCH_TMA(FAMV, TV)                                                         \
+    if( a.wmap ) k_stack_add_streamed<FAMV, TV, true><<<items, 256, 0, st>>>(a, chunks);  \
+    else k_stack_add_streamed<FAMV, TV, false><<<items, 256, 0, st>>>(a, chunks)
     switch ( depth ) {
-    case SST_DEPTH_U8: if( fam == FAM_AFFINE ) SST_LAUNCH_TMA(FAM_AFFINE, uint8_t); else SST_LAUNCH_TMA(FAM_HOMOG, uint8_t); break;
-    case SST_DEPTH_U16: if( fam == FAM_AFFINE ) SST_LAUNCH_TMA(FAM_AFFINE, uint16_t); else SST_LAUNCH_TMA(FAM_HOMOG, uint16_t); break;
-    default: if( fam == FAM_AFFINE ) SST_LAUNCH_TMA(FAM_AFFINE, float); else SST_LAUNCH_TMA(FAM_HOMOG, float); break;
+    case SST_DEPTH_U8:
+      if( fam == FAM_AFFINE ) { SST_LAUNCH_TMA(FAM_AFFINE, uint8_t); } else { SST_LAUNCH_TMA(FAM_HOMOG, uint8_t); }
+      break;
+    case SST_DEPTH_U16:
+      if( fam == FAM_AFFINE ) { SST_LAUNCH_TMA(FAM_AFFINE, uint16_t); } else { SST_LAUNCH_TMA(FAM_HOMOG, uint16_t); }
+      break;
+    default:
+      if( fam == FAM_AFFINE ) { SST_LAUNCH_TMA(FAM_AFFINE, float); } else { SST_LAUNCH_TMA(FAM_HOMOG, float); }
+      break;
     }
 #undef SST_LAUNCH_TMA
     cudaError_t e = cudaGetLastError();

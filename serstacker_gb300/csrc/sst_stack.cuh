@@ -21,7 +21,7 @@ struct StackArgs {
   size_t plane;             // floats per plane
   int border;               // image border mode of the remap (SST_BORDER_*)
   const float * wmap = nullptr;   // optional per-pixel weight maps (n x plane, output grid)
-  int * err = nullptr;            // optional: set to 1 when a bounded wait for a tile copy gave up
+  int * err = nullptr;            // optional error flag (set to 1 on a kernel-side failure; no kernel waits today)
   // optional scratch for frame chunks: (max_chunks - 1) x 4 planes of partial
   // sums, so that one tile's frames can be split over several CTAs
   float * part = nullptr;

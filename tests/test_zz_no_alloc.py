@@ -5,8 +5,9 @@ the library call cudaMalloc (a host whose own pool owns all device memory, a
 real-time loop that cannot take cudaMalloc's device-wide synchronisation): it
 runs the same warp + weight + compensated accumulate kernels with its
 per-frame scratch in a fixed device array and the accumulator planes owned by
-the caller, and returns SST_OK only when no bounded tile-copy wait gave up. This test feeds both entry points the
-same device-resident frames, parameters and weights, twice in a row, and
+the caller, and returns SST_OK only when the kernels' error flag stayed
+clear. This test feeds both entry points the same device-resident frames,
+parameters and weights, twice in a row, and
 checks the caller-owned planes against the object's planes after each call.
 It is collected last so a stop-at-first-failure run has run every other test.
 """
