@@ -278,8 +278,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--frames", type=int, default=2000)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--chunk", type=int, default=512,
-                    help="frames per streamed chunk in the e2e leg (a quarter of it for the raw Bayer frames)")
+    ap.add_argument("--chunk", type=int, default=1280,
+                    help="largest streamed chunk of the e2e leg (chunks grow from a quarter of it; "
+                         "a quarter of it for the raw Bayer frames)")
     ap.add_argument("--ref-sample", type=int, default=128, help="frames per step of the --impl reference arm")
     ap.add_argument("--cpu-sample", type=int, default=1024,
                     help="frames of the cpu_baseline sample (the FP32 CPU restatement on all host cores)")

@@ -516,7 +516,9 @@ int sst_linear_interpolation_inpaint(float * image, size_t row_stride, int width
  * (c_image_stacking_pipeline.cc:1653-1658, 1704-1713); kradius <= 0 disables
  * the maps (weight 1), as weights_required does. Host frames are streamed to the
  * device in chunks whose copies overlap the registration of the previous
- * chunk. Outputs follow `on_device` and may be NULL. */
+ * chunk; the chunks grow x 2.5 from a quarter of the chunk size set by
+ * sst_set_chunk_frames up to it (the first copy is the only one that cannot
+ * overlap). Outputs follow `on_device` and may be NULL. */
 int sst_stack_frames(sst_ecch * reg, sst_weighted_average * acc, const void * frames, int depth, int n,
     int width, int height, size_t row_stride, size_t frame_stride, double scale, int on_device,
     int num_passes, const sst_motion_model * passes, int border, int weighting,
@@ -538,8 +540,11 @@ int sst_stack_bayer_frames(sst_ecch * reg, sst_weighted_average * const * acc, c
     int num_passes, const sst_motion_model * passes, int border, int weighting,
     float * params_out, int32_t * status_out, float * rho_out, float * weight_out, void * stream);
 
-/* Frames per chunk used by sst_stack_frames (default 512): each chunk's host-to-device
- * copy overlaps the previous chunk's registration and stacking. */
+/* Largest chunk of frames used by sst_stack_frames (default 512): device
+ * frames are processed in chunks of this size; host frames in chunks growing
+ * from a quarter of it, each chunk's host-to-device copy overlapping the
+ * previous chunk's registration and stacking (two staging buffers of this
+ * many frames). */
 int sst_set_chunk_frames(sst_ecch * h, int frames);
 
 /* Level iterations as CUDA graph WHILE loops (enable = 1, the default): each

@@ -1427,6 +1427,36 @@ extern "C" int sst_weighted_average_load_state(sst_weighted_average * a, const f
 
 /* ================================================ streamed pipeline */
 
+/* Frames per chunk of a streamed sequence (sst_stack_frames and its Bayer
+ * form). Device frames: chunks of `chunk` frames. Host frames: the copy of
+ * the first chunk cannot overlap anything, and every chunk pays the
+ * registration's convergence tail once, so the chunks grow geometrically
+ * (x 2.5, a frame's registration takes about 2.5 times its copy) from a
+ * quarter of `chunk` up to `chunk`; a remainder is absorbed into the chunk
+ * before it when that stays within `chunk`. */
+static std::vector<int> chunk_plan(int n, int chunk, bool host)
+{
+  std::vector<int> sizes;
+  if( !host ) {
+    for( int f0 = 0; f0 < n; f0 += chunk ) sizes.push_back(std::min(chunk, n - f0));
+    return sizes;
+  }
+  int first = std::min(chunk, std::max(64, chunk / 4));
+  if( n <= first ) return { n };
+  sizes.push_back(first);
+  int rem = n - first;
+  while ( rem > 0 ) {
+    const int nxt = (int) std::min<long long>(chunk, ((long long) sizes.back() * 5 + 1) / 2);
+    int take;
+    if( rem <= nxt ) take = rem;
+    else if( rem <= chunk && rem - nxt < sizes.back() / 2 ) take = rem;
+    else take = nxt;
+    sizes.push_back(take);
+    rem -= take;
+  }
+  return sizes;
+}
+
 extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const void * frames, int depth, int n,
     int width, int height, size_t row_stride, size_t frame_stride, double scale, int on_device,
     int num_passes, const sst_motion_model * passes, int border, int weighting,
@@ -1465,9 +1495,8 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
   SST_CK(h->res_status.ensure((size_t) n * sizeof(int32_t)));
   SST_CK(h->res_rho.ensure((size_t) n * sizeof(float)));
   SST_CK(h->res_weight.ensure((size_t) n * sizeof(float)));
-  int buf = 0;
-  for( int f0 = 0; f0 < n; f0 += chunk, buf ^= 1 ) {
-    const int nc = std::min(chunk, n - f0);
+  int buf = 0, f0 = 0;
+  for( const int nc : chunk_plan(n, chunk, !on_device) ) {
     const uint8_t * fsrc = (const uint8_t *) frames + (size_t) f0 * frame_stride;
     const void * d_frames = fsrc;
     if( !on_device ) {
@@ -1487,6 +1516,7 @@ extern "C" int sst_stack_frames(sst_ecch * h, sst_weighted_average * acc, const 
     SST_TRY(copy_out(h->res_status.as<int32_t>() + f0, h->out_status.p, (size_t) nc * sizeof(int32_t), 1, st));
     SST_TRY(copy_out(h->res_rho.as<float>() + f0, h->out_rho.p, (size_t) nc * sizeof(float), 1, st));
     SST_TRY(copy_out(h->res_weight.as<float>() + f0, h->out_weight.p, (size_t) nc * sizeof(float), 1, st));
+    f0 += nc, buf ^= 1;
   }
   SST_TRY(copy_out(params_out, h->res_params.p, (size_t) n * 12 * sizeof(float), on_device, st));
   SST_TRY(copy_out(status_out, h->res_status.p, (size_t) n * sizeof(int32_t), on_device, st));
@@ -1557,9 +1587,8 @@ extern "C" int sst_stack_bayer_frames(sst_ecch * h, sst_weighted_average * const
   sst_weighted_average * a0 = acc[0];
   SST_CK(a0->coeffs.ensure((size_t) chunk * SST_NCOEF * sizeof(float)));
   SST_CK(a0->weff.ensure((size_t) chunk * sizeof(float)));
-  int buf = 0;
-  for( int f0 = 0; f0 < n; f0 += chunk, buf ^= 1 ) {
-    const int nc = std::min(chunk, n - f0);
+  int buf = 0, f0 = 0;
+  for( const int nc : chunk_plan(n, chunk, !on_device) ) {
     const uint8_t * fsrc = (const uint8_t *) frames + (size_t) f0 * frame_stride;
     const void * d_frames = fsrc;
     if( !on_device ) {
@@ -1604,6 +1633,7 @@ extern "C" int sst_stack_bayer_frames(sst_ecch * h, sst_weighted_average * const
     SST_TRY(copy_out(h->res_status.as<int32_t>() + f0, h->out_status.p, (size_t) nc * sizeof(int32_t), 1, st));
     SST_TRY(copy_out(h->res_rho.as<float>() + f0, h->out_rho.p, (size_t) nc * sizeof(float), 1, st));
     SST_TRY(copy_out(h->res_weight.as<float>() + f0, h->out_weight.p, (size_t) nc * sizeof(float), 1, st));
+    f0 += nc, buf ^= 1;
   }
   SST_TRY(copy_out(params_out, h->res_params.p, (size_t) n * 12 * sizeof(float), on_device, st));
   SST_TRY(copy_out(status_out, h->res_status.p, (size_t) n * sizeof(int32_t), on_device, st));
