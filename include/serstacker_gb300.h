@@ -355,6 +355,21 @@ int sst_calibrate_frames(const void * frames, int depth, int n, int width, int h
 int sst_debayer_nn2(const void * frames, int depth, int n, int width, int height, size_t row_stride,
     size_t frame_stride, int colorid, void * dst, size_t dst_row_stride, size_t dst_frame_stride, void * stream);
 
+/* read_input_frame's bad-pixel filter (c_image_stacking_pipeline_base.cc:
+ * 200-216, input_options.filter_bad_pixels with bad_pixels_variation_threshold
+ * k): Bayer frames (colorid 8..11, even sizes) take bayer_denoise
+ * (core/io/debayer.cc:1480-1612): per Bayer plane (the 2 x 2 cell positions)
+ * the 3 x 3 median (BORDER_REPLICATE) and mad = |p - median|, mad's
+ * normalized 3 x 3 box mean (BORDER_REFLECT_101, rounded for integer
+ * frames), and p -> median where |median - p| > k mad + minvar (1 for
+ * integer frames, 1/256 for f32). Other frames take median_filter_bad_pixels
+ * (core/proc/bad_pixels.cc:14-70), the same with 5 x 5 windows on the whole
+ * frame. n device frames (u8, u16, f32, one channel) into n device frames;
+ * dst may equal frames (strides in bytes, 0: packed). */
+int sst_filter_bad_pixels(const void * frames, int depth, int n, int width, int height, size_t row_stride,
+    size_t frame_stride, int colorid, double variation_threshold, void * dst, size_t dst_row_stride,
+    size_t dst_frame_stride, void * stream);
+
 /* ------------------------------------------------------ post-stack steps */
 
 /* average_pyramid_inpaint (core/proc/inpaint/average_pyramid_inpaint.cc:

@@ -134,6 +134,8 @@ def lib():
             "orc_debayer_nn2_f32": (i, [p, i, i, i, p]),
             "orc_optimal_dft_size": (i, [i]),
             "orc_linear_inpaint": (None, [p, p, i, i, i]),
+            "orc_filter_bad_pixels_u16": (i, [p, i, i, i, d, p]),
+            "orc_filter_bad_pixels_f32": (i, [p, i, i, i, d, p]),
             "orc_fft_average": (i, [p, i, i, i, i, p]),
             "orc_focus_stack": (i, [p, p, i, i, i, i, i, i, i, p, i, p]),
             "orc_canvas_average": (i, [p, i, i, i, i, i, p, p, p, p, p, p, p, p]),
@@ -869,3 +871,21 @@ def linear_inpaint(image, mask):
     m = np.ascontiguousarray(mask, np.uint8)
     lib().orc_linear_inpaint(_ptr(a), _ptr(m), w, h, cn)
     return a[..., 0] if np.ndim(image) == 2 else a
+
+
+def filter_bad_pixels(frame, colorid=0, threshold=3.0):
+    """read_input_frame's bad-pixel filter (median_filter_bad_pixels,
+    core/proc/bad_pixels.cc:14-70, or bayer_denoise, core/io/debayer.cc:
+    1480-1612, for colorid 8..11) of one u16 or f32 frame"""
+    a = np.ascontiguousarray(frame)
+    h, w = a.shape
+    out = np.empty_like(a)
+    if a.dtype == np.uint16:
+        r = lib().orc_filter_bad_pixels_u16(_ptr(a), w, h, colorid, threshold, _ptr(out))
+    else:
+        a = np.ascontiguousarray(a, np.float32)
+        out = np.empty_like(a)
+        r = lib().orc_filter_bad_pixels_f32(_ptr(a), w, h, colorid, threshold, _ptr(out))
+    if r != 0:
+        raise ValueError("filter_bad_pixels: odd size for a Bayer frame")
+    return out

@@ -265,6 +265,8 @@ int orc_debayer_nn2_f32(const float * src, int w, int h, int colorid, float * ds
 /* other accumulators (sst_oracle_accum.cc) */
 int orc_optimal_dft_size(int n);
 void orc_linear_inpaint(double * image, const uint8_t * mask, int w, int h, int cn);
+int orc_filter_bad_pixels_u16(const uint16_t * src, int w, int h, int colorid, double threshold, uint16_t * dst);
+int orc_filter_bad_pixels_f32(const float * src, int w, int h, int colorid, double threshold, float * dst);
 int orc_fft_average(const double * frames, int n, int w, int h, int cn, double * avg);
 int orc_focus_stack(const double * frames, const uint8_t * masks, int n, int w, int h, int cn, int policy,
     int inpaint, int avgchannel, const double * G, int gk, double * avg);

@@ -591,3 +591,70 @@ extern "C" void orc_linear_inpaint(double * image, const uint8_t * mask, int w, 
   linear_inpaint(m, mask);
   to_hwc(m, image);
 }
+
+namespace {
+
+/* median_filter_bad_pixels / bayer_denoise on one plane view: the plane pixel
+ * (x, y) is frame pixel (step x + ox, step y + oy) */
+template<class T>
+void bad_pixels_plane(const T * src, T * dst, int w, int step, int ox, int oy, int pw, int ph, int ks, float k,
+    float mv, bool integral)
+{
+  const int r = ks / 2;
+  auto at = [&](int x, int y) -> float { return (float) src[(size_t) (step * y + oy) * w + step * x + ox]; };
+  std::vector<float> med((size_t) pw * ph), mad((size_t) pw * ph);
+  std::vector<float> win(ks * ks);
+  for( int y = 0; y < ph; ++y ) {
+    for( int x = 0; x < pw; ++x ) {
+      for( int j = 0; j < ks; ++j )
+        for( int i = 0; i < ks; ++i )
+          win[j * ks + i] = at(std::min(std::max(x + i - r, 0), pw - 1), std::min(std::max(y + j - r, 0), ph - 1));
+      std::nth_element(win.begin(), win.begin() + ks * ks / 2, win.end());
+      const float m = win[ks * ks / 2];
+      med[(size_t) y * pw + x] = m;
+      mad[(size_t) y * pw + x] = std::fabs(at(x, y) - m);
+    }
+  }
+  for( int y = 0; y < ph; ++y ) {
+    for( int x = 0; x < pw; ++x ) {
+      double s = 0;
+      for( int j = 0; j < ks; ++j )
+        for( int i = 0; i < ks; ++i ) s += mad[(size_t) reflect101_idx(y + j - r, ph) * pw + reflect101_idx(x + i - r, pw)];
+      const float q = integral ? (float) (((long long) s + ks * ks / 2) / (ks * ks)) : (float) (s * (1.0 / (ks * ks)));
+      const float p = at(x, y), m = med[(size_t) y * pw + x];
+      const float t = (float) ((double) k * q);
+      const float thr = (float) ((double) t + mv);
+      dst[(size_t) (step * y + oy) * w + step * x + ox] = (T) (std::fabs(m - p) > thr ? m : p);
+    }
+  }
+}
+
+template<class T>
+int filter_bad_pixels(const T * src, int w, int h, int colorid, double threshold, T * dst, bool integral)
+{
+  const bool bayer = colorid >= 8 && colorid <= 11;
+  if( bayer && ((w & 1) || (h & 1)) ) return -1;
+  memcpy(dst, src, (size_t) w * h * sizeof(T));
+  const float k = (float) threshold, mv = integral ? 1.f : 1.f / 256.f;
+  if( bayer ) {
+    for( int p = 0; p < 4; ++p ) bad_pixels_plane<T>(src, dst, w, 2, p & 1, p >> 1, w / 2, h / 2, 3, k, mv, integral);
+  }
+  else bad_pixels_plane<T>(src, dst, w, 1, 0, 0, w, h, 5, k, mv, integral);
+  return 0;
+}
+
+}  // namespace
+
+/* read_input_frame's bad-pixel filter (median_filter_bad_pixels,
+ * core/proc/bad_pixels.cc:14-70; bayer_denoise, core/io/debayer.cc:1480-1612)
+ * of one u16 or f32 frame; exact for u16 */
+extern "C" int orc_filter_bad_pixels_u16(const uint16_t * src, int w, int h, int colorid, double threshold,
+    uint16_t * dst)
+{
+  return filter_bad_pixels<uint16_t>(src, w, h, colorid, threshold, dst, true);
+}
+
+extern "C" int orc_filter_bad_pixels_f32(const float * src, int w, int h, int colorid, double threshold, float * dst)
+{
+  return filter_bad_pixels<float>(src, w, h, colorid, threshold, dst, false);
+}

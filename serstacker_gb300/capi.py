@@ -195,6 +195,7 @@ def lib():
             "sst_average_pyramid_inpaint": (i, [p, sz, p, sz, i, i, i, p, sz, p, sz, i, p]),
             "sst_calibrate_frames": (i, [p, i, i, i, i, sz, sz, d, p, sz, p, sz, p, sz, sz, p]),
             "sst_debayer_nn2": (i, [p, i, i, i, i, sz, sz, i, p, sz, sz, p]),
+            "sst_filter_bad_pixels": (i, [p, i, i, i, i, sz, sz, i, d, p, sz, sz, p]),
             "sst_lpg_options_default": (None, [p]),
             "sst_optimal_dft_size": (i, [i]),
             "sst_focus_stack_options_default": (None, [p]),
@@ -1172,6 +1173,26 @@ def debayer_nn2(raw, colorid: int):
                                  colorid, out.data_ptr(), 0, 0, None), "sst_debayer_nn2")
     res = out.cpu().numpy()
     return res.view(np.uint16) if r.dtype == np.uint16 else res
+
+
+def filter_bad_pixels(frames, colorid: int = 0, threshold: float = 3.0):
+    """sst_filter_bad_pixels: frames (n, h, w) or (h, w) numpy u8 / u16 / f32
+    (colorid 8..11: Bayer mosaics) -> filtered frames of the same dtype
+    (through device buffers)"""
+    import torch
+    r = np.ascontiguousarray(frames)
+    single = r.ndim == 2
+    if single:
+        r = r[None]
+    n, h, w = r.shape
+    dev = torch.from_numpy(r.view(np.int16) if r.dtype == np.uint16 else r).cuda()
+    out = torch.empty_like(dev)
+    _check(lib().sst_filter_bad_pixels(dev.data_ptr(), _NP_DEPTH[r.dtype], n, w, h, w * r.itemsize,
+                                       w * h * r.itemsize, colorid, threshold, out.data_ptr(), 0, 0, None),
+           "sst_filter_bad_pixels")
+    res = out.cpu().numpy()
+    res = res.view(np.uint16) if r.dtype == np.uint16 else res
+    return res[0] if single else res
 
 
 def average_pyramid_inpaint(image: np.ndarray, mask: np.ndarray, max_levels: int = 100):

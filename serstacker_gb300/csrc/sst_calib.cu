@@ -13,7 +13,10 @@
  *
  * Also read_input_frame's DEBAYER_NN2 demosaic of raw Bayer frames
  * (c_image_stacking_pipeline_base.cc:220-235, nninterpolation in
- * core/debayer.cc:828-1161) into BGR frames, one thread per pixel.
+ * core/debayer.cc:828-1161) into BGR frames, one thread per pixel, and its
+ * bad-pixel filter (:200-216): per (Bayer plane) pixel a KS x KS median by a
+ * register bitonic network and its absolute deviation, then the box mean of
+ * the deviations decides whether the median replaces the pixel.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -106,6 +109,107 @@ __global__ void __launch_bounds__(128) k_debayer_nn2(const uint8_t * frames, int
   }
   T * d = (T *) (dst + (size_t) blockIdx.z * dfs + (size_t) y * drs) + (size_t) x * 3;
   d[0] = out[0], d[1] = out[1], d[2] = out[2];
+}
+
+/* --- bad pixels: median_filter_bad_pixels (core/proc/bad_pixels.cc:14-70) and
+ * bayer_denoise (core/io/debayer.cc:1480-1612) --- */
+
+/* ascending bitonic sort of N (a power of two) registers; the indices are
+ * compile-time constants once unrolled */
+template<int N>
+__device__ __forceinline__ void bitonic_sort(float (&v)[N])
+{
+#pragma unroll
+  for( int k = 2; k <= N; k <<= 1 ) {
+#pragma unroll
+    for( int j = k >> 1; j > 0; j >>= 1 ) {
+#pragma unroll
+      for( int i = 0; i < N; ++i ) {
+        const int l = i ^ j;
+        if( l > i ) {
+          const float a = v[i], b = v[l];
+          const bool up = (i & k) == 0;
+          v[i] = up ? fminf(a, b) : fmaxf(a, b);
+          v[l] = up ? fmaxf(a, b) : fminf(a, b);
+        }
+      }
+    }
+  }
+}
+
+template<typename T>
+__device__ __forceinline__ float plane_px(const uint8_t * f, size_t rs, int step, int ox, int oy, int x, int y)
+{
+  return (float) ((const T *) (f + (size_t) (step * y + oy) * rs))[step * x + ox];
+}
+
+/* per plane pixel: the KS x KS median (cv::medianBlur, BORDER_REPLICATE) and
+ * mad = |p - median|; plane z = frame * nplanes + p samples the frame at
+ * (step x + (p & 1), step y + (p >> 1)) */
+template<typename T, int KS>
+__global__ void __launch_bounds__(256) k_bad_median(const uint8_t * src, size_t rs, size_t fs, int pw, int ph, int step,
+    int nplanes, float * med, float * mad)
+{
+  constexpr int N = KS * KS <= 16 ? 16 : 32, R = KS / 2;
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if( x >= pw || y >= ph ) return;
+  const int f = blockIdx.z / nplanes, p = blockIdx.z - f * nplanes;
+  const int ox = step == 2 ? (p & 1) : 0, oy = step == 2 ? (p >> 1) : 0;
+  const uint8_t * fb = src + (size_t) f * fs;
+  float v[N];
+#pragma unroll
+  for( int j = 0; j < KS; ++j ) {
+    const int yy = min(max(y + j - R, 0), ph - 1);
+#pragma unroll
+    for( int i = 0; i < KS; ++i ) v[j * KS + i] = plane_px<T>(fb, rs, step, ox, oy, min(max(x + i - R, 0), pw - 1), yy);
+  }
+  const float p0 = v[R * KS + R];
+#pragma unroll
+  for( int i = KS * KS; i < N; ++i ) v[i] = 3.0e38f;
+  bitonic_sort<N>(v);
+  const float m = v[KS * KS / 2];
+  const size_t o = (size_t) blockIdx.z * pw * ph + (size_t) y * pw + x;
+  med[o] = m;
+  mad[o] = fabsf(p0 - m);
+}
+
+/* the normalized KS x KS box mean of mad (BORDER_REFLECT_101; rounded to the
+ * nearest integer for integer frames), then p -> median where
+ * |median - p| > k mad + minvar */
+template<typename T, int KS>
+__global__ void __launch_bounds__(256) k_bad_apply(const uint8_t * src, size_t rs, size_t fs, int pw, int ph, int step,
+    int nplanes, const float * med, const float * mad, float k, float minvar, uint8_t * dst, size_t drs, size_t dfs)
+{
+  constexpr int R = KS / 2;
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if( x >= pw || y >= ph ) return;
+  const int f = blockIdx.z / nplanes, p = blockIdx.z - f * nplanes;
+  const int ox = step == 2 ? (p & 1) : 0, oy = step == 2 ? (p >> 1) : 0;
+  const float * md = mad + (size_t) blockIdx.z * pw * ph;
+  double s = 0;
+#pragma unroll
+  for( int j = 0; j < KS; ++j ) {
+    int yy = y + j - R;
+    if( ph == 1 ) yy = 0;
+    else while ( yy < 0 || yy >= ph ) yy = yy < 0 ? -yy : 2 * (ph - 1) - yy;
+#pragma unroll
+    for( int i = 0; i < KS; ++i ) {
+      int xx = x + i - R;
+      if( pw == 1 ) xx = 0;
+      else while ( xx < 0 || xx >= pw ) xx = xx < 0 ? -xx : 2 * (pw - 1) - xx;
+      s += (double) md[(size_t) yy * pw + xx];
+    }
+  }
+  float q;
+  if( sizeof(T) < 4 ) {   // integer frames: saturate_cast of sum / KS^2 (never a tie: KS^2 is odd)
+    const long long is = (long long) s;
+    q = (float) ((is + KS * KS / 2) / (KS * KS));
+  }
+  else q = (float) (s * (1.0 / (KS * KS)));
+  const float p0 = plane_px<T>(src + (size_t) f * fs, rs, step, ox, oy, x, y);
+  const float m = med[(size_t) blockIdx.z * pw * ph + (size_t) y * pw + x];
+  const float out = fabsf(m - p0) > __fadd_rn(__fmul_rn(k, q), minvar) ? m : p0;
+  ((T *) (dst + (size_t) f * dfs + (size_t) (step * y + oy) * drs))[step * x + ox] = (T) out;
 }
 
 }  // namespace cal
@@ -205,5 +309,58 @@ extern "C" int sst_debayer_nn2(const void * frames, int depth, int n, int width,
   }
   SST_CCK(cudaGetLastError());
   sst_internal_count_launches(1);
+  return SST_OK;
+}
+
+/* read_input_frame's bad-pixel filter (c_image_stacking_pipeline_base.cc:
+ * 200-216): Bayer frames bayer_denoise (3 x 3 per Bayer plane), others
+ * median_filter_bad_pixels (5 x 5) */
+extern "C" int sst_filter_bad_pixels(const void * frames, int depth, int n, int width, int height, size_t row_stride,
+    size_t frame_stride, int colorid, double variation_threshold, void * dst, size_t dst_row_stride,
+    size_t dst_frame_stride, void * stream)
+{
+  if( !frames || !dst ) return cfail(SST_ERR_INVALID_ARG, "sst_filter_bad_pixels: NULL argument");
+  const bool bayer = colorid >= SST_COLORID_BAYER_RGGB && colorid <= SST_COLORID_BAYER_BGGR;
+  if( n < 1 || n > 16383 || width < 1 || height < 1 || (bayer && ((width & 1) || (height & 1))) )
+    return cfail(SST_ERR_INVALID_ARG, "n in 1..16383, width, height >= 1 (even for Bayer frames)");
+  const int db = depth_bytes(depth);
+  if( db == 0 ) return cfail(SST_ERR_INVALID_ARG, "depth must be u8, u16 or f32");
+  if( dst_row_stride == 0 ) dst_row_stride = (size_t) width * db;
+  if( dst_frame_stride == 0 ) dst_frame_stride = dst_row_stride * height;
+  if( row_stride < (size_t) width * db || (n > 1 && frame_stride < row_stride * height) ||
+      dst_row_stride < (size_t) width * db || (n > 1 && dst_frame_stride < dst_row_stride * height) ||
+      (row_stride % db) || (frame_stride % db) || (dst_row_stride % db) || (dst_frame_stride % db) )
+    return cfail(SST_ERR_INVALID_ARG, "invalid or misaligned strides");
+  cudaStream_t st = (cudaStream_t) stream;
+  const int step = bayer ? 2 : 1, np = bayer ? 4 : 1;
+  const int pw = width / step, ph = height / step;
+  const size_t planes = (size_t) n * np * pw * ph;
+  ScopedBuf med, mad;
+  SST_CCK(med.ensure(planes * sizeof(float)));
+  SST_CCK(mad.ensure(planes * sizeof(float)));
+  const dim3 grid((pw + 31) / 32, (ph + 7) / 8, n * np);
+  const uint8_t * f = (const uint8_t *) frames;
+  uint8_t * d = (uint8_t *) dst;
+  const float k = (float) variation_threshold, mv = depth == SST_DEPTH_F32 ? 1.f / 256.f : 1.f;
+#define SST_BAD(TV, KSV)                                                                                         \
+  sst::cal::k_bad_median<TV, KSV><<<grid, 256, 0, st>>>(f, row_stride, frame_stride, pw, ph, step, np,           \
+      med.as<float>(), mad.as<float>());                                                                         \
+  sst::cal::k_bad_apply<TV, KSV><<<grid, 256, 0, st>>>(f, row_stride, frame_stride, pw, ph, step, np,            \
+      med.as<float>(), mad.as<float>(), k, mv, d, dst_row_stride, dst_frame_stride)
+  switch ( depth ) {
+  case SST_DEPTH_U8:
+    if( bayer ) { SST_BAD(uint8_t, 3); } else { SST_BAD(uint8_t, 5); }
+    break;
+  case SST_DEPTH_U16:
+    if( bayer ) { SST_BAD(uint16_t, 3); } else { SST_BAD(uint16_t, 5); }
+    break;
+  default:
+    if( bayer ) { SST_BAD(float, 3); } else { SST_BAD(float, 5); }
+    break;
+  }
+#undef SST_BAD
+  SST_CCK(cudaGetLastError());
+  sst_internal_count_launches(2);
+  SST_CCK(cudaStreamSynchronize(st));   // the scratch planes are released on return
   return SST_OK;
 }

@@ -295,3 +295,12 @@ def test_accumulator_host_checks(capi):
         assert lib.sst_canvas_average_compute(c, buf, 0, None, 0, 1.0, None, None, 0, None) == -4
     finally:
         lib.sst_canvas_average_destroy(c)
+
+
+def test_filter_bad_pixels_argument_checks(capi):
+    """sst_filter_bad_pixels rejects bad arguments before any GPU work"""
+    lib = capi.lib()
+    assert lib.sst_filter_bad_pixels(None, capi.DEPTH_U16, 1, 8, 8, 16, 128, 0, 3.0, 1, 0, 0, None) == -1
+    assert lib.sst_filter_bad_pixels(1, capi.DEPTH_U16, 1, 9, 8, 18, 144, 8, 3.0, 1, 0, 0, None) == -1   # odd Bayer
+    assert lib.sst_filter_bad_pixels(1, 6, 1, 8, 8, 64, 512, 0, 3.0, 1, 0, 0, None) == -1               # f64
+    assert lib.sst_filter_bad_pixels(1, capi.DEPTH_U16, 1, 8, 8, 14, 128, 0, 3.0, 1, 0, 0, None) == -1  # short rows

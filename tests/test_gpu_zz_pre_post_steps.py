@@ -112,3 +112,31 @@ def test_debayer_nn2_bit_exact(gpu, oracle, colorid, dtype):
         want = O.debayer_nn2(raw[i], colorid)
         assert got[i].dtype == want.dtype
         assert np.array_equal(got[i].view(np.uint8), want.view(np.uint8)), i
+
+
+@pytest.mark.parametrize("colorid", [0, 8, 11])
+@pytest.mark.parametrize("dtype", [np.uint16, np.float32, np.uint8])
+def test_filter_bad_pixels_bit_exact(gpu, oracle, colorid, dtype):
+    """read_input_frame's bad-pixel filter (median_filter_bad_pixels 5 x 5 /
+    bayer_denoise 3 x 3 per Bayer plane) against the oracle: bitwise"""
+    C, O = gpu, oracle
+    rng = np.random.default_rng(colorid + 3)
+    n, h, w = 3, 58, 84
+    if dtype == np.float32:
+        raw = rng.normal(0.4, 0.01, (n, h, w)).astype(np.float32)
+        hot = 0.9
+    else:
+        top = 65535 if dtype == np.uint16 else 255
+        raw = np.clip(rng.normal(0.4 * top, 0.01 * top, (n, h, w)), 0, top).astype(dtype)
+        hot = top
+    for i in range(n):
+        raw[i, rng.integers(0, h, 25), rng.integers(0, w, 25)] = hot
+        raw[i, rng.integers(0, h, 10), rng.integers(0, w, 10)] = 0
+    got = C.filter_bad_pixels(raw, colorid, 3.0)
+    for i in range(n):
+        if dtype == np.uint8:
+            want = O.filter_bad_pixels(raw[i].astype(np.uint16), colorid, 3.0).astype(np.uint8)
+        else:
+            want = O.filter_bad_pixels(raw[i], colorid, 3.0)
+        assert np.array_equal(got[i].view(np.uint8), want.view(np.uint8)), (i, (got[i] != want).sum())
+        assert (got[i] != raw[i]).sum() >= 20

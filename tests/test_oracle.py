@@ -873,3 +873,24 @@ def test_canvas_average_known_answers(oracle):
     assert acc3.shape == (200, 300) and list(st3) == [0, 0] and list(last3) == [74, 50, w, h]
     assert np.all(W3[80:120, 184:244] == 1) and np.all(W3[50:90, 74:134] == 1) and W3.sum() == 2 * w * h
     assert np.allclose(acc3[80:120, 184:244], fr[0]) and np.allclose(acc3[50:90, 74:134], fr[1])
+
+
+def test_filter_bad_pixels_known_answers(oracle):
+    """median_filter_bad_pixels / bayer_denoise: on a flat frame a hot and a
+    cold pixel take the window median (the flat value), nothing else moves;
+    in a Bayer mosaic only the pixel's own plane counts"""
+    O = oracle
+    f = np.full((30, 40), 1000, np.uint16)
+    f[7, 9], f[20, 31] = 9000, 3
+    g = O.filter_bad_pixels(f, 0, 3.0)
+    assert g[7, 9] == 1000 and g[20, 31] == 1000 and (g != f).sum() == 2
+    # RGGB cells of values 100, 200, 300, 400; a hot pixel in the G1 plane (x odd, y even)
+    m = np.zeros((30, 40), np.uint16)
+    m[0::2, 0::2], m[0::2, 1::2], m[1::2, 0::2], m[1::2, 1::2] = 100, 200, 300, 400
+    m[10, 13] = 5000
+    b = O.filter_bad_pixels(m, 8, 3.0)
+    assert b[10, 13] == 200 and (b != m).sum() == 1
+    # a pixel within k * mad + 1 of the median stays
+    n = np.full((30, 40), 1000, np.uint16)
+    n[15, 15] = 1001
+    assert np.array_equal(O.filter_bad_pixels(n, 0, 3.0), n)
