@@ -19,6 +19,14 @@
  *   sst_gb300::c_ser_reader        core/io/c_ser_file.h:136-174
  *   sst_gb300::c_ser_writer        core/io/c_ser_file.h:183-213
  *   sst_gb300::average_pyramid_inpaint  core/proc/inpaint/average_pyramid_inpaint.h:14-18
+ *   sst_gb300::linear_interpolation_inpaint  core/proc/inpaint/linear_interpolation_inpaint.h
+ *   sst_gb300::c_lpg_options, c_lpg_sharpness_measure
+ *                                  core/proc/sharpness_measure/c_lpg_sharpness_measure.h:22-80
+ *   sst_gb300::c_frame_accumulation_with_fft, c_canvas_average,
+ *   c_laplacian_pyramid_focus_stacking
+ *                                  core/average/c_frame_accumulation.h:65-199
+ * (read_input_frame's NN2 debayer and bad-pixel filter work on device frames:
+ * sst_debayer_nn2 / sst_filter_bad_pixels of the C ABI.)
  * Images are passed as `image_view` (pointer, size, OpenCV depth code,
  * stride) instead of cv::Mat, so this header needs no OpenCV; define
  * SST_GB300_WITH_OPENCV before including it to get cv::Mat overloads.
@@ -860,6 +868,223 @@ private:
   image_transform _transform;
   bool _have_transform = false;
   int _w = 0, _hh = 0;
+};
+
+/* linear_interpolation_inpaint(image, mask) (core/proc/inpaint/
+ * linear_interpolation_inpaint.cc) on the GPU: a host FP32 image of
+ * `channels` interleaved channels (packed rows), in place */
+inline bool linear_interpolation_inpaint(std::vector<float> & image, const std::vector<uint8_t> & mask, int width,
+    int height, int channels = 1)
+{
+  if( image.size() != (size_t) width * height * channels || mask.size() != (size_t) width * height ) return false;
+  return sst_linear_interpolation_inpaint(image.data(), 0, width, height, channels, mask.data(), 0, 0, nullptr) == SST_OK;
+}
+
+/* c_lpg_options (c_lpg_sharpness_measure.h:22-28) */
+struct c_lpg_options {
+  double k = 2;
+  double p = 2;
+  int dscale = 2;
+  int uscale = 6;
+};
+
+/* c_lpg_sharpness_measure (c_lpg_sharpness_measure.h:44-80): lpg() maps and
+ * the sharpness metric of a host image */
+class c_lpg_sharpness_measure {
+public:
+  explicit c_lpg_sharpness_measure(const c_lpg_options & o = c_lpg_options())
+  {
+    const sst_lpg_options so = { o.k, o.p, o.dscale, o.uscale };
+    if( sst_lpg_create(&_h, &so) != SST_OK ) _h = nullptr;
+  }
+  ~c_lpg_sharpness_measure() { if( _h ) sst_lpg_destroy(_h); }
+  c_lpg_sharpness_measure(const c_lpg_sharpness_measure &) = delete;
+  c_lpg_sharpness_measure & operator=(const c_lpg_sharpness_measure &) = delete;
+
+  /* create_sharpness_map (the map at the image's size) and the metric, the
+   * map's mean over the nonzero pixels of `mask` (empty view: all pixels) */
+  bool compute(const image_view & image, std::vector<float> & map, double * metric = nullptr,
+      const image_view & mask = image_view())
+  {
+    if( !_h || image.empty() ) return false;
+    map.resize((size_t) image.width * image.height);
+    double m = 0;
+    const bool ok = sst_lpg_compute(_h, image.data, image.depth, 1, image.width, image.height, image.stride,
+        image.stride * image.height, (const uint8_t *) mask.data, mask.stride, mask.stride * mask.height, 0,
+        map.data(), &m, nullptr) == SST_OK;
+    if( metric ) *metric = m;
+    return ok;
+  }
+
+  sst_lpg * handle() const { return _h; }
+
+private:
+  sst_lpg * _h = nullptr;
+};
+
+/* c_frame_accumulation_with_fft (c_frame_accumulation.h:168-199) */
+class c_frame_accumulation_with_fft {
+public:
+  c_frame_accumulation_with_fft() { if( sst_fft_average_create(&_h) != SST_OK ) _h = nullptr; }
+  ~c_frame_accumulation_with_fft() { if( _h ) sst_fft_average_destroy(_h); }
+  c_frame_accumulation_with_fft(const c_frame_accumulation_with_fft &) = delete;
+  c_frame_accumulation_with_fft & operator=(const c_frame_accumulation_with_fft &) = delete;
+
+  /* add(src) for one host frame of `channels` interleaved channels */
+  bool add(const image_view & src, int channels = 1, double scale = 1.0)
+  {
+    if( !_h || src.empty() ) return false;
+    if( sst_fft_average_add(_h, src.data, src.depth, 1, src.width, src.height, channels, src.stride,
+            src.stride * src.height, scale, 0, nullptr) != SST_OK )
+      return false;
+    _w = src.width, _hh = src.height, _cn = channels;
+    return true;
+  }
+
+  /* compute(avg, mask): avg width x height x channels FP32, mask all 255 */
+  bool compute(std::vector<float> & avg, std::vector<uint8_t> & mask) const
+  {
+    if( !_h ) return false;
+    avg.resize((size_t) _w * _hh * _cn);
+    mask.resize((size_t) _w * _hh);
+    return sst_fft_average_compute(_h, avg.data(), 0, mask.data(), 0, 0, nullptr) == SST_OK;
+  }
+
+  void clear() { if( _h ) sst_fft_average_clear(_h); }
+  int accumulated_frames() const { return _h ? sst_fft_average_accumulated_frames(_h) : 0; }
+
+private:
+  sst_fft_average * _h = nullptr;
+  int _w = 0, _hh = 0, _cn = 1;
+};
+
+/* a cv::Rect */
+struct rect {
+  int x = 0, y = 0, width = 0, height = 0;
+  rect() = default;
+  rect(int x_, int y_, int w_, int h_) : x(x_), y(y_), width(w_), height(h_) {}
+  bool empty() const { return width <= 0 || height <= 0; }
+};
+
+/* c_canvas_average (c_frame_accumulation.h:65-146) */
+class c_canvas_average {
+public:
+  c_canvas_average() { if( sst_canvas_average_create(&_h, 0, 0) != SST_OK ) _h = nullptr; }
+  ~c_canvas_average() { if( _h ) sst_canvas_average_destroy(_h); }
+  c_canvas_average(const c_canvas_average &) = delete;
+  c_canvas_average & operator=(const c_canvas_average &) = delete;
+
+  void setCanvasSize(int width, int height) { if( _h ) sst_canvas_average_set_canvas_size(_h, width, height); }
+
+  /* add(current_image, current_weights_or_mask, rmap, new_canvas_bbox): rmap
+   * holds bbox.width x bbox.height x 2 floats (empty with an empty box: no
+   * remap); weights: an empty view, a u8 mask or f32 weights */
+  bool add(const image_view & image, const image_view & weights, const std::vector<float> & rmap,
+      const rect & new_canvas_bbox, int channels = 1, double scale = 1.0)
+  {
+    if( !_h || image.empty() ) return false;
+    if( !rmap.empty() && rmap.size() != (size_t) new_canvas_bbox.width * new_canvas_bbox.height * 2 ) return false;
+    const int32_t box[4] = { new_canvas_bbox.x, new_canvas_bbox.y, new_canvas_bbox.width, new_canvas_bbox.height };
+    if( sst_canvas_average_add(_h, image.data, image.depth, image.width, image.height, channels, image.stride, scale,
+            weights.data, weights.depth, weights.stride, rmap.empty() ? nullptr : rmap.data(),
+            new_canvas_bbox.empty() ? nullptr : box, 0, nullptr) != SST_OK )
+      return false;
+    _cn = channels;
+    return true;
+  }
+
+  /* compute(avg, mask, dscale, -1, rbbox): the canvas or its part in rbbox */
+  bool compute(std::vector<float> & avg, std::vector<uint8_t> & mask, double dscale = 1.0, const rect & rbbox = rect(),
+      rect * out_box = nullptr) const
+  {
+    int cw = 0, ch = 0;
+    if( !_h || sst_canvas_average_state(_h, &cw, &ch, nullptr, nullptr) != SST_OK ) return false;
+    const int bw = rbbox.empty() ? cw : rbbox.width, bh = rbbox.empty() ? ch : rbbox.height;
+    avg.resize((size_t) bw * bh * _cn);
+    mask.resize((size_t) bw * bh);
+    const int32_t rb[4] = { rbbox.x, rbbox.y, rbbox.width, rbbox.height };
+    int32_t ob[4] = { 0, 0, 0, 0 };
+    if( sst_canvas_average_compute(_h, avg.data(), (size_t) bw * _cn * sizeof(float), mask.data(), (size_t) bw,
+            dscale, rbbox.empty() ? nullptr : rb, ob, 0, nullptr) != SST_OK )
+      return false;
+    if( out_box ) *out_box = rect(ob[0], ob[1], ob[2], ob[3]);
+    return true;
+  }
+
+  rect last_bbox() const
+  {
+    int32_t b[4] = { 0, 0, 0, 0 };
+    if( _h ) sst_canvas_average_state(_h, nullptr, nullptr, b, nullptr);
+    return rect(b[0], b[1], b[2], b[3]);
+  }
+
+  int accumulated_frames() const
+  {
+    int n = 0;
+    if( _h ) sst_canvas_average_state(_h, nullptr, nullptr, nullptr, &n);
+    return n;
+  }
+
+  void clear() { if( _h ) sst_canvas_average_clear(_h); }
+
+private:
+  sst_canvas_average * _h = nullptr;
+  int _cn = 1;
+};
+
+/* c_laplacian_pyramid_focus_stacking::options (c_frame_accumulation.h:
+ * 158-164); fusing_policy takes c_laplacian_pyramid_focus_stacking's enum */
+struct c_laplacian_pyramid_focus_stacking_options {
+  int fusing_policy = SST_FOCUS_SELECT_MAX_ENERGY;
+  bool inpaint_mask_holes = true;
+  bool avgchannel = true;
+  int kradius = 0;
+  double ksigma = 0;
+};
+
+/* c_laplacian_pyramid_focus_stacking (c_frame_accumulation.h:149-191) */
+class c_laplacian_pyramid_focus_stacking {
+public:
+  enum fusing_policy { select_max_energy = SST_FOCUS_SELECT_MAX_ENERGY, weighted_average = SST_FOCUS_WEIGHTED_AVERAGE };
+  typedef c_laplacian_pyramid_focus_stacking_options options;
+
+  explicit c_laplacian_pyramid_focus_stacking(const options & o = options())
+  {
+    const sst_focus_stack_options so = { (int32_t) o.fusing_policy, o.inpaint_mask_holes ? 1 : 0,
+        o.avgchannel ? 1 : 0, o.kradius, o.ksigma };
+    if( sst_focus_stack_create(&_h, &so) != SST_OK ) _h = nullptr;
+  }
+  ~c_laplacian_pyramid_focus_stacking() { if( _h ) sst_focus_stack_destroy(_h); }
+  c_laplacian_pyramid_focus_stacking(const c_laplacian_pyramid_focus_stacking &) = delete;
+  c_laplacian_pyramid_focus_stacking & operator=(const c_laplacian_pyramid_focus_stacking &) = delete;
+
+  /* add(src, mask): one host frame of `channels` interleaved channels; mask an
+   * empty view or a u8 mask */
+  bool add(const image_view & src, const image_view & mask = image_view(), int channels = 1, double scale = 1.0)
+  {
+    if( !_h || src.empty() ) return false;
+    if( sst_focus_stack_add(_h, src.data, src.depth, 1, src.width, src.height, channels, src.stride,
+            src.stride * src.height, scale, (const uint8_t *) mask.data, mask.stride, mask.stride * mask.height, 0,
+            nullptr) != SST_OK )
+      return false;
+    _w = src.width, _hh = src.height, _cn = channels;
+    return true;
+  }
+
+  /* compute(avg): width x height x channels FP32 */
+  bool compute(std::vector<float> & avg) const
+  {
+    if( !_h ) return false;
+    avg.resize((size_t) _w * _hh * _cn);
+    return sst_focus_stack_compute(_h, avg.data(), 0, 0, nullptr) == SST_OK;
+  }
+
+  void clear() { if( _h ) sst_focus_stack_clear(_h); }
+  int accumulated_frames() const { return _h ? sst_focus_stack_accumulated_frames(_h) : 0; }
+
+private:
+  sst_focus_stack * _h = nullptr;
+  int _w = 0, _hh = 0, _cn = 1;
 };
 
 }  // namespace sst_gb300

@@ -109,6 +109,22 @@ int main() {
   if( ba.bayer_pattern() != SST_COLORID_BAYER_GRBG ) return 18;
   sst_gb300::c_eccflow_options fo;
   if( fo.support_scale != 5 || fo.scale_factor != 0.5 ) return 19;
+  sst_gb300::c_lpg_options lpo;
+  if( lpo.k != 2 || lpo.p != 2 || lpo.dscale != 2 || lpo.uscale != 6 ) return 20;
+  sst_gb300::c_lpg_sharpness_measure lpg(lpo);
+  if( !lpg.handle() ) return 21;
+  sst_gb300::c_laplacian_pyramid_focus_stacking::options fso;
+  if( fso.fusing_policy != sst_gb300::c_laplacian_pyramid_focus_stacking::select_max_energy ||
+      !fso.inpaint_mask_holes || !fso.avgchannel || fso.kradius != 0 || fso.ksigma != 0 ) return 22;
+  sst_gb300::c_laplacian_pyramid_focus_stacking fs(fso);
+  sst_gb300::c_frame_accumulation_with_fft fft;
+  sst_gb300::c_canvas_average canvas;
+  canvas.setCanvasSize(640, 480);
+  if( fs.accumulated_frames() != 0 || fft.accumulated_frames() != 0 || canvas.accumulated_frames() != 0 ||
+      !canvas.last_bbox().empty() ) return 23;
+  std::vector<float> none;
+  if( fft.compute(none, *new std::vector<uint8_t>()) ) return 24;      // nothing accumulated
+  if( canvas.add(sst_gb300::image_view(), sst_gb300::image_view(), none, sst_gb300::rect()) ) return 25;
   std::printf("ok %s\n", sst_version());
   return 0;
 }
