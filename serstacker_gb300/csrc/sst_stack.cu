@@ -996,12 +996,160 @@ __global__ void __launch_bounds__(256) k_stack_bayer_planes(BayerPlanesArgs a)
   }
 }
 
+/* The four-plane Bayer stack for the affine and projective families in the
+ * form of k_stack_add_streamed: one output column of BP_PPT rows per thread,
+ * warps on their own (interior tests 8 frames per ballot, four-corner window
+ * validity at the border), FP32 partials of SA_FLUSH frames in registers and
+ * the compensated sums of the four planes and the weight in thread-private
+ * shared slots. */
+constexpr int BP_PPT = 2, BP_TY = 2 * 256 / SA_TX;   // Bayer planes: 64 x 8 tiles, 2 rows per thread
+
+template<int FAM, bool WMAP>
+__global__ void __launch_bounds__(256, 3) k_stack_bayer_streamed(BayerPlanesArgs a)
+{
+  constexpr int NQ = 10;                              // S, cS of four planes; W, cW
+  __shared__ float s_acc[NQ][BP_PPT][256];
+  const int tx0 = blockIdx.x * SA_TX, ty0 = blockIdx.y * BP_TY;
+  const int lx = threadIdx.x % SA_TX, yb = ty0 + (threadIdx.x / SA_TX) * BP_PPT;
+  const int x = tx0 + lx;
+  const int xw = tx0 + (lx & ~31);
+  const int wx0 = max(xw - 2, 0), wx1 = min(xw + 33, a.pw - 1);
+  const int wy0 = max(yb - 2, 0), wy1 = min(yb + BP_PPT + 1, a.ph - 1);
+  const bool active = xw < a.pw && yb < a.ph;          // warp-uniform
+  const bool xin = x < a.pw;
+  const int lane = threadIdx.x & 31;
+  float pS[BP_PPT][4], pW[BP_PPT];
+#pragma unroll
+  for( int k = 0; k < BP_PPT; ++k ) {
+    pW[k] = 0.f;
+#pragma unroll
+    for( int q = 0; q < 4; ++q ) pS[k][q] = 0.f;
+#pragma unroll
+    for( int q = 0; q < NQ; ++q ) s_acc[q][k][threadIdx.x] = 0.f;
+  }
+  int since = 0;
+  unsigned inner8 = 0u;
+  for( int f = 0; f < a.n && active; ++f ) {
+    if( (f & 7) == 0 ) {
+      const int fl = f + (lane >> 2);
+      bool ok = false;
+      if( fl < a.n ) {
+        const float4 * cq = (const float4 *) (a.coeffs + (size_t) fl * SST_NCOEF);
+        const float4 r0 = __ldg(cq), r1 = __ldg(cq + 1), r3 = __ldg(cq + 3);
+        float cc[SST_NCOEF];
+        cc[0] = r0.x, cc[1] = r0.y, cc[2] = r0.z, cc[3] = r0.w, cc[4] = r1.x, cc[5] = r1.y, cc[6] = r1.z, cc[7] = r1.w;
+        cc[8] = cc[9] = cc[10] = cc[11] = 0.f;
+        cc[12] = r3.x, cc[13] = r3.y, cc[14] = r3.z, cc[15] = r3.w;
+        ok = point_interior<FAM>(cc, (lane & 1) ? wx1 : wx0, (lane & 2) ? wy1 : wy0, a.pw, a.ph);
+      }
+      inner8 = __ballot_sync(0xffffffffu, ok);
+    }
+    const bool inner = ((inner8 >> (4 * (f & 7))) & 0xFu) == 0xFu;
+    const float wf = __ldg(a.weights + f);
+    if( !(wf > 0.f) ) continue;                       // uniform over the CTA
+    const float4 * cp = (const float4 *) (a.coeffs + (size_t) f * SST_NCOEF);
+    const float4 q0 = __ldg(cp), q1 = __ldg(cp + 1), q3 = __ldg(cp + 3);
+    float c[SST_NCOEF];
+    c[0] = q0.x, c[1] = q0.y, c[2] = q0.z, c[3] = q0.w, c[4] = q1.x, c[5] = q1.y, c[6] = q1.z, c[7] = q1.w;
+    c[8] = c[9] = c[10] = c[11] = 0.f;
+    c[12] = q3.x, c[13] = q3.y, c[14] = q3.z, c[15] = q3.w;
+    const uint8_t * fb = a.frames + (size_t) f * a.frame_stride;
+    if( xin ) {
+#pragma unroll
+      for( int k = 0; k < BP_PPT; ++k ) {
+        const int y = yb + k;
+        if( y >= a.ph ) continue;
+        if( !inner && !window_valid<FAM>(c, x, y, a.pw, a.ph, a.pw, a.ph) ) continue;
+        const spos s = warp_pos<FAM>(c, x, y);
+        const float wp = WMAP ? wf * __ldg(a.wmap + (size_t) f * a.plane + (size_t) y * a.pw + x) : wf;
+        const float wsc = wp * a.scale;
+        if( inner || (s.x0 >= 0 && s.x0 < a.pw - 1 && s.y0 >= 0 && s.y0 < a.ph - 1) ) {
+          // raw rows 2 y0 .. 2 y0 + 3, columns 2 x0 .. 2 x0 + 3 (two u32 per row)
+          const uint8_t * r = fb + (size_t) (2 * s.y0) * a.row_stride + (size_t) s.x0 * 4;
+          uint32_t q[4][2];
+#pragma unroll
+          for( int rr = 0; rr < 4; ++rr ) {
+            q[rr][0] = __ldg((const uint32_t *) (r + (size_t) rr * a.row_stride));
+            q[rr][1] = __ldg((const uint32_t *) (r + (size_t) rr * a.row_stride) + 1);
+          }
+#pragma unroll
+          for( int p = 0; p < 4; ++p ) {
+            const int dy = p >> 1, sh = (p & 1) * 16;
+            const float v00 = (float) ((q[dy][0] >> sh) & 0xffffu), v01 = (float) ((q[dy][1] >> sh) & 0xffffu);
+            const float v10 = (float) ((q[dy + 2][0] >> sh) & 0xffffu), v11 = (float) ((q[dy + 2][1] >> sh) & 0xffffu);
+            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+            pS[k][p] = fmaf(wsc, fmaf(s.fy, t1 - t0, t0), pS[k][p]);
+          }
+        }
+        else {
+#pragma unroll
+          for( int p = 0; p < 4; ++p ) {
+            const float v00 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0, s.y0, p, a.border);
+            const float v01 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0 + 1, s.y0, p, a.border);
+            const float v10 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0, s.y0 + 1, p, a.border);
+            const float v11 = raw_tap(fb, a.row_stride, a.pw, a.ph, s.x0 + 1, s.y0 + 1, p, a.border);
+            const float t0 = fmaf(s.fx, v01 - v00, v00), t1 = fmaf(s.fx, v11 - v10, v10);
+            pS[k][p] = fmaf(wsc, fmaf(s.fy, t1 - t0, t0), pS[k][p]);
+          }
+        }
+        pW[k] += wp;
+      }
+    }
+    if( ++since == SA_FLUSH ) {
+#pragma unroll
+      for( int k = 0; k < BP_PPT; ++k ) {
+#pragma unroll
+        for( int p = 0; p < 4; ++p ) {
+          float S = s_acc[2 * p][k][threadIdx.x], cS = s_acc[2 * p + 1][k][threadIdx.x];
+          kahan_add(S, cS, pS[k][p]);
+          s_acc[2 * p][k][threadIdx.x] = S, s_acc[2 * p + 1][k][threadIdx.x] = cS;
+          pS[k][p] = 0.f;
+        }
+        float Wt = s_acc[8][k][threadIdx.x], cW = s_acc[9][k][threadIdx.x];
+        kahan_add(Wt, cW, pW[k]);
+        s_acc[8][k][threadIdx.x] = Wt, s_acc[9][k][threadIdx.x] = cW;
+        pW[k] = 0.f;
+      }
+      since = 0;
+    }
+  }
+  if( xin ) {
+#pragma unroll
+    for( int k = 0; k < BP_PPT; ++k ) {
+      const int y = yb + k;
+      if( y >= a.ph ) continue;
+      const size_t i = (size_t) y * a.pw + x;
+      float Wt = s_acc[8][k][threadIdx.x], cW = s_acc[9][k][threadIdx.x];
+      kahan_add(Wt, cW, pW[k]);
+#pragma unroll
+      for( int p = 0; p < 4; ++p ) {
+        float S = s_acc[2 * p][k][threadIdx.x], cS = s_acc[2 * p + 1][k][threadIdx.x];
+        kahan_add(S, cS, pS[k][p]);
+        float * P = a.acc[p];
+        float gS = P[i], gcS = P[a.plane + i], gW = P[2 * a.plane + i], gcW = P[3 * a.plane + i];
+        kahan_add(gS, gcS, S);
+        gcS += cS;
+        kahan_add(gW, gcW, Wt);
+        gcW += cW;
+        P[i] = gS, P[a.plane + i] = gcS, P[2 * a.plane + i] = gW, P[3 * a.plane + i] = gcW;
+      }
+    }
+  }
+}
+
 cudaError_t launch_stack_bayer_planes(const BayerPlanesArgs & a, int motion, cudaStream_t st)
 {
-  dim3 grid((a.pw + SA_TX - 1) / SA_TX, (a.ph + SA_TY - 1) / SA_TY);
+  const dim3 grid((a.pw + SA_TX - 1) / SA_TX, (a.ph + SA_TY - 1) / SA_TY);
+  const dim3 sgrid((a.pw + SA_TX - 1) / SA_TX, (a.ph + BP_TY - 1) / BP_TY);
   switch ( motion_family(motion) ) {
-  case FAM_AFFINE: k_stack_bayer_planes<FAM_AFFINE><<<grid, 256, 0, st>>>(a); break;
-  case FAM_HOMOG: k_stack_bayer_planes<FAM_HOMOG><<<grid, 256, 0, st>>>(a); break;
+  case FAM_AFFINE:
+    if( a.wmap ) k_stack_bayer_streamed<FAM_AFFINE, true><<<sgrid, 256, 0, st>>>(a);
+    else k_stack_bayer_streamed<FAM_AFFINE, false><<<sgrid, 256, 0, st>>>(a);
+    break;
+  case FAM_HOMOG:
+    if( a.wmap ) k_stack_bayer_streamed<FAM_HOMOG, true><<<sgrid, 256, 0, st>>>(a);
+    else k_stack_bayer_streamed<FAM_HOMOG, false><<<sgrid, 256, 0, st>>>(a);
+    break;
   default: k_stack_bayer_planes<FAM_QUAD><<<grid, 256, 0, st>>>(a); break;
   }
   return cudaGetLastError();
