@@ -294,10 +294,12 @@ def main():
     ap.add_argument("--unrolled-schedule", action="store_true",
                     help="level iterations as the unrolled launch schedule instead of graph WHILE loops "
                          "(per-kernel profilers do not profile kernels of graphs with conditional nodes)")
-    ap.add_argument("--workload", choices=["mono", "bayer", "roi", "flow", "config0"], default="mono",
+    ap.add_argument("--workload", choices=["mono", "bayer", "roi", "flow", "config0", "steps"], default="mono",
                     help="mono: the headline 1280x960 sequence; bayer: raw RGGB 3096x2080 frames; "
                          "roi: uneven-ROI crops (--frames crops); flow: c_eccflow on 1024^2 frames; "
-                         "config0: 64 u8 640x480 frames, plain FA euclidean")
+                         "config0: 64 u8 640x480 frames, plain FA euclidean; steps: read_input_frame's debayer and "
+                         "bad-pixel filter, LPG weights, the FFT / canvas / focus-stacking accumulators and the "
+                         "linear inpaint, each timed on its own")
     ap.add_argument("--roi-method", choices=["fa", "lm"], default="fa")
     ap.add_argument("--roi-sample", type=int, default=8, help="crops checked against the oracle")
     ap.add_argument("--flow-sample", type=int, default=32, help="frames checked against the oracle (flow)")
@@ -327,8 +329,9 @@ def main():
             import torch.distributed as dist
             dist.destroy_process_group()
         return
-    if args.workload in ("bayer", "roi", "flow", "config0"):
-        {"bayer": main_bayer, "roi": main_roi, "flow": main_flow, "config0": main_config0}[args.workload](
+    if args.workload in ("bayer", "roi", "flow", "config0", "steps"):
+        {"bayer": main_bayer, "roi": main_roi, "flow": main_flow, "config0": main_config0,
+         "steps": main_steps}[args.workload](
             args, ws, rank, local)
         if ws > 1:
             import torch.distributed as dist
@@ -1231,6 +1234,151 @@ def main_flow(args, ws_, rank, local):
                 "config": {**flow_cfg(n), "parallelism": f"replicas x{ws_}"}, "roofline": roof,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "accuracy": acc,
                 "adjoint": adjoint_line}
+        print(json.dumps(line), flush=True)
+
+
+STEPS_RAW_W, STEPS_RAW_H = 3096, 2080
+
+
+def main_steps(args, ws_, rank, local):
+    """The steps either side of the stacking loop and the other accumulators,
+    each timed on its own with device-resident synthetic inputs (CUDA events,
+    warm-up first): read_input_frame's NN2 debayer and bad-pixel filter on raw
+    RGGB 3096x2080 u16 frames; LPG maps, the FFT average, the Laplacian focus
+    stack and the canvas average on 1280x960 frames; linear_interpolation_inpaint
+    of one 1280x960 image. Each entry gives frames/s, the algorithmic bytes per
+    pixel and GB/s against the measured HBM peak, and the FP64 oracle timed on
+    one frame on one host core (cpu_baseline, kind port)."""
+    import ctypes as Cty
+    import torch
+    import oracle as O
+    from serstacker_gb300 import capi as C
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    lib = C.lib()
+    O.build()
+    peak, peak_kind = measured_peaks()
+    n = min(args.frames, 64)
+    reps = max(1, args.steps)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(SEED + 7)
+
+    def timeit(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def cpu_rate(fn):
+        t0 = time.perf_counter()
+        fn()
+        return 1.0 / (time.perf_counter() - t0)
+
+    def entry(ms, frames, px, bytes_per_px, what, cpu, sample="one frame of the same size through the FP64 oracle"):
+        gbs = frames * px * bytes_per_px / (ms / 1e3) / 1e9
+        return {"frames_per_s": frames / (ms / 1e3), "ms_per_call": ms, "frames_per_call": frames,
+                "alg_bytes_per_px": bytes_per_px, "achieved_gbs": gbs, "frac_of_hbm": gbs / peak,
+                "workload": what, "cpu_baseline": {"value": cpu, "unit": "frames/s", "cores": 1, "kind": "port",
+                                                   "sample": sample}}
+
+    res = {}
+    raw_px = STEPS_RAW_W * STEPS_RAW_H
+    raw = torch.randint(0, 4096, (n, STEPS_RAW_H, STEPS_RAW_W), generator=gen, device=device,
+                        dtype=torch.int32).to(torch.int16)
+    bgr = torch.empty((n, STEPS_RAW_H, STEPS_RAW_W, 3), dtype=torch.int16, device=device)
+    raw0 = raw[0].cpu().numpy().view(np.uint16)
+
+    def nn2():
+        C._check(lib.sst_debayer_nn2(raw.data_ptr(), C.DEPTH_U16, n, STEPS_RAW_W, STEPS_RAW_H, STEPS_RAW_W * 2,
+                                     raw_px * 2, 8, bgr.data_ptr(), 0, 0, None), "sst_debayer_nn2")
+    res["debayer_nn2"] = entry(timeit(nn2), n, raw_px, 8, f"{n} raw RGGB {STEPS_RAW_W}x{STEPS_RAW_H} u16 -> BGR u16",
+                               cpu_rate(lambda: O.debayer_nn2(raw0, 8)))
+    flt = torch.empty_like(raw)
+
+    def bad():
+        C._check(lib.sst_filter_bad_pixels(raw.data_ptr(), C.DEPTH_U16, n, STEPS_RAW_W, STEPS_RAW_H, STEPS_RAW_W * 2,
+                                           raw_px * 2, 8, 3.0, flt.data_ptr(), 0, 0, None), "sst_filter_bad_pixels")
+    res["bad_pixels_bayer"] = entry(timeit(bad), n, raw_px, 4,
+                                    f"{n} raw RGGB {STEPS_RAW_W}x{STEPS_RAW_H} u16, bayer_denoise k = 3",
+                                    cpu_rate(lambda: O.filter_bad_pixels(raw0, 8, 3.0)))
+    del raw, bgr, flt
+    torch.cuda.empty_cache()
+
+    px = WIDTH * HEIGHT
+    frames, _, _ = make_workload(n, device)
+    fr32 = (frames.to(torch.int32) & 0xffff).to(torch.float32) * SCALE
+    f0 = fr32[0].cpu().numpy().astype(np.float64)
+    lpg = C.c_lpg_sharpness_measure()
+    maps = torch.empty((n, HEIGHT, WIDTH), dtype=torch.float32, device=device)
+    mets = (Cty.c_double * n)()
+
+    def lpg_run():
+        C._check(lib.sst_lpg_compute(lpg._h, frames.data_ptr(), C.DEPTH_U16, n, WIDTH, HEIGHT, WIDTH * 2, px * 2, None,
+                                     0, 0, 1, maps.data_ptr(), mets, None), "sst_lpg_compute")
+    res["lpg"] = entry(timeit(lpg_run), n, px, 6, f"{n} u16 1280x960 frames, c_lpg_options defaults (k 2, p 2, "
+                       "dscale 2, uscale 6), maps + metrics", cpu_rate(lambda: O.lpg(f0)))
+    fft = C.c_frame_accumulation_with_fft()
+
+    def fft_run():
+        C._check(lib.sst_fft_average_clear(fft._h), "clear")
+        C._check(lib.sst_fft_average_add(fft._h, fr32.data_ptr(), C.DEPTH_F32, n, WIDTH, HEIGHT, 1, WIDTH * 4, px * 4,
+                                         1.0, 1, None), "sst_fft_average_add")
+    fsmall = f0[:240, :320]
+    res["fft_average_add"] = entry(timeit(fft_run), n, px, 4,
+                                   f"{n} f32 1280x960 frames (an optimal DFT size): R2C + spectral weights",
+                                   cpu_rate(lambda: O.fft_average(fsmall[None])),
+                                   "one 320x240 frame through the FP64 oracle's direct DFT")
+    fs = C.c_laplacian_pyramid_focus_stacking()
+    nf = min(n, 16)
+
+    def focus_run():
+        C._check(lib.sst_focus_stack_clear(fs._h), "clear")
+        C._check(lib.sst_focus_stack_add(fs._h, fr32.data_ptr(), C.DEPTH_F32, nf, WIDTH, HEIGHT, 1, WIDTH * 4, px * 4,
+                                         1.0, None, 0, 0, 1, None), "sst_focus_stack_add")
+    res["focus_stack_add"] = entry(timeit(focus_run), nf, px, 4, f"{nf} f32 1280x960 frames, select_max_energy",
+                                   cpu_rate(lambda: O.focus_stack(f0[None])))
+    cv = C.c_canvas_average((WIDTH * 3 // 2, HEIGHT * 3 // 2))
+    bw, bh = WIDTH - 64, HEIGHT - 64
+    yy, xx = torch.meshgrid(torch.arange(bh, device=device, dtype=torch.float32),
+                            torch.arange(bw, device=device, dtype=torch.float32), indexing="ij")
+    rmap = torch.stack([xx + 17.3, yy + 9.6], dim=-1).contiguous()
+    box = (Cty.c_int32 * 4)(300, 250, bw, bh)
+
+    def canvas_run():
+        C._check(lib.sst_canvas_average_clear(cv._h), "clear")
+        for i in range(n):
+            C._check(lib.sst_canvas_average_add(cv._h, fr32[i].data_ptr(), C.DEPTH_F32, WIDTH, HEIGHT, 1, WIDTH * 4, 1.0,
+                                                None, 0, 0, None if i == 0 else rmap.data_ptr(),
+                                                None if i == 0 else box, 1, None), "sst_canvas_average_add")
+    rmap_np = rmap.cpu().numpy().astype(np.float64)
+    boxes = np.array([[0, 0, 0, 0], [300, 250, bw, bh]], np.int32)
+    res["canvas_average_add"] = entry(
+        timeit(canvas_run), n, bw * bh, 16,
+        f"{n} f32 1280x960 frames remapped onto a 1920x1440 canvas (one launch per frame)",
+        2 * cpu_rate(lambda: O.canvas_average(np.stack([f0, f0]), boxes=boxes, rmaps=[None, rmap_np],
+                                               canvas=(WIDTH * 3 // 2, HEIGHT * 3 // 2))),
+        "two frames (the first placed, the second remapped) through the FP64 oracle")
+    img = fr32[0].clone()
+    holes = (torch.rand((HEIGHT, WIDTH), generator=gen, device=device) > 0.05).to(torch.uint8) * 255
+
+    def inpaint_run():
+        C._check(lib.sst_linear_interpolation_inpaint(img.data_ptr(), 0, WIDTH, HEIGHT, 1, holes.data_ptr(), 0, 1, None),
+                 "sst_linear_interpolation_inpaint")
+    hm = holes.cpu().numpy()
+    res["linear_inpaint"] = entry(timeit(inpaint_run), 1, px, 13, "one f32 1280x960 image, 5 % random holes",
+                                  cpu_rate(lambda: O.linear_inpaint(f0, hm)))
+    if rank == 0:
+        line = {"metric": "read_input_frame steps, LPG weights and the other accumulators on GB300 (each on its own)",
+                "workload": "steps", "n_gpus": ws_, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+                "peak_gbs": peak, "peak_source": peak_kind, "results": res,
+                "note": "device-resident inputs, CUDA events; alg_bytes_per_px counts the frame bytes read and the "
+                        "result bytes written; cpu_baseline: the FP64 oracle on one host core"}
         print(json.dumps(line), flush=True)
 
 

@@ -22,6 +22,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <type_traits>
 
 #include "sst_host.h"
 
@@ -58,57 +59,75 @@ __device__ __forceinline__ int bayer_color(int colorid, int x, int y)
 }
 
 template<typename T, typename A>
-__device__ __forceinline__ A nn2_at(const uint8_t * f, size_t rs, int w, int h, int x, int y)
-{
-  x = x < 0 ? -x : (x >= w ? 2 * (w - 1) - x : x);
-  y = y < 0 ? -y : (y >= h ? 2 * (h - 1) - y : y);
-  return (A) ((const T *) (f + (size_t) y * rs))[x];
-}
-
-template<typename T, typename A>
 __device__ __forceinline__ T nn2_mean(A s, int n)
 {
-  if constexpr( sizeof(A) == 8 ) return (T) ((s + n / 2) / n);
+  if constexpr( sizeof(A) == 4 && !std::is_floating_point<A>::value ) return (T) ((s + n / 2) / n);
   else return (T) __fdiv_rn(s, (float) n);
 }
 
-/* nninterpolation (core/debayer.cc:828-1161): one thread per pixel; sums in
- * A (int64 for integer frames, f32 for float ones) in the order N W E S /
- * NW NE SW SE / W E / N S */
+/* nninterpolation (core/debayer.cc:828-1161): one thread per 2 x 2 Bayer
+ * cell, which holds the 4 x 4 raw block around it (rows and columns -1 .. +2,
+ * BORDER_REFLECT_101) and writes its four BGR pixels. Sums in A (int for
+ * integer frames: the rounded means (s + n / 2) / n are those of 64-bit sums;
+ * f32 for float ones) in the order N W E S / NW NE SW SE / W E / N S. */
 template<typename T, typename A>
 __global__ void __launch_bounds__(128) k_debayer_nn2(const uint8_t * frames, int w, int h, size_t rs, size_t fs,
     int colorid, uint8_t * dst, size_t drs, size_t dfs)
 {
-  const int x = blockIdx.x * 128 + threadIdx.x, y = blockIdx.y;
-  if( x >= w ) return;
+  const int cx = blockIdx.x * 128 + threadIdx.x, cy = blockIdx.y;
+  if( 2 * cx >= w ) return;
   const uint8_t * f = frames + (size_t) blockIdx.z * fs;
-  const int own = bayer_color(colorid, x, y);
-  T out[3];
+  int xs[4], ys[4];
 #pragma unroll
-  for( int ch = 0; ch < 3; ++ch ) {
-    if( ch == own ) out[ch] = (T) nn2_at<T, A>(f, rs, w, h, x, y);
-    else if( ch == 1 ) {
-      A s = nn2_at<T, A>(f, rs, w, h, x, y - 1);
-      s = s + nn2_at<T, A>(f, rs, w, h, x - 1, y);
-      s = s + nn2_at<T, A>(f, rs, w, h, x + 1, y);
-      s = s + nn2_at<T, A>(f, rs, w, h, x, y + 1);
-      out[ch] = nn2_mean<T, A>(s, 4);
-    }
-    else if( own == 1 ) {
-      if( bayer_color(colorid, x + 1, y) == ch )
-        out[ch] = nn2_mean<T, A>(nn2_at<T, A>(f, rs, w, h, x - 1, y) + nn2_at<T, A>(f, rs, w, h, x + 1, y), 2);
-      else out[ch] = nn2_mean<T, A>(nn2_at<T, A>(f, rs, w, h, x, y - 1) + nn2_at<T, A>(f, rs, w, h, x, y + 1), 2);
-    }
-    else {
-      A s = nn2_at<T, A>(f, rs, w, h, x - 1, y - 1);
-      s = s + nn2_at<T, A>(f, rs, w, h, x + 1, y - 1);
-      s = s + nn2_at<T, A>(f, rs, w, h, x - 1, y + 1);
-      s = s + nn2_at<T, A>(f, rs, w, h, x + 1, y + 1);
-      out[ch] = nn2_mean<T, A>(s, 4);
-    }
+  for( int k = 0; k < 4; ++k ) {
+    const int x = 2 * cx - 1 + k, y = 2 * cy - 1 + k;
+    xs[k] = x < 0 ? -x : (x >= w ? 2 * (w - 1) - x : x);
+    ys[k] = y < 0 ? -y : (y >= h ? 2 * (h - 1) - y : y);
   }
-  T * d = (T *) (dst + (size_t) blockIdx.z * dfs + (size_t) y * drs) + (size_t) x * 3;
-  d[0] = out[0], d[1] = out[1], d[2] = out[2];
+  A v[4][4];
+#pragma unroll
+  for( int r = 0; r < 4; ++r ) {
+    const T * row = (const T *) (f + (size_t) ys[r] * rs);
+#pragma unroll
+    for( int c = 0; c < 4; ++c ) v[r][c] = (A) row[xs[c]];
+  }
+#pragma unroll
+  for( int dy = 0; dy < 2; ++dy ) {
+    T out[6];
+#pragma unroll
+    for( int dx = 0; dx < 2; ++dx ) {
+      const int r = 1 + dy, c = 1 + dx;
+      const int own = bayer_color(colorid, 2 * cx + dx, 2 * cy + dy);
+#pragma unroll
+      for( int ch = 0; ch < 3; ++ch ) {
+        T o;
+        if( ch == own ) o = (T) v[r][c];
+        else if( ch == 1 ) {
+          A s = v[r - 1][c];
+          s = s + v[r][c - 1];
+          s = s + v[r][c + 1];
+          s = s + v[r + 1][c];
+          o = nn2_mean<T, A>(s, 4);
+        }
+        else if( own == 1 ) {
+          // the colour of the horizontal neighbours takes their mean, the other the vertical one
+          const bool horiz = bayer_color(colorid, 2 * cx + dx + 1, 2 * cy + dy) == ch;
+          o = horiz ? nn2_mean<T, A>(v[r][c - 1] + v[r][c + 1], 2) : nn2_mean<T, A>(v[r - 1][c] + v[r + 1][c], 2);
+        }
+        else {
+          A s = v[r - 1][c - 1];
+          s = s + v[r - 1][c + 1];
+          s = s + v[r + 1][c - 1];
+          s = s + v[r + 1][c + 1];
+          o = nn2_mean<T, A>(s, 4);
+        }
+        out[dx * 3 + ch] = o;
+      }
+    }
+    T * d = (T *) (dst + (size_t) blockIdx.z * dfs + (size_t) (2 * cy + dy) * drs) + (size_t) 6 * cx;
+#pragma unroll
+    for( int k = 0; k < 6; ++k ) d[k] = out[k];
+  }
 }
 
 /* --- bad pixels: median_filter_bad_pixels (core/proc/bad_pixels.cc:14-70) and
@@ -186,7 +205,9 @@ __global__ void __launch_bounds__(256) k_bad_apply(const uint8_t * src, size_t r
   const int f = blockIdx.z / nplanes, p = blockIdx.z - f * nplanes;
   const int ox = step == 2 ? (p & 1) : 0, oy = step == 2 ? (p >> 1) : 0;
   const float * md = mad + (size_t) blockIdx.z * pw * ph;
-  double s = 0;
+  // integer frames: exact integer sums; f32 frames: FP64 sums, in the same order
+  typedef typename std::conditional<(sizeof(T) < 4), int, double>::type Acc;
+  Acc s = 0;
 #pragma unroll
   for( int j = 0; j < KS; ++j ) {
     int yy = y + j - R;
@@ -197,15 +218,12 @@ __global__ void __launch_bounds__(256) k_bad_apply(const uint8_t * src, size_t r
       int xx = x + i - R;
       if( pw == 1 ) xx = 0;
       else while ( xx < 0 || xx >= pw ) xx = xx < 0 ? -xx : 2 * (pw - 1) - xx;
-      s += (double) md[(size_t) yy * pw + xx];
+      s += (Acc) md[(size_t) yy * pw + xx];
     }
   }
   float q;
-  if( sizeof(T) < 4 ) {   // integer frames: saturate_cast of sum / KS^2 (never a tie: KS^2 is odd)
-    const long long is = (long long) s;
-    q = (float) ((is + KS * KS / 2) / (KS * KS));
-  }
-  else q = (float) (s * (1.0 / (KS * KS)));
+  if( sizeof(T) < 4 ) q = (float) (((int) s + KS * KS / 2) / (KS * KS));   // saturate_cast of sum / KS^2 (never a tie)
+  else q = (float) ((double) s * (1.0 / (KS * KS)));
   const float p0 = plane_px<T>(src + (size_t) f * fs, rs, step, ox, oy, x, y);
   const float m = med[(size_t) blockIdx.z * pw * ph + (size_t) y * pw + x];
   const float out = fabsf(m - p0) > __fadd_rn(__fmul_rn(k, q), minvar) ? m : p0;
@@ -290,16 +308,16 @@ extern "C" int sst_debayer_nn2(const void * frames, int depth, int n, int width,
       (row_stride % db) || (frame_stride % db) || (dst_row_stride % db) || (dst_frame_stride % db) )
     return cfail(SST_ERR_INVALID_ARG, "invalid or misaligned strides");
   cudaStream_t st = (cudaStream_t) stream;
-  const dim3 grid((width + 127) / 128, height, n);
+  const dim3 grid((width / 2 + 127) / 128, height / 2, n);   // one thread per 2 x 2 cell
   const uint8_t * f = (const uint8_t *) frames;
   uint8_t * d = (uint8_t *) dst;
   switch ( depth ) {
   case SST_DEPTH_U8:
-    sst::cal::k_debayer_nn2<uint8_t, long long><<<grid, 128, 0, st>>>(f, width, height, row_stride, frame_stride,
+    sst::cal::k_debayer_nn2<uint8_t, int><<<grid, 128, 0, st>>>(f, width, height, row_stride, frame_stride,
         colorid, d, dst_row_stride, dst_frame_stride);
     break;
   case SST_DEPTH_U16:
-    sst::cal::k_debayer_nn2<uint16_t, long long><<<grid, 128, 0, st>>>(f, width, height, row_stride, frame_stride,
+    sst::cal::k_debayer_nn2<uint16_t, int><<<grid, 128, 0, st>>>(f, width, height, row_stride, frame_stride,
         colorid, d, dst_row_stride, dst_frame_stride);
     break;
   default:

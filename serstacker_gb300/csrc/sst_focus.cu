@@ -4,7 +4,7 @@
  * (core/proc/inpaint/linear_interpolation_inpaint.cc) on the GPU.
  *
  * add() works on batches of frames: planar FP32 conversion, the optional
- * hole filling (row and column scans, one thread per row / column, iterated
+ * hole filling (row and column scans, one warp per row / column, iterated
  * until no hole gains a value), build_laplacian_pyramid (core/proc/
  * laplacian_pyramid.cc:45-96; tap-table pyrDown / pyrUp, minimum size 8) for
  * every frame of the batch at once, the u8 mask pyramid (cv::buildPyramid)
@@ -61,15 +61,20 @@ __global__ void k_to_interleaved(const float * src, int w, int h, int cn, float 
 
 /* --- linear_interpolation_inpaint: rows / columns of hole runs --- */
 
-/* one thread per (frame, row) [rows] or (frame, column) [columns]: for each run of
- * holes, the values and distances of _interpolate_holes_h2 / _v2 */
-__global__ void k_inpaint_scan(const float * img, const uint8_t * mask, int w, int h, int cn, int nf, int rows,
-    float * out, float * dist)
+/* one warp per (frame, row) [rows] or (frame, column) [columns]: the values
+ * and distances of _interpolate_holes_h2 / _v2 for every hole of the line.
+ * Each lane takes a contiguous chunk of the line; the last valid position
+ * before its chunk and the first one after it come from a prefix max / suffix
+ * min over the lanes, so each hole run (which may span chunks) is filled from
+ * the same end points s and e as the sequential scan, with the same FP32
+ * operations. */
+__global__ void __launch_bounds__(256) k_inpaint_scan(const float * img, const uint8_t * mask, int w, int h, int cn,
+    int nf, int rows, float * out, float * dist)
 {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int wid = (int) ((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   const int lines = rows ? h : w, len = rows ? w : h;
-  if( t >= lines * nf ) return;
-  const int f = t / lines, line = t - f * lines;
+  if( wid >= lines * nf ) return;                       // the whole warp
+  const int f = wid / lines, line = wid - f * lines;
   const size_t plane = (size_t) w * h;
   const size_t step = rows ? 1 : (size_t) w;
   const size_t base = rows ? (size_t) line * w : (size_t) line;
@@ -77,39 +82,62 @@ __global__ void k_inpaint_scan(const float * img, const uint8_t * mask, int w, i
   const float * im = img + (size_t) f * cn * plane + base;
   float * o = out + (size_t) f * cn * plane + base;
   float * d = dist + (size_t) f * plane + base;
-  for( int start = 0; start < len; ) {
-    while ( start < len && m[(size_t) start * step] ) d[(size_t) start * step] = 0.f, ++start;
-    if( start >= len ) break;
-    int end = start + 1;
-    while ( end < len && !m[(size_t) end * step] ) ++end;
-    if( start > 0 && end < len ) {
-      const int s = start - 1, e = end;
-      const float scale = __fdiv_rn(1.0f, (float) (end - start));
-      for( int x = start; x < e; ++x ) {
-        d[(size_t) x * step] = (float) max(x - s, e - x);
+  const int chunk = (len + 31) / 32;
+  const int c0 = min(lane * chunk, len), c1 = min(c0 + chunk, len);
+  int lastv = -1, firstv = len;
+  for( int x = c0; x < c1; ++x ) {
+    if( m[(size_t) x * step] ) {
+      if( firstv == len ) firstv = x;
+      lastv = x;
+    }
+  }
+  int pre = lastv, suf = firstv;
+#pragma unroll
+  for( int k = 1; k < 32; k <<= 1 ) {
+    const int a = __shfl_up_sync(0xffffffffu, pre, k), b = __shfl_down_sync(0xffffffffu, suf, k);
+    if( lane >= k ) pre = max(pre, a);
+    if( lane + k < 32 ) suf = min(suf, b);
+  }
+  int before = __shfl_up_sync(0xffffffffu, pre, 1), after = __shfl_down_sync(0xffffffffu, suf, 1);
+  if( lane == 0 ) before = -1;
+  if( lane == 31 ) after = len;
+  int s = before;                                       // the last valid position before x
+  for( int x = c0; x < c1; ) {
+    if( m[(size_t) x * step] ) {
+      d[(size_t) x * step] = 0.f;
+      s = x++;
+      continue;
+    }
+    int pe = x + 1;
+    while ( pe < c1 && !m[(size_t) pe * step] ) ++pe;
+    const int e = pe < c1 ? pe : after;                 // the first valid position after the run
+    if( s >= 0 && e < len ) {
+      const float scale = __fdiv_rn(1.0f, (float) (e - s - 1));
+      for( int q = x; q < pe; ++q ) {
+        d[(size_t) q * step] = (float) max(q - s, e - q);
         for( int c = 0; c < cn; ++c ) {
           const float sv = im[c * plane + (size_t) s * step], ev = im[c * plane + (size_t) e * step];
           const float kk = __fmul_rn(__fsub_rn(ev, sv), scale);
-          o[c * plane + (size_t) x * step] = __fadd_rn(sv, __fmul_rn((float) (x - s), kk));
+          o[c * plane + (size_t) q * step] = __fadd_rn(sv, __fmul_rn((float) (q - s), kk));
         }
       }
     }
-    else if( start > 0 ) {
-      for( int x = start; x < len; ++x ) {
-        d[(size_t) x * step] = (float) (x - start + 1);
-        for( int c = 0; c < cn; ++c ) o[c * plane + (size_t) x * step] = im[c * plane + (size_t) (start - 1) * step];
+    else if( s >= 0 ) {
+      for( int q = x; q < pe; ++q ) {
+        d[(size_t) q * step] = (float) (q - s);
+        for( int c = 0; c < cn; ++c ) o[c * plane + (size_t) q * step] = im[c * plane + (size_t) s * step];
       }
     }
-    else if( end < len ) {
-      for( int x = start; x < end; ++x ) {
-        d[(size_t) x * step] = (float) (end - x);
-        for( int c = 0; c < cn; ++c ) o[c * plane + (size_t) x * step] = im[c * plane + (size_t) end * step];
+    else if( e < len ) {
+      for( int q = x; q < pe; ++q ) {
+        d[(size_t) q * step] = (float) (e - q);
+        for( int c = 0; c < cn; ++c ) o[c * plane + (size_t) q * step] = im[c * plane + (size_t) e * step];
       }
     }
     else {
-      for( int x = start; x < end; ++x ) d[(size_t) x * step] = 0.f;
+      for( int q = x; q < pe; ++q ) d[(size_t) q * step] = 0.f;
     }
-    start = end;
+    x = pe;
   }
 }
 
@@ -398,8 +426,8 @@ int inpaint_batch(float * img, uint8_t * mask, int w, int h, int cn, int nf, flo
   std::vector<int> filled(nf);
   for( int it = 0; it < w * h + 1; ++it ) {
     SST_FSCK(cudaMemsetAsync(counters, 0, nf * sizeof(int), st));
-    k_inpaint_scan<<<g1((size_t) h * nf), 256, 0, st>>>(img, mask, w, h, cn, nf, 1, ih, hd);
-    k_inpaint_scan<<<g1((size_t) w * nf), 256, 0, st>>>(img, mask, w, h, cn, nf, 0, iv, vd);
+    k_inpaint_scan<<<g1((size_t) h * nf * 32), 256, 0, st>>>(img, mask, w, h, cn, nf, 1, ih, hd);
+    k_inpaint_scan<<<g1((size_t) w * nf * 32), 256, 0, st>>>(img, mask, w, h, cn, nf, 0, iv, vd);
     k_inpaint_fill<<<g2(w, h, nf), 256, 0, st>>>(img, mask, ih, iv, hd, vd, w, h, cn, counters);
     SST_FSCK(cudaGetLastError());
     sst_internal_count_launches(3);

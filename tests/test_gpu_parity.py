@@ -324,3 +324,46 @@ def test_pipeline_focus_weights_match_oracle(gpu, oracle):
     ref_avg = S[both] / W[both]
     rel = np.abs(avg[both] - ref_avg) / np.maximum(np.abs(ref_avg), 0.01 * float(ref_avg.max()))
     assert rel.max() <= 1e-4, rel.max()
+
+
+def test_host_streamed_chunks_match_device_path(gpu, oracle):
+    """sst_stack_frames on host frames streams them in growing chunks (here
+    64, 128 and 108 frames of 300 with 128-frame staging): registration is
+    per frame, so parameters, statuses and rho equal the device-resident
+    call's bitwise; the stack differs only in where its compensated partial
+    sums are merged (1e-6 relative)."""
+    import torch
+    C = gpu
+    w, h, n = 160, 120, 300
+    sc = synth.Scene(w, h, 0.28 * min(w, h))
+    frames, _, _ = synth.make_sequence_np(sc, n, seed=17, kind="config1", dtype=np.uint16, gain=64.0,
+                                          blur_range=(0.8, 2.0))
+    ref = synth.reference_np(sc) * 64.0
+    scale = 1.0 / 65535.0
+    opts = C.default_options(method=1, maxlevel=3, max_iterations=40, epsx=0.01, minimum_image_size=16, min_rho=0.5)
+    results = []
+    for host in (False, True):
+        reg = C.c_ecch(opts)
+        reg.set_reference_image(ref.astype(np.float32), scale=scale)
+        reg.set_chunk_frames(128)
+        acc = C.c_weigthed_average(w, h)
+        if host:
+            out = C.stack_frames(reg, acc, frames, [3, 4], scale, weighting=1)
+        else:
+            dev = torch.from_numpy(frames.view(np.int16)).cuda()
+            outs = {"params": torch.zeros((n, 12), dtype=torch.float32, device="cuda"),
+                    "status": torch.zeros(n, dtype=torch.int32, device="cuda"),
+                    "rho": torch.zeros(n, dtype=torch.float32, device="cuda"),
+                    "weight": torch.zeros(n, dtype=torch.float32, device="cuda")}
+            C.stack_frames(reg, acc, dev.data_ptr(), [3, 4], scale, weighting=1, on_device=True, n=n, width=w,
+                           height=h, depth=C.DEPTH_U16, row_stride=w * 2, frame_stride=w * h * 2, outputs=outs)
+            torch.cuda.synchronize()
+            out = {k: v.cpu().numpy() for k, v in outs.items()}
+        avg, mask = acc.compute()
+        results.append((out, avg, mask))
+    (od, ad, md), (oh, ah, mh) = results
+    for k in ("params", "status", "rho", "weight"):
+        assert np.array_equal(od[k], oh[k]), k
+    assert np.array_equal(md, mh)
+    sel = md > 0
+    assert np.abs(ad[sel] - ah[sel]).max() <= 1e-6 * np.abs(ad[sel]).max()
