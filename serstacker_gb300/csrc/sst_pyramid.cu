@@ -9,11 +9,11 @@
  *   IC Gauss-Newton matrix        : ecc_compute_hessian_matrix (ecc2.cc:295-321) of the
  *                                   steepest-descent images (c_image_transform.cc)
  *
- * All kernels are batched over frames (grid.z) and stage halo'd tiles in
- * shared memory; each input pixel is read from HBM once per kernel.
+ * All kernels are batched over frames; each input pixel is read from HBM
+ * once per kernel (the fused level 0 + 1 pass re-reads only its strips'
+ * nine-row halos, from L2 mostly).
  */
 #include "sst_engine.cuh"
-#include "sst_tma.cuh"
 
 namespace sst {
 
@@ -302,337 +302,310 @@ cudaError_t launch_pyrdown_ragged(const float * src, const RaggedImg * jobs, int
 
 /* ------------------------- fused convert + pre-smooth + first pyrDown */
 
-/* One CTA per 128 x 32 level-0 tile (and its 64 x 16 level-1 tile). One TMA
- * copy stages the raw input window (tile + 2 + R rows above and below, and
- * enough columns for the smoothed window). The window is converted to scaled
- * FP32 once. The separable 7-tap Gaussian gives the smoothed window S: 36
- * rows (level-0 y = ty0 - 2 ... ty0 + 33) by 136 columns (x = tx0 - 4 ...
- * tx0 + 131, so the tile's own cells start on a 16-byte boundary). Its tile
- * part is stored as level 0; the 5-tap pyrDown of S (rows first, as pyrDown)
- * gives level 1. So level 0 is written once and never read back.
- * Borders: out-of-image input cells take the nearest in-image cell
- * (REPLICATE, as sepFilter2D). Out-of-image cells of S that pyrDown taps
- * reach take the reflected cell (REFLECT_101, as pyrDown). */
-constexpr int FP_TX = 128, FP_TY = 32, FP_R = 3;
-constexpr int FP_SW = FP_TX + 8, FP_SH = FP_TY + 4;       // smoothed window
-constexpr int FP_IH = FP_SH + 2 * FP_R;                   // input rows
+/* One warp per strip of PS_TX = 120 level-0 columns by BH rows (and the strip's
+ * 60 x BH/2 level-1 cells). Lane l owns the four smoothed columns
+ * x0 = tx0 - 4 + 4l ... x0 + 3 and sweeps the strip's input rows top to bottom:
+ *  - each input row (loaded PS_D rows ahead into registers) is converted and
+ *    scaled; the 7-tap horizontal Gaussian reads the neighbouring lanes'
+ *    cells through a per-warp row buffer in shared memory;
+ *  - the vertical Gaussian adds each horizontal row into the seven smoothed
+ *    rows it reaches (a ring of seven float4 accumulators, taps in order), so
+ *    the smoothed row S of input row r is complete six rows later;
+ *  - S is stored as level 0 where it lies in the strip, and its horizontal
+ *    5-tap pyrDown (two level-1 columns per lane) enters a ring of five rows,
+ *    from which every second S row gives one level-1 row (rows first, as
+ *    pyrDown).
+ * Lanes 0 and 31 compute halo columns only. Level 0 is written once and never
+ * read back; no barrier, wait or shared-memory pass involves more than a warp.
+ * Borders: input cells outside the image take the nearest in-image cell
+ * (REPLICATE, as sepFilter2D); cells of S that pyrDown taps reach outside the
+ * image take the reflected cell (REFLECT_101, as pyrDown): columns in the row
+ * buffer, rows in the ring. */
+constexpr int PS_TX = 120;        // level-0 columns per strip
+constexpr int PS_D = 7;           // input rows in flight per lane
+constexpr int PS_BUF = 136;       // row buffer: x = tx0 - 8 ... tx0 + 127
+constexpr int PS_WARPS = 4;       // warps (strips) per CTA
 
-template<typename T>
-struct fp_geom {
-  static constexpr int VEC = 16 / (int) sizeof(T);                          // elements per 16 bytes
-  static constexpr int XA = VEC >= 7 ? VEC : 8;                            // left margin: >= 4 + R, 16 B, 4 floats
-  static constexpr int IW = (XA + FP_SW + VEC - 1) / VEC * VEC;            // input row (16-byte multiple)
-  static constexpr size_t IN_BYTES = ((size_t) IW * FP_IH * sizeof(T) + 127) / 128 * 128;
-  static constexpr size_t F_BYTES = ((size_t) IW * FP_IH * sizeof(float) + 127) / 128 * 128;
-  static constexpr size_t H_BYTES = (size_t) FP_IH * FP_SW * sizeof(float);
-  static constexpr size_t SMEM = 128 + 2 * IN_BYTES + F_BYTES + H_BYTES + 32;   // two input windows
-  static_assert((size_t) FP_SH * FP_SW * sizeof(float) <= F_BYTES, "S aliases the converted window");
-  static_assert(XA % 4 == 0 && XA >= 4 + FP_R, "left margin");
+template<typename T> struct ps_raw;                       // a lane's four input cells as loaded
+template<> struct ps_raw<uint8_t> { typedef uint32_t type; };
+template<> struct ps_raw<uint16_t> { typedef uint2 type; };
+template<> struct ps_raw<float> { typedef float4 type; };
+
+__device__ __forceinline__ uint32_t ps_load(const uint8_t * row, int x) { return __ldg((const uint32_t *) (row + x)); }
+__device__ __forceinline__ uint2 ps_load(const uint16_t * row, int x) { return __ldg((const uint2 *) (row + x)); }
+__device__ __forceinline__ float4 ps_load(const float * row, int x) { return __ldg((const float4 *) (row + x)); }
+
+/* the four cells x ... x + 3 with each column clamped into the image */
+__device__ __forceinline__ uint32_t ps_load_clamped(const uint8_t * row, int x, int w)
+{
+  uint32_t q = 0;
+#pragma unroll
+  for( int k = 0; k < 4; ++k ) q |= (uint32_t) __ldg(row + clampi(x + k, 0, w - 1)) << (8 * k);
+  return q;
+}
+
+__device__ __forceinline__ uint2 ps_load_clamped(const uint16_t * row, int x, int w)
+{
+  uint32_t e[4];
+#pragma unroll
+  for( int k = 0; k < 4; ++k ) e[k] = __ldg(row + clampi(x + k, 0, w - 1));
+  return make_uint2(e[0] | (e[1] << 16), e[2] | (e[3] << 16));
+}
+
+__device__ __forceinline__ float4 ps_load_clamped(const float * row, int x, int w)
+{
+  return make_float4(__ldg(row + clampi(x, 0, w - 1)), __ldg(row + clampi(x + 1, 0, w - 1)),
+      __ldg(row + clampi(x + 2, 0, w - 1)), __ldg(row + clampi(x + 3, 0, w - 1)));
+}
+
+__device__ __forceinline__ float4 ps_convert(uint32_t q, float s)
+{
+  return make_float4((float) (q & 0xffu) * s, (float) ((q >> 8) & 0xffu) * s, (float) ((q >> 16) & 0xffu) * s,
+      (float) (q >> 24) * s);
+}
+
+__device__ __forceinline__ float4 ps_convert(uint2 q, float s)
+{
+  return make_float4((float) (q.x & 0xffffu) * s, (float) (q.x >> 16) * s, (float) (q.y & 0xffffu) * s,
+      (float) (q.y >> 16) * s);
+}
+
+__device__ __forceinline__ float4 ps_convert(float4 q, float s)
+{
+  return make_float4(q.x * s, q.y * s, q.z * s, q.w * s);
+}
+
+/* pyrDown's [1 4 6 4 1] / 16 of five taps */
+__device__ __forceinline__ float pyr5f(float a, float b, float c, float d, float e)
+{
+  return fmaf(c, 0.375f, fmaf(a + e, 0.0625f, (b + d) * 0.25f));
+}
+
+__device__ __forceinline__ float4 hgauss4(const float (&g)[7], const float (&v)[12])
+{
+  float o[4];
+#pragma unroll
+  for( int c = 0; c < 4; ++c ) {
+    float a = 0.f;
+#pragma unroll
+    for( int i = 0; i < 7; ++i ) a = fmaf(g[i], v[c + 1 + i], a);
+    o[c] = a;
+  }
+  return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+__device__ __forceinline__ float4 fma4(float g, float4 v, float4 a)
+{
+  return make_float4(fmaf(g, v.x, a.x), fmaf(g, v.y, a.y), fmaf(g, v.z, a.z), fmaf(g, v.w, a.w));
+}
+
+/* Strips of one launch: the interior strips (every lane's cells inside the
+ * image: 8 <= tx0 and tx0 + 124 <= w), or the edge strips (the first one and
+ * those from `first` on). Two launches keep each kernel's loop free of the
+ * other's clamped loads. */
+struct StripSet {
+  int first, count;   // interior: strips first ... first + count - 1; edge: 0, then first ... first + count - 2
+  int edge;
 };
 
-/* eight consecutive elements (16-byte aligned for u16 / f32, 8-byte for u8) as floats */
-__device__ __forceinline__ void load8(const uint16_t * p, float (&v)[8])
+template<typename T, int BH, bool EDGE>
+__global__ void __launch_bounds__(32 * PS_WARPS, 4) k_convert_pyr1(const T * __restrict__ src, size_t row_elems,
+    size_t frame_elems, int w, int h, StripSet ss, int gy, int n, float scale, const float * __restrict__ gk,
+    float * dst0, float * dst1, int dw, int dh, size_t dst_stride, int vec0, int vec1)
 {
-  const uint4 q = *reinterpret_cast<const uint4 *>(p);
-  const uint32_t u[4] = { q.x, q.y, q.z, q.w };
+  static_assert(BH % 2 == 0, "level-1 rows pair level-0 rows");
+  constexpr int NR = BH + 9;                                  // input rows of a strip
+  __shared__ __align__(16) float s_buf[PS_WARPS][3][PS_BUF];  // per warp: two input rows, one S row
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long item = (long long) blockIdx.x * PS_WARPS + warp;
+  const int per_frame = ss.count * gy;
+  if( item >= (long long) per_frame * n ) return;             // uniform over the warp
+  const int z = (int) (item / per_frame), rem = (int) (item - (long long) z * per_frame);
+  const int by = rem / ss.count, k = rem - by * ss.count;
+  const int bx = !EDGE ? ss.first + k : k == 0 ? 0 : ss.first + k - 1;
+  const int tx0 = bx * PS_TX, ty0 = by * BH;
+  const int x0 = tx0 - 4 + 4 * lane;
+  const int xe = max(tx0 - 5, 0);                             // lane 0's extra input cell
+  const T * frame = src + (size_t) z * frame_elems;
+  float * rin = s_buf[warp][0];
+  float * srow = s_buf[warp][2];
+  for( int q = lane; q < 3 * PS_BUF; q += 32 ) rin[q] = 0.f;  // cells no lane writes are read as halo
+  float g[7];
 #pragma unroll
-  for( int k = 0; k < 4; ++k ) v[2 * k] = (float) (u[k] & 0xffffu), v[2 * k + 1] = (float) (u[k] >> 16);
-}
+  for( int i = 0; i < 7; ++i ) g[i] = __ldg(gk + i);
 
-__device__ __forceinline__ void load8(const uint8_t * p, float (&v)[8])
-{
-  const uint2 q = *reinterpret_cast<const uint2 *>(p);
+  // input rows ty0 - 5 + r, r = 0 ... NR - 1 (clamped into the image), PS_D in flight
+  typename ps_raw<T>::type q[PS_D];
+  T qe[PS_D];
+  const T * rowp = frame;
 #pragma unroll
-  for( int k = 0; k < 4; ++k ) v[k] = (float) ((q.x >> (8 * k)) & 0xffu), v[4 + k] = (float) ((q.y >> (8 * k)) & 0xffu);
-}
-
-__device__ __forceinline__ void load8(const float * p, float (&v)[8])
-{
-  const float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 4);
-  v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
-}
-
-__device__ __forceinline__ float4 pyr5(float4 a, float4 b, float4 c, float4 d, float4 e)
-{
-  float4 r;
-  r.x = (a.x + e.x) * 0.0625f + (b.x + d.x) * 0.25f + c.x * 0.375f;
-  r.y = (a.y + e.y) * 0.0625f + (b.y + d.y) * 0.25f + c.y * 0.375f;
-  r.z = (a.z + e.z) * 0.0625f + (b.z + d.z) * 0.25f + c.z * 0.375f;
-  r.w = (a.w + e.w) * 0.0625f + (b.w + d.w) * 0.25f + c.w * 0.375f;
-  return r;
-}
-
-/* Persistent: each CTA walks (frame, tile) items frame-major, and the input
- * window of its next item is copied into the second buffer while the current
- * item computes. */
-template<typename T>
-__global__ void __launch_bounds__(256, 3) k_convert_pyr1(const __grid_constant__ CUtensorMap tmap, int w, int h,
-    int gx, int gy, int n, float scale, const float * __restrict__ gk, float * dst0, float * dst1, int dw, int dh,
-    size_t dst_stride, int * err)
-{
-  using G = fp_geom<T>;
-  constexpr int IW = G::IW;
-  constexpr int IN_ELEMS = (int) (G::IN_BYTES / sizeof(T));
-  extern __shared__ unsigned char fp_smem[];
-  unsigned char * base = (unsigned char *) (((uintptr_t) fp_smem + 127) & ~(uintptr_t) 127);
-  T * s_in0 = (T *) base;                                         // two FP_IH x IW raw input windows
-  float * s_f = (float *) (base + 2 * G::IN_BYTES);               // FP_IH x IW scaled FP32; then S: FP_SH x FP_SW
-  float * s_h = (float *) (base + 2 * G::IN_BYTES + G::F_BYTES);  // FP_IH x FP_SW horizontal pass; then pyrDown rows
-  float * s_S = s_f;
-  uint64_t * bar = (uint64_t *) (base + 2 * G::IN_BYTES + G::F_BYTES + G::H_BYTES);
-  uint32_t * s_infl = (uint32_t *) (bar + 2);                     // copies in flight, kept by thread 0
-  int * s_gaveup = (int *) (s_infl + 1);                          // [2]: a wait gave up on this buffer
-
-  const int per_frame = gx * gy, items = per_frame * n;
-  if( (int) blockIdx.x >= items ) return;                         // uniform over the CTA
-  if( threadIdx.x == 0 ) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    *s_infl = 0u;
-    s_gaveup[0] = s_gaveup[1] = 0;
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  for( int i = 0; i < PS_D; ++i ) {
+    rowp = frame + (size_t) clampi(ty0 - 5 + i, 0, h - 1) * row_elems;
+    q[i] = EDGE ? ps_load_clamped(rowp, x0, w) : ps_load(rowp, x0);
+    qe[i] = lane == 0 ? __ldg(rowp + xe) : (T) 0;
   }
-  __syncthreads();
-  if( threadIdx.x == 0 ) {
-    const int z = blockIdx.x / per_frame, rem = blockIdx.x - z * per_frame, by = rem / gx, bx = rem - by * gx;
-    mbar_expect_tx(&bar[0], IW * FP_IH * sizeof(T));
-    tma_load_3d(s_in0, &tmap, bx * FP_TX - G::XA, by * FP_TY - 2 - FP_R, z, &bar[0]);
-    inflight_issued(s_infl, 0, 0u);
-  }
-  float g[2 * FP_R + 1];
+  float4 A[7];
 #pragma unroll
-  for( int i = 0; i <= 2 * FP_R; ++i ) g[i] = __ldg(gk + i);
-  uint32_t phases = 0u;
-  bool timed_out = false, stop = false;
-  int b = 0;
-  for( int item = blockIdx.x; item < items; item += gridDim.x, b ^= 1 ) {
-    // the next item's window goes into the other buffer, last read by the
-    // convert pass two items ago (every thread is past the barrier after it);
-    // the previous item's wait flag was written before that item's barriers
-    stop = stop || s_gaveup[b ^ 1];
-    const int nitem = item + gridDim.x;
-    if( threadIdx.x == 0 && nitem < items && !stop ) {
-      const int z = nitem / per_frame, rem = nitem - z * per_frame, by = rem / gx, bx = rem - by * gx;
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_expect_tx(&bar[b ^ 1], IW * FP_IH * sizeof(T));
-      tma_load_3d(s_in0 + (b ^ 1) * IN_ELEMS, &tmap, bx * FP_TX - G::XA, by * FP_TY - 2 - FP_R, z, &bar[b ^ 1]);
-      inflight_issued(s_infl, b ^ 1, (phases >> (b ^ 1)) & 1u);
-    }
-    const int z = item / per_frame, rem = item - z * per_frame, by = rem / gx, bx = rem - by * gx;
-    const int tx0 = bx * FP_TX, ty0 = by * FP_TY;
-    const int wx0 = tx0 - G::XA, wy0 = ty0 - 2 - FP_R;            // input window origin
-    const T * s_in = s_in0 + b * IN_ELEMS;
-    if( !stop ) {
-      if( !mbar_wait_bounded(&bar[b], (phases >> b) & 1u) ) timed_out = true, s_gaveup[b] = 1;
-      else if( threadIdx.x == 0 ) inflight_landed(s_infl, b);
-      phases ^= 1u << b;
-    }
+  for( int i = 0; i < 7; ++i ) A[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 p0 = make_float2(0.f, 0.f), p1 = p0, p2 = p0, p3 = p0;   // level-1 ring: S rows s - 4 ... s - 1
+  // level 0: S rows s = 2 ... s_end0 - 1 (y = ty0 - 2 + s) of lanes 1 ... 30 inside the image
+  const bool st0 = lane >= 1 && lane <= 30 && x0 < w;
+  const bool st0v = st0 && vec0 && x0 + 3 < w;
+  const int s_end0 = min(BH + 2, h - ty0 + 2);
+  float * o0 = dst0 + (size_t) z * dst_stride + (size_t) ty0 * w + x0;   // row y = ty0 (s = 2)
+  // level 1: rows i = 0 ... i_end - 1 (y1 = ty0 / 2 + i), columns x1, x1 + 1
+  const int x1 = tx0 / 2 + 2 * lane - 2;
+  const bool st1 = lane >= 1 && lane <= 30 && x1 < dw;
+  const bool st1v = st1 && vec1 && x1 + 1 < dw;
+  const int i_end = min(BH / 2, dh - ty0 / 2);
+  float * o1 = dst1 + (size_t) z * dst_stride + (size_t) (ty0 / 2) * dw + x1;
+  __syncwarp();
 
-    // convert + scale; where the window leaves the image, each cell takes the
-    // nearest in-image cell (REPLICATE)
-    const bool edge_in = wx0 < 0 || wx0 + IW > w || wy0 < 0 || wy0 + FP_IH > h;
-    if( !edge_in ) {
-      for( int q = threadIdx.x; q < FP_IH * (IW / 8); q += 256 ) {
-        const int r = q / (IW / 8), c = (q - r * (IW / 8)) * 8;
-        float v[8];
-        load8(s_in + r * IW + c, v);
-        float * o = s_f + r * IW + c;
-        *reinterpret_cast<float4 *>(o) = make_float4(v[0] * scale, v[1] * scale, v[2] * scale, v[3] * scale);
-        *reinterpret_cast<float4 *>(o + 4) = make_float4(v[4] * scale, v[5] * scale, v[6] * scale, v[7] * scale);
+#pragma unroll 1
+  for( int r0 = 0; r0 < NR; r0 += 7 ) {
+#pragma unroll
+    for( int j = 0; j < 7; ++j ) {
+      const int r = r0 + j;
+      if( r >= NR ) break;
+      // convert this row's cells, then refill the slot with row r + PS_D
+      const float4 f = ps_convert(q[j], scale);
+      const float fe = (float) qe[j] * scale;
+      if( r + PS_D < NR ) {
+        const int yl = ty0 - 5 + r + PS_D;
+        if( yl >= 1 && yl <= h - 1 ) rowp += row_elems;
+        q[j] = EDGE ? ps_load_clamped(rowp, x0, w) : ps_load(rowp, x0);
+        if( lane == 0 ) qe[j] = __ldg(rowp + xe);
       }
-    }
-    else {
-      for( int q = threadIdx.x; q < FP_IH * IW; q += 256 ) {
-        const int r = q / IW, c = q - r * IW;
-        const int rs = clampi(wy0 + r, 0, h - 1) - wy0, cs = clampi(wx0 + c, 0, w - 1) - wx0;
-        s_f[q] = (float) s_in[rs * IW + cs] * scale;
+      // horizontal Gaussian through the row buffer (alternate buffers per row)
+      float * rb = rin + (r & 1) * PS_BUF;
+      *reinterpret_cast<float4 *>(rb + 4 * lane + 4) = f;
+      if( lane == 0 ) rb[3] = fe;
+      __syncwarp();
+      const float4 lo = *reinterpret_cast<const float4 *>(rb + 4 * lane);
+      const float4 hi = *reinterpret_cast<const float4 *>(rb + 4 * lane + 8);
+      const float v[12] = { lo.x, lo.y, lo.z, lo.w, f.x, f.y, f.z, f.w, hi.x, hi.y, hi.z, hi.w };
+      const float4 H = hgauss4(g, v);
+      // vertical Gaussian: smoothed row r - i takes tap i in slot (j - i) mod 7;
+      // tap 0 starts the row's sum; rows outside 0 ... NR - 7 are never read
+#pragma unroll
+      for( int i = 0; i < 7; ++i ) {
+        const int sl = (j - i + 7) % 7;
+        A[sl] = i == 0 ? fma4(g[0], H, make_float4(0.f, 0.f, 0.f, 0.f)) : fma4(g[i], H, A[sl]);
       }
-    }
-    __syncthreads();
-
-    // horizontal Gaussian: S column c (x = tx0 - 4 + c) reads converted columns
-    // c + XA - 7 ... c + XA - 1; four columns per item from three 16-byte loads
-    for( int q = threadIdx.x; q < FP_IH * (FP_SW / 4); q += 256 ) {
-      const int r = q / (FP_SW / 4), c0 = (q - r * (FP_SW / 4)) * 4;
-      const float * p = s_f + r * IW + c0 + G::XA - 8;
-      float v[12];
-  #pragma unroll
-      for( int k = 0; k < 3; ++k ) {
-        const float4 t = *reinterpret_cast<const float4 *>(p + 4 * k);
-        v[4 * k] = t.x, v[4 * k + 1] = t.y, v[4 * k + 2] = t.z, v[4 * k + 3] = t.w;
-      }
-      float o[4];
-  #pragma unroll
-      for( int j = 0; j < 4; ++j ) {
-        float a = 0.f;
-  #pragma unroll
-        for( int i = 0; i <= 2 * FP_R; ++i ) a = fmaf(g[i], v[j + 1 + i], a);
-        o[j] = a;
-      }
-      *reinterpret_cast<float4 *>(s_h + r * FP_SW + c0) = make_float4(o[0], o[1], o[2], o[3]);
-    }
-    __syncthreads();
-
-    // vertical Gaussian: S row s (y = ty0 - 2 + s) reads rows s ... s + 2R of the
-    // horizontal pass; 4 rows x 4 columns per item (S overwrites the converted window)
-    for( int q = threadIdx.x; q < (FP_SH / 4) * (FP_SW / 4); q += 256 ) {
-      const int rg = q / (FP_SW / 4), c0 = (q - rg * (FP_SW / 4)) * 4, s0 = rg * 4;
-      float4 v[4 + 2 * FP_R];
-  #pragma unroll
-      for( int i = 0; i < 4 + 2 * FP_R; ++i ) v[i] = *reinterpret_cast<const float4 *>(s_h + (s0 + i) * FP_SW + c0);
-  #pragma unroll
-      for( int j = 0; j < 4; ++j ) {
-        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-  #pragma unroll
-        for( int i = 0; i <= 2 * FP_R; ++i ) {
-          a.x = fmaf(g[i], v[j + i].x, a.x), a.y = fmaf(g[i], v[j + i].y, a.y);
-          a.z = fmaf(g[i], v[j + i].z, a.z), a.w = fmaf(g[i], v[j + i].w, a.w);
+      if( r < 6 ) continue;
+      // smoothed row s complete (y = ty0 - 2 + s)
+      const int s = r - 6;
+      const float4 S = A[(j + 1) % 7];
+      if( s >= 2 && s < s_end0 ) {
+        if( st0v ) *reinterpret_cast<float4 *>(o0) = S;
+        else if( st0 ) {
+          o0[0] = S.x;
+          if( x0 + 1 < w ) o0[1] = S.y;
+          if( x0 + 2 < w ) o0[2] = S.z;
+          if( x0 + 3 < w ) o0[3] = S.w;
         }
-        *reinterpret_cast<float4 *>(s_S + (s0 + j) * FP_SW + c0) = a;
+        o0 += w;
       }
-    }
-    __syncthreads();
-
-    // level 0: the tile's cells of S (rows 2 ... 33, columns 4 ... 131)
-    float * out0 = dst0 + (size_t) z * dst_stride;
-    const bool vec0 = (w & 3) == 0;
-    for( int q = threadIdx.x; q < FP_TY * (FP_TX / 4); q += 256 ) {
-      const int i = q / (FP_TX / 4), k = q - i * (FP_TX / 4);
-      const int y = ty0 + i, x = tx0 + 4 * k;
-      if( y >= h || x >= w ) continue;
-      const float4 v = *reinterpret_cast<const float4 *>(s_S + (i + 2) * FP_SW + 4 + 4 * k);
-      float * o = out0 + (size_t) y * w + x;
-      if( vec0 && x + 3 < w ) *reinterpret_cast<float4 *>(o) = v;
-      else {
-        o[0] = v.x;
-        if( x + 1 < w ) o[1] = v.y;
-        if( x + 2 < w ) o[2] = v.z;
-        if( x + 3 < w ) o[3] = v.w;
+      // horizontal pyrDown of S: level-1 columns x1 (taps x0 - 2 ... x0 + 2) and
+      // x1 + 1 (taps x0 ... x0 + 4)
+      *reinterpret_cast<float4 *>(srow + 4 * lane + 4) = S;
+      __syncwarp();
+      float4 c = S;
+      if( EDGE ) {
+        if( lane < 4 ) {
+          const int x = lane < 2 ? lane - 2 : w + lane - 2, kk = x - tx0 + 8;
+          if( kk >= 0 && kk < PS_BUF ) srow[kk] = srow[reflect101(x, w) - tx0 + 8];
+        }
+        __syncwarp();
+        c = *reinterpret_cast<const float4 *>(srow + 4 * lane + 4);
       }
-    }
-
-    // REFLECT_101 the cells of S that pyrDown taps reach outside the image
-    // (x in {-2, -1, w, w + 1}, then y likewise), from in-image cells of S
-    const bool edge_s = tx0 == 0 || ty0 == 0 || tx0 + FP_TX + 4 > w || ty0 + FP_TY + 2 > h;
-    if( edge_s ) {
-      for( int q = threadIdx.x; q < FP_SH * 4; q += 256 ) {
-        const int s = q >> 2, k = q & 3;
-        const int x = k < 2 ? k - 2 : w + k - 2, c = x - (tx0 - 4);
-        if( c >= 0 && c < FP_SW ) s_S[s * FP_SW + c] = s_S[s * FP_SW + clampi(reflect101(x, w) - (tx0 - 4), 0, FP_SW - 1)];
+      const float2 l = *reinterpret_cast<const float2 *>(srow + 4 * lane + 2);
+      const float rr = srow[4 * lane + 8];
+      const float2 p = make_float2(pyr5f(l.x, l.y, c.x, c.y, c.z), pyr5f(c.x, c.y, c.z, c.w, rr));
+      if( s & 1 ) {
+        p3 = p;
+        continue;
       }
-      __syncthreads();
-      for( int q = threadIdx.x; q < 4 * FP_SW; q += 256 ) {
-        const int k = q / FP_SW, c = q - k * FP_SW;
-        const int y = k < 2 ? k - 2 : h + k - 2, s = y - (ty0 - 2);
-        if( s >= 0 && s < FP_SH ) s_S[s * FP_SW + c] = s_S[clampi(reflect101(y, h) - (ty0 - 2), 0, FP_SH - 1) * FP_SW + c];
+      if( s >= 4 ) {
+        // level-1 row i = (s - 4) / 2 at y = ty0 + 2i from S rows s - 4 ... s (REFLECT_101 rows)
+        const int i = (s - 4) >> 1, yy = ty0 + 2 * i;
+        float2 a = p0, b = p1, d = p3, e = p;
+        if( yy == 0 || yy + 2 >= h ) {
+          if( yy == 0 ) a = e, b = d;
+          if( yy + 2 == h ) e = p2;
+          if( yy + 1 == h ) d = b, e = a;
+        }
+        if( i < i_end ) {
+          const float2 o = make_float2(pyr5f(a.x, b.x, p2.x, d.x, e.x), pyr5f(a.y, b.y, p2.y, d.y, e.y));
+          if( st1v ) *reinterpret_cast<float2 *>(o1) = o;
+          else if( st1 ) {
+            o1[0] = o.x;
+            if( x1 + 1 < dw ) o1[1] = o.y;
+          }
+          o1 += dw;
+        }
       }
-    }
-    __syncthreads();
-
-    // pyrDown [1 4 6 4 1] / 16, rows first (as pyrDown): level-1 column j
-    // (x = tx0 + 2j) reads S columns 2j + 2 ... 2j + 6; four columns per item
-    constexpr int TX1 = FP_TX / 2, TY1 = FP_TY / 2;
-    float * s_p = s_h;                                              // FP_SH x TX1
-    for( int q = threadIdx.x; q < FP_SH * (TX1 / 4); q += 256 ) {
-      const int s = q / (TX1 / 4), k = q - s * (TX1 / 4);
-      const float * p = s_S + s * FP_SW + 8 * k;
-      float v[16];
-  #pragma unroll
-      for( int m = 0; m < 4; ++m ) {
-        const float4 t = *reinterpret_cast<const float4 *>(p + 4 * m);
-        v[4 * m] = t.x, v[4 * m + 1] = t.y, v[4 * m + 2] = t.z, v[4 * m + 3] = t.w;
-      }
-      float o[4];
-  #pragma unroll
-      for( int m = 0; m < 4; ++m ) {
-        const float * a = v + 2 * m + 2;
-        o[m] = (a[0] + a[4]) * 0.0625f + (a[1] + a[3]) * 0.25f + a[2] * 0.375f;
-      }
-      *reinterpret_cast<float4 *>(s_p + s * TX1 + 4 * k) = make_float4(o[0], o[1], o[2], o[3]);
-    }
-    __syncthreads();
-    // then columns: level-1 row i (y = ty0 + 2i) reads rows 2i ... 2i + 4
-    float * out1 = dst1 + (size_t) z * dst_stride;
-    const bool vec1 = (dw & 3) == 0;
-    for( int q = threadIdx.x; q < TY1 * (TX1 / 4); q += 256 ) {
-      const int i = q / (TX1 / 4), k = q - i * (TX1 / 4);
-      const int y1 = ty0 / 2 + i, x1 = tx0 / 2 + 4 * k;
-      if( y1 >= dh || x1 >= dw ) continue;
-      const float * p = s_p + (2 * i) * TX1 + 4 * k;
-      const float4 o = pyr5(*reinterpret_cast<const float4 *>(p), *reinterpret_cast<const float4 *>(p + TX1),
-          *reinterpret_cast<const float4 *>(p + 2 * TX1), *reinterpret_cast<const float4 *>(p + 3 * TX1),
-          *reinterpret_cast<const float4 *>(p + 4 * TX1));
-      float * d = out1 + (size_t) y1 * dw + x1;
-      if( vec1 && x1 + 3 < dw ) *reinterpret_cast<float4 *>(d) = o;
-      else {
-        d[0] = o.x;
-        if( x1 + 1 < dw ) d[1] = o.y;
-        if( x1 + 2 < dw ) d[2] = o.z;
-        if( x1 + 3 < dw ) d[3] = o.w;
-      }
+      p0 = p2, p1 = p3, p2 = p;
     }
   }
-  if( threadIdx.x == 0 ) inflight_drain(s_infl, bar);
-  if( timed_out && err ) atomicExch(err, 1);
 }
 
 template<typename T>
-static cudaError_t launch_fp(const CUtensorMap & map, int n, int w, int h, float scale, const float * gk, float * dst0,
-    float * dst1, int dw, int dh, size_t dst_stride, int * err, cudaStream_t st)
+static cudaError_t launch_fp(const void * src, size_t row_stride, size_t frame_stride, int n, int w, int h, float scale,
+    const float * gk, float * dst0, float * dst1, int dw, int dh, size_t dst_stride, cudaStream_t st)
 {
-  static int slots = 0;                       // resident CTAs on the device
-  if( !slots ) {
-    cudaError_t e = cudaFuncSetAttribute(k_convert_pyr1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) fp_geom<T>::SMEM);
+  constexpr int BH = 64;
+  const int gx = (w + PS_TX - 1) / PS_TX, gy = (h + BH - 1) / BH;
+  // interior strips: 1 ... bmin - 1 (bmin = the first strip with tx0 + 124 > w)
+  const int bmin = w >= 124 ? std::min(gx, (w - 124) / PS_TX + 1) : 1;
+  const StripSet in = { 1, std::max(0, bmin - 1), 0 };
+  const StripSet ed = { bmin, 1 + (gx - bmin), 1 };
+  const int vec0 = (w & 3) == 0 && (dst_stride & 3) == 0 && ((uintptr_t) dst0 & 15) == 0;
+  const int vec1 = (dw & 1) == 0 && (dst_stride & 1) == 0 && ((uintptr_t) dst1 & 7) == 0;
+  for( const StripSet & ss : { in, ed } ) {
+    if( ss.count <= 0 ) continue;
+    const long long items = (long long) ss.count * gy * n;
+    const long long blocks = (items + PS_WARPS - 1) / PS_WARPS;
+    if( blocks > (1ll << 30) ) return cudaErrorInvalidValue;
+    if( ss.edge ) k_convert_pyr1<T, BH, true><<<(unsigned) blocks, 32 * PS_WARPS, 0, st>>>((const T *) src,
+        row_stride / sizeof(T), frame_stride / sizeof(T), w, h, ss, gy, n, scale, gk, dst0, dst1, dw, dh, dst_stride,
+        vec0, vec1);
+    else k_convert_pyr1<T, BH, false><<<(unsigned) blocks, 32 * PS_WARPS, 0, st>>>((const T *) src,
+        row_stride / sizeof(T), frame_stride / sizeof(T), w, h, ss, gy, n, scale, gk, dst0, dst1, dw, dh, dst_stride,
+        vec0, vec1);
+    const cudaError_t e = cudaGetLastError();
     if( e != cudaSuccess ) return e;
-    int dev = 0, sms = 0, per_sm = 0;
-    if( (e = cudaGetDevice(&dev)) != cudaSuccess ) return e;
-    if( (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ) return e;
-    if( (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_convert_pyr1<T>, 256, fp_geom<T>::SMEM)) != cudaSuccess )
-      return e;
-    slots = sms * (per_sm > 0 ? per_sm : 1);
   }
-  const int gx = (w + FP_TX - 1) / FP_TX, gy = (h + FP_TY - 1) / FP_TY;
-  const long long items = (long long) gx * gy * n;
-  if( items > (1ll << 30) ) return cudaErrorInvalidValue;
-  const int grid = (int) (items < slots ? items : slots);
-  k_convert_pyr1<T><<<grid, 256, fp_geom<T>::SMEM, st>>>(map, w, h, gx, gy, n, scale, gk, dst0, dst1, dw, dh, dst_stride, err);
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 /* Level 0 and level 1 of n frames in one pass when the pre-smoothing is the
- * 7-tap Gaussian and the frames meet the TMA layout rules; *done = false
- * (nothing launched) otherwise, and the caller builds the levels separately. */
+ * 7-tap Gaussian and the rows allow the lanes' vector loads (base and strides
+ * multiples of four cells); *done = false (nothing launched) otherwise, and
+ * the caller builds the levels separately. */
 cudaError_t launch_convert_pyr1(const void * src, int depth, int n, int w, int h, size_t row_stride,
     size_t frame_stride, double scale, const float * gk, int ksize, float * dst0, float * dst1, int dw, int dh,
     size_t dst_stride, int * err, cudaStream_t st, bool * done)
 {
+  (void) err;                                   // the pass holds no waits
   *done = false;
-  if( !gk || ksize != 2 * FP_R + 1 || w < 8 || h < 8 || n < 1 || n > 65535 || 2 * dw > w + 1 || 2 * dh > h + 1 )
-    return cudaSuccess;
-  CUtensorMap map;
-  const uint64_t dims[3] = { (uint64_t) w, (uint64_t) h, (uint64_t) n };
-  const uint64_t strides[2] = { (uint64_t) row_stride, (uint64_t) (n > 1 ? frame_stride : row_stride * h) };
-  cudaError_t e = cudaSuccess;
+  if( !gk || ksize != 7 || w < 8 || h < 8 || n < 1 || 2 * dw > w + 1 || 2 * dh > h + 1 ) return cudaSuccess;
+  const size_t esz = depth == SST_DEPTH_U8 ? 1 : depth == SST_DEPTH_U16 ? 2 : depth == SST_DEPTH_F32 ? 4 : 0;
+  if( !esz ) return cudaSuccess;
+  const size_t al = 4 * esz;                    // a lane's four cells
+  if( ((uintptr_t) src % al) || row_stride % al || (n > 1 && frame_stride % al) ) return cudaSuccess;
+  if( n == 1 ) frame_stride = row_stride * h;
+  cudaError_t e;
   switch ( depth ) {
-  case SST_DEPTH_U8: {
-    const uint32_t box[3] = { (uint32_t) fp_geom<uint8_t>::IW, (uint32_t) FP_IH, 1 };
-    if( !encode_tensor_3d(&map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, src, dims, strides, box) ) return cudaSuccess;
-    e = launch_fp<uint8_t>(map, n, w, h, (float) scale, gk, dst0, dst1, dw, dh, dst_stride, err, st);
+  case SST_DEPTH_U8:
+    e = launch_fp<uint8_t>(src, row_stride, frame_stride, n, w, h, (float) scale, gk, dst0, dst1, dw, dh, dst_stride, st);
     break;
-  }
-  case SST_DEPTH_U16: {
-    const uint32_t box[3] = { (uint32_t) fp_geom<uint16_t>::IW, (uint32_t) FP_IH, 1 };
-    if( !encode_tensor_3d(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, src, dims, strides, box) ) return cudaSuccess;
-    e = launch_fp<uint16_t>(map, n, w, h, (float) scale, gk, dst0, dst1, dw, dh, dst_stride, err, st);
+  case SST_DEPTH_U16:
+    e = launch_fp<uint16_t>(src, row_stride, frame_stride, n, w, h, (float) scale, gk, dst0, dst1, dw, dh, dst_stride, st);
     break;
-  }
-  case SST_DEPTH_F32: {
-    const uint32_t box[3] = { (uint32_t) fp_geom<float>::IW, (uint32_t) FP_IH, 1 };
-    if( !encode_tensor_3d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, src, dims, strides, box) ) return cudaSuccess;
-    e = launch_fp<float>(map, n, w, h, (float) scale, gk, dst0, dst1, dw, dh, dst_stride, err, st);
+  default:
+    e = launch_fp<float>(src, row_stride, frame_stride, n, w, h, (float) scale, gk, dst0, dst1, dw, dh, dst_stride, st);
     break;
-  }
-  default: return cudaSuccess;
   }
   if( e == cudaSuccess ) *done = true;
   return e;
