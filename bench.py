@@ -502,8 +502,26 @@ def run_e2e(args, ws, n, frames, reg, acc, passes, frame_bytes):
     barrier(ws)
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000.0 / args.steps, ws)
     d2h = n * (12 * 4 + 3 * 4) + WIDTH * HEIGHT * 5
-    return {"value": ws * n / (e2e_ms / 1000.0), "unit": "frames/s", "h2d_bytes_per_step": n * frame_bytes,
+    # this host's copy rate for the same pinned frames in chunk-sized copies: the
+    # step cannot finish before its frames have crossed
+    total = n * frame_bytes
+    dev = torch.empty(min(n, args.chunk) * frame_bytes, dtype=torch.uint8, device="cuda")
+    src = host_frames.view(torch.uint8).view(-1)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    off = 0
+    while off < total:
+        m = min(dev.numel(), total - off)
+        dev[:m].copy_(src[off:off + m], non_blocking=True)
+        off += m
+    ev1.record()
+    torch.cuda.synchronize()
+    copy_ms = ev0.elapsed_time(ev1)
+    del dev
+    return {"value": ws * n / (e2e_ms / 1000.0), "unit": "frames/s", "h2d_bytes_per_step": total,
             "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+            "h2d_copy_gbs": total / (copy_ms * 1e6), "h2d_copy_ms": copy_ms,
             "api": "sst_stack_frames (host pinned) + sst_weighted_average_compute"}
 
 

@@ -358,21 +358,19 @@ __device__ __forceinline__ float4 ps_load_clamped(const float * row, int x, int 
       __ldg(row + clampi(x + 2, 0, w - 1)), __ldg(row + clampi(x + 3, 0, w - 1)));
 }
 
-__device__ __forceinline__ float4 ps_convert(uint32_t q, float s)
+__device__ __forceinline__ float4 ps_convert(uint32_t q)
 {
-  return make_float4((float) (q & 0xffu) * s, (float) ((q >> 8) & 0xffu) * s, (float) ((q >> 16) & 0xffu) * s,
-      (float) (q >> 24) * s);
+  return make_float4((float) (q & 0xffu), (float) ((q >> 8) & 0xffu), (float) ((q >> 16) & 0xffu), (float) (q >> 24));
 }
 
-__device__ __forceinline__ float4 ps_convert(uint2 q, float s)
+__device__ __forceinline__ float4 ps_convert(uint2 q)
 {
-  return make_float4((float) (q.x & 0xffffu) * s, (float) (q.x >> 16) * s, (float) (q.y & 0xffffu) * s,
-      (float) (q.y >> 16) * s);
+  return make_float4((float) (q.x & 0xffffu), (float) (q.x >> 16), (float) (q.y & 0xffffu), (float) (q.y >> 16));
 }
 
-__device__ __forceinline__ float4 ps_convert(float4 q, float s)
+__device__ __forceinline__ float4 ps_convert(float4 q)
 {
-  return make_float4(q.x * s, q.y * s, q.z * s, q.w * s);
+  return q;
 }
 
 /* pyrDown's [1 4 6 4 1] / 16 of five taps */
@@ -381,22 +379,26 @@ __device__ __forceinline__ float pyr5f(float a, float b, float c, float d, float
   return fmaf(c, 0.375f, fmaf(a + e, 0.0625f, (b + d) * 0.25f));
 }
 
-__device__ __forceinline__ float4 hgauss4(const float (&g)[7], const float (&v)[12])
+/* The 7-tap horizontal Gaussian of four columns: v holds the cells from four
+ * left of the lane's first column; column c takes v[c + 1] ... v[c + 7] in tap
+ * order. Column pairs (0, 1) and (2, 3) run as paired FP32 FMAs (each lane an
+ * ordinary fmaf, so the sums are those of the scalar loop). */
+__device__ __forceinline__ float4 hgauss4(const float2 (&g)[7], const float (&v)[12])
 {
-  float o[4];
+  float2 a = make_float2(0.f, 0.f), b = a;
 #pragma unroll
-  for( int c = 0; c < 4; ++c ) {
-    float a = 0.f;
-#pragma unroll
-    for( int i = 0; i < 7; ++i ) a = fmaf(g[i], v[c + 1 + i], a);
-    o[c] = a;
+  for( int i = 0; i < 7; ++i ) {
+    a = __ffma2_rn(g[i], make_float2(v[1 + i], v[2 + i]), a);
+    b = __ffma2_rn(g[i], make_float2(v[3 + i], v[4 + i]), b);
   }
-  return make_float4(o[0], o[1], o[2], o[3]);
+  return make_float4(a.x, a.y, b.x, b.y);
 }
 
-__device__ __forceinline__ float4 fma4(float g, float4 v, float4 a)
+/* pyrDown's five-tap weights on two columns at once (pyr5f per lane) */
+__device__ __forceinline__ float2 pyr5f2(float2 a, float2 b, float2 c, float2 d, float2 e)
 {
-  return make_float4(fmaf(g, v.x, a.x), fmaf(g, v.y, a.y), fmaf(g, v.z, a.z), fmaf(g, v.w, a.w));
+  return __ffma2_rn(c, make_float2(0.375f, 0.375f), __ffma2_rn(__fadd2_rn(a, e), make_float2(0.0625f, 0.0625f),
+      __fmul2_rn(__fadd2_rn(b, d), make_float2(0.25f, 0.25f))));
 }
 
 /* Strips of one launch: the interior strips (every lane's cells inside the
@@ -415,7 +417,8 @@ __global__ void __launch_bounds__(32 * PS_WARPS, 4) k_convert_pyr1(const T * __r
 {
   static_assert(BH % 2 == 0, "level-1 rows pair level-0 rows");
   constexpr int NR = BH + 9;                                  // input rows of a strip
-  __shared__ __align__(16) float s_buf[PS_WARPS][3][PS_BUF];  // per warp: two input rows, one S row
+  static_assert(NR % 7 == 0, "whole periods of the seven-row ring");
+  __shared__ __align__(16) float s_buf[PS_WARPS][2][PS_BUF];  // per warp: input row, S row
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long item = (long long) blockIdx.x * PS_WARPS + warp;
   const int per_frame = ss.count * gy;
@@ -428,13 +431,15 @@ __global__ void __launch_bounds__(32 * PS_WARPS, 4) k_convert_pyr1(const T * __r
   const int xe = max(tx0 - 5, 0);                             // lane 0's extra input cell
   const T * frame = src + (size_t) z * frame_elems;
   float * rin = s_buf[warp][0];
-  float * srow = s_buf[warp][2];
-  for( int q = lane; q < 3 * PS_BUF; q += 32 ) rin[q] = 0.f;  // cells no lane writes are read as halo
-  float g[7];
+  float * srow = s_buf[warp][1];
+  for( int q = lane; q < 2 * PS_BUF; q += 32 ) rin[q] = 0.f;  // cells no lane writes are read as halo
+  float2 g[7];                                                // each tap twice, for the paired FMAs
 #pragma unroll
-  for( int i = 0; i < 7; ++i ) g[i] = __ldg(gk + i);
+  for( int i = 0; i < 7; ++i ) g[i].x = g[i].y = __ldg(gk + i);
+  const float2 sc = make_float2(scale, scale);
 
-  // input rows ty0 - 5 + r, r = 0 ... NR - 1 (clamped into the image), PS_D in flight
+  // input rows ty0 - 5 + r, r = 0 ... NR - 1 (clamped into the image), PS_D in flight;
+  // the row pointer of row r + PS_D moves on while that row is inside the image
   typename ps_raw<T>::type q[PS_D];
   T qe[PS_D];
   const T * rowp = frame;
@@ -444,45 +449,47 @@ __global__ void __launch_bounds__(32 * PS_WARPS, 4) k_convert_pyr1(const T * __r
     q[i] = EDGE ? ps_load_clamped(rowp, x0, w) : ps_load(rowp, x0);
     qe[i] = lane == 0 ? __ldg(rowp + xe) : (T) 0;
   }
-  float4 A[7];
+  const int r_adv_end = h - 3 - ty0;                          // row r + PS_D = ty0 + 2 + r <= h - 1
+  float2 A[7], B[7];                                          // columns (0, 1) and (2, 3) of the seven rows
 #pragma unroll
-  for( int i = 0; i < 7; ++i ) A[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for( int i = 0; i < 7; ++i ) A[i] = B[i] = make_float2(0.f, 0.f);
   float2 p0 = make_float2(0.f, 0.f), p1 = p0, p2 = p0, p3 = p0;   // level-1 ring: S rows s - 4 ... s - 1
   // level 0: S rows s = 2 ... s_end0 - 1 (y = ty0 - 2 + s) of lanes 1 ... 30 inside the image
   const bool st0 = lane >= 1 && lane <= 30 && x0 < w;
   const bool st0v = st0 && vec0 && x0 + 3 < w;
-  const int s_end0 = min(BH + 2, h - ty0 + 2);
+  const unsigned n0 = (unsigned) max(0, min(BH, h - ty0));   // level-0 rows of the strip
   float * o0 = dst0 + (size_t) z * dst_stride + (size_t) ty0 * w + x0;   // row y = ty0 (s = 2)
   // level 1: rows i = 0 ... i_end - 1 (y1 = ty0 / 2 + i), columns x1, x1 + 1
   const int x1 = tx0 / 2 + 2 * lane - 2;
   const bool st1 = lane >= 1 && lane <= 30 && x1 < dw;
   const bool st1v = st1 && vec1 && x1 + 1 < dw;
   const int i_end = min(BH / 2, dh - ty0 / 2);
+  const bool rfix = ty0 == 0 || ty0 + BH + 2 > h;             // pyrDown rows reach outside the image
   float * o1 = dst1 + (size_t) z * dst_stride + (size_t) (ty0 / 2) * dw + x1;
   __syncwarp();
 
 #pragma unroll 1
   for( int r0 = 0; r0 < NR; r0 += 7 ) {
+    const bool refill = r0 + 7 < NR;                          // rows r0 + 7 ... r0 + 13 exist
 #pragma unroll
     for( int j = 0; j < 7; ++j ) {
       const int r = r0 + j;
-      if( r >= NR ) break;
       // convert this row's cells, then refill the slot with row r + PS_D
-      const float4 f = ps_convert(q[j], scale);
+      const float4 fr = ps_convert(q[j]);
+      const float2 f01 = __fmul2_rn(make_float2(fr.x, fr.y), sc), f23 = __fmul2_rn(make_float2(fr.z, fr.w), sc);
+      const float4 f = make_float4(f01.x, f01.y, f23.x, f23.y);
       const float fe = (float) qe[j] * scale;
-      if( r + PS_D < NR ) {
-        const int yl = ty0 - 5 + r + PS_D;
-        if( yl >= 1 && yl <= h - 1 ) rowp += row_elems;
+      if( refill ) {
+        if( r <= r_adv_end ) rowp += row_elems;
         q[j] = EDGE ? ps_load_clamped(rowp, x0, w) : ps_load(rowp, x0);
         if( lane == 0 ) qe[j] = __ldg(rowp + xe);
       }
-      // horizontal Gaussian through the row buffer (alternate buffers per row)
-      float * rb = rin + (r & 1) * PS_BUF;
-      *reinterpret_cast<float4 *>(rb + 4 * lane + 4) = f;
-      if( lane == 0 ) rb[3] = fe;
+      // horizontal Gaussian through the row buffer
+      *reinterpret_cast<float4 *>(rin + 4 * lane + 4) = f;
+      if( lane == 0 ) rin[3] = fe;
       __syncwarp();
-      const float4 lo = *reinterpret_cast<const float4 *>(rb + 4 * lane);
-      const float4 hi = *reinterpret_cast<const float4 *>(rb + 4 * lane + 8);
+      const float4 lo = *reinterpret_cast<const float4 *>(rin + 4 * lane);
+      const float4 hi = *reinterpret_cast<const float4 *>(rin + 4 * lane + 8);
       const float v[12] = { lo.x, lo.y, lo.z, lo.w, f.x, f.y, f.z, f.w, hi.x, hi.y, hi.z, hi.w };
       const float4 H = hgauss4(g, v);
       // vertical Gaussian: smoothed row r - i takes tap i in slot (j - i) mod 7;
@@ -490,14 +497,23 @@ __global__ void __launch_bounds__(32 * PS_WARPS, 4) k_convert_pyr1(const T * __r
 #pragma unroll
       for( int i = 0; i < 7; ++i ) {
         const int sl = (j - i + 7) % 7;
-        A[sl] = i == 0 ? fma4(g[0], H, make_float4(0.f, 0.f, 0.f, 0.f)) : fma4(g[i], H, A[sl]);
+        const float2 h01 = make_float2(H.x, H.y), h23 = make_float2(H.z, H.w);
+        A[sl] = i == 0 ? __fmul2_rn(g[0], h01) : __ffma2_rn(g[i], h01, A[sl]);
+        B[sl] = i == 0 ? __fmul2_rn(g[0], h23) : __ffma2_rn(g[i], h23, B[sl]);
       }
-      if( r < 6 ) continue;
-      // smoothed row s complete (y = ty0 - 2 + s)
+      if( r < 6 ) {
+        __syncwarp();                                         // the row buffer is rewritten next row
+        continue;
+      }
+      // smoothed row s complete (y = ty0 - 2 + s); the S-row barrier below also
+      // orders this row's input-buffer reads before the next row's writes
       const int s = r - 6;
-      const float4 S = A[(j + 1) % 7];
-      if( s >= 2 && s < s_end0 ) {
-        if( st0v ) *reinterpret_cast<float4 *>(o0) = S;
+      const float4 S = make_float4(A[(j + 1) % 7].x, A[(j + 1) % 7].y, B[(j + 1) % 7].x, B[(j + 1) % 7].y);
+      if( (unsigned) (s - 2) < n0 ) {
+        if( !EDGE && vec0 ) {                                 // interior strips: lanes 1 ... 30 inside the image
+          if( st0 ) *reinterpret_cast<float4 *>(o0) = S;
+        }
+        else if( st0v ) *reinterpret_cast<float4 *>(o0) = S;
         else if( st0 ) {
           o0[0] = S.x;
           if( x0 + 1 < w ) o0[1] = S.y;
@@ -528,16 +544,20 @@ __global__ void __launch_bounds__(32 * PS_WARPS, 4) k_convert_pyr1(const T * __r
       }
       if( s >= 4 ) {
         // level-1 row i = (s - 4) / 2 at y = ty0 + 2i from S rows s - 4 ... s (REFLECT_101 rows)
-        const int i = (s - 4) >> 1, yy = ty0 + 2 * i;
+        const int i = (s - 4) >> 1;
         float2 a = p0, b = p1, d = p3, e = p;
-        if( yy == 0 || yy + 2 >= h ) {
+        if( rfix ) {
+          const int yy = ty0 + 2 * i;
           if( yy == 0 ) a = e, b = d;
           if( yy + 2 == h ) e = p2;
           if( yy + 1 == h ) d = b, e = a;
         }
         if( i < i_end ) {
-          const float2 o = make_float2(pyr5f(a.x, b.x, p2.x, d.x, e.x), pyr5f(a.y, b.y, p2.y, d.y, e.y));
-          if( st1v ) *reinterpret_cast<float2 *>(o1) = o;
+          const float2 o = pyr5f2(a, b, p2, d, e);
+          if( !EDGE && vec1 ) {
+            if( st1 ) *reinterpret_cast<float2 *>(o1) = o;
+          }
+          else if( st1v ) *reinterpret_cast<float2 *>(o1) = o;
           else if( st1 ) {
             o1[0] = o.x;
             if( x1 + 1 < dw ) o1[1] = o.y;
@@ -554,10 +574,12 @@ template<typename T>
 static cudaError_t launch_fp(const void * src, size_t row_stride, size_t frame_stride, int n, int w, int h, float scale,
     const float * gk, float * dst0, float * dst1, int dw, int dh, size_t dst_stride, cudaStream_t st)
 {
-  constexpr int BH = 64;
+  constexpr int BH = 96;
   const int gx = (w + PS_TX - 1) / PS_TX, gy = (h + BH - 1) / BH;
   // interior strips: 1 ... bmin - 1 (bmin = the first strip with tx0 + 124 > w)
-  const int bmin = w >= 124 ? std::min(gx, (w - 124) / PS_TX + 1) : 1;
+  // (and whose level-1 columns all lie inside dw; the interior launch stores without column tests)
+  int bmin = w >= 124 ? std::min(gx, (w - 124) / PS_TX + 1) : 1;
+  while ( bmin > 1 && (bmin - 1) * (PS_TX / 2) + PS_TX / 2 > dw ) --bmin;
   const StripSet in = { 1, std::max(0, bmin - 1), 0 };
   const StripSet ed = { bmin, 1 + (gx - bmin), 1 };
   const int vec0 = (w & 3) == 0 && (dst_stride & 3) == 0 && ((uintptr_t) dst0 & 15) == 0;
