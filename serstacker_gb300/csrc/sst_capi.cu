@@ -1101,6 +1101,7 @@ struct sst_weighted_average {
   DevBuf part;                         // partial sums of the frame chunks of one batch
   DevBuf err;                          // the stacking kernels' error flag (StackArgs::err)
   DevBuf focus_e, focus_w, gk_focus;   // focus weighting: energy maps, blurred maps, Gaussian taps
+  DevBuf out_avg, out_mask;            // device staging of compute() results bound for host memory
   int gk_n = 0;
   sst_local_variance * lv = nullptr;   // local-variance weighting (created on first use)
   sst_local_variance_options lvo = { 2, 1, 3 };
@@ -1111,7 +1112,7 @@ struct sst_weighted_average {
   ~sst_weighted_average()
   {
     acc.release(), coeffs.release(), weff.release(), src.release(), wsrc.release(), part.release(), err.release();
-    focus_e.release(), focus_w.release(), gk_focus.release();
+    focus_e.release(), focus_w.release(), gk_focus.release(), out_avg.release(), out_mask.release();
     sst_local_variance_destroy(lv);
   }
 };
@@ -1314,7 +1315,7 @@ extern "C" int sst_weighted_average_add_warped_batch(sst_weighted_average * a, c
   const float * dparams = params;
   const int32_t * dstatus = status;
   const float * dweights = weights;
-  DevBuf tf, tp, ts, tw;
+  ScopedBuf tf, tp, ts, tw;
   if( !on_device ) {
     SST_CK(tf.ensure(frame_stride * n));
     SST_CK(cudaMemcpyAsync(tf.p, frames, frame_stride * n, cudaMemcpyHostToDevice, st));
@@ -1355,13 +1356,13 @@ extern "C" int sst_weighted_average_compute(sst_weighted_average * a, float * av
     SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, avg, mask, nullptr, st));
     return SST_OK;
   }
-  DevBuf da, dm;
-  if( avg ) SST_CK(da.ensure(N * sizeof(float)));
-  if( mask ) SST_CK(dm.ensure(N));
-  SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, avg ? da.as<float>() : nullptr,
-      mask ? dm.as<uint8_t>() : nullptr, nullptr, st));
-  if( avg ) SST_CK(cudaMemcpyAsync(avg, da.p, N * sizeof(float), cudaMemcpyDeviceToHost, st));
-  if( mask ) SST_CK(cudaMemcpyAsync(mask, dm.p, N, cudaMemcpyDeviceToHost, st));
+  // staged in buffers kept with the accumulator: no allocation per call
+  if( avg ) SST_CK(a->out_avg.ensure(N * sizeof(float)));
+  if( mask ) SST_CK(a->out_mask.ensure(N));
+  SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, avg ? a->out_avg.as<float>() : nullptr,
+      mask ? a->out_mask.as<uint8_t>() : nullptr, nullptr, st));
+  if( avg ) SST_CK(cudaMemcpyAsync(avg, a->out_avg.p, N * sizeof(float), cudaMemcpyDeviceToHost, st));
+  if( mask ) SST_CK(cudaMemcpyAsync(mask, a->out_mask.p, N, cudaMemcpyDeviceToHost, st));
   SST_CK(cudaStreamSynchronize(st));
   return SST_OK;
 }
@@ -1375,7 +1376,7 @@ extern "C" int sst_weighted_average_get_acc_counters(sst_weighted_average * a, f
     SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, nullptr, nullptr, accw, st));
     return SST_OK;
   }
-  DevBuf d;
+  ScopedBuf d;
   SST_CK(d.ensure(N * sizeof(float)));
   SST_CK_LAUNCH(launch_stack_compute(a->acc.as<float>(), N, (int) N, nullptr, nullptr, d.as<float>(), st));
   SST_CK(cudaMemcpyAsync(accw, d.p, N * sizeof(float), cudaMemcpyDeviceToHost, st));
@@ -1390,7 +1391,7 @@ extern "C" int sst_weighted_average_reinitialize(sst_weighted_average * a, const
   cudaStream_t st = (cudaStream_t) stream;
   const size_t N = a->plane();
   const float * da = avg, * dw = accw;
-  DevBuf ta, tw;
+  ScopedBuf ta, tw;
   if( !on_device ) {
     SST_CK(ta.ensure(N * sizeof(float)));
     SST_CK(tw.ensure(N * sizeof(float)));
@@ -1669,7 +1670,7 @@ extern "C" int sst_remap(const void * src, int depth, int src_width, int src_hei
   model_set_params(*model, s, p);
   float c[SST_NCOEF];
   model_warp_coeffs(*model, s, c);
-  DevBuf dc;
+  ScopedBuf dc;
   SST_CK(dc.ensure(sizeof(c)));
   SST_CK(cudaMemcpyAsync(dc.p, c, sizeof(c), cudaMemcpyHostToDevice, st));
   SST_CK_LAUNCH(launch_remap(src, depth, src_width, src_height, row_stride, scale, model->type, dc.as<float>(), border,

@@ -198,7 +198,7 @@ extern "C" int sst_average_pyramid_inpaint(const float * src, size_t src_stride,
   const int L = (int) lw.size();
   std::vector<size_t> off(L + 1, 0);
   for( int l = 0; l < L; ++l ) off[l + 1] = off[l] + (size_t) lw[l] * lh[l];
-  DevBuf bI, bM, bO, bflag, bsrc, bmask, bdst, bdmask;
+  ScopedBuf bI, bM, bO, bflag, bsrc, bmask, bdst, bdmask;
   SST_ICK(bI.ensure(off[L] * sizeof(float)));
   SST_ICK(bM.ensure(off[L] * sizeof(float)));
   SST_ICK(bO.ensure(off[L] * sizeof(float)));

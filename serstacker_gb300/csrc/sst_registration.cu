@@ -663,7 +663,7 @@ extern "C" int sst_remap_rmap(const void * src, int depth, int src_width, int sr
     return fail(SST_ERR_UNSUPPORTED, "unsupported border mode");
   cudaStream_t st = (cudaStream_t) stream;
   const size_t dplane = (size_t) dst_width * dst_height;
-  DevBuf raw, hs, hm, hmask, hdst, hdm;
+  ScopedBuf raw, hs, hm, hmask, hdst, hdm;
   const void * d_src = src;
   const float * d_rmap = rmap;
   const uint8_t * d_smask = src_mask;
@@ -742,7 +742,7 @@ extern "C" int sst_image_transform_create_remap(const sst_motion_model * model, 
   if( model->type < 0 || model->type > 7 ) return fail(SST_ERR_INVALID_ARG, "invalid motion type");
   if( width < 1 || height < 1 ) return fail(SST_ERR_INVALID_ARG, "invalid size");
   cudaStream_t st = (cudaStream_t) stream;
-  DevBuf dp, dc, dm;
+  ScopedBuf dp, dc, dm;
   SST_RCK(dp.ensure(12 * sizeof(float)));
   SST_RCK(dc.ensure(SST_NCOEF * sizeof(float)));
   SST_RCK(cudaMemcpyAsync(dp.p, params, model_nparams(*model) * sizeof(float),
