@@ -3,9 +3,12 @@ scale), Gaussian pre-smooth (sepFilter2D, REPLICATE) and pyrDown levels
 (5-tap, REFLECT_101, c_ecch::compute_next_pyramid_layer_size).
 
 Levels 0 and 1 come from the fused convert + pre-smooth + pyrDown pass when
-the frames meet its layout rules (7-tap Gaussian, 16-byte row strides), else
-from the two-kernel path; both are covered, including partial tiles at the
-right and bottom edges and images narrower than one tile.
+the frames meet its layout rules (7-tap Gaussian, rows whose base and stride
+allow a lane's four-cell loads), else from the two-kernel path; both are
+covered. The fused pass works in strips of 120 columns by 96 rows (interior
+and edge strips launched apart); the cases include strips cut by the right
+edge, bands cut by the bottom edge, frames narrower than one strip and
+shorter than one band.
 
 Tolerance: 2e-6 of the level's largest magnitude per pixel (FP32 sums of 7
 and 5 taps against FP64).
@@ -48,6 +51,10 @@ def _check(got, want, what):
     (208, 150, np.uint8),        # fused: u8 window alignment
     (136, 70, np.uint16),        # fused: 8 columns / 6 rows in the last tiles
     (132, 40, np.float32),       # fused: 4 level-0 and 2 level-1 columns in the last tile
+    (121, 97, np.uint16),        # fused: a one-column second strip, a one-row second band
+    (244, 193, np.uint8),        # fused: one interior strip, 244-byte rows (4-byte, not 16-byte multiples)
+    (364, 17, np.float32),       # fused: 17 rows (two levels), one band cut short
+    (100, 300, np.uint16),       # fused: narrower than one strip (edge launch only), four bands
     (333, 277, np.float32),      # two-kernel path: 1332-byte rows
     (1283, 101, np.uint16),      # two-kernel path: 2566-byte rows
 ])
