@@ -1674,8 +1674,11 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
         }
         float tr = (float) (threadIdx.x >> 7);
         if( pl.inside ) {
+          // every sample counts (full coverage): the count is known in advance
+          if( y0r < yend ) acc[5] = (float) ((yend - 1 - y0r) / 2 + 1);
+          const float * rp = a.refT + (size_t) y0r * a.w + x;
 #pragma unroll 4
-        for( int y = y0r; y < yend; y += 2, tr += 2.f ) {
+        for( int y = y0r; y < yend; y += 2, tr += 2.f, rp += 2 * a.w ) {
           float X, Y;
           if( FAM == FAM_AFFINE ) {
             X = fmaf(c[1], tr, e0);
@@ -1691,13 +1694,12 @@ __global__ void __launch_bounds__(256, 4) k_correlation_tma(CorrArgs a, const __
           const int o = (int) min((unsigned) (iy * PB_W + ix), (unsigned) (PB_W * PB_H - PB_W - 2));
           const float v00 = box[o], v01 = box[o + 1], v10 = box[o + PB_W], v11 = box[o + PB_W + 1];
           const float t0 = fmaf(ax, v01 - v00, v00), t1 = fmaf(ax, v11 - v10, v10);
-          const float av = __ldg(a.refT + (size_t) y * a.w + x) - a.tshift;
+          const float av = __ldg(rp) - a.tshift;
           const float bv = fmaf(ay, t1 - t0, t0) - a.tshift;
           acc[0] += av, acc[1] += bv;
           acc[2] = fmaf(av, av, acc[2]);
           acc[3] = fmaf(bv, bv, acc[3]);
           acc[4] = fmaf(av, bv, acc[4]);
-          acc[5] += 1.f;
         }
         }
         else {

@@ -893,22 +893,35 @@ __global__ void __launch_bounds__(256) k_lap_energy(const float * pyr, size_t py
   const float * img = pyr + (size_t) f * pyr_stride + lvl_off;
   const int tiles_x = (w + LE_TX - 1) / LE_TX;
   const int tx0 = (t % tiles_x) * LE_TX, ty0 = (t / tiles_x) * LE_TY;
-  float s = 0.f, cnt = 0.f;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // each thread walks 16 consecutive rows of one column with the rows above and
+  // below in registers; the left and right neighbours come from the adjacent
+  // lanes, and the warp's outer lanes load theirs. Cells are read clamped into the
+  // image; only interior pixels count.
   const int x = tx0 + (threadIdx.x & (LE_TX - 1));
-  if( x >= 1 && x < w - 1 ) {
+  const int ya = ty0 + (threadIdx.x >> 7) * (LE_TY / 2);
+  const bool inx = x >= 1 && x < w - 1;
+  const float * col = img + min(x, w - 1);
+  const float * side = img + clampi(lane == 0 ? x - 1 : x + 1, 0, w - 1);   // lanes 0 and 31 only
+  float s = 0.f, cnt = 0.f;
+  float up = __ldg(col + (size_t) clampi(ya - 1, 0, h - 1) * w);
+  float c = __ldg(col + (size_t) clampi(ya, 0, h - 1) * w);
 #pragma unroll 4
-    for( int k = 0; k < LE_TY / 2; ++k ) {
-      const int y = ty0 + (threadIdx.x >> 7) + 2 * k;
-      if( y >= 1 && y < h - 1 ) {
-        const float * p = img + (size_t) y * w + x;
-        const float l = (__ldg(p - 1) + __ldg(p + 1)) + (__ldg(p - w) + __ldg(p + w)) - 4.f * __ldg(p);
-        s = fmaf(l, l, s);
-        cnt += 1.f;
-      }
+  for( int k = 0; k < LE_TY / 2; ++k ) {
+    const int y = ya + k;
+    const size_t ro = (size_t) clampi(y, 0, h - 1) * w;
+    const float dn = __ldg(col + (size_t) clampi(y + 1, 0, h - 1) * w);
+    float l_ = __shfl_up_sync(0xffffffffu, c, 1), r_ = __shfl_down_sync(0xffffffffu, c, 1);
+    if( lane == 0 ) l_ = __ldg(side + ro);
+    if( lane == 31 ) r_ = __ldg(side + ro);
+    if( inx && y >= 1 && y < h - 1 ) {
+      const float l = (l_ + r_) + (up + dn) - 4.f * c;
+      s = fmaf(l, l, s);
+      cnt += 1.f;
     }
+    up = c, c = dn;
   }
   // FP32 within warps (16 values per thread, 32 lanes), FP64 across the 8 warps
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   s = warp_sum(s);
   cnt = warp_sum(cnt);
   if( lane == 0 ) s_red[wid * 2] = s, s_red[wid * 2 + 1] = cnt;
