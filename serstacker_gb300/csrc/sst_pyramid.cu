@@ -309,8 +309,9 @@ cudaError_t launch_pyrdown_ragged(const float * src, const RaggedImg * jobs, int
  *    scaled; the 7-tap horizontal Gaussian reads the neighbouring lanes'
  *    cells through a per-warp row buffer in shared memory;
  *  - the vertical Gaussian adds each horizontal row into the seven smoothed
- *    rows it reaches (a ring of seven float4 accumulators, taps in order), so
- *    the smoothed row S of input row r is complete six rows later;
+ *    rows it reaches (a ring of seven rows of accumulators, two column pairs
+ *    each in paired FP32 FMAs, taps in order), so the smoothed row S of input
+ *    row r is complete six rows later;
  *  - S is stored as level 0 where it lies in the strip, and its horizontal
  *    5-tap pyrDown (two level-1 columns per lane) enters a ring of five rows,
  *    from which every second S row gives one level-1 row (rows first, as
