@@ -610,14 +610,14 @@ __device__ __forceinline__ int item_frame(const PassArgs & a, int item, int nite
 
 /* FP64 sum, in warp order, of the 8 warp sums of an item (lanes < NS of
  * one warp) stored as that item's tile partials */
-template<int NS>
+template<int NS, int NW = 8>
 __device__ __forceinline__ void store_item_sums(const PassArgs & a, int f, int t, const float * scratch)
 {
   const int lane = threadIdx.x & 31;
   if( lane < NS ) {
     double s = 0;
 #pragma unroll
-    for( int wv = 0; wv < 8; ++wv ) s += (double) scratch[wv * NS + lane];
+    for( int wv = 0; wv < NW; ++wv ) s += (double) scratch[wv * NS + lane];
     a.partials[(size_t) f * a.part_stride + (size_t) t * NS + lane] = s;
   }
 }
@@ -627,18 +627,26 @@ __device__ __forceinline__ void store_item_sums(const PassArgs & a, int f, int t
  * the gathers become shared-memory loads with no address arithmetic in
  * 64 bits, and the next item's copy is in flight while this one computes.
  * Items whose taps leave the level or the box take the global path. */
-// (the projective pass needs more registers per thread: three CTAs per SM)
+// The projective pass runs 128 threads per CTA (four CTAs per SM, shared memory
+// bound): each thread takes twice the samples per item, so the per-item plan,
+// barrier and reduction weigh half as much, and the registers the projective
+// positions need fit without spills. The affine pass keeps 256 (its occupancy
+// matters more).
+template<int FAM>
+__host__ __device__ constexpr int pw_threads() { return FAM == FAM_HOMOG ? 128 : 256; }
+
 template<int METHOD, int FAM, int JK, int M, int TXS>
-__global__ void __launch_bounds__(256, FAM == FAM_HOMOG ? 3 : 4) k_pass_pointwise_tma(PassArgs a, const __grid_constant__ CUtensorMap tmap)
+__global__ void __launch_bounds__(pw_threads<FAM>(), 4) k_pass_pointwise_tma(PassArgs a, const __grid_constant__ CUtensorMap tmap)
 {
   constexpr int NS = M + 2;
   constexpr int NP = column_sums<JK, M>::N;
+  constexpr int NT = pw_threads<FAM>(), NW = NT / 32;
   constexpr int PB_W = TXS + 16;                    // footprint box width (tile + 16 px)
-  constexpr int RS = 256 / TXS;                     // rows between a thread's samples
+  constexpr int RS = NT / TXS;                      // rows between a thread's samples
   constexpr int RSH = TXS == 128 ? 7 : 6;           // log2 TXS
   __shared__ __align__(128) float s_box[2][PB_H * PB_W];
   __shared__ __align__(8) uint64_t s_bar[2];
-  __shared__ float s_red[2][8 * NS];     // warp sums of the current and the previous item
+  __shared__ float s_red[2][NW * NS];    // warp sums of the current and the previous item
   __shared__ float s_c[3][16];
   __shared__ ItemPlan s_plan[3];
   __shared__ uint32_t s_infl;             // copies in flight, kept by thread 0
@@ -698,7 +706,7 @@ __global__ void __launch_bounds__(256, FAM == FAM_HOMOG ? 3 : 4) k_pass_pointwis
       tma_load_3d(s_box[b ^ 1], &tmap, s_plan[nslot].bx0, s_plan[nslot].by0, s_plan[nslot].f, &s_bar[b ^ 1]);
       inflight_issued(&s_infl, b ^ 1, (phases >> (b ^ 1)) & 1u);
     }
-    if( pf >= 0 && (threadIdx.x >> 5) == 1 ) store_item_sums<NS>(a, pf, pt, s_red[b ^ 1]);
+    if( pf >= 0 && (threadIdx.x >> 5) == 1 ) store_item_sums<NS, NW>(a, pf, pt, s_red[b ^ 1]);
     const ItemPlan pl = s_plan[slot];
     pf = pl.f, pt = pl.t;
     float c[16];
@@ -904,7 +912,7 @@ __global__ void __launch_bounds__(256, FAM == FAM_HOMOG ? 3 : 4) k_pass_pointwis
     warp_sums_to<NS>(acc, &s_red[b][(threadIdx.x >> 5) * NS]);
   }
   __syncthreads();
-  if( pf >= 0 && (threadIdx.x >> 5) == 1 ) store_item_sums<NS>(a, pf, pt, s_red[b ^ 1]);
+  if( pf >= 0 && (threadIdx.x >> 5) == 1 ) store_item_sums<NS, NW>(a, pf, pt, s_red[b ^ 1]);
   if( threadIdx.x == 0 ) inflight_drain(&s_infl, s_bar);
   if( timed_out && a.err ) atomicExch(a.err, 1);
 }
@@ -1164,7 +1172,7 @@ cudaError_t launch_solve(int method, const PassArgs & a, int grid, cudaStream_t 
 
 /* persistent grid: every SM filled to the kernel's occupancy */
 template<typename K>
-static int persistent_grid(K kernel)
+static int persistent_grid(K kernel, int nt = 256)
 {
   static int sms = 0;
   if( !sms ) {
@@ -1174,7 +1182,7 @@ static int persistent_grid(K kernel)
     if( sms <= 0 ) sms = 1;
   }
   int per_sm = 0;
-  if( cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1 ) {
+  if( cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nt, 0) != cudaSuccess || per_sm < 1 ) {
     cudaGetLastError();
     per_sm = 1;
   }
@@ -1186,15 +1194,17 @@ static cudaError_t launch_t(const PassArgs & a, int grid, cudaStream_t st, const
 {
   if constexpr( METHOD == M_IC || METHOD == M_ICLM ) {
     if( map && FAM != FAM_QUAD ) {
+      // a tuned grid counts CTAs of 256 threads
+      constexpr int NT = pw_threads<FAM>();
       if( a.tile_w == 64 ) {
         static int g = 0;
-        if( !g ) g = persistent_grid(k_pass_pointwise_tma<METHOD, FAM, JK, M, 64>);
-        k_pass_pointwise_tma<METHOD, FAM, JK, M, 64><<<grid > 0 ? grid : g, 256, 0, st>>>(a, *map);
+        if( !g ) g = persistent_grid(k_pass_pointwise_tma<METHOD, FAM, JK, M, 64>, NT);
+        k_pass_pointwise_tma<METHOD, FAM, JK, M, 64><<<grid > 0 ? grid * (256 / NT) : g, NT, 0, st>>>(a, *map);
       }
       else {
         static int g = 0;
-        if( !g ) g = persistent_grid(k_pass_pointwise_tma<METHOD, FAM, JK, M, PW_TX>);
-        k_pass_pointwise_tma<METHOD, FAM, JK, M, PW_TX><<<grid > 0 ? grid : g, 256, 0, st>>>(a, *map);
+        if( !g ) g = persistent_grid(k_pass_pointwise_tma<METHOD, FAM, JK, M, PW_TX>, NT);
+        k_pass_pointwise_tma<METHOD, FAM, JK, M, PW_TX><<<grid > 0 ? grid * (256 / NT) : g, NT, 0, st>>>(a, *map);
       }
       return cudaGetLastError();
     }
